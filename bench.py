@@ -1,0 +1,365 @@
+"""Benchmark of the ACSF + BPNN hot path on one GB300 (config C2 of the benchmark set).
+
+One step = one pass of the hot path over the whole C2 dataset (2,000 periodic structures of
+64-256 atoms, two species, 96 ACSF features, network 96-32-32-1 tanh, FP32):
+  featurise   neighbour search + G2/G5 values + z-score (training statistics)
+  train       one L-BFGS training iteration of the reference's nTrain loop (update with the
+              current gradient incl. line search, then forward + loss + backward + FP64
+              gradient reduction at the new parameters)
+  predict     energies and analytical forces of every atom at the new parameters
+Metric: atoms/s = atoms in the dataset / step time (train+predict).
+
+`value`: inputs resident in HBM, CUDA events on the library's stream around every step,
+L2 flushed (a 256 MiB write) between steps outside the timed events.
+`e2e`: the same step through the public API with host buffers: coordinates copied in, energies
+and forces copied out, inside the timed region.
+
+--impl reference times the CPU restatement of the reference's own algorithm (the oracle:
+neighbour list rebuilt per atom and G-function, dense dG/dR) with all host threads on a
+bounded sample of the same workload.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "atoms/s train+predict (C2: featurise + L-BFGS iteration + energies/forces)"
+UNIT = "atoms/s"
+L2_FLUSH_BYTES = 256 << 20
+
+
+def load_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as fh:
+            d = json.load(fh)
+        return float(d["hbm_gbs"]), float(d["bf16_tflops"]), "measured"
+    return 6800.0, 1900.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle-reason samples during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device=0):
+        self.device = device
+        self.samples = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                self.samples.append(parts)
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        sm = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        mx = [float(s[2]) for s in self.samples if s[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for s in self.samples for k in range(4)
+                          if s[5 + k].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(self.samples)}
+
+
+def setup(cfg_name, nstruct, precision):
+    from fortnet_gb300 import api, synthetic
+
+    cfg = synthetic.CONFIGS[cfg_name]
+    ds = synthetic.generate(cfg, nstruct=nstruct)
+    funcs = synthetic.gfunctions(cfg)
+    dims = synthetic.network_dims(cfg)
+    ctx = api.Context(precision)
+    ctx.upload(ds)
+    ctx.set_species(ds.species)
+    ctx.set_gfunctions(funcs)
+    ctx.neighbors()
+    ctx.acsf(download=False)
+    zprec = ctx.zscore(weights=ds.weights)
+    params = api.Rng(cfg.seed).init_params(dims, len(cfg.atomic_numbers))
+    ctx.set_network(dims, "tanh", params)
+    ctx.set_targets(ds)
+    ctx.optimizer_init("lbfgs", 1e-20, 1e-6, 1e4, memory=1000, linemin=True)
+    return ctx, ds, zprec, funcs, dims, params
+
+
+def device_step(ctx, zprec):
+    ctx.neighbors()
+    ctx.acsf(download=False)
+    ctx.zscore(zprec=zprec)
+    ctx.train_iteration("mse")
+    ctx.lib.fnetg_predict(ctx.h, None, None)
+    ctx.lib.fnetg_forces(ctx.h, None)
+
+
+def e2e_step(ctx, zprec, coords_pinned, out_energy, out_forces):
+    ctx.update_coords(coords_pinned)
+    ctx.neighbors()
+    ctx.acsf(download=False)
+    ctx.zscore(zprec=zprec)
+    loss, _, _ = ctx.train_iteration("mse")
+    at, gl = ctx.predict()
+    out_energy[:] = gl
+    out_forces[:] = ctx.forces()
+    return loss
+
+
+def algorithmic_bytes(ctx, ds, funcs, dims):
+    """Bytes each kernel family must move per launch (see DESIGN: roofline)."""
+    N, S = ds.ntot, ds.nstruct
+    P = ctx.neighbors()
+    nf = dims[0]
+    fp = 4
+    return {
+        # positions (24 B double + 16 B float) per candidate atom read once per image-visited
+        # structure is L1/L2 traffic; HBM: per atom coords + pair records written
+        "neighbors": N * (24 + 16 + 8) + P * (4 + 4 + 16 + 8),
+        # pair records in, feature rows out
+        "acsf": P * (16 + 4 + 4) + N * (8 + 4) + P * 1 + N * nf * fp,
+        "forces": P * (16 + 4 + 4) + N * nf * fp + N * 8 + P * 24,
+        "mlp_forward": N * nf * fp + N * 8,
+        "mlp_backward": N * nf * fp + N * 8,
+        "mlp_jacobian": N * nf * fp + N * nf * fp,
+        "zscore": 2 * N * (nf - 0) * fp,
+    }
+
+
+def run_ours(args):
+    from fortnet_gb300 import api
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist  # replicas only: barrier + max-over-ranks timing
+
+        dist.init_process_group("gloo")
+    import torch
+
+    torch.cuda.set_device(local)
+    precision = api.FP32
+    ctx, ds, zprec, funcs, dims, params = setup(args.config, args.nstruct, precision)
+    stream = torch.cuda.ExternalStream(ctx.stream())
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+    N = ds.ntot
+    for _ in range(args.warmup):
+        device_step(ctx, zprec)
+    ctx.synchronize()
+    if dist:
+        dist.barrier()
+    ctx.profile(True)
+    ctx.profile_reset()
+    launches0 = ctx.launch_count()
+    times = []
+    with ClockSampler(local) as clk:
+        for _ in range(args.steps):
+            flush.fill_(1.0)
+            torch.cuda.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            device_step(ctx, zprec)
+            e1.record(stream)
+            e1.synchronize()
+            times.append(e0.elapsed_time(e1))
+    torch.cuda.synchronize()
+    launches = ctx.launch_count() - launches0
+    ms_step = float(np.mean(times))
+    if dist:
+        t = torch.tensor([ms_step], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_step = float(t.item())
+    # per-kernel device time inside the timed steps
+    fams = ["neighbors", "scan", "acsf", "zscore", "mlp_forward", "mlp_backward",
+            "mlp_jacobian", "forces", "reduce", "loss", "optimizer", "params"]
+    prof = {f: ctx.profile_read(f) for f in fams}
+    ctx.profile(False)
+    value = N * world / (ms_step / 1e3)
+    # ---- end to end through the public API with host buffers
+    coords = np.ascontiguousarray(ds.coords)
+    energy = np.zeros((ds.nstruct, 1))
+    forces = np.zeros((N, 1, 3))
+    for _ in range(2):
+        e2e_step(ctx, zprec, coords, energy, forces)
+    ctx.synchronize()
+    t0 = time.perf_counter()
+    esteps = max(2, min(args.steps, 5))
+    for _ in range(esteps):
+        e2e_step(ctx, zprec, coords, energy, forces)
+    ctx.synchronize()
+    e2e_ms = (time.perf_counter() - t0) * 1e3 / esteps
+    h2d = coords.nbytes
+    d2h = energy.nbytes + forces.nbytes + 8
+    # ---- roofline of the dominant kernel family
+    hbm, _, peak_kind = load_peaks()
+    bytes_alg = algorithmic_bytes(ctx, ds, funcs, dims)
+    dom = max((f for f in fams if prof[f][1] > 0), key=lambda f: prof[f][0])
+    dom_ms = prof[dom][0] / max(prof[dom][1], 1)
+    per_launch_bytes = bytes_alg.get(dom, 0) / max(1, prof[dom][1] / args.steps)
+    achieved = per_launch_bytes / (dom_ms / 1e3) / 1e9 if dom_ms > 0 else 0.0
+    out = {
+        "metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_step, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded C2 generator: dense-liquid cells, Morse targets)",
+        "config": {"workload": f"{args.config}: {ds.nstruct} structures, {N} atoms, "
+                               f"{dims[0]} features, net {'-'.join(map(str, dims))}, L-BFGS",
+                   "l2": "flushed between timed steps (256 MiB write)",
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "e2e": {"value": round(N / (e2e_ms / 1e3), 1), "unit": UNIT,
+                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+        "gpu_launches": int(launches),
+        "roofline": {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1),
+                     "peak": hbm, "unit": "GB/s", "frac": round(achieved / hbm, 4),
+                     "traffic": None, "peak_source": peak_kind},
+        "kernels_ms_per_step": {f: round(prof[f][0] / args.steps, 4) for f in fams
+                                if prof[f][1] > 0},
+        "clocks": clk.summary(),
+    }
+    if not args.no_cpu_baseline and rank == 0 and world == 1:
+        out["cpu_baseline"] = cpu_baseline(args, sample_structs=args.cpu_sample, threads=1)
+    if rank == 0:
+        print(json.dumps(out))
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+def cpu_step(ds, funcs, dims, params, zprec, nthreads):
+    """The same step on the oracle (the reference's algorithm restated on the CPU)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+
+    vals = O.acsf(ds, funcs, mode=0, nthreads=nthreads)
+    feats = O.zscore_apply(vals, zprec)
+    dd, pred = O.train_gradients(dims, "tanh", params, feats, ds)
+    g, _ = O.update_prepare(dims, "tanh", params, dd, 0.0, 0.0, float(ds.weights.sum()))
+    newp = np.stack([O.Lbfgs(params[s], 1e-20, 1e-6, 1e4, 1000, True, False).next(0.0, g[s])[0]
+                     for s in range(params.shape[0])])
+    dd, _ = O.train_gradients(dims, "tanh", newp, feats, ds)
+    out = O.predict(dims, "tanh", newp, feats, ds.species)
+    jac = O.jacobian(dims, "tanh", newp, feats, ds.species)
+    O.forces(ds, funcs, zprec, jac)
+    return out
+
+
+def cpu_baseline(args, sample_structs, threads):
+    from fortnet_gb300 import api, synthetic
+
+    cfg = synthetic.CONFIGS[args.config]
+    ds = synthetic.generate(cfg, nstruct=sample_structs)
+    funcs = synthetic.gfunctions(cfg)
+    dims = synthetic.network_dims(cfg)
+    params = api.Rng(cfg.seed).init_params(dims, len(cfg.atomic_numbers))
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+
+    zprec = O.zscore_stats(O.acsf(ds, funcs, mode=1), ds)
+    t0 = time.perf_counter()
+    cpu_step(ds, funcs, dims, params, zprec, threads)
+    dt = time.perf_counter() - t0
+    return {"value": round(ds.ntot / dt, 2), "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{ds.nstruct} C2 structures ({ds.ntot} atoms), one step; the oracle "
+                      f"restates the reference loop structure (per-(atom, G) neighbour rebuild, "
+                      f"dense dG/dR)", "seconds": round(dt, 2)}
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    from fortnet_gb300 import api, synthetic
+
+    cfg = synthetic.CONFIGS[args.config]
+    ds = synthetic.generate(cfg, nstruct=args.ref_sample)
+    funcs = synthetic.gfunctions(cfg)
+    dims = synthetic.network_dims(cfg)
+    params = api.Rng(cfg.seed).init_params(dims, len(cfg.atomic_numbers))
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+
+    zprec = O.zscore_stats(O.acsf(ds, funcs, mode=1, nthreads=threads), ds)
+    for _ in range(args.warmup if args.warmup < 1 else 1):
+        cpu_step(ds, funcs, dims, params, zprec, threads)
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        cpu_step(ds, funcs, dims, params, zprec, threads)
+        times.append(time.perf_counter() - t0)
+    dt = float(np.mean(times))
+    v = ds.ntot / dt
+    print(json.dumps({
+        "impl": "reference", "metric": METRIC, "value": round(v, 2), "unit": UNIT, "n_gpus": 0,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(dt * 1e3, 1),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded C2 generator)",
+        "config": {"workload": f"{args.config} sample: {ds.nstruct} structures, {ds.ntot} atoms"},
+        "cpu_baseline": {"value": round(v, 2), "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"{ds.nstruct} C2 structures per step (oracle restatement of "
+                                   f"the reference algorithm; the Fortran program cannot be "
+                                   f"built here)"},
+        "e2e": {"value": round(v, 2), "unit": UNIT, "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--config", default="C2")
+    ap.add_argument("--nstruct", type=int, default=None)
+    ap.add_argument("--cpu-sample", type=int, default=4)
+    ap.add_argument("--ref-sample", type=int, default=32)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

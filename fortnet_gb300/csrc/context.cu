@@ -1,0 +1,934 @@
+// Context management and the C-ABI entry points of libfnetg.
+#include <algorithm>
+#include <cstdio>
+#include <array>
+#include <set>
+
+#include "internal.cuh"
+
+using namespace fnetg;
+
+namespace fnetg {
+
+int fail(fnetg_ctx *c, int code, const std::string &msg) {
+  if (c) c->err = msg;
+  return code;
+}
+
+int cuda_fail(fnetg_ctx *c, cudaError_t e, const char *where) {
+  char buf[512];
+  snprintf(buf, sizeof buf, "CUDA error %d (%s) in %s", (int)e, cudaGetErrorString(e), where);
+  if (c) c->err = buf;
+  return e == cudaErrorMemoryAllocation ? FNETG_E_NOMEM : FNETG_E_CUDA;
+}
+
+int num_sms() {
+  static int n = 0;
+  if (!n) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    if (n <= 0) n = 1;
+  }
+  return n;
+}
+
+static cudaEvent_t pool_event(fnetg_ctx *c) {
+  if (c->ev_free.empty()) {
+    cudaEvent_t e = nullptr;
+    cudaEventCreate(&e);
+    return e;
+  }
+  cudaEvent_t e = c->ev_free.back();
+  c->ev_free.pop_back();
+  return e;
+}
+
+LaunchScope::LaunchScope(fnetg_ctx *ctx, const char *n) : c(ctx), name(n) {
+  c->launches++;
+  if (c->prof) {
+    e0 = pool_event(c);
+    cudaEventRecord(e0, c->stream);
+  }
+}
+
+LaunchScope::~LaunchScope() {
+  if (!c->prof) return;
+  cudaEvent_t e1 = pool_event(c);
+  cudaEventRecord(e1, c->stream);
+  c->ev_pending.push_back({name, e0, e1});
+}
+
+// resolves recorded launch events into the per-kernel table (after the stream has drained)
+void resolve_profile(fnetg_ctx *c) {
+  if (c->ev_pending.empty()) return;
+  cudaStreamSynchronize(c->stream);
+  for (auto &p : c->ev_pending) {
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, p.e0, p.e1);
+    auto &e = c->prof_tab[p.name];
+    e.ms += ms;
+    e.launches += 1;
+    c->ev_free.push_back(p.e0);
+    c->ev_free.push_back(p.e1);
+  }
+  c->ev_pending.clear();
+}
+
+}  // namespace fnetg
+
+// ---------------------------------------------------------------------------------------
+// Reciprocal lattice exactly as the reference derives it (fnetdata.F90:1141-1148 with
+// determinant33 / invert33 of lib_dftbp/simplealgebra.F90:41-125, then a transpose).
+// This file is compiled with -ffp-contract=off so the host arithmetic is not fused.
+static int recvecs2p(const double *L, double *R) {
+#define M(i, j) L[((i)-1) + 3 * ((j)-1)]
+  double tmp = M(1, 1) * (M(2, 2) * M(3, 3) - M(3, 2) * M(2, 3));
+  tmp = tmp - M(1, 2) * (M(2, 1) * M(3, 3) - M(3, 1) * M(2, 3));
+  tmp = tmp + M(1, 3) * (M(2, 1) * M(3, 2) - M(3, 1) * M(2, 2));
+  const double det = tmp;
+  if (!(std::fabs(det) >= 1e-12)) return -1;
+  double inv[9];
+#define INV(i, j) inv[((i)-1) + 3 * ((j)-1)]
+  INV(1, 1) = -(M(2, 3) * M(3, 2)) + M(2, 2) * M(3, 3);
+  INV(2, 1) = M(2, 3) * M(3, 1) - M(2, 1) * M(3, 3);
+  INV(3, 1) = -(M(2, 2) * M(3, 1)) + M(2, 1) * M(3, 2);
+  INV(1, 2) = M(1, 3) * M(3, 2) - M(1, 2) * M(3, 3);
+  INV(2, 2) = -(M(1, 3) * M(3, 1)) + M(1, 1) * M(3, 3);
+  INV(3, 2) = M(1, 2) * M(3, 1) - M(1, 1) * M(3, 2);
+  INV(1, 3) = -(M(1, 3) * M(2, 2)) + M(1, 2) * M(2, 3);
+  INV(2, 3) = M(1, 3) * M(2, 1) - M(1, 1) * M(2, 3);
+  INV(3, 3) = -(M(1, 2) * M(2, 1)) + M(1, 1) * M(2, 2);
+  for (int k = 0; k < 9; k++) inv[k] = inv[k] / det;
+  for (int i = 0; i < 3; i++)
+    for (int j = 0; j < 3; j++) R[i + 3 * j] = inv[j + 3 * i];
+#undef M
+#undef INV
+  return 0;
+}
+
+// image ranges of TLatPointIter_init / getRanges (latpointiter.F90:226-253), extension 1
+int fnetg_lattice_ranges(const double *L, double rcut, int32_t *lohi) {
+  double R[9];
+  if (recvecs2p(L, R)) return -1;
+  for (int ii = 0; ii < 3; ii++) {
+    const double *col = R + 3 * ii;
+    double s = col[0] * col[0];
+    s = s + col[1] * col[1];
+    s = s + col[2] * col[2];
+    int itmp = (int)std::floor(rcut * std::sqrt(s));
+    lohi[2 * ii] = -(itmp + 1);
+    lohi[2 * ii + 1] = itmp + 1;
+  }
+  return 0;
+}
+
+// ---------------------------------------------------------------------------------------
+extern "C" {
+
+int fnetg_abi_version(void) { return FNETG_ABI_VERSION; }
+
+int fnetg_create(fnetg_ctx **out, int32_t precision, int32_t device) {
+  if (!out) return FNETG_E_INVALID;
+  *out = nullptr;
+  if (precision != FNETG_FP32 && precision != FNETG_FP64) return FNETG_E_INVALID;
+  fnetg_ctx *ctx = new fnetg_ctx();
+  ctx->prec = precision;
+  ctx->device = device;
+  cudaError_t e = cudaSetDevice(device);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev0);
+  if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev1);
+  if (e == cudaSuccess) e = cudaMallocHost(&ctx->h_pinned, 4096);
+  if (e != cudaSuccess) {
+    delete ctx;
+    return e == cudaErrorMemoryAllocation ? FNETG_E_NOMEM : FNETG_E_CUDA;
+  }
+  *out = ctx;
+  return FNETG_OK;
+}
+
+int fnetg_destroy(fnetg_ctx *ctx) {
+  if (!ctx) return FNETG_E_INVALID;
+  cudaSetDevice(ctx->device);
+  if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  if (ctx->h_pinned) cudaFreeHost(ctx->h_pinned);
+  for (auto &p : ctx->ev_pending) {
+    cudaEventDestroy(p.e0);
+    cudaEventDestroy(p.e1);
+  }
+  for (auto e : ctx->ev_free) cudaEventDestroy(e);
+  if (ctx->ev0) cudaEventDestroy(ctx->ev0);
+  if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+  cudaStream_t s = ctx->stream;
+  delete ctx;  // DBuf destructors free device memory
+  if (s) cudaStreamDestroy(s);
+  return FNETG_OK;
+}
+
+const char *fnetg_last_error(const fnetg_ctx *ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+int fnetg_get_stream(fnetg_ctx *ctx, void **stream) {
+  if (!ctx || !stream) return FNETG_E_INVALID;
+  *stream = (void *)ctx->stream;
+  return FNETG_OK;
+}
+
+int fnetg_synchronize(fnetg_ctx *ctx) {
+  if (!ctx) return FNETG_E_INVALID;
+  FNETG_CUDA(cudaStreamSynchronize(ctx->stream));
+  return FNETG_OK;
+}
+
+int fnetg_profile_enable(fnetg_ctx *ctx, int32_t enable) {
+  if (!ctx) return FNETG_E_INVALID;
+  ctx->prof = enable != 0;
+  return FNETG_OK;
+}
+
+int fnetg_profile_read(fnetg_ctx *ctx, const char *name, double *ms, int64_t *launches) {
+  if (!ctx || !name) return FNETG_E_INVALID;
+  resolve_profile(ctx);
+  auto it = ctx->prof_tab.find(name);
+  if (it == ctx->prof_tab.end()) {
+    if (ms) *ms = 0.0;
+    if (launches) *launches = 0;
+    return -1;
+  }
+  if (ms) *ms = it->second.ms;
+  if (launches) *launches = it->second.launches;
+  return FNETG_OK;
+}
+
+int fnetg_profile_reset(fnetg_ctx *ctx) {
+  if (!ctx) return FNETG_E_INVALID;
+  resolve_profile(ctx);
+  ctx->prof_tab.clear();
+  ctx->launches = 0;
+  return FNETG_OK;
+}
+
+int64_t fnetg_launch_count(fnetg_ctx *ctx) { return ctx ? ctx->launches : -1; }
+
+// ---------------------------------------------------------------------------------------
+static void invalidate_geometry(fnetg_ctx *ctx) {
+  ctx->nb_valid = false;
+  ctx->feats_valid = false;
+}
+
+static int rebuild_buckets(fnetg_ctx *ctx, bool order_changes);
+
+// per-atom species code (index into the atomic numbers the G-functions reference, -1 none)
+static int refresh_codes(fnetg_ctx *ctx) {
+  std::vector<int8_t> code(std::max<int64_t>(ctx->N, 1), -1);
+  for (int64_t a = 0; a < ctx->N; a++)
+    for (size_t z = 0; z < ctx->zcodes.size(); z++)
+      if (ctx->h_atnum[a] == ctx->zcodes[z]) code[a] = (int8_t)z;
+  FNETG_CUDA(ctx->d_code.ensure(std::max<int64_t>(ctx->N, 1)));
+  if (ctx->N > 0)
+    FNETG_CUDA(cudaMemcpy(ctx->d_code.p, code.data(), ctx->N, cudaMemcpyHostToDevice));
+  return FNETG_OK;
+}
+
+int fnetg_upload_structures(fnetg_ctx *ctx, int32_t nstruct, const int64_t *atom_offsets,
+                            const int32_t *atnum, const double *coords, const int32_t *periodic,
+                            const double *latvecs, const double *ext, int32_t next) {
+  if (!ctx) return FNETG_E_INVALID;
+  FNETG_CHECK(nstruct >= 0 && atom_offsets && (nstruct == 0 || (atnum && coords)),
+              FNETG_E_INVALID, "upload_structures: null array");
+  FNETG_CHECK(atom_offsets[0] == 0, FNETG_E_SHAPE, "atom_offsets[0] must be 0");
+  for (int s = 0; s < nstruct; s++)
+    FNETG_CHECK(atom_offsets[s + 1] >= atom_offsets[s], FNETG_E_SHAPE,
+                "atom_offsets must be non-decreasing");
+  const int64_t N = atom_offsets[nstruct];
+  FNETG_CHECK(N < (int64_t(1) << 31), FNETG_E_UNSUPPORTED, "more than 2^31 atoms");
+  FNETG_CHECK(next >= 0 && (next == 0 || ext), FNETG_E_INVALID, "external features");
+  for (int64_t q = 0; q < 3 * N; q++)
+    FNETG_CHECK(std::isfinite(coords[q]), FNETG_E_GEOMETRY, "non-finite coordinate");
+  cudaSetDevice(ctx->device);
+  ctx->S = nstruct;
+  ctx->N = N;
+  ctx->next = next;
+  ctx->h_off.assign(atom_offsets, atom_offsets + nstruct + 1);
+  ctx->h_atnum.assign(atnum, atnum + N);
+  ctx->h_periodic.assign(nstruct, 0);
+  ctx->h_lat.assign((size_t)9 * nstruct, 0.0);
+  for (int s = 0; s < nstruct; s++) {
+    ctx->h_periodic[s] = periodic ? (periodic[s] != 0) : 0;
+    if (ctx->h_periodic[s]) {
+      FNETG_CHECK(latvecs, FNETG_E_INVALID, "periodic structure without lattice vectors");
+      for (int k = 0; k < 9; k++) ctx->h_lat[9 * s + k] = latvecs[9 * s + k];
+      double R[9];
+      if (recvecs2p(latvecs + 9 * s, R))
+        return fail(ctx, FNETG_E_GEOMETRY,
+                    "dependent lattice vectors in structure " + std::to_string(s));
+    }
+  }
+  std::vector<int32_t> astruct(N);
+  for (int s = 0; s < nstruct; s++)
+    for (int64_t a = atom_offsets[s]; a < atom_offsets[s + 1]; a++) astruct[a] = s;
+  // bounding boxes (float, with the structure's extent) for image pruning
+  std::vector<float> bbox((size_t)6 * std::max(nstruct, 1), 0.f);
+  std::vector<V4<float>> cf(std::max<int64_t>(N, 1));
+  for (int s = 0; s < nstruct; s++) {
+    double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+    for (int64_t a = atom_offsets[s]; a < atom_offsets[s + 1]; a++)
+      for (int c = 0; c < 3; c++) {
+        lo[c] = std::min(lo[c], coords[3 * a + c]);
+        hi[c] = std::max(hi[c], coords[3 * a + c]);
+      }
+    for (int c = 0; c < 3; c++) {
+      bbox[6 * s + c] = (float)lo[c];
+      bbox[6 * s + 3 + c] = (float)hi[c];
+    }
+  }
+  // float copies relative to each structure's bounding-box corner keep the pre-filter's
+  // rounding independent of where the structure sits in space
+  for (int s = 0; s < nstruct; s++) {
+    double ref[3];
+    for (int c = 0; c < 3; c++) ref[c] = (double)bbox[6 * s + c];
+    for (int64_t a = atom_offsets[s]; a < atom_offsets[s + 1]; a++)
+      cf[a] = V4<float>{(float)(coords[3 * a] - ref[0]), (float)(coords[3 * a + 1] - ref[1]),
+                        (float)(coords[3 * a + 2] - ref[2]), 0.f};
+    for (int c = 0; c < 3; c++) {
+      bbox[6 * s + 3 + c] = (float)((double)bbox[6 * s + 3 + c] - ref[c]);
+      bbox[6 * s + c] = 0.f;
+    }
+  }
+  FNETG_CUDA(ctx->d_off.ensure(sizeof(int64_t) * (nstruct + 1)));
+  FNETG_CUDA(ctx->d_atom_struct.ensure(sizeof(int32_t) * std::max<int64_t>(N, 1)));
+  FNETG_CUDA(ctx->d_coords.ensure(sizeof(double) * 3 * std::max<int64_t>(N, 1)));
+  FNETG_CUDA(ctx->d_coordsf.ensure(sizeof(V4<float>) * std::max<int64_t>(N, 1)));
+  FNETG_CUDA(ctx->d_atnum.ensure(sizeof(int32_t) * std::max<int64_t>(N, 1)));
+  FNETG_CUDA(ctx->d_lat.ensure(sizeof(double) * 9 * std::max(nstruct, 1)));
+  FNETG_CUDA(ctx->d_bbox.ensure(sizeof(float) * 6 * std::max(nstruct, 1)));
+  FNETG_CUDA(ctx->d_periodic.ensure(sizeof(int32_t) * std::max(nstruct, 1)));
+  cudaStream_t st = ctx->stream;
+  FNETG_CUDA(cudaMemcpyAsync(ctx->d_off.p, atom_offsets, sizeof(int64_t) * (nstruct + 1),
+                             cudaMemcpyHostToDevice, st));
+  if (N > 0) {
+    FNETG_CUDA(cudaMemcpyAsync(ctx->d_atom_struct.p, astruct.data(), sizeof(int32_t) * N,
+                               cudaMemcpyHostToDevice, st));
+    FNETG_CUDA(cudaMemcpyAsync(ctx->d_coords.p, coords, sizeof(double) * 3 * N,
+                               cudaMemcpyHostToDevice, st));
+    FNETG_CUDA(cudaMemcpyAsync(ctx->d_coordsf.p, cf.data(), sizeof(V4<float>) * N,
+                               cudaMemcpyHostToDevice, st));
+    FNETG_CUDA(cudaMemcpyAsync(ctx->d_atnum.p, atnum, sizeof(int32_t) * N,
+                               cudaMemcpyHostToDevice, st));
+  }
+  if (nstruct > 0) {
+    FNETG_CUDA(cudaMemcpyAsync(ctx->d_lat.p, ctx->h_lat.data(), sizeof(double) * 9 * nstruct,
+                               cudaMemcpyHostToDevice, st));
+    FNETG_CUDA(cudaMemcpyAsync(ctx->d_bbox.p, bbox.data(), sizeof(float) * 6 * nstruct,
+                               cudaMemcpyHostToDevice, st));
+    FNETG_CUDA(cudaMemcpyAsync(ctx->d_periodic.p, ctx->h_periodic.data(),
+                               sizeof(int32_t) * nstruct, cudaMemcpyHostToDevice, st));
+  }
+  if (next > 0 && N > 0) {
+    FNETG_CUDA(ctx->d_ext.ensure(sizeof(double) * N * next));
+    FNETG_CUDA(cudaMemcpyAsync(ctx->d_ext.p, ext, sizeof(double) * N * next,
+                               cudaMemcpyHostToDevice, st));
+  }
+  FNETG_CUDA(cudaStreamSynchronize(st));
+  invalidate_geometry(ctx);
+  ctx->targets_set = false;
+  // default: every atom in sub-network 0 until fnetg_set_species
+  ctx->h_species.assign(N, 0);
+  ctx->species_set = false;
+  int rc = refresh_codes(ctx);
+  if (rc) return rc;
+  return rebuild_buckets(ctx, true);
+}
+
+int fnetg_update_coords(fnetg_ctx *ctx, const double *coords) {
+  if (!ctx || !coords) return FNETG_E_INVALID;
+  FNETG_CHECK(ctx->N > 0, FNETG_E_INVALID, "no structures uploaded");
+  std::vector<int64_t> off = ctx->h_off;
+  std::vector<int32_t> atnum = ctx->h_atnum, per = ctx->h_periodic;
+  std::vector<double> lat = ctx->h_lat;
+  std::vector<int32_t> sp = ctx->h_species;
+  bool had_species = ctx->species_set;
+  std::vector<double> ext;
+  int32_t next = ctx->next;
+  if (next > 0) {
+    ext.resize((size_t)ctx->N * next);
+    FNETG_CUDA(cudaMemcpy(ext.data(), ctx->d_ext.p, sizeof(double) * ext.size(),
+                          cudaMemcpyDeviceToHost));
+  }
+  int rc = fnetg_upload_structures(ctx, ctx->S, off.data(), atnum.data(), coords, per.data(),
+                                   lat.data(), next ? ext.data() : nullptr, next);
+  if (rc) return rc;
+  if (had_species) return fnetg_set_species(ctx, sp.data());
+  return FNETG_OK;
+}
+
+// species buckets: rows of every sub-network contiguous, tiles never straddle species
+static int rebuild_buckets(fnetg_ctx *ctx, bool order_changes) {
+  const int64_t N = ctx->N;
+  int nsp = 1;
+  for (int64_t a = 0; a < N; a++) nsp = std::max(nsp, ctx->h_species[a] + 1);
+  if (ctx->net_set) nsp = std::max(nsp, ctx->nsp);
+  std::vector<int64_t> cnt(nsp + 1, 0);
+  for (int64_t a = 0; a < N; a++) cnt[ctx->h_species[a] + 1]++;
+  for (int s = 0; s < nsp; s++) cnt[s + 1] += cnt[s];
+  ctx->h_bucket_off = cnt;
+  std::vector<int32_t> bpos(std::max<int64_t>(N, 1)), bperm(std::max<int64_t>(N, 1));
+  std::vector<int64_t> fill(cnt.begin(), cnt.end() - 1);
+  for (int64_t a = 0; a < N; a++) {
+    int64_t r = fill[ctx->h_species[a]]++;
+    bpos[a] = (int32_t)r;
+    bperm[r] = (int32_t)a;
+  }
+  ctx->tile_rows = ctx->prec == FNETG_FP64 ? 32 : 64;
+  std::vector<int32_t> tiles;
+  for (int s = 0; s < nsp; s++)
+    for (int64_t r = cnt[s]; r < cnt[s + 1]; r += ctx->tile_rows) {
+      tiles.push_back(s);
+      tiles.push_back((int32_t)r);
+      tiles.push_back((int32_t)std::min<int64_t>(ctx->tile_rows, cnt[s + 1] - r));
+      tiles.push_back(0);
+    }
+  ctx->ntiles = (int64_t)tiles.size() / 4;
+  // first tile of every species (tiles are grouped by species in order)
+  std::vector<int64_t> t0(nsp + 1, 0);
+  for (int64_t t = 0; t < ctx->ntiles; t++) t0[tiles[4 * t] + 1]++;
+  for (int s = 0; s < nsp; s++) t0[s + 1] += t0[s];
+  FNETG_CUDA(ctx->d_sp_tile0.ensure(sizeof(int64_t) * (nsp + 1)));
+  FNETG_CUDA(cudaMemcpy(ctx->d_sp_tile0.p, t0.data(), sizeof(int64_t) * (nsp + 1),
+                        cudaMemcpyHostToDevice));
+  FNETG_CUDA(ctx->d_species.ensure(sizeof(int32_t) * std::max<int64_t>(N, 1)));
+  FNETG_CUDA(ctx->d_bpos.ensure(sizeof(int32_t) * std::max<int64_t>(N, 1)));
+  FNETG_CUDA(ctx->d_bperm.ensure(sizeof(int32_t) * std::max<int64_t>(N, 1)));
+  FNETG_CUDA(ctx->d_tiles.ensure(sizeof(int32_t) * std::max<size_t>(tiles.size(), 4)));
+  if (N > 0) {
+    FNETG_CUDA(cudaMemcpy(ctx->d_species.p, ctx->h_species.data(), sizeof(int32_t) * N,
+                          cudaMemcpyHostToDevice));
+    FNETG_CUDA(cudaMemcpy(ctx->d_bpos.p, bpos.data(), sizeof(int32_t) * N, cudaMemcpyHostToDevice));
+    FNETG_CUDA(cudaMemcpy(ctx->d_bperm.p, bperm.data(), sizeof(int32_t) * N,
+                          cudaMemcpyHostToDevice));
+  }
+  if (!tiles.empty())
+    FNETG_CUDA(cudaMemcpy(ctx->d_tiles.p, tiles.data(), sizeof(int32_t) * tiles.size(),
+                          cudaMemcpyHostToDevice));
+  if (order_changes) ctx->feats_valid = false;
+  return FNETG_OK;
+}
+
+int fnetg_set_species(fnetg_ctx *ctx, const int32_t *species) {
+  if (!ctx || (!species && ctx->N > 0)) return FNETG_E_INVALID;
+  for (int64_t a = 0; a < ctx->N; a++)
+    FNETG_CHECK(species[a] >= 0 && species[a] < 1024, FNETG_E_INVALID, "species index");
+  if (ctx->net_set)
+    for (int64_t a = 0; a < ctx->N; a++)
+      FNETG_CHECK(species[a] < ctx->nsp, FNETG_E_SHAPE, "species index >= number of networks");
+  ctx->h_species.assign(species, species + ctx->N);
+  ctx->species_set = true;
+  // features are stored in bucket order; a new order needs a fresh featurisation
+  return rebuild_buckets(ctx, true);
+}
+
+// ---------------------------------------------------------------------------------------
+int fnetg_set_gfunctions(fnetg_ctx *ctx, int32_t ng, const fnetg_gfunc *g) {
+  if (!ctx || ng < 0 || (ng > 0 && !g)) return FNETG_E_INVALID;
+  FNETG_CHECK(ng <= 4096, FNETG_E_UNSUPPORTED, "more than 4096 G-functions");
+  std::vector<int32_t> zs;
+  std::set<double> rset;
+  for (int k = 0; k < ng; k++) {
+    const fnetg_gfunc &f = g[k];
+    FNETG_CHECK(f.type >= 1 && f.type <= 5, FNETG_E_INVALID, "G-function type must be 1..5");
+    FNETG_CHECK(f.rcut > 0.0 && std::isfinite(f.rcut), FNETG_E_INVALID, "cutoff must be > 0");
+    FNETG_CHECK(f.atomid >= 0, FNETG_E_INVALID, "atomid must be >= 0");
+    if (f.atomid > 0)
+      FNETG_CHECK(f.atomid <= ctx->next, FNETG_E_SHAPE, "atomid beyond the external features");
+    rset.insert(f.rcut);
+    for (int z : {f.z1, f.z2})
+      if (z != 0 && std::find(zs.begin(), zs.end(), z) == zs.end()) zs.push_back(z);
+  }
+  FNETG_CHECK((int)zs.size() <= kMaxSpeciesCodes, FNETG_E_UNSUPPORTED,
+              "more than 8 distinct atomic numbers in the G-functions");
+  FNETG_CHECK((int)rset.size() <= kMaxRcutClasses, FNETG_E_UNSUPPORTED,
+              "more than 8 distinct cutoffs");
+  ctx->gf.assign(g, g + ng);
+  ctx->zcodes = zs;
+  ctx->rcut_classes.assign(rset.begin(), rset.end());
+  auto code_of = [&](int z) -> int {
+    if (z == 0) return -1;
+    return (int)(std::find(zs.begin(), zs.end(), z) - zs.begin());
+  };
+  auto rclass_of = [&](double r) -> int {
+    return (int)(std::find(ctx->rcut_classes.begin(), ctx->rcut_classes.end(), r) -
+                 ctx->rcut_classes.begin());
+  };
+  ctx->h_rad.clear();
+  ctx->h_ang.clear();
+  ctx->h_groups.clear();
+  ctx->ecls_eta.clear();
+  ctx->ecls_rclass.clear();
+  ctx->ecls_atomid.clear();
+  std::vector<GDesc> ang;
+  for (int k = 0; k < ng; k++) {
+    const fnetg_gfunc &f = g[k];
+    GDesc d{};
+    d.type = f.type;
+    bool resolved = !(f.z1 == 0 && f.z2 == 0);
+    d.chan1 = resolved ? code_of(f.z1) : -1;
+    d.chan2 = resolved ? (f.type >= 4 ? code_of(f.z2) : d.chan1) : -1;
+    d.atomid = f.atomid;
+    d.out = k;
+    d.rclass = rclass_of(f.rcut);
+    d.rcut = f.rcut;
+    d.kappa = f.kappa;
+    d.rs = f.rs;
+    d.eta = f.eta;
+    d.lambda = f.lambda;
+    d.xi = f.xi;
+    d.pref = std::pow(2.0, 1.0 - f.xi);
+    d.xi_int = (f.xi >= 1.0 && f.xi <= 16.0 && f.xi == std::floor(f.xi)) ? (int)f.xi : 0;
+    d.eclass = -1;
+    if (f.type >= 4) {
+      int e = -1;
+      for (size_t q = 0; q < ctx->ecls_eta.size(); q++)
+        if (ctx->ecls_eta[q] == f.eta && ctx->ecls_rclass[q] == d.rclass &&
+            ctx->ecls_atomid[q] == f.atomid)
+          e = (int)q;
+      if (e < 0) {
+        FNETG_CHECK((int)ctx->ecls_eta.size() < kMaxEtaClasses, FNETG_E_UNSUPPORTED,
+                    "more than 16 distinct (eta, cutoff, atomid) among angular functions");
+        e = (int)ctx->ecls_eta.size();
+        ctx->ecls_eta.push_back(f.eta);
+        ctx->ecls_rclass.push_back(d.rclass);
+        ctx->ecls_atomid.push_back(f.atomid);
+      }
+      d.eclass = e;
+      ang.push_back(d);
+    } else {
+      ctx->h_rad.push_back(d);
+    }
+  }
+  // group angular functions by list channels, cutoff and atom-id column (stable), at most
+  // kMaxGroupFuncs per group
+  std::vector<std::array<int, 4>> chans;
+  for (auto &d : ang) {
+    std::array<int, 4> c{d.chan1, d.chan2, d.rclass, d.atomid};
+    if (std::find(chans.begin(), chans.end(), c) == chans.end()) chans.push_back(c);
+  }
+  for (auto &c : chans) {
+    std::vector<GDesc> members;
+    for (auto &d : ang)
+      if (d.chan1 == c[0] && d.chan2 == c[1] && d.rclass == c[2] && d.atomid == c[3])
+        members.push_back(d);
+    for (size_t q0 = 0; q0 < members.size(); q0 += kMaxGroupFuncs) {
+      AGroup grp{};
+      grp.chan1 = c[0];
+      grp.chan2 = c[1];
+      grp.same = (c[0] == c[1]) ? 1 : 0;
+      grp.atomid = c[3];
+      grp.first = (int)ctx->h_ang.size();
+      grp.count = (int)std::min<size_t>(kMaxGroupFuncs, members.size() - q0);
+      grp.has_g4 = 0;
+      for (int q = 0; q < grp.count; q++) {
+        ctx->h_ang.push_back(members[q0 + q]);
+        if (members[q0 + q].type == 4) grp.has_g4 = 1;
+      }
+      ctx->h_groups.push_back(grp);
+    }
+  }
+  FNETG_CUDA(ctx->d_rad.ensure(sizeof(GDesc) * std::max<size_t>(ctx->h_rad.size(), 1)));
+  FNETG_CUDA(ctx->d_ang.ensure(sizeof(GDesc) * std::max<size_t>(ctx->h_ang.size(), 1)));
+  FNETG_CUDA(ctx->d_groups.ensure(sizeof(AGroup) * std::max<size_t>(ctx->h_groups.size(), 1)));
+  FNETG_CUDA(ctx->d_ecls_eta.ensure(sizeof(double) * kMaxEtaClasses));
+  FNETG_CUDA(ctx->d_ecls_rclass.ensure(sizeof(int) * kMaxEtaClasses));
+  FNETG_CUDA(ctx->d_ecls_atomid.ensure(sizeof(int) * kMaxEtaClasses));
+  FNETG_CUDA(ctx->d_rcls.ensure(sizeof(double) * kMaxRcutClasses));
+  if (!ctx->h_rad.empty())
+    FNETG_CUDA(cudaMemcpy(ctx->d_rad.p, ctx->h_rad.data(), sizeof(GDesc) * ctx->h_rad.size(),
+                          cudaMemcpyHostToDevice));
+  if (!ctx->h_ang.empty())
+    FNETG_CUDA(cudaMemcpy(ctx->d_ang.p, ctx->h_ang.data(), sizeof(GDesc) * ctx->h_ang.size(),
+                          cudaMemcpyHostToDevice));
+  if (!ctx->h_groups.empty())
+    FNETG_CUDA(cudaMemcpy(ctx->d_groups.p, ctx->h_groups.data(),
+                          sizeof(AGroup) * ctx->h_groups.size(), cudaMemcpyHostToDevice));
+  if (!ctx->ecls_eta.empty()) {
+    FNETG_CUDA(cudaMemcpy(ctx->d_ecls_eta.p, ctx->ecls_eta.data(),
+                          sizeof(double) * ctx->ecls_eta.size(), cudaMemcpyHostToDevice));
+    FNETG_CUDA(cudaMemcpy(ctx->d_ecls_rclass.p, ctx->ecls_rclass.data(),
+                          sizeof(int) * ctx->ecls_rclass.size(), cudaMemcpyHostToDevice));
+    FNETG_CUDA(cudaMemcpy(ctx->d_ecls_atomid.p, ctx->ecls_atomid.data(),
+                          sizeof(int) * ctx->ecls_atomid.size(), cudaMemcpyHostToDevice));
+  }
+  if (!ctx->rcut_classes.empty())
+    FNETG_CUDA(cudaMemcpy(ctx->d_rcls.p, ctx->rcut_classes.data(),
+                          sizeof(double) * ctx->rcut_classes.size(), cudaMemcpyHostToDevice));
+  ctx->nb_valid = false;
+  ctx->feats_valid = false;
+  ctx->zprec_valid = false;
+  ctx->nf = ng + (int)ctx->ext_idx.size();
+  return refresh_codes(ctx);
+}
+
+int fnetg_neighbors(fnetg_ctx *ctx, double rcut, int64_t *npairs) {
+  if (!ctx) return FNETG_E_INVALID;
+  if (rcut <= 0.0) {
+    FNETG_CHECK(!ctx->rcut_classes.empty(), FNETG_E_INVALID,
+                "neighbors: no cutoff given and no G-functions set");
+    rcut = ctx->rcut_classes.back();
+  }
+  int rc = run_neighbors(ctx, rcut);
+  if (rc) return rc;
+  if (npairs) *npairs = ctx->P;
+  return FNETG_OK;
+}
+
+int fnetg_get_neighbors(fnetg_ctx *ctx, int64_t *pair_offsets, int32_t *j, int32_t *shift,
+                        double *d2) {
+  if (!ctx) return FNETG_E_INVALID;
+  FNETG_CHECK(ctx->nb_valid, FNETG_E_INVALID, "get_neighbors: no neighbour list");
+  FNETG_CUDA(cudaStreamSynchronize(ctx->stream));
+  const int64_t N = ctx->N, P = ctx->P;
+  std::vector<int64_t> off(N + 1);
+  FNETG_CUDA(cudaMemcpy(off.data(), ctx->d_poff.p, sizeof(int64_t) * (N + 1),
+                        cudaMemcpyDeviceToHost));
+  if (pair_offsets) memcpy(pair_offsets, off.data(), sizeof(int64_t) * (N + 1));
+  if (j && P > 0) {
+    FNETG_CUDA(cudaMemcpy(j, ctx->d_pj.p, sizeof(int32_t) * P, cudaMemcpyDeviceToHost));
+    // convert to structure-local indices
+    for (int s = 0; s < ctx->S; s++)
+      for (int64_t a = ctx->h_off[s]; a < ctx->h_off[s + 1]; a++)
+        for (int64_t q = off[a]; q < off[a + 1]; q++) j[q] -= (int32_t)ctx->h_off[s];
+  }
+  if (shift && P > 0) {
+    std::vector<uint32_t> meta(P);
+    FNETG_CUDA(cudaMemcpy(meta.data(), ctx->d_pmeta.p, sizeof(uint32_t) * P,
+                          cudaMemcpyDeviceToHost));
+    for (int64_t q = 0; q < P; q++)
+      for (int c = 0; c < 3; c++) shift[3 * q + c] = (int32_t)(int8_t)((meta[q] >> (8 * c)) & 0xff);
+  }
+  if (d2 && P > 0)
+    FNETG_CUDA(cudaMemcpy(d2, ctx->d_d2.p, sizeof(double) * P, cudaMemcpyDeviceToHost));
+  return FNETG_OK;
+}
+
+int fnetg_acsf(fnetg_ctx *ctx, double *vals) {
+  if (!ctx) return FNETG_E_INVALID;
+  FNETG_CHECK(!ctx->gf.empty(), FNETG_E_INVALID, "acsf: no G-functions set");
+  if (!ctx->nb_valid) {
+    int rc = run_neighbors(ctx, ctx->rcut_classes.back());
+    if (rc) return rc;
+  }
+  int rc = run_acsf(ctx);
+  if (rc) return rc;
+  rc = run_ext_inputs(ctx);
+  if (rc) return rc;
+  ctx->zprec_valid = false;
+  if (vals) {
+    const int ng = (int)ctx->gf.size();
+    int32_t nf = 0;
+    std::vector<double> all((size_t)ctx->N * ctx->nf);
+    rc = fnetg_get_features(ctx, all.data(), &nf);
+    if (rc) return rc;
+    for (int64_t a = 0; a < ctx->N; a++)
+      for (int k = 0; k < ng; k++) vals[a * ng + k] = all[a * nf + k];
+  }
+  return FNETG_OK;
+}
+
+int fnetg_acsf_zscore(fnetg_ctx *ctx, const int32_t *weights, double *zprec, int32_t compute) {
+  if (!ctx || !zprec) return FNETG_E_INVALID;
+  FNETG_CHECK(ctx->feats_valid, FNETG_E_INVALID, "acsf_zscore: no features computed");
+  const int ng = (int)ctx->gf.size();
+  if (!compute) ctx->h_zprec.assign(zprec, zprec + 2 * ng);
+  int rc = run_zscore(ctx, weights, compute != 0);
+  if (rc) return rc;
+  if (compute) memcpy(zprec, ctx->h_zprec.data(), sizeof(double) * 2 * ng);
+  ctx->zprec_valid = true;
+  return FNETG_OK;
+}
+
+int fnetg_set_external_inputs(fnetg_ctx *ctx, int32_t n, const int32_t *indices) {
+  if (!ctx || n < 0 || (n > 0 && !indices)) return FNETG_E_INVALID;
+  for (int k = 0; k < n; k++)
+    FNETG_CHECK(indices[k] >= 1 && indices[k] <= ctx->next, FNETG_E_SHAPE,
+                "external input index out of range");
+  ctx->ext_idx.assign(indices, indices + n);
+  ctx->nf = (int)ctx->gf.size() + n;
+  ctx->feats_valid = false;
+  return FNETG_OK;
+}
+
+int fnetg_get_features(fnetg_ctx *ctx, double *feats, int32_t *nf_out) {
+  if (!ctx) return FNETG_E_INVALID;
+  FNETG_CHECK(ctx->feats_valid, FNETG_E_INVALID, "get_features: no features computed");
+  FNETG_CUDA(cudaStreamSynchronize(ctx->stream));
+  const int nf = ctx->nf;
+  if (nf_out) *nf_out = nf;
+  if (!feats) return FNETG_OK;
+  const int64_t N = ctx->N;
+  std::vector<int32_t> bpos(N);
+  if (N > 0)
+    FNETG_CUDA(cudaMemcpy(bpos.data(), ctx->d_bpos.p, sizeof(int32_t) * N, cudaMemcpyDeviceToHost));
+  if (ctx->prec == FNETG_FP64) {
+    std::vector<double> buf((size_t)N * nf);
+    if (N > 0)
+      FNETG_CUDA(cudaMemcpy(buf.data(), ctx->d_feat.p, sizeof(double) * buf.size(),
+                            cudaMemcpyDeviceToHost));
+    for (int64_t a = 0; a < N; a++)
+      for (int k = 0; k < nf; k++) feats[a * nf + k] = buf[(size_t)bpos[a] * nf + k];
+  } else {
+    std::vector<float> buf((size_t)N * nf);
+    if (N > 0)
+      FNETG_CUDA(cudaMemcpy(buf.data(), ctx->d_feat.p, sizeof(float) * buf.size(),
+                            cudaMemcpyDeviceToHost));
+    for (int64_t a = 0; a < N; a++)
+      for (int k = 0; k < nf; k++) feats[a * nf + k] = buf[(size_t)bpos[a] * nf + k];
+  }
+  return FNETG_OK;
+}
+
+int fnetg_set_features(fnetg_ctx *ctx, int32_t nf, const double *feats) {
+  if (!ctx || nf <= 0 || (!feats && ctx->N > 0)) return FNETG_E_INVALID;
+  const int64_t N = ctx->N;
+  std::vector<int32_t> bpos(std::max<int64_t>(N, 1));
+  if (N > 0)
+    FNETG_CUDA(cudaMemcpy(bpos.data(), ctx->d_bpos.p, sizeof(int32_t) * N, cudaMemcpyDeviceToHost));
+  const size_t es = ctx->prec == FNETG_FP64 ? 8 : 4;
+  FNETG_CUDA(ctx->d_feat.ensure(es * std::max<int64_t>(N, 1) * nf));
+  if (ctx->prec == FNETG_FP64) {
+    std::vector<double> buf((size_t)N * nf);
+    for (int64_t a = 0; a < N; a++)
+      for (int k = 0; k < nf; k++) buf[(size_t)bpos[a] * nf + k] = feats[a * nf + k];
+    if (N > 0)
+      FNETG_CUDA(cudaMemcpy(ctx->d_feat.p, buf.data(), 8 * buf.size(), cudaMemcpyHostToDevice));
+  } else {
+    std::vector<float> buf((size_t)N * nf);
+    for (int64_t a = 0; a < N; a++)
+      for (int k = 0; k < nf; k++) buf[(size_t)bpos[a] * nf + k] = (float)feats[a * nf + k];
+    if (N > 0)
+      FNETG_CUDA(cudaMemcpy(ctx->d_feat.p, buf.data(), 4 * buf.size(), cudaMemcpyHostToDevice));
+  }
+  ctx->nf = nf;
+  ctx->feats_valid = true;
+  ctx->zprec_valid = false;
+  return FNETG_OK;
+}
+
+// ---------------------------------------------------------------------------------------
+int64_t fnetg_nparams(int32_t nlayer, const int32_t *dims) {
+  if (nlayer < 2 || !dims) return -1;
+  int64_t n = 0;
+  for (int l = 0; l < nlayer - 1; l++) n += (int64_t)dims[l] * dims[l + 1];
+  n += dims[nlayer - 1];
+  for (int l = 0; l < nlayer; l++) n += dims[l];
+  return n;
+}
+
+int fnetg_set_network(fnetg_ctx *ctx, int32_t nspecies, int32_t nlayer, const int32_t *dims,
+                      int32_t activation, const double *params) {
+  if (!ctx || !dims || !params) return FNETG_E_INVALID;
+  FNETG_CHECK(nspecies >= 1 && nspecies <= 64, FNETG_E_INVALID, "1..64 sub-networks");
+  FNETG_CHECK(nlayer >= 2 && nlayer <= kMaxLayers, FNETG_E_UNSUPPORTED, "2..16 layers");
+  FNETG_CHECK(activation >= 0 && activation <= 9, FNETG_E_INVALID, "activation code");
+  for (int l = 0; l < nlayer; l++)
+    FNETG_CHECK(dims[l] >= 1 && dims[l] <= kMaxWidth, FNETG_E_UNSUPPORTED,
+                "layer widths must be 1..256");
+  for (int64_t a = 0; a < ctx->N; a++)
+    FNETG_CHECK(ctx->h_species[a] < nspecies, FNETG_E_SHAPE,
+                "an atom's species index exceeds the number of sub-networks");
+  ctx->nsp = nspecies;
+  ctx->nlayer = nlayer;
+  ctx->dims.assign(dims, dims + nlayer);
+  ctx->act = activation;
+  ctx->nparams = fnetg_nparams(nlayer, dims);
+  ctx->woff.assign(nlayer, 0);
+  ctx->boff.assign(nlayer, 0);
+  int64_t ind = 0;
+  for (int l = 0; l < nlayer; l++) {
+    ctx->woff[l] = ind;
+    ind += (int64_t)dims[l] * (l < nlayer - 1 ? dims[l + 1] : 1);
+  }
+  for (int l = 0; l < nlayer; l++) {
+    ctx->boff[l] = ind;
+    ind += dims[l];
+  }
+  const size_t n = (size_t)nspecies * ctx->nparams;
+  for (size_t q = 0; q < n; q++)
+    FNETG_CHECK(std::isfinite(params[q]), FNETG_E_INVALID, "non-finite network parameter");
+  FNETG_CUDA(ctx->d_params64.ensure(sizeof(double) * n));
+  FNETG_CUDA(ctx->d_params.ensure((ctx->prec == FNETG_FP64 ? 8 : 4) * n));
+  FNETG_CUDA(cudaMemcpy(ctx->d_params64.p, params, sizeof(double) * n, cudaMemcpyHostToDevice));
+  ctx->net_set = true;
+  ctx->opt_set = false;
+  // the bucket order depends on the species only: features stay valid
+  int rc = rebuild_buckets(ctx, false);
+  if (rc) return rc;
+  return run_params_to_compute(ctx);
+}
+
+int fnetg_get_params(fnetg_ctx *ctx, double *params) {
+  if (!ctx || !params) return FNETG_E_INVALID;
+  FNETG_CHECK(ctx->net_set, FNETG_E_INVALID, "get_params: no network");
+  FNETG_CUDA(cudaStreamSynchronize(ctx->stream));
+  FNETG_CUDA(cudaMemcpy(params, ctx->d_params64.p, sizeof(double) * ctx->nsp * ctx->nparams,
+                        cudaMemcpyDeviceToHost));
+  return FNETG_OK;
+}
+
+static int check_ready_for_network(fnetg_ctx *ctx) {
+  FNETG_CHECK(ctx->net_set, FNETG_E_INVALID, "no network set");
+  FNETG_CHECK(ctx->feats_valid, FNETG_E_INVALID, "no features computed");
+  FNETG_CHECK(ctx->nf == ctx->dims[0], FNETG_E_SHAPE,
+              "network input width differs from the number of features");
+  return FNETG_OK;
+}
+
+int fnetg_predict(fnetg_ctx *ctx, double *atomic_out, double *global_out) {
+  if (!ctx) return FNETG_E_INVALID;
+  int rc = check_ready_for_network(ctx);
+  if (rc) return rc;
+  rc = run_predict(ctx);
+  if (rc) return rc;
+  if (!atomic_out && !global_out) return FNETG_OK;
+  FNETG_CUDA(cudaStreamSynchronize(ctx->stream));
+  const int nout = ctx->dims.back();
+  std::vector<double> out((size_t)ctx->N * nout);
+  if (ctx->N > 0)
+    FNETG_CUDA(cudaMemcpy(out.data(), ctx->d_out.p, sizeof(double) * out.size(),
+                          cudaMemcpyDeviceToHost));
+  if (atomic_out) memcpy(atomic_out, out.data(), sizeof(double) * out.size());
+  if (global_out) {
+    for (int s = 0; s < ctx->S; s++)
+      for (int o = 0; o < nout; o++) {
+        double acc = 0.0;
+        for (int64_t a = ctx->h_off[s]; a < ctx->h_off[s + 1]; a++) acc += out[a * nout + o];
+        global_out[(size_t)s * nout + o] = acc;
+      }
+  }
+  return FNETG_OK;
+}
+
+int fnetg_jacobian(fnetg_ctx *ctx, double *jac) {
+  if (!ctx || !jac) return FNETG_E_INVALID;
+  int rc = check_ready_for_network(ctx);
+  if (rc) return rc;
+  const int nout = ctx->dims.back(), nf = ctx->nf;
+  const int64_t N = ctx->N;
+  std::vector<double> buf((size_t)std::max<int64_t>(N, 1) * nf);
+  for (int o = 0; o < nout; o++) {
+    rc = run_jacobian(ctx, o, nullptr);
+    if (rc) return rc;
+    FNETG_CUDA(cudaStreamSynchronize(ctx->stream));
+    if (N > 0)
+      FNETG_CUDA(cudaMemcpy(buf.data(), ctx->d_jac.p, sizeof(double) * N * nf,
+                            cudaMemcpyDeviceToHost));
+    for (int64_t a = 0; a < N; a++)
+      for (int f = 0; f < nf; f++) jac[(a * nout + o) * nf + f] = buf[a * nf + f];
+  }
+  return FNETG_OK;
+}
+
+int fnetg_forces(fnetg_ctx *ctx, double *forces) {
+  if (!ctx) return FNETG_E_INVALID;
+  int rc = check_ready_for_network(ctx);
+  if (rc) return rc;
+  FNETG_CHECK(ctx->nb_valid, FNETG_E_INVALID, "forces: no neighbour list");
+  rc = run_forces(ctx);
+  if (rc) return rc;
+  if (forces) {
+    FNETG_CUDA(cudaStreamSynchronize(ctx->stream));
+    const int nout = ctx->dims.back();
+    if (ctx->N > 0)
+      FNETG_CUDA(cudaMemcpy(forces, ctx->d_forces.p, sizeof(double) * ctx->N * nout * 3,
+                            cudaMemcpyDeviceToHost));
+  }
+  return FNETG_OK;
+}
+
+// ---------------------------------------------------------------------------------------
+int fnetg_set_targets(fnetg_ctx *ctx, int32_t ngt, int32_t nat, const double *gt,
+                      const double *at, const double *atomic_w, const int32_t *weights) {
+  if (!ctx || ngt < 0 || nat < 0) return FNETG_E_INVALID;
+  FNETG_CHECK(ngt + nat > 0, FNETG_E_INVALID, "no targets");
+  FNETG_CHECK(ngt == 0 || gt, FNETG_E_INVALID, "global targets missing");
+  FNETG_CHECK(nat == 0 || at, FNETG_E_INVALID, "atomic targets missing");
+  const int64_t N = ctx->N;
+  const int S = ctx->S;
+  ctx->ngt = ngt;
+  ctx->nat = nat;
+  std::vector<double> aw(std::max<int64_t>(N, 1), 1.0);
+  if (atomic_w) aw.assign(atomic_w, atomic_w + N);
+  std::vector<int32_t> w(std::max(S, 1), 1);
+  if (weights) w.assign(weights, weights + S);
+  double sw = 0.0;
+  for (int s = 0; s < S; s++) sw += (double)w[s];
+  ctx->sum_weights = sw;
+  // per-structure sum of atomic weights (loss weighting, loss.F90:556-559)
+  std::vector<double> saw(std::max(S, 1), 0.0);
+  for (int s = 0; s < S; s++) {
+    double acc = 0.0;
+    for (int64_t a = ctx->h_off[s]; a < ctx->h_off[s + 1]; a++) acc = acc + aw[a];
+    saw[s] = acc;
+  }
+  FNETG_CUDA(ctx->d_gt.ensure(sizeof(double) * std::max<int64_t>((int64_t)S * ngt, 1)));
+  FNETG_CUDA(ctx->d_at.ensure(sizeof(double) * std::max<int64_t>(N * nat, 1)));
+  FNETG_CUDA(ctx->d_aw.ensure(sizeof(double) * std::max<int64_t>(N, 1)));
+  FNETG_CUDA(ctx->d_w.ensure(sizeof(int32_t) * std::max(S, 1)));
+  FNETG_CUDA(ctx->d_struct_aw.ensure(sizeof(double) * std::max(S, 1)));
+  if (ngt > 0 && S > 0)
+    FNETG_CUDA(cudaMemcpy(ctx->d_gt.p, gt, sizeof(double) * S * ngt, cudaMemcpyHostToDevice));
+  if (nat > 0 && N > 0)
+    FNETG_CUDA(cudaMemcpy(ctx->d_at.p, at, sizeof(double) * N * nat, cudaMemcpyHostToDevice));
+  if (N > 0)
+    FNETG_CUDA(cudaMemcpy(ctx->d_aw.p, aw.data(), sizeof(double) * N, cudaMemcpyHostToDevice));
+  if (S > 0) {
+    FNETG_CUDA(cudaMemcpy(ctx->d_w.p, w.data(), sizeof(int32_t) * S, cudaMemcpyHostToDevice));
+    FNETG_CUDA(cudaMemcpy(ctx->d_struct_aw.p, saw.data(), sizeof(double) * S,
+                          cudaMemcpyHostToDevice));
+  }
+  ctx->targets_set = true;
+  return FNETG_OK;
+}
+
+int fnetg_train_gradients(fnetg_ctx *ctx, int32_t loss, const int32_t *order, double *grad,
+                          double *loss_out, double *atomic_out) {
+  if (!ctx) return FNETG_E_INVALID;
+  int rc = check_ready_for_network(ctx);
+  if (rc) return rc;
+  FNETG_CHECK(ctx->targets_set, FNETG_E_INVALID, "train_gradients: no targets");
+  FNETG_CHECK(ctx->ngt + ctx->nat == ctx->dims.back(), FNETG_E_SHAPE,
+              "network outputs must equal the number of targets");
+  FNETG_CHECK(loss >= 0 && loss <= 3, FNETG_E_INVALID, "loss code");
+  rc = run_train_gradients(ctx, loss, order, true);
+  if (rc) return rc;
+  FNETG_CUDA(cudaStreamSynchronize(ctx->stream));
+  if (grad)
+    FNETG_CUDA(cudaMemcpy(grad, ctx->d_grad64.p, sizeof(double) * ctx->nsp * ctx->nparams,
+                          cudaMemcpyDeviceToHost));
+  if (loss_out)
+    FNETG_CUDA(cudaMemcpy(loss_out, ctx->d_scalars.p, sizeof(double), cudaMemcpyDeviceToHost));
+  if (atomic_out && ctx->N > 0)
+    FNETG_CUDA(cudaMemcpy(atomic_out, ctx->d_out.p, sizeof(double) * ctx->N * ctx->dims.back(),
+                          cudaMemcpyDeviceToHost));
+  return FNETG_OK;
+}
+
+int fnetg_update_prepare(fnetg_ctx *ctx, double *grad, double strength, double alpha,
+                         double *grad_norm) {
+  if (!ctx || !grad) return FNETG_E_INVALID;
+  FNETG_CHECK(ctx->net_set, FNETG_E_INVALID, "update_prepare: no network");
+  FNETG_CHECK(ctx->sum_weights > 0.0 || !ctx->targets_set, FNETG_E_INVALID, "sum of weights");
+  const size_t n = (size_t)ctx->nsp * ctx->nparams;
+  FNETG_CUDA(ctx->d_grad64.ensure(sizeof(double) * n));
+  FNETG_CUDA(cudaMemcpyAsync(ctx->d_grad64.p, grad, sizeof(double) * n, cudaMemcpyHostToDevice,
+                             ctx->stream));
+  if (!ctx->targets_set) ctx->sum_weights = 1.0;
+  int rc = run_update_prepare(ctx, strength, alpha);
+  if (rc) return rc;
+  FNETG_CUDA(cudaStreamSynchronize(ctx->stream));
+  FNETG_CUDA(cudaMemcpy(grad, ctx->d_grad64.p, sizeof(double) * n, cudaMemcpyDeviceToHost));
+  if (grad_norm)
+    FNETG_CUDA(cudaMemcpy(grad_norm, ctx->d_scalars.as<double>() + 1, sizeof(double),
+                          cudaMemcpyDeviceToHost));
+  return FNETG_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,214 @@
+// Internal definitions of the fnetg library (context, device buffers, launch plumbing).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "../../include/fnetg.h"
+
+namespace fnetg {
+
+// ---------------------------------------------------------------------------------------
+// small vector types with explicit alignment (the deprecated double4 is avoided)
+template <typename T> struct __align__(4 * sizeof(T)) V4 { T x, y, z, w; };
+
+constexpr int kMaxSpeciesCodes = 8;   // distinct atomic numbers referenced by G-functions
+constexpr int kMaxRcutClasses = 8;    // distinct cutoffs in one G-function set
+constexpr int kMaxEtaClasses = 16;    // distinct (eta, rcut, atomid) of angular functions
+constexpr int kMaxGroupFuncs = 32;    // angular functions evaluated together per channel
+constexpr int kMaxLayers = 16;
+constexpr int kMaxWidth = 256;        // widest network layer supported by the SIMT MLP
+
+// G-function descriptor as the kernels see it (prepared on the host).
+struct GDesc {
+  int type;     // 1..5
+  int chan1;    // species code of list 1, -1 = all atoms (unresolved)
+  int chan2;    // species code of list 2 (angular), -1 = all atoms
+  int atomid;   // 0 or 1-based external-feature column
+  int out;      // output column in the feature row
+  int rclass;   // cutoff class
+  int eclass;   // E-table class (angular), -1 if none
+  int xi_int;   // xi as an integer in [1, 16] if integral, else 0
+  double rcut, kappa, rs, eta, lambda, xi, pref;  // pref = 2^(1 - xi)
+};
+
+// A group of angular functions sharing list channels (evaluated in one triplet sweep).
+struct AGroup {
+  int chan1, chan2;  // species codes, -1 = all
+  int same;          // 1 if the two lists are the same list (Z1 == Z2 or unresolved)
+  int first, count;  // range into the angular descriptor array
+  int has_g4;
+  int atomid;        // shared by every function of the group (0 = none)
+};
+
+// Device buffer with grow-only reallocation.
+struct DBuf {
+  void *p = nullptr;
+  size_t bytes = 0;
+  ~DBuf() { release(); }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+  }
+  cudaError_t ensure(size_t n) {
+    if (n <= bytes && p) return cudaSuccess;
+    release();
+    if (n == 0) n = 16;
+    cudaError_t e = cudaMalloc(&p, n);
+    if (e == cudaSuccess) bytes = n;
+    else p = nullptr;
+    return e;
+  }
+  template <typename T> T *as() const { return static_cast<T *>(p); }
+};
+
+struct ProfEntry {
+  double ms = 0.0;
+  int64_t launches = 0;
+};
+
+struct PendingLaunch {
+  const char *name;
+  cudaEvent_t e0, e1;
+};
+
+}  // namespace fnetg
+
+struct fnetg_ctx {
+  int prec = FNETG_FP32;
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::string err;
+
+  // structures
+  int32_t S = 0;
+  int64_t N = 0;
+  std::vector<int64_t> h_off;
+  std::vector<int32_t> h_atnum, h_periodic;
+  std::vector<double> h_lat;
+  int32_t next = 0;
+  fnetg::DBuf d_off, d_atom_struct, d_coords, d_coordsf, d_atnum, d_lat, d_ranges, d_bbox,
+      d_ext, d_periodic;
+
+  // species (sub-network index per atom) and bucketing
+  bool species_set = false;
+  std::vector<int32_t> h_species;
+  std::vector<int64_t> h_bucket_off;  // [nsp+1] rows of every species bucket
+  std::vector<int64_t> h_tiles;       // packed (species, row0, nrows) triples for MLP tiles
+  fnetg::DBuf d_species, d_bpos, d_bperm, d_tiles;
+  int64_t ntiles = 0;
+  int tile_rows = 0;
+
+  // G-functions
+  std::vector<fnetg_gfunc> gf;
+  std::vector<fnetg::GDesc> h_rad, h_ang;
+  std::vector<fnetg::AGroup> h_groups;
+  std::vector<double> rcut_classes;
+  std::vector<double> ecls_eta;
+  std::vector<int> ecls_rclass, ecls_atomid;
+  std::vector<int32_t> zcodes;  // atomic numbers of species codes
+  fnetg::DBuf d_rad, d_ang, d_groups, d_code, d_ecls_eta, d_ecls_rclass, d_ecls_atomid,
+      d_rcls;
+
+  // neighbour list
+  bool nb_valid = false;
+  double nb_rcut = 0.0;
+  int64_t P = 0;
+  int max_pairs = 0;
+  fnetg::DBuf d_pcount, d_poff, d_pj, d_pmeta, d_rij, d_d2, d_scan_tmp, d_maxp;
+
+  // features (bucketed rows, compute precision)
+  int nf = 0;
+  bool feats_valid = false;
+  std::vector<int32_t> ext_idx;
+  fnetg::DBuf d_feat, d_zprec, d_zpart, d_extidx;
+  std::vector<double> h_zprec;
+  bool zprec_valid = false;
+
+  // network
+  bool net_set = false;
+  int nsp = 0, nlayer = 0, act = 0;
+  std::vector<int32_t> dims;
+  int64_t nparams = 0;
+  std::vector<int64_t> woff, boff;
+  fnetg::DBuf d_params64, d_params, d_ref_of_compute, d_sp_tile0;
+
+  // outputs / training
+  int ngt = 0, nat = 0;
+  bool targets_set = false;
+  fnetg::DBuf d_gt, d_at, d_aw, d_w, d_out, d_gsum, d_lossgrad, d_losspart, d_gpart, d_grad64,
+      d_order, d_jac, d_jacT, d_forces, d_scalars, d_struct_aw;
+  double sum_weights = 0.0;
+
+  // optimiser state (device)
+  bool opt_set = false;
+  int opt_kind = 0;
+  bool opt_started = false;
+  fnetg::DBuf d_opt;        // per-species optimiser state blocks (FP64)
+  size_t opt_stride = 0;    // doubles per species block
+  double opt_threshold = 0, opt_min_disp = 0, opt_max_disp = 0, opt_lr = 0;
+  int opt_mem = 0, opt_linemin = 1, opt_qn = 0;
+  fnetg::DBuf d_xnew, d_conv;
+  void *h_pinned = nullptr;  // small pinned staging area for scalars
+
+  // profiling
+  bool prof = false;
+  std::map<std::string, fnetg::ProfEntry> prof_tab;
+  std::vector<fnetg::PendingLaunch> ev_pending;
+  std::vector<cudaEvent_t> ev_free;
+  int64_t launches = 0;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+};
+
+namespace fnetg {
+
+// error helpers -------------------------------------------------------------------------
+int fail(fnetg_ctx *c, int code, const std::string &msg);
+int cuda_fail(fnetg_ctx *c, cudaError_t e, const char *where);
+
+#define FNETG_CUDA(call)                                        \
+  do {                                                          \
+    cudaError_t _e = (call);                                    \
+    if (_e != cudaSuccess) return ::fnetg::cuda_fail(ctx, _e, #call); \
+  } while (0)
+
+#define FNETG_CHECK(cond, code, msg)                   \
+  do {                                                 \
+    if (!(cond)) return ::fnetg::fail(ctx, code, msg); \
+  } while (0)
+
+// launch accounting: every kernel launch of the library goes through these
+struct LaunchScope {
+  fnetg_ctx *c;
+  const char *name;
+  cudaEvent_t e0 = nullptr;
+  LaunchScope(fnetg_ctx *ctx, const char *n);
+  ~LaunchScope();
+};
+
+inline int ceil_div(int64_t a, int64_t b) { return (int)((a + b - 1) / b); }
+int num_sms();
+void resolve_profile(fnetg_ctx *c);
+
+// kernels' host entry points (one per translation unit)
+int run_neighbors(fnetg_ctx *ctx, double rcut);
+int run_acsf(fnetg_ctx *ctx);
+int run_zscore(fnetg_ctx *ctx, const int32_t *weights, bool compute);
+int run_ext_inputs(fnetg_ctx *ctx);
+int run_predict(fnetg_ctx *ctx);
+int run_jacobian(fnetg_ctx *ctx, int out_index, void *dst);
+int run_forces(fnetg_ctx *ctx);
+int run_train_gradients(fnetg_ctx *ctx, int loss, const int32_t *order, bool need_predict);
+int run_update_prepare(fnetg_ctx *ctx, double strength, double alpha);
+int run_optimizer_step(fnetg_ctx *ctx);
+int run_params_to_compute(fnetg_ctx *ctx);
+int exclusive_scan_i64(fnetg_ctx *ctx, const int64_t *in, int64_t *out, int64_t n);
+
+}  // namespace fnetg

@@ -1,0 +1,706 @@
+// Training on the device: per-structure output sums, losses and loss gradients
+// (lib_common/loss.F90:217-721, TBpnn_sysTrain bpnn.F90:654-701), the gradient
+// preparation of TBpnn_update (bpnn.F90:751-766, elastic net nestedtypes.F90:336-370) and
+// the optimisers — steepest descent (lib_dftbp/steepdesc.F90:126-204) and L-BFGS with its
+// line minimiser (lib_dftbp/lbfgs.F90:283-488, linemin.F90:141-391) — with one CTA per
+// sub-network holding the optimiser state in FP64 device memory.
+#include <algorithm>
+
+#include "internal.cuh"
+
+namespace fnetg {
+
+int run_mlp_backward(fnetg_ctx *ctx);
+
+namespace {
+
+constexpr double kEps = 2.220446049250313e-16;        // epsilon(1.0_dp)
+constexpr double kGoldenMeanP1 = 1.6180339887498949;  // lib_dftbp/constants.F90:131
+constexpr int kOptThreads = 512;
+
+__device__ __forceinline__ double lossgrad(int loss, double p, double t) {
+  switch (loss) {
+    case FNETG_LOSS_RMS: return (p - t) / sqrt((p - t) * (p - t));
+    case FNETG_LOSS_MAE: return (p - t) / fabs(p - t);
+    case FNETG_LOSS_MAPE: return 100.0 * (p - t) / (t * t * fabs(p / t - 1.0));
+    default: return 2.0 * (p - t);
+  }
+}
+
+// simple losses accumulate these two sums; finish() turns them into the loss value
+__device__ __forceinline__ double loss_term(int loss, double p, double t) {
+  switch (loss) {
+    case FNETG_LOSS_MAE: return fabs(t - p);
+    case FNETG_LOSS_MAPE: return fabs((t - p) / t);
+    default: return (t - p) * (t - p);
+  }
+}
+__device__ __forceinline__ double loss_finish(int loss, double sum, int n) {
+  switch (loss) {
+    case FNETG_LOSS_RMS: return sqrt(sum / (double)n);
+    case FNETG_LOSS_MAPE: return 100.0 * sum / (double)n;
+    default: return sum / (double)n;
+  }
+}
+
+struct LossArgs {
+  int S;
+  const int64_t *off;
+  const double *out;      // [N][nout]
+  int nout, ngt, nat;
+  const double *gt, *at, *aw, *saw;
+  const int32_t *w;
+  int loss;
+  double *delta;          // [N][nout] scaled output gradients
+  double *part;           // [S][2] loss numerator / denominator per structure
+};
+
+// one warp per structure
+__global__ void loss_kernel(LossArgs a) {
+  const int lane = threadIdx.x & 31;
+  const int s = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (s >= a.S) return;
+  const int64_t a0 = a.off[s], a1 = a.off[s + 1];
+  const int n = (int)(a1 - a0);
+  const double ws = a.w ? (double)a.w[s] : 1.0;
+  double num = 0.0, den = 0.0;
+  if (a.ngt > 0) {
+    double lsum = 0.0;
+    for (int o = 0; o < a.ngt; o++) {
+      double sum = 0.0;
+      for (int64_t at = a0 + lane; at < a1; at += 32) sum += a.out[at * a.nout + o];
+#pragma unroll
+      for (int k = 16; k > 0; k >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, k);
+      const double t = a.gt[(int64_t)s * a.ngt + o];
+      const double lg = lossgrad(a.loss, sum, t);
+      lsum += loss_term(a.loss, sum, t);
+      for (int64_t at = a0 + lane; at < a1; at += 32)
+        a.delta[at * a.nout + o] = lg * a.aw[at] / (double)n * ws;
+    }
+    num += ws * a.saw[s] * loss_finish(a.loss, lsum, a.ngt);
+    den += ws * a.saw[s];
+  }
+  if (a.nat > 0) {
+    double ln = 0.0, ld = 0.0;
+    for (int64_t at = a0 + lane; at < a1; at += 32) {
+      double lsum = 0.0;
+      for (int t = 0; t < a.nat; t++) {
+        const double p = a.out[at * a.nout + a.ngt + t];
+        const double tg = a.at[at * a.nat + t];
+        lsum += loss_term(a.loss, p, tg);
+        a.delta[at * a.nout + a.ngt + t] = lossgrad(a.loss, p, tg) * a.aw[at] / (double)n * ws;
+      }
+      ln += ws * a.aw[at] * loss_finish(a.loss, lsum, a.nat);
+      ld += ws * a.aw[at];
+    }
+#pragma unroll
+    for (int k = 16; k > 0; k >>= 1) {
+      ln += __shfl_xor_sync(0xffffffffu, ln, k);
+      ld += __shfl_xor_sync(0xffffffffu, ld, k);
+    }
+    num += ln;
+    den += ld;
+  }
+  if (lane == 0) {
+    a.part[2 * s] = num;
+    a.part[2 * s + 1] = den;
+  }
+}
+
+template <int NT> __device__ double block_sum(double v, double *sh) {
+  const int t = threadIdx.x;
+  __syncthreads();
+  sh[t] = v;
+  __syncthreads();
+  for (int o = NT / 2; o > 0; o >>= 1) {
+    if (t < o) sh[t] += sh[t + o];
+    __syncthreads();
+  }
+  const double r = sh[0];
+  __syncthreads();
+  return r;
+}
+
+template <int NT> __device__ double block_max(double v, double *sh) {
+  const int t = threadIdx.x;
+  __syncthreads();
+  sh[t] = v;
+  __syncthreads();
+  for (int o = NT / 2; o > 0; o >>= 1) {
+    if (t < o) sh[t] = fmax(sh[t], sh[t + o]);
+    __syncthreads();
+  }
+  const double r = sh[0];
+  __syncthreads();
+  return r;
+}
+
+__global__ void loss_reduce_kernel(const double *part, int S, double *scalars) {
+  __shared__ double sh[1024];
+  double num = 0.0, den = 0.0;
+  for (int s = threadIdx.x; s < S; s += blockDim.x) {
+    num += part[2 * s];
+    den += part[2 * s + 1];
+  }
+  num = block_sum<1024>(num, sh);
+  den = block_sum<1024>(den, sh);
+  if (threadIdx.x == 0) scalars[0] = num / den;
+}
+
+// elastic net (nestedtypes.F90:336-370), 1/sum(w), per-species sum of squares
+__global__ void update_prepare_kernel(const double *params, double *grad, int64_t np, int64_t nw,
+                                      double lam, double alpha, double sumw, double *sq) {
+  __shared__ double sh[kOptThreads];
+  const int s = blockIdx.x;
+  const double *p = params + s * np;
+  double *g = grad + s * np;
+  double acc = 0.0;
+  for (int64_t q = threadIdx.x; q < np; q += blockDim.x) {
+    double v = g[q];
+    if (q < nw) {
+      const double ww = p[q];
+      const double sgn = ww == 0.0 ? 0.0 : (ww > 0.0 ? 1.0 : -1.0);
+      v = v + lam / (double)nw * ((1.0 - alpha) * ww + alpha * sgn);
+    }
+    v = v / sumw;
+    g[q] = v;
+    acc += v * v;
+  }
+  acc = block_sum<kOptThreads>(acc, sh);
+  if (threadIdx.x == 0) sq[s] = acc;
+}
+
+__global__ void norm_finish_kernel(const double *sq, int nsp, double *scalars) {
+  double acc = 0.0;
+  for (int s = 0; s < nsp; s++) acc += sq[s];
+  scalars[1] = sqrt(acc);
+}
+
+// ---------------------------------------------------------------- steepest descent
+struct SdState {
+  double tol, maxdisp, lr;
+};
+
+__global__ void sd_kernel(double *params, const double *grad, int64_t np, SdState st,
+                          int *conv_flags) {
+  __shared__ double sh[kOptThreads];
+  const int s = blockIdx.x;
+  double *x = params + s * np;
+  const double *g = grad + s * np;
+  if (conv_flags[s]) return;  // sticky convergence: xNew = xOld
+  double gmax = 0.0;
+  for (int64_t q = threadIdx.x; q < np; q += blockDim.x) gmax = fmax(gmax, fabs(g[q]));
+  gmax = block_max<kOptThreads>(gmax, sh);
+  if (gmax < st.tol) {
+    if (threadIdx.x == 0) conv_flags[s] = 1;
+    return;
+  }
+  double mx = 0.0;
+  for (int64_t q = threadIdx.x; q < np; q += blockDim.x) mx = fmax(mx, fabs(-1.0 * st.lr * g[q]));
+  mx = block_max<kOptThreads>(mx, sh);
+  for (int64_t q = threadIdx.x; q < np; q += blockDim.x) {
+    const double d = -1.0 * st.lr * g[q];
+    x[q] = mx <= st.maxdisp ? x[q] + d : x[q] + (st.maxdisp / mx) * d;
+  }
+}
+
+// ---------------------------------------------------------------- L-BFGS + line minimiser
+// state layout per species (doubles): vectors xx, xold, gg, dir, x0, d0, dxt, qq (n each),
+// ss, yy (mem*n each), rho, alph (mem each), scalars (32)
+enum {
+  SC_ITER = 0, SC_STATE, SC_IITER, SC_CONV, SC_XX0, SC_XX1, SC_DX0, SC_DX1, SC_XCUR, SC_MAXX,
+  SC_FIRST, SC_CONVERGED, SC_NS = 32
+};
+
+struct LbView {
+  double *xx, *xold, *gg, *dir, *x0, *d0, *dxt, *qq, *ss, *yy, *rho, *alph, *sc;
+};
+
+__host__ __device__ inline size_t lb_stride(int64_t n, int mem) {
+  return (size_t)8 * n + (size_t)2 * mem * n + (size_t)2 * mem + SC_NS;
+}
+
+__device__ LbView lb_view(double *base, int64_t n, int mem) {
+  LbView v;
+  double *p = base;
+  v.xx = p; p += n;
+  v.xold = p; p += n;
+  v.gg = p; p += n;
+  v.dir = p; p += n;
+  v.x0 = p; p += n;
+  v.d0 = p; p += n;
+  v.dxt = p; p += n;
+  v.qq = p; p += n;
+  v.ss = p; p += (size_t)mem * n;
+  v.yy = p; p += (size_t)mem * n;
+  v.rho = p; p += mem;
+  v.alph = p; p += mem;
+  v.sc = p;
+  return v;
+}
+
+struct LbParams {
+  int64_t n;
+  int mem;
+  double tol, maxdisp;
+  int linesearch;
+  double qn_maxdisp;
+};
+
+__device__ double bdot(const double *a, const double *b, int64_t n, double *sh) {
+  double acc = 0.0;
+  for (int64_t q = threadIdx.x; q < n; q += blockDim.x) acc += a[q] * b[q];
+  return block_sum<kOptThreads>(acc, sh);
+}
+
+__device__ double bmaxabs(const double *a, int64_t n, double *sh) {
+  double acc = 0.0;
+  for (int64_t q = threadIdx.x; q < n; q += blockDim.x) acc = fmax(acc, fabs(a[q]));
+  return block_max<kOptThreads>(acc, sh);
+}
+
+__device__ void bcopy(double *dst, const double *src, int64_t n) {
+  for (int64_t q = threadIdx.x; q < n; q += blockDim.x) dst[q] = src[q];
+  __syncthreads();
+}
+
+// TLbfgs_calcDirection (lbfgs.F90:387-488); slots never written hold zeros and are skipped
+// (they leave qq and dir bit-identical)
+__device__ void lb_direction(LbView &v, const LbParams &P, const double *xx, const double *g,
+                             double *sh) {
+  const int64_t n = P.n;
+  const int mem = P.mem;
+  int iter = (int)v.sc[SC_ITER];
+  if (iter == 0) {
+    for (int64_t q = threadIdx.x; q < n; q += blockDim.x) {
+      v.gg[q] = g[q];
+      v.dir[q] = -g[q];
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) v.sc[SC_ITER] = 1;
+    __syncthreads();
+    return;
+  }
+  const int ne = (iter - 1) % mem;
+  double *s = v.ss + (size_t)ne * n, *y = v.yy + (size_t)ne * n;
+  for (int64_t q = threadIdx.x; q < n; q += blockDim.x) {
+    s[q] = xx[q] - v.xold[q];
+    y[q] = g[q] - v.gg[q];
+  }
+  __syncthreads();
+  const double beta = bdot(y, s, n, sh);
+  if (threadIdx.x == 0) v.rho[ne] = 1.0 / fmax(fabs(beta), kEps);
+  for (int64_t q = threadIdx.x; q < n; q += blockDim.x) {
+    v.xold[q] = xx[q];
+    v.gg[q] = g[q];
+  }
+  __syncthreads();
+  double diag;
+  if (iter == 1) {
+    diag = 1.0;
+  } else {
+    const double yy2 = bdot(y, y, n, sh);
+    diag = bdot(s, y, n, sh) / fmax(yy2, kEps);
+  }
+  const int used = iter < mem ? iter : mem;  // slots holding history
+  bcopy(v.qq, g, n);
+  for (int m = 0; m < mem; m++) {
+    const int ii = ((ne - m) % mem + mem) % mem;
+    if (m >= used) break;
+    const double al = v.rho[ii] * bdot(v.ss + (size_t)ii * n, v.qq, n, sh);
+    if (threadIdx.x == 0) v.alph[ii] = al;
+    for (int64_t q = threadIdx.x; q < n; q += blockDim.x) v.qq[q] = v.qq[q] - al * v.yy[(size_t)ii * n + q];
+    __syncthreads();
+  }
+  for (int64_t q = threadIdx.x; q < n; q += blockDim.x) v.dir[q] = diag * v.qq[q];
+  __syncthreads();
+  const int oldest = (ne + 1) % mem;
+  for (int m = 0; m < mem; m++) {
+    const int ii = (oldest + m) % mem;
+    // the reference visits every slot; unwritten slots (rho == 0) change nothing
+    const bool written = used >= mem || (ii <= ne && ii > ne - used);
+    if (!written) continue;
+    const double b = v.rho[ii] * bdot(v.yy + (size_t)ii * n, v.dir, n, sh);
+    const double al = v.alph[ii];
+    for (int64_t q = threadIdx.x; q < n; q += blockDim.x)
+      v.dir[q] = v.dir[q] + v.ss[(size_t)ii * n + q] * (al - b);
+    __syncthreads();
+  }
+  for (int64_t q = threadIdx.x; q < n; q += blockDim.x) v.dir[q] = -v.dir[q];
+  __syncthreads();
+  if (threadIdx.x == 0) v.sc[SC_ITER] = iter + 1;
+  __syncthreads();
+}
+
+// TLineMin reset (linemin.F90:141-176)
+__device__ void lm_reset(LbView &v, const LbParams &P, const double *x0, const double *d0,
+                         double first, double *sh) {
+  const int64_t n = P.n;
+  const double tmp = sqrt(bdot(d0, d0, n, sh));
+  for (int64_t q = threadIdx.x; q < n; q += blockDim.x) {
+    v.x0[q] = x0[q];
+    v.d0[q] = d0[q] / tmp;
+  }
+  __syncthreads();
+  const double dmax = bmaxabs(v.d0, n, sh);
+  if (threadIdx.x == 0) {
+    v.sc[SC_STATE] = 1;
+    v.sc[SC_IITER] = 0;
+    v.sc[SC_XX0] = v.sc[SC_XX1] = 0.0;
+    v.sc[SC_DX0] = v.sc[SC_DX1] = 0.0;
+    v.sc[SC_XCUR] = 0.0;
+    v.sc[SC_FIRST] = first;
+    v.sc[SC_MAXX] = P.maxdisp / dmax;
+    v.sc[SC_CONV] = 0;
+  }
+  __syncthreads();
+}
+
+// next / next_local (linemin.F90:179-391); uu receives the next point, returns convergence
+__device__ bool lm_next(LbView &v, const LbParams &P, double fu, const double *du, double *uu,
+                        double *sh) {
+  const int64_t n = P.n;
+  __shared__ int s_ret, s_flip;
+  if (v.sc[SC_CONV] != 0.0) {
+    bcopy(uu, v.x0, n);
+    return true;
+  }
+  const double dcur0 = bdot(du, v.d0, n, sh);
+  if (threadIdx.x == 0) {
+    double *sc = v.sc;
+    sc[SC_IITER] += 1;
+    double dcur = dcur0;
+    s_ret = 0;
+    s_flip = 0;
+    const int iiter = (int)sc[SC_IITER];
+    if ((fabs(dcur) < P.tol && (int)sc[SC_STATE] == 3) || iiter > 10) {
+      s_ret = 1;
+    } else {
+      int state = (int)sc[SC_STATE];
+      int next_state = state;
+      double xnew = 0.0, tmp, qq, aa, bb, cc;
+      double xcur = sc[SC_XCUR];
+      if (state == 1) {
+        if (dcur > 0.0) {
+          s_flip = 1;
+          dcur = -dcur;
+        }
+        sc[SC_XX0] = xcur;
+        sc[SC_DX0] = dcur;
+        xnew = sc[SC_FIRST];
+        next_state = 2;
+      }
+      if (state == 2) {
+        if (dcur < 0.0) {
+          xnew = xcur + kGoldenMeanP1 * (xcur - sc[SC_XX0]);
+          sc[SC_XX0] = xcur;
+          sc[SC_DX0] = dcur;
+          next_state = 2;
+        } else {
+          state = 3;
+          sc[SC_STATE] = 3;
+        }
+      }
+      if (state == 3) {
+        bool done = false;
+        next_state = 3;
+        double xx0 = sc[SC_XX0], xx1 = sc[SC_XX1], dx0 = sc[SC_DX0], dx1 = sc[SC_DX1];
+        if (iiter > 2 && fabs(xx0 - xx1) > kEps) {
+          qq = (xcur - xx0) / (xx0 - xx1);
+          tmp = dcur - dx0;
+          cc = qq * qq * (dx1 - dx0);
+          aa = qq * tmp + cc;
+          bb = 2.0 * qq * tmp + cc + tmp;
+          cc = (qq + 1.0) * dcur;
+          tmp = bb * bb - 4 * aa * cc;
+          if (tmp >= 0.0) {
+            tmp = sqrt(tmp);
+            aa = bb > 0.0 ? bb + tmp : bb - tmp;
+            if (fabs(aa) > kEps) {
+              xnew = xcur - (xcur - xx0) * 2.0 * cc / aa;
+              if (((xx0 < xnew) == (xnew < xx1)) && ((dcur < 0.0) == (xnew > xcur))) {
+                if (xnew > xcur) {
+                  xx0 = xcur;
+                  dx0 = dcur;
+                } else {
+                  xx1 = xcur;
+                  dx1 = dcur;
+                }
+                done = true;
+              }
+            }
+          }
+        }
+        if (!done) {
+          if (dcur < 0.0) {
+            xx0 = xcur;
+            dx0 = dcur;
+          } else {
+            xx1 = xcur;
+            dx1 = dcur;
+          }
+          tmp = dx0 - dx1;
+          if (fabs(tmp) > kEps) {
+            xnew = (xx1 * dx0 - xx0 * dx1) / tmp;
+            if ((xx0 < xnew) == (xnew < xx1)) done = true;
+          }
+        }
+        if (!done) xnew = 0.5 * (xx0 + xx1);
+        sc[SC_XX0] = xx0;
+        sc[SC_XX1] = xx1;
+        sc[SC_DX0] = dx0;
+        sc[SC_DX1] = dx1;
+      }
+      tmp = xnew - xcur;
+      if (fabs(tmp) <= sc[SC_MAXX]) xcur = xnew;
+      else xcur = xcur + copysign(sc[SC_MAXX], tmp);
+      sc[SC_XCUR] = xcur;
+      sc[SC_STATE] = next_state;
+    }
+  }
+  __syncthreads();
+  if (s_ret) {
+    const double xcur = v.sc[SC_XCUR];
+    for (int64_t q = threadIdx.x; q < n; q += blockDim.x) {
+      v.x0[q] = v.x0[q] + xcur * v.d0[q];
+      v.d0[q] = du[q];
+      uu[q] = v.x0[q];
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      v.sc[SC_XX0] = fu;
+      v.sc[SC_XX1] = xcur;
+      v.sc[SC_CONV] = 1;
+    }
+    __syncthreads();
+    return true;
+  }
+  if (s_flip)
+    for (int64_t q = threadIdx.x; q < n; q += blockDim.x) v.d0[q] = -v.d0[q];
+  __syncthreads();
+  const double xcur = v.sc[SC_XCUR];
+  for (int64_t q = threadIdx.x; q < n; q += blockDim.x) uu[q] = v.x0[q] + xcur * v.d0[q];
+  __syncthreads();
+  return false;
+}
+
+// TLbfgs_next (lbfgs.F90:283-359); params holds xNew on exit
+__global__ void lbfgs_kernel(double *state, size_t stride, double *params, const double *grad,
+                             LbParams P, int *conv_flags) {
+  __shared__ double sh[kOptThreads];
+  const int s = blockIdx.x;
+  LbView v = lb_view(state + (size_t)s * stride, P.n, P.mem);
+  const double *dx = grad + (size_t)s * P.n;
+  double *xnew = params + (size_t)s * P.n;
+  const int64_t n = P.n;
+  const double fx = 0.0;  // the reference passes a loss value that the line minimiser only stores
+  const double gmax = bmaxabs(dx, n, sh);
+  if (gmax < P.tol) {
+    if (threadIdx.x == 0) conv_flags[s] = 1;
+    bcopy(xnew, v.xx, n);
+    return;
+  }
+  if (threadIdx.x == 0) conv_flags[s] = 0;
+  bcopy(v.dxt, dx, n);
+  if (P.linesearch && (int)v.sc[SC_ITER] > 0) {
+    const bool lconv = lm_next(v, P, fx, dx, v.xx, sh);
+    if (lconv) {
+      bcopy(v.dxt, v.d0, n);
+    } else {
+      bcopy(xnew, v.xx, n);
+      return;
+    }
+  }
+  lb_direction(v, P, v.xx, v.dxt, sh);
+  if (P.linesearch) {
+    lm_reset(v, P, v.xx, v.dir, 1.0, sh);
+    lm_next(v, P, fx, dx, v.xx, sh);
+  } else {
+    if (P.qn_maxdisp > 0.0) {
+      const double dmax = bmaxabs(v.dir, n, sh);
+      if (dmax > P.qn_maxdisp)
+        for (int64_t q = threadIdx.x; q < n; q += blockDim.x)
+          v.dir[q] = v.dir[q] * P.qn_maxdisp / dmax;
+      __syncthreads();
+    }
+    for (int64_t q = threadIdx.x; q < n; q += blockDim.x) v.xx[q] = v.xx[q] + v.dir[q];
+    __syncthreads();
+  }
+  bcopy(xnew, v.xx, n);
+}
+
+__global__ void lbfgs_reset_kernel(double *state, size_t stride, const double *params,
+                                   int64_t n, int mem) {
+  const int s = blockIdx.x;
+  double *base = state + (size_t)s * stride;
+  for (size_t q = threadIdx.x; q < stride; q += blockDim.x) base[q] = 0.0;
+  __syncthreads();
+  LbView v = lb_view(base, n, mem);
+  for (int64_t q = threadIdx.x; q < n; q += blockDim.x) {
+    v.xx[q] = params[(size_t)s * n + q];
+    v.xold[q] = params[(size_t)s * n + q];
+  }
+}
+
+}  // namespace
+
+int run_train_gradients(fnetg_ctx *ctx, int loss, const int32_t *order, bool need_predict) {
+  (void)order;  // only the accumulation order changes with the reference's shuffle
+  const int64_t N = ctx->N;
+  const int S = ctx->S;
+  const int nout = ctx->dims.back();
+  int rc;
+  if (need_predict) {
+    rc = run_predict(ctx);
+    if (rc) return rc;
+  }
+  FNETG_CUDA(ctx->d_lossgrad.ensure(sizeof(double) * std::max<int64_t>(N, 1) * nout));
+  FNETG_CUDA(ctx->d_losspart.ensure(sizeof(double) * 2 * std::max(S, 1)));
+  FNETG_CUDA(ctx->d_scalars.ensure(sizeof(double) * 16));
+  LossArgs a{};
+  a.S = S;
+  a.off = ctx->d_off.as<int64_t>();
+  a.out = ctx->d_out.as<double>();
+  a.nout = nout;
+  a.ngt = ctx->ngt;
+  a.nat = ctx->nat;
+  a.gt = ctx->d_gt.as<double>();
+  a.at = ctx->d_at.as<double>();
+  a.aw = ctx->d_aw.as<double>();
+  a.saw = ctx->d_struct_aw.as<double>();
+  a.w = ctx->d_w.as<int32_t>();
+  a.loss = loss;
+  a.delta = ctx->d_lossgrad.as<double>();
+  a.part = ctx->d_losspart.as<double>();
+  if (S > 0) {
+    LaunchScope ls(ctx, "loss");
+    loss_kernel<<<ceil_div(S, 8), 256, 0, ctx->stream>>>(a);
+    FNETG_CUDA(cudaGetLastError());
+  }
+  {
+    LaunchScope ls(ctx, "loss");
+    loss_reduce_kernel<<<1, 1024, 0, ctx->stream>>>(ctx->d_losspart.as<double>(), S,
+                                                     ctx->d_scalars.as<double>());
+    FNETG_CUDA(cudaGetLastError());
+  }
+  return run_mlp_backward(ctx);
+}
+
+int run_update_prepare(fnetg_ctx *ctx, double strength, double alpha) {
+  FNETG_CUDA(ctx->d_scalars.ensure(sizeof(double) * 16));
+  FNETG_CUDA(ctx->d_conv.ensure(sizeof(int) * 64 + sizeof(double) * 64));
+  double *sq = reinterpret_cast<double *>(ctx->d_conv.as<int>() + 64);
+  const int64_t nw = ctx->boff[0];
+  {
+    LaunchScope ls(ctx, "optimizer");
+    update_prepare_kernel<<<ctx->nsp, kOptThreads, 0, ctx->stream>>>(
+        ctx->d_params64.as<double>(), ctx->d_grad64.as<double>(), ctx->nparams, nw, strength,
+        alpha, ctx->sum_weights, sq);
+  }
+  {
+    LaunchScope ls(ctx, "optimizer");
+    norm_finish_kernel<<<1, 1, 0, ctx->stream>>>(sq, ctx->nsp, ctx->d_scalars.as<double>());
+  }
+  FNETG_CUDA(cudaGetLastError());
+  return FNETG_OK;
+}
+
+int run_optimizer_step(fnetg_ctx *ctx) {
+  int *conv = ctx->d_conv.as<int>();
+  if (ctx->opt_kind == FNETG_OPT_SD) {
+    SdState st{ctx->opt_threshold, ctx->opt_max_disp, ctx->opt_lr};
+    LaunchScope ls(ctx, "optimizer");
+    sd_kernel<<<ctx->nsp, kOptThreads, 0, ctx->stream>>>(ctx->d_params64.as<double>(),
+                                                          ctx->d_grad64.as<double>(),
+                                                          ctx->nparams, st, conv);
+  } else {
+    LbParams P{ctx->nparams, ctx->opt_mem, ctx->opt_threshold, ctx->opt_max_disp,
+               ctx->opt_linemin, ctx->opt_qn ? ctx->opt_max_disp : -1.0};
+    LaunchScope ls(ctx, "optimizer");
+    lbfgs_kernel<<<ctx->nsp, kOptThreads, 0, ctx->stream>>>(
+        ctx->d_opt.as<double>(), ctx->opt_stride, ctx->d_params64.as<double>(),
+        ctx->d_grad64.as<double>(), P, conv);
+  }
+  FNETG_CUDA(cudaGetLastError());
+  return run_params_to_compute(ctx);
+}
+
+}  // namespace fnetg
+
+using namespace fnetg;
+
+extern "C" {
+
+int fnetg_optimizer_init(fnetg_ctx *ctx, int32_t kind, double threshold, double min_disp,
+                         double max_disp, double learning_rate, int32_t memory, int32_t linemin,
+                         int32_t qn_max_disp) {
+  if (!ctx) return FNETG_E_INVALID;
+  FNETG_CHECK(ctx->net_set, FNETG_E_INVALID, "optimizer_init: no network");
+  FNETG_CHECK(kind == FNETG_OPT_SD || kind == FNETG_OPT_LBFGS, FNETG_E_INVALID, "optimiser kind");
+  FNETG_CHECK(threshold > 0.0 && max_disp > 0.0, FNETG_E_INVALID,
+              "threshold and maximal displacement must be > 0");
+  ctx->opt_kind = kind;
+  ctx->opt_threshold = threshold;
+  ctx->opt_min_disp = min_disp;
+  ctx->opt_max_disp = max_disp;
+  ctx->opt_lr = learning_rate;
+  ctx->opt_mem = std::max(1, memory);
+  ctx->opt_linemin = linemin ? 1 : 0;
+  ctx->opt_qn = qn_max_disp ? 1 : 0;
+  FNETG_CUDA(ctx->d_conv.ensure(sizeof(int) * 64 + sizeof(double) * 64));
+  FNETG_CUDA(cudaMemsetAsync(ctx->d_conv.p, 0, sizeof(int) * 64, ctx->stream));
+  if (kind == FNETG_OPT_LBFGS) {
+    ctx->opt_stride = lb_stride(ctx->nparams, ctx->opt_mem);
+    FNETG_CUDA(ctx->d_opt.ensure(sizeof(double) * ctx->opt_stride * ctx->nsp));
+    LaunchScope ls(ctx, "optimizer");
+    lbfgs_reset_kernel<<<ctx->nsp, kOptThreads, 0, ctx->stream>>>(
+        ctx->d_opt.as<double>(), ctx->opt_stride, ctx->d_params64.as<double>(), ctx->nparams,
+        ctx->opt_mem);
+    FNETG_CUDA(cudaGetLastError());
+  }
+  FNETG_CUDA(cudaStreamSynchronize(ctx->stream));
+  ctx->opt_set = true;
+  ctx->opt_started = false;
+  return FNETG_OK;
+}
+
+int fnetg_train_iteration(fnetg_ctx *ctx, int32_t loss, double regu_strength, double regu_alpha,
+                          const int32_t *order, double *loss_out, double *grad_norm_out,
+                          int32_t *converged) {
+  if (!ctx) return FNETG_E_INVALID;
+  FNETG_CHECK(ctx->opt_set, FNETG_E_INVALID, "train_iteration: optimizer not initialised");
+  FNETG_CHECK(ctx->targets_set, FNETG_E_INVALID, "train_iteration: no targets");
+  FNETG_CHECK(ctx->feats_valid, FNETG_E_INVALID, "train_iteration: no features");
+  FNETG_CHECK(ctx->nf == ctx->dims[0], FNETG_E_SHAPE, "network input width");
+  FNETG_CHECK(ctx->ngt + ctx->nat == ctx->dims.back(), FNETG_E_SHAPE,
+              "network outputs must equal the number of targets");
+  FNETG_CHECK(loss >= 0 && loss <= 3, FNETG_E_INVALID, "loss code");
+  int rc;
+  if (!ctx->opt_started) {
+    rc = run_train_gradients(ctx, loss, order, true);
+    if (rc) return rc;
+    ctx->opt_started = true;
+  }
+  rc = run_update_prepare(ctx, regu_strength, regu_alpha);
+  if (rc) return rc;
+  // the gradient norm of this update is reported like the reference's tmpGradients
+  double *pin = static_cast<double *>(ctx->h_pinned);
+  FNETG_CUDA(cudaMemcpyAsync(pin + 1, ctx->d_scalars.as<double>() + 1, sizeof(double),
+                             cudaMemcpyDeviceToHost, ctx->stream));
+  rc = run_optimizer_step(ctx);
+  if (rc) return rc;
+  rc = run_train_gradients(ctx, loss, order, true);
+  if (rc) return rc;
+  FNETG_CUDA(cudaMemcpyAsync(pin, ctx->d_scalars.as<double>(), sizeof(double),
+                             cudaMemcpyDeviceToHost, ctx->stream));
+  int *pconv = reinterpret_cast<int *>(pin + 8);
+  FNETG_CUDA(cudaMemcpyAsync(pconv, ctx->d_conv.p, sizeof(int) * ctx->nsp, cudaMemcpyDeviceToHost,
+                             ctx->stream));
+  FNETG_CUDA(cudaStreamSynchronize(ctx->stream));
+  if (loss_out) *loss_out = pin[0];
+  if (grad_norm_out) *grad_norm_out = pin[1];
+  if (converged) *converged = pconv[ctx->nsp - 1];  // the last sub-network's flag (bpnn.F90:774)
+  return FNETG_OK;
+}
+
+}  // extern "C"

@@ -760,7 +760,8 @@ static void gfunc_grad(const orc_gfunc *gf, const double *ci, double atomId, con
  * array(:,g,i,i) = -sum(array(:,g,i,idx(:)), dim=2), evaluated after the assignment. */
 #define PR(c, g, i, j) prime[(c) + 3 * ((int64_t)(g) + ng * ((int64_t)(i) + (int64_t)N * (j)))]
 
-int orc_acsf_prime(const orc_batch *b, int32_t s, const orc_gfunc *g, int32_t ng, double *prime) {
+int orc_acsf_prime_ex(const orc_batch *b, int32_t s, const orc_gfunc *g, int32_t ng,
+                      int32_t physical, double *prime) {
   geo_t geo;
   if (geo_of(b, s, &geo)) return -1;
   int N = geo.natom;
@@ -785,6 +786,24 @@ int orc_acsf_prime(const orc_batch *b, int32_t s, const orc_gfunc *g, int32_t ng
         grad = (double *)realloc(grad, gcap * sizeof(double));
       }
       gfunc_grad(gf, ci, c.atomId, &c.l1, &c.l2, grad);
+      if (physical) {
+        /* every image contributes: dG/dr_j += grad, dG/dr_i -= grad */
+        for (int q = 0; q < c.l1.n; q++)
+          for (int cc = 0; cc < 3; cc++) {
+            PR(cc, k, i, c.l1.idx[q]) += grad[3 * q + cc];
+            PR(cc, k, i, i) -= grad[3 * q + cc];
+          }
+        if (gf->type >= 4 && gf->z1 != gf->z2) {
+          glist s1 = c.l2, s2 = c.l1;
+          gfunc_grad(gf, ci, c.atomId, &s1, &s2, grad);
+          for (int q = 0; q < s1.n; q++)
+            for (int cc = 0; cc < 3; cc++) {
+              PR(cc, k, i, s1.idx[q]) += grad[3 * q + cc];
+              PR(cc, k, i, i) -= grad[3 * q + cc];
+            }
+        }
+        continue;
+      }
       for (int q = 0; q < c.l1.n; q++)
         for (int cc = 0; cc < 3; cc++) PR(cc, k, i, c.l1.idx[q]) = grad[3 * q + cc];
       double sum[3] = {0.0, 0.0, 0.0};
@@ -808,6 +827,10 @@ int orc_acsf_prime(const orc_batch *b, int32_t s, const orc_gfunc *g, int32_t ng
   free(grad);
   gwork_free(&w);
   return 0;
+}
+
+int orc_acsf_prime(const orc_batch *b, int32_t s, const orc_gfunc *g, int32_t ng, double *prime) {
+  return orc_acsf_prime_ex(b, s, g, ng, 0, prime);
 }
 
 /* ====================================================================================
@@ -1089,13 +1112,13 @@ double orc_update_prepare(const orc_net *net, const double *params, int32_t nspe
  * Forces: forceAnalysis_analytical (forces.F90:317-425) on the dense dG/dR of
  * iGeoAcsfGrad, z-scored like applyZscorePrime (acsf.F90:515-536).
  * ==================================================================================== */
-int orc_forces(const orc_batch *b, const orc_gfunc *g, int32_t ng, const double *zprec,
-               int32_t nout, const double *jac, double *forces) {
+int orc_forces_ex(const orc_batch *b, const orc_gfunc *g, int32_t ng, const double *zprec,
+                  int32_t nout, const double *jac, int32_t physical, double *forces) {
   for (int s = 0; s < b->nstruct; s++) {
     int64_t a0 = b->atom_offsets[s];
     int N = (int)(b->atom_offsets[s + 1] - a0);
     double *prime = (double *)malloc(sizeof(double) * 3 * (size_t)ng * N * N + 8);
-    if (orc_acsf_prime(b, s, g, ng, prime)) { free(prime); return -1; }
+    if (orc_acsf_prime_ex(b, s, g, ng, physical, prime)) { free(prime); return -1; }
     if (zprec)
       for (int k = 0; k < ng; k++) {
         if (zprec[ng + k] < 1e-08) continue;
@@ -1117,6 +1140,11 @@ int orc_forces(const orc_batch *b, const orc_gfunc *g, int32_t ng, const double 
   return 0;
 }
 #undef PR
+
+int orc_forces(const orc_batch *b, const orc_gfunc *g, int32_t ng, const double *zprec,
+               int32_t nout, const double *jac, double *forces) {
+  return orc_forces_ex(b, g, ng, zprec, nout, jac, 0, forces);
+}
 
 /* ====================================================================================
  * Optimisers

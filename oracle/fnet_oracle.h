@@ -83,6 +83,10 @@ int orc_acsf(const orc_batch *b, const orc_gfunc *g, int32_t ng, int32_t mode, d
  * prime in Fortran order (3, ng, N, N): prime[c + 3*(g + ng*(i + N*j))] = dG_g(i)/dr_j[c],
  * with the reference's vector-subscript assignment semantics. */
 int orc_acsf_prime(const orc_batch *b, int32_t s, const orc_gfunc *g, int32_t ng, double *prime);
+/* physical = 1: every periodic image adds its own derivative (the exact dG/dR); it equals the
+ * reference's array whenever no atom has two images of one atom inside the cutoff. */
+int orc_acsf_prime_ex(const orc_batch *b, int32_t s, const orc_gfunc *g, int32_t ng,
+                      int32_t physical, double *prime);
 
 /* ---- z-score (acsf.F90:445-536) ---- */
 void orc_zscore_stats(const double *vals, int64_t ntot, int32_t ng, const int64_t *atom_offsets,
@@ -117,6 +121,8 @@ double orc_update_prepare(const orc_net *net, const double *params, int32_t nspe
 /* ---- forces (forces.F90:317-425) ---- forces[a*3*nout + c + 3*o] */
 int orc_forces(const orc_batch *b, const orc_gfunc *g, int32_t ng, const double *zprec,
                int32_t nout, const double *jac, double *forces);
+int orc_forces_ex(const orc_batch *b, const orc_gfunc *g, int32_t ng, const double *zprec,
+                  int32_t nout, const double *jac, int32_t physical, double *forces);
 
 /* ---- optimisers ---- */
 /* steepest descent (lib_dftbp/steepdesc.F90:104-204) */

@@ -1,0 +1,72 @@
+"""The C-ABI library builds, loads and exports every entry point of include/fnetg.h; its
+host-side initialisation RNG reproduces the reference's RANLUX draws (no GPU needed)."""
+
+import os
+import re
+
+import numpy as np
+
+import oracle as O
+from fortnet_gb300 import api
+
+HEADER = os.path.join(os.path.dirname(__file__), "..", "include", "fnetg.h")
+
+
+def declared_symbols():
+    text = open(HEADER).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(fnetg_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_library_exports_every_declared_symbol():
+    lib = api.load()
+    syms = declared_symbols()
+    assert len(syms) > 30
+    missing = [s for s in syms if not hasattr(lib, s)]
+    assert not missing, missing
+
+
+def test_abi_version():
+    assert api.load().fnetg_abi_version() == 1
+
+
+def test_nparams_matches_reference_count():
+    # nBiases + nWeights of TNetwork_countParams (network.F90:126-142)
+    for dims in ([8, 10, 10, 1], [96, 32, 32, 1], [168, 64, 64, 1], [3, 2]):
+        d = np.asarray(dims, dtype=np.int32)
+        n = api.load().fnetg_nparams(len(d), d.ctypes.data)
+        ref = sum(dims) + sum(dims[i] * dims[i + 1] for i in range(len(dims) - 1)) + dims[-1]
+        assert n == ref
+
+
+def test_ranlux_stream_matches_oracle():
+    for seed in (1, 123456, 2**31 - 1):
+        a = api.Rng(seed).uniform(5000)
+        b = O.Ranlux(seed).get(5000)
+        assert np.array_equal(a, b)
+
+
+def test_initial_parameters_match_oracle():
+    for dims, nsp in (([18, 3, 3, 1], 2), ([96, 32, 32, 1], 2), ([8, 10, 10, 1], 1)):
+        a = api.Rng(123456).init_params(dims, nsp)
+        b = O.Ranlux(123456).init_bpnn(dims, "tanh", nsp)
+        assert np.array_equal(a, b)
+
+
+def test_shuffle_matches_oracle():
+    r1, r2 = api.Rng(99), O.Ranlux(99)
+    x = np.arange(1, 101, dtype=np.int32)
+    for _ in range(3):
+        a = r1.shuffle(x)
+        b = r2.shuffle(x)
+        assert np.array_equal(a, b)
+        x = a
+
+
+def test_no_gpu_context_creation_fails_cleanly():
+    import ctypes as C
+
+    lib = api.load()
+    h = C.c_void_p()
+    rc = lib.fnetg_create(C.byref(h), 16, 0)  # invalid precision
+    assert rc == -1 and not h.value

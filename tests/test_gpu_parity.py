@@ -1,0 +1,301 @@
+"""Parity of the CUDA library (through its C-ABI) with the oracle and with the reference's
+own golden outputs.
+
+* neighbour pair sets and per-atom order: bit-exact against the oracle's restatement of the
+  reference iterator (including squared distances), on every reference dataset and on
+  synthetic cells smaller than the cutoff (self images, repeated images) and clusters;
+* ACSF values: FP64 within 1e-11 relative (summation order only), FP32 within 2e-5 of the
+  per-feature scale;
+* every golden prediction / validation / analytical-force / training case of the reference's
+  regression suite through the FP64 library at the reference driver's tolerance
+  (rtol 1e-9, atol 1e-10, testwithworkdir.py:24-25);
+* forces on cells with repeated images against the oracle's exact (physical) derivative;
+* FP32 energies within 1e-5 relative and forces within 1e-4 of the force scale of the
+  FP64 oracle.
+"""
+
+import numpy as np
+import pytest
+
+import golden_cases as G
+import gpu_flows
+import oracle as O
+from fortnet_gb300 import api, synthetic
+from fortnet_gb300.fnetdata import Dataset
+from fortnet_gb300.gfunctions import GFunction
+
+pytestmark = pytest.mark.gpu
+
+DATASETS = sorted({G.load_case(n).settings["dataset"] for n in G.case_names()})
+
+
+def small_cell_dataset(seed=7, n=6, L_bohr=5.0, nstruct=3, species=(1, 8)):
+    """Tiny periodic cells (L < rcut): self images and repeated images of every atom."""
+    rng = np.random.default_rng(seed)
+    coords, atnum, lat = [], [], []
+    for s in range(nstruct):
+        L = L_bohr * (1.0 + 0.3 * s)
+        coords.append(rng.uniform(0, L, size=(n, 3)))
+        atnum.append(rng.choice(species, size=n).astype(np.int32))
+        M = np.diag([L, L * 1.1, L * 0.95]) + rng.normal(0, 0.2, size=(3, 3))
+        lat.append(M.T.reshape(9))  # columns are lattice vectors
+    off = np.arange(nstruct + 1, dtype=np.int64) * n
+    ntot = n * nstruct
+    return Dataset(atom_offsets=off, coords=np.concatenate(coords), atnum=np.concatenate(atnum),
+                   species=np.zeros(ntot, dtype=np.int32), periodic=np.ones(nstruct, np.int32),
+                   latvecs=np.asarray(lat), atomic_numbers=np.asarray(species, np.int32),
+                   weights=np.ones(nstruct, np.int32), atomic_weights=np.ones(ntot),
+                   global_targets=np.zeros((nstruct, 1)), atomic_targets=np.zeros((ntot, 0)))
+
+
+def cluster_dataset(seed=3):
+    rng = np.random.default_rng(seed)
+    sizes = [1, 2, 9, 40]
+    coords = [rng.uniform(0, 12.0, size=(n, 3)) for n in sizes]
+    atnum = [rng.choice([1, 6], size=n).astype(np.int32) for n in sizes]
+    off = np.concatenate([[0], np.cumsum(sizes)]).astype(np.int64)
+    ntot = int(off[-1])
+    return Dataset(atom_offsets=off, coords=np.concatenate(coords), atnum=np.concatenate(atnum),
+                   species=np.zeros(ntot, dtype=np.int32), periodic=np.zeros(len(sizes), np.int32),
+                   latvecs=np.zeros((len(sizes), 9)), atomic_numbers=np.asarray([1, 6], np.int32),
+                   weights=np.ones(len(sizes), np.int32), atomic_weights=np.ones(ntot),
+                   global_targets=np.zeros((len(sizes), 1)), atomic_targets=np.zeros((ntot, 0)))
+
+
+def check_neighbors(ds, rcut, precision=api.FP64):
+    ref = O.neighbours(ds, rcut)
+    with api.Context(precision) as ctx:
+        ctx.upload(ds)
+        ctx.neighbors(rcut)
+        got = ctx.get_neighbors()
+    np.testing.assert_array_equal(got[0], ref[0])  # per-atom counts
+    np.testing.assert_array_equal(got[1], ref[1])  # neighbour index, in iterator order
+    np.testing.assert_array_equal(got[2], ref[2])  # image translation
+    np.testing.assert_array_equal(got[3], ref[3])  # squared distance, bit for bit
+    return int(ref[0][-1])
+
+
+@pytest.mark.parametrize("name", DATASETS)
+def test_neighbor_pairs_bit_exact_reference_datasets(name):
+    ds = G.load_dataset(name)
+    for rcut in (4.0 / 0.529177249, 7.0):
+        check_neighbors(ds, rcut)
+
+
+@pytest.mark.parametrize("precision", [api.FP32, api.FP64])
+def test_neighbor_pairs_bit_exact_small_cells_and_clusters(precision):
+    assert check_neighbors(small_cell_dataset(), 11.3, precision) > 0
+    assert check_neighbors(small_cell_dataset(seed=9, L_bohr=3.0), 7.5, precision) > 0
+    check_neighbors(cluster_dataset(), 6.0, precision)
+
+
+def test_neighbor_pairs_bit_exact_synthetic_c2():
+    ds = synthetic.generate("C2", nstruct=40)
+    rc = synthetic.CONFIGS["C2"].rcut / 0.529177249
+    assert check_neighbors(ds, rc) > 100000
+
+
+def acsf_on_gpu(ds, funcs, precision):
+    with api.Context(precision) as ctx:
+        ctx.upload(ds)
+        ctx.set_gfunctions(funcs)
+        return ctx.acsf()
+
+
+def mixed_functions(rcut, zs=(1, 8), atomid=0):
+    base = [GFunction("g1", rcut, atomid=atomid), GFunction("g2", rcut, rs=1.5, eta=0.3, atomid=atomid),
+            GFunction("g3", rcut, kappa=0.7, atomid=atomid),
+            GFunction("g4", rcut, eta=0.05, lam=1.0, xi=2.0, atomid=atomid),
+            GFunction("g4", rcut, eta=0.02, lam=-1.0, xi=1.0, atomid=atomid),
+            GFunction("g5", rcut, eta=0.05, lam=-1.0, xi=4.0, atomid=atomid),
+            GFunction("g5", rcut, eta=0.01, lam=1.0, xi=3.5, atomid=atomid)]
+    from fortnet_gb300.gfunctions import process_acsf_functions
+    return base + process_acsf_functions(base, zs)
+
+
+@pytest.mark.parametrize("kind", ["small_cells", "clusters", "c2"])
+def test_acsf_values_fp64_and_fp32(kind):
+    if kind == "small_cells":
+        ds, funcs = small_cell_dataset(), mixed_functions(7.0)
+    elif kind == "clusters":
+        ds, funcs = cluster_dataset(), mixed_functions(6.0, zs=(1, 6))
+    else:
+        cfg = synthetic.CONFIGS["C2"]
+        ds, funcs = synthetic.generate(cfg, nstruct=12), synthetic.gfunctions(cfg)
+    ref = O.acsf(ds, funcs)
+    g64 = acsf_on_gpu(ds, funcs, api.FP64)
+    np.testing.assert_allclose(g64, ref, rtol=1e-11, atol=1e-13)
+    g32 = acsf_on_gpu(ds, funcs, api.FP32)
+    scale = np.maximum(np.abs(ref).max(axis=0), 1e-30)
+    assert np.max(np.abs(g32 - ref) / scale) < 2e-5
+
+
+GOLDEN_PRED = [n for n in G.case_names() if G.load_case(n).settings["mode"] != "train"]
+GOLDEN_TRAIN = [n for n in G.case_names() if G.load_case(n).settings["mode"] == "train"]
+
+
+@pytest.mark.parametrize("name", GOLDEN_PRED)
+def test_golden_prediction_fp64(name):
+    case = G.load_case(name)
+    pred, forces = gpu_flows.prediction(case, api.FP64)
+    np.testing.assert_allclose(pred, case.arrays["out_rawpredictions"], rtol=G.RTOL, atol=G.ATOL)
+    if forces is not None:
+        np.testing.assert_allclose(forces.reshape(forces.shape[0], -1), case.arrays["out_forces"],
+                                   rtol=G.RTOL, atol=G.ATOL)
+
+
+@pytest.mark.parametrize("name", GOLDEN_TRAIN)
+def test_golden_training_fp64(name):
+    case = G.load_case(name)
+    zprec, params = gpu_flows.training(case, api.FP64)
+    out = case.net("out_")
+    np.testing.assert_allclose(params, out["params"], rtol=G.RTOL, atol=G.ATOL)
+    if zprec is not None and out["zprec"] is not None:
+        np.testing.assert_allclose(zprec, out["zprec"], rtol=G.RTOL, atol=G.ATOL)
+
+
+def test_golden_prediction_fp32_tolerances():
+    """FP32 plain form: energies within 1e-5 relative, forces within 1e-4 of the force scale."""
+    for name in GOLDEN_PRED:
+        case = G.load_case(name)
+        pred, forces = gpu_flows.prediction(case, api.FP32)
+        ref = case.arrays["out_rawpredictions"]
+        ds = case.ds
+        e = np.add.reduceat(pred, ds.atom_offsets[:-1], axis=0)
+        er = np.add.reduceat(ref, ds.atom_offsets[:-1], axis=0)
+        assert np.max(np.abs(e - er) / np.maximum(np.abs(er), 1e-3)) < 1e-5, name
+        if forces is not None:
+            fr = case.arrays["out_forces"]
+            f = forces.reshape(forces.shape[0], -1)
+            assert np.max(np.abs(f - fr)) < 1e-4 * max(np.abs(fr).max(), 1e-3), name
+
+
+def oracle_energy_forces(ds, funcs, zprec, dims, act, params, sp, physical=True):
+    vals = O.acsf(ds, funcs)
+    feats = O.zscore_apply(vals, zprec)
+    pred = O.predict(dims, act, params, feats, sp)
+    jac = O.jacobian(dims, act, params, feats, sp)
+    F = O.forces(ds, funcs, zprec, jac, physical=physical)
+    return pred, F
+
+
+@pytest.mark.parametrize("precision", [api.FP64, api.FP32])
+def test_forces_with_repeated_images_match_exact_derivative(precision):
+    ds = small_cell_dataset(seed=11, n=5, L_bohr=6.0)
+    funcs = mixed_functions(7.0)
+    nf = len(funcs)
+    dims = [nf, 6, 5, 1]
+    params = O.Ranlux(5).init_bpnn(dims, "tanh", 1)
+    params[0, -12:] = np.linspace(-0.3, 0.3, 12)  # non-zero biases
+    vals = O.acsf(ds, funcs)
+    zprec = O.zscore_stats(vals, ds)
+    sp = np.zeros(ds.ntot, dtype=np.int32)
+    pred_ref, F_ref = oracle_energy_forces(ds, funcs, zprec, dims, "tanh", params, sp)
+    with api.Context(precision) as ctx:
+        ctx.upload(ds)
+        ctx.set_species(sp)
+        ctx.set_gfunctions(funcs)
+        ctx.acsf(download=False)
+        ctx.zscore(zprec=zprec)
+        ctx.set_network(dims, "tanh", params)
+        pred, _ = ctx.predict()
+        F = ctx.forces()
+    tol = 1e-10 if precision == api.FP64 else 1e-4
+    np.testing.assert_allclose(pred, pred_ref, rtol=tol, atol=tol)
+    assert np.max(np.abs(F - F_ref)) <= tol * max(1.0, np.abs(F_ref).max())
+
+
+def test_forces_match_finite_differences_of_the_oracle_energy():
+    ds = small_cell_dataset(seed=13, n=4, L_bohr=6.5, nstruct=1)
+    funcs = mixed_functions(7.0)
+    dims = [len(funcs), 5, 1]
+    params = O.Ranlux(9).init_bpnn(dims, "tanh", 1)
+    vals = O.acsf(ds, funcs)
+    zprec = O.zscore_stats(vals, ds)
+    sp = np.zeros(ds.ntot, dtype=np.int32)
+
+    def energy(coords):
+        d2 = Dataset(**{**ds.__dict__, "coords": coords})
+        v = O.zscore_apply(O.acsf(d2, funcs), zprec)
+        return O.predict(dims, "tanh", params, v, sp).sum()
+
+    h = 1e-5
+    F_fd = np.zeros((ds.ntot, 3))
+    for a in range(ds.ntot):
+        for c in range(3):
+            cp = ds.coords.copy()
+            cm = ds.coords.copy()
+            cp[a, c] += h
+            cm[a, c] -= h
+            F_fd[a, c] = -(energy(cp) - energy(cm)) / (2 * h)
+    with api.Context(api.FP64) as ctx:
+        ctx.upload(ds)
+        ctx.set_species(sp)
+        ctx.set_gfunctions(funcs)
+        ctx.acsf(download=False)
+        ctx.zscore(zprec=zprec)
+        ctx.set_network(dims, "tanh", params)
+        F = ctx.forces()[:, 0, :]
+    np.testing.assert_allclose(F, F_fd, rtol=1e-6, atol=1e-7)
+
+
+def test_c2_energies_fp32_within_1e5_of_fp64_oracle():
+    cfg = synthetic.CONFIGS["C2"]
+    ds = synthetic.generate(cfg, nstruct=16)
+    funcs = synthetic.gfunctions(cfg)
+    dims = synthetic.network_dims(cfg)
+    params = O.Ranlux(1002).init_bpnn(dims, "tanh", 2)
+    vals = O.acsf(ds, funcs)
+    zprec = O.zscore_stats(vals, ds)
+    feats = O.zscore_apply(vals, zprec)
+    pred = O.predict(dims, "tanh", params, feats, ds.species)
+    with api.Context(api.FP32) as ctx:
+        ctx.upload(ds)
+        ctx.set_species(ds.species)
+        ctx.set_gfunctions(funcs)
+        ctx.acsf(download=False)
+        z = ctx.zscore(weights=ds.weights)
+        ctx.set_network(dims, "tanh", params)
+        _, glob = ctx.predict()
+    np.testing.assert_allclose(z, zprec, rtol=1e-5, atol=1e-7)
+    e_ref = np.add.reduceat(pred, ds.atom_offsets[:-1], axis=0)
+    assert np.max(np.abs(glob - e_ref) / np.abs(e_ref)) < 1e-5
+
+
+@pytest.mark.parametrize("optimizer", ["sd", "lbfgs"])
+def test_training_iterations_match_oracle(optimizer):
+    """Several full training iterations (gradient, update, optimiser incl. line search)."""
+    cfg = synthetic.CONFIGS["C1"]
+    ds = synthetic.generate(cfg, nstruct=12)
+    funcs = synthetic.gfunctions(cfg)
+    dims = synthetic.network_dims(cfg)
+    params0 = O.Ranlux(4).init_bpnn(dims, "tanh", 1)
+    vals = O.acsf(ds, funcs)
+    zprec = O.zscore_stats(vals, ds)
+    feats = O.zscore_apply(vals, zprec)
+    niter = 6
+    opt = (O.SteepestDescent(params0[0], 1e-30, 5e-2, 0.01) if optimizer == "sd"
+           else O.Lbfgs(params0[0], 1e-30, 1e-6, 1.0, 20, True, False))
+    params = params0.copy()
+    dd, _ = O.train_gradients(dims, "tanh", params, feats, ds)
+    ref_hist = []
+    for _ in range(niter):
+        g, _ = O.update_prepare(dims, "tanh", params, dd, 0.0, 0.0, float(ds.weights.sum()))
+        params = opt.next(0.0, g[0])[0][None, :]
+        dd, _ = O.train_gradients(dims, "tanh", params, feats, ds)
+        ref_hist.append(params.copy())
+    with api.Context(api.FP64) as ctx:
+        ctx.upload(ds)
+        ctx.set_species(ds.species)
+        ctx.set_gfunctions(funcs)
+        ctx.acsf(download=False)
+        ctx.zscore(zprec=zprec)
+        ctx.set_network(dims, "tanh", params0)
+        ctx.set_targets(ds)
+        if optimizer == "sd":
+            ctx.optimizer_init("sd", 1e-30, 1e-6, 5e-2, 0.01)
+        else:
+            ctx.optimizer_init("lbfgs", 1e-30, 1e-6, 1.0, memory=20, linemin=True)
+        for it in range(niter):
+            ctx.train_iteration("mse")
+            np.testing.assert_allclose(ctx.params(), ref_hist[it], rtol=1e-8, atol=1e-10)
