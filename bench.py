@@ -214,8 +214,10 @@ def run_ours(args):
     prof = {f: ctx.profile_read(f) for f in fams}
     ctx.profile(False)
     value = N * world / (ms_step / 1e3)
-    # ---- end to end through the public API with host buffers
-    coords = np.ascontiguousarray(ds.coords)
+    # ---- end to end through the public API with host buffers (pinned)
+    coords_t = torch.empty((N, 3), dtype=torch.float64, pin_memory=True)
+    coords = coords_t.numpy()
+    coords[:] = ds.coords
     energy = np.zeros((ds.nstruct, 1))
     forces = np.zeros((N, 1, 3))
     for _ in range(2):
@@ -278,7 +280,7 @@ def cpu_step(ds, funcs, dims, params, zprec, nthreads):
     dd, _ = O.train_gradients(dims, "tanh", newp, feats, ds)
     out = O.predict(dims, "tanh", newp, feats, ds.species)
     jac = O.jacobian(dims, "tanh", newp, feats, ds.species)
-    O.forces(ds, funcs, zprec, jac)
+    O.forces(ds, funcs, zprec, jac, nthreads=nthreads)
     return out
 
 

@@ -267,34 +267,6 @@ int fnetg_upload_structures(fnetg_ctx *ctx, int32_t nstruct, const int64_t *atom
   std::vector<int32_t> astruct(N);
   for (int s = 0; s < nstruct; s++)
     for (int64_t a = atom_offsets[s]; a < atom_offsets[s + 1]; a++) astruct[a] = s;
-  // bounding boxes (float, with the structure's extent) for image pruning
-  std::vector<float> bbox((size_t)6 * std::max(nstruct, 1), 0.f);
-  std::vector<V4<float>> cf(std::max<int64_t>(N, 1));
-  for (int s = 0; s < nstruct; s++) {
-    double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
-    for (int64_t a = atom_offsets[s]; a < atom_offsets[s + 1]; a++)
-      for (int c = 0; c < 3; c++) {
-        lo[c] = std::min(lo[c], coords[3 * a + c]);
-        hi[c] = std::max(hi[c], coords[3 * a + c]);
-      }
-    for (int c = 0; c < 3; c++) {
-      bbox[6 * s + c] = (float)lo[c];
-      bbox[6 * s + 3 + c] = (float)hi[c];
-    }
-  }
-  // float copies relative to each structure's bounding-box corner keep the pre-filter's
-  // rounding independent of where the structure sits in space
-  for (int s = 0; s < nstruct; s++) {
-    double ref[3];
-    for (int c = 0; c < 3; c++) ref[c] = (double)bbox[6 * s + c];
-    for (int64_t a = atom_offsets[s]; a < atom_offsets[s + 1]; a++)
-      cf[a] = V4<float>{(float)(coords[3 * a] - ref[0]), (float)(coords[3 * a + 1] - ref[1]),
-                        (float)(coords[3 * a + 2] - ref[2]), 0.f};
-    for (int c = 0; c < 3; c++) {
-      bbox[6 * s + 3 + c] = (float)((double)bbox[6 * s + 3 + c] - ref[c]);
-      bbox[6 * s + c] = 0.f;
-    }
-  }
   FNETG_CUDA(ctx->d_off.ensure(sizeof(int64_t) * (nstruct + 1)));
   FNETG_CUDA(ctx->d_atom_struct.ensure(sizeof(int32_t) * std::max<int64_t>(N, 1)));
   FNETG_CUDA(ctx->d_coords.ensure(sizeof(double) * 3 * std::max<int64_t>(N, 1)));
@@ -311,15 +283,11 @@ int fnetg_upload_structures(fnetg_ctx *ctx, int32_t nstruct, const int64_t *atom
                                cudaMemcpyHostToDevice, st));
     FNETG_CUDA(cudaMemcpyAsync(ctx->d_coords.p, coords, sizeof(double) * 3 * N,
                                cudaMemcpyHostToDevice, st));
-    FNETG_CUDA(cudaMemcpyAsync(ctx->d_coordsf.p, cf.data(), sizeof(V4<float>) * N,
-                               cudaMemcpyHostToDevice, st));
     FNETG_CUDA(cudaMemcpyAsync(ctx->d_atnum.p, atnum, sizeof(int32_t) * N,
                                cudaMemcpyHostToDevice, st));
   }
   if (nstruct > 0) {
     FNETG_CUDA(cudaMemcpyAsync(ctx->d_lat.p, ctx->h_lat.data(), sizeof(double) * 9 * nstruct,
-                               cudaMemcpyHostToDevice, st));
-    FNETG_CUDA(cudaMemcpyAsync(ctx->d_bbox.p, bbox.data(), sizeof(float) * 6 * nstruct,
                                cudaMemcpyHostToDevice, st));
     FNETG_CUDA(cudaMemcpyAsync(ctx->d_periodic.p, ctx->h_periodic.data(),
                                sizeof(int32_t) * nstruct, cudaMemcpyHostToDevice, st));
@@ -328,6 +296,23 @@ int fnetg_upload_structures(fnetg_ctx *ctx, int32_t nstruct, const int64_t *atom
     FNETG_CUDA(ctx->d_ext.ensure(sizeof(double) * N * next));
     FNETG_CUDA(cudaMemcpyAsync(ctx->d_ext.p, ext, sizeof(double) * N * next,
                                cudaMemcpyHostToDevice, st));
+  }
+  {
+    int rc = prepare_coords(ctx);
+    if (rc) return rc;
+  }
+  ctx->max_extent = 0.0;
+  for (int s = 0; s < nstruct; s++) {
+    double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+    for (int64_t a = atom_offsets[s]; a < atom_offsets[s + 1]; a++)
+      for (int c = 0; c < 3; c++) {
+        lo[c] = std::min(lo[c], coords[3 * a + c]);
+        hi[c] = std::max(hi[c], coords[3 * a + c]);
+      }
+    if (atom_offsets[s + 1] > atom_offsets[s])
+      ctx->max_extent = std::max(ctx->max_extent, std::sqrt((hi[0] - lo[0]) * (hi[0] - lo[0]) +
+                                                             (hi[1] - lo[1]) * (hi[1] - lo[1]) +
+                                                             (hi[2] - lo[2]) * (hi[2] - lo[2])));
   }
   FNETG_CUDA(cudaStreamSynchronize(st));
   invalidate_geometry(ctx);
@@ -341,24 +326,30 @@ int fnetg_upload_structures(fnetg_ctx *ctx, int32_t nstruct, const int64_t *atom
 }
 
 int fnetg_update_coords(fnetg_ctx *ctx, const double *coords) {
-  if (!ctx || !coords) return FNETG_E_INVALID;
-  FNETG_CHECK(ctx->N > 0, FNETG_E_INVALID, "no structures uploaded");
-  std::vector<int64_t> off = ctx->h_off;
-  std::vector<int32_t> atnum = ctx->h_atnum, per = ctx->h_periodic;
-  std::vector<double> lat = ctx->h_lat;
-  std::vector<int32_t> sp = ctx->h_species;
-  bool had_species = ctx->species_set;
-  std::vector<double> ext;
-  int32_t next = ctx->next;
-  if (next > 0) {
-    ext.resize((size_t)ctx->N * next);
-    FNETG_CUDA(cudaMemcpy(ext.data(), ctx->d_ext.p, sizeof(double) * ext.size(),
-                          cudaMemcpyDeviceToHost));
-  }
-  int rc = fnetg_upload_structures(ctx, ctx->S, off.data(), atnum.data(), coords, per.data(),
-                                   lat.data(), next ? ext.data() : nullptr, next);
+  if (!ctx || (!coords && ctx->N > 0)) return FNETG_E_INVALID;
+  const int64_t N = ctx->N;
+  for (int64_t q = 0; q < 3 * N; q++)
+    FNETG_CHECK(std::isfinite(coords[q]), FNETG_E_GEOMETRY, "non-finite coordinate");
+  if (N > 0)
+    FNETG_CUDA(cudaMemcpyAsync(ctx->d_coords.p, coords, sizeof(double) * 3 * N,
+                               cudaMemcpyHostToDevice, ctx->stream));
+  int rc = prepare_coords(ctx);
   if (rc) return rc;
-  if (had_species) return fnetg_set_species(ctx, sp.data());
+  double ext = 0.0;
+  for (int s = 0; s < ctx->S; s++) {
+    double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+    for (int64_t a = ctx->h_off[s]; a < ctx->h_off[s + 1]; a++)
+      for (int c = 0; c < 3; c++) {
+        lo[c] = std::min(lo[c], coords[3 * a + c]);
+        hi[c] = std::max(hi[c], coords[3 * a + c]);
+      }
+    if (ctx->h_off[s + 1] > ctx->h_off[s])
+      ext = std::max(ext, std::sqrt((hi[0] - lo[0]) * (hi[0] - lo[0]) +
+                                    (hi[1] - lo[1]) * (hi[1] - lo[1]) +
+                                    (hi[2] - lo[2]) * (hi[2] - lo[2])));
+  }
+  ctx->max_extent = ext;
+  invalidate_geometry(ctx);
   return FNETG_OK;
 }
 
@@ -505,8 +496,76 @@ int fnetg_set_gfunctions(fnetg_ctx *ctx, int32_t ng, const fnetg_gfunc *g) {
       ctx->h_rad.push_back(d);
     }
   }
-  // group angular functions by list channels, cutoff and atom-id column (stable), at most
-  // kMaxGroupFuncs per group
+  // G5 functions with a small integer xi take the moment form; the rest (G4, other xi) the
+  // triplet sweep
+  std::vector<GDesc> mom, trip;
+  for (auto &d : ang) {
+    if (d.type == 5 && d.xi_int >= 1 && d.xi_int <= kMaxMomentDegree) mom.push_back(d);
+    else trip.push_back(d);
+  }
+  ang = trip;
+  ctx->h_mfunc.clear();
+  ctx->h_mcoef.clear();
+  ctx->h_combo.clear();
+  ctx->mom_degree = 0;
+  for (auto &d : mom) ctx->mom_degree = std::max(ctx->mom_degree, d.xi_int);
+  const int D = ctx->mom_degree;
+  ctx->n_mono = D > 0 ? (D + 1) * (D + 2) * (D + 3) / 6 : 0;
+  const int nz = (int)zs.size(), ne = (int)ctx->ecls_eta.size();
+  ctx->h_cidx.assign((size_t)(nz + 1) * std::max(ne, 1), -1);
+  auto combo_of = [&](int chan, int e) -> int {
+    int &slot = ctx->h_cidx[(size_t)(chan + 1) * ne + e];
+    if (slot < 0) {
+      slot = (int)ctx->h_combo.size() / 2;
+      ctx->h_combo.push_back(chan);
+      ctx->h_combo.push_back(e);
+    }
+    return slot;
+  };
+  // monomials ordered by degree, then by descending x and y exponents
+  std::vector<std::array<int, 3>> mono;
+  for (int m = 0; m <= D; m++)
+    for (int a = m; a >= 0; a--)
+      for (int b = m - a; b >= 0; b--) mono.push_back({a, b, m - a - b});
+  auto fact = [](int n) {
+    double r = 1.0;
+    for (int k = 2; k <= n; k++) r *= k;
+    return r;
+  };
+  for (auto &d : mom) {
+    MFunc mf{};
+    mf.k1 = combo_of(d.chan1, d.eclass);
+    mf.k2 = combo_of(d.chan2, d.eclass);
+    mf.out = d.out;
+    ctx->h_mfunc.push_back(mf);
+    for (auto &al : mono) {
+      const int m = al[0] + al[1] + al[2];
+      double c = 0.0;
+      if (m <= d.xi_int) {
+        const double binom = fact(d.xi_int) / (fact(m) * fact(d.xi_int - m));
+        const double w = fact(m) / (fact(al[0]) * fact(al[1]) * fact(al[2]));
+        c = d.pref * binom * std::pow(d.lambda, m) * w;
+      }
+      ctx->h_mcoef.push_back(c);
+    }
+  }
+  ctx->n_combo = (int)ctx->h_combo.size() / 2;
+  FNETG_CUDA(ctx->d_mfunc.ensure(sizeof(MFunc) * std::max<size_t>(ctx->h_mfunc.size(), 1)));
+  FNETG_CUDA(ctx->d_mcoef.ensure(sizeof(double) * std::max<size_t>(ctx->h_mcoef.size(), 1)));
+  FNETG_CUDA(ctx->d_combo.ensure(sizeof(int32_t) * std::max<size_t>(ctx->h_combo.size(), 2)));
+  FNETG_CUDA(ctx->d_cidx.ensure(sizeof(int32_t) * std::max<size_t>(ctx->h_cidx.size(), 1)));
+  if (!ctx->h_mfunc.empty()) {
+    FNETG_CUDA(cudaMemcpy(ctx->d_mfunc.p, ctx->h_mfunc.data(), sizeof(MFunc) * ctx->h_mfunc.size(),
+                          cudaMemcpyHostToDevice));
+    FNETG_CUDA(cudaMemcpy(ctx->d_mcoef.p, ctx->h_mcoef.data(),
+                          sizeof(double) * ctx->h_mcoef.size(), cudaMemcpyHostToDevice));
+    FNETG_CUDA(cudaMemcpy(ctx->d_combo.p, ctx->h_combo.data(),
+                          sizeof(int32_t) * ctx->h_combo.size(), cudaMemcpyHostToDevice));
+  }
+  FNETG_CUDA(cudaMemcpy(ctx->d_cidx.p, ctx->h_cidx.data(), sizeof(int32_t) * ctx->h_cidx.size(),
+                        cudaMemcpyHostToDevice));
+  // group the remaining angular functions by list channels, cutoff and atom-id column
+  // (stable), at most kMaxGroupFuncs per group
   std::vector<std::array<int, 4>> chans;
   for (auto &d : ang) {
     std::array<int, 4> c{d.chan1, d.chan2, d.rclass, d.atomid};
@@ -604,8 +663,12 @@ int fnetg_get_neighbors(fnetg_ctx *ctx, int64_t *pair_offsets, int32_t *j, int32
     for (int64_t q = 0; q < P; q++)
       for (int c = 0; c < 3; c++) shift[3 * q + c] = (int32_t)(int8_t)((meta[q] >> (8 * c)) & 0xff);
   }
-  if (d2 && P > 0)
+  if (d2 && P > 0) {
+    int rc = pair_d2(ctx);
+    if (rc) return rc;
+    FNETG_CUDA(cudaStreamSynchronize(ctx->stream));
     FNETG_CUDA(cudaMemcpy(d2, ctx->d_d2.p, sizeof(double) * P, cudaMemcpyDeviceToHost));
+  }
   return FNETG_OK;
 }
 

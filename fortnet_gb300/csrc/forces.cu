@@ -2,127 +2,24 @@
 // lib_analysis/forces.F90:317-425, on the ACSF derivatives of gFuncGrad / iGeoAcsfGrad,
 // lib_descriptors/acsf.F90:870-939, 1496-1697) as a fused adjoint contraction.
 //
-// Instead of materialising the dense [3, nG, N, N] derivative array, every centre atom i
-// contracts dE/dG_i (the network Jacobian divided by the z-score deviations) with the
-// derivatives of its own G-values on the fly: one warp per atom stages the pair tile,
-// accumulates w_p = sum_g dE/dG_ig * dG_ig/dv_p for every neighbour image p (radial terms
-// lanes-over-pairs, angular terms lanes-over-(row, column-chunk) of the triplet matrix with
-// shared-memory accumulation), and scatters F_j -= w_p, F_i += w_p with FP64 atomics.
-// Each periodic image contributes its own derivative (physical forces).
+// The dense [3, nG, N, N] derivative array is never formed: every centre atom contracts
+// dE/dG_i (network Jacobian divided by the z-score deviations) with the derivatives of its own
+// G-values on the fly.  One warp per atom over the shared neighbour tile (tile.cuh) accumulates
+// w_p = sum_g dE/dG_ig * dG_ig/dv_p for every neighbour image p:
+//   radial terms     lanes over pairs;
+//   integer-xi G5    adjoint moments Q_k(alpha) = sum_f J_f coef_f(alpha) M_other(alpha), then per
+//                    pair w_p += sum_k Q_k(alpha) d(E u^alpha)/dv_p — O(N_nb) per atom;
+//   G4 / other xi    lanes over (row, column chunk) of the triplet matrix with shared-memory
+//                    accumulation.
+// Forces are scattered as F_j -= w_p, F_i += w_p with FP64 atomics; every periodic image
+// contributes its own derivative (physical forces), self images cancel.
 #include <algorithm>
 
-#include "internal.cuh"
+#include "tile.cuh"
 
 namespace fnetg {
 
 namespace {
-
-constexpr double kPi = 3.14159265358979323846;
-
-template <typename T> struct ForceArgs {
-  int64_t natoms;
-  const int64_t *poff;
-  const int32_t *pj;
-  const uint32_t *pmeta;
-  const V4<T> *rij;
-  const int8_t *code;
-  const double *ext;
-  int next;
-  const GDesc *rad;
-  int nrad;
-  const GDesc *ang;
-  const AGroup *groups;
-  int ngroups;
-  const double *ecls_eta;
-  const int *ecls_rclass;
-  const int *ecls_atomid;
-  int necls;
-  const double *rcls;
-  int nrcls;
-  int nz;
-  int cap;
-  int ng;
-  const T *J;   // [N][nf] atom order, dE/dG (raw features)
-  int nf;
-  double *F;    // [N][nout][3]
-  int out_index, nout;
-};
-
-template <typename T> struct FTile {
-  V4<T> *v;
-  V4<T> *w;        // pair force accumulators (x, y, z)
-  T *fc, *dfc;     // [nrcls][cap]
-  T *E, *D;        // [necls][cap]
-  uint32_t *info;
-  int32_t *pj;
-  uint16_t *lists;
-  int *cnt;
-  T *jv;           // [ng] dE/dG of the centre atom
-  T *gpar;         // [5][32] lambda, xi, eta, Jw, rcut
-  int *gint;       // [3][32] xi_int, eclass, type
-  T *idv;          // [cap] atom ids of the group's column (G4 third cutoff)
-};
-
-template <typename T> __host__ __device__ size_t ftile_bytes(int cap, int nrcls, int necls, int nz, int ng) {
-  size_t b = 0;
-  b += 2 * sizeof(V4<T>) * cap;
-  b += sizeof(T) * (size_t)cap * 2 * (nrcls + necls);
-  b += (sizeof(uint32_t) + sizeof(int32_t)) * cap;
-  b += sizeof(T) * (ng + 5 * 32);
-  b += sizeof(int) * (3 * 32 + 8);
-  b += sizeof(uint16_t) * (size_t)cap * nz;
-  b += sizeof(T) * cap;
-  return (b + 127) / 128 * 128;
-}
-
-template <typename T>
-__device__ FTile<T> fcarve(unsigned char *p, int cap, int nrcls, int necls, int nz, int ng) {
-  FTile<T> t;
-  t.v = reinterpret_cast<V4<T> *>(p);
-  p += sizeof(V4<T>) * cap;
-  t.w = reinterpret_cast<V4<T> *>(p);
-  p += sizeof(V4<T>) * cap;
-  t.fc = reinterpret_cast<T *>(p);
-  p += sizeof(T) * (size_t)cap * nrcls;
-  t.dfc = reinterpret_cast<T *>(p);
-  p += sizeof(T) * (size_t)cap * nrcls;
-  t.E = reinterpret_cast<T *>(p);
-  p += sizeof(T) * (size_t)cap * necls;
-  t.D = reinterpret_cast<T *>(p);
-  p += sizeof(T) * (size_t)cap * necls;
-  t.jv = reinterpret_cast<T *>(p);
-  p += sizeof(T) * ng;
-  t.gpar = reinterpret_cast<T *>(p);
-  p += sizeof(T) * 5 * 32;
-  t.idv = reinterpret_cast<T *>(p);
-  p += sizeof(T) * cap;
-  t.info = reinterpret_cast<uint32_t *>(p);
-  p += sizeof(uint32_t) * cap;
-  t.pj = reinterpret_cast<int32_t *>(p);
-  p += sizeof(int32_t) * cap;
-  t.gint = reinterpret_cast<int *>(p);
-  p += sizeof(int) * 3 * 32;
-  t.cnt = reinterpret_cast<int *>(p);
-  p += sizeof(int) * 8;
-  t.lists = reinterpret_cast<uint16_t *>(p);
-  return t;
-}
-
-template <typename T> __device__ __forceinline__ T f_exp(T x);
-template <> __device__ __forceinline__ float f_exp<float>(float x) { return expf(x); }
-template <> __device__ __forceinline__ double f_exp<double>(double x) { return exp(x); }
-template <typename T> __device__ __forceinline__ T f_cos(T x);
-template <> __device__ __forceinline__ float f_cos<float>(float x) { return cosf(x); }
-template <> __device__ __forceinline__ double f_cos<double>(double x) { return cos(x); }
-template <typename T> __device__ __forceinline__ T f_sin(T x);
-template <> __device__ __forceinline__ float f_sin<float>(float x) { return sinf(x); }
-template <> __device__ __forceinline__ double f_sin<double>(double x) { return sin(x); }
-template <typename T> __device__ __forceinline__ T f_pow(T b, T e);
-template <> __device__ __forceinline__ float f_pow<float>(float b, float e) { return powf(b, e); }
-template <> __device__ __forceinline__ double f_pow<double>(double b, double e) { return pow(b, e); }
-template <typename T> __device__ __forceinline__ T f_sqrt(T x);
-template <> __device__ __forceinline__ float f_sqrt<float>(float x) { return sqrtf(x); }
-template <> __device__ __forceinline__ double f_sqrt<double>(double x) { return sqrt(x); }
 
 template <typename T> __device__ __forceinline__ T ipow_or_pow(T base, int n, T e) {
   // base^e where n = e if e is a small positive integer (n == 0: general power)
@@ -131,19 +28,14 @@ template <typename T> __device__ __forceinline__ T ipow_or_pow(T base, int n, T 
     for (int k = 0; k < n; k++) r *= base;
     return r;
   }
-  return f_pow<T>(base, e);
-}
-
-template <typename T>
-__device__ __forceinline__ T aid(const double *ext, int next, int atomid, int64_t a) {
-  return atomid > 0 ? (T)ext[a * next + (atomid - 1)] : (T)1;
+  return m_pow<T>(base, e);
 }
 
 template <typename T> __device__ __forceinline__ void sh_add(T *p, T v) { atomicAdd(p, v); }
 
 // rows over list R, columns over list C: w[row] += fac * d/dv_row of sum_f Jw_f t_f(row, col)
 template <typename T>
-__device__ void angular_side(const ForceArgs<T> &a, FTile<T> &tl, const AGroup &G,
+__device__ void angular_side(const TileArgs<T> &a, Tile<T> &tl, const AGroup &G,
                              const uint16_t *lr, int nr, const uint16_t *lc, int nc, T fac,
                              int lane) {
   if (nr == 0 || nc == 0) return;
@@ -171,7 +63,7 @@ __device__ void angular_side(const ForceArgs<T> &a, FTile<T> &tl, const AGroup &
         ex = vp.x - vq.x;
         ey = vp.y - vq.y;
         ez = vp.z - vq.z;
-        rpq = f_sqrt<T>(ex * ex + ey * ey + ez * ez);
+        rpq = m_sqrt<T>(ex * ex + ey * ey + ez * ez);
       }
       T A = 0, B = 0, C = 0;
 #pragma unroll 4
@@ -180,7 +72,7 @@ __device__ void angular_side(const ForceArgs<T> &a, FTile<T> &tl, const AGroup &
         const int xn = tl.gint[f], e = tl.gint[32 + f], ty = tl.gint[64 + f];
         const T base = (T)1 + lam * c;
         const T angm1 = xn > 1 ? ipow_or_pow<T>(base, xn - 1, xi - (T)1)
-                               : (xn == 1 ? (T)1 : f_pow<T>(base, xi - (T)1));
+                               : (xn == 1 ? (T)1 : m_pow<T>(base, xi - (T)1));
         const T ang = angm1 * base;
         const T angd = xi * lam * angm1;
         const T Ep = tl.E[e * a.cap + p], Eq = tl.E[e * a.cap + q], Dp = tl.D[e * a.cap + p];
@@ -191,9 +83,9 @@ __device__ void angular_side(const ForceArgs<T> &a, FTile<T> &tl, const AGroup &
             gg = 0;
             ggd = 0;
           } else {
-            const T ee = f_exp<T>(-(eta * rpq * rpq));
-            const T fcq = (T)0.5 * (f_cos<T>((T)kPi * rpq / rcut4) + (T)1);
-            const T dfq = (T)-0.5 * ((T)kPi / rcut4) * f_sin<T>((T)kPi * rpq / rcut4);
+            const T ee = m_exp<T>(-(eta * rpq * rpq));
+            const T fcq = (T)0.5 * (m_cos<T>((T)kPi * rpq / rcut4) + (T)1);
+            const T dfq = (T)-0.5 * ((T)kPi / rcut4) * m_sin<T>((T)kPi * rpq / rcut4);
             gg = ee * fcq;
             ggd = ee * (dfq - (T)2 * eta * rpq * fcq);
             if (G.atomid > 0) {
@@ -227,76 +119,80 @@ __device__ void angular_side(const ForceArgs<T> &a, FTile<T> &tl, const AGroup &
   }
 }
 
-template <typename T>
-__global__ void __launch_bounds__(256) forces_kernel(ForceArgs<T> a) {
+
+// per-pair derivative of the moment terms, degree D known at compile time
+template <typename T, int D>
+__device__ __forceinline__ void moment_pair_force(const TileArgs<T> &a, Tile<T> &tl, int q,
+                                                  int z) {
+  constexpr int NM = n_mono_of(D);
+  const V4<T> u = tl.u[q];
+  const T r = u.w;
+  T px[D + 1], py[D + 1], pz[D + 1];
+  px[0] = py[0] = pz[0] = (T)1;
+#pragma unroll
+  for (int d = 1; d <= D; d++) {
+    px[d] = px[d - 1] * u.x;
+    py[d] = py[d - 1] * u.y;
+    pz[d] = pz[d - 1] * u.z;
+  }
+  T wx = 0, wy = 0, wz = 0;
+  for (int e = 0; e < a.necls; e++) {
+    const int ks = (z >= 0 && z < a.nz) ? a.cidx[(z + 1) * a.necls + e] : -1;
+    const int ka = a.cidx[e];
+    if (ks < 0 && ka < 0) continue;
+    const T *Qs = ks >= 0 ? tl.Q + ks * a.n_mono : nullptr;
+    const T *Qa = ka >= 0 ? tl.Q + ka * a.n_mono : nullptr;
+    T P = 0, gx = 0, gy = 0, gz = 0;
+#pragma unroll
+    for (int al = 0; al < NM; al++) {
+      const int ea = kMonoTab[al][0], eb = kMonoTab[al][1], ec = kMonoTab[al][2];
+      T c = 0;
+      if (Qs) c += Qs[al];
+      if (Qa) c += Qa[al];
+      P += c * px[ea] * py[eb] * pz[ec];
+      if (ea > 0) gx += c * (T)ea * px[ea > 0 ? ea - 1 : 0] * py[eb] * pz[ec];
+      if (eb > 0) gy += c * (T)eb * px[ea] * py[eb > 0 ? eb - 1 : 0] * pz[ec];
+      if (ec > 0) gz += c * (T)ec * px[ea] * py[eb] * pz[ec > 0 ? ec - 1 : 0];
+    }
+    const T Ee = tl.E[e * a.cap + q], De = tl.D[e * a.cap + q];
+    const T gu = gx * u.x + gy * u.y + gz * u.z;
+    const T s = Ee / r;
+    wx += De * P * u.x + s * (gx - gu * u.x);
+    wy += De * P * u.y + s * (gy - gu * u.y);
+    wz += De * P * u.z + s * (gz - gu * u.z);
+  }
+  tl.w[q].x += wx;
+  tl.w[q].y += wy;
+  tl.w[q].z += wz;
+}
+
+template <typename T, int D>
+__global__ void __launch_bounds__(256) forces_kernel(TileArgs<T> a) {
   extern __shared__ __align__(128) unsigned char smem[];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int wpb = blockDim.x >> 5;
-  const size_t tb = ftile_bytes<T>(a.cap, a.nrcls, a.necls, a.nz, a.ng);
-  FTile<T> tl = fcarve<T>(smem + tb * warp, a.cap, a.nrcls, a.necls, a.nz, a.ng);
+  const size_t tb = tile_bytes<T>(a.cap, a.nrcls, a.necls, a.nz, a.ncombo, a.n_mono, a.ng, true);
+  Tile<T> tl = carve_tile<T>(smem + tb * warp, a, true);
   for (int64_t i = (int64_t)blockIdx.x * wpb + warp; i < a.natoms; i += (int64_t)gridDim.x * wpb) {
     const int64_t p0 = a.poff[i];
     const int np = (int)(a.poff[i + 1] - p0);
     for (int g = lane; g < a.ng; g += 32) tl.jv[g] = a.J[i * a.nf + g];
-    for (int q = lane; q < np; q += 32) {
-      const V4<T> v = a.rij[p0 + q];
-      tl.v[q] = v;
-      tl.w[q] = V4<T>{0, 0, 0, 0};
-      const int32_t j = a.pj[p0 + q];
-      tl.pj[q] = j;
-      const uint32_t rmask = a.pmeta[p0 + q] >> 24;
-      const int c = a.code[j];
-      tl.info[q] = (uint32_t)(c & 0xff) | ((uint32_t)(j == i) << 8) | (rmask << 16);
-      for (int rc = 0; rc < a.nrcls; rc++) {
-        const T rcut = (T)a.rcls[rc];
-        const bool in = (rmask >> rc) & 1u;
-        tl.fc[rc * a.cap + q] = in ? (T)0.5 * (f_cos<T>((T)kPi * v.w / rcut) + (T)1) : (T)0;
-        tl.dfc[rc * a.cap + q] =
-            in ? (T)-0.5 * ((T)kPi / rcut) * f_sin<T>((T)kPi * v.w / rcut) : (T)0;
-      }
-      for (int e = 0; e < a.necls; e++) {
-        const T eta = (T)a.ecls_eta[e];
-        const int rc = a.ecls_rclass[e];
-        const T ex = f_exp<T>(-(eta * (v.w * v.w)));
-        T ids = (T)1;
-        if (a.ecls_atomid[e] > 0)
-          ids = aid<T>(a.ext, a.next, a.ecls_atomid[e], i) * aid<T>(a.ext, a.next, a.ecls_atomid[e], j);
-        const T f = tl.fc[rc * a.cap + q], df = tl.dfc[rc * a.cap + q];
-        tl.E[e * a.cap + q] = ex * f * ids;
-        tl.D[e * a.cap + q] = ex * (df - (T)2 * eta * v.w * f) * ids;
-      }
-    }
-    __syncwarp();
-    for (int z = 0; z < a.nz; z++) {
-      int base = 0;
-      for (int q0 = 0; q0 < np; q0 += 32) {
-        const int q = q0 + lane;
-        bool in = false;
-        if (q < np) {
-          const uint32_t inf = tl.info[q];
-          in = ((int)(inf & 0xff) == z) || ((inf >> 8) & 1u);
-        }
-        const unsigned m = __ballot_sync(0xffffffffu, in);
-        if (in) tl.lists[z * a.cap + base + __popc(m & ((1u << lane) - 1u))] = (uint16_t)q;
-        base += __popc(m);
-      }
-      if (lane == 0) tl.cnt[z] = base;
-    }
-    __syncwarp();
+    stage_tile<T>(a, tl, i, p0, np, lane, true);
     // ---- radial: lanes over pairs
     for (int q = lane; q < np; q += 32) {
       const uint32_t inf = tl.info[q];
       const int code = (int)(inf & 0xff);
       const bool self = (inf >> 8) & 1u;
+      if (self) continue;  // self images do not move relative to the centre
       const T r = tl.v[q].w;
       T dsum = 0;
       for (int g = 0; g < a.nrad; g++) {
         const GDesc d = a.rad[g];
-        if (d.chan1 >= 0 && code != d.chan1 && !self) continue;
+        if (d.chan1 >= 0 && code != d.chan1) continue;
         if (!((inf >> (16 + d.rclass)) & 1u)) continue;
         T fc = tl.fc[d.rclass * a.cap + q], dfc = tl.dfc[d.rclass * a.cap + q];
         if (d.atomid > 0) {
-          const T ids = aid<T>(a.ext, a.next, d.atomid, i) * aid<T>(a.ext, a.next, d.atomid, tl.pj[q]);
+          const T ids = atom_id<T>(a.ext, a.next, d.atomid, i) * atom_id<T>(a.ext, a.next, d.atomid, tl.pj[q]);
           fc *= ids;
           dfc *= ids;
         }
@@ -305,21 +201,44 @@ __global__ void __launch_bounds__(256) forces_kernel(ForceArgs<T> a) {
           dg = dfc;
         } else if (d.type == 2) {
           const T x = r - (T)d.rs;
-          dg = f_exp<T>(-((T)d.eta * (x * x))) * (dfc - (T)2 * (T)d.eta * x * fc);
+          dg = m_exp<T>(-((T)d.eta * (x * x))) * (dfc - (T)2 * (T)d.eta * x * fc);
         } else {
           const T kr = (T)d.kappa * r;
-          dg = f_cos<T>(kr) * dfc - (T)d.kappa * f_sin<T>(kr) * fc;
+          dg = m_cos<T>(kr) * dfc - (T)d.kappa * m_sin<T>(kr) * fc;
         }
         dsum += tl.jv[d.out] * dg;
       }
-      const V4<T> v = tl.v[q];
-      const T s = dsum / r;
-      tl.w[q].x += s * v.x;
-      tl.w[q].y += s * v.y;
-      tl.w[q].z += s * v.z;
+      const V4<T> u = tl.u[q];
+      tl.w[q].x += dsum * u.x;
+      tl.w[q].y += dsum * u.y;
+      tl.w[q].z += dsum * u.z;
+    }
+    // ---- integer-xi G5 through adjoint moments
+    if (D > 0 && a.ncombo > 0) {
+      compute_moments<T>(a, tl, np, lane);
+      const int items = a.ncombo * a.n_mono;
+      for (int it = lane; it < items; it += 32) {
+        const int k = it / a.n_mono, al = it % a.n_mono;
+        T acc = 0;
+        for (int f = 0; f < a.nmf; f++) {
+          const MFunc mf = a.mfunc[f];
+          if (mf.k1 != k && mf.k2 != k) continue;
+          const T cj = tl.jv[mf.out] * (T)a.mcoef[(int64_t)f * a.n_mono + al];
+          if (mf.k1 == k) acc += cj * tl.M[mf.k2 * a.n_mono + al];
+          if (mf.k2 == k) acc += cj * tl.M[mf.k1 * a.n_mono + al];
+        }
+        tl.Q[it] = acc;
+      }
+      __syncwarp();
+      for (int q = lane; q < np; q += 32) {
+        const uint32_t inf = tl.info[q];
+        if ((inf >> 8) & 1u) continue;
+        const int z = (int)(inf & 0xff);
+        moment_pair_force<T, (D > 0 ? D : 1)>(a, tl, q, z == 0xff ? -1 : z);
+      }
     }
     __syncwarp();
-    // ---- angular groups
+    // ---- remaining angular groups (triplet sweep)
     for (int gi = 0; gi < a.ngroups; gi++) {
       const AGroup G = a.groups[gi];
       __syncwarp();
@@ -335,7 +254,7 @@ __global__ void __launch_bounds__(256) forces_kernel(ForceArgs<T> a) {
         if (lane == 0) tl.gpar[128] = (T)d.rcut;
       }
       if (G.has_g4 && G.atomid > 0)
-        for (int q = lane; q < np; q += 32) tl.idv[q] = aid<T>(a.ext, a.next, G.atomid, tl.pj[q]);
+        for (int q = lane; q < np; q += 32) tl.idv[q] = atom_id<T>(a.ext, a.next, G.atomid, tl.pj[q]);
       __syncwarp();
       const uint16_t *l1 = G.chan1 >= 0 ? tl.lists + G.chan1 * a.cap : nullptr;
       const uint16_t *l2 = G.chan2 >= 0 ? tl.lists + G.chan2 * a.cap : nullptr;
@@ -380,23 +299,15 @@ __global__ void __launch_bounds__(256) forces_kernel(ForceArgs<T> a) {
   }
 }
 
-template <typename T> int launch_forces(fnetg_ctx *ctx) {
-  const int64_t N = ctx->N;
-  const int nout = ctx->dims.back();
-  const int nf = ctx->nf;
-  const int ng = (int)ctx->gf.size();
-  FNETG_CUDA(ctx->d_forces.ensure(sizeof(double) * std::max<int64_t>(N, 1) * nout * 3));
-  FNETG_CUDA(cudaMemsetAsync(ctx->d_forces.p, 0, sizeof(double) * std::max<int64_t>(N, 1) * nout * 3,
-                             ctx->stream));
-  FNETG_CUDA(ctx->d_jacT.ensure(sizeof(T) * std::max<int64_t>(N, 1) * nf));
-  if (N == 0) return FNETG_OK;
-  ForceArgs<T> a{};
-  a.natoms = N;
+template <typename T> void fill_tile_args_forces(fnetg_ctx *ctx, TileArgs<T> &a) {
+  a = TileArgs<T>{};
+  a.natoms = ctx->N;
   a.poff = ctx->d_poff.as<int64_t>();
   a.pj = ctx->d_pj.as<int32_t>();
   a.pmeta = ctx->d_pmeta.as<uint32_t>();
   a.rij = static_cast<const V4<T> *>(ctx->d_rij.p);
   a.code = ctx->d_code.as<int8_t>();
+  a.bpos = ctx->d_bpos.as<int32_t>();
   a.ext = ctx->d_ext.as<double>();
   a.next = ctx->next;
   a.rad = ctx->d_rad.as<GDesc>();
@@ -412,21 +323,29 @@ template <typename T> int launch_forces(fnetg_ctx *ctx) {
   a.nrcls = (int)ctx->rcut_classes.size();
   a.nz = (int)ctx->zcodes.size();
   a.cap = std::max(32, (ctx->max_pairs + 31) / 32 * 32);
-  a.ng = ng;
-  a.J = ctx->d_jacT.as<T>();
-  a.nf = nf;
-  a.F = ctx->d_forces.as<double>();
-  a.nout = nout;
-  const size_t tb = ftile_bytes<T>(a.cap, a.nrcls, a.necls, a.nz, ng);
+  a.mfunc = ctx->d_mfunc.as<MFunc>();
+  a.nmf = (int)ctx->h_mfunc.size();
+  a.mcoef = ctx->d_mcoef.as<double>();
+  a.combo = ctx->d_combo.as<int32_t>();
+  a.ncombo = ctx->n_combo;
+  a.cidx = ctx->d_cidx.as<int32_t>();
+  a.n_mono = ctx->n_mono;
+  a.nf = ctx->nf;
+  a.ng = (int)ctx->gf.size();
+}
+
+template <typename T, int D> int launch_forces_d(fnetg_ctx *ctx, TileArgs<T> &a, int nout) {
+  const int64_t N = ctx->N;
+  const size_t tb = tile_bytes<T>(a.cap, a.nrcls, a.necls, a.nz, a.ncombo, a.n_mono, a.ng, true);
   int wpb = 8;
-  while (wpb > 1 && tb * wpb > 200 * 1024) wpb >>= 1;
+  while (wpb > 1 && tb * wpb > 160 * 1024) wpb >>= 1;
   FNETG_CHECK(tb * wpb <= 227 * 1024, FNETG_E_UNSUPPORTED,
               "neighbour tile of one atom exceeds shared memory");
   const size_t smem = tb * wpb;
-  FNETG_CUDA(cudaFuncSetAttribute(forces_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  FNETG_CUDA(cudaFuncSetAttribute(forces_kernel<T, D>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)smem));
   int per_sm = 1;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, forces_kernel<T>, wpb * 32, smem);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, forces_kernel<T, D>, wpb * 32, smem);
   const int64_t want = (N + wpb - 1) / wpb;
   const int blocks = (int)std::max<int64_t>(
       1, std::min<int64_t>(want, (int64_t)num_sms() * std::max(per_sm, 1) * 8));
@@ -435,10 +354,33 @@ template <typename T> int launch_forces(fnetg_ctx *ctx) {
     if (rc) return rc;
     a.out_index = o;
     LaunchScope ls(ctx, "forces");
-    forces_kernel<T><<<blocks, wpb * 32, smem, ctx->stream>>>(a);
+    forces_kernel<T, D><<<blocks, wpb * 32, smem, ctx->stream>>>(a);
     FNETG_CUDA(cudaGetLastError());
   }
   return FNETG_OK;
+}
+
+template <typename T> int launch_forces(fnetg_ctx *ctx) {
+  const int64_t N = ctx->N;
+  const int nout = ctx->dims.back();
+  const int nf = ctx->nf;
+  FNETG_CUDA(ctx->d_forces.ensure(sizeof(double) * std::max<int64_t>(N, 1) * nout * 3));
+  FNETG_CUDA(cudaMemsetAsync(ctx->d_forces.p, 0, sizeof(double) * std::max<int64_t>(N, 1) * nout * 3,
+                             ctx->stream));
+  FNETG_CUDA(ctx->d_jacT.ensure(sizeof(T) * std::max<int64_t>(N, 1) * nf));
+  if (N == 0) return FNETG_OK;
+  TileArgs<T> a;
+  fill_tile_args_forces<T>(ctx, a);
+  a.J = ctx->d_jacT.as<T>();
+  a.F = ctx->d_forces.as<double>();
+  a.nout = nout;
+  switch (ctx->mom_degree) {
+    case 0: return launch_forces_d<T, 0>(ctx, a, nout);
+    case 1: return launch_forces_d<T, 1>(ctx, a, nout);
+    case 2: return launch_forces_d<T, 2>(ctx, a, nout);
+    case 3: return launch_forces_d<T, 3>(ctx, a, nout);
+    default: return launch_forces_d<T, 4>(ctx, a, nout);
+  }
 }
 
 }  // namespace

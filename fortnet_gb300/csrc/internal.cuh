@@ -47,6 +47,16 @@ struct AGroup {
   int atomid;        // shared by every function of the group (0 = none)
 };
 
+// Angular G5 function with an integer xi <= kMaxMomentDegree, evaluated through moment tensors:
+// sum_{j,k} (1 + lambda u_j.u_k)^xi E_j E_k = sum_alpha coef(alpha) M1(alpha) M2(alpha).
+constexpr int kMaxMomentDegree = 4;
+constexpr int kMaxMono = 35;  // monomials of degree <= 4 in three variables
+struct MFunc {
+  int k1, k2;  // moment combos (list, eta class) of the two neighbour lists
+  int out;     // output column
+  int pad;
+};
+
 // Device buffer with grow-only reallocation.
 struct DBuf {
   void *p = nullptr;
@@ -114,6 +124,13 @@ struct fnetg_ctx {
   std::vector<double> ecls_eta;
   std::vector<int> ecls_rclass, ecls_atomid;
   std::vector<int32_t> zcodes;  // atomic numbers of species codes
+  // moment form of the integer-xi G5 functions
+  int mom_degree = 0, n_mono = 0, n_combo = 0;
+  std::vector<fnetg::MFunc> h_mfunc;
+  std::vector<double> h_mcoef;      // [nmf][n_mono]
+  std::vector<int32_t> h_combo;     // [ncombo][2] (list code or -1 = all, eta class)
+  std::vector<int32_t> h_cidx;      // [(nz+1) * necls] combo index, -1 if unused
+  fnetg::DBuf d_mfunc, d_mcoef, d_combo, d_cidx;
   fnetg::DBuf d_rad, d_ang, d_groups, d_code, d_ecls_eta, d_ecls_rclass, d_ecls_atomid,
       d_rcls;
 
@@ -122,7 +139,9 @@ struct fnetg_ctx {
   double nb_rcut = 0.0;
   int64_t P = 0;
   int max_pairs = 0;
-  fnetg::DBuf d_pcount, d_poff, d_pj, d_pmeta, d_rij, d_d2, d_scan_tmp, d_maxp;
+  bool d2_valid = false;
+  double max_extent = 0.0;  // largest structure bounding-box extent (Bohr)
+  fnetg::DBuf d_pcount, d_poff, d_pj, d_pmeta, d_rij, d_d2, d_scan_tmp, d_maxp, d_rcls2;
 
   // features (bucketed rows, compute precision)
   int nf = 0;
@@ -199,6 +218,8 @@ void resolve_profile(fnetg_ctx *c);
 
 // kernels' host entry points (one per translation unit)
 int run_neighbors(fnetg_ctx *ctx, double rcut);
+int prepare_coords(fnetg_ctx *ctx);
+int pair_d2(fnetg_ctx *ctx);
 int run_acsf(fnetg_ctx *ctx);
 int run_zscore(fnetg_ctx *ctx, const int32_t *weights, bool compute);
 int run_ext_inputs(fnetg_ctx *ctx);

@@ -28,132 +28,193 @@ struct NbArgs {
   const double *lat;
   const int32_t *ranges;  // [S*6] lo0,hi0,lo1,hi1,lo2,hi2 (periodic) — zeros otherwise
   const int32_t *periodic;
-  const float *bbox;      // [S*6] lo, hi
+  const float *bbox;      // [S*6] lo, hi (relative frame)
   int64_t natoms;
   double rc2;             // rcut*rcut (exact decision)
-  float rc2_filter;       // generous float bound for the pre-filter
-  float rc_filter;
+  float rc2_lo, rc2_hi;   // float distances below / above are decided without FP64
   const double *rcls;     // cutoff classes (ascending)
+  const float *rcls2_lo, *rcls2_hi;
   int nrcls;
+  int exact_geometry;     // FP64 displacement / distance for every accepted pair
   // fill pass
   const int64_t *poff;
   int64_t *count;
   int32_t *pj;
   uint32_t *pmeta;
   void *rij;              // V4<T>
-  double *d2out;
+  double *d2out;          // optional
   int *maxp;
 };
 
 __device__ __forceinline__ double exact_d2(const double *ci, const double *cj, const double *cv,
                                            double *d) {
-  double nc0 = __dadd_rn(cj[0], cv[0]);
-  double nc1 = __dadd_rn(cj[1], cv[1]);
-  double nc2 = __dadd_rn(cj[2], cv[2]);
-  d[0] = __dsub_rn(nc0, ci[0]);  // neighbour - centre (sign irrelevant for d2)
+  // the reference's arithmetic: nc = c_j + cellVec, d2 = sum((c_i - nc)**2) in index order
+  const double nc0 = __dadd_rn(cj[0], cv[0]);
+  const double nc1 = __dadd_rn(cj[1], cv[1]);
+  const double nc2 = __dadd_rn(cj[2], cv[2]);
+  d[0] = __dsub_rn(nc0, ci[0]);  // neighbour - centre; (c_i - nc)^2 == (nc - c_i)^2 exactly
   d[1] = __dsub_rn(nc1, ci[1]);
   d[2] = __dsub_rn(nc2, ci[2]);
-  double e0 = __dsub_rn(ci[0], nc0), e1 = __dsub_rn(ci[1], nc1), e2 = __dsub_rn(ci[2], nc2);
-  double s = __dmul_rn(e0, e0);
-  s = __dadd_rn(s, __dmul_rn(e1, e1));
-  s = __dadd_rn(s, __dmul_rn(e2, e2));
+  double s = __dmul_rn(d[0], d[0]);
+  s = __dadd_rn(s, __dmul_rn(d[1], d[1]));
+  s = __dadd_rn(s, __dmul_rn(d[2], d[2]));
   return s;
+}
+
+__device__ __forceinline__ void cell_vector(const double *L, int n1, int n2, int n3, double *cv) {
+  // matmul(latVecs, n) summed in index order
+  for (int c = 0; c < 3; c++) {
+    double v = __dmul_rn(L[c + 0], (double)n1);
+    v = __dadd_rn(v, __dmul_rn(L[c + 3], (double)n2));
+    v = __dadd_rn(v, __dmul_rn(L[c + 6], (double)n3));
+    cv[c] = v;
+  }
 }
 
 template <typename T, bool kFill>
 __global__ void __launch_bounds__(256) nb_kernel(NbArgs a) {
+  __shared__ int blk_max;
+  if (threadIdx.x == 0) blk_max = 0;
+  __syncthreads();
   const int lane = threadIdx.x & 31;
   const int64_t i = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-  if (i >= a.natoms) return;
-  const int s = a.astruct[i];
-  const int64_t a0 = a.off[s];
-  const int n = (int)(a.off[s + 1] - a0);
-  const int il = (int)(i - a0);
-  double ci[3] = {a.coords[3 * i], a.coords[3 * i + 1], a.coords[3 * i + 2]};
-  const V4<float> cif = a.cf[i];
-  int64_t wpos = 0;
-  if (kFill) wpos = a.poff[i];
-  int64_t cnt = 0;
-  const bool per = a.periodic[s] != 0;
-  int lo0 = 0, hi0 = 0, lo1 = 0, hi1 = 0, lo2 = 0, hi2 = 0;
-  if (per) {
-    lo0 = a.ranges[6 * s + 0]; hi0 = a.ranges[6 * s + 1];
-    lo1 = a.ranges[6 * s + 2]; hi1 = a.ranges[6 * s + 3];
-    lo2 = a.ranges[6 * s + 4]; hi2 = a.ranges[6 * s + 5];
-  }
-  const double *L = a.lat + 9 * s;
-  const float *bb = a.bbox + 6 * s;
-  // image index -1 is the central cell
-  const int n1span = hi0 - lo0 + 1, n2span = hi1 - lo1 + 1, n3span = hi2 - lo2 + 1;
-  const int nimg = per ? n1span * n2span * n3span : 0;
-  for (int img = -1; img < nimg; img++) {
-    int n1 = 0, n2 = 0, n3 = 0;
-    double cv[3] = {0.0, 0.0, 0.0};
-    int tstart = 1, tcount = n - 1;
-    if (img >= 0) {
-      n1 = lo0 + img / (n2span * n3span);
-      n2 = lo1 + (img / n3span) % n2span;
-      n3 = lo2 + img % n3span;
-      if (n1 == 0 && n2 == 0 && n3 == 0) continue;
-      for (int c = 0; c < 3; c++) {
-        double v = __dmul_rn(L[c + 0], (double)n1);
-        v = __dadd_rn(v, __dmul_rn(L[c + 3], (double)n2));
-        v = __dadd_rn(v, __dmul_rn(L[c + 6], (double)n3));
-        cv[c] = v;
-      }
-      tstart = 0;
-      tcount = n;
-      // prune the whole image when the shifted bounding box is out of reach
-      float dd = 0.f;
-      const float cvf[3] = {(float)cv[0], (float)cv[1], (float)cv[2]};
-      const float p[3] = {cif.x, cif.y, cif.z};
-      for (int c = 0; c < 3; c++) {
-        float lo = bb[c] + cvf[c], hi = bb[3 + c] + cvf[c];
-        float e = p[c] < lo ? lo - p[c] : (p[c] > hi ? p[c] - hi : 0.f);
-        dd += e * e;
-      }
-      if (dd > a.rc2_filter) continue;
+  if (i < a.natoms) {
+    const int s = a.astruct[i];
+    const int64_t a0 = a.off[s];
+    const int n = (int)(a.off[s + 1] - a0);
+    const int il = (int)(i - a0);
+    const double ci[3] = {a.coords[3 * i], a.coords[3 * i + 1], a.coords[3 * i + 2]};
+    const V4<float> cif = a.cf[i];
+    int64_t wpos = 0;
+    if (kFill) wpos = a.poff[i];
+    int64_t cnt = 0;
+    const bool per = a.periodic[s] != 0;
+    int lo0 = 0, hi0 = 0, lo1 = 0, hi1 = 0, lo2 = 0, hi2 = 0;
+    if (per) {
+      lo0 = a.ranges[6 * s + 0]; hi0 = a.ranges[6 * s + 1];
+      lo1 = a.ranges[6 * s + 2]; hi1 = a.ranges[6 * s + 3];
+      lo2 = a.ranges[6 * s + 4]; hi2 = a.ranges[6 * s + 5];
     }
-    const float cvf0 = (float)cv[0], cvf1 = (float)cv[1], cvf2 = (float)cv[2];
-    for (int base = 0; base < tcount; base += 32) {
-      const int t = tstart + base + lane;
-      bool ok = false;
-      double d[3] = {0, 0, 0}, dist2 = 0.0;
-      int64_t j = 0;
-      if (base + lane < tcount) {
-        j = a0 + (il + t) % n;
-        const V4<float> cjf = a.cf[j];
-        float e0 = cif.x - (cjf.x + cvf0), e1 = cif.y - (cjf.y + cvf1), e2 = cif.z - (cjf.z + cvf2);
-        float df = e0 * e0 + e1 * e1 + e2 * e2;
-        if (df <= a.rc2_filter) {
-          double cj[3] = {a.coords[3 * j], a.coords[3 * j + 1], a.coords[3 * j + 2]};
-          dist2 = exact_d2(ci, cj, cv, d);
-          ok = dist2 <= a.rc2;
+    const double *L = a.lat + 9 * s;
+    const float *bb = a.bbox + 6 * s;
+    const int n2span = hi1 - lo1 + 1, n3span = hi2 - lo2 + 1;
+    const int nimg = per ? (hi0 - lo0 + 1) * n2span * n3span : 0;
+    // image -1 is the central cell, then lattice points n1 outer .. n3 inner
+    for (int img = -1; img < nimg; img++) {
+      int n1 = 0, n2 = 0, n3 = 0;
+      double cv[3] = {0.0, 0.0, 0.0};
+      int tstart = 1, tcount = n - 1;
+      if (img >= 0) {
+        n1 = lo0 + img / (n2span * n3span);
+        n2 = lo1 + (img / n3span) % n2span;
+        n3 = lo2 + img % n3span;
+        if (n1 == 0 && n2 == 0 && n3 == 0) continue;
+        cell_vector(L, n1, n2, n3, cv);
+        tstart = 0;
+        tcount = n;
+        // skip the image when the shifted bounding box is out of reach
+        float dd = 0.f;
+        const float cvf[3] = {(float)cv[0], (float)cv[1], (float)cv[2]};
+        const float p[3] = {cif.x, cif.y, cif.z};
+        for (int c = 0; c < 3; c++) {
+          const float lo = bb[c] + cvf[c], hi = bb[3 + c] + cvf[c];
+          const float e = p[c] < lo ? lo - p[c] : (p[c] > hi ? p[c] - hi : 0.f);
+          dd += e * e;
         }
+        if (dd > a.rc2_hi) continue;
       }
-      const unsigned m = __ballot_sync(0xffffffffu, ok);
-      if (kFill && ok) {
-        const int64_t q = wpos + cnt + __popc(m & ((1u << lane) - 1u));
-        a.pj[q] = (int32_t)j;
-        uint32_t mask = 0;
-        for (int c = 0; c < a.nrcls; c++)
-          if (dist2 <= __dmul_rn(a.rcls[c], a.rcls[c])) mask |= 1u << c;
-        a.pmeta[q] = ((uint32_t)(uint8_t)(int8_t)n1) | ((uint32_t)(uint8_t)(int8_t)n2 << 8) |
-                     ((uint32_t)(uint8_t)(int8_t)n3 << 16) | (mask << 24);
-        V4<T> v;
-        v.x = (T)d[0];
-        v.y = (T)d[1];
-        v.z = (T)d[2];
-        v.w = (T)sqrt(dist2);
-        reinterpret_cast<V4<T> *>(a.rij)[q] = v;
-        a.d2out[q] = dist2;
+      const float cvf0 = (float)cv[0], cvf1 = (float)cv[1], cvf2 = (float)cv[2];
+      for (int base = 0; base < tcount; base += 32) {
+        bool ok = false;
+        int jl = 0;
+        float df = 0.f;
+        if (base + lane < tcount) {
+          jl = il + tstart + base + lane;
+          if (jl >= n) jl -= n;
+          const V4<float> cjf = a.cf[a0 + jl];
+          const float e0 = (cjf.x + cvf0) - cif.x, e1 = (cjf.y + cvf1) - cif.y,
+                      e2 = (cjf.z + cvf2) - cif.z;
+          df = e0 * e0 + e1 * e1 + e2 * e2;
+          if (df <= a.rc2_lo) {
+            ok = true;
+          } else if (df <= a.rc2_hi) {
+            // within the float error bound of the cutoff: the reference's FP64 decision
+            const int64_t j = a0 + jl;
+            const double cj[3] = {a.coords[3 * j], a.coords[3 * j + 1], a.coords[3 * j + 2]};
+            double d[3];
+            ok = exact_d2(ci, cj, cv, d) <= a.rc2;
+          }
+        }
+        const unsigned m = __ballot_sync(0xffffffffu, ok);
+        if (kFill && ok) {
+          const int64_t j = a0 + jl;
+          const int64_t q = wpos + cnt + __popc(m & ((1u << lane) - 1u));
+          a.pj[q] = (int32_t)j;
+          const double cj[3] = {a.coords[3 * j], a.coords[3 * j + 1], a.coords[3 * j + 2]};
+          double d[3];
+          uint32_t mask = 0;
+          V4<T> v;
+          if (a.exact_geometry || a.d2out) {
+            const double dist2 = exact_d2(ci, cj, cv, d);
+            for (int c = 0; c < a.nrcls; c++)
+              if (dist2 <= __dmul_rn(a.rcls[c], a.rcls[c])) mask |= 1u << c;
+            if (a.d2out) a.d2out[q] = dist2;
+            v.w = (T)sqrt(dist2);
+          } else {
+            // displacement from the FP64 coordinates (accurate), distance in float
+            d[0] = (cj[0] + cv[0]) - ci[0];
+            d[1] = (cj[1] + cv[1]) - ci[1];
+            d[2] = (cj[2] + cv[2]) - ci[2];
+            const float fx = (float)d[0], fy = (float)d[1], fz = (float)d[2];
+            v.w = (T)sqrtf(fx * fx + fy * fy + fz * fz);
+            for (int c = 0; c < a.nrcls; c++) {
+              if (df <= a.rcls2_lo[c]) {
+                mask |= 1u << c;
+              } else if (df <= a.rcls2_hi[c]) {
+                double e[3];
+                if (exact_d2(ci, cj, cv, e) <= __dmul_rn(a.rcls[c], a.rcls[c])) mask |= 1u << c;
+              }
+            }
+          }
+          a.pmeta[q] = ((uint32_t)(uint8_t)(int8_t)n1) | ((uint32_t)(uint8_t)(int8_t)n2 << 8) |
+                       ((uint32_t)(uint8_t)(int8_t)n3 << 16) | (mask << 24);
+          v.x = (T)d[0];
+          v.y = (T)d[1];
+          v.z = (T)d[2];
+          reinterpret_cast<V4<T> *>(a.rij)[q] = v;
+        }
+        cnt += __popc(m);
       }
-      cnt += __popc(m);
+    }
+    if (!kFill && lane == 0) {
+      a.count[i] = cnt;
+      atomicMax(&blk_max, (int)cnt);
     }
   }
-  if (!kFill && lane == 0) {
-    a.count[i] = cnt;
-    atomicMax(a.maxp, (int)cnt);
+  if (!kFill) {
+    __syncthreads();
+    if (threadIdx.x == 0) atomicMax(a.maxp, blk_max);
+  }
+}
+
+// exact squared distances of every stored pair (parity downloads only)
+__global__ void pair_d2_kernel(const int64_t *poff, const int32_t *pj, const uint32_t *pmeta,
+                               const int32_t *astruct, const double *coords, const double *lat,
+                               int64_t natoms, double *d2out) {
+  const int lane = threadIdx.x & 31;
+  const int64_t i = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (i >= natoms) return;
+  const double ci[3] = {coords[3 * i], coords[3 * i + 1], coords[3 * i + 2]};
+  const double *L = lat + 9 * astruct[i];
+  for (int64_t q = poff[i] + lane; q < poff[i + 1]; q += 32) {
+    const uint32_t m = pmeta[q];
+    const int n1 = (int8_t)(m & 0xff), n2 = (int8_t)((m >> 8) & 0xff), n3 = (int8_t)((m >> 16) & 0xff);
+    double cv[3] = {0.0, 0.0, 0.0};
+    if (n1 || n2 || n3) cell_vector(L, n1, n2, n3, cv);
+    const int64_t j = pj[q];
+    const double cj[3] = {coords[3 * j], coords[3 * j + 1], coords[3 * j + 2]};
+    double d[3];
+    d2out[q] = exact_d2(ci, cj, cv, d);
   }
 }
 
@@ -206,7 +267,56 @@ __global__ void scan_add_kernel(int64_t *out, const int64_t *sums, int64_t n, in
   if (g == 0) out[n] = *total;
 }
 
+// Float copies of the coordinates relative to each structure's bounding-box corner (the float
+// pre-filter's rounding then does not depend on where a structure sits) and the boxes.
+__global__ void prep_coords_kernel(const double *coords, const int64_t *off, V4<float> *cf,
+                                   float *bbox, int S) {
+  __shared__ double lo[3][256], hi[3][256];
+  const int s = blockIdx.x;
+  if (s >= S) return;
+  const int64_t a0 = off[s], a1 = off[s + 1];
+  double l[3] = {1e300, 1e300, 1e300}, h[3] = {-1e300, -1e300, -1e300};
+  for (int64_t a = a0 + threadIdx.x; a < a1; a += blockDim.x)
+    for (int c = 0; c < 3; c++) {
+      l[c] = fmin(l[c], coords[3 * a + c]);
+      h[c] = fmax(h[c], coords[3 * a + c]);
+    }
+  for (int c = 0; c < 3; c++) {
+    lo[c][threadIdx.x] = l[c];
+    hi[c][threadIdx.x] = h[c];
+  }
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o)
+      for (int c = 0; c < 3; c++) {
+        lo[c][threadIdx.x] = fmin(lo[c][threadIdx.x], lo[c][threadIdx.x + o]);
+        hi[c][threadIdx.x] = fmax(hi[c][threadIdx.x], hi[c][threadIdx.x + o]);
+      }
+    __syncthreads();
+  }
+  double ref[3];
+  for (int c = 0; c < 3; c++) ref[c] = (double)(float)lo[c][0];
+  for (int64_t a = a0 + threadIdx.x; a < a1; a += blockDim.x)
+    cf[a] = V4<float>{(float)(coords[3 * a] - ref[0]), (float)(coords[3 * a + 1] - ref[1]),
+                      (float)(coords[3 * a + 2] - ref[2]), 0.f};
+  if (threadIdx.x == 0)
+    for (int c = 0; c < 3; c++) {
+      bbox[6 * s + c] = 0.f;
+      bbox[6 * s + 3 + c] = (float)(hi[c][0] - ref[c]);
+    }
+}
+
 }  // namespace
+
+int prepare_coords(fnetg_ctx *ctx) {
+  if (ctx->S == 0) return FNETG_OK;
+  LaunchScope ls(ctx, "coords");
+  prep_coords_kernel<<<ctx->S, 256, 0, ctx->stream>>>(
+      ctx->d_coords.as<double>(), ctx->d_off.as<int64_t>(), ctx->d_coordsf.as<V4<float>>(),
+      ctx->d_bbox.as<float>(), ctx->S);
+  FNETG_CUDA(cudaGetLastError());
+  return FNETG_OK;
+}
 
 // out has n+1 entries (out[n] = total)
 int exclusive_scan_i64(fnetg_ctx *ctx, const int64_t *in, int64_t *out, int64_t n) {
@@ -267,12 +377,42 @@ int run_neighbors(fnetg_ctx *ctx, double rcut) {
   a.bbox = ctx->d_bbox.as<float>();
   a.natoms = N;
   a.rc2 = rcut * rcut;
-  // float pre-filter bound: generous relative and absolute margins over the exact bound
-  const double rcf = rcut * (1.0 + 1e-4) + 1e-3;
-  a.rc2_filter = (float)(rcf * rcf);
-  a.rc_filter = (float)rcf;
+  // Float error bound of the pre-filter: coordinates relative to each structure's box corner
+  // are at most `reach` in magnitude (box extent plus the farthest image translation); each of
+  // the few float roundings of a component difference is below 2^-23 * reach, so the squared
+  // distance is off by less than 8 * 2^-23 * reach * rcut + 2^-20 * rcut^2.
+  double reach = 0.0;
+  for (int s = 0; s < S; s++) {
+    double shift = 0.0;
+    if (ctx->h_periodic[s]) {
+      for (int k = 0; k < 3; k++) {
+        const double *col = ctx->h_lat.data() + 9 * s + 3 * k;
+        const double len = std::sqrt(col[0] * col[0] + col[1] * col[1] + col[2] * col[2]);
+        const int nmax = std::max(std::abs(ranges[6 * s + 2 * k]), std::abs(ranges[6 * s + 2 * k + 1]));
+        shift += len * nmax;
+      }
+    }
+    reach = std::max(reach, shift);
+  }
+  reach += ctx->max_extent + rcut;
+  auto margin = [&](double rc) { return 16.0 * 1.2e-7 * reach * rc + 1e-6 * rc * rc + 1e-6; };
+  a.rc2_lo = (float)(rcut * rcut - margin(rcut));
+  a.rc2_hi = (float)(rcut * rcut + margin(rcut));
+  std::vector<float> rlo(kMaxRcutClasses, 0.f), rhi(kMaxRcutClasses, 0.f);
+  for (size_t c = 0; c < rcls.size(); c++) {
+    rlo[c] = (float)(rcls[c] * rcls[c] - margin(rcls[c]));
+    rhi[c] = (float)(rcls[c] * rcls[c] + margin(rcls[c]));
+  }
+  FNETG_CUDA(ctx->d_rcls2.ensure(sizeof(float) * 2 * kMaxRcutClasses));
+  FNETG_CUDA(cudaMemcpyAsync(ctx->d_rcls2.p, rlo.data(), sizeof(float) * kMaxRcutClasses,
+                             cudaMemcpyHostToDevice, ctx->stream));
+  FNETG_CUDA(cudaMemcpyAsync(ctx->d_rcls2.as<float>() + kMaxRcutClasses, rhi.data(),
+                             sizeof(float) * kMaxRcutClasses, cudaMemcpyHostToDevice, ctx->stream));
   a.rcls = ctx->d_rcls.as<double>();
+  a.rcls2_lo = ctx->d_rcls2.as<float>();
+  a.rcls2_hi = ctx->d_rcls2.as<float>() + kMaxRcutClasses;
   a.nrcls = (int)rcls.size();
+  a.exact_geometry = ctx->prec == FNETG_FP64 ? 1 : 0;
   a.count = ctx->d_pcount.as<int64_t>();
   a.maxp = ctx->d_maxp.as<int>();
   const int threads = 256, wpb = threads / 32;
@@ -299,12 +439,11 @@ int run_neighbors(fnetg_ctx *ctx, double rcut) {
   FNETG_CUDA(ctx->d_pj.ensure(sizeof(int32_t) * std::max<int64_t>(P, 1)));
   FNETG_CUDA(ctx->d_pmeta.ensure(sizeof(uint32_t) * std::max<int64_t>(P, 1)));
   FNETG_CUDA(ctx->d_rij.ensure(4 * es * std::max<int64_t>(P, 1)));
-  FNETG_CUDA(ctx->d_d2.ensure(sizeof(double) * std::max<int64_t>(P, 1)));
   a.poff = ctx->d_poff.as<int64_t>();
   a.pj = ctx->d_pj.as<int32_t>();
   a.pmeta = ctx->d_pmeta.as<uint32_t>();
   a.rij = ctx->d_rij.p;
-  a.d2out = ctx->d_d2.as<double>();
+  a.d2out = nullptr;
   if (N > 0 && P > 0) {
     LaunchScope ls(ctx, "neighbors");
     if (ctx->prec == FNETG_FP64)
@@ -314,10 +453,26 @@ int run_neighbors(fnetg_ctx *ctx, double rcut) {
     FNETG_CUDA(cudaGetLastError());
   }
   ctx->P = P;
+  ctx->d2_valid = false;
   ctx->max_pairs = maxp;
   ctx->nb_rcut = rcut;
   ctx->nb_valid = true;
   ctx->feats_valid = false;
+  return FNETG_OK;
+}
+
+int pair_d2(fnetg_ctx *ctx) {
+  if (ctx->d2_valid) return FNETG_OK;
+  FNETG_CUDA(ctx->d_d2.ensure(sizeof(double) * std::max<int64_t>(ctx->P, 1)));
+  if (ctx->N > 0 && ctx->P > 0) {
+    LaunchScope ls(ctx, "neighbors");
+    pair_d2_kernel<<<ceil_div(ctx->N, 8), 256, 0, ctx->stream>>>(
+        ctx->d_poff.as<int64_t>(), ctx->d_pj.as<int32_t>(), ctx->d_pmeta.as<uint32_t>(),
+        ctx->d_atom_struct.as<int32_t>(), ctx->d_coords.as<double>(), ctx->d_lat.as<double>(),
+        ctx->N, ctx->d_d2.as<double>());
+    FNETG_CUDA(cudaGetLastError());
+  }
+  ctx->d2_valid = true;
   return FNETG_OK;
 }
 

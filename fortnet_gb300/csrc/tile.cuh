@@ -1,0 +1,272 @@
+// Per-atom neighbour tile shared by the ACSF value and force kernels.
+//
+// One warp owns one centre atom.  Its neighbour images are staged in shared memory once:
+// displacement and distance, unit vector, neighbour index, species code / self-image flag /
+// cutoff-class mask, the cutoff functions of every cutoff class and, per angular eta class,
+// E(r) = exp(-eta r^2) fc(r) [id_i id_j] and (forces) dE/dr.  The per-species lists of
+// buildGFunctionNeighborlists (lib_descriptors/acsf.F90:943-1066) become ordered index lists
+// over the tile — the centre atom's periodic self-images belong to every species list, as in
+// the reference's species-reduced geometries.  Moments M_k(alpha) = sum_{j in list} E_j u_j^alpha
+// of every (list, eta class) combo feed the integer-xi G5 functions.
+#pragma once
+
+#include "internal.cuh"
+
+namespace fnetg {
+
+constexpr double kPi = 3.14159265358979323846;  // lib_dftbp/constants.F90:15
+
+// monomial exponents (x, y, z), ordered by degree then descending x and y exponents
+__device__ constexpr int kMonoTab[kMaxMono][3] = {
+    {0, 0, 0}, {1, 0, 0}, {0, 1, 0}, {0, 0, 1}, {2, 0, 0}, {1, 1, 0}, {1, 0, 1}, {0, 2, 0},
+    {0, 1, 1}, {0, 0, 2}, {3, 0, 0}, {2, 1, 0}, {2, 0, 1}, {1, 2, 0}, {1, 1, 1}, {1, 0, 2},
+    {0, 3, 0}, {0, 2, 1}, {0, 1, 2}, {0, 0, 3}, {4, 0, 0}, {3, 1, 0}, {3, 0, 1}, {2, 2, 0},
+    {2, 1, 1}, {2, 0, 2}, {1, 3, 0}, {1, 2, 1}, {1, 1, 2}, {1, 0, 3}, {0, 4, 0}, {0, 3, 1},
+    {0, 2, 2}, {0, 1, 3}, {0, 0, 4}};
+
+__host__ __device__ constexpr int n_mono_of(int D) { return (D + 1) * (D + 2) * (D + 3) / 6; }
+
+template <typename T> __device__ __forceinline__ T m_exp(T x);
+template <> __device__ __forceinline__ float m_exp<float>(float x) { return expf(x); }
+template <> __device__ __forceinline__ double m_exp<double>(double x) { return exp(x); }
+template <typename T> __device__ __forceinline__ T m_cos(T x);
+template <> __device__ __forceinline__ float m_cos<float>(float x) { return cosf(x); }
+template <> __device__ __forceinline__ double m_cos<double>(double x) { return cos(x); }
+template <typename T> __device__ __forceinline__ T m_sin(T x);
+template <> __device__ __forceinline__ float m_sin<float>(float x) { return sinf(x); }
+template <> __device__ __forceinline__ double m_sin<double>(double x) { return sin(x); }
+template <typename T> __device__ __forceinline__ T m_pow(T b, T e);
+template <> __device__ __forceinline__ float m_pow<float>(float b, float e) { return powf(b, e); }
+template <> __device__ __forceinline__ double m_pow<double>(double b, double e) { return pow(b, e); }
+template <typename T> __device__ __forceinline__ T m_sqrt(T x);
+template <> __device__ __forceinline__ float m_sqrt<float>(float x) { return sqrtf(x); }
+template <> __device__ __forceinline__ double m_sqrt<double>(double x) { return sqrt(x); }
+
+template <typename T> __device__ __forceinline__ T warp_sum(T v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+template <typename T>
+__device__ __forceinline__ T atom_id(const double *ext, int next, int atomid, int64_t a) {
+  return atomid > 0 ? (T)ext[a * next + (atomid - 1)] : (T)1;
+}
+
+// base^n for a small positive integer n (exact repeated multiplication), else pow(base, e)
+template <typename T> __device__ __forceinline__ T int_pow(T base, int n, T e) {
+  if (n > 0) {
+    T r = base;
+    for (int k = 1; k < n; k++) r *= base;
+    return r;
+  }
+  return m_pow<T>(base, e);
+}
+
+// Everything the per-atom kernels read (one struct for both kernels).
+template <typename T> struct TileArgs {
+  int64_t natoms;
+  const int64_t *poff;
+  const int32_t *pj;
+  const uint32_t *pmeta;
+  const V4<T> *rij;
+  const int8_t *code;
+  const int32_t *bpos;
+  const double *ext;
+  int next;
+  const GDesc *rad;
+  int nrad;
+  const GDesc *ang;       // triplet-sweep functions
+  const AGroup *groups;
+  int ngroups;
+  const double *ecls_eta;
+  const int *ecls_rclass;
+  const int *ecls_atomid;
+  int necls;
+  const double *rcls;
+  int nrcls;
+  int nz;
+  int cap;
+  // moment form
+  const MFunc *mfunc;
+  int nmf;
+  const double *mcoef;    // [nmf][n_mono]
+  const int32_t *combo;   // [ncombo][2]
+  int ncombo;
+  const int32_t *cidx;    // [(nz+1)*necls]
+  int n_mono;
+  // values
+  T *feat;
+  int nf;
+  // forces
+  int ng;
+  const T *J;
+  double *F;
+  int out_index, nout;
+};
+
+template <typename T> struct Tile {
+  V4<T> *v;         // dx, dy, dz, r (neighbour minus centre)
+  V4<T> *u;         // unit vector, r
+  V4<T> *w;         // pair force accumulators (forces kernel only)
+  T *fc, *dfc;      // [nrcls][cap]
+  T *E, *D;         // [necls][cap]
+  uint32_t *info;   // code | self << 8 | rmask << 16
+  int32_t *pj;
+  T *idv;           // [cap] atom ids of a group's column
+  T *gpar;          // [5][32]
+  int *gint;        // [3][32]
+  int *cnt;         // [8]
+  T *M;             // [ncombo][n_mono] moments
+  T *Q;             // [ncombo][n_mono] adjoint moments (forces)
+  T *jv;            // [ng] dE/dG of the centre atom (forces)
+  uint16_t *lists;  // [nz][cap]
+};
+
+template <typename T>
+__host__ __device__ inline size_t tile_bytes(int cap, int nrcls, int necls, int nz, int ncombo,
+                                             int nmono, int ng, bool forces) {
+  size_t b = 0;
+  b += sizeof(V4<T>) * cap * (forces ? 3 : 2);
+  b += sizeof(T) * (size_t)cap * (nrcls + necls) * (forces ? 2 : 1);
+  b += sizeof(T) * cap;                       // idv
+  b += sizeof(T) * 5 * 32;                    // gpar
+  b += sizeof(T) * (size_t)ncombo * nmono * (forces ? 2 : 1);
+  b += forces ? sizeof(T) * ng : 0;
+  b = (b + 7) / 8 * 8;
+  b += sizeof(uint32_t) * cap + sizeof(int32_t) * cap;
+  b += sizeof(int) * (3 * 32 + 8);
+  b += sizeof(uint16_t) * (size_t)cap * nz;
+  return (b + 127) / 128 * 128;
+}
+
+template <typename T>
+__device__ Tile<T> carve_tile(unsigned char *p, const TileArgs<T> &a, bool forces) {
+  Tile<T> t;
+  const int cap = a.cap;
+  t.v = reinterpret_cast<V4<T> *>(p);
+  p += sizeof(V4<T>) * cap;
+  t.u = reinterpret_cast<V4<T> *>(p);
+  p += sizeof(V4<T>) * cap;
+  t.w = nullptr;
+  if (forces) {
+    t.w = reinterpret_cast<V4<T> *>(p);
+    p += sizeof(V4<T>) * cap;
+  }
+  t.fc = reinterpret_cast<T *>(p);
+  p += sizeof(T) * (size_t)cap * a.nrcls;
+  t.E = reinterpret_cast<T *>(p);
+  p += sizeof(T) * (size_t)cap * a.necls;
+  t.dfc = t.D = nullptr;
+  if (forces) {
+    t.dfc = reinterpret_cast<T *>(p);
+    p += sizeof(T) * (size_t)cap * a.nrcls;
+    t.D = reinterpret_cast<T *>(p);
+    p += sizeof(T) * (size_t)cap * a.necls;
+  }
+  t.idv = reinterpret_cast<T *>(p);
+  p += sizeof(T) * cap;
+  t.gpar = reinterpret_cast<T *>(p);
+  p += sizeof(T) * 5 * 32;
+  t.M = reinterpret_cast<T *>(p);
+  p += sizeof(T) * (size_t)a.ncombo * a.n_mono;
+  t.Q = t.jv = nullptr;
+  if (forces) {
+    t.Q = reinterpret_cast<T *>(p);
+    p += sizeof(T) * (size_t)a.ncombo * a.n_mono;
+    t.jv = reinterpret_cast<T *>(p);
+    p += sizeof(T) * a.ng;
+  }
+  p = reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(p) + 7) & ~uintptr_t(7));
+  t.info = reinterpret_cast<uint32_t *>(p);
+  p += sizeof(uint32_t) * cap;
+  t.pj = reinterpret_cast<int32_t *>(p);
+  p += sizeof(int32_t) * cap;
+  t.gint = reinterpret_cast<int *>(p);
+  p += sizeof(int) * 3 * 32;
+  t.cnt = reinterpret_cast<int *>(p);
+  p += sizeof(int) * 8;
+  t.lists = reinterpret_cast<uint16_t *>(p);
+  return t;
+}
+
+// Stage the pair tile of atom i (all lanes), build the ordered species lists.
+template <typename T>
+__device__ void stage_tile(const TileArgs<T> &a, Tile<T> &t, int64_t i, int64_t p0, int np,
+                           int lane, bool forces) {
+  for (int q = lane; q < np; q += 32) {
+    const V4<T> v = a.rij[p0 + q];
+    t.v[q] = v;
+    const T rinv = (T)1 / v.w;
+    t.u[q] = V4<T>{v.x * rinv, v.y * rinv, v.z * rinv, v.w};
+    if (forces) t.w[q] = V4<T>{0, 0, 0, 0};
+    const int32_t j = a.pj[p0 + q];
+    t.pj[q] = j;
+    const uint32_t rmask = a.pmeta[p0 + q] >> 24;
+    const int c = a.code[j];
+    t.info[q] = (uint32_t)(c & 0xff) | ((uint32_t)(j == i) << 8) | (rmask << 16);
+    for (int rc = 0; rc < a.nrcls; rc++) {
+      const T rcut = (T)a.rcls[rc];
+      const bool in = (rmask >> rc) & 1u;
+      t.fc[rc * a.cap + q] = in ? (T)0.5 * (m_cos<T>((T)kPi * v.w / rcut) + (T)1) : (T)0;
+      if (forces)
+        t.dfc[rc * a.cap + q] = in ? (T)-0.5 * ((T)kPi / rcut) * m_sin<T>((T)kPi * v.w / rcut) : (T)0;
+    }
+    for (int e = 0; e < a.necls; e++) {
+      const T eta = (T)a.ecls_eta[e];
+      const int aid = a.ecls_atomid[e];
+      const int rc = a.ecls_rclass[e];
+      const T ex = m_exp<T>(-(eta * (v.w * v.w)));
+      T ids = (T)1;
+      if (aid > 0) ids = atom_id<T>(a.ext, a.next, aid, i) * atom_id<T>(a.ext, a.next, aid, j);
+      const T f = t.fc[rc * a.cap + q];
+      t.E[e * a.cap + q] = ex * f * ids;
+      if (forces) t.D[e * a.cap + q] = ex * (t.dfc[rc * a.cap + q] - (T)2 * eta * v.w * f) * ids;
+    }
+  }
+  __syncwarp();
+  for (int z = 0; z < a.nz; z++) {
+    int base = 0;
+    for (int q0 = 0; q0 < np; q0 += 32) {
+      const int q = q0 + lane;
+      bool in = false;
+      if (q < np) {
+        const uint32_t inf = t.info[q];
+        in = ((int)(inf & 0xff) == z) || ((inf >> 8) & 1u);
+      }
+      const unsigned m = __ballot_sync(0xffffffffu, in);
+      if (in) t.lists[z * a.cap + base + __popc(m & ((1u << lane) - 1u))] = (uint16_t)q;
+      base += __popc(m);
+    }
+    if (lane == 0) t.cnt[z] = base;
+  }
+  __syncwarp();
+}
+
+// M_k(alpha) = sum over list(k) of E_e(k)(j) u_j^alpha, items (k, alpha) over lanes, list order
+template <typename T>
+__device__ void compute_moments(const TileArgs<T> &a, Tile<T> &t, int np, int lane) {
+  const int items = a.ncombo * a.n_mono;
+  for (int it = lane; it < items; it += 32) {
+    const int k = it / a.n_mono, al = it % a.n_mono;
+    const int z = a.combo[2 * k], e = a.combo[2 * k + 1];
+    const int ex = kMonoTab[al][0], ey = kMonoTab[al][1], ez = kMonoTab[al][2];
+    const uint16_t *lst = z >= 0 ? t.lists + z * a.cap : nullptr;
+    const int n = z >= 0 ? t.cnt[z] : np;
+    const T *E = t.E + e * a.cap;
+    T acc = 0;
+    for (int kk = 0; kk < n; kk++) {
+      const int q = lst ? lst[kk] : kk;
+      const V4<T> u = t.u[q];
+      T m = E[q];
+      for (int c = 0; c < ex; c++) m *= u.x;
+      for (int c = 0; c < ey; c++) m *= u.y;
+      for (int c = 0; c < ez; c++) m *= u.z;
+      acc += m;
+    }
+    t.M[it] = acc;
+  }
+  __syncwarp();
+}
+
+}  // namespace fnetg

@@ -1112,32 +1112,60 @@ double orc_update_prepare(const orc_net *net, const double *params, int32_t nspe
  * Forces: forceAnalysis_analytical (forces.F90:317-425) on the dense dG/dR of
  * iGeoAcsfGrad, z-scored like applyZscorePrime (acsf.F90:515-536).
  * ==================================================================================== */
+typedef struct {
+  const orc_batch *b;
+  const orc_gfunc *g;
+  int ng;
+  const double *zprec;
+  int nout;
+  const double *jac;
+  int physical;
+  double *forces;
+} fjob;
+
+static int forces_struct(void *vctx, int s, void *scratch) {
+  (void)scratch;
+  fjob *J = (fjob *)vctx;
+  const orc_batch *b = J->b;
+  const int ng = J->ng, nout = J->nout;
+  int64_t a0 = b->atom_offsets[s];
+  int N = (int)(b->atom_offsets[s + 1] - a0);
+  double *prime = (double *)malloc(sizeof(double) * 3 * (size_t)ng * N * N + 8);
+  if (orc_acsf_prime_ex(b, s, J->g, ng, J->physical, prime)) {
+    free(prime);
+    return -1;
+  }
+  if (J->zprec)
+    for (int k = 0; k < ng; k++) {
+      if (J->zprec[ng + k] < 1e-08) continue;
+      for (int i = 0; i < N; i++)
+        for (int j = 0; j < N; j++)
+          for (int c = 0; c < 3; c++) PR(c, k, i, j) = PR(c, k, i, j) / J->zprec[ng + k];
+    }
+  double *forces = J->forces;
+  for (int q = 0; q < N * 3 * nout; q++) forces[a0 * 3 * nout + q] = 0.0;
+  for (int fa = 0; fa < N; fa++)
+    for (int i = 0; i < N; i++)
+      for (int k = 0; k < ng; k++)
+        for (int c = 0; c < 3; c++)
+          for (int o = 0; o < nout; o++) {
+            double *F = forces + (a0 + fa) * 3 * nout;
+            F[c + 3 * o] = F[c + 3 * o] - J->jac[(a0 + i) * nout * ng + o + (int64_t)nout * k] * PR(c, k, i, fa);
+          }
+  free(prime);
+  return 0;
+}
+
+int orc_forces_mt(const orc_batch *b, const orc_gfunc *g, int32_t ng, const double *zprec,
+                  int32_t nout, const double *jac, int32_t physical, double *forces,
+                  int32_t nthreads) {
+  fjob J = {b, g, ng, zprec, nout, jac, physical, forces};
+  return run_blocks(b->nstruct, nthreads, &J, forces_struct, 8, NULL);
+}
+
 int orc_forces_ex(const orc_batch *b, const orc_gfunc *g, int32_t ng, const double *zprec,
                   int32_t nout, const double *jac, int32_t physical, double *forces) {
-  for (int s = 0; s < b->nstruct; s++) {
-    int64_t a0 = b->atom_offsets[s];
-    int N = (int)(b->atom_offsets[s + 1] - a0);
-    double *prime = (double *)malloc(sizeof(double) * 3 * (size_t)ng * N * N + 8);
-    if (orc_acsf_prime_ex(b, s, g, ng, physical, prime)) { free(prime); return -1; }
-    if (zprec)
-      for (int k = 0; k < ng; k++) {
-        if (zprec[ng + k] < 1e-08) continue;
-        for (int i = 0; i < N; i++)
-          for (int j = 0; j < N; j++)
-            for (int c = 0; c < 3; c++) PR(c, k, i, j) = PR(c, k, i, j) / zprec[ng + k];
-      }
-    for (int q = 0; q < N * 3 * nout; q++) forces[a0 * 3 * nout + q] = 0.0;
-    for (int fa = 0; fa < N; fa++)
-      for (int i = 0; i < N; i++)
-        for (int k = 0; k < ng; k++)
-          for (int c = 0; c < 3; c++)
-            for (int o = 0; o < nout; o++) {
-              double *F = forces + (a0 + fa) * 3 * nout;
-              F[c + 3 * o] = F[c + 3 * o] - jac[(a0 + i) * nout * ng + o + (int64_t)nout * k] * PR(c, k, i, fa);
-            }
-    free(prime);
-  }
-  return 0;
+  return orc_forces_mt(b, g, ng, zprec, nout, jac, physical, forces, 1);
 }
 #undef PR
 

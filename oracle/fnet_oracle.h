@@ -123,6 +123,10 @@ int orc_forces(const orc_batch *b, const orc_gfunc *g, int32_t ng, const double 
                int32_t nout, const double *jac, double *forces);
 int orc_forces_ex(const orc_batch *b, const orc_gfunc *g, int32_t ng, const double *zprec,
                   int32_t nout, const double *jac, int32_t physical, double *forces);
+/* the same with structures split over nthreads host threads (contiguous blocks) */
+int orc_forces_mt(const orc_batch *b, const orc_gfunc *g, int32_t ng, const double *zprec,
+                  int32_t nout, const double *jac, int32_t physical, double *forces,
+                  int32_t nthreads);
 
 /* ---- optimisers ---- */
 /* steepest descent (lib_dftbp/steepdesc.F90:104-204) */

@@ -73,6 +73,7 @@ def lib():
         L.orc_update_prepare.argtypes = [vp, vp, i32, vp, dbl, dbl, dbl]
         L.orc_forces.argtypes = [vp, vp, i32, vp, i32, vp, vp]
         L.orc_forces_ex.argtypes = [vp, vp, i32, vp, i32, vp, i32, vp]
+        L.orc_forces_mt.argtypes = [vp, vp, i32, vp, i32, vp, i32, vp, i32]
         L.orc_sd_new.restype = vp
         L.orc_sd_new.argtypes = [i32, dbl, dbl, dbl, vp]
         L.orc_sd_next.argtypes = [vp, vp, vp]
@@ -219,7 +220,7 @@ def jacobian(dims, activation, params, feats, species):
     return out.reshape(feats.shape[0], nf, nout).transpose(0, 2, 1).copy()
 
 
-def forces(ds, funcs, zprec, jac, physical=False):
+def forces(ds, funcs, zprec, jac, physical=False, nthreads=1):
     """Analytical forces [Ntot, nOut, 3] from per-atom Jacobians [Ntot, nOut, nG]; physical
     selects the exact derivative (every periodic image contributes) over the reference's."""
     b = Batch(ds)
@@ -228,7 +229,8 @@ def forces(ds, funcs, zprec, jac, physical=False):
     jf = np.ascontiguousarray(jac.transpose(0, 2, 1).reshape(jac.shape[0], -1))
     z = None if zprec is None else np.ascontiguousarray(zprec, dtype=np.float64).reshape(-1)
     out = np.zeros(ds.ntot * 3 * nout)
-    rc = lib().orc_forces_ex(b.ref, g, len(funcs), _p(z), nout, _p(jf), int(physical), _p(out))
+    rc = lib().orc_forces_mt(b.ref, g, len(funcs), _p(z), nout, _p(jf), int(physical), _p(out),
+                             int(nthreads))
     if rc:
         raise RuntimeError(f"orc_forces failed ({rc})")
     return out.reshape(ds.ntot, nout, 3)
