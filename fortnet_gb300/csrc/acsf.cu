@@ -18,7 +18,7 @@ namespace fnetg {
 
 namespace {
 
-template <typename T>
+template <typename T, int D>
 __global__ void __launch_bounds__(256) acsf_kernel(TileArgs<T> a) {
   extern __shared__ __align__(128) unsigned char smem[];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -31,10 +31,12 @@ __global__ void __launch_bounds__(256) acsf_kernel(TileArgs<T> a) {
     const int np = (int)(a.poff[i + 1] - p0);
     const int64_t row = a.bpos[i];
     stage_tile<T>(a, t, i, p0, np, lane, false);
-    if (a.ncombo > 0) compute_moments<T>(a, t, np, lane);
+    if (D > 0 && a.ncombo > 0) compute_moments<T, (D > 0 ? D : 1)>(a, t, np, lane);
     // ---- radial functions: lanes over functions, list order
     for (int g = lane; g < a.nrad; g += 32) {
       const GDesc d = a.rad[g];
+      const T *P = a.radp + 8 * g;
+      const T kappa = P[1], rs = P[2], eta = P[3];
       const uint16_t *lst = d.chan1 >= 0 ? t.lists + d.chan1 * a.cap : nullptr;
       const int n = d.chan1 >= 0 ? t.cnt[d.chan1] : np;
       const T *fcr = t.fc + d.rclass * a.cap;
@@ -50,10 +52,10 @@ __global__ void __launch_bounds__(256) acsf_kernel(TileArgs<T> a) {
         if (d.type == 1) {
           term = fc;
         } else if (d.type == 2) {
-          const T x = r - (T)d.rs;
-          term = m_exp<T>(-((T)d.eta * (x * x))) * fc;
+          const T x = r - rs;
+          term = m_exp<T>(-(eta * (x * x))) * fc;
         } else {
-          term = m_cos<T>((T)d.kappa * r) * fc;
+          term = m_cos<T>(kappa * r) * fc;
         }
         acc += term;
       }
@@ -62,10 +64,10 @@ __global__ void __launch_bounds__(256) acsf_kernel(TileArgs<T> a) {
     // ---- integer-xi G5 through moments: lanes over functions
     for (int f = lane; f < a.nmf; f += 32) {
       const MFunc mf = a.mfunc[f];
-      const double *cf = a.mcoef + (int64_t)f * a.n_mono;
+      const T *cf = a.mcoef + (int64_t)f * a.n_mono;
       const T *M1 = t.M + mf.k1 * a.n_mono, *M2 = t.M + mf.k2 * a.n_mono;
       T acc = 0;
-      for (int al = 0; al < a.n_mono; al++) acc += (T)cf[al] * M1[al] * M2[al];
+      for (int al = 0; al < a.n_mono; al++) acc += cf[al] * M1[al] * M2[al];
       a.feat[row * a.nf + mf.out] = acc;
     }
     // ---- remaining angular groups: lanes over triplets
@@ -74,14 +76,15 @@ __global__ void __launch_bounds__(256) acsf_kernel(TileArgs<T> a) {
       __syncwarp();
       if (lane < G.count) {
         const GDesc d = a.ang[G.first + lane];
-        t.gpar[lane] = (T)d.lambda;
-        t.gpar[32 + lane] = (T)d.xi;
-        t.gpar[64 + lane] = (T)d.eta;
-        t.gpar[96 + lane] = (T)d.pref;
+        const T *P = a.angp + 8 * (G.first + lane);
+        t.gpar[lane] = P[4];
+        t.gpar[32 + lane] = P[5];
+        t.gpar[64 + lane] = P[3];
+        t.gpar[96 + lane] = P[6];
         t.gint[lane] = d.xi_int;
         t.gint[32 + lane] = d.eclass;
         t.gint[64 + lane] = d.type;
-        if (lane == 0) t.gpar[128] = (T)d.rcut;
+        if (lane == 0) t.gpar[128] = P[0];
       }
       if (G.has_g4 && G.atomid > 0)
         for (int q = lane; q < np; q += 32) t.idv[q] = atom_id<T>(a.ext, a.next, G.atomid, t.pj[q]);
@@ -220,19 +223,24 @@ template <typename T> void fill_tile_args(fnetg_ctx *ctx, TileArgs<T> &a) {
   a.rad = ctx->d_rad.as<GDesc>();
   a.nrad = (int)ctx->h_rad.size();
   a.ang = ctx->d_ang.as<GDesc>();
+  const bool dbl = sizeof(T) == 8;
+  a.radp = static_cast<const T *>(dbl ? ctx->d_radpar_d.p : ctx->d_radpar_f.p);
+  a.angp = static_cast<const T *>(dbl ? ctx->d_angpar_d.p : ctx->d_angpar_f.p);
   a.groups = ctx->d_groups.as<AGroup>();
   a.ngroups = (int)ctx->h_groups.size();
-  a.ecls_eta = ctx->d_ecls_eta.as<double>();
+  a.ecls_eta = static_cast<const T *>(dbl ? ctx->d_ecls_eta.p : ctx->d_ecls_eta_f.p);
   a.ecls_rclass = ctx->d_ecls_rclass.as<int>();
   a.ecls_atomid = ctx->d_ecls_atomid.as<int>();
   a.necls = (int)ctx->ecls_eta.size();
-  a.rcls = ctx->d_rcls.as<double>();
+  a.rcls = static_cast<const T *>(dbl ? ctx->d_rcls.p : ctx->d_rcls_f.p);
   a.nrcls = (int)ctx->rcut_classes.size();
   a.nz = (int)ctx->zcodes.size();
   a.cap = std::max(32, (ctx->max_pairs + 31) / 32 * 32);
   a.mfunc = ctx->d_mfunc.as<MFunc>();
   a.nmf = (int)ctx->h_mfunc.size();
-  a.mcoef = ctx->d_mcoef.as<double>();
+  a.mcoef = static_cast<const T *>(dbl ? ctx->d_mcoef.p : ctx->d_mcoef_f.p);
+  a.qoff = ctx->d_qoff.as<int32_t>();
+  a.qent = ctx->d_qent.as<int32_t>();
   a.combo = ctx->d_combo.as<int32_t>();
   a.ncombo = ctx->n_combo;
   a.cidx = ctx->d_cidx.as<int32_t>();
@@ -242,13 +250,8 @@ template <typename T> void fill_tile_args(fnetg_ctx *ctx, TileArgs<T> &a) {
   a.ng = (int)ctx->gf.size();
 }
 
-template <typename T> int launch_acsf(fnetg_ctx *ctx) {
+template <typename T, int D> int launch_acsf_d(fnetg_ctx *ctx, TileArgs<T> &a) {
   const int64_t N = ctx->N;
-  FNETG_CUDA(ctx->d_feat.ensure(sizeof(T) * std::max<int64_t>(N, 1) * std::max(ctx->nf, 1)));
-  if (N == 0) return FNETG_OK;
-  TileArgs<T> a;
-  fill_tile_args<T>(ctx, a);
-  FNETG_CHECK(a.cap <= 65535, FNETG_E_UNSUPPORTED, "more than 65535 neighbours of one atom");
   const size_t tb =
       tile_bytes<T>(a.cap, a.nrcls, a.necls, a.nz, a.ncombo, a.n_mono, a.ng, false);
   int wpb = 8;
@@ -256,17 +259,33 @@ template <typename T> int launch_acsf(fnetg_ctx *ctx) {
   FNETG_CHECK(tb * wpb <= 227 * 1024, FNETG_E_UNSUPPORTED,
               "neighbour tile of one atom exceeds shared memory");
   const size_t smem = tb * wpb;
-  FNETG_CUDA(cudaFuncSetAttribute(acsf_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  FNETG_CUDA(cudaFuncSetAttribute(acsf_kernel<T, D>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)smem));
   int per_sm = 1;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, acsf_kernel<T>, wpb * 32, smem);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, acsf_kernel<T, D>, wpb * 32, smem);
   const int64_t want = (N + wpb - 1) / wpb;
   const int blocks = (int)std::max<int64_t>(
       1, std::min<int64_t>(want, (int64_t)num_sms() * std::max(per_sm, 1) * 8));
   LaunchScope ls(ctx, "acsf");
-  acsf_kernel<T><<<blocks, wpb * 32, smem, ctx->stream>>>(a);
+  acsf_kernel<T, D><<<blocks, wpb * 32, smem, ctx->stream>>>(a);
   FNETG_CUDA(cudaGetLastError());
   return FNETG_OK;
+}
+
+template <typename T> int launch_acsf(fnetg_ctx *ctx) {
+  const int64_t N = ctx->N;
+  FNETG_CUDA(ctx->d_feat.ensure(sizeof(T) * std::max<int64_t>(N, 1) * std::max(ctx->nf, 1)));
+  if (N == 0) return FNETG_OK;
+  TileArgs<T> a;
+  fill_tile_args<T>(ctx, a);
+  FNETG_CHECK(a.cap <= 65535, FNETG_E_UNSUPPORTED, "more than 65535 neighbours of one atom");
+  switch (ctx->mom_degree) {
+    case 0: return launch_acsf_d<T, 0>(ctx, a);
+    case 1: return launch_acsf_d<T, 1>(ctx, a);
+    case 2: return launch_acsf_d<T, 2>(ctx, a);
+    case 3: return launch_acsf_d<T, 3>(ctx, a);
+    default: return launch_acsf_d<T, 4>(ctx, a);
+  }
 }
 
 template <typename T> int launch_zscore(fnetg_ctx *ctx, const int32_t *weights, bool compute) {

@@ -550,6 +550,37 @@ int fnetg_set_gfunctions(fnetg_ctx *ctx, int32_t ng, const fnetg_gfunc *g) {
     }
   }
   ctx->n_combo = (int)ctx->h_combo.size() / 2;
+  // per-combo list of the moment functions whose Q (adjoint moment) it receives
+  std::vector<int32_t> qoff(ctx->n_combo + 1, 0), qent;
+  for (int k = 0; k < ctx->n_combo; k++) {
+    qoff[k] = (int32_t)qent.size() / 2;
+    for (size_t f = 0; f < ctx->h_mfunc.size(); f++) {
+      const MFunc &mf = ctx->h_mfunc[f];
+      if (mf.k1 == k) {
+        qent.push_back((int32_t)f);
+        qent.push_back(mf.k2);
+      }
+      if (mf.k2 == k) {
+        qent.push_back((int32_t)f);
+        qent.push_back(mf.k1);
+      }
+    }
+  }
+  qoff[ctx->n_combo] = (int32_t)qent.size() / 2;
+  FNETG_CUDA(ctx->d_qoff.ensure(sizeof(int32_t) * (ctx->n_combo + 1)));
+  FNETG_CUDA(ctx->d_qent.ensure(sizeof(int32_t) * std::max<size_t>(qent.size(), 2)));
+  FNETG_CUDA(cudaMemcpy(ctx->d_qoff.p, qoff.data(), sizeof(int32_t) * qoff.size(),
+                        cudaMemcpyHostToDevice));
+  if (!qent.empty())
+    FNETG_CUDA(cudaMemcpy(ctx->d_qent.p, qent.data(), sizeof(int32_t) * qent.size(),
+                          cudaMemcpyHostToDevice));
+  {
+    std::vector<float> cf(ctx->h_mcoef.begin(), ctx->h_mcoef.end());
+    FNETG_CUDA(ctx->d_mcoef_f.ensure(sizeof(float) * std::max<size_t>(cf.size(), 1)));
+    if (!cf.empty())
+      FNETG_CUDA(cudaMemcpy(ctx->d_mcoef_f.p, cf.data(), sizeof(float) * cf.size(),
+                            cudaMemcpyHostToDevice));
+  }
   FNETG_CUDA(ctx->d_mfunc.ensure(sizeof(MFunc) * std::max<size_t>(ctx->h_mfunc.size(), 1)));
   FNETG_CUDA(ctx->d_mcoef.ensure(sizeof(double) * std::max<size_t>(ctx->h_mcoef.size(), 1)));
   FNETG_CUDA(ctx->d_combo.ensure(sizeof(int32_t) * std::max<size_t>(ctx->h_combo.size(), 2)));
@@ -619,6 +650,36 @@ int fnetg_set_gfunctions(fnetg_ctx *ctx, int32_t ng, const fnetg_gfunc *g) {
   if (!ctx->rcut_classes.empty())
     FNETG_CUDA(cudaMemcpy(ctx->d_rcls.p, ctx->rcut_classes.data(),
                           sizeof(double) * ctx->rcut_classes.size(), cudaMemcpyHostToDevice));
+  {
+    auto params = [](const std::vector<GDesc> &v, std::vector<double> &pd, std::vector<float> &pf) {
+      pd.clear();
+      for (auto &d : v) {
+        const double q[8] = {d.rcut, d.kappa, d.rs, d.eta, d.lambda, d.xi, d.pref, 0.0};
+        pd.insert(pd.end(), q, q + 8);
+      }
+      if (pd.empty()) pd.assign(8, 0.0);
+      pf.assign(pd.begin(), pd.end());
+    };
+    std::vector<double> pd;
+    std::vector<float> pf;
+    params(ctx->h_rad, pd, pf);
+    FNETG_CUDA(ctx->d_radpar_d.ensure(sizeof(double) * pd.size()));
+    FNETG_CUDA(ctx->d_radpar_f.ensure(sizeof(float) * pf.size()));
+    FNETG_CUDA(cudaMemcpy(ctx->d_radpar_d.p, pd.data(), sizeof(double) * pd.size(), cudaMemcpyHostToDevice));
+    FNETG_CUDA(cudaMemcpy(ctx->d_radpar_f.p, pf.data(), sizeof(float) * pf.size(), cudaMemcpyHostToDevice));
+    params(ctx->h_ang, pd, pf);
+    FNETG_CUDA(ctx->d_angpar_d.ensure(sizeof(double) * pd.size()));
+    FNETG_CUDA(ctx->d_angpar_f.ensure(sizeof(float) * pf.size()));
+    FNETG_CUDA(cudaMemcpy(ctx->d_angpar_d.p, pd.data(), sizeof(double) * pd.size(), cudaMemcpyHostToDevice));
+    FNETG_CUDA(cudaMemcpy(ctx->d_angpar_f.p, pf.data(), sizeof(float) * pf.size(), cudaMemcpyHostToDevice));
+    std::vector<float> ef(kMaxEtaClasses, 0.f), rf(kMaxRcutClasses, 0.f);
+    for (size_t q = 0; q < ctx->ecls_eta.size(); q++) ef[q] = (float)ctx->ecls_eta[q];
+    for (size_t q = 0; q < ctx->rcut_classes.size(); q++) rf[q] = (float)ctx->rcut_classes[q];
+    FNETG_CUDA(ctx->d_ecls_eta_f.ensure(sizeof(float) * kMaxEtaClasses));
+    FNETG_CUDA(ctx->d_rcls_f.ensure(sizeof(float) * kMaxRcutClasses));
+    FNETG_CUDA(cudaMemcpy(ctx->d_ecls_eta_f.p, ef.data(), sizeof(float) * kMaxEtaClasses, cudaMemcpyHostToDevice));
+    FNETG_CUDA(cudaMemcpy(ctx->d_rcls_f.p, rf.data(), sizeof(float) * kMaxRcutClasses, cudaMemcpyHostToDevice));
+  }
   ctx->nb_valid = false;
   ctx->feats_valid = false;
   ctx->zprec_valid = false;

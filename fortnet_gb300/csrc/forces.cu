@@ -189,6 +189,7 @@ __global__ void __launch_bounds__(256) forces_kernel(TileArgs<T> a) {
       for (int g = 0; g < a.nrad; g++) {
         const GDesc d = a.rad[g];
         if (d.chan1 >= 0 && code != d.chan1) continue;
+        const T *P = a.radp + 8 * g;
         if (!((inf >> (16 + d.rclass)) & 1u)) continue;
         T fc = tl.fc[d.rclass * a.cap + q], dfc = tl.dfc[d.rclass * a.cap + q];
         if (d.atomid > 0) {
@@ -200,11 +201,11 @@ __global__ void __launch_bounds__(256) forces_kernel(TileArgs<T> a) {
         if (d.type == 1) {
           dg = dfc;
         } else if (d.type == 2) {
-          const T x = r - (T)d.rs;
-          dg = m_exp<T>(-((T)d.eta * (x * x))) * (dfc - (T)2 * (T)d.eta * x * fc);
+          const T x = r - P[2], eta = P[3];
+          dg = m_exp<T>(-(eta * (x * x))) * (dfc - (T)2 * eta * x * fc);
         } else {
-          const T kr = (T)d.kappa * r;
-          dg = m_cos<T>(kr) * dfc - (T)d.kappa * m_sin<T>(kr) * fc;
+          const T kr = P[1] * r;
+          dg = m_cos<T>(kr) * dfc - P[1] * m_sin<T>(kr) * fc;
         }
         dsum += tl.jv[d.out] * dg;
       }
@@ -215,17 +216,15 @@ __global__ void __launch_bounds__(256) forces_kernel(TileArgs<T> a) {
     }
     // ---- integer-xi G5 through adjoint moments
     if (D > 0 && a.ncombo > 0) {
-      compute_moments<T>(a, tl, np, lane);
+      compute_moments<T, (D > 0 ? D : 1)>(a, tl, np, lane);
       const int items = a.ncombo * a.n_mono;
       for (int it = lane; it < items; it += 32) {
         const int k = it / a.n_mono, al = it % a.n_mono;
         T acc = 0;
-        for (int f = 0; f < a.nmf; f++) {
-          const MFunc mf = a.mfunc[f];
-          if (mf.k1 != k && mf.k2 != k) continue;
-          const T cj = tl.jv[mf.out] * (T)a.mcoef[(int64_t)f * a.n_mono + al];
-          if (mf.k1 == k) acc += cj * tl.M[mf.k2 * a.n_mono + al];
-          if (mf.k2 == k) acc += cj * tl.M[mf.k1 * a.n_mono + al];
+        for (int e = a.qoff[k]; e < a.qoff[k + 1]; e++) {
+          const int f = a.qent[2 * e], ko = a.qent[2 * e + 1];
+          acc += tl.jv[a.mfunc[f].out] * a.mcoef[(int64_t)f * a.n_mono + al] *
+                 tl.M[ko * a.n_mono + al];
         }
         tl.Q[it] = acc;
       }
@@ -244,14 +243,15 @@ __global__ void __launch_bounds__(256) forces_kernel(TileArgs<T> a) {
       __syncwarp();
       if (lane < G.count) {
         const GDesc d = a.ang[G.first + lane];
-        tl.gpar[lane] = (T)d.lambda;
-        tl.gpar[32 + lane] = (T)d.xi;
-        tl.gpar[64 + lane] = (T)d.eta;
-        tl.gpar[96 + lane] = tl.jv[d.out] * (T)d.pref;
+        const T *P = a.angp + 8 * (G.first + lane);
+        tl.gpar[lane] = P[4];
+        tl.gpar[32 + lane] = P[5];
+        tl.gpar[64 + lane] = P[3];
+        tl.gpar[96 + lane] = tl.jv[d.out] * P[6];
         tl.gint[lane] = d.xi_int;
         tl.gint[32 + lane] = d.eclass;
         tl.gint[64 + lane] = d.type;
-        if (lane == 0) tl.gpar[128] = (T)d.rcut;
+        if (lane == 0) tl.gpar[128] = P[0];
       }
       if (G.has_g4 && G.atomid > 0)
         for (int q = lane; q < np; q += 32) tl.idv[q] = atom_id<T>(a.ext, a.next, G.atomid, tl.pj[q]);
@@ -313,19 +313,24 @@ template <typename T> void fill_tile_args_forces(fnetg_ctx *ctx, TileArgs<T> &a)
   a.rad = ctx->d_rad.as<GDesc>();
   a.nrad = (int)ctx->h_rad.size();
   a.ang = ctx->d_ang.as<GDesc>();
+  const bool dbl = sizeof(T) == 8;
+  a.radp = static_cast<const T *>(dbl ? ctx->d_radpar_d.p : ctx->d_radpar_f.p);
+  a.angp = static_cast<const T *>(dbl ? ctx->d_angpar_d.p : ctx->d_angpar_f.p);
   a.groups = ctx->d_groups.as<AGroup>();
   a.ngroups = (int)ctx->h_groups.size();
-  a.ecls_eta = ctx->d_ecls_eta.as<double>();
+  a.ecls_eta = static_cast<const T *>(dbl ? ctx->d_ecls_eta.p : ctx->d_ecls_eta_f.p);
   a.ecls_rclass = ctx->d_ecls_rclass.as<int>();
   a.ecls_atomid = ctx->d_ecls_atomid.as<int>();
   a.necls = (int)ctx->ecls_eta.size();
-  a.rcls = ctx->d_rcls.as<double>();
+  a.rcls = static_cast<const T *>(dbl ? ctx->d_rcls.p : ctx->d_rcls_f.p);
   a.nrcls = (int)ctx->rcut_classes.size();
   a.nz = (int)ctx->zcodes.size();
   a.cap = std::max(32, (ctx->max_pairs + 31) / 32 * 32);
   a.mfunc = ctx->d_mfunc.as<MFunc>();
   a.nmf = (int)ctx->h_mfunc.size();
-  a.mcoef = ctx->d_mcoef.as<double>();
+  a.mcoef = static_cast<const T *>(dbl ? ctx->d_mcoef.p : ctx->d_mcoef_f.p);
+  a.qoff = ctx->d_qoff.as<int32_t>();
+  a.qent = ctx->d_qent.as<int32_t>();
   a.combo = ctx->d_combo.as<int32_t>();
   a.ncombo = ctx->n_combo;
   a.cidx = ctx->d_cidx.as<int32_t>();

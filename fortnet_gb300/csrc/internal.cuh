@@ -130,7 +130,9 @@ struct fnetg_ctx {
   std::vector<double> h_mcoef;      // [nmf][n_mono]
   std::vector<int32_t> h_combo;     // [ncombo][2] (list code or -1 = all, eta class)
   std::vector<int32_t> h_cidx;      // [(nz+1) * necls] combo index, -1 if unused
-  fnetg::DBuf d_mfunc, d_mcoef, d_combo, d_cidx;
+  fnetg::DBuf d_mfunc, d_mcoef, d_combo, d_cidx, d_qoff, d_qent;
+  // kernel parameter copies in both arithmetic widths: [rcut, kappa, rs, eta, lambda, xi, pref, 0]
+  fnetg::DBuf d_radpar_f, d_radpar_d, d_angpar_f, d_angpar_d, d_mcoef_f, d_ecls_eta_f, d_rcls_f;
   fnetg::DBuf d_rad, d_ang, d_groups, d_code, d_ecls_eta, d_ecls_rclass, d_ecls_atomid,
       d_rcls;
 
@@ -141,6 +143,7 @@ struct fnetg_ctx {
   int max_pairs = 0;
   bool d2_valid = false;
   double max_extent = 0.0;  // largest structure bounding-box extent (Bohr)
+  fnetg::DBuf d_img_off, d_imgs;
   fnetg::DBuf d_pcount, d_poff, d_pj, d_pmeta, d_rij, d_d2, d_scan_tmp, d_maxp, d_rcls2;
 
   // features (bucketed rows, compute precision)

@@ -26,8 +26,8 @@ struct NbArgs {
   const double *coords;
   const V4<float> *cf;
   const double *lat;
-  const int32_t *ranges;  // [S*6] lo0,hi0,lo1,hi1,lo2,hi2 (periodic) — zeros otherwise
-  const int32_t *periodic;
+  const int64_t *img_off;  // [S+1] per-structure range into the image table
+  const V4<double> *imgs;  // cell vectors (x, y, z, packed n1/n2/n3) in the iterator's order
   const float *bbox;      // [S*6] lo, hi (relative frame)
   int64_t natoms;
   double rc2;             // rcut*rcut (exact decision)
@@ -88,28 +88,22 @@ __global__ void __launch_bounds__(256) nb_kernel(NbArgs a) {
     int64_t wpos = 0;
     if (kFill) wpos = a.poff[i];
     int64_t cnt = 0;
-    const bool per = a.periodic[s] != 0;
-    int lo0 = 0, hi0 = 0, lo1 = 0, hi1 = 0, lo2 = 0, hi2 = 0;
-    if (per) {
-      lo0 = a.ranges[6 * s + 0]; hi0 = a.ranges[6 * s + 1];
-      lo1 = a.ranges[6 * s + 2]; hi1 = a.ranges[6 * s + 3];
-      lo2 = a.ranges[6 * s + 4]; hi2 = a.ranges[6 * s + 5];
-    }
-    const double *L = a.lat + 9 * s;
     const float *bb = a.bbox + 6 * s;
-    const int n2span = hi1 - lo1 + 1, n3span = hi2 - lo2 + 1;
-    const int nimg = per ? (hi0 - lo0 + 1) * n2span * n3span : 0;
-    // image -1 is the central cell, then lattice points n1 outer .. n3 inner
-    for (int img = -1; img < nimg; img++) {
+    const int64_t im0 = a.img_off[s], im1 = a.img_off[s + 1];
+    // image -1 is the central cell, then the lattice points of the table (n1 outer .. n3 inner)
+    for (int64_t img = im0 - 1; img < im1; img++) {
       int n1 = 0, n2 = 0, n3 = 0;
       double cv[3] = {0.0, 0.0, 0.0};
       int tstart = 1, tcount = n - 1;
-      if (img >= 0) {
-        n1 = lo0 + img / (n2span * n3span);
-        n2 = lo1 + (img / n3span) % n2span;
-        n3 = lo2 + img % n3span;
-        if (n1 == 0 && n2 == 0 && n3 == 0) continue;
-        cell_vector(L, n1, n2, n3, cv);
+      if (img >= im0) {
+        const V4<double> iv = a.imgs[img];
+        cv[0] = iv.x;
+        cv[1] = iv.y;
+        cv[2] = iv.z;
+        const uint32_t packed = (uint32_t)__double_as_longlong(iv.w);
+        n1 = (int8_t)(packed & 0xff);
+        n2 = (int8_t)((packed >> 8) & 0xff);
+        n3 = (int8_t)((packed >> 16) & 0xff);
         tstart = 0;
         tcount = n;
         // skip the image when the shifted bounding box is out of reach
@@ -353,9 +347,42 @@ int run_neighbors(fnetg_ctx *ctx, double rcut) {
       FNETG_CHECK(std::abs(ranges[6 * s + c]) <= 127, FNETG_E_UNSUPPORTED,
                   "more than 127 periodic images along a lattice vector");
   }
-  FNETG_CUDA(ctx->d_ranges.ensure(sizeof(int32_t) * ranges.size()));
-  FNETG_CUDA(cudaMemcpyAsync(ctx->d_ranges.p, ranges.data(), sizeof(int32_t) * ranges.size(),
+  // lattice points of every structure in the iterator's order (latpointiter.F90:121-174,
+  // origin excluded) with the cell vector matmul(latVecs, n) summed in index order
+  std::vector<int64_t> img_off(S + 1, 0);
+  std::vector<V4<double>> imgs;
+  for (int s = 0; s < S; s++) {
+    img_off[s] = (int64_t)imgs.size();
+    if (!ctx->h_periodic[s]) continue;
+    const int32_t *r = ranges.data() + 6 * s;
+    const double *L = ctx->h_lat.data() + 9 * s;
+    for (int n1 = r[0]; n1 <= r[1]; n1++)
+      for (int n2 = r[2]; n2 <= r[3]; n2++)
+        for (int n3 = r[4]; n3 <= r[5]; n3++) {
+          if (n1 == 0 && n2 == 0 && n3 == 0) continue;
+          double cv[3];
+          for (int c = 0; c < 3; c++) {
+            double v = L[c + 0] * (double)n1;
+            v = v + L[c + 3] * (double)n2;
+            v = v + L[c + 6] * (double)n3;
+            cv[c] = v;
+          }
+          const uint64_t packed = (uint64_t)((uint32_t)(uint8_t)(int8_t)n1 |
+                                             ((uint32_t)(uint8_t)(int8_t)n2 << 8) |
+                                             ((uint32_t)(uint8_t)(int8_t)n3 << 16));
+          double w;
+          std::memcpy(&w, &packed, sizeof w);
+          imgs.push_back(V4<double>{cv[0], cv[1], cv[2], w});
+        }
+  }
+  img_off[S] = (int64_t)imgs.size();
+  FNETG_CUDA(ctx->d_img_off.ensure(sizeof(int64_t) * (S + 1)));
+  FNETG_CUDA(ctx->d_imgs.ensure(sizeof(V4<double>) * std::max<size_t>(imgs.size(), 1)));
+  FNETG_CUDA(cudaMemcpyAsync(ctx->d_img_off.p, img_off.data(), sizeof(int64_t) * (S + 1),
                              cudaMemcpyHostToDevice, ctx->stream));
+  if (!imgs.empty())
+    FNETG_CUDA(cudaMemcpyAsync(ctx->d_imgs.p, imgs.data(), sizeof(V4<double>) * imgs.size(),
+                               cudaMemcpyHostToDevice, ctx->stream));
   FNETG_CUDA(ctx->d_pcount.ensure(sizeof(int64_t) * std::max<int64_t>(N, 1)));
   FNETG_CUDA(ctx->d_poff.ensure(sizeof(int64_t) * (N + 1)));
   FNETG_CUDA(ctx->d_maxp.ensure(sizeof(int) * 4));
@@ -371,9 +398,8 @@ int run_neighbors(fnetg_ctx *ctx, double rcut) {
   a.astruct = ctx->d_atom_struct.as<int32_t>();
   a.coords = ctx->d_coords.as<double>();
   a.cf = ctx->d_coordsf.as<V4<float>>();
-  a.lat = ctx->d_lat.as<double>();
-  a.ranges = ctx->d_ranges.as<int32_t>();
-  a.periodic = ctx->d_periodic.as<int32_t>();
+  a.img_off = ctx->d_img_off.as<int64_t>();
+  a.imgs = ctx->d_imgs.as<V4<double>>();
   a.bbox = ctx->d_bbox.as<float>();
   a.natoms = N;
   a.rc2 = rcut * rcut;

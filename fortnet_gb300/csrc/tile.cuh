@@ -75,22 +75,26 @@ template <typename T> struct TileArgs {
   const double *ext;
   int next;
   const GDesc *rad;
+  const T *radp;          // [nrad][8] parameters in the kernel's width
   int nrad;
   const GDesc *ang;       // triplet-sweep functions
+  const T *angp;          // [nang][8]
   const AGroup *groups;
   int ngroups;
-  const double *ecls_eta;
+  const T *ecls_eta;
   const int *ecls_rclass;
   const int *ecls_atomid;
   int necls;
-  const double *rcls;
+  const T *rcls;
   int nrcls;
   int nz;
   int cap;
   // moment form
   const MFunc *mfunc;
   int nmf;
-  const double *mcoef;    // [nmf][n_mono]
+  const T *mcoef;         // [nmf][n_mono]
+  const int32_t *qoff;    // [ncombo+1] per-combo adjoint lists
+  const int32_t *qent;    // (function, other combo) pairs
   const int32_t *combo;   // [ncombo][2]
   int ncombo;
   const int32_t *cidx;    // [(nz+1)*necls]
@@ -206,14 +210,14 @@ __device__ void stage_tile(const TileArgs<T> &a, Tile<T> &t, int64_t i, int64_t 
     const int c = a.code[j];
     t.info[q] = (uint32_t)(c & 0xff) | ((uint32_t)(j == i) << 8) | (rmask << 16);
     for (int rc = 0; rc < a.nrcls; rc++) {
-      const T rcut = (T)a.rcls[rc];
+      const T rcut = a.rcls[rc];
       const bool in = (rmask >> rc) & 1u;
       t.fc[rc * a.cap + q] = in ? (T)0.5 * (m_cos<T>((T)kPi * v.w / rcut) + (T)1) : (T)0;
       if (forces)
         t.dfc[rc * a.cap + q] = in ? (T)-0.5 * ((T)kPi / rcut) * m_sin<T>((T)kPi * v.w / rcut) : (T)0;
     }
     for (int e = 0; e < a.necls; e++) {
-      const T eta = (T)a.ecls_eta[e];
+      const T eta = a.ecls_eta[e];
       const int aid = a.ecls_atomid[e];
       const int rc = a.ecls_rclass[e];
       const T ex = m_exp<T>(-(eta * (v.w * v.w)));
@@ -243,28 +247,68 @@ __device__ void stage_tile(const TileArgs<T> &a, Tile<T> &t, int64_t i, int64_t 
   __syncwarp();
 }
 
-// M_k(alpha) = sum over list(k) of E_e(k)(j) u_j^alpha, items (k, alpha) over lanes, list order
+// Sum of v[0..31] over the warp's lanes, returned on lane l for index l: each of the five
+// butterfly steps exchanges half of the remaining values (31 shuffles instead of 160).
 template <typename T>
+__device__ __forceinline__ T transpose_reduce32(T *v, int lane) {
+#pragma unroll
+  for (int s = 16; s >= 1; s >>= 1) {
+    const bool upper = (lane & s) != 0;
+#pragma unroll
+    for (int k = 0; k < s; k++) {
+      const T send = upper ? v[k] : v[k + s];
+      const T keep = upper ? v[k + s] : v[k];
+      v[k] = keep + __shfl_xor_sync(0xffffffffu, send, s);
+    }
+  }
+  return v[0];
+}
+
+// M_k(alpha) = sum over list(k) of E_e(k)(j) u_j^alpha for every (list, eta class) combo k:
+// lanes over the list's pairs, monomials of degree <= D unrolled, warp reduction per combo.
+template <typename T, int D>
 __device__ void compute_moments(const TileArgs<T> &a, Tile<T> &t, int np, int lane) {
-  const int items = a.ncombo * a.n_mono;
-  for (int it = lane; it < items; it += 32) {
-    const int k = it / a.n_mono, al = it % a.n_mono;
+  constexpr int NM = n_mono_of(D);
+  for (int k = 0; k < a.ncombo; k++) {
     const int z = a.combo[2 * k], e = a.combo[2 * k + 1];
-    const int ex = kMonoTab[al][0], ey = kMonoTab[al][1], ez = kMonoTab[al][2];
     const uint16_t *lst = z >= 0 ? t.lists + z * a.cap : nullptr;
     const int n = z >= 0 ? t.cnt[z] : np;
     const T *E = t.E + e * a.cap;
-    T acc = 0;
-    for (int kk = 0; kk < n; kk++) {
+    T acc[NM > 32 ? NM : 32];
+#pragma unroll
+    for (int al = 0; al < (NM > 32 ? NM : 32); al++) acc[al] = 0;
+    for (int kk = lane; kk < n; kk += 32) {
       const int q = lst ? lst[kk] : kk;
       const V4<T> u = t.u[q];
-      T m = E[q];
-      for (int c = 0; c < ex; c++) m *= u.x;
-      for (int c = 0; c < ey; c++) m *= u.y;
-      for (int c = 0; c < ez; c++) m *= u.z;
-      acc += m;
+      const T w = E[q];
+      T px[D + 1], py[D + 1], pz[D + 1];
+      px[0] = py[0] = pz[0] = (T)1;
+#pragma unroll
+      for (int d = 1; d <= D; d++) {
+        px[d] = px[d - 1] * u.x;
+        py[d] = py[d - 1] * u.y;
+        pz[d] = pz[d - 1] * u.z;
+      }
+#pragma unroll
+      for (int al = 0; al < NM; al++)
+        acc[al] += w * (px[kMonoTab[al][0]] * py[kMonoTab[al][1]] * pz[kMonoTab[al][2]]);
     }
-    t.M[it] = acc;
+    T *M = t.M + k * a.n_mono;
+    if (NM >= 32) {
+      const T mine = transpose_reduce32<T>(acc, lane);
+      M[lane] = mine;
+#pragma unroll
+      for (int al = 32; al < NM; al++) {
+        const T sres = warp_sum<T>(acc[al]);
+        if (lane == 0) M[al] = sres;
+      }
+    } else {
+#pragma unroll
+      for (int al = 0; al < NM; al++) {
+        const T sres = warp_sum<T>(acc[al]);
+        if (lane == al) M[al] = sres;
+      }
+    }
   }
   __syncwarp();
 }
