@@ -270,7 +270,7 @@ int fnetg_upload_structures(fnetg_ctx *ctx, int32_t nstruct, const int64_t *atom
   FNETG_CUDA(ctx->d_off.ensure(sizeof(int64_t) * (nstruct + 1)));
   FNETG_CUDA(ctx->d_atom_struct.ensure(sizeof(int32_t) * std::max<int64_t>(N, 1)));
   FNETG_CUDA(ctx->d_coords.ensure(sizeof(double) * 3 * std::max<int64_t>(N, 1)));
-  FNETG_CUDA(ctx->d_coordsf.ensure(sizeof(V4<float>) * std::max<int64_t>(N, 1)));
+  FNETG_CUDA(ctx->d_coordsf.ensure(sizeof(V4<float>) * 2 * std::max<int64_t>(N, 1)));
   FNETG_CUDA(ctx->d_atnum.ensure(sizeof(int32_t) * std::max<int64_t>(N, 1)));
   FNETG_CUDA(ctx->d_lat.ensure(sizeof(double) * 9 * std::max(nstruct, 1)));
   FNETG_CUDA(ctx->d_bbox.ensure(sizeof(float) * 6 * std::max(nstruct, 1)));

@@ -104,6 +104,8 @@ struct fnetg_ctx {
   std::vector<int32_t> h_atnum, h_periodic;
   std::vector<double> h_lat;
   int32_t next = 0;
+  // d_coordsf: [2N] float coordinates relative to the structure's box corner, high parts then
+  // the low parts (coordinate - high part)
   fnetg::DBuf d_off, d_atom_struct, d_coords, d_coordsf, d_atnum, d_lat, d_ranges, d_bbox,
       d_ext, d_periodic;
 
@@ -143,7 +145,7 @@ struct fnetg_ctx {
   int max_pairs = 0;
   bool d2_valid = false;
   double max_extent = 0.0;  // largest structure bounding-box extent (Bohr)
-  fnetg::DBuf d_img_off, d_imgs;
+  fnetg::DBuf d_img_off, d_imgs, d_imgs_f;
   fnetg::DBuf d_pcount, d_poff, d_pj, d_pmeta, d_rij, d_d2, d_scan_tmp, d_maxp, d_rcls2;
 
   // features (bucketed rows, compute precision)

@@ -4,11 +4,13 @@
 // computed here in reverse mode).
 //
 // Feature rows are stored species-bucketed, so every CTA works on a tile of rows of ONE
-// sub-network and reads one weight set.  One thread per row; hidden activations live in
-// shared memory (one padded row per thread, bank-conflict free), weights are read from a
-// kernel-friendly copy (row-major [d_in][d_out] per layer) through warp-uniform vector
-// loads, eight (FP32) or four (FP64) output neurons per pass.  Per-tile weight-gradient
-// partials are reduced across tiles in FP64.
+// sub-network and reads one weight set.  A CTA takes its tile in chunks of RC rows; each layer
+// is a small GEMM over the chunk with activations kept transposed in shared memory
+// ([width][RC + 4], rows contiguous) and a 4-row x 4-output register tile per thread: one
+// 16-byte shared load of four rows and one 16-byte weight load feed 16 FMAs.  The compute
+// layout pads every weight row to a multiple of four (zeros) and stores W ([d_in][d_out])
+// for the forward pass and W^T ([d_out][d_in]) for the backward pass.  Per-tile
+// weight-gradient partials are reduced across tiles in FP64.
 #include <algorithm>
 
 #include "internal.cuh"
@@ -17,16 +19,20 @@ namespace fnetg {
 
 namespace {
 
+constexpr int kMlpThreads = 128;
+
+__host__ __device__ inline int pad4(int x) { return (x + 3) & ~3; }
+
 struct NetDesc {
   int nlayer;
   int dims[kMaxLayers];
-  int64_t cw[kMaxLayers];  // compute-layout weight offset of layer l (d_l x d_{l+1}, row-major)
-  int64_t cb[kMaxLayers];  // compute-layout bias offset of layer l+1
-  int64_t stride;          // compute-layout parameters per species
+  int64_t cw[kMaxLayers];  // W of layer l: [d_l][pad4(d_{l+1})] row-major
+  int64_t cb[kMaxLayers];  // bias of layer l+1: [pad4(d_{l+1})]
+  int64_t ct[kMaxLayers];  // W^T of layer l: [d_{l+1}][pad4(d_l)] row-major
+  int64_t stride;          // gradient-layout parameters per species (W and b parts)
+  int64_t pstride;         // compute-layout parameters per species (W, b, W^T)
   int act;
-  int hidden_w;            // sum of hidden widths (z storage per row)
-  int zoff[kMaxLayers];    // offset of layer l's z in a row's scratch (l = 1..L-2)
-  int maxw;
+  int maxd;                // largest width of layers 1..L-1 (delta buffers)
 };
 
 template <typename T> __device__ __forceinline__ T act_f(int t, T x) {
@@ -89,35 +95,228 @@ template <> __device__ __forceinline__ float act_d<float>(int t, float x) {
   }
 }
 
-// One dense layer for one row: out[o] = b[o] + sum_k in[k] * W[k][o] for o in [0, dout).
-// `in` is a row of stride 1 (shared or global), `W` row-major [din][dout].
-template <typename T, int OB>
-__device__ __forceinline__ void dense_row(const T *__restrict__ W, const T *__restrict__ b,
-                                          const T *in, int din, int dout, T *z_out) {
-  for (int o0 = 0; o0 < dout; o0 += OB) {
-    T acc[OB];
+// activation and its derivative at z in one evaluation
+template <typename T> __device__ __forceinline__ void act_fd(int t, T z, T &f, T &d) {
+  if (t == FNETG_ACT_TANH) {
+    const T th = tanh(z);
+    f = th;
+    d = (T)1 - th * th;
+  } else if (t == FNETG_ACT_SIGMOID) {
+    const T sg = (T)1 / ((T)1 + exp(-z));
+    f = sg;
+    d = sg * ((T)1 - sg);
+  } else {
+    f = act_f<T>(t, z);
+    d = act_d<T>(t, z);
+  }
+}
+template <> __device__ __forceinline__ void act_fd<float>(int t, float z, float &f, float &d) {
+  if (t == FNETG_ACT_TANH) {
+    const float th = tanhf(z);
+    f = th;
+    d = 1.f - th * th;
+  } else if (t == FNETG_ACT_SIGMOID) {
+    const float sg = 1.f / (1.f + expf(-z));
+    f = sg;
+    d = sg * (1.f - sg);
+  } else {
+    f = act_f<float>(t, z);
+    d = act_d<float>(t, z);
+  }
+}
+
+template <typename T> __device__ __forceinline__ V4<T> lds4(const T *p) {
+  return *reinterpret_cast<const V4<T> *>(p);
+}
+__device__ __forceinline__ V4<float> ldg4(const float *p) {
+  const float4 v = __ldg(reinterpret_cast<const float4 *>(p));
+  return V4<float>{v.x, v.y, v.z, v.w};
+}
+__device__ __forceinline__ V4<double> ldg4(const double *p) {
+  const double2 a = __ldg(reinterpret_cast<const double2 *>(p));
+  const double2 b = __ldg(reinterpret_cast<const double2 *>(p) + 1);
+  return V4<double>{a.x, a.y, b.x, b.y};
+}
+template <typename T> __device__ __forceinline__ void sts4(T *p, T a, T b, T c, T d) {
+  *reinterpret_cast<V4<T> *>(p) = V4<T>{a, b, c, d};
+}
+template <typename T> __device__ __forceinline__ T comp(const V4<T> &v, int i) {
+  return i == 0 ? v.x : (i == 1 ? v.y : (i == 2 ? v.z : v.w));
+}
+
+// acc[i][j] += x_i * w_j
+template <typename T>
+__device__ __forceinline__ void fma44(T (&acc)[4][4], const V4<T> &x, const V4<T> &w) {
+  const T xs[4] = {x.x, x.y, x.z, x.w}, ws[4] = {w.x, w.y, w.z, w.w};
 #pragma unroll
-    for (int u = 0; u < OB; u++) acc[u] = (o0 + u < dout) ? b[o0 + u] : (T)0;
-    if (o0 + OB <= dout) {
-      for (int k = 0; k < din; k++) {
-        const T x = in[k];
-        const T *w = W + (int64_t)k * dout + o0;
+  for (int i = 0; i < 4; i++)
 #pragma unroll
-        for (int u = 0; u < OB; u++) acc[u] += x * __ldg(w + u);
-      }
-    } else {
-      for (int k = 0; k < din; k++) {
-        const T x = in[k];
-        const T *w = W + (int64_t)k * dout + o0;
+    for (int j = 0; j < 4; j++) acc[i][j] += xs[i] * ws[j];
+}
+
+// Y[o][r] = b[o] + sum_k X[k][r] W[k][o] for the chunk's RC rows.  hidden: Y = f(z) and
+// Fp (if given) = f'(z); otherwise Y = z.  Columns o >= dout are not written.
+template <typename T>
+__device__ void layer_forward(const T *X, int din, const T *__restrict__ W,
+                              const T *__restrict__ b, int dout, T *Y, T *Fp, int RC, int RCP,
+                              bool hidden, int act) {
+  const int ngr = RC >> 2, dp = pad4(dout), items = ngr * (dp >> 2);
+  for (int it = threadIdx.x; it < items; it += blockDim.x) {
+    const int r0 = (it % ngr) << 2, o0 = (it / ngr) << 2;
+    const V4<T> bb = ldg4(b + o0);
+    T acc[4][4];
 #pragma unroll
-        for (int u = 0; u < OB; u++)
-          if (o0 + u < dout) acc[u] += x * __ldg(w + u);
+    for (int i = 0; i < 4; i++) {
+      acc[i][0] = bb.x;
+      acc[i][1] = bb.y;
+      acc[i][2] = bb.z;
+      acc[i][3] = bb.w;
+    }
+    const T *xp = X + r0;
+    const T *wp = W + o0;
+#pragma unroll 4
+    for (int k = 0; k < din; k++) fma44(acc, lds4(xp + (int64_t)k * RCP), ldg4(wp + (int64_t)k * dp));
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+      if (o0 + j >= dout) break;
+      if (hidden) {
+        T f[4], d[4];
+#pragma unroll
+        for (int i = 0; i < 4; i++) act_fd<T>(act, acc[i][j], f[i], d[i]);
+        sts4(Y + (int64_t)(o0 + j) * RCP + r0, f[0], f[1], f[2], f[3]);
+        if (Fp) sts4(Fp + (int64_t)(o0 + j) * RCP + r0, d[0], d[1], d[2], d[3]);
+      } else {
+        sts4(Y + (int64_t)(o0 + j) * RCP + r0, acc[0][j], acc[1][j], acc[2][j], acc[3][j]);
       }
     }
-#pragma unroll
-    for (int u = 0; u < OB; u++)
-      if (o0 + u < dout) z_out[o0 + u] = acc[u];
   }
+}
+
+// Dn[k][r] = (Fp[k][r] if given) * sum_o WT[o][k] D[o][r]
+template <typename T>
+__device__ void layer_backward(const T *D, int dout, const T *__restrict__ WT, int din,
+                               const T *Fp, T *Dn, int RC, int RCP) {
+  const int ngr = RC >> 2, kp = pad4(din), items = ngr * (kp >> 2);
+  for (int it = threadIdx.x; it < items; it += blockDim.x) {
+    const int r0 = (it % ngr) << 2, k0 = (it / ngr) << 2;
+    T acc[4][4];
+#pragma unroll
+    for (int i = 0; i < 4; i++)
+#pragma unroll
+      for (int j = 0; j < 4; j++) acc[i][j] = (T)0;
+    const T *dp_ = D + r0;
+    const T *wp = WT + k0;
+#pragma unroll 4
+    for (int o = 0; o < dout; o++)
+      fma44(acc, lds4(dp_ + (int64_t)o * RCP), ldg4(wp + (int64_t)o * kp));
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+      if (k0 + j >= din) break;
+      T v[4] = {acc[0][j], acc[1][j], acc[2][j], acc[3][j]};
+      if (Fp) {
+        const V4<T> f = lds4(Fp + (int64_t)(k0 + j) * RCP + r0);
+        v[0] *= f.x;
+        v[1] *= f.y;
+        v[2] *= f.z;
+        v[3] *= f.w;
+      }
+      sts4(Dn + (int64_t)(k0 + j) * RCP + r0, v[0], v[1], v[2], v[3]);
+    }
+  }
+}
+
+// Gradient partials of one layer over the chunk: G_W[k][o] (+)= sum_r A[k][r] D[o][r],
+// G_b[o] (+)= sum_r D[o][r].  A thread owns the k's kq + i * (pad4(din) / 4) (consecutive k
+// across a warp's lanes: conflict-free shared loads) and four consecutive o's.
+template <typename T>
+__device__ void layer_wgrad(const T *A, int din, const T *D, int dout, T *GW, T *Gb, int RC,
+                            int RCP, bool first) {
+  const int KQ = pad4(din) >> 2, dp = pad4(dout), OQ = dp >> 2;
+  const int items = KQ * OQ + OQ;
+  for (int it = threadIdx.x; it < items; it += blockDim.x) {
+    if (it < KQ * OQ) {
+      const int kq = it % KQ, o0 = (it / KQ) << 2;
+      T acc[4][4];
+#pragma unroll
+      for (int i = 0; i < 4; i++)
+#pragma unroll
+        for (int j = 0; j < 4; j++) acc[i][j] = (T)0;
+      int kk[4];
+#pragma unroll
+      for (int i = 0; i < 4; i++) kk[i] = min(kq + i * KQ, din - 1);
+      const int oo[4] = {min(o0, dout - 1), min(o0 + 1, dout - 1), min(o0 + 2, dout - 1),
+                         min(o0 + 3, dout - 1)};
+      for (int r = 0; r < RC; r += 4) {
+        V4<T> a4[4], d4[4];
+#pragma unroll
+        for (int i = 0; i < 4; i++) a4[i] = lds4(A + (int64_t)kk[i] * RCP + r);
+#pragma unroll
+        for (int j = 0; j < 4; j++) d4[j] = lds4(D + (int64_t)oo[j] * RCP + r);
+#pragma unroll
+        for (int i = 0; i < 4; i++)
+#pragma unroll
+          for (int j = 0; j < 4; j++)
+            acc[i][j] += a4[i].x * d4[j].x + a4[i].y * d4[j].y + a4[i].z * d4[j].z +
+                         a4[i].w * d4[j].w;
+      }
+#pragma unroll
+      for (int i = 0; i < 4; i++) {
+        const int k = kq + i * KQ;
+        if (k >= din) break;
+        T *g = GW + (int64_t)k * dp + o0;
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+          if (o0 + j >= dout) break;
+          g[j] = first ? acc[i][j] : g[j] + acc[i][j];
+        }
+      }
+    } else {
+      const int o0 = (it - KQ * OQ) << 2;
+      T acc[4] = {(T)0, (T)0, (T)0, (T)0};
+      for (int r = 0; r < RC; r += 4)
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+          if (o0 + j < dout) {
+            const V4<T> d4 = lds4(D + (int64_t)(o0 + j) * RCP + r);
+            acc[j] += (d4.x + d4.y) + (d4.z + d4.w);
+          }
+        }
+#pragma unroll
+      for (int j = 0; j < 4; j++)
+        if (o0 + j < dout) Gb[o0 + j] = first ? acc[j] : Gb[o0 + j] + acc[j];
+    }
+  }
+}
+
+// Shared-memory plan of a chunk (element offsets): A_l (l = 0..L-2) inputs of every layer,
+// Fp_l (l = 1..L-2) activation derivatives, two delta buffers of maxd rows.
+struct SmemPlan {
+  int64_t A[kMaxLayers], F[kMaxLayers], D0, D1, total;
+};
+__host__ __device__ inline SmemPlan smem_plan(const NetDesc &n, int RCP, bool keep_all) {
+  SmemPlan p{};
+  int64_t o = 0;
+  const int L = n.nlayer;
+  if (keep_all) {
+    for (int l = 0; l < L - 1; l++) {
+      p.A[l] = o;
+      o += (int64_t)pad4(n.dims[l]) * RCP;
+    }
+    for (int l = 1; l < L - 1; l++) {
+      p.F[l] = o;
+      o += (int64_t)pad4(n.dims[l]) * RCP;
+    }
+  } else {
+    // forward only: A_0, then hidden layers ping-pong in the delta buffers
+    p.A[0] = 0;
+    o = (int64_t)pad4(n.dims[0]) * RCP;
+  }
+  p.D0 = o;
+  o += (int64_t)pad4(n.maxd) * RCP;
+  p.D1 = o;
+  o += (int64_t)pad4(n.maxd) * RCP;
+  p.total = o;
+  return p;
 }
 
 template <typename T> struct MlpArgs {
@@ -127,10 +326,12 @@ template <typename T> struct MlpArgs {
   int nf;
   const int4 *tiles;      // (species, row0, nrows, 0)
   const int32_t *bperm;   // row -> atom
+  int RC, RCP;            // rows per chunk, padded row stride of the shared buffers
+  SmemPlan pl;            // shared-memory offsets (kernel parameter: indexed without local copies)
   double *out;            // [N][nout] atom order (forward)
   // backward
   const double *delta_out;  // [N][nout] atom order: scaled loss gradient of the outputs
-  T *gpart;               // [ntiles][stride] per-tile gradient partials (compute layout)
+  T *gpart;               // [ntiles][stride] per-tile gradient partials (gradient layout)
   // jacobian
   int jac_out;            // output index
   const double *zsd;      // z-score standard deviations (or null), length ng
@@ -139,214 +340,178 @@ template <typename T> struct MlpArgs {
   T *jacT;                // [N][nf] atom order scaled by 1/sd (forces)
 };
 
-// smem row stride (odd in 4-byte words for conflict-free per-thread rows)
-__host__ __device__ inline int row_stride(int w, int elem) {
-  int s = w;
-  if (elem == 4) s |= 1;
-  else s = (s % 2 == 0) ? s + 1 : s;
-  return s;
+// chunk rows -> X[k][r] (zero rows past the tile's end), global reads coalesced along k
+template <typename T>
+__device__ void load_features(const MlpArgs<T> &a, int64_t row0, int nrows, T *X) {
+  const int nf = a.nf;
+  for (int e = threadIdx.x; e < a.RC * nf; e += blockDim.x) {
+    const int r = e / nf, k = e - r * nf;
+    X[(int64_t)k * a.RCP + r] = r < nrows ? a.feat[(row0 + r) * nf + k] : (T)0;
+  }
 }
 
-template <typename T, int OB>
-__global__ void mlp_forward_kernel(MlpArgs<T> a) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
+template <typename T>
+__global__ void __launch_bounds__(kMlpThreads) mlp_forward_kernel(MlpArgs<T> a) {
+  extern __shared__ __align__(32) unsigned char smem_raw[];
   T *sm = reinterpret_cast<T *>(smem_raw);
   const int4 tl = a.tiles[blockIdx.x];
-  const int t = threadIdx.x;
-  if (t >= tl.z) return;
-  const int64_t row = tl.y + t;
   const NetDesc &n = a.net;
-  const T *P = a.params + (int64_t)tl.x * n.stride;
-  const int rs = row_stride(2 * n.maxw, sizeof(T));
-  T *buf = sm + (int64_t)t * rs;
-  T *A = buf, *B = buf + n.maxw;
-  const T *in = a.feat + row * a.nf;
   const int L = n.nlayer;
-  for (int l = 0; l < L - 1; l++) {
-    const int din = n.dims[l], dout = n.dims[l + 1];
-    T *dst = (l % 2 == 0) ? A : B;
-    dense_row<T, OB>(P + n.cw[l], P + n.cb[l], in, din, dout, dst);
-    if (l < L - 2)
-      for (int o = 0; o < dout; o++) dst[o] = act_f<T>(n.act, dst[o]);
-    in = dst;
-  }
+  const T *P = a.params + (int64_t)tl.x * n.pstride;
+  const SmemPlan &pl = a.pl;
   const int nout = n.dims[L - 1];
-  const int64_t atom = a.bperm[row];
-  for (int o = 0; o < nout; o++) a.out[atom * nout + o] = (double)in[o];
+  for (int c0 = 0; c0 < tl.z; c0 += a.RC) {
+    const int nrows = min(a.RC, tl.z - c0);
+    const int64_t row0 = tl.y + c0;
+    load_features(a, row0, nrows, sm + pl.A[0]);
+    __syncthreads();
+    const T *in = sm + pl.A[0];
+    for (int l = 0; l < L - 1; l++) {
+      T *dst = sm + ((l & 1) ? pl.D1 : pl.D0);
+      layer_forward<T>(in, n.dims[l], P + n.cw[l], P + n.cb[l], n.dims[l + 1], dst, nullptr,
+                       a.RC, a.RCP, l < L - 2, n.act);
+      __syncthreads();
+      in = dst;
+    }
+    for (int e = threadIdx.x; e < nrows * nout; e += blockDim.x) {
+      const int r = e / nout, o = e - r * nout;
+      a.out[(int64_t)a.bperm[row0 + r] * nout + o] = (double)in[(int64_t)o * a.RCP + r];
+    }
+    __syncthreads();
+  }
+}
+
+// Forward keeping every layer's inputs and activation derivatives of the chunk.
+template <typename T>
+__device__ void forward_keep(const MlpArgs<T> &a, const T *P, const SmemPlan &pl, T *sm) {
+  const NetDesc &n = a.net;
+  const int L = n.nlayer;
+  for (int l = 0; l < L - 2; l++) {
+    layer_forward<T>(sm + pl.A[l], n.dims[l], P + n.cw[l], P + n.cb[l], n.dims[l + 1],
+                     sm + pl.A[l + 1], sm + pl.F[l + 1], a.RC, a.RCP, true, n.act);
+    __syncthreads();
+  }
 }
 
 // Reverse-mode Jacobian of output jac_out with respect to the row's inputs.
-template <typename T, int OB>
-__global__ void mlp_jacobian_kernel(MlpArgs<T> a) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
+template <typename T>
+__global__ void __launch_bounds__(kMlpThreads) mlp_jacobian_kernel(MlpArgs<T> a) {
+  extern __shared__ __align__(32) unsigned char smem_raw[];
   T *sm = reinterpret_cast<T *>(smem_raw);
   const int4 tl = a.tiles[blockIdx.x];
-  const int t = threadIdx.x;
-  if (t >= tl.z) return;
-  const int64_t row = tl.y + t;
   const NetDesc &n = a.net;
-  const T *P = a.params + (int64_t)tl.x * n.stride;
   const int L = n.nlayer;
-  const int rs = row_stride(n.hidden_w + 2 * n.maxw, sizeof(T));
-  T *Z = sm + (int64_t)t * rs;        // z of hidden layers
-  T *D0 = Z + n.hidden_w;             // delta ping
-  T *D1 = D0 + n.maxw;                // delta pong
-  // forward, keeping z of the hidden layers
-  const T *in = a.feat + row * a.nf;
-  for (int l = 0; l < L - 2; l++) {
-    const int din = n.dims[l], dout = n.dims[l + 1];
-    T *z = Z + n.zoff[l + 1];
-    dense_row<T, OB>(P + n.cw[l], P + n.cb[l], in, din, dout, z);
-    // activations of layer l+1 are needed as the next input: keep them in D0 temporarily
-    T *act = (l % 2 == 0) ? D0 : D1;
-    for (int o = 0; o < dout; o++) act[o] = act_f<T>(n.act, z[o]);
-    in = act;
-  }
-  // delta of the output layer (linear): unit vector e_o
-  const int nout = n.dims[L - 1];
-  T *dcur = D0;
-  for (int o = 0; o < nout; o++) dcur[o] = (o == a.jac_out) ? (T)1 : (T)0;
-  T *dnext = D1;
-  for (int l = L - 2; l >= 0; l--) {
-    const int din = n.dims[l], dout = n.dims[l + 1];
-    const T *W = P + n.cw[l];
-    for (int k = 0; k < din; k++) {
-      const T *w = W + (int64_t)k * dout;
-      T s = 0;
-      for (int o = 0; o < dout; o++) s += __ldg(w + o) * dcur[o];
-      if (l >= 1) s *= act_d<T>(n.act, Z[n.zoff[l] + k]);
-      dnext[k] = s;
+  const T *P = a.params + (int64_t)tl.x * n.pstride;
+  const SmemPlan &pl = a.pl;
+  const int nout = n.dims[L - 1], nf = a.nf;
+  for (int c0 = 0; c0 < tl.z; c0 += a.RC) {
+    const int nrows = min(a.RC, tl.z - c0);
+    const int64_t row0 = tl.y + c0;
+    load_features(a, row0, nrows, sm + pl.A[0]);
+    __syncthreads();
+    forward_keep(a, P, pl, sm);
+    // delta of the (linear) output layer: the unit vector of output jac_out
+    T *dcur = sm + pl.D0, *dnext = sm + pl.D1;
+    for (int e = threadIdx.x; e < nout * a.RC; e += blockDim.x) {
+      const int o = e / a.RC, r = e - o * a.RC;
+      dcur[(int64_t)o * a.RCP + r] = (o == a.jac_out) ? (T)1 : (T)0;
     }
-    T *tmp = dcur;
-    dcur = dnext;
-    dnext = tmp;
-  }
-  const int64_t atom = a.bperm[row];
-  for (int k = 0; k < a.nf; k++) {
-    const T v = dcur[k];
-    if (a.jac64) a.jac64[atom * a.nf + k] = (double)v;
-    if (a.jacT) {
-      T s = v;
-      if (a.zsd && k < a.ng) {
-        const double sd = a.zsd[k];
-        if (sd >= 1e-08) s = (T)((double)v / sd);
+    __syncthreads();
+    for (int l = L - 2; l >= 1; l--) {
+      layer_backward<T>(dcur, n.dims[l + 1], P + n.ct[l], n.dims[l], sm + pl.F[l], dnext, a.RC,
+                        a.RCP);
+      __syncthreads();
+      T *tmp = dcur;
+      dcur = dnext;
+      dnext = tmp;
+    }
+    // input layer: no activation; the result replaces the features of the chunk
+    T *J = sm + pl.A[0];
+    layer_backward<T>(dcur, n.dims[1], P + n.ct[0], n.dims[0], nullptr, J, a.RC, a.RCP);
+    __syncthreads();
+    for (int e = threadIdx.x; e < nrows * nf; e += blockDim.x) {
+      const int r = e / nf, k = e - r * nf;
+      const T v = J[(int64_t)k * a.RCP + r];
+      const int64_t atom = a.bperm[row0 + r];
+      if (a.jac64) a.jac64[atom * nf + k] = (double)v;
+      if (a.jacT) {
+        T s = v;
+        if (a.zsd && k < a.ng) {
+          const double sd = a.zsd[k];
+          if (sd >= 1e-08) s = (T)((double)v / sd);
+        }
+        a.jacT[atom * nf + k] = s;
       }
-      a.jacT[atom * a.nf + k] = s;
     }
+    __syncthreads();
   }
 }
 
-// Forward + backward of a tile; per-tile gradient partials in the compute layout.
-template <typename T, int OB>
-__global__ void mlp_backward_kernel(MlpArgs<T> a) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
+// Forward + backward of a tile; per-tile gradient partials in the gradient layout.
+template <typename T>
+__global__ void __launch_bounds__(kMlpThreads) mlp_backward_kernel(MlpArgs<T> a) {
+  extern __shared__ __align__(32) unsigned char smem_raw[];
   T *sm = reinterpret_cast<T *>(smem_raw);
   const int4 tl = a.tiles[blockIdx.x];
-  const int t = threadIdx.x;
-  const int R = blockDim.x;
   const NetDesc &n = a.net;
   const int L = n.nlayer;
-  const T *P = a.params + (int64_t)tl.x * n.stride;
-  // per-row scratch: z (hidden), then delta of every layer >= 1 (sum of widths 1..L-1)
-  int dw_total = 0;
-  for (int l = 1; l < L; l++) dw_total += n.dims[l];
-  const int rs = row_stride(n.hidden_w + dw_total, sizeof(T));
-  T *row_base = sm + (int64_t)t * rs;
-  T *Z = row_base;
-  T *Dl = Z + n.hidden_w;             // deltas, layer l at doff(l)
-  auto doff = [&](int l) {
-    int o = 0;
-    for (int m = 1; m < l; m++) o += n.dims[m];
-    return o;
-  };
-  const bool active = t < tl.z;
-  const int64_t row = tl.y + (active ? t : 0);
-  if (active) {
-    const T *in = a.feat + row * a.nf;
-    for (int l = 0; l < L - 2; l++) {
-      const int din = n.dims[l], dout = n.dims[l + 1];
-      T *z = Z + n.zoff[l + 1];
-      dense_row<T, OB>(P + n.cw[l], P + n.cb[l], in, din, dout, z);
-      // next input: activations, kept in the delta area of layer l+1 until the backward
-      T *actbuf = Dl + doff(l + 1);
-      for (int o = 0; o < dout; o++) actbuf[o] = act_f<T>(n.act, z[o]);
-      in = actbuf;
-    }
-    // output deltas (linear output layer): scaled loss gradients
-    const int nout = n.dims[L - 1];
-    const int64_t atom = a.bperm[row];
-    T *dL = Dl + doff(L - 1);
-    for (int o = 0; o < nout; o++) dL[o] = (T)a.delta_out[atom * nout + o];
-    // back-propagate: delta_l = (W_l delta_{l+1}) * f'(z_l) for hidden layers l
-    for (int l = L - 2; l >= 1; l--) {
-      const int din = n.dims[l], dout = n.dims[l + 1];
-      const T *W = P + n.cw[l];
-      const T *dn = Dl + doff(l + 1);
-      T *dc = Dl + doff(l);
-      for (int k = 0; k < din; k++) {
-        const T *w = W + (int64_t)k * dout;
-        T s = 0;
-        for (int o = 0; o < dout; o++) s += __ldg(w + o) * dn[o];
-        dc[k] = s * act_d<T>(n.act, Z[n.zoff[l] + k]);
-      }
-    }
-  } else {
-    // inactive rows contribute zero deltas
-    for (int q = 0; q < dw_total; q++) Dl[q] = (T)0;
-    for (int q = 0; q < n.hidden_w; q++) Z[q] = (T)0;
-  }
-  __syncthreads();
-  // weight gradients: dW_l[k][o] = sum_rows a_l[row][k] * delta_{l+1}[row][o];
-  // bias gradients db_{l+1}[o] = sum_rows delta_{l+1}[row][o]
+  const T *P = a.params + (int64_t)tl.x * n.pstride;
   T *G = a.gpart + (int64_t)blockIdx.x * n.stride;
-  const int nrows = tl.z;
-  for (int l = 0; l < L - 1; l++) {
-    const int din = n.dims[l], dout = n.dims[l + 1];
-    const int dof = doff(l + 1);
-    const int64_t nw = (int64_t)din * dout;
-    for (int64_t e = t; e < nw + dout; e += R) {
-      T acc = 0;
-      if (e < nw) {
-        const int k = (int)(e / dout), o = (int)(e % dout);
-        for (int r = 0; r < nrows; r++) {
-          const T *rb = sm + (int64_t)r * rs;
-          T ak;
-          if (l == 0) ak = a.feat[(tl.y + r) * (int64_t)a.nf + k];
-          else ak = act_f<T>(n.act, rb[n.zoff[l] + k]);
-          acc += ak * rb[n.hidden_w + dof + o];
-        }
-        G[n.cw[l] + e] = acc;
-      } else {
-        const int o = (int)(e - nw);
-        for (int r = 0; r < nrows; r++) acc += sm[(int64_t)r * rs + n.hidden_w + dof + o];
-        G[n.cb[l] + o] = acc;
-      }
+  const SmemPlan &pl = a.pl;
+  const int nout = n.dims[L - 1];
+  for (int c0 = 0; c0 < tl.z; c0 += a.RC) {
+    const int nrows = min(a.RC, tl.z - c0);
+    const int64_t row0 = tl.y + c0;
+    load_features(a, row0, nrows, sm + pl.A[0]);
+    __syncthreads();
+    forward_keep(a, P, pl, sm);
+    // output deltas (linear output layer): scaled loss gradients; zero past the tile's end
+    T *dcur = sm + pl.D0, *dnext = sm + pl.D1;
+    for (int e = threadIdx.x; e < nout * a.RC; e += blockDim.x) {
+      const int o = e / a.RC, r = e - o * a.RC;
+      dcur[(int64_t)o * a.RCP + r] =
+          r < nrows ? (T)a.delta_out[(int64_t)a.bperm[row0 + r] * nout + o] : (T)0;
+    }
+    __syncthreads();
+    for (int l = L - 2; l >= 0; l--) {
+      layer_wgrad<T>(sm + pl.A[l], n.dims[l], dcur, n.dims[l + 1], G + n.cw[l], G + n.cb[l],
+                     a.RC, a.RCP, c0 == 0);
+      if (l >= 1)
+        layer_backward<T>(dcur, n.dims[l + 1], P + n.ct[l], n.dims[l], sm + pl.F[l], dnext,
+                          a.RC, a.RCP);
+      __syncthreads();
+      T *tmp = dcur;
+      dcur = dnext;
+      dnext = tmp;
     }
   }
 }
 
 // FP64 sum of the per-tile partials of every species, written in the reference layout.
 template <typename T>
-__global__ void grad_reduce_kernel(const T *gpart, const int4 *tiles, const int64_t *sp_tile0,
-                                   NetDesc net, const int64_t *ref_of_compute, int64_t nparams,
+__global__ void grad_reduce_kernel(const T *gpart, const int64_t *sp_tile0, NetDesc net,
+                                   const int64_t *ref_of_compute, int64_t nparams,
                                    double *grad64) {
   const int s = blockIdx.y;
   const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= net.stride) return;
+  const int64_t ref = ref_of_compute[q];
+  if (ref < 0) return;
   const int64_t t0 = sp_tile0[s], t1 = sp_tile0[s + 1];
   double acc = 0.0;
   for (int64_t t = t0; t < t1; t++) acc += (double)gpart[t * net.stride + q];
-  grad64[(int64_t)s * nparams + ref_of_compute[q]] = acc;
+  grad64[(int64_t)s * nparams + ref] = acc;
 }
 
-// reference layout (FP64 master) -> compute layout (T)
+// reference layout (FP64 master) -> compute layout (T); padding entries are zero
 template <typename T>
 __global__ void params_convert_kernel(const double *p64, T *pc, NetDesc net,
                                       const int64_t *ref_of_compute, int64_t nparams, int nsp) {
   const int s = blockIdx.y;
   const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (q >= net.stride || s >= nsp) return;
-  pc[(int64_t)s * net.stride + q] = (T)p64[(int64_t)s * nparams + ref_of_compute[q]];
+  if (q >= net.pstride || s >= nsp) return;
+  const int64_t ref = ref_of_compute[q];
+  pc[(int64_t)s * net.pstride + q] = ref < 0 ? (T)0 : (T)p64[(int64_t)s * nparams + ref];
 }
 
 struct Layouts {
@@ -359,51 +524,48 @@ Layouts make_layouts(fnetg_ctx *ctx) {
   NetDesc &n = Lo.net;
   n.nlayer = ctx->nlayer;
   n.act = ctx->act;
-  n.maxw = 1;
+  n.maxd = 1;
   for (int l = 0; l < ctx->nlayer; l++) {
     n.dims[l] = ctx->dims[l];
-    n.maxw = std::max(n.maxw, ctx->dims[l]);
+    if (l >= 1) n.maxd = std::max(n.maxd, ctx->dims[l]);
   }
   int64_t ind = 0;
-  n.hidden_w = 0;
   for (int l = 0; l < ctx->nlayer - 1; l++) {
     n.cw[l] = ind;
-    ind += (int64_t)ctx->dims[l] * ctx->dims[l + 1];
+    ind += (int64_t)ctx->dims[l] * pad4(ctx->dims[l + 1]);
     n.cb[l] = ind;
-    ind += ctx->dims[l + 1];
+    ind += pad4(ctx->dims[l + 1]);
   }
   n.stride = ind;
-  for (int l = 1; l < ctx->nlayer - 1; l++) {
-    n.zoff[l] = n.hidden_w;
-    n.hidden_w += ctx->dims[l];
+  for (int l = 0; l < ctx->nlayer - 1; l++) {
+    n.ct[l] = ind;
+    ind += (int64_t)ctx->dims[l + 1] * pad4(ctx->dims[l]);
   }
-  Lo.ref_of_compute.assign(n.stride, 0);
+  n.pstride = ind;
+  Lo.ref_of_compute.assign(n.pstride, -1);
   for (int l = 0; l < ctx->nlayer - 1; l++) {
     const int din = ctx->dims[l], dout = ctx->dims[l + 1];
     for (int k = 0; k < din; k++)
-      for (int o = 0; o < dout; o++)
-        Lo.ref_of_compute[n.cw[l] + (int64_t)k * dout + o] = ctx->woff[l] + k + (int64_t)din * o;
+      for (int o = 0; o < dout; o++) {
+        const int64_t ref = ctx->woff[l] + k + (int64_t)din * o;
+        Lo.ref_of_compute[n.cw[l] + (int64_t)k * pad4(dout) + o] = ref;
+        Lo.ref_of_compute[n.ct[l] + (int64_t)o * pad4(din) + k] = ref;
+      }
     for (int o = 0; o < dout; o++) Lo.ref_of_compute[n.cb[l] + o] = ctx->boff[l + 1] + o;
   }
   return Lo;
 }
 
-
-template <typename T> constexpr int out_block() { return sizeof(T) == 4 ? 8 : 4; }
-
-template <typename T> size_t fwd_smem(const NetDesc &n, int R) {
-  return sizeof(T) * (size_t)R * row_stride(2 * n.maxw, sizeof(T));
-}
-template <typename T> size_t jac_smem(const NetDesc &n, int R) {
-  return sizeof(T) * (size_t)R * row_stride(n.hidden_w + 2 * n.maxw, sizeof(T));
-}
-template <typename T> size_t bwd_smem(const NetDesc &n, int R) {
-  int dw_total = 0;
-  for (int l = 1; l < n.nlayer; l++) dw_total += n.dims[l];
-  return sizeof(T) * (size_t)R * row_stride(n.hidden_w + dw_total, sizeof(T));
+// Rows per chunk: the tile's rows, halved until the chunk's buffers leave room for two CTAs
+// per SM (or reach four rows).
+template <typename T> int chunk_rows(const NetDesc &n, int tile_rows, bool keep_all) {
+  int RC = pad4(tile_rows);
+  while (RC > 4 && sizeof(T) * smem_plan(n, RC + 4, keep_all).total > 100 * 1024) RC >>= 1;
+  return RC;
 }
 
-template <typename T> int prepare(fnetg_ctx *ctx, Layouts &Lo, MlpArgs<T> &a) {
+template <typename T> int prepare(fnetg_ctx *ctx, Layouts &Lo, MlpArgs<T> &a, bool keep_all,
+                                  size_t &smem) {
   Lo = make_layouts(ctx);
   a = MlpArgs<T>{};
   a.net = Lo.net;
@@ -412,25 +574,26 @@ template <typename T> int prepare(fnetg_ctx *ctx, Layouts &Lo, MlpArgs<T> &a) {
   a.nf = ctx->nf;
   a.tiles = ctx->d_tiles.as<int4>();
   a.bperm = ctx->d_bperm.as<int32_t>();
+  a.RC = chunk_rows<T>(Lo.net, ctx->tile_rows, keep_all);
+  a.RCP = a.RC + 4;
+  a.pl = smem_plan(Lo.net, a.RCP, keep_all);
+  smem = sizeof(T) * (size_t)a.pl.total;
+  FNETG_CHECK(smem <= 227 * 1024, FNETG_E_UNSUPPORTED, "network too wide for shared memory");
   return FNETG_OK;
 }
 
 template <typename K> int set_smem(fnetg_ctx *ctx, K kernel, size_t bytes) {
-  FNETG_CHECK(bytes <= 227 * 1024, FNETG_E_UNSUPPORTED, "network too wide for shared memory");
   FNETG_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
   return FNETG_OK;
 }
 
 template <typename T> int do_params(fnetg_ctx *ctx) {
-  Layouts Lo;
-  MlpArgs<T> a;
-  int rc = prepare<T>(ctx, Lo, a);
-  if (rc) return rc;
-  FNETG_CUDA(ctx->d_ref_of_compute.ensure(sizeof(int64_t) * std::max<int64_t>(Lo.net.stride, 1)));
+  const Layouts Lo = make_layouts(ctx);
+  FNETG_CUDA(ctx->d_ref_of_compute.ensure(sizeof(int64_t) * std::max<int64_t>(Lo.net.pstride, 1)));
   FNETG_CUDA(cudaMemcpy(ctx->d_ref_of_compute.p, Lo.ref_of_compute.data(),
-                        sizeof(int64_t) * Lo.net.stride, cudaMemcpyHostToDevice));
-  FNETG_CUDA(ctx->d_params.ensure(sizeof(T) * ctx->nsp * Lo.net.stride));
-  dim3 grid(ceil_div(Lo.net.stride, 256), ctx->nsp);
+                        sizeof(int64_t) * Lo.net.pstride, cudaMemcpyHostToDevice));
+  FNETG_CUDA(ctx->d_params.ensure(sizeof(T) * ctx->nsp * Lo.net.pstride));
+  dim3 grid(ceil_div(Lo.net.pstride, 256), ctx->nsp);
   LaunchScope ls(ctx, "params");
   params_convert_kernel<T><<<grid, 256, 0, ctx->stream>>>(
       ctx->d_params64.as<double>(), ctx->d_params.as<T>(), Lo.net,
@@ -442,18 +605,17 @@ template <typename T> int do_params(fnetg_ctx *ctx) {
 template <typename T> int do_predict(fnetg_ctx *ctx) {
   Layouts Lo;
   MlpArgs<T> a;
-  int rc = prepare<T>(ctx, Lo, a);
+  size_t sm = 0;
+  int rc = prepare<T>(ctx, Lo, a, false, sm);
   if (rc) return rc;
   const int nout = ctx->dims.back();
   FNETG_CUDA(ctx->d_out.ensure(sizeof(double) * std::max<int64_t>(ctx->N, 1) * nout));
   a.out = ctx->d_out.as<double>();
   if (ctx->ntiles == 0) return FNETG_OK;
-  const int R = ctx->tile_rows;
-  const size_t sm = fwd_smem<T>(Lo.net, R);
-  rc = set_smem(ctx, mlp_forward_kernel<T, out_block<T>()>, sm);
+  rc = set_smem(ctx, mlp_forward_kernel<T>, sm);
   if (rc) return rc;
   LaunchScope ls(ctx, "mlp_forward");
-  mlp_forward_kernel<T, out_block<T>()><<<(unsigned)ctx->ntiles, R, sm, ctx->stream>>>(a);
+  mlp_forward_kernel<T><<<(unsigned)ctx->ntiles, kMlpThreads, sm, ctx->stream>>>(a);
   FNETG_CUDA(cudaGetLastError());
   return FNETG_OK;
 }
@@ -461,7 +623,8 @@ template <typename T> int do_predict(fnetg_ctx *ctx) {
 template <typename T> int do_jacobian(fnetg_ctx *ctx, int o, void *dstT) {
   Layouts Lo;
   MlpArgs<T> a;
-  int rc = prepare<T>(ctx, Lo, a);
+  size_t sm = 0;
+  int rc = prepare<T>(ctx, Lo, a, true, sm);
   if (rc) return rc;
   const int nf = ctx->nf;
   a.jac_out = o;
@@ -474,12 +637,10 @@ template <typename T> int do_jacobian(fnetg_ctx *ctx, int o, void *dstT) {
     a.jac64 = ctx->d_jac.as<double>();
   }
   if (ctx->ntiles == 0) return FNETG_OK;
-  const int R = ctx->tile_rows;
-  const size_t sm = jac_smem<T>(Lo.net, R);
-  rc = set_smem(ctx, mlp_jacobian_kernel<T, out_block<T>()>, sm);
+  rc = set_smem(ctx, mlp_jacobian_kernel<T>, sm);
   if (rc) return rc;
   LaunchScope ls(ctx, "mlp_jacobian");
-  mlp_jacobian_kernel<T, out_block<T>()><<<(unsigned)ctx->ntiles, R, sm, ctx->stream>>>(a);
+  mlp_jacobian_kernel<T><<<(unsigned)ctx->ntiles, kMlpThreads, sm, ctx->stream>>>(a);
   FNETG_CUDA(cudaGetLastError());
   return FNETG_OK;
 }
@@ -487,7 +648,8 @@ template <typename T> int do_jacobian(fnetg_ctx *ctx, int o, void *dstT) {
 template <typename T> int do_backward(fnetg_ctx *ctx) {
   Layouts Lo;
   MlpArgs<T> a;
-  int rc = prepare<T>(ctx, Lo, a);
+  size_t sm = 0;
+  int rc = prepare<T>(ctx, Lo, a, true, sm);
   if (rc) return rc;
   a.delta_out = ctx->d_lossgrad.as<double>();
   FNETG_CUDA(ctx->d_gpart.ensure(sizeof(T) * std::max<int64_t>(ctx->ntiles, 1) * Lo.net.stride));
@@ -496,19 +658,17 @@ template <typename T> int do_backward(fnetg_ctx *ctx) {
   FNETG_CUDA(cudaMemsetAsync(ctx->d_grad64.p, 0, sizeof(double) * ctx->nsp * ctx->nparams,
                              ctx->stream));
   if (ctx->ntiles > 0) {
-    const int R = ctx->tile_rows;
-    const size_t sm = bwd_smem<T>(Lo.net, R);
-    rc = set_smem(ctx, mlp_backward_kernel<T, out_block<T>()>, sm);
+    rc = set_smem(ctx, mlp_backward_kernel<T>, sm);
     if (rc) return rc;
     LaunchScope ls(ctx, "mlp_backward");
-    mlp_backward_kernel<T, out_block<T>()><<<(unsigned)ctx->ntiles, R, sm, ctx->stream>>>(a);
+    mlp_backward_kernel<T><<<(unsigned)ctx->ntiles, kMlpThreads, sm, ctx->stream>>>(a);
     FNETG_CUDA(cudaGetLastError());
   }
   {
     dim3 grid(ceil_div(Lo.net.stride, 256), ctx->nsp);
     LaunchScope ls(ctx, "reduce");
     grad_reduce_kernel<T><<<grid, 256, 0, ctx->stream>>>(
-        ctx->d_gpart.as<T>(), ctx->d_tiles.as<int4>(), ctx->d_sp_tile0.as<int64_t>(), Lo.net,
+        ctx->d_gpart.as<T>(), ctx->d_sp_tile0.as<int64_t>(), Lo.net,
         ctx->d_ref_of_compute.as<int64_t>(), ctx->nparams, ctx->d_grad64.as<double>());
     FNETG_CUDA(cudaGetLastError());
   }

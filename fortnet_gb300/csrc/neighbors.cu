@@ -24,10 +24,12 @@ struct NbArgs {
   const int64_t *off;
   const int32_t *astruct;
   const double *coords;
-  const V4<float> *cf;
+  const V4<float> *cf;     // [N] high parts of the relative float coordinates
+  const V4<float> *cl;     // [N] low parts
   const double *lat;
   const int64_t *img_off;  // [S+1] per-structure range into the image table
   const V4<double> *imgs;  // cell vectors (x, y, z, packed n1/n2/n3) in the iterator's order
+  const V4<float> *imgf;   // [2 * images] float high parts (w: packed n1/n2/n3), low parts
   const float *bbox;      // [S*6] lo, hi (relative frame)
   int64_t natoms;
   double rc2;             // rcut*rcut (exact decision)
@@ -61,6 +63,21 @@ __device__ __forceinline__ double exact_d2(const double *ci, const double *cj, c
   return s;
 }
 
+// the reference's FP64 squared distance of centre ci and atom j shifted by image img
+// (-1: central cell); d receives the displacement
+__device__ __forceinline__ double exact_pair(const NbArgs &a, const double *ci, int64_t j,
+                                             int64_t img, double (&d)[3]) {
+  double cv[3] = {0.0, 0.0, 0.0};
+  if (img >= 0) {
+    const V4<double> iv = a.imgs[img];
+    cv[0] = iv.x;
+    cv[1] = iv.y;
+    cv[2] = iv.z;
+  }
+  const double cj[3] = {a.coords[3 * j], a.coords[3 * j + 1], a.coords[3 * j + 2]};
+  return exact_d2(ci, cj, cv, d);
+}
+
 __device__ __forceinline__ void cell_vector(const double *L, int n1, int n2, int n3, double *cv) {
   // matmul(latVecs, n) summed in index order
   for (int c = 0; c < 3; c++) {
@@ -69,6 +86,24 @@ __device__ __forceinline__ void cell_vector(const double *L, int n1, int n2, int
     v = __dadd_rn(v, __dmul_rn(L[c + 6], (double)n3));
     cv[c] = v;
   }
+}
+
+// (a + b) - c for a = ah + al, b = bh + bl, c = ch + cl, each part a float: error-free
+// transformations (Knuth's TwoSum) of the two high-part operations plus the low parts, so the
+// result is the float rounding of the double-float value, all on the FP32 pipe.
+__device__ __forceinline__ float two_sum(float a, float b, float &err) {
+  const float s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  err = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+  return s;
+}
+
+__device__ __forceinline__ float disp_df(float ah, float al, float bh, float bl, float ch,
+                                         float cl) {
+  float e1, e2;
+  const float s = two_sum(ah, bh, e1);
+  const float t = two_sum(s, -ch, e2);
+  return __fadd_rn(t, __fadd_rn(__fadd_rn(e1, e2), __fsub_rn(__fadd_rn(al, bl), cl)));
 }
 
 template <typename T, bool kFill>
@@ -85,6 +120,7 @@ __global__ void __launch_bounds__(256) nb_kernel(NbArgs a) {
     const int il = (int)(i - a0);
     const double ci[3] = {a.coords[3 * i], a.coords[3 * i + 1], a.coords[3 * i + 2]};
     const V4<float> cif = a.cf[i];
+    const V4<float> cil = a.cl[i];
     int64_t wpos = 0;
     if (kFill) wpos = a.poff[i];
     int64_t cnt = 0;
@@ -92,51 +128,44 @@ __global__ void __launch_bounds__(256) nb_kernel(NbArgs a) {
     const int64_t im0 = a.img_off[s], im1 = a.img_off[s + 1];
     // image -1 is the central cell, then the lattice points of the table (n1 outer .. n3 inner)
     for (int64_t img = im0 - 1; img < im1; img++) {
-      int n1 = 0, n2 = 0, n3 = 0;
-      double cv[3] = {0.0, 0.0, 0.0};
+      V4<float> ch{0.f, 0.f, 0.f, 0.f}, cvl{0.f, 0.f, 0.f, 0.f};
+      uint32_t packed = 0;
       int tstart = 1, tcount = n - 1;
       if (img >= im0) {
-        const V4<double> iv = a.imgs[img];
-        cv[0] = iv.x;
-        cv[1] = iv.y;
-        cv[2] = iv.z;
-        const uint32_t packed = (uint32_t)__double_as_longlong(iv.w);
-        n1 = (int8_t)(packed & 0xff);
-        n2 = (int8_t)((packed >> 8) & 0xff);
-        n3 = (int8_t)((packed >> 16) & 0xff);
+        ch = a.imgf[2 * img];
+        packed = __float_as_uint(ch.w);
         tstart = 0;
         tcount = n;
         // skip the image when the shifted bounding box is out of reach
-        float dd = 0.f;
-        const float cvf[3] = {(float)cv[0], (float)cv[1], (float)cv[2]};
         const float p[3] = {cif.x, cif.y, cif.z};
+        const float cvf[3] = {ch.x, ch.y, ch.z};
+        float dd = 0.f;
         for (int c = 0; c < 3; c++) {
           const float lo = bb[c] + cvf[c], hi = bb[3 + c] + cvf[c];
           const float e = p[c] < lo ? lo - p[c] : (p[c] > hi ? p[c] - hi : 0.f);
           dd += e * e;
         }
         if (dd > a.rc2_hi) continue;
+        if (kFill && !a.exact_geometry) cvl = a.imgf[2 * img + 1];
       }
-      const float cvf0 = (float)cv[0], cvf1 = (float)cv[1], cvf2 = (float)cv[2];
       for (int base = 0; base < tcount; base += 32) {
         bool ok = false;
         int jl = 0;
         float df = 0.f;
+        V4<float> cjf{0.f, 0.f, 0.f, 0.f};
         if (base + lane < tcount) {
           jl = il + tstart + base + lane;
           if (jl >= n) jl -= n;
-          const V4<float> cjf = a.cf[a0 + jl];
-          const float e0 = (cjf.x + cvf0) - cif.x, e1 = (cjf.y + cvf1) - cif.y,
-                      e2 = (cjf.z + cvf2) - cif.z;
+          cjf = a.cf[a0 + jl];
+          const float e0 = (cjf.x + ch.x) - cif.x, e1 = (cjf.y + ch.y) - cif.y,
+                      e2 = (cjf.z + ch.z) - cif.z;
           df = e0 * e0 + e1 * e1 + e2 * e2;
           if (df <= a.rc2_lo) {
             ok = true;
           } else if (df <= a.rc2_hi) {
             // within the float error bound of the cutoff: the reference's FP64 decision
-            const int64_t j = a0 + jl;
-            const double cj[3] = {a.coords[3 * j], a.coords[3 * j + 1], a.coords[3 * j + 2]};
             double d[3];
-            ok = exact_d2(ci, cj, cv, d) <= a.rc2;
+            ok = exact_pair(a, ci, a0 + jl, img >= im0 ? img : -1, d) <= a.rc2;
           }
         }
         const unsigned m = __ballot_sync(0xffffffffu, ok);
@@ -144,37 +173,41 @@ __global__ void __launch_bounds__(256) nb_kernel(NbArgs a) {
           const int64_t j = a0 + jl;
           const int64_t q = wpos + cnt + __popc(m & ((1u << lane) - 1u));
           a.pj[q] = (int32_t)j;
-          const double cj[3] = {a.coords[3 * j], a.coords[3 * j + 1], a.coords[3 * j + 2]};
-          double d[3];
           uint32_t mask = 0;
           V4<T> v;
           if (a.exact_geometry || a.d2out) {
-            const double dist2 = exact_d2(ci, cj, cv, d);
+            double d[3];
+            const double dist2 = exact_pair(a, ci, j, img >= im0 ? img : -1, d);
             for (int c = 0; c < a.nrcls; c++)
               if (dist2 <= __dmul_rn(a.rcls[c], a.rcls[c])) mask |= 1u << c;
             if (a.d2out) a.d2out[q] = dist2;
+            v.x = (T)d[0];
+            v.y = (T)d[1];
+            v.z = (T)d[2];
             v.w = (T)sqrt(dist2);
           } else {
-            // displacement from the FP64 coordinates (accurate), distance in float
-            d[0] = (cj[0] + cv[0]) - ci[0];
-            d[1] = (cj[1] + cv[1]) - ci[1];
-            d[2] = (cj[2] + cv[2]) - ci[2];
-            const float fx = (float)d[0], fy = (float)d[1], fz = (float)d[2];
+            // displacement in double-float arithmetic from the split coordinates, rounded
+            // once to float; distance in float
+            const V4<float> cjl = a.cl[j];
+            const float fx = disp_df(cjf.x, cjl.x, ch.x, cvl.x, cif.x, cil.x);
+            const float fy = disp_df(cjf.y, cjl.y, ch.y, cvl.y, cif.y, cil.y);
+            const float fz = disp_df(cjf.z, cjl.z, ch.z, cvl.z, cif.z, cil.z);
+            v.x = (T)fx;
+            v.y = (T)fy;
+            v.z = (T)fz;
             v.w = (T)sqrtf(fx * fx + fy * fy + fz * fz);
             for (int c = 0; c < a.nrcls; c++) {
               if (df <= a.rcls2_lo[c]) {
                 mask |= 1u << c;
               } else if (df <= a.rcls2_hi[c]) {
-                double e[3];
-                if (exact_d2(ci, cj, cv, e) <= __dmul_rn(a.rcls[c], a.rcls[c])) mask |= 1u << c;
+                double d[3];
+                if (exact_pair(a, ci, j, img >= im0 ? img : -1, d) <=
+                    __dmul_rn(a.rcls[c], a.rcls[c]))
+                  mask |= 1u << c;
               }
             }
           }
-          a.pmeta[q] = ((uint32_t)(uint8_t)(int8_t)n1) | ((uint32_t)(uint8_t)(int8_t)n2 << 8) |
-                       ((uint32_t)(uint8_t)(int8_t)n3 << 16) | (mask << 24);
-          v.x = (T)d[0];
-          v.y = (T)d[1];
-          v.z = (T)d[2];
+          a.pmeta[q] = (packed & 0xffffffu) | (mask << 24);
           reinterpret_cast<V4<T> *>(a.rij)[q] = v;
         }
         cnt += __popc(m);
@@ -264,7 +297,7 @@ __global__ void scan_add_kernel(int64_t *out, const int64_t *sums, int64_t n, in
 // Float copies of the coordinates relative to each structure's bounding-box corner (the float
 // pre-filter's rounding then does not depend on where a structure sits) and the boxes.
 __global__ void prep_coords_kernel(const double *coords, const int64_t *off, V4<float> *cf,
-                                   float *bbox, int S) {
+                                   V4<float> *cl, float *bbox, int S) {
   __shared__ double lo[3][256], hi[3][256];
   const int s = blockIdx.x;
   if (s >= S) return;
@@ -290,9 +323,16 @@ __global__ void prep_coords_kernel(const double *coords, const int64_t *off, V4<
   }
   double ref[3];
   for (int c = 0; c < 3; c++) ref[c] = (double)(float)lo[c][0];
-  for (int64_t a = a0 + threadIdx.x; a < a1; a += blockDim.x)
-    cf[a] = V4<float>{(float)(coords[3 * a] - ref[0]), (float)(coords[3 * a + 1] - ref[1]),
-                      (float)(coords[3 * a + 2] - ref[2]), 0.f};
+  for (int64_t a = a0 + threadIdx.x; a < a1; a += blockDim.x) {
+    // high part = float rounding of the FP64 relative coordinate, low part = float rounding
+    // of the remainder: together they hold the relative coordinate to about 2^-48 of itself
+    const double r0 = coords[3 * a] - ref[0], r1 = coords[3 * a + 1] - ref[1],
+                 r2 = coords[3 * a + 2] - ref[2];
+    const float h0 = (float)r0, h1 = (float)r1, h2 = (float)r2;
+    cf[a] = V4<float>{h0, h1, h2, 0.f};
+    cl[a] = V4<float>{(float)(r0 - (double)h0), (float)(r1 - (double)h1), (float)(r2 - (double)h2),
+                      0.f};
+  }
   if (threadIdx.x == 0)
     for (int c = 0; c < 3; c++) {
       bbox[6 * s + c] = 0.f;
@@ -307,7 +347,8 @@ int prepare_coords(fnetg_ctx *ctx) {
   LaunchScope ls(ctx, "coords");
   prep_coords_kernel<<<ctx->S, 256, 0, ctx->stream>>>(
       ctx->d_coords.as<double>(), ctx->d_off.as<int64_t>(), ctx->d_coordsf.as<V4<float>>(),
-      ctx->d_bbox.as<float>(), ctx->S);
+      ctx->d_coordsf.as<V4<float>>() + std::max<int64_t>(ctx->N, 1), ctx->d_bbox.as<float>(),
+      ctx->S);
   FNETG_CUDA(cudaGetLastError());
   return FNETG_OK;
 }
@@ -351,6 +392,7 @@ int run_neighbors(fnetg_ctx *ctx, double rcut) {
   // origin excluded) with the cell vector matmul(latVecs, n) summed in index order
   std::vector<int64_t> img_off(S + 1, 0);
   std::vector<V4<double>> imgs;
+  std::vector<V4<float>> imgs_f;
   for (int s = 0; s < S; s++) {
     img_off[s] = (int64_t)imgs.size();
     if (!ctx->h_periodic[s]) continue;
@@ -373,16 +415,30 @@ int run_neighbors(fnetg_ctx *ctx, double rcut) {
           double w;
           std::memcpy(&w, &packed, sizeof w);
           imgs.push_back(V4<double>{cv[0], cv[1], cv[2], w});
+          float h[3], l[3];
+          for (int c = 0; c < 3; c++) {
+            h[c] = (float)cv[c];
+            l[c] = (float)(cv[c] - (double)h[c]);
+          }
+          float pw;
+          const uint32_t p32 = (uint32_t)packed;
+          std::memcpy(&pw, &p32, sizeof pw);
+          imgs_f.push_back(V4<float>{h[0], h[1], h[2], pw});
+          imgs_f.push_back(V4<float>{l[0], l[1], l[2], 0.f});
         }
   }
   img_off[S] = (int64_t)imgs.size();
   FNETG_CUDA(ctx->d_img_off.ensure(sizeof(int64_t) * (S + 1)));
   FNETG_CUDA(ctx->d_imgs.ensure(sizeof(V4<double>) * std::max<size_t>(imgs.size(), 1)));
+  FNETG_CUDA(ctx->d_imgs_f.ensure(sizeof(V4<float>) * std::max<size_t>(imgs_f.size(), 1)));
   FNETG_CUDA(cudaMemcpyAsync(ctx->d_img_off.p, img_off.data(), sizeof(int64_t) * (S + 1),
                              cudaMemcpyHostToDevice, ctx->stream));
-  if (!imgs.empty())
+  if (!imgs.empty()) {
     FNETG_CUDA(cudaMemcpyAsync(ctx->d_imgs.p, imgs.data(), sizeof(V4<double>) * imgs.size(),
                                cudaMemcpyHostToDevice, ctx->stream));
+    FNETG_CUDA(cudaMemcpyAsync(ctx->d_imgs_f.p, imgs_f.data(), sizeof(V4<float>) * imgs_f.size(),
+                               cudaMemcpyHostToDevice, ctx->stream));
+  }
   FNETG_CUDA(ctx->d_pcount.ensure(sizeof(int64_t) * std::max<int64_t>(N, 1)));
   FNETG_CUDA(ctx->d_poff.ensure(sizeof(int64_t) * (N + 1)));
   FNETG_CUDA(ctx->d_maxp.ensure(sizeof(int) * 4));
@@ -398,6 +454,8 @@ int run_neighbors(fnetg_ctx *ctx, double rcut) {
   a.astruct = ctx->d_atom_struct.as<int32_t>();
   a.coords = ctx->d_coords.as<double>();
   a.cf = ctx->d_coordsf.as<V4<float>>();
+  a.cl = ctx->d_coordsf.as<V4<float>>() + std::max<int64_t>(N, 1);
+  a.imgf = ctx->d_imgs_f.as<V4<float>>();
   a.img_off = ctx->d_img_off.as<int64_t>();
   a.imgs = ctx->d_imgs.as<V4<double>>();
   a.bbox = ctx->d_bbox.as<float>();
