@@ -110,12 +110,17 @@ __global__ void __launch_bounds__(256) acsf_kernel(TileArgs<T> a) {
           // domain of acos
           T c = dot / (vp.w * vq.w + (T)1e-13);
           c = c > (T)1 ? (T)1 : (c < (T)-1 ? (T)-1 : c);
+          // j = k: the reference's 1 - cos is ~1e-13 / r^2; float division lands a few ulp
+          // off 1, which (1 - c)-type terms weighted by E_j^2 would turn into noise
+          if (sizeof(T) == 4 && p == q) c = (T)1;
           T fjk = 1, rjk2 = 0;
           if (G.has_g4) {
             const T ex = vp.x - vq.x, ey = vp.y - vq.y, ez = vp.z - vq.z;
             rjk2 = ex * ex + ey * ey + ez * ez;
             const T rjk = m_sqrt<T>(rjk2);
-            fjk = rjk > rcut_g4 ? (T)0 : (T)0.5 * (m_cos<T>((T)kPi * rjk / rcut_g4) + (T)1);
+            T fcv, dfv;
+            cutoff_fc<T>(min(rjk, rcut_g4), rcut_g4, fcv, dfv);
+            fjk = rjk > rcut_g4 ? (T)0 : fcv;
             if (G.atomid > 0) fjk *= t.idv[p] * t.idv[q];
           }
 #pragma unroll
@@ -197,16 +202,38 @@ __global__ void zfinish_kernel(const double *part, int nparts, int ng, double de
   out[f] = is_std ? sqrt(acc / denom) : acc / denom;
 }
 
-template <typename T>
-__global__ void zapply_kernel(T *feat, int nf, int ng, int64_t N, const double *zprec) {
+// FP64 contexts: the reference's (x - mean) / sd in FP64 for bit-level parity
+__global__ void zapply_kernel_d(double *feat, int nf, int ng, int64_t N, const double *zprec) {
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= N * ng) return;
   const int64_t r = t / ng;
   const int f = (int)(t % ng);
   const double sd = zprec[ng + f];
   if (sd < 1e-08) return;
-  T *x = feat + r * nf + f;
-  *x = (T)(((double)*x - zprec[f]) / sd);
+  double *x = feat + r * nf + f;
+  *x = (*x - zprec[f]) / sd;
+}
+
+// FP32 contexts: float mean and inverse deviation (zf[f], zf[ng + f]; inverse 0 = column
+// left as it is), one row per thread group, all float arithmetic
+__global__ void zapply_kernel_f(float *feat, int nf, int ng, int64_t N, const float *zf) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= N * ng) return;
+  const int64_t r = t / ng;
+  const int f = (int)(t - r * ng);
+  const float inv = zf[ng + f];
+  if (inv == 0.f) return;
+  float *x = feat + r * nf + f;
+  *x = (*x - zf[f]) * inv;
+}
+
+// float copies of the statistics for the FP32 kernels
+__global__ void zfloat_kernel(const double *zprec, int ng, float *zf) {
+  const int f = blockIdx.x * blockDim.x + threadIdx.x;
+  if (f >= ng) return;
+  const double sd = zprec[ng + f];
+  zf[f] = (float)zprec[f];
+  zf[ng + f] = sd < 1e-08 ? 0.f : (float)(1.0 / sd);
 }
 
 template <typename T> void fill_tile_args(fnetg_ctx *ctx, TileArgs<T> &a) {
@@ -347,10 +374,20 @@ template <typename T> int launch_zscore(fnetg_ctx *ctx, const int32_t *weights, 
     FNETG_CUDA(cudaMemcpyAsync(z, ctx->h_zprec.data(), sizeof(double) * 2 * ng,
                                cudaMemcpyHostToDevice, ctx->stream));
   }
+  if (ng > 0) {
+    FNETG_CUDA(ctx->d_zprec_f.ensure(sizeof(float) * 2 * ng));
+    LaunchScope ls(ctx, "zscore");
+    zfloat_kernel<<<ceil_div(ng, 128), 128, 0, ctx->stream>>>(z, ng, ctx->d_zprec_f.as<float>());
+    FNETG_CUDA(cudaGetLastError());
+  }
   if (N > 0 && ng > 0) {
     LaunchScope ls(ctx, "zscore");
-    zapply_kernel<T><<<ceil_div(N * ng, 256), 256, 0, ctx->stream>>>(ctx->d_feat.as<T>(), nf, ng,
-                                                                     N, z);
+    if (sizeof(T) == 8)
+      zapply_kernel_d<<<ceil_div(N * ng, 256), 256, 0, ctx->stream>>>(ctx->d_feat.as<double>(),
+                                                                      nf, ng, N, z);
+    else
+      zapply_kernel_f<<<ceil_div(N * ng, 256), 256, 0, ctx->stream>>>(
+          ctx->d_feat.as<float>(), nf, ng, N, ctx->d_zprec_f.as<float>());
     FNETG_CUDA(cudaGetLastError());
   }
   return FNETG_OK;

@@ -384,6 +384,7 @@ static int rebuild_buckets(fnetg_ctx *ctx, bool order_changes) {
   std::vector<int64_t> t0(nsp + 1, 0);
   for (int64_t t = 0; t < ctx->ntiles; t++) t0[tiles[4 * t] + 1]++;
   for (int s = 0; s < nsp; s++) t0[s + 1] += t0[s];
+  ctx->h_sp_tile0 = t0;
   FNETG_CUDA(ctx->d_sp_tile0.ensure(sizeof(int64_t) * (nsp + 1)));
   FNETG_CUDA(cudaMemcpy(ctx->d_sp_tile0.p, t0.data(), sizeof(int64_t) * (nsp + 1),
                         cudaMemcpyHostToDevice));

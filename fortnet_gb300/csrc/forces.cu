@@ -58,6 +58,7 @@ __device__ void angular_side(const TileArgs<T> &a, Tile<T> &tl, const AGroup &G,
       const T uqx = vq.x / rq, uqy = vq.y / rq, uqz = vq.z / rq;
       T c = (vp.x * vq.x + vp.y * vq.y + vp.z * vq.z) / (rp * rq + (T)1e-13);
       c = c > (T)1 ? (T)1 : (c < (T)-1 ? (T)-1 : c);
+      if (sizeof(T) == 4 && p == q) c = (T)1;  // j = k exactly (see the ACSF kernel)
       T g = 1, gd = 0, rpq = 0, ex = 0, ey = 0, ez = 0;
       if (G.has_g4) {
         ex = vp.x - vq.x;
@@ -84,8 +85,9 @@ __device__ void angular_side(const TileArgs<T> &a, Tile<T> &tl, const AGroup &G,
             ggd = 0;
           } else {
             const T ee = m_exp<T>(-(eta * rpq * rpq));
-            const T fcq = (T)0.5 * (m_cos<T>((T)kPi * rpq / rcut4) + (T)1);
-            const T dfq = (T)-0.5 * ((T)kPi / rcut4) * m_sin<T>((T)kPi * rpq / rcut4);
+            // rpq <= rcut4: the argument lies in [0, pi]
+            T fcq, dfq;
+            cutoff_fc<T>(rpq, rcut4, fcq, dfq);
             gg = ee * fcq;
             ggd = ee * (dfq - (T)2 * eta * rpq * fcq);
             if (G.atomid > 0) {

@@ -152,7 +152,7 @@ struct fnetg_ctx {
   int nf = 0;
   bool feats_valid = false;
   std::vector<int32_t> ext_idx;
-  fnetg::DBuf d_feat, d_zprec, d_zpart, d_extidx;
+  fnetg::DBuf d_feat, d_zprec, d_zprec_f, d_zpart, d_extidx;
   std::vector<double> h_zprec;
   bool zprec_valid = false;
 
@@ -162,7 +162,9 @@ struct fnetg_ctx {
   std::vector<int32_t> dims;
   int64_t nparams = 0;
   std::vector<int64_t> woff, boff;
+  std::vector<int64_t> h_sp_tile0;  // [nsp+1] first MLP tile of every species
   fnetg::DBuf d_params64, d_params, d_ref_of_compute, d_sp_tile0;
+  fnetg::DBuf d_gchunk;  // FP64 gradient sums of tile chunks
 
   // outputs / training
   int ngt = 0, nat = 0;

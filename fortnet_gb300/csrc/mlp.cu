@@ -110,15 +110,25 @@ template <typename T> __device__ __forceinline__ void act_fd(int t, T z, T &f, T
     d = act_d<T>(t, z);
   }
 }
+// Float path: derivatives free of cancellation for saturated units.  1 - tanh^2 loses
+// log2(1 / (1 - tanh^2)) bits near |tanh| = 1; sech^2 z = 4t / (1 + t)^2 with t = exp(-2|z|)
+// does not.  sigma (1 - sigma) = e / (1 + e)^2 with e = exp(-|z|) likewise.
 template <> __device__ __forceinline__ void act_fd<float>(int t, float z, float &f, float &d) {
   if (t == FNETG_ACT_TANH) {
     const float th = tanhf(z);
     f = th;
-    d = 1.f - th * th;
+    if (fabsf(z) < 0.55f) {
+      d = 1.f - th * th;
+    } else {
+      const float e = expf(-2.f * fabsf(z));
+      const float q = 1.f + e;
+      d = 4.f * e / (q * q);
+    }
   } else if (t == FNETG_ACT_SIGMOID) {
-    const float sg = 1.f / (1.f + expf(-z));
-    f = sg;
-    d = sg * (1.f - sg);
+    const float e = expf(-fabsf(z));
+    const float q = 1.f + e;
+    f = z >= 0.f ? 1.f / q : e / q;
+    d = e / (q * q);
   } else {
     f = act_f<float>(t, z);
     d = act_d<float>(t, z);
@@ -334,7 +344,8 @@ template <typename T> struct MlpArgs {
   T *gpart;               // [ntiles][stride] per-tile gradient partials (gradient layout)
   // jacobian
   int jac_out;            // output index
-  const double *zsd;      // z-score standard deviations (or null), length ng
+  const double *zsd;      // z-score standard deviations (or null), length ng (FP64 path)
+  const float *zinv;      // inverse deviations, 0 = unscaled column (or null), length ng (FP32)
   int ng;                 // number of ACSF columns (z-score applies to these)
   double *jac64;          // [N][nf] atom order (API)
   T *jacT;                // [N][nf] atom order scaled by 1/sd (forces)
@@ -436,9 +447,14 @@ __global__ void __launch_bounds__(kMlpThreads) mlp_jacobian_kernel(MlpArgs<T> a)
       if (a.jac64) a.jac64[atom * nf + k] = (double)v;
       if (a.jacT) {
         T s = v;
-        if (a.zsd && k < a.ng) {
-          const double sd = a.zsd[k];
-          if (sd >= 1e-08) s = (T)((double)v / sd);
+        if (sizeof(T) == 8) {
+          if (a.zsd && k < a.ng) {
+            const double sd = a.zsd[k];
+            if (sd >= 1e-08) s = (T)((double)v / sd);
+          }
+        } else if (a.zinv && k < a.ng) {
+          const float inv = a.zinv[k];
+          if (inv != 0.f) s = (T)((float)v * inv);
         }
         a.jacT[atom * nf + k] = s;
       }
@@ -487,9 +503,25 @@ __global__ void __launch_bounds__(kMlpThreads) mlp_backward_kernel(MlpArgs<T> a)
   }
 }
 
-// FP64 sum of the per-tile partials of every species, written in the reference layout.
+// FP64 sums of the per-tile partials over chunks of kGradChunk consecutive tiles of one
+// species (grid: parameter blocks x species x chunks), then the chunk sums in chunk order:
+// a fixed summation order, so repeated calls give identical gradients.
+constexpr int kGradChunk = 32;
+
 template <typename T>
-__global__ void grad_reduce_kernel(const T *gpart, const int64_t *sp_tile0, NetDesc net,
+__global__ void grad_chunk_kernel(const T *gpart, const int64_t *sp_tile0, int64_t stride,
+                                  int nchunk, double *gchunk) {
+  const int s = blockIdx.y, c = blockIdx.z;
+  const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= stride) return;
+  const int64_t t0 = sp_tile0[s] + (int64_t)c * kGradChunk;
+  const int64_t t1 = min(sp_tile0[s + 1], t0 + kGradChunk);
+  double acc = 0.0;
+  for (int64_t t = t0; t < t1; t++) acc += (double)gpart[t * stride + q];
+  gchunk[((int64_t)s * nchunk + c) * stride + q] = acc;
+}
+
+__global__ void grad_finish_kernel(const double *gchunk, int nchunk, NetDesc net,
                                    const int64_t *ref_of_compute, int64_t nparams,
                                    double *grad64) {
   const int s = blockIdx.y;
@@ -497,9 +529,8 @@ __global__ void grad_reduce_kernel(const T *gpart, const int64_t *sp_tile0, NetD
   if (q >= net.stride) return;
   const int64_t ref = ref_of_compute[q];
   if (ref < 0) return;
-  const int64_t t0 = sp_tile0[s], t1 = sp_tile0[s + 1];
   double acc = 0.0;
-  for (int64_t t = t0; t < t1; t++) acc += (double)gpart[t * net.stride + q];
+  for (int c = 0; c < nchunk; c++) acc += gchunk[((int64_t)s * nchunk + c) * net.stride + q];
   grad64[(int64_t)s * nparams + ref] = acc;
 }
 
@@ -632,6 +663,7 @@ template <typename T> int do_jacobian(fnetg_ctx *ctx, int o, void *dstT) {
   if (dstT) {
     a.jacT = static_cast<T *>(dstT);
     a.zsd = ctx->zprec_valid ? ctx->d_zprec.as<double>() + ctx->gf.size() : nullptr;
+    a.zinv = ctx->zprec_valid ? ctx->d_zprec_f.as<float>() + ctx->gf.size() : nullptr;
   } else {
     FNETG_CUDA(ctx->d_jac.ensure(sizeof(double) * std::max<int64_t>(ctx->N, 1) * nf));
     a.jac64 = ctx->d_jac.as<double>();
@@ -664,12 +696,26 @@ template <typename T> int do_backward(fnetg_ctx *ctx) {
     mlp_backward_kernel<T><<<(unsigned)ctx->ntiles, kMlpThreads, sm, ctx->stream>>>(a);
     FNETG_CUDA(cudaGetLastError());
   }
+  int64_t maxt = 0;
+  for (size_t k = 0; k + 1 < ctx->h_sp_tile0.size(); k++)
+    maxt = std::max(maxt, ctx->h_sp_tile0[k + 1] - ctx->h_sp_tile0[k]);
+  const int nchunk = (int)std::max<int64_t>(1, (maxt + kGradChunk - 1) / kGradChunk);
+  FNETG_CUDA(ctx->d_gchunk.ensure(sizeof(double) * ctx->nsp * nchunk * Lo.net.stride));
+  {
+    dim3 grid(ceil_div(Lo.net.stride, 256), ctx->nsp, nchunk);
+    LaunchScope ls(ctx, "reduce");
+    grad_chunk_kernel<T><<<grid, 256, 0, ctx->stream>>>(ctx->d_gpart.as<T>(),
+                                                        ctx->d_sp_tile0.as<int64_t>(),
+                                                        Lo.net.stride, nchunk,
+                                                        ctx->d_gchunk.as<double>());
+    FNETG_CUDA(cudaGetLastError());
+  }
   {
     dim3 grid(ceil_div(Lo.net.stride, 256), ctx->nsp);
     LaunchScope ls(ctx, "reduce");
-    grad_reduce_kernel<T><<<grid, 256, 0, ctx->stream>>>(
-        ctx->d_gpart.as<T>(), ctx->d_sp_tile0.as<int64_t>(), Lo.net,
-        ctx->d_ref_of_compute.as<int64_t>(), ctx->nparams, ctx->d_grad64.as<double>());
+    grad_finish_kernel<<<grid, 256, 0, ctx->stream>>>(
+        ctx->d_gchunk.as<double>(), nchunk, Lo.net, ctx->d_ref_of_compute.as<int64_t>(),
+        ctx->nparams, ctx->d_grad64.as<double>());
     FNETG_CUDA(cudaGetLastError());
   }
   return FNETG_OK;

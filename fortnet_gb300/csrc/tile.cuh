@@ -26,8 +26,38 @@ __device__ constexpr int kMonoTab[kMaxMono][3] = {
 
 __host__ __device__ constexpr int n_mono_of(int D) { return (D + 1) * (D + 2) * (D + 3) / 6; }
 
+// Float exp on the FMA/ALU pipes only (the library's range reduction spends conversion
+// instructions, which GB300 issues on its narrow FP64 pipe).  Cody-Waite reduction:
+// n = round(x log2 e) by adding 1.5 * 2^23 (the float sum rounds to an integer; n is read back
+// from the bit pattern), z = x - n ln2 with ln2 split in a 15-bit head (n * head exact) and a
+// tail, e^z from its Taylor series through z^7 (|z| <= ln2 / 2: truncation < 1e-8), and the
+// scaling by 2^n added to the exponent field.  Max error 1.3 ulp on [-86.5, 88.7]; results
+// below exp(-86.5) are flushed to zero.
+__device__ __forceinline__ float exp_cw(float x) {
+  constexpr float kLog2e = 1.44269504088896341f;
+  constexpr float kLn2Hi = 0.693145751953125f;       // ln 2 to 15 significant bits
+  constexpr float kLn2Lo = 1.428606765330187e-06f;   // ln 2 - kLn2Hi
+  constexpr float kRound = 12582912.f;               // 1.5 * 2^23
+  const float xc = fminf(fmaxf(x, -86.5f), 88.7f);
+  const float t = fmaf(xc, kLog2e, kRound);
+  const float n = t - kRound;
+  const int ni = __float_as_int(t) - __float_as_int(kRound);
+  float z = fmaf(-n, kLn2Hi, xc);
+  z = fmaf(-n, kLn2Lo, z);
+  float p = 1.f / 5040.f;
+  p = fmaf(p, z, 1.f / 720.f);
+  p = fmaf(p, z, 1.f / 120.f);
+  p = fmaf(p, z, 1.f / 24.f);
+  p = fmaf(p, z, 1.f / 6.f);
+  p = fmaf(p, z, 0.5f);
+  p = fmaf(p, z, 1.f);
+  p = fmaf(p, z, 1.f);
+  const float r = __int_as_float(__float_as_int(p) + (ni << 23));
+  return x != x ? x : (x < -86.5f ? 0.f : r);
+}
+
 template <typename T> __device__ __forceinline__ T m_exp(T x);
-template <> __device__ __forceinline__ float m_exp<float>(float x) { return expf(x); }
+template <> __device__ __forceinline__ float m_exp<float>(float x) { return exp_cw(x); }
 template <> __device__ __forceinline__ double m_exp<double>(double x) { return exp(x); }
 template <typename T> __device__ __forceinline__ T m_cos(T x);
 template <> __device__ __forceinline__ float m_cos<float>(float x) { return cosf(x); }
@@ -35,6 +65,50 @@ template <> __device__ __forceinline__ double m_cos<double>(double x) { return c
 template <typename T> __device__ __forceinline__ T m_sin(T x);
 template <> __device__ __forceinline__ float m_sin<float>(float x) { return sinf(x); }
 template <> __device__ __forceinline__ double m_sin<double>(double x) { return sin(x); }
+// Cutoff function fc(r) = (cos(pi r / rc) + 1) / 2 and its derivative -(pi / 2rc) sin(pi r / rc)
+// for r <= rc.  FP64: the reference's formulas (acsf.F90:1240-1262).  FP32: the same values
+// through half angles, fc = sin^2 phi and dfc = -(pi / rc) sin phi cos phi with
+// phi = (pi / 2)(rc - r) / rc, which keeps full relative accuracy as r -> rc where the
+// reference form cancels; sin and cos from their Taylor series (through u^13 / u^12, Horner in
+// u^2) on an angle u in [0, pi/4] (truncation below 1e-13).
+template <typename T> __device__ __forceinline__ void cutoff_fc(T r, T rc, T &fc, T &dfc);
+template <>
+__device__ __forceinline__ void cutoff_fc<double>(double r, double rc, double &fc, double &dfc) {
+  fc = 0.5 * (cos(kPi * r / rc) + 1.0);
+  dfc = -0.5 * (kPi / rc) * sin(kPi * r / rc);
+}
+__device__ __forceinline__ void sincos_taylor(float u, float &s, float &c) {
+  const float w = u * u;
+  float ps = 1.f / 6227020800.f;   // 1/13!
+  ps = fmaf(ps, w, -1.f / 39916800.f);
+  ps = fmaf(ps, w, 1.f / 362880.f);
+  ps = fmaf(ps, w, -1.f / 5040.f);
+  ps = fmaf(ps, w, 1.f / 120.f);
+  ps = fmaf(ps, w, -1.f / 6.f);
+  ps = fmaf(ps, w, 1.f);
+  float pc = 1.f / 479001600.f;    // 1/12!
+  pc = fmaf(pc, w, -1.f / 3628800.f);
+  pc = fmaf(pc, w, 1.f / 40320.f);
+  pc = fmaf(pc, w, -1.f / 720.f);
+  pc = fmaf(pc, w, 1.f / 24.f);
+  pc = fmaf(pc, w, -0.5f);
+  pc = fmaf(pc, w, 1.f);
+  s = u * ps;
+  c = pc;
+}
+template <>
+__device__ __forceinline__ void cutoff_fc<float>(float r, float rc, float &fc, float &dfc) {
+  // sin phi = cos theta and cos phi = sin theta for theta = (pi / 2) r / rc: the series run on
+  // the smaller of the two angles (<= pi/4), so both ends of [0, rc] keep relative accuracy
+  const float phi = (float)(kPi / 2.0) * ((rc - r) / rc);
+  const float theta = (float)(kPi / 2.0) * (r / rc);
+  float sm, cm;
+  sincos_taylor(fminf(phi, theta), sm, cm);
+  const float s = phi <= theta ? sm : cm, c = phi <= theta ? cm : sm;
+  fc = s * s;
+  dfc = -((float)kPi / rc) * (s * c);
+}
+
 template <typename T> __device__ __forceinline__ T m_pow(T b, T e);
 template <> __device__ __forceinline__ float m_pow<float>(float b, float e) { return powf(b, e); }
 template <> __device__ __forceinline__ double m_pow<double>(double b, double e) { return pow(b, e); }
@@ -212,9 +286,10 @@ __device__ void stage_tile(const TileArgs<T> &a, Tile<T> &t, int64_t i, int64_t 
     for (int rc = 0; rc < a.nrcls; rc++) {
       const T rcut = a.rcls[rc];
       const bool in = (rmask >> rc) & 1u;
-      t.fc[rc * a.cap + q] = in ? (T)0.5 * (m_cos<T>((T)kPi * v.w / rcut) + (T)1) : (T)0;
-      if (forces)
-        t.dfc[rc * a.cap + q] = in ? (T)-0.5 * ((T)kPi / rcut) * m_sin<T>((T)kPi * v.w / rcut) : (T)0;
+      T fcv, dfv;
+      cutoff_fc<T>(in ? v.w : rcut, rcut, fcv, dfv);
+      t.fc[rc * a.cap + q] = in ? fcv : (T)0;
+      if (forces) t.dfc[rc * a.cap + q] = in ? dfv : (T)0;
     }
     for (int e = 0; e < a.necls; e++) {
       const T eta = a.ecls_eta[e];
