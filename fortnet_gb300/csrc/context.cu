@@ -497,6 +497,21 @@ int fnetg_set_gfunctions(fnetg_ctx *ctx, int32_t ng, const fnetg_gfunc *g) {
       ctx->h_rad.push_back(d);
     }
   }
+  // radial functions grouped by list channel (all atoms first, then species codes in order):
+  // a pair visits the all-atom segment and its own species' segment only
+  std::stable_sort(ctx->h_rad.begin(), ctx->h_rad.end(),
+                   [](const GDesc &x, const GDesc &y) { return x.chan1 < y.chan1; });
+  ctx->rad_seg.assign(kMaxSpeciesCodes + 2, 0);
+  {
+    int nall = 0;
+    for (auto &d : ctx->h_rad) nall += d.chan1 < 0 ? 1 : 0;
+    ctx->rad_seg[1] = nall;
+    int pos = nall;
+    for (int c = 0; c < (int)zs.size(); c++) {
+      for (auto &d : ctx->h_rad) pos += d.chan1 == c ? 1 : 0;
+      ctx->rad_seg[c + 2] = pos;
+    }
+  }
   // G5 functions with a small integer xi take the moment form; the rest (G4, other xi) the
   // triplet sweep
   std::vector<GDesc> mom, trip;

@@ -122,13 +122,30 @@ __device__ void angular_side(const TileArgs<T> &a, Tile<T> &tl, const AGroup &G,
 }
 
 
-// per-pair derivative of the moment terms, degree D known at compile time
+// Per-pair derivative of the moment terms, degree D known at compile time.  The eta classes
+// are folded first (the derivative is linear in the adjoint moments):
+//   cD(alpha) = sum_e D_e Qc_e(alpha),  cE(alpha) = sum_e E_e Qc_e(alpha),
+//   w += P_D(u) u + (grad P_E(u) - (grad P_E(u) . u) u) / r
+// with P_c(u) = sum_alpha c(alpha) u^alpha.
 template <typename T, int D>
 __device__ __forceinline__ void moment_pair_force(const TileArgs<T> &a, Tile<T> &tl, int q,
-                                                  int z) {
+                                                  int zz) {
   constexpr int NM = n_mono_of(D);
   const V4<T> u = tl.u[q];
-  const T r = u.w;
+  T cD[NM], cE[NM];
+#pragma unroll
+  for (int al = 0; al < NM; al++) cD[al] = cE[al] = (T)0;
+  const T *Qz = tl.Qc + (int64_t)zz * a.necls * NM;
+  for (int e = 0; e < a.necls; e++) {
+    const T Ee = tl.E[e * a.cap + q], De = tl.D[e * a.cap + q];
+    const T *Qe = Qz + e * NM;
+#pragma unroll
+    for (int al = 0; al < NM; al++) {
+      const T qv = Qe[al];
+      cD[al] += De * qv;
+      cE[al] += Ee * qv;
+    }
+  }
   T px[D + 1], py[D + 1], pz[D + 1];
   px[0] = py[0] = pz[0] = (T)1;
 #pragma unroll
@@ -137,35 +154,31 @@ __device__ __forceinline__ void moment_pair_force(const TileArgs<T> &a, Tile<T> 
     py[d] = py[d - 1] * u.y;
     pz[d] = pz[d - 1] * u.z;
   }
-  T wx = 0, wy = 0, wz = 0;
-  for (int e = 0; e < a.necls; e++) {
-    const int ks = (z >= 0 && z < a.nz) ? a.cidx[(z + 1) * a.necls + e] : -1;
-    const int ka = a.cidx[e];
-    if (ks < 0 && ka < 0) continue;
-    const T *Qs = ks >= 0 ? tl.Q + ks * a.n_mono : nullptr;
-    const T *Qa = ka >= 0 ? tl.Q + ka * a.n_mono : nullptr;
-    T P = 0, gx = 0, gy = 0, gz = 0;
+  T P = 0, gx = 0, gy = 0, gz = 0;
 #pragma unroll
-    for (int al = 0; al < NM; al++) {
-      const int ea = kMonoTab[al][0], eb = kMonoTab[al][1], ec = kMonoTab[al][2];
-      T c = 0;
-      if (Qs) c += Qs[al];
-      if (Qa) c += Qa[al];
-      P += c * px[ea] * py[eb] * pz[ec];
-      if (ea > 0) gx += c * (T)ea * px[ea > 0 ? ea - 1 : 0] * py[eb] * pz[ec];
-      if (eb > 0) gy += c * (T)eb * px[ea] * py[eb > 0 ? eb - 1 : 0] * pz[ec];
-      if (ec > 0) gz += c * (T)ec * px[ea] * py[eb] * pz[ec > 0 ? ec - 1 : 0];
-    }
-    const T Ee = tl.E[e * a.cap + q], De = tl.D[e * a.cap + q];
-    const T gu = gx * u.x + gy * u.y + gz * u.z;
-    const T s = Ee / r;
-    wx += De * P * u.x + s * (gx - gu * u.x);
-    wy += De * P * u.y + s * (gy - gu * u.y);
-    wz += De * P * u.z + s * (gz - gu * u.z);
+  for (int al = 0; al < NM; al++) {
+    const int ea = kMonoTab[al][0], eb = kMonoTab[al][1], ec = kMonoTab[al][2];
+    P += cD[al] * (px[ea] * py[eb] * pz[ec]);
+    if (ea > 0) gx += ((T)ea * cE[al]) * (px[ea > 0 ? ea - 1 : 0] * py[eb] * pz[ec]);
+    if (eb > 0) gy += ((T)eb * cE[al]) * (px[ea] * py[eb > 0 ? eb - 1 : 0] * pz[ec]);
+    if (ec > 0) gz += ((T)ec * cE[al]) * (px[ea] * py[eb] * pz[ec > 0 ? ec - 1 : 0]);
   }
-  tl.w[q].x += wx;
-  tl.w[q].y += wy;
-  tl.w[q].z += wz;
+  const T gu = gx * u.x + gy * u.y + gz * u.z;
+  const T ir = (T)1 / u.w;
+  tl.w[q].x += P * u.x + ir * (gx - gu * u.x);
+  tl.w[q].y += P * u.y + ir * (gy - gu * u.y);
+  tl.w[q].z += P * u.z + ir * (gz - gu * u.z);
+}
+
+// Radial function parameters staged once per CTA: p0 = rs (G2) or kappa (G3), p1 = eta,
+// meta = type | rclass << 4 | atomid << 8.
+template <typename T> struct RadEntry {
+  T p0, p1;
+  int out, meta;
+};
+
+template <typename T> __host__ __device__ inline size_t radtab_bytes(int nrad) {
+  return ((size_t)sizeof(RadEntry<T>) * nrad + 127) / 128 * 128;
 }
 
 template <typename T, int D>
@@ -174,13 +187,21 @@ __global__ void __launch_bounds__(256) forces_kernel(TileArgs<T> a) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int wpb = blockDim.x >> 5;
   const size_t tb = tile_bytes<T>(a.cap, a.nrcls, a.necls, a.nz, a.ncombo, a.n_mono, a.ng, true);
-  Tile<T> tl = carve_tile<T>(smem + tb * warp, a, true);
+  RadEntry<T> *rt = reinterpret_cast<RadEntry<T> *>(smem);
+  for (int g = threadIdx.x; g < a.nrad; g += blockDim.x) {
+    const GDesc d = a.rad[g];
+    const T *P = a.radp + 8 * g;
+    rt[g] = RadEntry<T>{d.type == 3 ? P[1] : P[2], P[3], d.out,
+                        d.type | (d.rclass << 4) | (d.atomid << 8)};
+  }
+  __syncthreads();
+  Tile<T> tl = carve_tile<T>(smem + radtab_bytes<T>(a.nrad) + tb * warp, a, true);
   for (int64_t i = (int64_t)blockIdx.x * wpb + warp; i < a.natoms; i += (int64_t)gridDim.x * wpb) {
     const int64_t p0 = a.poff[i];
     const int np = (int)(a.poff[i + 1] - p0);
     for (int g = lane; g < a.ng; g += 32) tl.jv[g] = a.J[i * a.nf + g];
     stage_tile<T>(a, tl, i, p0, np, lane, true);
-    // ---- radial: lanes over pairs
+    // ---- radial: lanes over pairs, each over the all-atom functions and its species' own
     for (int q = lane; q < np; q += 32) {
       const uint32_t inf = tl.info[q];
       const int code = (int)(inf & 0xff);
@@ -188,28 +209,34 @@ __global__ void __launch_bounds__(256) forces_kernel(TileArgs<T> a) {
       if (self) continue;  // self images do not move relative to the centre
       const T r = tl.v[q].w;
       T dsum = 0;
-      for (int g = 0; g < a.nrad; g++) {
-        const GDesc d = a.rad[g];
-        if (d.chan1 >= 0 && code != d.chan1) continue;
-        const T *P = a.radp + 8 * g;
-        if (!((inf >> (16 + d.rclass)) & 1u)) continue;
-        T fc = tl.fc[d.rclass * a.cap + q], dfc = tl.dfc[d.rclass * a.cap + q];
-        if (d.atomid > 0) {
-          const T ids = atom_id<T>(a.ext, a.next, d.atomid, i) * atom_id<T>(a.ext, a.next, d.atomid, tl.pj[q]);
-          fc *= ids;
-          dfc *= ids;
+      const int nseg = code < a.nz ? 2 : 1;
+      for (int sg = 0; sg < nseg; sg++) {
+        const int g0 = sg == 0 ? 0 : a.rad_seg[code + 1];
+        const int g1 = sg == 0 ? a.rad_seg[1] : a.rad_seg[code + 2];
+        for (int g = g0; g < g1; g++) {
+          const RadEntry<T> re = rt[g];
+          const int rcl = (re.meta >> 4) & 15;
+          if (!((inf >> (16 + rcl)) & 1u)) continue;
+          T fc = tl.fc[rcl * a.cap + q], dfc = tl.dfc[rcl * a.cap + q];
+          const int aid = re.meta >> 8;
+          if (aid > 0) {
+            const T ids = atom_id<T>(a.ext, a.next, aid, i) * atom_id<T>(a.ext, a.next, aid, tl.pj[q]);
+            fc *= ids;
+            dfc *= ids;
+          }
+          const int ty = re.meta & 15;
+          T dg;
+          if (ty == 1) {
+            dg = dfc;
+          } else if (ty == 2) {
+            const T x = r - re.p0, eta = re.p1;
+            dg = m_exp<T>(-(eta * (x * x))) * (dfc - (T)2 * eta * x * fc);
+          } else {
+            const T kr = re.p0 * r;
+            dg = m_cos<T>(kr) * dfc - re.p0 * m_sin<T>(kr) * fc;
+          }
+          dsum += tl.jv[re.out] * dg;
         }
-        T dg;
-        if (d.type == 1) {
-          dg = dfc;
-        } else if (d.type == 2) {
-          const T x = r - P[2], eta = P[3];
-          dg = m_exp<T>(-(eta * (x * x))) * (dfc - (T)2 * eta * x * fc);
-        } else {
-          const T kr = P[1] * r;
-          dg = m_cos<T>(kr) * dfc - P[1] * m_sin<T>(kr) * fc;
-        }
-        dsum += tl.jv[d.out] * dg;
       }
       const V4<T> u = tl.u[q];
       tl.w[q].x += dsum * u.x;
@@ -218,24 +245,37 @@ __global__ void __launch_bounds__(256) forces_kernel(TileArgs<T> a) {
     }
     // ---- integer-xi G5 through adjoint moments
     if (D > 0 && a.ncombo > 0) {
+      constexpr int NM = n_mono_of(D > 0 ? D : 1);
       compute_moments<T, (D > 0 ? D : 1)>(a, tl, np, lane);
-      const int items = a.ncombo * a.n_mono;
-      for (int it = lane; it < items; it += 32) {
-        const int k = it / a.n_mono, al = it % a.n_mono;
+      for (int it = lane; it < a.ncombo * NM; it += 32) {
+        const int k = it / NM, al = it - k * NM;
         T acc = 0;
         for (int e = a.qoff[k]; e < a.qoff[k + 1]; e++) {
           const int f = a.qent[2 * e], ko = a.qent[2 * e + 1];
-          acc += tl.jv[a.mfunc[f].out] * a.mcoef[(int64_t)f * a.n_mono + al] *
-                 tl.M[ko * a.n_mono + al];
+          acc += tl.jv[a.mfunc[f].out] * a.mcoef[(int64_t)f * NM + al] * tl.M[ko * NM + al];
         }
         tl.Q[it] = acc;
       }
+      __syncwarp();
+      // a pair of species code z sees the combos of its own list and of the all-atom list
+      for (int zz = 0; zz <= a.nz; zz++)
+        for (int e = 0; e < a.necls; e++) {
+          const int ks = zz < a.nz ? a.cidx[(zz + 1) * a.necls + e] : -1;
+          const int ka = a.cidx[e];
+          T *dst = tl.Qc + ((int64_t)zz * a.necls + e) * NM;
+          for (int al = lane; al < NM; al += 32) {
+            T v = 0;
+            if (ks >= 0) v += tl.Q[ks * NM + al];
+            if (ka >= 0) v += tl.Q[ka * NM + al];
+            dst[al] = v;
+          }
+        }
       __syncwarp();
       for (int q = lane; q < np; q += 32) {
         const uint32_t inf = tl.info[q];
         if ((inf >> 8) & 1u) continue;
         const int z = (int)(inf & 0xff);
-        moment_pair_force<T, (D > 0 ? D : 1)>(a, tl, q, z == 0xff ? -1 : z);
+        moment_pair_force<T, (D > 0 ? D : 1)>(a, tl, q, z < a.nz ? z : a.nz);
       }
     }
     __syncwarp();
@@ -314,6 +354,8 @@ template <typename T> void fill_tile_args_forces(fnetg_ctx *ctx, TileArgs<T> &a)
   a.next = ctx->next;
   a.rad = ctx->d_rad.as<GDesc>();
   a.nrad = (int)ctx->h_rad.size();
+  for (int c = 0; c < kMaxSpeciesCodes + 2; c++)
+    a.rad_seg[c] = c < (int)ctx->rad_seg.size() ? ctx->rad_seg[c] : 0;
   a.ang = ctx->d_ang.as<GDesc>();
   const bool dbl = sizeof(T) == 8;
   a.radp = static_cast<const T *>(dbl ? ctx->d_radpar_d.p : ctx->d_radpar_f.p);
@@ -344,11 +386,12 @@ template <typename T> void fill_tile_args_forces(fnetg_ctx *ctx, TileArgs<T> &a)
 template <typename T, int D> int launch_forces_d(fnetg_ctx *ctx, TileArgs<T> &a, int nout) {
   const int64_t N = ctx->N;
   const size_t tb = tile_bytes<T>(a.cap, a.nrcls, a.necls, a.nz, a.ncombo, a.n_mono, a.ng, true);
+  const size_t rb = radtab_bytes<T>(a.nrad);
   int wpb = 8;
-  while (wpb > 1 && tb * wpb > 160 * 1024) wpb >>= 1;
-  FNETG_CHECK(tb * wpb <= 227 * 1024, FNETG_E_UNSUPPORTED,
+  while (wpb > 1 && rb + tb * wpb > 160 * 1024) wpb >>= 1;
+  FNETG_CHECK(rb + tb * wpb <= 227 * 1024, FNETG_E_UNSUPPORTED,
               "neighbour tile of one atom exceeds shared memory");
-  const size_t smem = tb * wpb;
+  const size_t smem = rb + tb * wpb;
   FNETG_CUDA(cudaFuncSetAttribute(forces_kernel<T, D>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)smem));
   int per_sm = 1;

@@ -121,6 +121,8 @@ struct fnetg_ctx {
   // G-functions
   std::vector<fnetg_gfunc> gf;
   std::vector<fnetg::GDesc> h_rad, h_ang;
+  std::vector<int> rad_seg;  // [kMaxSpeciesCodes + 2]: all-atom radial functions [0, rad_seg[1]),
+                             // species code c in [rad_seg[c + 1], rad_seg[c + 2])
   std::vector<fnetg::AGroup> h_groups;
   std::vector<double> rcut_classes;
   std::vector<double> ecls_eta;

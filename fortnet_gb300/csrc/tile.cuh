@@ -151,6 +151,7 @@ template <typename T> struct TileArgs {
   const GDesc *rad;
   const T *radp;          // [nrad][8] parameters in the kernel's width
   int nrad;
+  int rad_seg[kMaxSpeciesCodes + 2];  // radial functions by list channel (see the context)
   const GDesc *ang;       // triplet-sweep functions
   const T *angp;          // [nang][8]
   const AGroup *groups;
@@ -197,6 +198,8 @@ template <typename T> struct Tile {
   int *cnt;         // [8]
   T *M;             // [ncombo][n_mono] moments
   T *Q;             // [ncombo][n_mono] adjoint moments (forces)
+  T *Qc;            // [nz + 1][necls][n_mono] adjoint moments of a pair's species list plus
+                    // the all-atom list, per eta class (forces; row nz: all-atom list only)
   T *jv;            // [ng] dE/dG of the centre atom (forces)
   uint16_t *lists;  // [nz][cap]
 };
@@ -210,6 +213,7 @@ __host__ __device__ inline size_t tile_bytes(int cap, int nrcls, int necls, int 
   b += sizeof(T) * cap;                       // idv
   b += sizeof(T) * 5 * 32;                    // gpar
   b += sizeof(T) * (size_t)ncombo * nmono * (forces ? 2 : 1);
+  if (forces && ncombo > 0) b += sizeof(T) * (size_t)(nz + 1) * necls * nmono;
   b += forces ? sizeof(T) * ng : 0;
   b = (b + 7) / 8 * 8;
   b += sizeof(uint32_t) * cap + sizeof(int32_t) * cap;
@@ -248,10 +252,14 @@ __device__ Tile<T> carve_tile(unsigned char *p, const TileArgs<T> &a, bool force
   p += sizeof(T) * 5 * 32;
   t.M = reinterpret_cast<T *>(p);
   p += sizeof(T) * (size_t)a.ncombo * a.n_mono;
-  t.Q = t.jv = nullptr;
+  t.Q = t.jv = t.Qc = nullptr;
   if (forces) {
     t.Q = reinterpret_cast<T *>(p);
     p += sizeof(T) * (size_t)a.ncombo * a.n_mono;
+    if (a.ncombo > 0) {
+      t.Qc = reinterpret_cast<T *>(p);
+      p += sizeof(T) * (size_t)(a.nz + 1) * a.necls * a.n_mono;
+    }
     t.jv = reinterpret_cast<T *>(p);
     p += sizeof(T) * a.ng;
   }
