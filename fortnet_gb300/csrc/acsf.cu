@@ -24,7 +24,7 @@ __global__ void __launch_bounds__(256) acsf_kernel(TileArgs<T> a) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int wpb = blockDim.x >> 5;
   const size_t tb =
-      tile_bytes<T>(a.cap, a.nrcls, a.necls, a.nz, a.ncombo, a.n_mono, a.ng, false);
+      tile_bytes<T>(a.cap, a.nrcls, a.necls, a.nz, a.ncombo, a.n_mono, a.ng, false, a.ngroups > 0);
   Tile<T> t = carve_tile<T>(smem + tb * warp, a, false);
   for (int64_t i = (int64_t)blockIdx.x * wpb + warp; i < a.natoms; i += (int64_t)gridDim.x * wpb) {
     const int64_t p0 = a.poff[i];
@@ -45,7 +45,7 @@ __global__ void __launch_bounds__(256) acsf_kernel(TileArgs<T> a) {
       for (int k = 0; k < n; k++) {
         const int q = lst ? lst[k] : k;
         if (!((t.info[q] >> (16 + d.rclass)) & 1u)) continue;
-        const T r = t.v[q].w;
+        const T r = t.u[q].w;
         T fc = fcr[q];
         if (d.atomid > 0) fc *= idi * atom_id<T>(a.ext, a.next, d.atomid, t.pj[q]);
         T term;
@@ -280,19 +280,16 @@ template <typename T> void fill_tile_args(fnetg_ctx *ctx, TileArgs<T> &a) {
 template <typename T, int D> int launch_acsf_d(fnetg_ctx *ctx, TileArgs<T> &a) {
   const int64_t N = ctx->N;
   const size_t tb =
-      tile_bytes<T>(a.cap, a.nrcls, a.necls, a.nz, a.ncombo, a.n_mono, a.ng, false);
-  int wpb = 8;
-  while (wpb > 1 && tb * wpb > 160 * 1024) wpb >>= 1;
-  FNETG_CHECK(tb * wpb <= 227 * 1024, FNETG_E_UNSUPPORTED,
+      tile_bytes<T>(a.cap, a.nrcls, a.necls, a.nz, a.ncombo, a.n_mono, a.ng, false, a.ngroups > 0);
+  int wpb = 1, per_sm = 1;
+  size_t smem = 0;
+  const cudaError_t err = pick_warps(acsf_kernel<T, D>, 0, tb, wpb, smem, per_sm);
+  FNETG_CHECK(err != cudaErrorInvalidValue, FNETG_E_UNSUPPORTED,
               "neighbour tile of one atom exceeds shared memory");
-  const size_t smem = tb * wpb;
-  FNETG_CUDA(cudaFuncSetAttribute(acsf_kernel<T, D>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)smem));
-  int per_sm = 1;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, acsf_kernel<T, D>, wpb * 32, smem);
+  FNETG_CUDA(err);
   const int64_t want = (N + wpb - 1) / wpb;
   const int blocks = (int)std::max<int64_t>(
-      1, std::min<int64_t>(want, (int64_t)num_sms() * std::max(per_sm, 1) * 8));
+      1, std::min<int64_t>(want, (int64_t)num_sms() * per_sm * 8));
   LaunchScope ls(ctx, "acsf");
   acsf_kernel<T, D><<<blocks, wpb * 32, smem, ctx->stream>>>(a);
   FNETG_CUDA(cudaGetLastError());

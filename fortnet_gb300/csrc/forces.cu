@@ -186,7 +186,7 @@ __global__ void __launch_bounds__(256) forces_kernel(TileArgs<T> a) {
   extern __shared__ __align__(128) unsigned char smem[];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int wpb = blockDim.x >> 5;
-  const size_t tb = tile_bytes<T>(a.cap, a.nrcls, a.necls, a.nz, a.ncombo, a.n_mono, a.ng, true);
+  const size_t tb = tile_bytes<T>(a.cap, a.nrcls, a.necls, a.nz, a.ncombo, a.n_mono, a.ng, true, a.ngroups > 0);
   RadEntry<T> *rt = reinterpret_cast<RadEntry<T> *>(smem);
   for (int g = threadIdx.x; g < a.nrad; g += blockDim.x) {
     const GDesc d = a.rad[g];
@@ -207,7 +207,7 @@ __global__ void __launch_bounds__(256) forces_kernel(TileArgs<T> a) {
       const int code = (int)(inf & 0xff);
       const bool self = (inf >> 8) & 1u;
       if (self) continue;  // self images do not move relative to the centre
-      const T r = tl.v[q].w;
+      const T r = tl.u[q].w;
       T dsum = 0;
       const int nseg = code < a.nz ? 2 : 1;
       for (int sg = 0; sg < nseg; sg++) {
@@ -385,20 +385,17 @@ template <typename T> void fill_tile_args_forces(fnetg_ctx *ctx, TileArgs<T> &a)
 
 template <typename T, int D> int launch_forces_d(fnetg_ctx *ctx, TileArgs<T> &a, int nout) {
   const int64_t N = ctx->N;
-  const size_t tb = tile_bytes<T>(a.cap, a.nrcls, a.necls, a.nz, a.ncombo, a.n_mono, a.ng, true);
+  const size_t tb = tile_bytes<T>(a.cap, a.nrcls, a.necls, a.nz, a.ncombo, a.n_mono, a.ng, true, a.ngroups > 0);
   const size_t rb = radtab_bytes<T>(a.nrad);
-  int wpb = 8;
-  while (wpb > 1 && rb + tb * wpb > 160 * 1024) wpb >>= 1;
-  FNETG_CHECK(rb + tb * wpb <= 227 * 1024, FNETG_E_UNSUPPORTED,
+  int wpb = 1, per_sm = 1;
+  size_t smem = 0;
+  const cudaError_t err = pick_warps(forces_kernel<T, D>, rb, tb, wpb, smem, per_sm);
+  FNETG_CHECK(err != cudaErrorInvalidValue, FNETG_E_UNSUPPORTED,
               "neighbour tile of one atom exceeds shared memory");
-  const size_t smem = rb + tb * wpb;
-  FNETG_CUDA(cudaFuncSetAttribute(forces_kernel<T, D>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)smem));
-  int per_sm = 1;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, forces_kernel<T, D>, wpb * 32, smem);
+  FNETG_CUDA(err);
   const int64_t want = (N + wpb - 1) / wpb;
   const int blocks = (int)std::max<int64_t>(
-      1, std::min<int64_t>(want, (int64_t)num_sms() * std::max(per_sm, 1) * 8));
+      1, std::min<int64_t>(want, (int64_t)num_sms() * per_sm * 8));
   for (int o = 0; o < nout; o++) {
     int rc = run_jacobian(ctx, o, ctx->d_jacT.p);
     if (rc) return rc;

@@ -10,6 +10,8 @@
 // of every (list, eta class) combo feed the integer-xi G5 functions.
 #pragma once
 
+#include <algorithm>
+
 #include "internal.cuh"
 
 namespace fnetg {
@@ -206,11 +208,12 @@ template <typename T> struct Tile {
 
 template <typename T>
 __host__ __device__ inline size_t tile_bytes(int cap, int nrcls, int necls, int nz, int ncombo,
-                                             int nmono, int ng, bool forces) {
+                                             int nmono, int ng, bool forces, bool trip) {
+  // v and idv serve the triplet sweep only
   size_t b = 0;
-  b += sizeof(V4<T>) * cap * (forces ? 3 : 2);
+  b += sizeof(V4<T>) * cap * ((forces ? 2 : 1) + (trip ? 1 : 0));
   b += sizeof(T) * (size_t)cap * (nrcls + necls) * (forces ? 2 : 1);
-  b += sizeof(T) * cap;                       // idv
+  if (trip) b += sizeof(T) * cap;             // idv
   b += sizeof(T) * 5 * 32;                    // gpar
   b += sizeof(T) * (size_t)ncombo * nmono * (forces ? 2 : 1);
   if (forces && ncombo > 0) b += sizeof(T) * (size_t)(nz + 1) * necls * nmono;
@@ -226,8 +229,12 @@ template <typename T>
 __device__ Tile<T> carve_tile(unsigned char *p, const TileArgs<T> &a, bool forces) {
   Tile<T> t;
   const int cap = a.cap;
-  t.v = reinterpret_cast<V4<T> *>(p);
-  p += sizeof(V4<T>) * cap;
+  const bool trip = a.ngroups > 0;
+  t.v = nullptr;
+  if (trip) {
+    t.v = reinterpret_cast<V4<T> *>(p);
+    p += sizeof(V4<T>) * cap;
+  }
   t.u = reinterpret_cast<V4<T> *>(p);
   p += sizeof(V4<T>) * cap;
   t.w = nullptr;
@@ -246,8 +253,11 @@ __device__ Tile<T> carve_tile(unsigned char *p, const TileArgs<T> &a, bool force
     t.D = reinterpret_cast<T *>(p);
     p += sizeof(T) * (size_t)cap * a.necls;
   }
-  t.idv = reinterpret_cast<T *>(p);
-  p += sizeof(T) * cap;
+  t.idv = nullptr;
+  if (trip) {
+    t.idv = reinterpret_cast<T *>(p);
+    p += sizeof(T) * cap;
+  }
   t.gpar = reinterpret_cast<T *>(p);
   p += sizeof(T) * 5 * 32;
   t.M = reinterpret_cast<T *>(p);
@@ -276,13 +286,44 @@ __device__ Tile<T> carve_tile(unsigned char *p, const TileArgs<T> &a, bool force
   return t;
 }
 
+// Warps per CTA for a warp-per-atom kernel whose CTA needs `fixed` + wpb * `per_warp` bytes of
+// dynamic shared memory: the choice among 8, 4, 2, 1 with the most resident warps per SM
+// (ties go to the larger CTA).  Sets the kernel's shared-memory attributes for that choice.
+template <typename K>
+inline cudaError_t pick_warps(K kernel, size_t fixed, size_t per_warp, int &wpb, size_t &smem,
+                              int &ctas_per_sm) {
+  cudaError_t err = cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                         (int)cudaSharedmemCarveoutMaxShared);
+  if (err != cudaSuccess) return err;
+  int best_w = 0, best_warps = -1, best_ctas = 0;
+  for (int w = 8; w >= 1; w >>= 1) {
+    const size_t bytes = fixed + per_warp * (size_t)w;
+    if (bytes > 227 * 1024) continue;
+    err = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    if (err != cudaSuccess) return err;
+    int ctas = 0;
+    err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ctas, kernel, w * 32, bytes);
+    if (err != cudaSuccess) return err;
+    if (ctas * w > best_warps) {
+      best_warps = ctas * w;
+      best_w = w;
+      best_ctas = ctas;
+    }
+  }
+  if (best_w == 0) return cudaErrorInvalidValue;
+  wpb = best_w;
+  smem = fixed + per_warp * (size_t)best_w;
+  ctas_per_sm = std::max(best_ctas, 1);
+  return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+}
+
 // Stage the pair tile of atom i (all lanes), build the ordered species lists.
 template <typename T>
 __device__ void stage_tile(const TileArgs<T> &a, Tile<T> &t, int64_t i, int64_t p0, int np,
                            int lane, bool forces) {
   for (int q = lane; q < np; q += 32) {
     const V4<T> v = a.rij[p0 + q];
-    t.v[q] = v;
+    if (t.v) t.v[q] = v;
     const T rinv = (T)1 / v.w;
     t.u[q] = V4<T>{v.x * rinv, v.y * rinv, v.z * rinv, v.w};
     if (forces) t.w[q] = V4<T>{0, 0, 0, 0};
