@@ -162,6 +162,20 @@ def algorithmic_bytes(ctx, ds, funcs, dims):
     }
 
 
+def profiled_traffic(kernel, config, natoms):
+    """DRAM bytes per launch of `kernel` from the committed ncu summary of this configuration
+    (bytes per atom measured on a small capture of the same workload, scaled by atoms)."""
+    path = os.path.join(ROOT, "profiles", f"{kernel}_kernel_{config}.md")
+    if not os.path.exists(path):
+        return None, None
+    with open(path) as fh:
+        for line in fh:
+            if line.startswith("dram_bytes_per_atom:"):
+                per_atom = float(line.split(":", 1)[1])
+                return int(per_atom * natoms), os.path.relpath(path, ROOT)
+    return None, None
+
+
 def run_ours(args):
     from fortnet_gb300 import api
 
@@ -238,6 +252,7 @@ def run_ours(args):
     dom_ms = prof[dom][0] / max(prof[dom][1], 1)
     per_launch_bytes = bytes_alg.get(dom, 0) / max(1, prof[dom][1] / args.steps)
     achieved = per_launch_bytes / (dom_ms / 1e3) / 1e9 if dom_ms > 0 else 0.0
+    traffic, traffic_src = profiled_traffic(dom, args.config, N)
     out = {
         "metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_step, 3),
@@ -252,7 +267,8 @@ def run_ours(args):
         "gpu_launches": int(launches),
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1),
                      "peak": hbm, "unit": "GB/s", "frac": round(achieved / hbm, 4),
-                     "traffic": None, "peak_source": peak_kind},
+                     "traffic": traffic, "traffic_source": traffic_src,
+                     "algorithmic_bytes": int(per_launch_bytes), "peak_source": peak_kind},
         "kernels_ms_per_step": {f: round(prof[f][0] / args.steps, 4) for f in fams
                                 if prof[f][1] > 0},
         "clocks": clk.summary(),
