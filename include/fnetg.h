@@ -121,6 +121,20 @@ int fnetg_acsf(fnetg_ctx *ctx, double *vals);
  * datapoint weights or 1 if weights is NULL) and returns it; compute = 0 uses the given
  * zprec.  Standardises the device-resident features in place. */
 int fnetg_acsf_zscore(fnetg_ctx *ctx, const int32_t *weights, double *zprec, int32_t compute);
+/* No counterpart in the reference.  The statistics half of fnetg_acsf_zscore(..., compute = 1)
+ * (weighted means and population standard deviations of the ACSF columns of the current,
+ * unstandardised features) for callers that must keep the library from allocating: a host
+ * program that owns a fixed device-memory budget, or a training/serving loop that cannot
+ * afford the device-wide synchronisation of cudaMalloc/cudaFree.  On success the call
+ * allocates no device or host memory: partial sums use a fixed 1 MiB device array inside the
+ * library, weights are read from device memory (d_weights: int32 [nstruct], or NULL for unit
+ * weights) and the result goes to d_zprec (device, double [2 * nG]: means, then deviations).
+ * Asynchronous on the context's stream; the features are not modified.  Limits: 1 <= nG <=
+ * 4095 (FNETG_E_UNSUPPORTED beyond).  The first call on a device looks up the scratch array's
+ * address (make it before any stream capture).  The scratch array is shared per device:
+ * calls that overlap in time (other streams or contexts on the same device) race, so
+ * serialise them. */
+int fnetg_acsf_zscore_stats_noalloc(fnetg_ctx *ctx, const int32_t *d_weights, double *d_zprec);
 /* TFeatures_collect (lib_types/features.F90:200-265): network inputs are
  * [ACSF ; external features ext[:, indices-1]].  n = 0 removes external inputs. */
 int fnetg_set_external_inputs(fnetg_ctx *ctx, int32_t n, const int32_t *indices);
