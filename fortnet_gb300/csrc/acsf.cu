@@ -31,7 +31,14 @@ __global__ void __launch_bounds__(256) acsf_kernel(TileArgs<T> a) {
     const int np = (int)(a.poff[i + 1] - p0);
     const int64_t row = a.bpos[i];
     stage_tile<T>(a, t, i, p0, np, lane, false);
-    if (D > 0 && a.ncombo > 0) compute_moments<T, (D > 0 ? D : 1)>(a, t, np, lane);
+    if (D > 0 && a.ncombo > 0) {
+      compute_moments<T, (D > 0 ? D : 1)>(a, t, np, lane);
+      if (a.mom) {
+        const int nm = a.ncombo * a.n_mono;
+        T *dst = a.mom + i * nm;
+        for (int k = lane; k < nm; k += 32) dst[k] = t.M[k];
+      }
+    }
     // ---- radial functions: lanes over functions, list order
     for (int g = lane; g < a.nrad; g += 32) {
       const GDesc d = a.rad[g];
@@ -303,6 +310,10 @@ template <typename T> int launch_acsf(fnetg_ctx *ctx) {
   TileArgs<T> a;
   fill_tile_args<T>(ctx, a);
   FNETG_CHECK(a.cap <= 65535, FNETG_E_UNSUPPORTED, "more than 65535 neighbours of one atom");
+  if (a.ncombo > 0) {
+    FNETG_CUDA(ctx->d_mom.ensure(sizeof(T) * (size_t)N * a.ncombo * a.n_mono));
+    a.mom = ctx->d_mom.as<T>();
+  }
   switch (ctx->mom_degree) {
     case 0: return launch_acsf_d<T, 0>(ctx, a);
     case 1: return launch_acsf_d<T, 1>(ctx, a);
@@ -413,6 +424,7 @@ int run_acsf(fnetg_ctx *ctx) {
   int rc = ctx->prec == FNETG_FP64 ? launch_acsf<double>(ctx) : launch_acsf<float>(ctx);
   if (rc) return rc;
   ctx->feats_valid = true;
+  ctx->mom_valid = ctx->n_combo > 0 && ctx->N > 0;
   return FNETG_OK;
 }
 

@@ -214,6 +214,7 @@ int64_t fnetg_launch_count(fnetg_ctx *ctx) { return ctx ? ctx->launches : -1; }
 static void invalidate_geometry(fnetg_ctx *ctx) {
   ctx->nb_valid = false;
   ctx->feats_valid = false;
+  ctx->mom_valid = false;
 }
 
 static int rebuild_buckets(fnetg_ctx *ctx, bool order_changes);
@@ -698,6 +699,7 @@ int fnetg_set_gfunctions(fnetg_ctx *ctx, int32_t ng, const fnetg_gfunc *g) {
   }
   ctx->nb_valid = false;
   ctx->feats_valid = false;
+  ctx->mom_valid = false;
   ctx->zprec_valid = false;
   ctx->nf = ng + (int)ctx->ext_idx.size();
   return refresh_codes(ctx);

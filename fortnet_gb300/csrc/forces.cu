@@ -246,7 +246,13 @@ __global__ void __launch_bounds__(256) forces_kernel(TileArgs<T> a) {
     // ---- integer-xi G5 through adjoint moments
     if (D > 0 && a.ncombo > 0) {
       constexpr int NM = n_mono_of(D > 0 ? D : 1);
-      compute_moments<T, (D > 0 ? D : 1)>(a, tl, np, lane);
+      if (a.mom_cached) {
+        const T *src = a.mom + i * (a.ncombo * NM);
+        for (int k = lane; k < a.ncombo * NM; k += 32) tl.M[k] = src[k];
+        __syncwarp();
+      } else {
+        compute_moments<T, (D > 0 ? D : 1)>(a, tl, np, lane);
+      }
       for (int it = lane; it < a.ncombo * NM; it += 32) {
         const int k = it / NM, al = it - k * NM;
         T acc = 0;
@@ -420,6 +426,10 @@ template <typename T> int launch_forces(fnetg_ctx *ctx) {
   fill_tile_args_forces<T>(ctx, a);
   a.J = ctx->d_jacT.as<T>();
   a.F = ctx->d_forces.as<double>();
+  if (ctx->mom_valid) {
+    a.mom = ctx->d_mom.as<T>();
+    a.mom_cached = 1;
+  }
   a.nout = nout;
   switch (ctx->mom_degree) {
     case 0: return launch_forces_d<T, 0>(ctx, a, nout);

@@ -148,6 +148,10 @@ struct fnetg_ctx {
   bool d2_valid = false;
   double max_extent = 0.0;  // largest structure bounding-box extent (Bohr)
   fnetg::DBuf d_img_off, d_imgs, d_imgs_f;
+  // G5 moments of every atom from the last ACSF launch ([N][ncombo][n_mono], compute width),
+  // reused by the force kernel while geometry, pairs and functions are unchanged
+  bool mom_valid = false;
+  fnetg::DBuf d_mom;
   fnetg::DBuf d_pcount, d_poff, d_pj, d_pmeta, d_rij, d_d2, d_scan_tmp, d_maxp, d_rcls2;
 
   // features (bucketed rows, compute precision)

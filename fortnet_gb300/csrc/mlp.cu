@@ -354,11 +354,11 @@ template <typename T> struct MlpArgs {
 // chunk rows -> X[k][r] (zero rows past the tile's end), global reads coalesced along k
 template <typename T>
 __device__ void load_features(const MlpArgs<T> &a, int64_t row0, int nrows, T *X) {
-  const int nf = a.nf;
-  for (int e = threadIdx.x; e < a.RC * nf; e += blockDim.x) {
-    const int r = e / nf, k = e - r * nf;
-    X[(int64_t)k * a.RCP + r] = r < nrows ? a.feat[(row0 + r) * nf + k] : (T)0;
-  }
+  // warp per row, lanes along the row
+  const int nf = a.nf, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  for (int r = threadIdx.x >> 5; r < a.RC; r += nw)
+    for (int k = lane; k < nf; k += 32)
+      X[(int64_t)k * a.RCP + r] = r < nrows ? a.feat[(row0 + r) * nf + k] : (T)0;
 }
 
 template <typename T>
@@ -384,9 +384,9 @@ __global__ void __launch_bounds__(kMlpThreads) mlp_forward_kernel(MlpArgs<T> a) 
       __syncthreads();
       in = dst;
     }
-    for (int e = threadIdx.x; e < nrows * nout; e += blockDim.x) {
-      const int r = e / nout, o = e - r * nout;
-      a.out[(int64_t)a.bperm[row0 + r] * nout + o] = (double)in[(int64_t)o * a.RCP + r];
+    for (int r = threadIdx.x; r < nrows; r += blockDim.x) {
+      const int64_t atom = a.bperm[row0 + r];
+      for (int o = 0; o < nout; o++) a.out[atom * nout + o] = (double)in[(int64_t)o * a.RCP + r];
     }
     __syncthreads();
   }
@@ -423,10 +423,8 @@ __global__ void __launch_bounds__(kMlpThreads) mlp_jacobian_kernel(MlpArgs<T> a)
     forward_keep(a, P, pl, sm);
     // delta of the (linear) output layer: the unit vector of output jac_out
     T *dcur = sm + pl.D0, *dnext = sm + pl.D1;
-    for (int e = threadIdx.x; e < nout * a.RC; e += blockDim.x) {
-      const int o = e / a.RC, r = e - o * a.RC;
-      dcur[(int64_t)o * a.RCP + r] = (o == a.jac_out) ? (T)1 : (T)0;
-    }
+    for (int r = threadIdx.x; r < a.RC; r += blockDim.x)
+      for (int o = 0; o < nout; o++) dcur[(int64_t)o * a.RCP + r] = (o == a.jac_out) ? (T)1 : (T)0;
     __syncthreads();
     for (int l = L - 2; l >= 1; l--) {
       layer_backward<T>(dcur, n.dims[l + 1], P + n.ct[l], n.dims[l], sm + pl.F[l], dnext, a.RC,
@@ -440,8 +438,9 @@ __global__ void __launch_bounds__(kMlpThreads) mlp_jacobian_kernel(MlpArgs<T> a)
     T *J = sm + pl.A[0];
     layer_backward<T>(dcur, n.dims[1], P + n.ct[0], n.dims[0], nullptr, J, a.RC, a.RCP);
     __syncthreads();
-    for (int e = threadIdx.x; e < nrows * nf; e += blockDim.x) {
-      const int r = e / nf, k = e - r * nf;
+    const int lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    for (int r = threadIdx.x >> 5; r < nrows; r += nw)
+    for (int k = lane; k < nf; k += 32) {
       const T v = J[(int64_t)k * a.RCP + r];
       const int64_t atom = a.bperm[row0 + r];
       if (a.jac64) a.jac64[atom * nf + k] = (double)v;
@@ -483,10 +482,10 @@ __global__ void __launch_bounds__(kMlpThreads) mlp_backward_kernel(MlpArgs<T> a)
     forward_keep(a, P, pl, sm);
     // output deltas (linear output layer): scaled loss gradients; zero past the tile's end
     T *dcur = sm + pl.D0, *dnext = sm + pl.D1;
-    for (int e = threadIdx.x; e < nout * a.RC; e += blockDim.x) {
-      const int o = e / a.RC, r = e - o * a.RC;
-      dcur[(int64_t)o * a.RCP + r] =
-          r < nrows ? (T)a.delta_out[(int64_t)a.bperm[row0 + r] * nout + o] : (T)0;
+    for (int r = threadIdx.x; r < a.RC; r += blockDim.x) {
+      const int64_t atom = r < nrows ? a.bperm[row0 + r] : 0;
+      for (int o = 0; o < nout; o++)
+        dcur[(int64_t)o * a.RCP + r] = r < nrows ? (T)a.delta_out[atom * nout + o] : (T)0;
     }
     __syncthreads();
     for (int l = L - 2; l >= 0; l--) {

@@ -542,6 +542,7 @@ int run_neighbors(fnetg_ctx *ctx, double rcut) {
   ctx->nb_rcut = rcut;
   ctx->nb_valid = true;
   ctx->feats_valid = false;
+  ctx->mom_valid = false;
   return FNETG_OK;
 }
 

@@ -176,6 +176,10 @@ template <typename T> struct TileArgs {
   int ncombo;
   const int32_t *cidx;    // [(nz+1)*necls]
   int n_mono;
+  // moment cache [natoms][ncombo][n_mono]: written by the ACSF kernel (mom != null), read by
+  // the force kernel when mom_cached
+  T *mom;
+  int mom_cached;
   // values
   T *feat;
   int nf;
