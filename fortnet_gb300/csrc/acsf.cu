@@ -24,7 +24,8 @@ __global__ void __launch_bounds__(256) acsf_kernel(TileArgs<T> a) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int wpb = blockDim.x >> 5;
   const size_t tb =
-      tile_bytes<T>(a.cap, a.nrcls, a.necls, a.nz, a.ncombo, a.n_mono, a.ng, false, a.ngroups > 0);
+      tile_bytes<T>(a.cap, a.nrcls, a.necls, a.nz, a.ncombo, a.n_mono, a.ng, false, a.ngroups > 0,
+                    tile_etab(a, false));
   Tile<T> t = carve_tile<T>(smem + tb * warp, a, false);
   for (int64_t i = (int64_t)blockIdx.x * wpb + warp; i < a.natoms; i += (int64_t)gridDim.x * wpb) {
     const int64_t p0 = a.poff[i];
@@ -287,7 +288,8 @@ template <typename T> void fill_tile_args(fnetg_ctx *ctx, TileArgs<T> &a) {
 template <typename T, int D> int launch_acsf_d(fnetg_ctx *ctx, TileArgs<T> &a) {
   const int64_t N = ctx->N;
   const size_t tb =
-      tile_bytes<T>(a.cap, a.nrcls, a.necls, a.nz, a.ncombo, a.n_mono, a.ng, false, a.ngroups > 0);
+      tile_bytes<T>(a.cap, a.nrcls, a.necls, a.nz, a.ncombo, a.n_mono, a.ng, false, a.ngroups > 0,
+                    tile_etab(a, false));
   int wpb = 1, per_sm = 1;
   size_t smem = 0;
   const cudaError_t err = pick_warps(acsf_kernel<T, D>, 0, tb, wpb, smem, per_sm);

@@ -122,30 +122,38 @@ __device__ void angular_side(const TileArgs<T> &a, Tile<T> &tl, const AGroup &G,
 }
 
 
-// Per-pair derivative of the moment terms, degree D known at compile time.  The eta classes
-// are folded first (the derivative is linear in the adjoint moments):
-//   cD(alpha) = sum_e D_e Qc_e(alpha),  cE(alpha) = sum_e E_e Qc_e(alpha),
-//   w += P_D(u) u + (grad P_E(u) - (grad P_E(u) . u) u) / r
-// with P_c(u) = sum_alpha c(alpha) u^alpha.
+// E_e(r) = exp(-eta_e r^2) fc(r) [id_i id_j] and D_e = dE_e/dr of pair q, from the tables when
+// the tile keeps them, else from the cutoff tables (the same operations as stage_tile).
+template <typename T>
+__device__ __forceinline__ void pair_e_d(const TileArgs<T> &a, const Tile<T> &tl, int q, int e,
+                                         T r, int64_t i, T &E, T &Dv) {
+  if (tl.E) {
+    E = tl.E[e * a.cap + q];
+    Dv = tl.D[e * a.cap + q];
+    return;
+  }
+  const T eta = a.ecls_eta[e];
+  const int rc = a.ecls_rclass[e];
+  const int aid = a.ecls_atomid[e];
+  const T f = tl.fc[rc * a.cap + q], df = tl.dfc[rc * a.cap + q];
+  T ids = (T)1;
+  if (aid > 0) ids = atom_id<T>(a.ext, a.next, aid, i) * atom_id<T>(a.ext, a.next, aid, tl.pj[q]);
+  const T ex = m_exp<T>(-(eta * (r * r)));
+  E = ex * f * ids;
+  Dv = ex * (df - (T)2 * eta * r * f) * ids;
+}
+
+// Per-pair derivative of the moment terms, degree D known at compile time.  Linear in the
+// adjoint moments, so with c_D(alpha) = sum_e D_e Qc_e(alpha) and c_E(alpha) = sum_e E_e Qc_e(alpha)
+//   w += P_D(u) u + (grad P_E(u) - (grad P_E(u) . u) u) / r,   P_c(u) = sum_alpha c(alpha) u^alpha.
+// Up to four eta classes are folded inside the unrolled monomial loop (no coefficient arrays
+// stay live); more classes take one polynomial pass per class.
 template <typename T, int D>
 __device__ __forceinline__ void moment_pair_force(const TileArgs<T> &a, Tile<T> &tl, int q,
-                                                  int zz) {
+                                                  int zz, int64_t i) {
   constexpr int NM = n_mono_of(D);
   const V4<T> u = tl.u[q];
-  T cD[NM], cE[NM];
-#pragma unroll
-  for (int al = 0; al < NM; al++) cD[al] = cE[al] = (T)0;
-  const T *Qz = tl.Qc + (int64_t)zz * a.necls * NM;
-  for (int e = 0; e < a.necls; e++) {
-    const T Ee = tl.E[e * a.cap + q], De = tl.D[e * a.cap + q];
-    const T *Qe = Qz + e * NM;
-#pragma unroll
-    for (int al = 0; al < NM; al++) {
-      const T qv = Qe[al];
-      cD[al] += De * qv;
-      cE[al] += Ee * qv;
-    }
-  }
+  const T r = u.w;
   T px[D + 1], py[D + 1], pz[D + 1];
   px[0] = py[0] = pz[0] = (T)1;
 #pragma unroll
@@ -155,16 +163,54 @@ __device__ __forceinline__ void moment_pair_force(const TileArgs<T> &a, Tile<T> 
     pz[d] = pz[d - 1] * u.z;
   }
   T P = 0, gx = 0, gy = 0, gz = 0;
+  const T *Qz = tl.Qc + (int64_t)zz * a.necls * NM;
+  if (a.necls <= 4) {
+    T Ee[4], De[4];
 #pragma unroll
-  for (int al = 0; al < NM; al++) {
-    const int ea = kMonoTab[al][0], eb = kMonoTab[al][1], ec = kMonoTab[al][2];
-    P += cD[al] * (px[ea] * py[eb] * pz[ec]);
-    if (ea > 0) gx += ((T)ea * cE[al]) * (px[ea > 0 ? ea - 1 : 0] * py[eb] * pz[ec]);
-    if (eb > 0) gy += ((T)eb * cE[al]) * (px[ea] * py[eb > 0 ? eb - 1 : 0] * pz[ec]);
-    if (ec > 0) gz += ((T)ec * cE[al]) * (px[ea] * py[eb] * pz[ec > 0 ? ec - 1 : 0]);
+    for (int e = 0; e < 4; e++) {
+      Ee[e] = De[e] = (T)0;
+      if (e < a.necls) pair_e_d<T>(a, tl, q, e, r, i, Ee[e], De[e]);
+    }
+#pragma unroll
+    for (int al = 0; al < NM; al++) {
+      T cd = 0, ce = 0;
+#pragma unroll
+      for (int e = 0; e < 4; e++) {
+        if (e < a.necls) {
+          const T qv = Qz[e * NM + al];
+          cd += De[e] * qv;
+          ce += Ee[e] * qv;
+        }
+      }
+      const int ea = kMonoTab[al][0], eb = kMonoTab[al][1], ec = kMonoTab[al][2];
+      P += cd * (px[ea] * py[eb] * pz[ec]);
+      if (ea > 0) gx += ((T)ea * ce) * (px[ea > 0 ? ea - 1 : 0] * py[eb] * pz[ec]);
+      if (eb > 0) gy += ((T)eb * ce) * (px[ea] * py[eb > 0 ? eb - 1 : 0] * pz[ec]);
+      if (ec > 0) gz += ((T)ec * ce) * (px[ea] * py[eb] * pz[ec > 0 ? ec - 1 : 0]);
+    }
+  } else {
+    for (int e = 0; e < a.necls; e++) {
+      T Ev, Dv;
+      pair_e_d<T>(a, tl, q, e, r, i, Ev, Dv);
+      const T *Qe = Qz + e * NM;
+      T pe = 0, hx = 0, hy = 0, hz = 0;
+#pragma unroll
+      for (int al = 0; al < NM; al++) {
+        const T qv = Qe[al];
+        const int ea = kMonoTab[al][0], eb = kMonoTab[al][1], ec = kMonoTab[al][2];
+        pe += qv * (px[ea] * py[eb] * pz[ec]);
+        if (ea > 0) hx += ((T)ea * qv) * (px[ea > 0 ? ea - 1 : 0] * py[eb] * pz[ec]);
+        if (eb > 0) hy += ((T)eb * qv) * (px[ea] * py[eb > 0 ? eb - 1 : 0] * pz[ec]);
+        if (ec > 0) hz += ((T)ec * qv) * (px[ea] * py[eb] * pz[ec > 0 ? ec - 1 : 0]);
+      }
+      P += Dv * pe;
+      gx += Ev * hx;
+      gy += Ev * hy;
+      gz += Ev * hz;
+    }
   }
   const T gu = gx * u.x + gy * u.y + gz * u.z;
-  const T ir = (T)1 / u.w;
+  const T ir = (T)1 / r;
   tl.w[q].x += P * u.x + ir * (gx - gu * u.x);
   tl.w[q].y += P * u.y + ir * (gy - gu * u.y);
   tl.w[q].z += P * u.z + ir * (gz - gu * u.z);
@@ -186,7 +232,8 @@ __global__ void __launch_bounds__(256) forces_kernel(TileArgs<T> a) {
   extern __shared__ __align__(128) unsigned char smem[];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int wpb = blockDim.x >> 5;
-  const size_t tb = tile_bytes<T>(a.cap, a.nrcls, a.necls, a.nz, a.ncombo, a.n_mono, a.ng, true, a.ngroups > 0);
+  const size_t tb = tile_bytes<T>(a.cap, a.nrcls, a.necls, a.nz, a.ncombo, a.n_mono, a.ng, true, a.ngroups > 0,
+                    tile_etab(a, true));
   RadEntry<T> *rt = reinterpret_cast<RadEntry<T> *>(smem);
   for (int g = threadIdx.x; g < a.nrad; g += blockDim.x) {
     const GDesc d = a.rad[g];
@@ -281,7 +328,7 @@ __global__ void __launch_bounds__(256) forces_kernel(TileArgs<T> a) {
         const uint32_t inf = tl.info[q];
         if ((inf >> 8) & 1u) continue;
         const int z = (int)(inf & 0xff);
-        moment_pair_force<T, (D > 0 ? D : 1)>(a, tl, q, z < a.nz ? z : a.nz);
+        moment_pair_force<T, (D > 0 ? D : 1)>(a, tl, q, z < a.nz ? z : a.nz, i);
       }
     }
     __syncwarp();
@@ -391,7 +438,8 @@ template <typename T> void fill_tile_args_forces(fnetg_ctx *ctx, TileArgs<T> &a)
 
 template <typename T, int D> int launch_forces_d(fnetg_ctx *ctx, TileArgs<T> &a, int nout) {
   const int64_t N = ctx->N;
-  const size_t tb = tile_bytes<T>(a.cap, a.nrcls, a.necls, a.nz, a.ncombo, a.n_mono, a.ng, true, a.ngroups > 0);
+  const size_t tb = tile_bytes<T>(a.cap, a.nrcls, a.necls, a.nz, a.ncombo, a.n_mono, a.ng, true, a.ngroups > 0,
+                    tile_etab(a, true));
   const size_t rb = radtab_bytes<T>(a.nrad);
   int wpb = 1, per_sm = 1;
   size_t smem = 0;

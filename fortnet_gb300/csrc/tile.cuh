@@ -210,13 +210,21 @@ template <typename T> struct Tile {
   uint16_t *lists;  // [nz][cap]
 };
 
+// Whether a tile keeps per-pair E/D tables: the value kernel always; the force kernel for
+// triplet groups or when the moments are recomputed rather than read from the cache.
+template <typename T> __host__ __device__ inline bool tile_etab(const TileArgs<T> &a, bool forces) {
+  return !forces || a.ngroups > 0 || !a.mom_cached;
+}
+
 template <typename T>
 __host__ __device__ inline size_t tile_bytes(int cap, int nrcls, int necls, int nz, int ncombo,
-                                             int nmono, int ng, bool forces, bool trip) {
-  // v and idv serve the triplet sweep only
+                                             int nmono, int ng, bool forces, bool trip,
+                                             bool etab) {
+  // v and idv serve the triplet sweep only; the E (and, for forces, D) tables are kept when
+  // etab (values, triplets, or moments not taken from the cache)
   size_t b = 0;
   b += sizeof(V4<T>) * cap * ((forces ? 2 : 1) + (trip ? 1 : 0));
-  b += sizeof(T) * (size_t)cap * (nrcls + necls) * (forces ? 2 : 1);
+  b += sizeof(T) * (size_t)cap * (nrcls + (etab ? necls : 0)) * (forces ? 2 : 1);
   if (trip) b += sizeof(T) * cap;             // idv
   b += sizeof(T) * 5 * 32;                    // gpar
   b += sizeof(T) * (size_t)ncombo * nmono * (forces ? 2 : 1);
@@ -246,16 +254,22 @@ __device__ Tile<T> carve_tile(unsigned char *p, const TileArgs<T> &a, bool force
     t.w = reinterpret_cast<V4<T> *>(p);
     p += sizeof(V4<T>) * cap;
   }
+  const bool etab = tile_etab(a, forces);
   t.fc = reinterpret_cast<T *>(p);
   p += sizeof(T) * (size_t)cap * a.nrcls;
-  t.E = reinterpret_cast<T *>(p);
-  p += sizeof(T) * (size_t)cap * a.necls;
+  t.E = nullptr;
+  if (etab) {
+    t.E = reinterpret_cast<T *>(p);
+    p += sizeof(T) * (size_t)cap * a.necls;
+  }
   t.dfc = t.D = nullptr;
   if (forces) {
     t.dfc = reinterpret_cast<T *>(p);
     p += sizeof(T) * (size_t)cap * a.nrcls;
-    t.D = reinterpret_cast<T *>(p);
-    p += sizeof(T) * (size_t)cap * a.necls;
+    if (etab) {
+      t.D = reinterpret_cast<T *>(p);
+      p += sizeof(T) * (size_t)cap * a.necls;
+    }
   }
   t.idv = nullptr;
   if (trip) {
@@ -344,7 +358,7 @@ __device__ void stage_tile(const TileArgs<T> &a, Tile<T> &t, int64_t i, int64_t 
       t.fc[rc * a.cap + q] = in ? fcv : (T)0;
       if (forces) t.dfc[rc * a.cap + q] = in ? dfv : (T)0;
     }
-    for (int e = 0; e < a.necls; e++) {
+    for (int e = 0; t.E && e < a.necls; e++) {
       const T eta = a.ecls_eta[e];
       const int aid = a.ecls_atomid[e];
       const int rc = a.ecls_rclass[e];
