@@ -29,7 +29,7 @@ __global__ void __launch_bounds__(256) acsf_kernel(TileArgs<T> a) {
   Tile<T> t = carve_tile<T>(smem + tb * warp, a, false);
   for (int64_t i = (int64_t)blockIdx.x * wpb + warp; i < a.natoms; i += (int64_t)gridDim.x * wpb) {
     const int64_t p0 = a.poff[i];
-    const int np = (int)(a.poff[i + 1] - p0);
+    const int np = (int)(a.pend[i] - p0);
     const int64_t row = a.bpos[i];
     stage_tile<T>(a, t, i, p0, np, lane, false);
     if (D > 0 && a.ncombo > 0) {
@@ -248,6 +248,7 @@ template <typename T> void fill_tile_args(fnetg_ctx *ctx, TileArgs<T> &a) {
   a = TileArgs<T>{};
   a.natoms = ctx->N;
   a.poff = ctx->d_poff.as<int64_t>();
+  a.pend = pair_end(ctx);
   a.pj = ctx->d_pj.as<int32_t>();
   a.pmeta = ctx->d_pmeta.as<uint32_t>();
   a.rij = static_cast<const V4<T> *>(ctx->d_rij.p);

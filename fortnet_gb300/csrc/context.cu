@@ -723,22 +723,35 @@ int fnetg_get_neighbors(fnetg_ctx *ctx, int64_t *pair_offsets, int32_t *j, int32
   if (!ctx) return FNETG_E_INVALID;
   FNETG_CHECK(ctx->nb_valid, FNETG_E_INVALID, "get_neighbors: no neighbour list");
   FNETG_CUDA(cudaStreamSynchronize(ctx->stream));
-  const int64_t N = ctx->N, P = ctx->P;
-  std::vector<int64_t> off(N + 1);
-  FNETG_CUDA(cudaMemcpy(off.data(), ctx->d_poff.p, sizeof(int64_t) * (N + 1),
-                        cudaMemcpyDeviceToHost));
+  const int64_t N = ctx->N, P = ctx->P, slots = ctx->pslots;
+  // device [begin, end) of every atom -> compact offsets
+  std::vector<int64_t> beg(std::max<int64_t>(N, 1)), end(std::max<int64_t>(N, 1)), off(N + 1, 0);
+  if (N > 0) {
+    FNETG_CUDA(cudaMemcpy(beg.data(), ctx->d_poff.p, sizeof(int64_t) * N, cudaMemcpyDeviceToHost));
+    FNETG_CUDA(cudaMemcpy(end.data(), fnetg::pair_end(ctx), sizeof(int64_t) * N,
+                          cudaMemcpyDeviceToHost));
+  }
+  for (int64_t a = 0; a < N; a++) off[a + 1] = off[a] + (end[a] - beg[a]);
+  FNETG_CHECK(off[N] == P, FNETG_E_CUDA, "get_neighbors: inconsistent pair offsets");
   if (pair_offsets) memcpy(pair_offsets, off.data(), sizeof(int64_t) * (N + 1));
+  auto compact = [&](const auto *src, auto *dst) {
+    for (int64_t a = 0; a < N; a++)
+      for (int64_t q = 0; q < end[a] - beg[a]; q++) dst[off[a] + q] = src[beg[a] + q];
+  };
   if (j && P > 0) {
-    FNETG_CUDA(cudaMemcpy(j, ctx->d_pj.p, sizeof(int32_t) * P, cudaMemcpyDeviceToHost));
+    std::vector<int32_t> all(slots);
+    FNETG_CUDA(cudaMemcpy(all.data(), ctx->d_pj.p, sizeof(int32_t) * slots, cudaMemcpyDeviceToHost));
+    compact(all.data(), j);
     // convert to structure-local indices
     for (int s = 0; s < ctx->S; s++)
       for (int64_t a = ctx->h_off[s]; a < ctx->h_off[s + 1]; a++)
         for (int64_t q = off[a]; q < off[a + 1]; q++) j[q] -= (int32_t)ctx->h_off[s];
   }
   if (shift && P > 0) {
-    std::vector<uint32_t> meta(P);
-    FNETG_CUDA(cudaMemcpy(meta.data(), ctx->d_pmeta.p, sizeof(uint32_t) * P,
+    std::vector<uint32_t> all(slots), meta(P);
+    FNETG_CUDA(cudaMemcpy(all.data(), ctx->d_pmeta.p, sizeof(uint32_t) * slots,
                           cudaMemcpyDeviceToHost));
+    compact(all.data(), meta.data());
     for (int64_t q = 0; q < P; q++)
       for (int c = 0; c < 3; c++) shift[3 * q + c] = (int32_t)(int8_t)((meta[q] >> (8 * c)) & 0xff);
   }
@@ -746,7 +759,9 @@ int fnetg_get_neighbors(fnetg_ctx *ctx, int64_t *pair_offsets, int32_t *j, int32
     int rc = pair_d2(ctx);
     if (rc) return rc;
     FNETG_CUDA(cudaStreamSynchronize(ctx->stream));
-    FNETG_CUDA(cudaMemcpy(d2, ctx->d_d2.p, sizeof(double) * P, cudaMemcpyDeviceToHost));
+    std::vector<double> all(slots);
+    FNETG_CUDA(cudaMemcpy(all.data(), ctx->d_d2.p, sizeof(double) * slots, cudaMemcpyDeviceToHost));
+    compact(all.data(), d2);
   }
   return FNETG_OK;
 }

@@ -245,7 +245,7 @@ __global__ void __launch_bounds__(256) forces_kernel(TileArgs<T> a) {
   Tile<T> tl = carve_tile<T>(smem + radtab_bytes<T>(a.nrad) + tb * warp, a, true);
   for (int64_t i = (int64_t)blockIdx.x * wpb + warp; i < a.natoms; i += (int64_t)gridDim.x * wpb) {
     const int64_t p0 = a.poff[i];
-    const int np = (int)(a.poff[i + 1] - p0);
+    const int np = (int)(a.pend[i] - p0);
     for (int g = lane; g < a.ng; g += 32) tl.jv[g] = a.J[i * a.nf + g];
     stage_tile<T>(a, tl, i, p0, np, lane, true);
     // ---- radial: lanes over pairs, each over the all-atom functions and its species' own
@@ -398,6 +398,7 @@ template <typename T> void fill_tile_args_forces(fnetg_ctx *ctx, TileArgs<T> &a)
   a = TileArgs<T>{};
   a.natoms = ctx->N;
   a.poff = ctx->d_poff.as<int64_t>();
+  a.pend = pair_end(ctx);
   a.pj = ctx->d_pj.as<int32_t>();
   a.pmeta = ctx->d_pmeta.as<uint32_t>();
   a.rij = static_cast<const V4<T> *>(ctx->d_rij.p);

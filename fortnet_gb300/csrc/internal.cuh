@@ -152,7 +152,13 @@ struct fnetg_ctx {
   // reused by the force kernel while geometry, pairs and functions are unchanged
   bool mom_valid = false;
   fnetg::DBuf d_mom;
-  fnetg::DBuf d_pcount, d_poff, d_pj, d_pmeta, d_rij, d_d2, d_scan_tmp, d_maxp, d_rcls2;
+  // Pairs of atom i: [poff[i], pend[i]).  Counted builds store them compactly (CSR, pend =
+  // poff + 1); slab builds at [i * cap, i * cap + count) with an explicit end array.
+  bool pslab = false;
+  int64_t pslots = 0;       // allocated pair slots (P when compact)
+  int64_t nb_cap_hint = 0;  // per-atom capacity for the next slab build (0: count first)
+  int64_t nb_hint_n = -1;   // atom count the capacity was measured on
+  fnetg::DBuf d_pcount, d_poff, d_pend, d_pj, d_pmeta, d_rij, d_d2, d_scan_tmp, d_maxp, d_rcls2;
 
   // features (bucketed rows, compute precision)
   int nf = 0;
@@ -233,6 +239,7 @@ void resolve_profile(fnetg_ctx *c);
 int run_neighbors(fnetg_ctx *ctx, double rcut);
 int prepare_coords(fnetg_ctx *ctx);
 int pair_d2(fnetg_ctx *ctx);
+const int64_t *pair_end(fnetg_ctx *ctx);  // device end offsets of every atom's pairs
 int run_acsf(fnetg_ctx *ctx);
 int run_zscore(fnetg_ctx *ctx, const int32_t *weights, bool compute);
 int run_ext_inputs(fnetg_ctx *ctx);

@@ -46,6 +46,12 @@ struct NbArgs {
   void *rij;              // V4<T>
   double *d2out;          // optional
   int *maxp;
+  // slab fill (slab_cap > 0): atom i's pairs at [i * slab_cap, i * slab_cap + count), the pass
+  // counts as well; begin/end offsets, overflow flag (count > slab_cap) and the pair total
+  int64_t slab_cap;
+  int64_t *pbeg, *pend;
+  int *overflow;
+  unsigned long long *total;
 };
 
 __device__ __forceinline__ double exact_d2(const double *ci, const double *cj, const double *cv,
@@ -109,7 +115,11 @@ __device__ __forceinline__ float disp_df(float ah, float al, float bh, float bl,
 template <typename T, bool kFill>
 __global__ void __launch_bounds__(256) nb_kernel(NbArgs a) {
   __shared__ int blk_max;
-  if (threadIdx.x == 0) blk_max = 0;
+  __shared__ unsigned long long blk_sum;
+  if (threadIdx.x == 0) {
+    blk_max = 0;
+    blk_sum = 0;
+  }
   __syncthreads();
   const int lane = threadIdx.x & 31;
   const int64_t i = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
@@ -122,7 +132,7 @@ __global__ void __launch_bounds__(256) nb_kernel(NbArgs a) {
     const V4<float> cif = a.cf[i];
     const V4<float> cil = a.cl[i];
     int64_t wpos = 0;
-    if (kFill) wpos = a.poff[i];
+    if (kFill) wpos = a.slab_cap > 0 ? i * a.slab_cap : a.poff[i];
     int64_t cnt = 0;
     const float *bb = a.bbox + 6 * s;
     const int64_t im0 = a.img_off[s], im1 = a.img_off[s + 1];
@@ -169,9 +179,10 @@ __global__ void __launch_bounds__(256) nb_kernel(NbArgs a) {
           }
         }
         const unsigned m = __ballot_sync(0xffffffffu, ok);
-        if (kFill && ok) {
+        const int64_t rank = cnt + __popc(m & ((1u << lane) - 1u));
+        if (kFill && ok && (a.slab_cap == 0 || rank < a.slab_cap)) {
           const int64_t j = a0 + jl;
-          const int64_t q = wpos + cnt + __popc(m & ((1u << lane) - 1u));
+          const int64_t q = wpos + rank;
           a.pj[q] = (int32_t)j;
           uint32_t mask = 0;
           V4<T> v;
@@ -213,27 +224,37 @@ __global__ void __launch_bounds__(256) nb_kernel(NbArgs a) {
         cnt += __popc(m);
       }
     }
-    if (!kFill && lane == 0) {
+    if ((!kFill || a.slab_cap > 0) && lane == 0) {
       a.count[i] = cnt;
       atomicMax(&blk_max, (int)cnt);
+      if (kFill) {
+        a.pbeg[i] = wpos;
+        a.pend[i] = wpos + min(cnt, a.slab_cap);
+        if (cnt > a.slab_cap) atomicExch(a.overflow, 1);
+        atomicAdd(&blk_sum, (unsigned long long)cnt);
+      }
     }
   }
-  if (!kFill) {
+  if (!kFill || a.slab_cap > 0) {
     __syncthreads();
-    if (threadIdx.x == 0) atomicMax(a.maxp, blk_max);
+    if (threadIdx.x == 0) {
+      atomicMax(a.maxp, blk_max);
+      if (kFill) atomicAdd(a.total, blk_sum);
+    }
   }
 }
 
 // exact squared distances of every stored pair (parity downloads only)
-__global__ void pair_d2_kernel(const int64_t *poff, const int32_t *pj, const uint32_t *pmeta,
-                               const int32_t *astruct, const double *coords, const double *lat,
-                               int64_t natoms, double *d2out) {
+__global__ void pair_d2_kernel(const int64_t *poff, const int64_t *pend, const int32_t *pj,
+                               const uint32_t *pmeta, const int32_t *astruct,
+                               const double *coords, const double *lat, int64_t natoms,
+                               double *d2out) {
   const int lane = threadIdx.x & 31;
   const int64_t i = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   if (i >= natoms) return;
   const double ci[3] = {coords[3 * i], coords[3 * i + 1], coords[3 * i + 2]};
   const double *L = lat + 9 * astruct[i];
-  for (int64_t q = poff[i] + lane; q < poff[i + 1]; q += 32) {
+  for (int64_t q = poff[i] + lane; q < pend[i]; q += 32) {
     const uint32_t m = pmeta[q];
     const int n1 = (int8_t)(m & 0xff), n2 = (int8_t)((m >> 8) & 0xff), n3 = (int8_t)((m >> 16) & 0xff);
     double cv[3] = {0.0, 0.0, 0.0};
@@ -501,6 +522,55 @@ int run_neighbors(fnetg_ctx *ctx, double rcut) {
   a.maxp = ctx->d_maxp.as<int>();
   const int threads = 256, wpb = threads / 32;
   const int blocks = std::max(1, ceil_div(N, wpb));
+  const size_t es = ctx->prec == FNETG_FP64 ? 8 : 4;
+  // Slab pass: with a per-atom capacity from the previous build of this dataset, one pass
+  // finds, counts and stores the pairs; an atom beyond the capacity sends the build down the
+  // counted path below.
+  if (N > 0 && ctx->nb_cap_hint > 0 && ctx->nb_hint_n == N) {
+    const int64_t cap = ctx->nb_cap_hint, slots = N * cap;
+    FNETG_CUDA(ctx->d_pj.ensure(sizeof(int32_t) * slots));
+    FNETG_CUDA(ctx->d_pmeta.ensure(sizeof(uint32_t) * slots));
+    FNETG_CUDA(ctx->d_rij.ensure(4 * es * slots));
+    FNETG_CUDA(ctx->d_pend.ensure(sizeof(int64_t) * N));
+    a.slab_cap = cap;
+    a.poff = nullptr;
+    a.pbeg = ctx->d_poff.as<int64_t>();
+    a.pend = ctx->d_pend.as<int64_t>();
+    a.overflow = ctx->d_maxp.as<int>() + 1;
+    a.total = reinterpret_cast<unsigned long long *>(ctx->d_maxp.as<int>() + 2);
+    a.pj = ctx->d_pj.as<int32_t>();
+    a.pmeta = ctx->d_pmeta.as<uint32_t>();
+    a.rij = ctx->d_rij.p;
+    a.d2out = nullptr;
+    {
+      LaunchScope ls(ctx, "neighbors");
+      if (ctx->prec == FNETG_FP64)
+        nb_kernel<double, true><<<blocks, threads, 0, ctx->stream>>>(a);
+      else
+        nb_kernel<float, true><<<blocks, threads, 0, ctx->stream>>>(a);
+      FNETG_CUDA(cudaGetLastError());
+    }
+    int flags[4] = {0, 0, 0, 0};
+    FNETG_CUDA(cudaMemcpyAsync(flags, ctx->d_maxp.p, sizeof(int) * 4, cudaMemcpyDeviceToHost,
+                               ctx->stream));
+    FNETG_CUDA(cudaStreamSynchronize(ctx->stream));
+    if (flags[1] == 0) {
+      unsigned long long total = 0;
+      std::memcpy(&total, flags + 2, sizeof total);
+      ctx->P = (int64_t)total;
+      ctx->pslots = slots;
+      ctx->pslab = true;
+      ctx->d2_valid = false;
+      ctx->max_pairs = flags[0];
+      ctx->nb_rcut = rcut;
+      ctx->nb_valid = true;
+      ctx->feats_valid = false;
+      ctx->mom_valid = false;
+      return FNETG_OK;
+    }
+    FNETG_CUDA(cudaMemsetAsync(ctx->d_maxp.p, 0, sizeof(int) * 4, ctx->stream));
+    a.slab_cap = 0;
+  }
   if (N > 0) {
     LaunchScope ls(ctx, "neighbors");
     if (ctx->prec == FNETG_FP64)
@@ -519,7 +589,6 @@ int run_neighbors(fnetg_ctx *ctx, double rcut) {
                              ctx->stream));
   FNETG_CUDA(cudaStreamSynchronize(ctx->stream));
   if (N == 0) P = 0;
-  const size_t es = ctx->prec == FNETG_FP64 ? 8 : 4;
   FNETG_CUDA(ctx->d_pj.ensure(sizeof(int32_t) * std::max<int64_t>(P, 1)));
   FNETG_CUDA(ctx->d_pmeta.ensure(sizeof(uint32_t) * std::max<int64_t>(P, 1)));
   FNETG_CUDA(ctx->d_rij.ensure(4 * es * std::max<int64_t>(P, 1)));
@@ -537,6 +606,11 @@ int run_neighbors(fnetg_ctx *ctx, double rcut) {
     FNETG_CUDA(cudaGetLastError());
   }
   ctx->P = P;
+  ctx->pslots = P;
+  ctx->pslab = false;
+  // capacity for the next build of this dataset: an eighth above the largest count
+  ctx->nb_cap_hint = N > 0 ? ((int64_t)maxp + maxp / 8 + 8 + 7) / 8 * 8 : 0;
+  ctx->nb_hint_n = N;
   ctx->d2_valid = false;
   ctx->max_pairs = maxp;
   ctx->nb_rcut = rcut;
@@ -546,13 +620,18 @@ int run_neighbors(fnetg_ctx *ctx, double rcut) {
   return FNETG_OK;
 }
 
+const int64_t *pair_end(fnetg_ctx *ctx) {
+  return ctx->pslab ? ctx->d_pend.as<int64_t>() : ctx->d_poff.as<int64_t>() + 1;
+}
+
 int pair_d2(fnetg_ctx *ctx) {
   if (ctx->d2_valid) return FNETG_OK;
-  FNETG_CUDA(ctx->d_d2.ensure(sizeof(double) * std::max<int64_t>(ctx->P, 1)));
+  FNETG_CUDA(ctx->d_d2.ensure(sizeof(double) * std::max<int64_t>(ctx->pslots, 1)));
   if (ctx->N > 0 && ctx->P > 0) {
     LaunchScope ls(ctx, "neighbors");
     pair_d2_kernel<<<ceil_div(ctx->N, 8), 256, 0, ctx->stream>>>(
-        ctx->d_poff.as<int64_t>(), ctx->d_pj.as<int32_t>(), ctx->d_pmeta.as<uint32_t>(),
+        ctx->d_poff.as<int64_t>(), pair_end(ctx), ctx->d_pj.as<int32_t>(),
+        ctx->d_pmeta.as<uint32_t>(),
         ctx->d_atom_struct.as<int32_t>(), ctx->d_coords.as<double>(), ctx->d_lat.as<double>(),
         ctx->N, ctx->d_d2.as<double>());
     FNETG_CUDA(cudaGetLastError());

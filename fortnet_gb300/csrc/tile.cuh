@@ -142,7 +142,8 @@ template <typename T> __device__ __forceinline__ T int_pow(T base, int n, T e) {
 // Everything the per-atom kernels read (one struct for both kernels).
 template <typename T> struct TileArgs {
   int64_t natoms;
-  const int64_t *poff;
+  const int64_t *poff;     // pairs of atom i: [poff[i], pend[i])
+  const int64_t *pend;
   const int32_t *pj;
   const uint32_t *pmeta;
   const V4<T> *rij;

@@ -101,6 +101,40 @@ def test_neighbor_pairs_bit_exact_synthetic_c2():
     assert check_neighbors(ds, rc) > 100000
 
 
+@pytest.mark.parametrize("precision", [api.FP32, api.FP64])
+def test_neighbor_rebuilds_slab_and_overflow(precision):
+    """A rebuild of the same dataset finds, counts and stores pairs in one slab pass; a denser
+    geometry overflows the per-atom capacity and falls back to the counted build.  Pair sets
+    stay bit-exact and the features of a slab build equal those of the counted build."""
+    import dataclasses
+
+    cfg = synthetic.CONFIGS["C2"]
+    ds = synthetic.generate(cfg, nstruct=12, targets=False)
+    rc = cfg.rcut / 0.529177249
+    ref = O.neighbours(ds, rc)
+    with api.Context(precision) as ctx:
+        ctx.upload(ds)
+        ctx.set_species(ds.species)
+        ctx.set_gfunctions(synthetic.gfunctions(cfg))
+        ctx.neighbors(rc)
+        first = ctx.acsf()
+        for _ in range(2):
+            ctx.neighbors(rc)
+            got = ctx.get_neighbors()
+            for k in range(4):
+                np.testing.assert_array_equal(got[k], ref[k])
+        np.testing.assert_array_equal(ctx.acsf(), first)
+        # half the cell: every atom gains neighbours, beyond the slab capacity
+        dense = dataclasses.replace(ds, coords=ds.coords * 0.5)
+        ref2 = O.neighbours(dense, rc)
+        assert np.diff(ref2[0]).max() > np.diff(ref[0]).max() * 1.2
+        ctx.update_coords(dense.coords)
+        ctx.neighbors(rc)
+        got = ctx.get_neighbors()
+        for k in range(4):
+            np.testing.assert_array_equal(got[k], ref2[k])
+
+
 def acsf_on_gpu(ds, funcs, precision):
     with api.Context(precision) as ctx:
         ctx.upload(ds)
