@@ -112,10 +112,73 @@ __device__ __forceinline__ float disp_df(float ah, float al, float bh, float bl,
   return __fadd_rn(t, __fadd_rn(__fadd_rn(e1, e2), __fsub_rn(__fadd_rn(al, bl), cl)));
 }
 
+constexpr int kNbWarps = 8;  // warps per CTA of the neighbour kernel
+
+// Store accepted pair (centre i, structure-local neighbour jl, image img or im0 - 1 for the
+// central cell) as the rank-th pair of atom i, at wpos + rank (within the slab capacity).
+template <typename T>
+__device__ __forceinline__ void store_pair(const NbArgs &a, const double *ci, const V4<float> &cif,
+                                           const V4<float> &cil, int64_t i, int64_t a0, int jl,
+                                           int img_i, int64_t im0, int64_t wpos, int64_t rank) {
+  if (a.slab_cap > 0 && rank >= a.slab_cap) return;
+  const int64_t img = img_i;
+  const int64_t j = a0 + jl;
+  const int64_t q = wpos + rank;
+  V4<float> ch{0.f, 0.f, 0.f, 0.f}, cvl{0.f, 0.f, 0.f, 0.f};
+  uint32_t packed = 0;
+  if (img >= im0) {
+    ch = a.imgf[2 * img];
+    cvl = a.imgf[2 * img + 1];
+    packed = __float_as_uint(ch.w);
+  }
+  const V4<float> cjf = a.cf[j];
+  a.pj[q] = (int32_t)j;
+  uint32_t mask = 0;
+  V4<T> v;
+  if (a.exact_geometry || a.d2out) {
+    double d[3];
+    const double dist2 = exact_pair(a, ci, j, img >= im0 ? img : -1, d);
+    for (int c = 0; c < a.nrcls; c++)
+      if (dist2 <= __dmul_rn(a.rcls[c], a.rcls[c])) mask |= 1u << c;
+    if (a.d2out) a.d2out[q] = dist2;
+    v.x = (T)d[0];
+    v.y = (T)d[1];
+    v.z = (T)d[2];
+    v.w = (T)sqrt(dist2);
+  } else {
+    // the pre-filter's float distance decides the cutoff classes outside their error bands
+    const float e0 = (cjf.x + ch.x) - cif.x, e1 = (cjf.y + ch.y) - cif.y,
+                e2 = (cjf.z + ch.z) - cif.z;
+    const float df = e0 * e0 + e1 * e1 + e2 * e2;
+    // displacement in double-float arithmetic from the split coordinates, rounded once to
+    // float; distance in float
+    const V4<float> cjl = a.cl[j];
+    const float fx = disp_df(cjf.x, cjl.x, ch.x, cvl.x, cif.x, cil.x);
+    const float fy = disp_df(cjf.y, cjl.y, ch.y, cvl.y, cif.y, cil.y);
+    const float fz = disp_df(cjf.z, cjl.z, ch.z, cvl.z, cif.z, cil.z);
+    v.x = (T)fx;
+    v.y = (T)fy;
+    v.z = (T)fz;
+    v.w = (T)sqrtf(fx * fx + fy * fy + fz * fz);
+    for (int c = 0; c < a.nrcls; c++) {
+      if (df <= a.rcls2_lo[c]) {
+        mask |= 1u << c;
+      } else if (df <= a.rcls2_hi[c]) {
+        double d[3];
+        if (exact_pair(a, ci, j, img >= im0 ? img : -1, d) <= __dmul_rn(a.rcls[c], a.rcls[c]))
+          mask |= 1u << c;
+      }
+    }
+  }
+  a.pmeta[q] = (packed & 0xffffffu) | (mask << 24);
+  reinterpret_cast<V4<T> *>(a.rij)[q] = v;
+}
+
 template <typename T, bool kFill>
 __global__ void __launch_bounds__(256) nb_kernel(NbArgs a) {
   __shared__ int blk_max;
   __shared__ unsigned long long blk_sum;
+  __shared__ int2 queue_all[kNbWarps][64];
   if (threadIdx.x == 0) {
     blk_max = 0;
     blk_sum = 0;
@@ -133,17 +196,18 @@ __global__ void __launch_bounds__(256) nb_kernel(NbArgs a) {
     const V4<float> cil = a.cl[i];
     int64_t wpos = 0;
     if (kFill) wpos = a.slab_cap > 0 ? i * a.slab_cap : a.poff[i];
+    int2 *queue = queue_all[threadIdx.x >> 5];
+    int qn = 0;           // queued accepted candidates (uniform across the warp)
+    int64_t stored = 0;   // accepted candidates already stored
     int64_t cnt = 0;
     const float *bb = a.bbox + 6 * s;
     const int64_t im0 = a.img_off[s], im1 = a.img_off[s + 1];
     // image -1 is the central cell, then the lattice points of the table (n1 outer .. n3 inner)
     for (int64_t img = im0 - 1; img < im1; img++) {
-      V4<float> ch{0.f, 0.f, 0.f, 0.f}, cvl{0.f, 0.f, 0.f, 0.f};
-      uint32_t packed = 0;
+      V4<float> ch{0.f, 0.f, 0.f, 0.f};
       int tstart = 1, tcount = n - 1;
       if (img >= im0) {
         ch = a.imgf[2 * img];
-        packed = __float_as_uint(ch.w);
         tstart = 0;
         tcount = n;
         // skip the image when the shifted bounding box is out of reach
@@ -156,7 +220,6 @@ __global__ void __launch_bounds__(256) nb_kernel(NbArgs a) {
           dd += e * e;
         }
         if (dd > a.rc2_hi) continue;
-        if (kFill && !a.exact_geometry) cvl = a.imgf[2 * img + 1];
       }
       for (int base = 0; base < tcount; base += 32) {
         bool ok = false;
@@ -179,50 +242,27 @@ __global__ void __launch_bounds__(256) nb_kernel(NbArgs a) {
           }
         }
         const unsigned m = __ballot_sync(0xffffffffu, ok);
-        const int64_t rank = cnt + __popc(m & ((1u << lane) - 1u));
-        if (kFill && ok && (a.slab_cap == 0 || rank < a.slab_cap)) {
-          const int64_t j = a0 + jl;
-          const int64_t q = wpos + rank;
-          a.pj[q] = (int32_t)j;
-          uint32_t mask = 0;
-          V4<T> v;
-          if (a.exact_geometry || a.d2out) {
-            double d[3];
-            const double dist2 = exact_pair(a, ci, j, img >= im0 ? img : -1, d);
-            for (int c = 0; c < a.nrcls; c++)
-              if (dist2 <= __dmul_rn(a.rcls[c], a.rcls[c])) mask |= 1u << c;
-            if (a.d2out) a.d2out[q] = dist2;
-            v.x = (T)d[0];
-            v.y = (T)d[1];
-            v.z = (T)d[2];
-            v.w = (T)sqrt(dist2);
-          } else {
-            // displacement in double-float arithmetic from the split coordinates, rounded
-            // once to float; distance in float
-            const V4<float> cjl = a.cl[j];
-            const float fx = disp_df(cjf.x, cjl.x, ch.x, cvl.x, cif.x, cil.x);
-            const float fy = disp_df(cjf.y, cjl.y, ch.y, cvl.y, cif.y, cil.y);
-            const float fz = disp_df(cjf.z, cjl.z, ch.z, cvl.z, cif.z, cil.z);
-            v.x = (T)fx;
-            v.y = (T)fy;
-            v.z = (T)fz;
-            v.w = (T)sqrtf(fx * fx + fy * fy + fz * fz);
-            for (int c = 0; c < a.nrcls; c++) {
-              if (df <= a.rcls2_lo[c]) {
-                mask |= 1u << c;
-              } else if (df <= a.rcls2_hi[c]) {
-                double d[3];
-                if (exact_pair(a, ci, j, img >= im0 ? img : -1, d) <=
-                    __dmul_rn(a.rcls[c], a.rcls[c]))
-                  mask |= 1u << c;
-              }
-            }
+        if (kFill) {
+          // queue the accepted candidates in iterator order; store them 32 at a time
+          if (ok) queue[qn + __popc(m & ((1u << lane) - 1u))] = make_int2(jl, (int)img);
+          qn += __popc(m);
+          __syncwarp();
+          if (qn >= 32) {
+            const int2 e = queue[lane];
+            store_pair<T>(a, ci, cif, cil, i, a0, e.x, e.y, im0, wpos, stored + lane);
+            __syncwarp();
+            if (lane < qn - 32) queue[lane] = queue[lane + 32];
+            __syncwarp();
+            qn -= 32;
+            stored += 32;
           }
-          a.pmeta[q] = (packed & 0xffffffu) | (mask << 24);
-          reinterpret_cast<V4<T> *>(a.rij)[q] = v;
         }
         cnt += __popc(m);
       }
+    }
+    if (kFill && lane < qn) {
+      const int2 e = queue[lane];
+      store_pair<T>(a, ci, cif, cil, i, a0, e.x, e.y, im0, wpos, stored + lane);
     }
     if ((!kFill || a.slab_cap > 0) && lane == 0) {
       a.count[i] = cnt;
@@ -520,7 +560,7 @@ int run_neighbors(fnetg_ctx *ctx, double rcut) {
   a.exact_geometry = ctx->prec == FNETG_FP64 ? 1 : 0;
   a.count = ctx->d_pcount.as<int64_t>();
   a.maxp = ctx->d_maxp.as<int>();
-  const int threads = 256, wpb = threads / 32;
+  const int threads = kNbWarps * 32, wpb = kNbWarps;
   const int blocks = std::max(1, ceil_div(N, wpb));
   const size_t es = ctx->prec == FNETG_FP64 ? 8 : 4;
   // Slab pass: with a per-atom capacity from the previous build of this dataset, one pass
