@@ -19,7 +19,7 @@ FP32, FP64 = 32, 64
 ACT = {"tanh": 0, "sigmoid": 1, "relu": 2, "lrelu": 3, "softplus": 4, "bent": 5, "atan": 6,
        "gaussian": 7, "heaviside": 8, "linear": 9}
 LOSS = {"mse": 0, "rms": 1, "mae": 2, "mape": 3}
-OPT = {"sd": 0, "lbfgs": 1}
+OPT = {"sd": 0, "lbfgs": 1, "cg": 2, "fire": 3}
 ERRORS = {-1: "invalid argument", -2: "shape mismatch", -3: "out of device memory",
           -4: "CUDA error", -5: "timeout", -6: "invalid geometry", -7: "unsupported"}
 

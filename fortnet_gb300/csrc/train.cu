@@ -245,6 +245,7 @@ struct LbParams {
   double tol, maxdisp;
   int linesearch;
   double qn_maxdisp;
+  double lm_tol;  // line-minimiser tolerance (L-BFGS: tol; CG: 1e4, conjgrad.F90:120)
 };
 
 __device__ double bdot(const double *a, const double *b, int64_t n, double *sh) {
@@ -373,7 +374,7 @@ __device__ bool lm_next(LbView &v, const LbParams &P, double fu, const double *d
     s_ret = 0;
     s_flip = 0;
     const int iiter = (int)sc[SC_IITER];
-    if ((fabs(dcur) < P.tol && (int)sc[SC_STATE] == 3) || iiter > 10) {
+    if ((fabs(dcur) < P.lm_tol && (int)sc[SC_STATE] == 3) || iiter > 10) {
       s_ret = 1;
     } else {
       int state = (int)sc[SC_STATE];
@@ -529,6 +530,142 @@ __global__ void lbfgs_kernel(double *state, size_t stride, double *params, const
   bcopy(xnew, v.xx, n);
 }
 
+// ---------------------------------------------------------------- conjugate gradients
+// conjGrad_next / next_local (conjgrad.F90:142-260).  State per species in the L-BFGS layout
+// with mem = 1: xx = uu, gg = gg, dir = hh, qq = scratch; SC_ITER = 0 before the first call
+// (st_1), 1 after; SC_CONVERGED sticky.
+__global__ void cg_kernel(double *state, size_t stride, double *params, const double *grad,
+                          LbParams P, int *conv_flags) {
+  __shared__ double sh[kOptThreads];
+  const int s = blockIdx.x;
+  LbView v = lb_view(state + (size_t)s * stride, P.n, 1);
+  const double *du = grad + (size_t)s * P.n;
+  double *xnew = params + (size_t)s * P.n;
+  const int64_t n = P.n;
+  const double fu = 0.0;  // stored by the line minimiser only
+  if (v.sc[SC_CONVERGED] == 0.0) {
+    if (v.sc[SC_ITER] == 0.0) {
+      const double gmax = bmaxabs(du, n, sh);
+      if (gmax < P.tol) {
+        for (int64_t q = threadIdx.x; q < n; q += blockDim.x) {
+          v.gg[q] = du[q];
+          v.dir[q] = q == 0 ? fu : 0.0;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) v.sc[SC_CONVERGED] = 1;
+      } else {
+        for (int64_t q = threadIdx.x; q < n; q += blockDim.x) {
+          v.gg[q] = -du[q];
+          v.dir[q] = v.gg[q];
+        }
+        __syncthreads();
+      }
+      const double first = 5.0 * sqrt(bdot(v.gg, v.gg, n, sh));
+      if (v.sc[SC_CONVERGED] == 0.0) lm_reset(v, P, v.xx, v.dir, first, sh);
+      if (threadIdx.x == 0) v.sc[SC_ITER] = 1;
+      __syncthreads();
+    }
+    bool conv_line = true;
+    while (v.sc[SC_CONVERGED] == 0.0 && conv_line) {
+      conv_line = lm_next(v, P, fu, du, v.xx, sh);
+      if (conv_line) {
+        const double *xi = v.d0;  // the line minimum's gradient
+        const double xmax = bmaxabs(xi, n, sh);
+        if (xmax < P.tol) {
+          if (threadIdx.x == 0) v.sc[SC_CONVERGED] = 1;
+          __syncthreads();
+        } else {
+          const double gg_abs = bdot(v.gg, v.gg, n, sh);
+          double acc = 0.0;
+          for (int64_t q = threadIdx.x; q < n; q += blockDim.x) acc += (xi[q] + v.gg[q]) * xi[q];
+          const double dg_abs = block_sum<kOptThreads>(acc, sh);
+          if (gg_abs < kEps) {
+            if (threadIdx.x == 0) v.sc[SC_CONVERGED] = 1;
+            __syncthreads();
+          } else {
+            for (int64_t q = threadIdx.x; q < n; q += blockDim.x) {
+              v.gg[q] = -xi[q];
+              v.dir[q] = v.gg[q] + (dg_abs / gg_abs) * v.dir[q];
+            }
+            __syncthreads();
+            bcopy(v.xx, v.x0, n);
+            lm_reset(v, P, v.xx, v.dir, v.sc[SC_XX1], sh);
+          }
+        }
+      }
+    }
+    if (v.sc[SC_CONVERGED] != 0.0) bcopy(v.xx, v.x0, n);
+  }
+  if (threadIdx.x == 0) conv_flags[s] = v.sc[SC_CONVERGED] != 0.0 ? 1 : 0;
+  bcopy(xnew, v.xx, n);
+}
+
+// ---------------------------------------------------------------- FIRE
+// TFire next / fireModifyVelocity (fire.F90:128-190).  State per species: xx = x, dir =
+// velocity; scalars SC_ITER = iter, SC_STATE = resetStep, SC_XX0 = a, SC_XX1 = dt.
+struct FireParams {
+  int64_t n;
+  double tol, dt_max;
+};
+
+__global__ void fire_kernel(double *state, size_t stride, double *params, const double *grad,
+                            FireParams P, int *conv_flags) {
+  __shared__ double sh[kOptThreads];
+  const int s = blockIdx.x;
+  LbView v = lb_view(state + (size_t)s * stride, P.n, 1);
+  const double *dx = grad + (size_t)s * P.n;
+  double *xnew = params + (size_t)s * P.n;
+  const int64_t n = P.n;
+  const double gmax = bmaxabs(dx, n, sh);
+  const int iter = (int)v.sc[SC_ITER];
+  if (gmax < P.tol) {
+    if (threadIdx.x == 0) conv_flags[s] = 1;
+  } else {
+    const double p = -1.0 * bdot(v.dir, dx, n, sh);
+    const double mv = sqrt(bdot(v.dir, v.dir, n, sh));
+    const double md = sqrt(bdot(dx, dx, n, sh));
+    double a = v.sc[SC_XX0], dt = v.sc[SC_XX1];
+    const int reset_step = (int)v.sc[SC_STATE];
+    for (int64_t q = threadIdx.x; q < n; q += blockDim.x)
+      v.dir[q] = (1.0 - a) * v.dir[q] - a * dx[q] * mv / md;
+    __syncthreads();
+    int new_reset = reset_step;
+    if (p < 0.0) {
+      for (int64_t q = threadIdx.x; q < n; q += blockDim.x) v.dir[q] = 0.0;
+      new_reset = iter;
+      dt = dt * 0.5;
+      a = 0.1;
+    } else if (iter - reset_step > 5) {
+      dt = fmin(dt * 1.1, P.dt_max);
+      a = a * 0.99;
+    }
+    __syncthreads();
+    for (int64_t q = threadIdx.x; q < n; q += blockDim.x) {
+      v.dir[q] = v.dir[q] - dt * dx[q];
+      v.xx[q] = v.xx[q] + v.dir[q] * dt;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      v.sc[SC_STATE] = new_reset;
+      v.sc[SC_XX0] = a;
+      v.sc[SC_XX1] = dt;
+      conv_flags[s] = 0;
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) v.sc[SC_ITER] = iter + 1;
+  bcopy(xnew, v.xx, n);
+}
+
+// FIRE reset (fire.F90:113-126) on top of the zeroed block: a = a_start = 0.1,
+// dt = dt_init = 0.1 dt_max (x = x0 and v = 0 come from lbfgs_reset_kernel)
+__global__ void fire_reset_kernel(double *state, size_t stride, int64_t n, double dt_max) {
+  if (threadIdx.x != 0) return;
+  LbView v = lb_view(state + (size_t)blockIdx.x * stride, n, 1);
+  v.sc[SC_XX0] = 0.1;
+  v.sc[SC_XX1] = 0.1 * dt_max;
+}
+
 __global__ void lbfgs_reset_kernel(double *state, size_t stride, const double *params,
                                    int64_t n, int mem) {
   const int s = blockIdx.x;
@@ -613,9 +750,21 @@ int run_optimizer_step(fnetg_ctx *ctx) {
     sd_kernel<<<ctx->nsp, kOptThreads, 0, ctx->stream>>>(ctx->d_params64.as<double>(),
                                                           ctx->d_grad64.as<double>(),
                                                           ctx->nparams, st, conv);
+  } else if (ctx->opt_kind == FNETG_OPT_CG) {
+    LbParams P{ctx->nparams, 1, ctx->opt_threshold, ctx->opt_max_disp, 1, -1.0, 10000.0};
+    LaunchScope ls(ctx, "optimizer");
+    cg_kernel<<<ctx->nsp, kOptThreads, 0, ctx->stream>>>(
+        ctx->d_opt.as<double>(), ctx->opt_stride, ctx->d_params64.as<double>(),
+        ctx->d_grad64.as<double>(), P, conv);
+  } else if (ctx->opt_kind == FNETG_OPT_FIRE) {
+    FireParams P{ctx->nparams, ctx->opt_threshold, ctx->opt_max_disp};
+    LaunchScope ls(ctx, "optimizer");
+    fire_kernel<<<ctx->nsp, kOptThreads, 0, ctx->stream>>>(
+        ctx->d_opt.as<double>(), ctx->opt_stride, ctx->d_params64.as<double>(),
+        ctx->d_grad64.as<double>(), P, conv);
   } else {
     LbParams P{ctx->nparams, ctx->opt_mem, ctx->opt_threshold, ctx->opt_max_disp,
-               ctx->opt_linemin, ctx->opt_qn ? ctx->opt_max_disp : -1.0};
+               ctx->opt_linemin, ctx->opt_qn ? ctx->opt_max_disp : -1.0, ctx->opt_threshold};
     LaunchScope ls(ctx, "optimizer");
     lbfgs_kernel<<<ctx->nsp, kOptThreads, 0, ctx->stream>>>(
         ctx->d_opt.as<double>(), ctx->opt_stride, ctx->d_params64.as<double>(),
@@ -636,7 +785,9 @@ int fnetg_optimizer_init(fnetg_ctx *ctx, int32_t kind, double threshold, double 
                          int32_t qn_max_disp) {
   if (!ctx) return FNETG_E_INVALID;
   FNETG_CHECK(ctx->net_set, FNETG_E_INVALID, "optimizer_init: no network");
-  FNETG_CHECK(kind == FNETG_OPT_SD || kind == FNETG_OPT_LBFGS, FNETG_E_INVALID, "optimiser kind");
+  FNETG_CHECK(kind == FNETG_OPT_SD || kind == FNETG_OPT_LBFGS || kind == FNETG_OPT_CG ||
+                  kind == FNETG_OPT_FIRE,
+              FNETG_E_INVALID, "optimiser kind");
   FNETG_CHECK(threshold > 0.0 && max_disp > 0.0, FNETG_E_INVALID,
               "threshold and maximal displacement must be > 0");
   ctx->opt_kind = kind;
@@ -649,13 +800,18 @@ int fnetg_optimizer_init(fnetg_ctx *ctx, int32_t kind, double threshold, double 
   ctx->opt_qn = qn_max_disp ? 1 : 0;
   FNETG_CUDA(ctx->d_conv.ensure(sizeof(int) * 64 + sizeof(double) * 64));
   FNETG_CUDA(cudaMemsetAsync(ctx->d_conv.p, 0, sizeof(int) * 64, ctx->stream));
-  if (kind == FNETG_OPT_LBFGS) {
-    ctx->opt_stride = lb_stride(ctx->nparams, ctx->opt_mem);
+  if (kind != FNETG_OPT_SD) {
+    // L-BFGS, CG and FIRE keep their state in the L-BFGS block layout (mem = 1 for CG/FIRE)
+    const int mem = kind == FNETG_OPT_LBFGS ? ctx->opt_mem : 1;
+    ctx->opt_stride = lb_stride(ctx->nparams, mem);
     FNETG_CUDA(ctx->d_opt.ensure(sizeof(double) * ctx->opt_stride * ctx->nsp));
     LaunchScope ls(ctx, "optimizer");
     lbfgs_reset_kernel<<<ctx->nsp, kOptThreads, 0, ctx->stream>>>(
         ctx->d_opt.as<double>(), ctx->opt_stride, ctx->d_params64.as<double>(), ctx->nparams,
-        ctx->opt_mem);
+        mem);
+    if (kind == FNETG_OPT_FIRE)
+      fire_reset_kernel<<<ctx->nsp, 32, 0, ctx->stream>>>(ctx->d_opt.as<double>(),
+                                                          ctx->opt_stride, ctx->nparams, max_disp);
     FNETG_CUDA(cudaGetLastError());
   }
   FNETG_CUDA(cudaStreamSynchronize(ctx->stream));

@@ -67,6 +67,8 @@ extern "C" {
 /* optimisers (lib_optimizers/optimizers.F90) */
 #define FNETG_OPT_SD 0
 #define FNETG_OPT_LBFGS 1
+#define FNETG_OPT_CG 2     /* conjgrad.F90 with linemin.F90 */
+#define FNETG_OPT_FIRE 3   /* fire.F90 */
 
 typedef struct fnetg_ctx fnetg_ctx;
 

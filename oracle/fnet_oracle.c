@@ -1476,6 +1476,137 @@ int orc_lbfgs_next(void *h, double fx, const double *dx, double *xnew) {
   return 0;
 }
 
+/* ---- conjugate gradients (conjgrad.F90:121-260): Polak-Ribiere directions with the line
+ * minimiser of linemin.F90 (10 evaluations per line, tolerance 1e4) ---------------------- */
+void *orc_cg_new(int32_t n, double tol, double maxdisp, const double *x0) {
+  opt_t *o = (opt_t *)calloc(1, sizeof(opt_t));
+  o->kind = 2;
+  o->n = n;
+  o->tol = tol;
+  o->gg = (double *)calloc(n, sizeof(double));  /* gg */
+  o->dir = (double *)calloc(n, sizeof(double)); /* hh */
+  o->xx = (double *)calloc(n, sizeof(double));  /* uu */
+  o->lm_x0 = (double *)calloc(n, sizeof(double));
+  o->lm_d0 = (double *)calloc(n, sizeof(double));
+  o->lm_miter = 10;
+  o->lm_tol = 10000.0;
+  o->lm_maxdisp = maxdisp;
+  memcpy(o->xx, x0, sizeof(double) * n); /* conjGrad_reset */
+  o->iter = 0;                           /* state st_1 */
+  o->converged = 0;
+  return o;
+}
+
+/* conjGrad_next / next_local (conjgrad.F90:142-260) */
+int orc_cg_next(void *h, double fu, const double *du, double *xnew) {
+  opt_t *o = (opt_t *)h;
+  const int n = o->n;
+  double *gg = o->gg, *hh = o->dir, *uu = o->xx;
+  if (!o->converged) {
+    if (o->iter == 0) {
+      double gmax = 0.0;
+      for (int i = 0; i < n; i++) gmax = fabs(du[i]) > gmax ? fabs(du[i]) : gmax;
+      if (gmax < o->tol) {
+        o->converged = 1;
+        memcpy(gg, du, sizeof(double) * n);
+        for (int i = 0; i < n; i++) hh[i] = 0.0;
+        hh[0] = fu;
+      } else {
+        for (int i = 0; i < n; i++) {
+          gg[i] = -du[i];
+          hh[i] = gg[i];
+        }
+      }
+      lm_reset(o, uu, hh, 5.0 * sqrt(dotn(gg, gg, n)));
+      o->iter = 1; /* state st_2 */
+    }
+    int conv_line = 1;
+    while (!o->converged && conv_line) {
+      conv_line = lm_next(o, fu, du, uu);
+      if (conv_line) {
+        const double *xi = o->lm_d0; /* getMinGrad */
+        double gmax = 0.0;
+        for (int i = 0; i < n; i++) gmax = fabs(xi[i]) > gmax ? fabs(xi[i]) : gmax;
+        if (gmax < o->tol) {
+          o->converged = 1;
+        } else {
+          const double gg_abs = dotn(gg, gg, n);
+          double dg_abs = 0.0;
+          for (int i = 0; i < n; i++) dg_abs = dg_abs + (xi[i] + gg[i]) * xi[i];
+          if (gg_abs < DP_EPS) {
+            o->converged = 1;
+          } else {
+            for (int i = 0; i < n; i++) {
+              gg[i] = -xi[i];
+              hh[i] = gg[i] + (dg_abs / gg_abs) * hh[i];
+            }
+            memcpy(uu, o->lm_x0, sizeof(double) * n); /* getMinX */
+            lm_reset(o, uu, hh, o->lm_xx[1]);          /* getMinLambda */
+          }
+        }
+      }
+    }
+    if (o->converged) memcpy(uu, o->lm_x0, sizeof(double) * n);
+  }
+  memcpy(xnew, uu, sizeof(double) * n);
+  return o->converged;
+}
+
+/* ---- FIRE (fire.F90:90-205) ---------------------------------------------------------- */
+void *orc_fire_new(int32_t n, double tol, double maxstep, const double *x0) {
+  opt_t *o = (opt_t *)calloc(1, sizeof(opt_t));
+  o->kind = 3;
+  o->n = n;
+  o->tol = tol;
+  o->xx = (double *)calloc(n, sizeof(double));   /* x */
+  o->dir = (double *)calloc(n, sizeof(double));  /* velocity */
+  o->maxdisp = maxstep;                          /* dt_max */
+  memcpy(o->xx, x0, sizeof(double) * n);         /* reset */
+  o->iter = 0;
+  o->mem = 0;                                    /* resetStep */
+  o->alpha = 0.1;                                /* a = a_start */
+  o->lr = 0.1 * maxstep;                         /* dt = dt_init */
+  return o;
+}
+
+static double magn(const double *v, int n) {
+  double s = 0.0;
+  for (int i = 0; i < n; i++) s = s + v[i] * v[i];
+  return sqrt(s);
+}
+
+int orc_fire_next(void *h, const double *dx, double *xnew) {
+  opt_t *o = (opt_t *)h;
+  const int n = o->n;
+  double *x = o->xx, *v = o->dir;
+  int conv;
+  double gmax = 0.0;
+  for (int i = 0; i < n; i++) gmax = fabs(dx[i]) > gmax ? fabs(dx[i]) : gmax;
+  if (gmax < o->tol) {
+    conv = 1;
+  } else {
+    /* fireModifyVelocity */
+    const double p = -1.0 * dotn(v, dx, n);
+    const double mv = magn(v, n), md = magn(dx, n);
+    for (int i = 0; i < n; i++) v[i] = (1.0 - o->alpha) * v[i] - o->alpha * dx[i] * mv / md;
+    if (p < 0.0) {
+      for (int i = 0; i < n; i++) v[i] = 0.0;
+      o->mem = o->iter;
+      o->lr = o->lr * 0.5;
+      o->alpha = 0.1;
+    } else if (o->iter - o->mem > 5) {
+      o->lr = o->lr * 1.1 < o->maxdisp ? o->lr * 1.1 : o->maxdisp;
+      o->alpha = o->alpha * 0.99;
+    }
+    for (int i = 0; i < n; i++) v[i] = v[i] - o->lr * dx[i];
+    for (int i = 0; i < n; i++) x[i] = x[i] + v[i] * o->lr;
+    conv = 0;
+  }
+  memcpy(xnew, x, sizeof(double) * n);
+  o->iter = o->iter + 1;
+  return conv;
+}
+
 void orc_opt_free(void *h) {
   opt_t *o = (opt_t *)h;
   if (!o) return;

@@ -136,6 +136,10 @@ int orc_sd_next(void *h, const double *grad, double *xnew);
 void *orc_lbfgs_new(int32_t n, double tol, double mindisp, double maxdisp, int32_t mem,
                     int32_t linesearch, int32_t qndisp, const double *x0);
 int orc_lbfgs_next(void *h, double fx, const double *grad, double *xnew);
+void *orc_cg_new(int32_t n, double tol, double maxdisp, const double *x0);
+int orc_cg_next(void *h, double fx, const double *grad, double *xnew);
+void *orc_fire_new(int32_t n, double tol, double maxstep, const double *x0);
+int orc_fire_next(void *h, const double *grad, double *xnew);
 void orc_opt_free(void *h);
 
 #ifdef __cplusplus

@@ -80,6 +80,12 @@ def lib():
         L.orc_lbfgs_new.restype = vp
         L.orc_lbfgs_new.argtypes = [i32, dbl, dbl, dbl, i32, i32, i32, vp]
         L.orc_lbfgs_next.argtypes = [vp, dbl, vp, vp]
+        L.orc_cg_new.restype = vp
+        L.orc_cg_new.argtypes = [i32, dbl, dbl, vp]
+        L.orc_cg_next.argtypes = [vp, dbl, vp, vp]
+        L.orc_fire_new.restype = vp
+        L.orc_fire_new.argtypes = [i32, dbl, dbl, vp]
+        L.orc_fire_next.argtypes = [vp, vp, vp]
         L.orc_opt_free.argtypes = [vp]
         _lib = L
     return _lib
@@ -349,6 +355,43 @@ class SteepestDescent:
         if getattr(self, "h", None) and _lib is not None:
             _lib.orc_opt_free(self.h)
             self.h = None
+
+
+class _Opt:
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.orc_opt_free(self.h)
+            self.h = None
+
+
+class ConjGrad(_Opt):
+    """conjgrad.F90 with its line minimiser (threshold, MaxDisplacement)."""
+
+    def __init__(self, x0, tol, maxdisp):
+        x0 = np.ascontiguousarray(x0, dtype=np.float64)
+        self.n = len(x0)
+        self.h = lib().orc_cg_new(self.n, tol, maxdisp, _p(x0))
+
+    def next(self, fx, grad):
+        g = np.ascontiguousarray(grad, dtype=np.float64)
+        x = np.zeros(self.n)
+        conv = lib().orc_cg_next(self.h, float(fx), _p(g), _p(x))
+        return x, bool(conv)
+
+
+class Fire(_Opt):
+    """fire.F90 (threshold, MaxDisplacement as the largest time step)."""
+
+    def __init__(self, x0, tol, maxstep):
+        x0 = np.ascontiguousarray(x0, dtype=np.float64)
+        self.n = len(x0)
+        self.h = lib().orc_fire_new(self.n, tol, maxstep, _p(x0))
+
+    def next(self, fx, grad):
+        g = np.ascontiguousarray(grad, dtype=np.float64)
+        x = np.zeros(self.n)
+        conv = lib().orc_fire_next(self.h, _p(g), _p(x))
+        return x, bool(conv)
 
 
 class Lbfgs:

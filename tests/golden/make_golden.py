@@ -173,7 +173,8 @@ def extract_case(ref_root, case, outdir):
         ext_spec = _get(ext[1], "Indices")
     if mode == "train":
         tname = training[0].lower() if training else "sd"
-        if tname not in ("sd", "lbfgs"):
+        tname = {"conjgrads": "cg", "conjgrad": "cg"}.get(tname, tname)
+        if tname not in ("sd", "lbfgs", "cg", "fire"):
             return None, f"optimizer {tname}"
         tb = training[1]
         settings.update({

@@ -116,6 +116,10 @@ def run_training(case, backend):
     if st["optimizer"] == "sd":
         opts = [backend.sd(params[s], st["threshold"], st["max_disp"], st["learning_rate"])
                 for s in range(nsp)]
+    elif st["optimizer"] == "cg":
+        opts = [backend.cg(params[s], st["threshold"], st["max_disp"]) for s in range(nsp)]
+    elif st["optimizer"] == "fire":
+        opts = [backend.fire(params[s], st["threshold"], st["max_disp"]) for s in range(nsp)]
     else:
         opts = [backend.lbfgs(params[s], st["threshold"], st["min_disp"], st["max_disp"],
                               st["memory"], st["linemin"], st["qn_max_disp"])

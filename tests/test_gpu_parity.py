@@ -312,7 +312,7 @@ def test_c2_energies_fp32_within_1e5_of_fp64_oracle():
     assert normwise(glob, e_ref) < 1e-5
 
 
-@pytest.mark.parametrize("optimizer", ["sd", "lbfgs"])
+@pytest.mark.parametrize("optimizer", ["sd", "lbfgs", "cg", "fire"])
 def test_training_iterations_match_oracle(optimizer):
     """Several full training iterations (gradient, update, optimiser incl. line search)."""
     cfg = synthetic.CONFIGS["C1"]
@@ -323,9 +323,11 @@ def test_training_iterations_match_oracle(optimizer):
     vals = O.acsf(ds, funcs)
     zprec = O.zscore_stats(vals, ds)
     feats = O.zscore_apply(vals, zprec)
-    niter = 6
-    opt = (O.SteepestDescent(params0[0], 1e-30, 5e-2, 0.01) if optimizer == "sd"
-           else O.Lbfgs(params0[0], 1e-30, 1e-6, 1.0, 20, True, False))
+    niter = 6 if optimizer != "cg" else 14  # CG: several line searches
+    opt = {"sd": lambda: O.SteepestDescent(params0[0], 1e-30, 5e-2, 0.01),
+           "lbfgs": lambda: O.Lbfgs(params0[0], 1e-30, 1e-6, 1.0, 20, True, False),
+           "cg": lambda: O.ConjGrad(params0[0], 1e-30, 1.0),
+           "fire": lambda: O.Fire(params0[0], 1e-30, 0.05)}[optimizer]()
     params = params0.copy()
     dd, _ = O.train_gradients(dims, "tanh", params, feats, ds)
     ref_hist = []
@@ -344,8 +346,12 @@ def test_training_iterations_match_oracle(optimizer):
         ctx.set_targets(ds)
         if optimizer == "sd":
             ctx.optimizer_init("sd", 1e-30, 1e-6, 5e-2, 0.01)
-        else:
+        elif optimizer == "lbfgs":
             ctx.optimizer_init("lbfgs", 1e-30, 1e-6, 1.0, memory=20, linemin=True)
+        elif optimizer == "cg":
+            ctx.optimizer_init("cg", 1e-30, 1e-6, 1.0)
+        else:
+            ctx.optimizer_init("fire", 1e-30, 1e-6, 0.05)
         for it in range(niter):
             ctx.train_iteration("mse")
             np.testing.assert_allclose(ctx.params(), ref_hist[it], rtol=1e-8, atol=1e-10)

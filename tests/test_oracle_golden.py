@@ -23,6 +23,8 @@ class OracleBackend:
     ranlux = staticmethod(lambda seed: O.Ranlux(seed))
     sd = staticmethod(lambda x0, tol, md, lr: O.SteepestDescent(x0, tol, md, lr))
     lbfgs = staticmethod(lambda x0, tol, mi, ma, mem, lm, qn: O.Lbfgs(x0, tol, mi, ma, mem, lm, qn))
+    cg = staticmethod(lambda x0, tol, ma: O.ConjGrad(x0, tol, ma))
+    fire = staticmethod(lambda x0, tol, ma: O.Fire(x0, tol, ma))
 
 
 @pytest.mark.parametrize("name", G.case_names())
