@@ -80,6 +80,7 @@ def load(build_if_missing=True):
         "fnetg_predict": (C.c_int, [vp, vp, vp]),
         "fnetg_jacobian": (C.c_int, [vp, vp]),
         "fnetg_forces": (C.c_int, [vp, vp]),
+        "fnetg_forces_fd": (C.c_int, [vp, C.c_double, vp]),
         "fnetg_set_targets": (C.c_int, [vp, i32, i32, vp, vp, vp, vp]),
         "fnetg_train_gradients": (C.c_int, [vp, i32, vp, vp, vp, vp]),
         "fnetg_update_prepare": (C.c_int, [vp, vp, dbl, dbl, vp]),
@@ -272,6 +273,13 @@ class Context:
         nout = self.dims[-1]
         out = np.zeros((self.ntot, nout, 3))
         self._check(self.lib.fnetg_forces(self.h, _p(out)))
+        return out
+
+    def forces_fd(self, delta):
+        """Central finite-difference forces [Ntot, nOut, 3] with displacement delta (Bohr)."""
+        nout = self.dims[-1]
+        out = np.zeros((self.ntot, nout, 3))
+        self._check(self.lib.fnetg_forces_fd(self.h, float(delta), _p(out)))
         return out
 
     # -- training ----------------------------------------------------------------------

@@ -166,6 +166,11 @@ int fnetg_jacobian(fnetg_ctx *ctx, double *jac);
  * image contributes); it equals the reference's whenever no atom sees two images of the
  * same atom within the cutoff. */
 int fnetg_forces(fnetg_ctx *ctx, double *forces);
+/* forceAnalysis_finiteDiff (lib_analysis/forces.F90:85-117, 182-306): central differences
+ * forces[a*nout*3 + o*3 + c] = (P_o(r_ac - delta) - P_o(r_ac + delta)) / (2 delta) of the
+ * structure's summed outputs, every displaced copy featurised with the z-score of the last
+ * fnetg_acsf_zscore call.  Runs the copies through the device pipeline in batches. */
+int fnetg_forces_fd(fnetg_ctx *ctx, double delta, double *forces);
 
 /* ---------------------------------------------------------------- training */
 /* Targets and weights of TDataset (fnetdata.F90:58-130). gt[S*ngt], at[Ntot*nat],

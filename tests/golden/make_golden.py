@@ -207,9 +207,11 @@ def extract_case(ref_root, case, outdir):
     analysis = _get(hsd, "Analysis/Forces")
     if analysis is not None:
         fm = analysis[0].lower() if isinstance(analysis, tuple) else str(analysis).lower()
-        if fm not in ("analytical",):
+        if fm not in ("analytical", "finitedifferences"):
             return None, f"forces {fm}"
-        settings["forces"] = "analytical"
+        settings["forces"] = fm
+        if fm == "finitedifferences":
+            settings["fd_delta"] = float(_get(analysis[1], "Delta", "1e-02"))
     dspath = str(_get(hsd, "Data/Dataset")).strip("'\"")
     dsfile = os.path.normpath(os.path.join(cdir, dspath))
     dsname = os.path.splitext(os.path.basename(dsfile))[0]

@@ -138,6 +138,45 @@ def run_training(case, backend):
     return zprec, params
 
 
+def fd_forces(backend, ds, inp, sp, delta):
+    """forceAnalysis_finiteDiff (forces.F90:182-306): central differences of each structure's
+    summed outputs under displacements -delta / +delta of one coordinate.  [Ntot, 3*nOut]"""
+    nout = inp["dims"][-1]
+    out = np.zeros((ds.ntot, 3 * nout))
+    for s in range(ds.nstruct):
+        a0, a1 = int(ds.atom_offsets[s]), int(ds.atom_offsets[s + 1])
+        n = a1 - a0
+        copies = []
+        for a in range(a0, a1):
+            for c in range(3):
+                for sign in (-1.0, 1.0):
+                    x = ds.coords[a0:a1].copy()
+                    x[a - a0, c] += sign * delta
+                    copies.append(x)
+        m = len(copies)
+        sub = Dataset(
+            atom_offsets=np.arange(m + 1, dtype=np.int64) * n, coords=np.concatenate(copies),
+            atnum=np.tile(ds.atnum[a0:a1], m), species=np.tile(sp[a0:a1], m),
+            periodic=np.repeat(ds.periodic[s:s + 1], m), latvecs=np.repeat(ds.latvecs[s:s + 1], m, 0),
+            atomic_numbers=ds.atomic_numbers, weights=np.ones(m, np.int32),
+            atomic_weights=np.ones(m * n), global_targets=np.zeros((m, 0)),
+            atomic_targets=np.zeros((m * n, 0)),
+            ext=None if ds.ext is None else np.tile(ds.ext[a0:a1], (m, 1)))
+        vals = backend.acsf(sub, inp["gfuncs"])
+        if inp["zprec"] is not None:
+            vals = backend.zscore_apply(vals, inp["zprec"])
+        feats = assemble_features(vals, sub, inp["ext_indices"])
+        pred = backend.predict(inp["dims"], inp["activation"], inp["params"], feats,
+                               np.tile(sp[a0:a1], m))
+        glob = np.add.reduceat(pred, sub.atom_offsets[:-1], axis=0)
+        k = 0
+        for a in range(a0, a1):
+            for c in range(3):
+                out[a, c::3] = (glob[k] - glob[k + 1]) / (2.0 * delta)
+                k += 2
+    return out
+
+
 def run_prediction(case, backend):
     """predict/validate-mode flow: features from the input netstat, iPredict per atom and
     (if requested) analytical forces.  Returns (raw predictions [Ntot,nOut], forces|None)."""
@@ -150,6 +189,8 @@ def run_prediction(case, backend):
     sp = species_index(ds, inp["atomic_numbers"])
     pred = backend.predict(inp["dims"], inp["activation"], inp["params"], feats, sp)
     forces = None
+    if case.settings.get("forces") == "finitedifferences":
+        forces = fd_forces(backend, ds, inp, sp, case.settings["fd_delta"])
     if case.settings.get("forces") == "analytical":
         jac = backend.jacobian(inp["dims"], inp["activation"], inp["params"], feats, sp)
         ng = len(inp["gfuncs"])

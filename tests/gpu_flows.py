@@ -30,6 +30,8 @@ def prediction(case, precision=api.FP64):
         forces = None
         if case.settings.get("forces") == "analytical":
             forces = ctx.forces()
+        elif case.settings.get("forces") == "finitedifferences":
+            forces = ctx.forces_fd(case.settings["fd_delta"])
         return pred, forces
 
 
