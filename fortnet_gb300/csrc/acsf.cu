@@ -40,7 +40,8 @@ __global__ void __launch_bounds__(256) acsf_kernel(TileArgs<T> a) {
         for (int k = lane; k < nm; k += 32) dst[k] = t.M[k];
       }
     }
-    // ---- radial functions: lanes over functions, list order
+    // ---- radial functions: lanes over functions; each lane walks its list with four
+    // independent partial sums (the cutoff table is zero outside a function's cutoff class)
     for (int g = lane; g < a.nrad; g += 32) {
       const GDesc d = a.rad[g];
       const T *P = a.radp + 8 * g;
@@ -49,25 +50,35 @@ __global__ void __launch_bounds__(256) acsf_kernel(TileArgs<T> a) {
       const int n = d.chan1 >= 0 ? t.cnt[d.chan1] : np;
       const T *fcr = t.fc + d.rclass * a.cap;
       const T idi = atom_id<T>(a.ext, a.next, d.atomid, i);
-      T acc = 0;
-      for (int k = 0; k < n; k++) {
-        const int q = lst ? lst[k] : k;
-        if (!((t.info[q] >> (16 + d.rclass)) & 1u)) continue;
+      auto term = [&](int q) -> T {
         const T r = t.u[q].w;
         T fc = fcr[q];
         if (d.atomid > 0) fc *= idi * atom_id<T>(a.ext, a.next, d.atomid, t.pj[q]);
-        T term;
-        if (d.type == 1) {
-          term = fc;
-        } else if (d.type == 2) {
+        if (d.type == 1) return fc;
+        if (d.type == 2) {
           const T x = r - rs;
-          term = m_exp<T>(-(eta * (x * x))) * fc;
-        } else {
-          term = m_cos<T>(kappa * r) * fc;
+          return m_exp<T>(-(eta * (x * x))) * fc;
         }
-        acc += term;
+        return m_cos<T>(kappa * r) * fc;
+      };
+      T acc0 = 0, acc1 = 0, acc2 = 0, acc3 = 0;
+      int k = 0;
+      for (; k + 4 <= n; k += 4) {
+        int q0 = k, q1 = k + 1, q2 = k + 2, q3 = k + 3;
+        if (lst) {
+          const uint2 w = *reinterpret_cast<const uint2 *>(lst + k);
+          q0 = (int)(w.x & 0xffffu);
+          q1 = (int)(w.x >> 16);
+          q2 = (int)(w.y & 0xffffu);
+          q3 = (int)(w.y >> 16);
+        }
+        acc0 += term(q0);
+        acc1 += term(q1);
+        acc2 += term(q2);
+        acc3 += term(q3);
       }
-      a.feat[row * a.nf + d.out] = acc;
+      for (; k < n; k++) acc0 += term(lst ? lst[k] : k);
+      a.feat[row * a.nf + d.out] = (acc0 + acc1) + (acc2 + acc3);
     }
     // ---- integer-xi G5 through moments: lanes over functions
     for (int f = lane; f < a.nmf; f += 32) {

@@ -228,7 +228,7 @@ template <typename T> __host__ __device__ inline size_t radtab_bytes(int nrad) {
 }
 
 template <typename T, int D>
-__global__ void __launch_bounds__(256) forces_kernel(TileArgs<T> a) {
+__global__ void __launch_bounds__(256, 3) forces_kernel(TileArgs<T> a) {
   extern __shared__ __align__(128) unsigned char smem[];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int wpb = blockDim.x >> 5;
@@ -255,36 +255,44 @@ __global__ void __launch_bounds__(256) forces_kernel(TileArgs<T> a) {
       const bool self = (inf >> 8) & 1u;
       if (self) continue;  // self images do not move relative to the centre
       const T r = tl.u[q].w;
-      T dsum = 0;
+      // dE/dr of the radial functions: the cutoff tables are zero outside a function's
+      // cutoff class; two independent partial sums per segment
+      auto dterm = [&](int g) -> T {
+        const RadEntry<T> re = rt[g];
+        const int rcl = (re.meta >> 4) & 15;
+        T fc = tl.fc[rcl * a.cap + q], dfc = tl.dfc[rcl * a.cap + q];
+        const int aid = re.meta >> 8;
+        if (aid > 0) {
+          const T ids = atom_id<T>(a.ext, a.next, aid, i) * atom_id<T>(a.ext, a.next, aid, tl.pj[q]);
+          fc *= ids;
+          dfc *= ids;
+        }
+        const int ty = re.meta & 15;
+        T dg;
+        if (ty == 1) {
+          dg = dfc;
+        } else if (ty == 2) {
+          const T x = r - re.p0, eta = re.p1;
+          dg = m_exp<T>(-(eta * (x * x))) * (dfc - (T)2 * eta * x * fc);
+        } else {
+          const T kr = re.p0 * r;
+          dg = m_cos<T>(kr) * dfc - re.p0 * m_sin<T>(kr) * fc;
+        }
+        return tl.jv[re.out] * dg;
+      };
+      T ds0 = 0, ds1 = 0;
       const int nseg = code < a.nz ? 2 : 1;
       for (int sg = 0; sg < nseg; sg++) {
         const int g0 = sg == 0 ? 0 : a.rad_seg[code + 1];
         const int g1 = sg == 0 ? a.rad_seg[1] : a.rad_seg[code + 2];
-        for (int g = g0; g < g1; g++) {
-          const RadEntry<T> re = rt[g];
-          const int rcl = (re.meta >> 4) & 15;
-          if (!((inf >> (16 + rcl)) & 1u)) continue;
-          T fc = tl.fc[rcl * a.cap + q], dfc = tl.dfc[rcl * a.cap + q];
-          const int aid = re.meta >> 8;
-          if (aid > 0) {
-            const T ids = atom_id<T>(a.ext, a.next, aid, i) * atom_id<T>(a.ext, a.next, aid, tl.pj[q]);
-            fc *= ids;
-            dfc *= ids;
-          }
-          const int ty = re.meta & 15;
-          T dg;
-          if (ty == 1) {
-            dg = dfc;
-          } else if (ty == 2) {
-            const T x = r - re.p0, eta = re.p1;
-            dg = m_exp<T>(-(eta * (x * x))) * (dfc - (T)2 * eta * x * fc);
-          } else {
-            const T kr = re.p0 * r;
-            dg = m_cos<T>(kr) * dfc - re.p0 * m_sin<T>(kr) * fc;
-          }
-          dsum += tl.jv[re.out] * dg;
+        int g = g0;
+        for (; g + 2 <= g1; g += 2) {
+          ds0 += dterm(g);
+          ds1 += dterm(g + 1);
         }
+        if (g < g1) ds0 += dterm(g);
       }
+      const T dsum = ds0 + ds1;
       const V4<T> u = tl.u[q];
       tl.w[q].x += dsum * u.x;
       tl.w[q].y += dsum * u.y;
