@@ -40,45 +40,60 @@ __global__ void __launch_bounds__(256) acsf_kernel(TileArgs<T> a) {
         for (int k = lane; k < nm; k += 32) dst[k] = t.M[k];
       }
     }
-    // ---- radial functions: lanes over functions; each lane walks its list with four
-    // independent partial sums (the cutoff table is zero outside a function's cutoff class)
-    for (int g = lane; g < a.nrad; g += 32) {
-      const GDesc d = a.rad[g];
-      const T *P = a.radp + 8 * g;
-      const T kappa = P[1], rs = P[2], eta = P[3];
-      const uint16_t *lst = d.chan1 >= 0 ? t.lists + d.chan1 * a.cap : nullptr;
-      const int n = d.chan1 >= 0 ? t.cnt[d.chan1] : np;
-      const T *fcr = t.fc + d.rclass * a.cap;
-      const T idi = atom_id<T>(a.ext, a.next, d.atomid, i);
-      auto term = [&](int q) -> T {
-        const T r = t.u[q].w;
-        T fc = fcr[q];
-        if (d.atomid > 0) fc *= idi * atom_id<T>(a.ext, a.next, d.atomid, t.pj[q]);
-        if (d.type == 1) return fc;
-        if (d.type == 2) {
-          const T x = r - rs;
-          return m_exp<T>(-(eta * (x * x))) * fc;
+    // ---- radial functions: items (function, part) over lanes; a function's list is split
+    // into rad_split contiguous parts on adjacent lanes (full lanes when the function count
+    // is not a multiple of 32), each part walked with four independent partial sums, the
+    // parts combined by shuffles.  The cutoff table is zero outside a function's class.
+    {
+      const int S = a.rad_split;
+      const int items = a.nrad * S;
+      for (int base = 0; base < items; base += 32) {
+        const int it = base + lane;
+        const int g = it / S, part = it - g * S;
+        T acc = 0;
+        if (it < items) {
+          const GDesc d = a.rad[g];
+          const T *P = a.radp + 8 * g;
+          const T kappa = P[1], rs = P[2], eta = P[3];
+          const uint16_t *lst = d.chan1 >= 0 ? t.lists + d.chan1 * a.cap : nullptr;
+          const int n = d.chan1 >= 0 ? t.cnt[d.chan1] : np;
+          const int chunk = ((n + S - 1) / S + 3) & ~3;
+          const int k0 = min(n, part * chunk), k1 = min(n, k0 + chunk);
+          const T *fcr = t.fc + d.rclass * a.cap;
+          const T idi = atom_id<T>(a.ext, a.next, d.atomid, i);
+          auto term = [&](int q) -> T {
+            const T r = t.u[q].w;
+            T fc = fcr[q];
+            if (d.atomid > 0) fc *= idi * atom_id<T>(a.ext, a.next, d.atomid, t.pj[q]);
+            if (d.type == 1) return fc;
+            if (d.type == 2) {
+              const T x = r - rs;
+              return m_exp<T>(-(eta * (x * x))) * fc;
+            }
+            return m_cos<T>(kappa * r) * fc;
+          };
+          T acc0 = 0, acc1 = 0, acc2 = 0, acc3 = 0;
+          int k = k0;
+          for (; k + 4 <= k1; k += 4) {
+            int q0 = k, q1 = k + 1, q2 = k + 2, q3 = k + 3;
+            if (lst) {
+              const uint2 w = *reinterpret_cast<const uint2 *>(lst + k);
+              q0 = (int)(w.x & 0xffffu);
+              q1 = (int)(w.x >> 16);
+              q2 = (int)(w.y & 0xffffu);
+              q3 = (int)(w.y >> 16);
+            }
+            acc0 += term(q0);
+            acc1 += term(q1);
+            acc2 += term(q2);
+            acc3 += term(q3);
+          }
+          for (; k < k1; k++) acc0 += term(lst ? lst[k] : k);
+          acc = (acc0 + acc1) + (acc2 + acc3);
         }
-        return m_cos<T>(kappa * r) * fc;
-      };
-      T acc0 = 0, acc1 = 0, acc2 = 0, acc3 = 0;
-      int k = 0;
-      for (; k + 4 <= n; k += 4) {
-        int q0 = k, q1 = k + 1, q2 = k + 2, q3 = k + 3;
-        if (lst) {
-          const uint2 w = *reinterpret_cast<const uint2 *>(lst + k);
-          q0 = (int)(w.x & 0xffffu);
-          q1 = (int)(w.x >> 16);
-          q2 = (int)(w.y & 0xffffu);
-          q3 = (int)(w.y >> 16);
-        }
-        acc0 += term(q0);
-        acc1 += term(q1);
-        acc2 += term(q2);
-        acc3 += term(q3);
+        for (int o = 1; o < S; o <<= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        if (it < items && part == 0) a.feat[row * a.nf + a.rad[g].out] = acc;
       }
-      for (; k < n; k++) acc0 += term(lst ? lst[k] : k);
-      a.feat[row * a.nf + d.out] = (acc0 + acc1) + (acc2 + acc3);
     }
     // ---- integer-xi G5 through moments: lanes over functions
     for (int f = lane; f < a.nmf; f += 32) {
@@ -324,6 +339,13 @@ template <typename T> int launch_acsf(fnetg_ctx *ctx) {
   TileArgs<T> a;
   fill_tile_args<T>(ctx, a);
   FNETG_CHECK(a.cap <= 65535, FNETG_E_UNSUPPORTED, "more than 65535 neighbours of one atom");
+  // radial split: the S in {1, 2, 4} with the fewest lane passes per list element
+  // (ceil(nrad S / 32) / S, ties to the smaller S)
+  a.rad_split = 1;
+  for (int S = 2; S <= 4; S <<= 1)
+    if ((double)ceil_div((int64_t)a.nrad * S, 32) / S <
+        (double)ceil_div((int64_t)a.nrad * a.rad_split, 32) / a.rad_split)
+      a.rad_split = S;
   if (a.ncombo > 0) {
     FNETG_CUDA(ctx->d_mom.ensure(sizeof(T) * (size_t)N * a.ncombo * a.n_mono));
     a.mom = ctx->d_mom.as<T>();

@@ -567,6 +567,67 @@ int fnetg_set_gfunctions(fnetg_ctx *ctx, int32_t ng, const fnetg_gfunc *g) {
     }
   }
   ctx->n_combo = (int)ctx->h_combo.size() / 2;
+  // Degree coefficients pc_f(m) = 2^(1-xi) C(xi, m) lambda^m (coef_f(alpha) = pc_f(|alpha|)
+  // times the multinomial m!/alpha!), and per combo k the partner groups: for each partner
+  // combo ko, the functions f whose adjoint sends M_ko into Q_k (listed twice when k1 = k2).
+  ctx->h_mpc.assign((size_t)ctx->h_mfunc.size() * (kMaxMomentDegree + 1), 0.0);
+  for (size_t f = 0; f < mom.size(); f++) {
+    const GDesc &d = mom[f];
+    for (int m = 0; m <= d.xi_int; m++)
+      ctx->h_mpc[f * (kMaxMomentDegree + 1) + m] =
+          d.pref * (fact(d.xi_int) / (fact(m) * fact(d.xi_int - m))) * std::pow(d.lambda, m);
+  }
+  std::vector<int32_t> qg_off(ctx->n_combo + 1, 0), qg_ko, qg_foff(1, 0), qg_f;
+  for (int k = 0; k < ctx->n_combo; k++) {
+    qg_off[k] = (int32_t)qg_ko.size();
+    std::vector<std::pair<int, std::vector<int32_t>>> groups;
+    auto add = [&](int ko, int f) {
+      for (auto &g : groups)
+        if (g.first == ko) {
+          g.second.push_back(f);
+          return;
+        }
+      groups.push_back({ko, {f}});
+    };
+    for (size_t f = 0; f < ctx->h_mfunc.size(); f++) {
+      const MFunc &mf = ctx->h_mfunc[f];
+      if (mf.k1 == k) add(mf.k2, (int)f);
+      if (mf.k2 == k) add(mf.k1, (int)f);
+    }
+    for (auto &g : groups) {
+      qg_ko.push_back(g.first);
+      qg_f.insert(qg_f.end(), g.second.begin(), g.second.end());
+      qg_foff.push_back((int32_t)qg_f.size());
+    }
+  }
+  qg_off[ctx->n_combo] = (int32_t)qg_ko.size();
+  ctx->n_qgroups = (int)qg_ko.size();
+  {
+    // [n_combo + 1] group offsets, [G] partner combos, [G + 1] entry offsets, [E] output
+    // column of each entry's function; the entries' degree coefficients follow in d_mpc_*
+    std::vector<int32_t> pack;
+    pack.insert(pack.end(), qg_off.begin(), qg_off.end());
+    pack.insert(pack.end(), qg_ko.begin(), qg_ko.end());
+    pack.insert(pack.end(), qg_foff.begin(), qg_foff.end());
+    for (int32_t f : qg_f) pack.push_back(ctx->h_mfunc[f].out);
+    std::vector<double> epc;
+    for (int32_t f : qg_f)
+      epc.insert(epc.end(), ctx->h_mpc.begin() + (size_t)f * (kMaxMomentDegree + 1),
+                 ctx->h_mpc.begin() + (size_t)(f + 1) * (kMaxMomentDegree + 1));
+    ctx->h_mpc = epc;
+    FNETG_CUDA(ctx->d_qgroups.ensure(sizeof(int32_t) * std::max<size_t>(pack.size(), 1)));
+    FNETG_CUDA(cudaMemcpy(ctx->d_qgroups.p, pack.data(), sizeof(int32_t) * pack.size(),
+                          cudaMemcpyHostToDevice));
+    std::vector<float> pcf(ctx->h_mpc.begin(), ctx->h_mpc.end());
+    FNETG_CUDA(ctx->d_mpc_d.ensure(sizeof(double) * std::max<size_t>(ctx->h_mpc.size(), 1)));
+    FNETG_CUDA(ctx->d_mpc_f.ensure(sizeof(float) * std::max<size_t>(pcf.size(), 1)));
+    if (!pcf.empty()) {
+      FNETG_CUDA(cudaMemcpy(ctx->d_mpc_d.p, ctx->h_mpc.data(), sizeof(double) * ctx->h_mpc.size(),
+                            cudaMemcpyHostToDevice));
+      FNETG_CUDA(cudaMemcpy(ctx->d_mpc_f.p, pcf.data(), sizeof(float) * pcf.size(),
+                            cudaMemcpyHostToDevice));
+    }
+  }
   // per-combo list of the moment functions whose Q (adjoint moment) it receives
   std::vector<int32_t> qoff(ctx->n_combo + 1, 0), qent;
   for (int k = 0; k < ctx->n_combo; k++) {

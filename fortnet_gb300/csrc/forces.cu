@@ -233,7 +233,7 @@ __global__ void __launch_bounds__(256, 3) forces_kernel(TileArgs<T> a) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int wpb = blockDim.x >> 5;
   const size_t tb = tile_bytes<T>(a.cap, a.nrcls, a.necls, a.nz, a.ncombo, a.n_mono, a.ng, true, a.ngroups > 0,
-                    tile_etab(a, true));
+                    tile_etab(a, true), tile_qwords(a));
   RadEntry<T> *rt = reinterpret_cast<RadEntry<T> *>(smem);
   for (int g = threadIdx.x; g < a.nrad; g += blockDim.x) {
     const GDesc d = a.rad[g];
@@ -243,6 +243,13 @@ __global__ void __launch_bounds__(256, 3) forces_kernel(TileArgs<T> a) {
   }
   __syncthreads();
   Tile<T> tl = carve_tile<T>(smem + radtab_bytes<T>(a.nrad) + tb * warp, a, true);
+  // degrees and multinomial weights of this lane's monomials (lane, lane + 32)
+  const int mdeg0 = lane < kMaxMono ? kMonoTab[lane][0] + kMonoTab[lane][1] + kMonoTab[lane][2] : 0;
+  const int mdeg1 = lane + 32 < kMaxMono
+                        ? kMonoTab[lane + 32][0] + kMonoTab[lane + 32][1] + kMonoTab[lane + 32][2]
+                        : 0;
+  const T mmult0 = lane < kMaxMono ? (T)kMonoMult[lane] : (T)0;
+  const T mmult1 = lane + 32 < kMaxMono ? (T)kMonoMult[lane + 32] : (T)0;
   for (int64_t i = (int64_t)blockIdx.x * wpb + warp; i < a.natoms; i += (int64_t)gridDim.x * wpb) {
     const int64_t p0 = a.poff[i];
     const int np = (int)(a.pend[i] - p0);
@@ -308,28 +315,42 @@ __global__ void __launch_bounds__(256, 3) forces_kernel(TileArgs<T> a) {
       } else {
         compute_moments<T, (D > 0 ? D : 1)>(a, tl, np, lane);
       }
-      for (int it = lane; it < a.ncombo * NM; it += 32) {
-        const int k = it / NM, al = it - k * NM;
+      // Adjoint moments, factorised: coef_f(alpha) = mult(alpha) pc_f(|alpha|), so for every
+      // partner group g (combo k receiving M of combo ko through functions F_g)
+      //   h_g(m) = sum_{f in F_g} J_out(f) pc_f(m),
+      //   Qc[z][e](alpha) = mult(alpha) sum_{k in {list z, all atoms}} sum_{g of k}
+      //                     h_g(|alpha|) M_{ko(g)}(alpha).
+      constexpr int KD = kMaxMomentDegree + 1;
+      const int32_t *qg_off = a.qg, *qg_ko = a.qg + a.ncombo + 1;
+      const int32_t *qg_eoff = qg_ko + a.nqg, *qg_out = qg_eoff + a.nqg + 1;
+      T *H = tl.Q;
+      for (int it = lane; it < a.nqg * KD; it += 32) {
+        const int g = it / KD, m = it - g * KD;
         T acc = 0;
-        for (int e = a.qoff[k]; e < a.qoff[k + 1]; e++) {
-          const int f = a.qent[2 * e], ko = a.qent[2 * e + 1];
-          acc += tl.jv[a.mfunc[f].out] * a.mcoef[(int64_t)f * NM + al] * tl.M[ko * NM + al];
-        }
-        tl.Q[it] = acc;
+        for (int e = qg_eoff[g]; e < qg_eoff[g + 1]; e++)
+          acc += tl.jv[qg_out[e]] * a.mpc[e * KD + m];
+        H[it] = acc;
       }
       __syncwarp();
-      // a pair of species code z sees the combos of its own list and of the all-atom list
+      // this lane's monomials lane and lane + 32 (degree and weight fixed per kernel)
       for (int zz = 0; zz <= a.nz; zz++)
         for (int e = 0; e < a.necls; e++) {
           const int ks = zz < a.nz ? a.cidx[(zz + 1) * a.necls + e] : -1;
           const int ka = a.cidx[e];
-          T *dst = tl.Qc + ((int64_t)zz * a.necls + e) * NM;
-          for (int al = lane; al < NM; al += 32) {
-            T v = 0;
-            if (ks >= 0) v += tl.Q[ks * NM + al];
-            if (ka >= 0) v += tl.Q[ka * NM + al];
-            dst[al] = v;
+          T v0 = 0, v1 = 0;
+          for (int side = 0; side < 2; side++) {
+            const int k = side == 0 ? ks : ka;
+            if (k < 0) continue;
+            for (int g = qg_off[k]; g < qg_off[k + 1]; g++) {
+              const T *Mk = tl.M + qg_ko[g] * NM;
+              const T *Hg = H + g * KD;
+              if (lane < NM) v0 += Hg[mdeg0] * Mk[lane];
+              if (lane + 32 < NM) v1 += Hg[mdeg1] * Mk[lane + 32];
+            }
           }
+          T *dst = tl.Qc + ((int64_t)zz * a.necls + e) * NM;
+          if (lane < NM) dst[lane] = mmult0 * v0;
+          if (lane + 32 < NM) dst[lane + 32] = mmult1 * v1;
         }
       __syncwarp();
       for (int q = lane; q < np; q += 32) {
@@ -437,6 +458,9 @@ template <typename T> void fill_tile_args_forces(fnetg_ctx *ctx, TileArgs<T> &a)
   a.mcoef = static_cast<const T *>(dbl ? ctx->d_mcoef.p : ctx->d_mcoef_f.p);
   a.qoff = ctx->d_qoff.as<int32_t>();
   a.qent = ctx->d_qent.as<int32_t>();
+  a.qg = ctx->d_qgroups.as<int32_t>();
+  a.nqg = ctx->n_qgroups;
+  a.mpc = static_cast<const T *>(dbl ? ctx->d_mpc_d.p : ctx->d_mpc_f.p);
   a.combo = ctx->d_combo.as<int32_t>();
   a.ncombo = ctx->n_combo;
   a.cidx = ctx->d_cidx.as<int32_t>();
@@ -448,7 +472,7 @@ template <typename T> void fill_tile_args_forces(fnetg_ctx *ctx, TileArgs<T> &a)
 template <typename T, int D> int launch_forces_d(fnetg_ctx *ctx, TileArgs<T> &a, int nout) {
   const int64_t N = ctx->N;
   const size_t tb = tile_bytes<T>(a.cap, a.nrcls, a.necls, a.nz, a.ncombo, a.n_mono, a.ng, true, a.ngroups > 0,
-                    tile_etab(a, true));
+                    tile_etab(a, true), tile_qwords(a));
   const size_t rb = radtab_bytes<T>(a.nrad);
   int wpb = 1, per_sm = 1;
   size_t smem = 0;

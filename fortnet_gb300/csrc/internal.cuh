@@ -135,6 +135,10 @@ struct fnetg_ctx {
   std::vector<int32_t> h_combo;     // [ncombo][2] (list code or -1 = all, eta class)
   std::vector<int32_t> h_cidx;      // [(nz+1) * necls] combo index, -1 if unused
   fnetg::DBuf d_mfunc, d_mcoef, d_combo, d_cidx, d_qoff, d_qent;
+  std::vector<double> h_mpc;    // [entries][kMaxMomentDegree + 1] degree coefficients of the
+                                // adjoint group entries
+  int n_qgroups = 0;            // adjoint partner groups over all combos
+  fnetg::DBuf d_qgroups, d_mpc_d, d_mpc_f;
   // kernel parameter copies in both arithmetic widths: [rcut, kappa, rs, eta, lambda, xi, pref, 0]
   fnetg::DBuf d_radpar_f, d_radpar_d, d_angpar_f, d_angpar_d, d_mcoef_f, d_ecls_eta_f, d_rcls_f;
   fnetg::DBuf d_rad, d_ang, d_groups, d_code, d_ecls_eta, d_ecls_rclass, d_ecls_atomid,

@@ -28,6 +28,20 @@ __device__ constexpr int kMonoTab[kMaxMono][3] = {
 
 __host__ __device__ constexpr int n_mono_of(int D) { return (D + 1) * (D + 2) * (D + 3) / 6; }
 
+// multinomial weights m! / (a! b! c!) of the monomials above
+__device__ constexpr int kMonoMult[kMaxMono] = {1, 1, 1, 1, 1, 2, 2, 1, 2, 1, 1, 3, 3, 3, 6, 3, 1, 3,
+                                                3, 1, 1, 4, 4, 6, 12, 6, 4, 12, 12, 4, 1, 4, 6, 4, 1};
+constexpr int mono_fact(int n) { return n <= 1 ? 1 : n * mono_fact(n - 1); }
+constexpr bool mono_mult_table_ok() {
+  for (int al = 0; al < kMaxMono; al++) {
+    const int a = kMonoTab[al][0], b = kMonoTab[al][1], c = kMonoTab[al][2];
+    if (kMonoMult[al] * mono_fact(a) * mono_fact(b) * mono_fact(c) != mono_fact(a + b + c))
+      return false;
+  }
+  return true;
+}
+static_assert(mono_mult_table_ok(), "multinomial table");
+
 // Float exp on the FMA/ALU pipes only (the library's range reduction spends conversion
 // instructions, which GB300 issues on its narrow FP64 pipe).  Cody-Waite reduction:
 // n = round(x log2 e) by adding 1.5 * 2^23 (the float sum rounds to an integer; n is read back
@@ -155,6 +169,7 @@ template <typename T> struct TileArgs {
   const T *radp;          // [nrad][8] parameters in the kernel's width
   int nrad;
   int rad_seg[kMaxSpeciesCodes + 2];  // radial functions by list channel (see the context)
+  int rad_split;          // value kernel: lanes per radial function (1, 2 or 4)
   const GDesc *ang;       // triplet-sweep functions
   const T *angp;          // [nang][8]
   const AGroup *groups;
@@ -177,6 +192,12 @@ template <typename T> struct TileArgs {
   int ncombo;
   const int32_t *cidx;    // [(nz+1)*necls]
   int n_mono;
+  // factorised adjoint (forces): partner groups packed as [ncombo + 1] group offsets, [nqg]
+  // partner combos, [nqg + 1] entry offsets, [entries] output columns; degree coefficients
+  // mpc[entry][kMaxMomentDegree + 1]
+  const int32_t *qg;
+  int nqg;
+  const T *mpc;
   // moment cache [natoms][ncombo][n_mono]: written by the ACSF kernel (mom != null), read by
   // the force kernel when mom_cached
   T *mom;
@@ -204,12 +225,17 @@ template <typename T> struct Tile {
   int *gint;        // [3][32]
   int *cnt;         // [8]
   T *M;             // [ncombo][n_mono] moments
-  T *Q;             // [ncombo][n_mono] adjoint moments (forces)
+  T *Q;             // [nqg][kMaxMomentDegree + 1] per-group degree sums h_g(m) (forces)
   T *Qc;            // [nz + 1][necls][n_mono] adjoint moments of a pair's species list plus
                     // the all-atom list, per eta class (forces; row nz: all-atom list only)
   T *jv;            // [ng] dE/dG of the centre atom (forces)
   uint16_t *lists;  // [nz][cap]
 };
+
+// Length of the force tile's adjoint scratch: the per-group degree sums h_g(m).
+template <typename T> __host__ __device__ inline int tile_qwords(const TileArgs<T> &a) {
+  return a.ncombo > 0 ? a.nqg * (kMaxMomentDegree + 1) : 0;
+}
 
 // Whether a tile keeps per-pair E/D tables: the value kernel always; the force kernel for
 // triplet groups or when the moments are recomputed rather than read from the cache.
@@ -220,7 +246,7 @@ template <typename T> __host__ __device__ inline bool tile_etab(const TileArgs<T
 template <typename T>
 __host__ __device__ inline size_t tile_bytes(int cap, int nrcls, int necls, int nz, int ncombo,
                                              int nmono, int ng, bool forces, bool trip,
-                                             bool etab) {
+                                             bool etab, int qwords = 0) {
   // v and idv serve the triplet sweep only; the E (and, for forces, D) tables are kept when
   // etab (values, triplets, or moments not taken from the cache)
   size_t b = 0;
@@ -228,7 +254,8 @@ __host__ __device__ inline size_t tile_bytes(int cap, int nrcls, int necls, int 
   b += sizeof(T) * (size_t)cap * (nrcls + (etab ? necls : 0)) * (forces ? 2 : 1);
   if (trip) b += sizeof(T) * cap;             // idv
   b += sizeof(T) * 5 * 32;                    // gpar
-  b += sizeof(T) * (size_t)ncombo * nmono * (forces ? 2 : 1);
+  b += sizeof(T) * (size_t)ncombo * nmono;
+  if (forces) b += sizeof(T) * (size_t)qwords;
   if (forces && ncombo > 0) b += sizeof(T) * (size_t)(nz + 1) * necls * nmono;
   b += forces ? sizeof(T) * ng : 0;
   b = (b + 7) / 8 * 8;
@@ -284,7 +311,7 @@ __device__ Tile<T> carve_tile(unsigned char *p, const TileArgs<T> &a, bool force
   t.Q = t.jv = t.Qc = nullptr;
   if (forces) {
     t.Q = reinterpret_cast<T *>(p);
-    p += sizeof(T) * (size_t)a.ncombo * a.n_mono;
+    p += sizeof(T) * (size_t)tile_qwords(a);
     if (a.ncombo > 0) {
       t.Qc = reinterpret_cast<T *>(p);
       p += sizeof(T) * (size_t)(a.nz + 1) * a.necls * a.n_mono;
