@@ -73,6 +73,53 @@ def build(force=False, verbose=False, extra=None):
     return LIB
 
 
+HOST_DIR = os.path.join(HERE, "host")
+HOST_LIB = os.path.join(OUT_DIR, "libfnetg_host.so")
+HOST_RUN = os.path.join(OUT_DIR, "fnetg_run")
+HOST_SOURCES = ["hdf5lite.cpp", "fnet_host.cpp"]
+
+
+def cuda_lib_dir():
+    return os.path.join(os.path.dirname(os.path.dirname(os.path.realpath(nvcc_path()))), "lib64")
+
+
+def host_flags():
+    """g++ flags for the C++ host layer and programs linked against it."""
+    return ["-std=c++17", "-O2", "-fPIC", "-ffp-contract=off", "-I", HOST_DIR,
+            "-I", os.path.join(HERE, "..", "include")]
+
+
+def host_link_flags():
+    return ["-L", OUT_DIR, "-lfnetg_host", "-lfnetg", "-L", cuda_lib_dir(), "-lcudart",
+            "-Wl,-rpath," + OUT_DIR, "-Wl,-rpath," + cuda_lib_dir()]
+
+
+def build_host(force=False):
+    """The C++ host layer (libfnetg_host.so) and the fnetg_run driver, on top of libfnetg."""
+    build()
+    srcs = [os.path.join(HOST_DIR, f) for f in HOST_SOURCES + ["fnetg_run.cpp"]]
+    hdrs = [os.path.join(HOST_DIR, f) for f in os.listdir(HOST_DIR) if f.endswith(".hpp")]
+    newest = max(os.path.getmtime(f) for f in srcs + hdrs + [LIB])
+    if (not force and os.path.exists(HOST_RUN) and os.path.exists(HOST_LIB)
+            and os.path.getmtime(HOST_RUN) >= newest and os.path.getmtime(HOST_LIB) >= newest):
+        return HOST_LIB
+    cmd = (["g++", "-shared", "-o", HOST_LIB + ".tmp"] + host_flags()
+           + [os.path.join(HOST_DIR, f) for f in HOST_SOURCES]
+           + ["-L", OUT_DIR, "-lfnetg", "-Wl,-rpath," + OUT_DIR])
+    res = subprocess.run(cmd, capture_output=True, text=True)
+    if res.returncode != 0:
+        raise RuntimeError(f"host library build failed:\n{res.stdout}\n{res.stderr}")
+    os.replace(HOST_LIB + ".tmp", HOST_LIB)
+    cmd = (["g++", "-o", HOST_RUN + ".tmp"] + host_flags()
+           + [os.path.join(HOST_DIR, "fnetg_run.cpp")] + host_link_flags())
+    res = subprocess.run(cmd, capture_output=True, text=True)
+    if res.returncode != 0:
+        raise RuntimeError(f"fnetg_run build failed:\n{res.stdout}\n{res.stderr}")
+    os.replace(HOST_RUN + ".tmp", HOST_RUN)
+    return HOST_LIB
+
+
 if __name__ == "__main__":
     print(build(force="--force" in sys.argv, verbose=True,
                 extra=["-Xptxas", "-v"] if "--ptxas" in sys.argv else None))
+    print(build_host(force="--force" in sys.argv))
