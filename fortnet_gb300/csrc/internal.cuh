@@ -179,6 +179,10 @@ struct fnetg_ctx {
   int64_t nparams = 0;
   std::vector<int64_t> woff, boff;
   std::vector<int64_t> h_sp_tile0;  // [nsp+1] first MLP tile of every species
+  // MLP launch variants picked by timing on first use, per precision and kernel kind
+  // (forward, Jacobian, backward), for the network shape mlp_dims
+  int mlp_cfg[6] = {-1, -1, -1, -1, -1, -1};
+  std::vector<int32_t> mlp_dims;
   fnetg::DBuf d_params64, d_params, d_ref_of_compute, d_sp_tile0;
   fnetg::DBuf d_gchunk;  // FP64 gradient sums of tile chunks
 

@@ -19,7 +19,6 @@ namespace fnetg {
 
 namespace {
 
-constexpr int kMlpThreads = 128;
 
 __host__ __device__ inline int pad4(int x) { return (x + 3) & ~3; }
 
@@ -154,40 +153,63 @@ template <typename T> __device__ __forceinline__ T comp(const V4<T> &v, int i) {
   return i == 0 ? v.x : (i == 1 ? v.y : (i == 2 ? v.z : v.w));
 }
 
+// OW consecutive weights (4 or 2) from shared (SW) or global memory (read-only path)
+template <typename T, int OW, bool SW>
+__device__ __forceinline__ void wload(const T *p, T (&w)[OW]) {
+  if constexpr (OW == 4) {
+    const V4<T> v = SW ? lds4(p) : ldg4(p);
+    w[0] = v.x;
+    w[1] = v.y;
+    w[2] = v.z;
+    w[3] = v.w;
+  } else {
+    if (SW) {
+      w[0] = p[0];
+      w[1] = p[1];
+    } else {
+      w[0] = __ldg(p);
+      w[1] = __ldg(p + 1);
+    }
+  }
+}
+
 // acc[i][j] += x_i * w_j
-template <typename T>
-__device__ __forceinline__ void fma44(T (&acc)[4][4], const V4<T> &x, const V4<T> &w) {
-  const T xs[4] = {x.x, x.y, x.z, x.w}, ws[4] = {w.x, w.y, w.z, w.w};
+template <typename T, int OW>
+__device__ __forceinline__ void fma4w(T (&acc)[4][OW], const V4<T> &x, const T (&w)[OW]) {
+  const T xs[4] = {x.x, x.y, x.z, x.w};
 #pragma unroll
   for (int i = 0; i < 4; i++)
 #pragma unroll
-    for (int j = 0; j < 4; j++) acc[i][j] += xs[i] * ws[j];
+    for (int j = 0; j < OW; j++) acc[i][j] += xs[i] * w[j];
 }
 
-// Y[o][r] = b[o] + sum_k X[k][r] W[k][o] for the chunk's RC rows.  hidden: Y = f(z) and
-// Fp (if given) = f'(z); otherwise Y = z.  Columns o >= dout are not written.
-template <typename T>
+// Y[o][r] = b[o] + sum_k X[k][r] W[k][o] for the chunk's RC rows; a thread computes a
+// 4-row x OW-output tile.  hidden: Y = f(z) and Fp (if given) = f'(z); otherwise Y = z.
+// Columns o >= dout are not written.
+template <typename T, int OW, bool SW>
 __device__ void layer_forward(const T *X, int din, const T *__restrict__ W,
                               const T *__restrict__ b, int dout, T *Y, T *Fp, int RC, int RCP,
                               bool hidden, int act) {
-  const int ngr = RC >> 2, dp = pad4(dout), items = ngr * (dp >> 2);
+  const int ngr = RC >> 2, dp = pad4(dout), items = ngr * ((dp + OW - 1) / OW);
   for (int it = threadIdx.x; it < items; it += blockDim.x) {
-    const int r0 = (it % ngr) << 2, o0 = (it / ngr) << 2;
-    const V4<T> bb = ldg4(b + o0);
-    T acc[4][4];
+    const int r0 = (it % ngr) << 2, o0 = (it / ngr) * OW;
+    T bb[OW];
+    wload<T, OW, SW>(b + o0, bb);
+    T acc[4][OW];
 #pragma unroll
-    for (int i = 0; i < 4; i++) {
-      acc[i][0] = bb.x;
-      acc[i][1] = bb.y;
-      acc[i][2] = bb.z;
-      acc[i][3] = bb.w;
-    }
+    for (int i = 0; i < 4; i++)
+#pragma unroll
+      for (int j = 0; j < OW; j++) acc[i][j] = bb[j];
     const T *xp = X + r0;
     const T *wp = W + o0;
 #pragma unroll 4
-    for (int k = 0; k < din; k++) fma44(acc, lds4(xp + (int64_t)k * RCP), ldg4(wp + (int64_t)k * dp));
+    for (int k = 0; k < din; k++) {
+      T w[OW];
+      wload<T, OW, SW>(wp + (int64_t)k * dp, w);
+      fma4w<T, OW>(acc, lds4(xp + (int64_t)k * RCP), w);
+    }
 #pragma unroll
-    for (int j = 0; j < 4; j++) {
+    for (int j = 0; j < OW; j++) {
       if (o0 + j >= dout) break;
       if (hidden) {
         T f[4], d[4];
@@ -202,25 +224,28 @@ __device__ void layer_forward(const T *X, int din, const T *__restrict__ W,
   }
 }
 
-// Dn[k][r] = (Fp[k][r] if given) * sum_o WT[o][k] D[o][r]
-template <typename T>
+// Dn[k][r] = (Fp[k][r] if given) * sum_o WT[o][k] D[o][r]; 4-row x OW-input tiles
+template <typename T, int OW, bool SW>
 __device__ void layer_backward(const T *D, int dout, const T *__restrict__ WT, int din,
                                const T *Fp, T *Dn, int RC, int RCP) {
-  const int ngr = RC >> 2, kp = pad4(din), items = ngr * (kp >> 2);
+  const int ngr = RC >> 2, kp = pad4(din), items = ngr * ((kp + OW - 1) / OW);
   for (int it = threadIdx.x; it < items; it += blockDim.x) {
-    const int r0 = (it % ngr) << 2, k0 = (it / ngr) << 2;
-    T acc[4][4];
+    const int r0 = (it % ngr) << 2, k0 = (it / ngr) * OW;
+    T acc[4][OW];
 #pragma unroll
     for (int i = 0; i < 4; i++)
 #pragma unroll
-      for (int j = 0; j < 4; j++) acc[i][j] = (T)0;
+      for (int j = 0; j < OW; j++) acc[i][j] = (T)0;
     const T *dp_ = D + r0;
     const T *wp = WT + k0;
 #pragma unroll 4
-    for (int o = 0; o < dout; o++)
-      fma44(acc, lds4(dp_ + (int64_t)o * RCP), ldg4(wp + (int64_t)o * kp));
+    for (int o = 0; o < dout; o++) {
+      T w[OW];
+      wload<T, OW, SW>(wp + (int64_t)o * kp, w);
+      fma4w<T, OW>(acc, lds4(dp_ + (int64_t)o * RCP), w);
+    }
 #pragma unroll
-    for (int j = 0; j < 4; j++) {
+    for (int j = 0; j < OW; j++) {
       if (k0 + j >= din) break;
       T v[4] = {acc[0][j], acc[1][j], acc[2][j], acc[3][j]};
       if (Fp) {
@@ -301,11 +326,14 @@ __device__ void layer_wgrad(const T *A, int din, const T *D, int dout, T *GW, T 
 // Shared-memory plan of a chunk (element offsets): A_l (l = 0..L-2) inputs of every layer,
 // Fp_l (l = 1..L-2) activation derivatives, two delta buffers of maxd rows.
 struct SmemPlan {
-  int64_t A[kMaxLayers], F[kMaxLayers], D0, D1, total;
+  int64_t A[kMaxLayers], F[kMaxLayers], D0, D1, W, total;  // W: staged weights (or -1)
 };
-__host__ __device__ inline SmemPlan smem_plan(const NetDesc &n, int RCP, bool keep_all) {
+__host__ __device__ inline SmemPlan smem_plan(const NetDesc &n, int RCP, bool keep_all,
+                                              bool sw = false) {
   SmemPlan p{};
-  int64_t o = 0;
+  // staged weights first (the compute layout of one species: W, b, W^T)
+  int64_t o = sw ? n.pstride : 0;
+  p.W = sw ? 0 : -1;
   const int L = n.nlayer;
   if (keep_all) {
     for (int l = 0; l < L - 1; l++) {
@@ -318,8 +346,8 @@ __host__ __device__ inline SmemPlan smem_plan(const NetDesc &n, int RCP, bool ke
     }
   } else {
     // forward only: A_0, then hidden layers ping-pong in the delta buffers
-    p.A[0] = 0;
-    o = (int64_t)pad4(n.dims[0]) * RCP;
+    p.A[0] = o;
+    o += (int64_t)pad4(n.dims[0]) * RCP;
   }
   p.D0 = o;
   o += (int64_t)pad4(n.maxd) * RCP;
@@ -335,6 +363,7 @@ template <typename T> struct MlpArgs {
   const T *feat;          // bucketed rows [N][nf]
   int nf;
   const int4 *tiles;      // (species, row0, nrows, 0)
+  int64_t ntiles;         // CTAs loop over the tiles in steps of gridDim.x
   const int32_t *bperm;   // row -> atom
   int RC, RCP;            // rows per chunk, padded row stride of the shared buffers
   SmemPlan pl;            // shared-memory offsets (kernel parameter: indexed without local copies)
@@ -361,143 +390,174 @@ __device__ void load_features(const MlpArgs<T> &a, int64_t row0, int nrows, T *X
       X[(int64_t)k * a.RCP + r] = r < nrows ? a.feat[(row0 + r) * nf + k] : (T)0;
 }
 
-template <typename T>
-__global__ void __launch_bounds__(kMlpThreads) mlp_forward_kernel(MlpArgs<T> a) {
+template <int OW> constexpr int mlp_threads() { return OW == 4 ? 128 : 256; }
+
+// The parameters of the tile's species: staged in shared memory once per species switch (SW),
+// else read from global memory.
+template <typename T, bool SW>
+__device__ __forceinline__ const T *tile_params(const MlpArgs<T> &a, int species, int &staged,
+                                                T *sm) {
+  const T *P = a.params + (int64_t)species * a.net.pstride;
+  if (!SW) return P;
+  T *sw = sm + a.pl.W;
+  if (species != staged) {
+    __syncthreads();
+    for (int64_t q = 4 * (int64_t)threadIdx.x; q < a.net.pstride; q += 4 * (int64_t)blockDim.x)
+      *reinterpret_cast<V4<T> *>(sw + q) = ldg4(P + q);
+    __syncthreads();
+    staged = species;
+  }
+  return sw;
+}
+
+template <typename T, int OW, bool SW>
+__global__ void __launch_bounds__(mlp_threads<OW>()) mlp_forward_kernel(MlpArgs<T> a) {
   extern __shared__ __align__(32) unsigned char smem_raw[];
   T *sm = reinterpret_cast<T *>(smem_raw);
-  const int4 tl = a.tiles[blockIdx.x];
   const NetDesc &n = a.net;
   const int L = n.nlayer;
-  const T *P = a.params + (int64_t)tl.x * n.pstride;
   const SmemPlan &pl = a.pl;
   const int nout = n.dims[L - 1];
-  for (int c0 = 0; c0 < tl.z; c0 += a.RC) {
-    const int nrows = min(a.RC, tl.z - c0);
-    const int64_t row0 = tl.y + c0;
-    load_features(a, row0, nrows, sm + pl.A[0]);
-    __syncthreads();
-    const T *in = sm + pl.A[0];
-    for (int l = 0; l < L - 1; l++) {
-      T *dst = sm + ((l & 1) ? pl.D1 : pl.D0);
-      layer_forward<T>(in, n.dims[l], P + n.cw[l], P + n.cb[l], n.dims[l + 1], dst, nullptr,
-                       a.RC, a.RCP, l < L - 2, n.act);
+  int staged = -1;
+  for (int64_t ti = blockIdx.x; ti < a.ntiles; ti += gridDim.x) {
+    const int4 tl = a.tiles[ti];
+    const T *P = tile_params<T, SW>(a, tl.x, staged, sm);
+    for (int c0 = 0; c0 < tl.z; c0 += a.RC) {
+      const int nrows = min(a.RC, tl.z - c0);
+      const int64_t row0 = tl.y + c0;
+      load_features(a, row0, nrows, sm + pl.A[0]);
       __syncthreads();
-      in = dst;
+      const T *in = sm + pl.A[0];
+      for (int l = 0; l < L - 1; l++) {
+        T *dst = sm + ((l & 1) ? pl.D1 : pl.D0);
+        layer_forward<T, OW, SW>(in, n.dims[l], P + n.cw[l], P + n.cb[l], n.dims[l + 1], dst,
+                                 nullptr, a.RC, a.RCP, l < L - 2, n.act);
+        __syncthreads();
+        in = dst;
+      }
+      for (int r = threadIdx.x; r < nrows; r += blockDim.x) {
+        const int64_t atom = a.bperm[row0 + r];
+        for (int o = 0; o < nout; o++) a.out[atom * nout + o] = (double)in[(int64_t)o * a.RCP + r];
+      }
+      __syncthreads();
     }
-    for (int r = threadIdx.x; r < nrows; r += blockDim.x) {
-      const int64_t atom = a.bperm[row0 + r];
-      for (int o = 0; o < nout; o++) a.out[atom * nout + o] = (double)in[(int64_t)o * a.RCP + r];
-    }
-    __syncthreads();
   }
 }
 
 // Forward keeping every layer's inputs and activation derivatives of the chunk.
-template <typename T>
+template <typename T, int OW, bool SW>
 __device__ void forward_keep(const MlpArgs<T> &a, const T *P, const SmemPlan &pl, T *sm) {
   const NetDesc &n = a.net;
   const int L = n.nlayer;
   for (int l = 0; l < L - 2; l++) {
-    layer_forward<T>(sm + pl.A[l], n.dims[l], P + n.cw[l], P + n.cb[l], n.dims[l + 1],
-                     sm + pl.A[l + 1], sm + pl.F[l + 1], a.RC, a.RCP, true, n.act);
+    layer_forward<T, OW, SW>(sm + pl.A[l], n.dims[l], P + n.cw[l], P + n.cb[l], n.dims[l + 1],
+                             sm + pl.A[l + 1], sm + pl.F[l + 1], a.RC, a.RCP, true, n.act);
     __syncthreads();
   }
 }
 
 // Reverse-mode Jacobian of output jac_out with respect to the row's inputs.
-template <typename T>
-__global__ void __launch_bounds__(kMlpThreads) mlp_jacobian_kernel(MlpArgs<T> a) {
+template <typename T, int OW, bool SW>
+__global__ void __launch_bounds__(mlp_threads<OW>()) mlp_jacobian_kernel(MlpArgs<T> a) {
   extern __shared__ __align__(32) unsigned char smem_raw[];
   T *sm = reinterpret_cast<T *>(smem_raw);
-  const int4 tl = a.tiles[blockIdx.x];
   const NetDesc &n = a.net;
   const int L = n.nlayer;
-  const T *P = a.params + (int64_t)tl.x * n.pstride;
   const SmemPlan &pl = a.pl;
   const int nout = n.dims[L - 1], nf = a.nf;
-  for (int c0 = 0; c0 < tl.z; c0 += a.RC) {
-    const int nrows = min(a.RC, tl.z - c0);
-    const int64_t row0 = tl.y + c0;
-    load_features(a, row0, nrows, sm + pl.A[0]);
-    __syncthreads();
-    forward_keep(a, P, pl, sm);
-    // delta of the (linear) output layer: the unit vector of output jac_out
-    T *dcur = sm + pl.D0, *dnext = sm + pl.D1;
-    for (int r = threadIdx.x; r < a.RC; r += blockDim.x)
-      for (int o = 0; o < nout; o++) dcur[(int64_t)o * a.RCP + r] = (o == a.jac_out) ? (T)1 : (T)0;
-    __syncthreads();
-    for (int l = L - 2; l >= 1; l--) {
-      layer_backward<T>(dcur, n.dims[l + 1], P + n.ct[l], n.dims[l], sm + pl.F[l], dnext, a.RC,
-                        a.RCP);
+  int staged = -1;
+  for (int64_t ti = blockIdx.x; ti < a.ntiles; ti += gridDim.x) {
+    const int4 tl = a.tiles[ti];
+    const T *P = tile_params<T, SW>(a, tl.x, staged, sm);
+    for (int c0 = 0; c0 < tl.z; c0 += a.RC) {
+      const int nrows = min(a.RC, tl.z - c0);
+      const int64_t row0 = tl.y + c0;
+      load_features(a, row0, nrows, sm + pl.A[0]);
       __syncthreads();
-      T *tmp = dcur;
-      dcur = dnext;
-      dnext = tmp;
-    }
-    // input layer: no activation; the result replaces the features of the chunk
-    T *J = sm + pl.A[0];
-    layer_backward<T>(dcur, n.dims[1], P + n.ct[0], n.dims[0], nullptr, J, a.RC, a.RCP);
-    __syncthreads();
-    const int lane = threadIdx.x & 31, nw = blockDim.x >> 5;
-    for (int r = threadIdx.x >> 5; r < nrows; r += nw)
-    for (int k = lane; k < nf; k += 32) {
-      const T v = J[(int64_t)k * a.RCP + r];
-      const int64_t atom = a.bperm[row0 + r];
-      if (a.jac64) a.jac64[atom * nf + k] = (double)v;
-      if (a.jacT) {
-        T s = v;
-        if (sizeof(T) == 8) {
-          if (a.zsd && k < a.ng) {
-            const double sd = a.zsd[k];
-            if (sd >= 1e-08) s = (T)((double)v / sd);
-          }
-        } else if (a.zinv && k < a.ng) {
-          const float inv = a.zinv[k];
-          if (inv != 0.f) s = (T)((float)v * inv);
-        }
-        a.jacT[atom * nf + k] = s;
+      forward_keep<T, OW, SW>(a, P, pl, sm);
+      // delta of the (linear) output layer: the unit vector of output jac_out
+      T *dcur = sm + pl.D0, *dnext = sm + pl.D1;
+      for (int r = threadIdx.x; r < a.RC; r += blockDim.x)
+        for (int o = 0; o < nout; o++)
+          dcur[(int64_t)o * a.RCP + r] = (o == a.jac_out) ? (T)1 : (T)0;
+      __syncthreads();
+      for (int l = L - 2; l >= 1; l--) {
+        layer_backward<T, OW, SW>(dcur, n.dims[l + 1], P + n.ct[l], n.dims[l], sm + pl.F[l],
+                                  dnext, a.RC, a.RCP);
+        __syncthreads();
+        T *tmp = dcur;
+        dcur = dnext;
+        dnext = tmp;
       }
+      // input layer: no activation; the result replaces the features of the chunk
+      T *J = sm + pl.A[0];
+      layer_backward<T, OW, SW>(dcur, n.dims[1], P + n.ct[0], n.dims[0], nullptr, J, a.RC,
+                                a.RCP);
+      __syncthreads();
+      const int lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+      for (int r = threadIdx.x >> 5; r < nrows; r += nw)
+        for (int k = lane; k < nf; k += 32) {
+          const T v = J[(int64_t)k * a.RCP + r];
+          const int64_t atom = a.bperm[row0 + r];
+          if (a.jac64) a.jac64[atom * nf + k] = (double)v;
+          if (a.jacT) {
+            T s = v;
+            if (sizeof(T) == 8) {
+              if (a.zsd && k < a.ng) {
+                const double sd = a.zsd[k];
+                if (sd >= 1e-08) s = (T)((double)v / sd);
+              }
+            } else if (a.zinv && k < a.ng) {
+              const float inv = a.zinv[k];
+              if (inv != 0.f) s = (T)((float)v * inv);
+            }
+            a.jacT[atom * nf + k] = s;
+          }
+        }
+      __syncthreads();
     }
-    __syncthreads();
   }
 }
 
 // Forward + backward of a tile; per-tile gradient partials in the gradient layout.
-template <typename T>
-__global__ void __launch_bounds__(kMlpThreads) mlp_backward_kernel(MlpArgs<T> a) {
+template <typename T, int OW, bool SW>
+__global__ void __launch_bounds__(mlp_threads<OW>()) mlp_backward_kernel(MlpArgs<T> a) {
   extern __shared__ __align__(32) unsigned char smem_raw[];
   T *sm = reinterpret_cast<T *>(smem_raw);
-  const int4 tl = a.tiles[blockIdx.x];
   const NetDesc &n = a.net;
   const int L = n.nlayer;
-  const T *P = a.params + (int64_t)tl.x * n.pstride;
-  T *G = a.gpart + (int64_t)blockIdx.x * n.stride;
   const SmemPlan &pl = a.pl;
   const int nout = n.dims[L - 1];
-  for (int c0 = 0; c0 < tl.z; c0 += a.RC) {
-    const int nrows = min(a.RC, tl.z - c0);
-    const int64_t row0 = tl.y + c0;
-    load_features(a, row0, nrows, sm + pl.A[0]);
-    __syncthreads();
-    forward_keep(a, P, pl, sm);
-    // output deltas (linear output layer): scaled loss gradients; zero past the tile's end
-    T *dcur = sm + pl.D0, *dnext = sm + pl.D1;
-    for (int r = threadIdx.x; r < a.RC; r += blockDim.x) {
-      const int64_t atom = r < nrows ? a.bperm[row0 + r] : 0;
-      for (int o = 0; o < nout; o++)
-        dcur[(int64_t)o * a.RCP + r] = r < nrows ? (T)a.delta_out[atom * nout + o] : (T)0;
-    }
-    __syncthreads();
-    for (int l = L - 2; l >= 0; l--) {
-      layer_wgrad<T>(sm + pl.A[l], n.dims[l], dcur, n.dims[l + 1], G + n.cw[l], G + n.cb[l],
-                     a.RC, a.RCP, c0 == 0);
-      if (l >= 1)
-        layer_backward<T>(dcur, n.dims[l + 1], P + n.ct[l], n.dims[l], sm + pl.F[l], dnext,
-                          a.RC, a.RCP);
+  int staged = -1;
+  for (int64_t ti = blockIdx.x; ti < a.ntiles; ti += gridDim.x) {
+    const int4 tl = a.tiles[ti];
+    const T *P = tile_params<T, SW>(a, tl.x, staged, sm);
+    T *G = a.gpart + ti * n.stride;
+    for (int c0 = 0; c0 < tl.z; c0 += a.RC) {
+      const int nrows = min(a.RC, tl.z - c0);
+      const int64_t row0 = tl.y + c0;
+      load_features(a, row0, nrows, sm + pl.A[0]);
       __syncthreads();
-      T *tmp = dcur;
-      dcur = dnext;
-      dnext = tmp;
+      forward_keep<T, OW, SW>(a, P, pl, sm);
+      // output deltas (linear output layer): scaled loss gradients; zero past the tile's end
+      T *dcur = sm + pl.D0, *dnext = sm + pl.D1;
+      for (int r = threadIdx.x; r < a.RC; r += blockDim.x) {
+        const int64_t atom = r < nrows ? a.bperm[row0 + r] : 0;
+        for (int o = 0; o < nout; o++)
+          dcur[(int64_t)o * a.RCP + r] = r < nrows ? (T)a.delta_out[atom * nout + o] : (T)0;
+      }
+      __syncthreads();
+      for (int l = L - 2; l >= 0; l--) {
+        layer_wgrad<T>(sm + pl.A[l], n.dims[l], dcur, n.dims[l + 1], G + n.cw[l], G + n.cb[l],
+                       a.RC, a.RCP, c0 == 0);
+        if (l >= 1)
+          layer_backward<T, OW, SW>(dcur, n.dims[l + 1], P + n.ct[l], n.dims[l], sm + pl.F[l],
+                                    dnext, a.RC, a.RCP);
+        __syncthreads();
+        T *tmp = dcur;
+        dcur = dnext;
+        dnext = tmp;
+      }
     }
   }
 }
@@ -586,35 +646,118 @@ Layouts make_layouts(fnetg_ctx *ctx) {
   return Lo;
 }
 
-// Rows per chunk: the tile's rows, halved until the chunk's buffers leave room for two CTAs
-// per SM (or reach four rows).
-template <typename T> int chunk_rows(const NetDesc &n, int tile_rows, bool keep_all) {
+// Rows per chunk: the tile's rows, halved until the chunk's buffers (and the staged weights)
+// leave room for two CTAs per SM (or reach four rows).
+template <typename T> int chunk_rows(const NetDesc &n, int tile_rows, bool keep_all, bool sw) {
   int RC = pad4(tile_rows);
-  while (RC > 4 && sizeof(T) * smem_plan(n, RC + 4, keep_all).total > 100 * 1024) RC >>= 1;
+  while (RC > 4 && sizeof(T) * smem_plan(n, RC + 4, keep_all, sw).total > 100 * 1024) RC >>= 1;
   return RC;
 }
 
-template <typename T> int prepare(fnetg_ctx *ctx, Layouts &Lo, MlpArgs<T> &a, bool keep_all,
-                                  size_t &smem) {
-  Lo = make_layouts(ctx);
+template <typename T> void prepare(fnetg_ctx *ctx, const Layouts &Lo, MlpArgs<T> &a,
+                                   bool keep_all, bool sw, size_t &smem) {
   a = MlpArgs<T>{};
   a.net = Lo.net;
   a.params = ctx->d_params.as<T>();
   a.feat = ctx->d_feat.as<T>();
   a.nf = ctx->nf;
   a.tiles = ctx->d_tiles.as<int4>();
+  a.ntiles = ctx->ntiles;
   a.bperm = ctx->d_bperm.as<int32_t>();
-  a.RC = chunk_rows<T>(Lo.net, ctx->tile_rows, keep_all);
+  a.RC = chunk_rows<T>(Lo.net, ctx->tile_rows, keep_all, sw);
   a.RCP = a.RC + 4;
-  a.pl = smem_plan(Lo.net, a.RCP, keep_all);
+  a.pl = smem_plan(Lo.net, a.RCP, keep_all, sw);
   smem = sizeof(T) * (size_t)a.pl.total;
+}
+
+// ---- launch variants and their selection ----------------------------------------------
+// Variant v: v & 2 -> 256 threads with 4 x 2 register tiles (else 128 threads, 4 x 4);
+// v & 1 -> weights staged in shared memory.  The first launch of a kind for a network
+// shape times every variant that fits and keeps the fastest for the context.
+enum MlpKind { kMlpForward = 0, kMlpJacobian = 1, kMlpBackward = 2 };
+
+template <typename T, int OW, bool SW> void *mlp_kernel_ptr(int kind) {
+  if (kind == kMlpForward) return (void *)mlp_forward_kernel<T, OW, SW>;
+  if (kind == kMlpJacobian) return (void *)mlp_jacobian_kernel<T, OW, SW>;
+  return (void *)mlp_backward_kernel<T, OW, SW>;
+}
+
+template <typename T> void *mlp_variant(int kind, int v) {
+  switch (v) {
+    case 0: return mlp_kernel_ptr<T, 4, false>(kind);
+    case 1: return mlp_kernel_ptr<T, 4, true>(kind);
+    case 2: return mlp_kernel_ptr<T, 2, false>(kind);
+    default: return mlp_kernel_ptr<T, 2, true>(kind);
+  }
+}
+
+template <typename T>
+int launch_variant(fnetg_ctx *ctx, int kind, int v, const Layouts &Lo, MlpArgs<T> &a) {
+  size_t smem = 0;
+  const MlpArgs<T> keep = a;
+  prepare<T>(ctx, Lo, a, kind != kMlpForward, (v & 1) != 0, smem);
+  // outputs and inputs set by the caller survive the re-preparation
+  a.out = keep.out;
+  a.delta_out = keep.delta_out;
+  a.gpart = keep.gpart;
+  a.jac_out = keep.jac_out;
+  a.zsd = keep.zsd;
+  a.zinv = keep.zinv;
+  a.ng = keep.ng;
+  a.jac64 = keep.jac64;
+  a.jacT = keep.jacT;
   FNETG_CHECK(smem <= 227 * 1024, FNETG_E_UNSUPPORTED, "network too wide for shared memory");
+  void *k = mlp_variant<T>(kind, v);
+  const int threads = (v & 2) ? 256 : 128;
+  FNETG_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  int per_sm = 0;
+  FNETG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, threads, smem));
+  FNETG_CHECK(per_sm > 0, FNETG_E_UNSUPPORTED, "MLP variant does not fit on an SM");
+  const int64_t grid = std::min<int64_t>(ctx->ntiles, (int64_t)num_sms() * per_sm);
+  void *args[] = {&a};
+  FNETG_CUDA(cudaLaunchKernel(k, dim3((unsigned)std::max<int64_t>(grid, 1)), dim3(threads), args,
+                              smem, ctx->stream));
   return FNETG_OK;
 }
 
-template <typename K> int set_smem(fnetg_ctx *ctx, K kernel, size_t bytes) {
-  FNETG_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
-  return FNETG_OK;
+template <typename T> bool variant_fits(fnetg_ctx *ctx, const Layouts &Lo, int kind, int v) {
+  MlpArgs<T> a;
+  size_t smem = 0;
+  prepare<T>(ctx, Lo, a, kind != kMlpForward, (v & 1) != 0, smem);
+  return smem <= 227 * 1024 && a.RC >= 16;
+}
+
+template <typename T>
+int run_mlp(fnetg_ctx *ctx, int kind, const Layouts &Lo, MlpArgs<T> &a, const char *label) {
+  if (ctx->ntiles == 0) return FNETG_OK;
+  const int pi = sizeof(T) == 8 ? 1 : 0;
+  if (ctx->mlp_dims != ctx->dims) {
+    for (auto &c : ctx->mlp_cfg) c = -1;
+    ctx->mlp_dims = ctx->dims;
+  }
+  int &cfg = ctx->mlp_cfg[pi * 3 + kind];
+  if (cfg < 0) {
+    float best = 0.f;
+    for (int v = 0; v < 4; v++) {
+      if (v != 0 && !variant_fits<T>(ctx, Lo, kind, v)) continue;
+      MlpArgs<T> b = a;
+      int rc = launch_variant<T>(ctx, kind, v, Lo, b);  // warm-up
+      if (rc) return rc;
+      FNETG_CUDA(cudaEventRecord(ctx->ev0, ctx->stream));
+      rc = launch_variant<T>(ctx, kind, v, Lo, b);
+      if (rc) return rc;
+      FNETG_CUDA(cudaEventRecord(ctx->ev1, ctx->stream));
+      FNETG_CUDA(cudaEventSynchronize(ctx->ev1));
+      float ms = 0.f;
+      FNETG_CUDA(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
+      if (cfg < 0 || ms < best) {
+        best = ms;
+        cfg = v;
+      }
+    }
+  }
+  LaunchScope ls(ctx, label);
+  return launch_variant<T>(ctx, kind, cfg, Lo, a);
 }
 
 template <typename T> int do_params(fnetg_ctx *ctx) {
@@ -633,29 +776,17 @@ template <typename T> int do_params(fnetg_ctx *ctx) {
 }
 
 template <typename T> int do_predict(fnetg_ctx *ctx) {
-  Layouts Lo;
-  MlpArgs<T> a;
-  size_t sm = 0;
-  int rc = prepare<T>(ctx, Lo, a, false, sm);
-  if (rc) return rc;
+  const Layouts Lo = make_layouts(ctx);
+  MlpArgs<T> a{};
   const int nout = ctx->dims.back();
   FNETG_CUDA(ctx->d_out.ensure(sizeof(double) * std::max<int64_t>(ctx->N, 1) * nout));
   a.out = ctx->d_out.as<double>();
-  if (ctx->ntiles == 0) return FNETG_OK;
-  rc = set_smem(ctx, mlp_forward_kernel<T>, sm);
-  if (rc) return rc;
-  LaunchScope ls(ctx, "mlp_forward");
-  mlp_forward_kernel<T><<<(unsigned)ctx->ntiles, kMlpThreads, sm, ctx->stream>>>(a);
-  FNETG_CUDA(cudaGetLastError());
-  return FNETG_OK;
+  return run_mlp<T>(ctx, kMlpForward, Lo, a, "mlp_forward");
 }
 
 template <typename T> int do_jacobian(fnetg_ctx *ctx, int o, void *dstT) {
-  Layouts Lo;
-  MlpArgs<T> a;
-  size_t sm = 0;
-  int rc = prepare<T>(ctx, Lo, a, true, sm);
-  if (rc) return rc;
+  const Layouts Lo = make_layouts(ctx);
+  MlpArgs<T> a{};
   const int nf = ctx->nf;
   a.jac_out = o;
   a.ng = (int)ctx->gf.size();
@@ -667,34 +798,20 @@ template <typename T> int do_jacobian(fnetg_ctx *ctx, int o, void *dstT) {
     FNETG_CUDA(ctx->d_jac.ensure(sizeof(double) * std::max<int64_t>(ctx->N, 1) * nf));
     a.jac64 = ctx->d_jac.as<double>();
   }
-  if (ctx->ntiles == 0) return FNETG_OK;
-  rc = set_smem(ctx, mlp_jacobian_kernel<T>, sm);
-  if (rc) return rc;
-  LaunchScope ls(ctx, "mlp_jacobian");
-  mlp_jacobian_kernel<T><<<(unsigned)ctx->ntiles, kMlpThreads, sm, ctx->stream>>>(a);
-  FNETG_CUDA(cudaGetLastError());
-  return FNETG_OK;
+  return run_mlp<T>(ctx, kMlpJacobian, Lo, a, "mlp_jacobian");
 }
 
 template <typename T> int do_backward(fnetg_ctx *ctx) {
-  Layouts Lo;
-  MlpArgs<T> a;
-  size_t sm = 0;
-  int rc = prepare<T>(ctx, Lo, a, true, sm);
-  if (rc) return rc;
+  const Layouts Lo = make_layouts(ctx);
+  MlpArgs<T> a{};
   a.delta_out = ctx->d_lossgrad.as<double>();
   FNETG_CUDA(ctx->d_gpart.ensure(sizeof(T) * std::max<int64_t>(ctx->ntiles, 1) * Lo.net.stride));
   a.gpart = ctx->d_gpart.as<T>();
   FNETG_CUDA(ctx->d_grad64.ensure(sizeof(double) * ctx->nsp * ctx->nparams));
   FNETG_CUDA(cudaMemsetAsync(ctx->d_grad64.p, 0, sizeof(double) * ctx->nsp * ctx->nparams,
                              ctx->stream));
-  if (ctx->ntiles > 0) {
-    rc = set_smem(ctx, mlp_backward_kernel<T>, sm);
-    if (rc) return rc;
-    LaunchScope ls(ctx, "mlp_backward");
-    mlp_backward_kernel<T><<<(unsigned)ctx->ntiles, kMlpThreads, sm, ctx->stream>>>(a);
-    FNETG_CUDA(cudaGetLastError());
-  }
+  int rc = run_mlp<T>(ctx, kMlpBackward, Lo, a, "mlp_backward");
+  if (rc) return rc;
   int64_t maxt = 0;
   for (size_t k = 0; k + 1 < ctx->h_sp_tile0.size(); k++)
     maxt = std::max(maxt, ctx->h_sp_tile0[k + 1] - ctx->h_sp_tile0[k]);
