@@ -273,6 +273,9 @@ def run_ours(args):
                                 if prof[f][1] > 0},
         "clocks": clk.summary(),
     }
+    if args.serve_requests > 0 and rank == 0:
+        ctx.close()
+        out["serving"] = serving_leg(args)
     if not args.no_cpu_baseline and rank == 0 and world == 1:
         out["cpu_baseline"] = cpu_baseline(args, sample_structs=args.cpu_sample, threads=1)
     if rank == 0:
@@ -280,6 +283,98 @@ def run_ours(args):
     if dist:
         dist.barrier()
         dist.destroy_process_group()
+
+
+def serving_leg(args):
+    """The C5 serving stream through the public service API (include/fnetg_serve.h): Poisson
+    arrivals at 2,000 req/s, each request one three-species periodic structure of 16-4,096
+    atoms (log-uniform) drawn from a pool of distinct structures, energies + forces of the C4
+    model (66-64-64-1, FP32).  Latency = completion - scheduled arrival, so a late submission
+    counts against the service."""
+    from fortnet_gb300 import api, synthetic
+
+    cfg = synthetic.CONFIGS["C5"]
+    pool = synthetic.generate(cfg, nstruct=args.serve_pool, targets=False)
+    funcs = synthetic.gfunctions(cfg)
+    dims = synthetic.network_dims(cfg)
+    # the reference's normalXavier draw scaled by 0.1: unscaled, its tanh units saturate on
+    # z-scored ACSF inputs (most atoms give the same output), unlike a trained network's
+    params = 0.1 * api.Rng(cfg.seed).init_params(dims, len(cfg.atomic_numbers))
+    with api.Context(api.FP64) as c:
+        c.upload(pool)
+        c.set_species(pool.species)
+        c.set_gfunctions(funcs)
+        c.acsf(download=False)
+        zprec = c.zscore(weights=pool.weights)
+    reqs = []
+    for s in range(pool.nstruct):
+        a, b = pool.atom_offsets[s], pool.atom_offsets[s + 1]
+        reqs.append((np.ascontiguousarray(pool.atnum[a:b], dtype=np.int32),
+                     np.ascontiguousarray(pool.coords[a:b]), np.ascontiguousarray(pool.latvecs[s])))
+    warm, n = args.serve_warmup, args.serve_requests
+    arr = synthetic.arrivals(warm + n, seed=cfg.seed)
+    pick = np.random.default_rng(cfg.seed + 11).integers(0, len(reqs), size=warm + n)
+    import queue as _queue
+
+    sys.setswitchinterval(0.0002)  # the submitter spins before each arrival
+    pending = _queue.Queue()
+    lat = np.zeros(warm + n)
+    done_ns = np.zeros(warm + n, dtype=np.int64)
+    with api.Server(cfg.atomic_numbers, funcs, zprec, dims, "tanh", params, precision=api.FP32,
+                    lanes=args.serve_lanes) as srv:
+        def waiter():
+            for _ in range(warm + n):
+                k, t, na = pending.get()
+                _, _, lat[k] = srv.wait(t, na, timeout=120.0)
+                done_ns[k] = srv.clock_ns()
+
+        th = threading.Thread(target=waiter)
+        th.start()
+        t0 = srv.clock_ns() + 50_000_000
+        for k in range(warm + n):
+            target = t0 + int(arr[k] * 1e9)
+            while True:
+                dt = target - srv.clock_ns()
+                if dt <= 0:
+                    break
+                if dt > 300_000:
+                    time.sleep((dt - 200_000) / 1e9)
+            an, xyz, lv = reqs[pick[k]]
+            t, na = srv.submit(an, xyz, lv, arrival_ns=target)
+            pending.put((k, t, na))
+        th.join()
+        st = srv.stats()
+    # FP32 service against an FP64 run of the same kernels on the first pool structures
+    chk = list(range(min(16, len(reqs))))
+    res = {}
+    for prec in (api.FP32, api.FP64):
+        with api.Server(cfg.atomic_numbers, funcs, zprec, dims, "tanh", params, precision=prec,
+                        lanes=1) as s2:
+            ts = [s2.submit(*reqs[k]) for k in chk]
+            res[prec] = [s2.wait(t, na, timeout=120.0) for t, na in ts]
+    e_err = max(abs(a[0][0] - b[0][0]) / abs(b[0][0]) for a, b in zip(res[api.FP32], res[api.FP64]))
+    f_err = max(float(np.max(np.abs(a[1] - b[1])) / np.max(np.abs(b[1])))
+                for a, b in zip(res[api.FP32], res[api.FP64]))
+    meas = lat[warm:]
+    atoms = int(sum(len(reqs[pick[k]][0]) for k in range(warm, warm + n)))
+    span = (done_ns[warm:].max() - (t0 + int(arr[warm] * 1e9))) / 1e9
+    return {
+        "workload": f"C5: Poisson {synthetic.C5_RATE:.0f} req/s, 16-4096 atoms log-uniform "
+                    f"(pool of {pool.nstruct} structures), model 66-64-64-1 tanh, energies + forces",
+        "requests": n, "warmup_requests": warm, "dtype": "f32",
+        "p50_ms": round(float(np.percentile(meas, 50)), 3),
+        "p99_ms": round(float(np.percentile(meas, 99)), 3),
+        "mean_ms": round(float(np.mean(meas)), 3), "max_ms": round(float(np.max(meas)), 3),
+        "atoms_per_s": round(atoms / span, 1),
+        "offered_atoms_per_s": round(atoms / (arr[-1] - arr[warm]), 1),
+        "lanes": st["lanes"], "batches": st["batches"],
+        "mean_batch_requests": round(st["requests"] / max(st["batches"], 1), 2),
+        "max_batch_requests": st["max_batch_requests"], "max_in_flight": st["max_in_flight"],
+        "device_bytes": st["device_bytes"],
+        "fp32_vs_fp64": {"structures": len(chk), "energy_rel": float(f"{e_err:.3g}"),
+                         "force_rel_of_max": float(f"{f_err:.3g}")},
+        "model_weights": "normalXavier (RANLUX, seed 1005) x 0.1",
+    }
 
 
 def cpu_step(ds, funcs, dims, params, zprec, nthreads):
@@ -372,6 +467,11 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=4)
     ap.add_argument("--ref-sample", type=int, default=32)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--serve-requests", type=int, default=20000,
+                    help="requests of the C5 serving stream (0: skip the serving leg)")
+    ap.add_argument("--serve-warmup", type=int, default=1000)
+    ap.add_argument("--serve-pool", type=int, default=64)
+    ap.add_argument("--serve-lanes", type=int, default=3)
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

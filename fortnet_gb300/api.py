@@ -97,6 +97,14 @@ def load(build_if_missing=True):
         "fnetg_profile_reset": (C.c_int, [vp]),
         "fnetg_launch_count": (i64, [vp]),
         "fnetg_synchronize": (C.c_int, [vp]),
+        "fnetg_server_create": (C.c_int, [C.POINTER(vp), vp, i32, vp, i32, vp, vp, i32, vp, i32,
+                                          vp]),
+        "fnetg_server_destroy": (C.c_int, [vp]),
+        "fnetg_server_last_error": (C.c_char_p, [vp]),
+        "fnetg_server_clock_ns": (i64, []),
+        "fnetg_server_submit": (C.c_int, [vp, i32, vp, vp, i32, vp, i64, C.POINTER(i64)]),
+        "fnetg_server_wait": (C.c_int, [vp, i64, dbl, vp, vp, C.POINTER(dbl)]),
+        "fnetg_server_stats_get": (C.c_int, [vp, vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -376,3 +384,93 @@ class Rng:
         if getattr(self, "h", None) and _lib is not None:
             _lib.fnetg_rng_destroy(self.h)
             self.h = None
+
+
+class _ServerConfig(C.Structure):
+    _fields_ = [("precision", C.c_int32), ("device", C.c_int32), ("lanes", C.c_int32),
+                ("pad", C.c_int32), ("max_batch_atoms", C.c_int64),
+                ("hbm_budget_bytes", C.c_int64)]
+
+
+class _ServerStats(C.Structure):
+    _fields_ = [("requests", C.c_int64), ("batches", C.c_int64), ("atoms", C.c_int64),
+                ("max_batch_atoms", C.c_int64), ("max_batch_requests", C.c_int64),
+                ("device_bytes", C.c_int64), ("batch_cap_atoms", C.c_int64),
+                ("lanes", C.c_int32), ("max_in_flight", C.c_int32), ("busy_s", C.c_double)]
+
+
+class Server:
+    """Energy/force prediction service (include/fnetg_serve.h): requests queued from any
+    thread, served by continuous batching over ``lanes`` concurrent device batches."""
+
+    def __init__(self, atomic_numbers, funcs, zprec, dims, activation, params, precision=FP32,
+                 device=0, lanes=0, max_batch_atoms=0, hbm_budget_bytes=0):
+        self.lib = load()
+        cfg = _ServerConfig(int(precision), int(device), int(lanes), 0, int(max_batch_atoms),
+                            int(hbm_budget_bytes))
+        g = pack(funcs) if not isinstance(funcs, np.ndarray) else funcs
+        self.ng = len(g)
+        self.dims = [int(d) for d in dims]
+        self.nout = self.dims[-1]
+        zn = _c(np.asarray(atomic_numbers), np.int32)
+        zp = _c(zprec, np.float64)
+        dm = _c(self.dims, np.int32)
+        pr = _c(params, np.float64)
+        h = C.c_void_p()
+        act = ACT[activation] if isinstance(activation, str) else int(activation)
+        rc = self.lib.fnetg_server_create(C.byref(h), C.byref(cfg), len(zn), _p(zn), self.ng,
+                                          g.ctypes.data_as(C.c_void_p), _p(zp), len(dm), _p(dm),
+                                          act, _p(pr))
+        if rc != 0:
+            raise FnetgError(rc, "fnetg_server_create failed")
+        self.h = h
+
+    def _check(self, rc):
+        if rc != 0:
+            msg = self.lib.fnetg_server_last_error(self.h)
+            raise FnetgError(rc, msg.decode() if msg else "")
+
+    def clock_ns(self):
+        return int(self.lib.fnetg_server_clock_ns())
+
+    def submit(self, atnum, coords, latvecs=None, arrival_ns=0):
+        """Queue one structure (coordinates in Bohr, [n, 3]); returns its ticket."""
+        an = _c(atnum, np.int32)
+        xyz = _c(coords, np.float64)
+        lat = None if latvecs is None else _c(latvecs, np.float64)
+        t = C.c_int64()
+        self._check(self.lib.fnetg_server_submit(self.h, len(an), _p(an), _p(xyz),
+                                                 0 if lat is None else 1, _p(lat),
+                                                 int(arrival_ns), C.byref(t)))
+        return t.value, len(an)
+
+    def wait(self, ticket, natoms, timeout=-1.0, forces=True):
+        """(energy[nout], forces[natoms, nout, 3] or None, latency in ms)."""
+        e = np.zeros(self.nout)
+        f = np.zeros((natoms, self.nout, 3)) if forces else None
+        lat = C.c_double()
+        self._check(self.lib.fnetg_server_wait(self.h, int(ticket), float(timeout), _p(e),
+                                               _p(f), C.byref(lat)))
+        return e, f, lat.value
+
+    def stats(self):
+        st = _ServerStats()
+        self._check(self.lib.fnetg_server_stats_get(self.h, C.byref(st)))
+        return {k: getattr(st, k) for k, _ in st._fields_}
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.fnetg_server_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()

@@ -17,7 +17,7 @@ CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libfnetg.so")
 SOURCES = ["context.cu", "neighbors.cu", "acsf.cu", "mlp.cu", "forces.cu", "train.cu", "rng.cu",
-           "noalloc.cu", "fd.cu"]
+           "noalloc.cu", "fd.cu", "serve.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

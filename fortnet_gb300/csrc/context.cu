@@ -4,6 +4,8 @@
 #include <array>
 #include <set>
 
+#include <mutex>
+
 #include "internal.cuh"
 
 using namespace fnetg;
@@ -23,14 +25,27 @@ int cuda_fail(fnetg_ctx *c, cudaError_t e, const char *where) {
 }
 
 int num_sms() {
-  static int n = 0;
-  if (!n) {
-    int dev = 0;
+  static const int n = [] {
+    int dev = 0, v = 0;
     cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
-    if (n <= 0) n = 1;
-  }
+    cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
+    return v > 0 ? v : 1;
+  }();
   return n;
+}
+
+cudaError_t raise_smem_limit(const void *kernel, size_t bytes) {
+  static std::mutex mu;
+  static std::map<std::pair<int, const void *>, size_t> limit;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  std::lock_guard<std::mutex> lk(mu);
+  size_t &cur = limit[{dev, kernel}];
+  if (bytes <= cur) return cudaSuccess;
+  e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  if (e == cudaSuccess) cur = bytes;
+  return e;
 }
 
 static cudaEvent_t pool_event(fnetg_ctx *c) {
@@ -227,7 +242,7 @@ static int refresh_codes(fnetg_ctx *ctx) {
       if (ctx->h_atnum[a] == ctx->zcodes[z]) code[a] = (int8_t)z;
   FNETG_CUDA(ctx->d_code.ensure(std::max<int64_t>(ctx->N, 1)));
   if (ctx->N > 0)
-    FNETG_CUDA(cudaMemcpy(ctx->d_code.p, code.data(), ctx->N, cudaMemcpyHostToDevice));
+    FNETG_CUDA(copy_sync(ctx, ctx->d_code.p, code.data(), ctx->N, cudaMemcpyHostToDevice));
   return FNETG_OK;
 }
 
@@ -387,21 +402,21 @@ static int rebuild_buckets(fnetg_ctx *ctx, bool order_changes) {
   for (int s = 0; s < nsp; s++) t0[s + 1] += t0[s];
   ctx->h_sp_tile0 = t0;
   FNETG_CUDA(ctx->d_sp_tile0.ensure(sizeof(int64_t) * (nsp + 1)));
-  FNETG_CUDA(cudaMemcpy(ctx->d_sp_tile0.p, t0.data(), sizeof(int64_t) * (nsp + 1),
+  FNETG_CUDA(copy_sync(ctx, ctx->d_sp_tile0.p, t0.data(), sizeof(int64_t) * (nsp + 1),
                         cudaMemcpyHostToDevice));
   FNETG_CUDA(ctx->d_species.ensure(sizeof(int32_t) * std::max<int64_t>(N, 1)));
   FNETG_CUDA(ctx->d_bpos.ensure(sizeof(int32_t) * std::max<int64_t>(N, 1)));
   FNETG_CUDA(ctx->d_bperm.ensure(sizeof(int32_t) * std::max<int64_t>(N, 1)));
   FNETG_CUDA(ctx->d_tiles.ensure(sizeof(int32_t) * std::max<size_t>(tiles.size(), 4)));
   if (N > 0) {
-    FNETG_CUDA(cudaMemcpy(ctx->d_species.p, ctx->h_species.data(), sizeof(int32_t) * N,
+    FNETG_CUDA(copy_sync(ctx, ctx->d_species.p, ctx->h_species.data(), sizeof(int32_t) * N,
                           cudaMemcpyHostToDevice));
-    FNETG_CUDA(cudaMemcpy(ctx->d_bpos.p, bpos.data(), sizeof(int32_t) * N, cudaMemcpyHostToDevice));
-    FNETG_CUDA(cudaMemcpy(ctx->d_bperm.p, bperm.data(), sizeof(int32_t) * N,
+    FNETG_CUDA(copy_sync(ctx, ctx->d_bpos.p, bpos.data(), sizeof(int32_t) * N, cudaMemcpyHostToDevice));
+    FNETG_CUDA(copy_sync(ctx, ctx->d_bperm.p, bperm.data(), sizeof(int32_t) * N,
                           cudaMemcpyHostToDevice));
   }
   if (!tiles.empty())
-    FNETG_CUDA(cudaMemcpy(ctx->d_tiles.p, tiles.data(), sizeof(int32_t) * tiles.size(),
+    FNETG_CUDA(copy_sync(ctx, ctx->d_tiles.p, tiles.data(), sizeof(int32_t) * tiles.size(),
                           cudaMemcpyHostToDevice));
   if (order_changes) ctx->feats_valid = false;
   return FNETG_OK;
@@ -616,15 +631,15 @@ int fnetg_set_gfunctions(fnetg_ctx *ctx, int32_t ng, const fnetg_gfunc *g) {
                  ctx->h_mpc.begin() + (size_t)(f + 1) * (kMaxMomentDegree + 1));
     ctx->h_mpc = epc;
     FNETG_CUDA(ctx->d_qgroups.ensure(sizeof(int32_t) * std::max<size_t>(pack.size(), 1)));
-    FNETG_CUDA(cudaMemcpy(ctx->d_qgroups.p, pack.data(), sizeof(int32_t) * pack.size(),
+    FNETG_CUDA(copy_sync(ctx, ctx->d_qgroups.p, pack.data(), sizeof(int32_t) * pack.size(),
                           cudaMemcpyHostToDevice));
     std::vector<float> pcf(ctx->h_mpc.begin(), ctx->h_mpc.end());
     FNETG_CUDA(ctx->d_mpc_d.ensure(sizeof(double) * std::max<size_t>(ctx->h_mpc.size(), 1)));
     FNETG_CUDA(ctx->d_mpc_f.ensure(sizeof(float) * std::max<size_t>(pcf.size(), 1)));
     if (!pcf.empty()) {
-      FNETG_CUDA(cudaMemcpy(ctx->d_mpc_d.p, ctx->h_mpc.data(), sizeof(double) * ctx->h_mpc.size(),
+      FNETG_CUDA(copy_sync(ctx, ctx->d_mpc_d.p, ctx->h_mpc.data(), sizeof(double) * ctx->h_mpc.size(),
                             cudaMemcpyHostToDevice));
-      FNETG_CUDA(cudaMemcpy(ctx->d_mpc_f.p, pcf.data(), sizeof(float) * pcf.size(),
+      FNETG_CUDA(copy_sync(ctx, ctx->d_mpc_f.p, pcf.data(), sizeof(float) * pcf.size(),
                             cudaMemcpyHostToDevice));
     }
   }
@@ -647,16 +662,16 @@ int fnetg_set_gfunctions(fnetg_ctx *ctx, int32_t ng, const fnetg_gfunc *g) {
   qoff[ctx->n_combo] = (int32_t)qent.size() / 2;
   FNETG_CUDA(ctx->d_qoff.ensure(sizeof(int32_t) * (ctx->n_combo + 1)));
   FNETG_CUDA(ctx->d_qent.ensure(sizeof(int32_t) * std::max<size_t>(qent.size(), 2)));
-  FNETG_CUDA(cudaMemcpy(ctx->d_qoff.p, qoff.data(), sizeof(int32_t) * qoff.size(),
+  FNETG_CUDA(copy_sync(ctx, ctx->d_qoff.p, qoff.data(), sizeof(int32_t) * qoff.size(),
                         cudaMemcpyHostToDevice));
   if (!qent.empty())
-    FNETG_CUDA(cudaMemcpy(ctx->d_qent.p, qent.data(), sizeof(int32_t) * qent.size(),
+    FNETG_CUDA(copy_sync(ctx, ctx->d_qent.p, qent.data(), sizeof(int32_t) * qent.size(),
                           cudaMemcpyHostToDevice));
   {
     std::vector<float> cf(ctx->h_mcoef.begin(), ctx->h_mcoef.end());
     FNETG_CUDA(ctx->d_mcoef_f.ensure(sizeof(float) * std::max<size_t>(cf.size(), 1)));
     if (!cf.empty())
-      FNETG_CUDA(cudaMemcpy(ctx->d_mcoef_f.p, cf.data(), sizeof(float) * cf.size(),
+      FNETG_CUDA(copy_sync(ctx, ctx->d_mcoef_f.p, cf.data(), sizeof(float) * cf.size(),
                             cudaMemcpyHostToDevice));
   }
   FNETG_CUDA(ctx->d_mfunc.ensure(sizeof(MFunc) * std::max<size_t>(ctx->h_mfunc.size(), 1)));
@@ -664,14 +679,14 @@ int fnetg_set_gfunctions(fnetg_ctx *ctx, int32_t ng, const fnetg_gfunc *g) {
   FNETG_CUDA(ctx->d_combo.ensure(sizeof(int32_t) * std::max<size_t>(ctx->h_combo.size(), 2)));
   FNETG_CUDA(ctx->d_cidx.ensure(sizeof(int32_t) * std::max<size_t>(ctx->h_cidx.size(), 1)));
   if (!ctx->h_mfunc.empty()) {
-    FNETG_CUDA(cudaMemcpy(ctx->d_mfunc.p, ctx->h_mfunc.data(), sizeof(MFunc) * ctx->h_mfunc.size(),
+    FNETG_CUDA(copy_sync(ctx, ctx->d_mfunc.p, ctx->h_mfunc.data(), sizeof(MFunc) * ctx->h_mfunc.size(),
                           cudaMemcpyHostToDevice));
-    FNETG_CUDA(cudaMemcpy(ctx->d_mcoef.p, ctx->h_mcoef.data(),
+    FNETG_CUDA(copy_sync(ctx, ctx->d_mcoef.p, ctx->h_mcoef.data(),
                           sizeof(double) * ctx->h_mcoef.size(), cudaMemcpyHostToDevice));
-    FNETG_CUDA(cudaMemcpy(ctx->d_combo.p, ctx->h_combo.data(),
+    FNETG_CUDA(copy_sync(ctx, ctx->d_combo.p, ctx->h_combo.data(),
                           sizeof(int32_t) * ctx->h_combo.size(), cudaMemcpyHostToDevice));
   }
-  FNETG_CUDA(cudaMemcpy(ctx->d_cidx.p, ctx->h_cidx.data(), sizeof(int32_t) * ctx->h_cidx.size(),
+  FNETG_CUDA(copy_sync(ctx, ctx->d_cidx.p, ctx->h_cidx.data(), sizeof(int32_t) * ctx->h_cidx.size(),
                         cudaMemcpyHostToDevice));
   // group the remaining angular functions by list channels, cutoff and atom-id column
   // (stable), at most kMaxGroupFuncs per group
@@ -709,24 +724,24 @@ int fnetg_set_gfunctions(fnetg_ctx *ctx, int32_t ng, const fnetg_gfunc *g) {
   FNETG_CUDA(ctx->d_ecls_atomid.ensure(sizeof(int) * kMaxEtaClasses));
   FNETG_CUDA(ctx->d_rcls.ensure(sizeof(double) * kMaxRcutClasses));
   if (!ctx->h_rad.empty())
-    FNETG_CUDA(cudaMemcpy(ctx->d_rad.p, ctx->h_rad.data(), sizeof(GDesc) * ctx->h_rad.size(),
+    FNETG_CUDA(copy_sync(ctx, ctx->d_rad.p, ctx->h_rad.data(), sizeof(GDesc) * ctx->h_rad.size(),
                           cudaMemcpyHostToDevice));
   if (!ctx->h_ang.empty())
-    FNETG_CUDA(cudaMemcpy(ctx->d_ang.p, ctx->h_ang.data(), sizeof(GDesc) * ctx->h_ang.size(),
+    FNETG_CUDA(copy_sync(ctx, ctx->d_ang.p, ctx->h_ang.data(), sizeof(GDesc) * ctx->h_ang.size(),
                           cudaMemcpyHostToDevice));
   if (!ctx->h_groups.empty())
-    FNETG_CUDA(cudaMemcpy(ctx->d_groups.p, ctx->h_groups.data(),
+    FNETG_CUDA(copy_sync(ctx, ctx->d_groups.p, ctx->h_groups.data(),
                           sizeof(AGroup) * ctx->h_groups.size(), cudaMemcpyHostToDevice));
   if (!ctx->ecls_eta.empty()) {
-    FNETG_CUDA(cudaMemcpy(ctx->d_ecls_eta.p, ctx->ecls_eta.data(),
+    FNETG_CUDA(copy_sync(ctx, ctx->d_ecls_eta.p, ctx->ecls_eta.data(),
                           sizeof(double) * ctx->ecls_eta.size(), cudaMemcpyHostToDevice));
-    FNETG_CUDA(cudaMemcpy(ctx->d_ecls_rclass.p, ctx->ecls_rclass.data(),
+    FNETG_CUDA(copy_sync(ctx, ctx->d_ecls_rclass.p, ctx->ecls_rclass.data(),
                           sizeof(int) * ctx->ecls_rclass.size(), cudaMemcpyHostToDevice));
-    FNETG_CUDA(cudaMemcpy(ctx->d_ecls_atomid.p, ctx->ecls_atomid.data(),
+    FNETG_CUDA(copy_sync(ctx, ctx->d_ecls_atomid.p, ctx->ecls_atomid.data(),
                           sizeof(int) * ctx->ecls_atomid.size(), cudaMemcpyHostToDevice));
   }
   if (!ctx->rcut_classes.empty())
-    FNETG_CUDA(cudaMemcpy(ctx->d_rcls.p, ctx->rcut_classes.data(),
+    FNETG_CUDA(copy_sync(ctx, ctx->d_rcls.p, ctx->rcut_classes.data(),
                           sizeof(double) * ctx->rcut_classes.size(), cudaMemcpyHostToDevice));
   {
     auto params = [](const std::vector<GDesc> &v, std::vector<double> &pd, std::vector<float> &pf) {
@@ -743,20 +758,20 @@ int fnetg_set_gfunctions(fnetg_ctx *ctx, int32_t ng, const fnetg_gfunc *g) {
     params(ctx->h_rad, pd, pf);
     FNETG_CUDA(ctx->d_radpar_d.ensure(sizeof(double) * pd.size()));
     FNETG_CUDA(ctx->d_radpar_f.ensure(sizeof(float) * pf.size()));
-    FNETG_CUDA(cudaMemcpy(ctx->d_radpar_d.p, pd.data(), sizeof(double) * pd.size(), cudaMemcpyHostToDevice));
-    FNETG_CUDA(cudaMemcpy(ctx->d_radpar_f.p, pf.data(), sizeof(float) * pf.size(), cudaMemcpyHostToDevice));
+    FNETG_CUDA(copy_sync(ctx, ctx->d_radpar_d.p, pd.data(), sizeof(double) * pd.size(), cudaMemcpyHostToDevice));
+    FNETG_CUDA(copy_sync(ctx, ctx->d_radpar_f.p, pf.data(), sizeof(float) * pf.size(), cudaMemcpyHostToDevice));
     params(ctx->h_ang, pd, pf);
     FNETG_CUDA(ctx->d_angpar_d.ensure(sizeof(double) * pd.size()));
     FNETG_CUDA(ctx->d_angpar_f.ensure(sizeof(float) * pf.size()));
-    FNETG_CUDA(cudaMemcpy(ctx->d_angpar_d.p, pd.data(), sizeof(double) * pd.size(), cudaMemcpyHostToDevice));
-    FNETG_CUDA(cudaMemcpy(ctx->d_angpar_f.p, pf.data(), sizeof(float) * pf.size(), cudaMemcpyHostToDevice));
+    FNETG_CUDA(copy_sync(ctx, ctx->d_angpar_d.p, pd.data(), sizeof(double) * pd.size(), cudaMemcpyHostToDevice));
+    FNETG_CUDA(copy_sync(ctx, ctx->d_angpar_f.p, pf.data(), sizeof(float) * pf.size(), cudaMemcpyHostToDevice));
     std::vector<float> ef(kMaxEtaClasses, 0.f), rf(kMaxRcutClasses, 0.f);
     for (size_t q = 0; q < ctx->ecls_eta.size(); q++) ef[q] = (float)ctx->ecls_eta[q];
     for (size_t q = 0; q < ctx->rcut_classes.size(); q++) rf[q] = (float)ctx->rcut_classes[q];
     FNETG_CUDA(ctx->d_ecls_eta_f.ensure(sizeof(float) * kMaxEtaClasses));
     FNETG_CUDA(ctx->d_rcls_f.ensure(sizeof(float) * kMaxRcutClasses));
-    FNETG_CUDA(cudaMemcpy(ctx->d_ecls_eta_f.p, ef.data(), sizeof(float) * kMaxEtaClasses, cudaMemcpyHostToDevice));
-    FNETG_CUDA(cudaMemcpy(ctx->d_rcls_f.p, rf.data(), sizeof(float) * kMaxRcutClasses, cudaMemcpyHostToDevice));
+    FNETG_CUDA(copy_sync(ctx, ctx->d_ecls_eta_f.p, ef.data(), sizeof(float) * kMaxEtaClasses, cudaMemcpyHostToDevice));
+    FNETG_CUDA(copy_sync(ctx, ctx->d_rcls_f.p, rf.data(), sizeof(float) * kMaxRcutClasses, cudaMemcpyHostToDevice));
   }
   ctx->nb_valid = false;
   ctx->feats_valid = false;
@@ -788,8 +803,8 @@ int fnetg_get_neighbors(fnetg_ctx *ctx, int64_t *pair_offsets, int32_t *j, int32
   // device [begin, end) of every atom -> compact offsets
   std::vector<int64_t> beg(std::max<int64_t>(N, 1)), end(std::max<int64_t>(N, 1)), off(N + 1, 0);
   if (N > 0) {
-    FNETG_CUDA(cudaMemcpy(beg.data(), ctx->d_poff.p, sizeof(int64_t) * N, cudaMemcpyDeviceToHost));
-    FNETG_CUDA(cudaMemcpy(end.data(), fnetg::pair_end(ctx), sizeof(int64_t) * N,
+    FNETG_CUDA(copy_sync(ctx, beg.data(), ctx->d_poff.p, sizeof(int64_t) * N, cudaMemcpyDeviceToHost));
+    FNETG_CUDA(copy_sync(ctx, end.data(), fnetg::pair_end(ctx), sizeof(int64_t) * N,
                           cudaMemcpyDeviceToHost));
   }
   for (int64_t a = 0; a < N; a++) off[a + 1] = off[a] + (end[a] - beg[a]);
@@ -801,7 +816,7 @@ int fnetg_get_neighbors(fnetg_ctx *ctx, int64_t *pair_offsets, int32_t *j, int32
   };
   if (j && P > 0) {
     std::vector<int32_t> all(slots);
-    FNETG_CUDA(cudaMemcpy(all.data(), ctx->d_pj.p, sizeof(int32_t) * slots, cudaMemcpyDeviceToHost));
+    FNETG_CUDA(copy_sync(ctx, all.data(), ctx->d_pj.p, sizeof(int32_t) * slots, cudaMemcpyDeviceToHost));
     compact(all.data(), j);
     // convert to structure-local indices
     for (int s = 0; s < ctx->S; s++)
@@ -810,7 +825,7 @@ int fnetg_get_neighbors(fnetg_ctx *ctx, int64_t *pair_offsets, int32_t *j, int32
   }
   if (shift && P > 0) {
     std::vector<uint32_t> all(slots), meta(P);
-    FNETG_CUDA(cudaMemcpy(all.data(), ctx->d_pmeta.p, sizeof(uint32_t) * slots,
+    FNETG_CUDA(copy_sync(ctx, all.data(), ctx->d_pmeta.p, sizeof(uint32_t) * slots,
                           cudaMemcpyDeviceToHost));
     compact(all.data(), meta.data());
     for (int64_t q = 0; q < P; q++)
@@ -821,7 +836,7 @@ int fnetg_get_neighbors(fnetg_ctx *ctx, int64_t *pair_offsets, int32_t *j, int32
     if (rc) return rc;
     FNETG_CUDA(cudaStreamSynchronize(ctx->stream));
     std::vector<double> all(slots);
-    FNETG_CUDA(cudaMemcpy(all.data(), ctx->d_d2.p, sizeof(double) * slots, cudaMemcpyDeviceToHost));
+    FNETG_CUDA(copy_sync(ctx, all.data(), ctx->d_d2.p, sizeof(double) * slots, cudaMemcpyDeviceToHost));
     compact(all.data(), d2);
   }
   return FNETG_OK;
@@ -884,18 +899,18 @@ int fnetg_get_features(fnetg_ctx *ctx, double *feats, int32_t *nf_out) {
   const int64_t N = ctx->N;
   std::vector<int32_t> bpos(N);
   if (N > 0)
-    FNETG_CUDA(cudaMemcpy(bpos.data(), ctx->d_bpos.p, sizeof(int32_t) * N, cudaMemcpyDeviceToHost));
+    FNETG_CUDA(copy_sync(ctx, bpos.data(), ctx->d_bpos.p, sizeof(int32_t) * N, cudaMemcpyDeviceToHost));
   if (ctx->prec == FNETG_FP64) {
     std::vector<double> buf((size_t)N * nf);
     if (N > 0)
-      FNETG_CUDA(cudaMemcpy(buf.data(), ctx->d_feat.p, sizeof(double) * buf.size(),
+      FNETG_CUDA(copy_sync(ctx, buf.data(), ctx->d_feat.p, sizeof(double) * buf.size(),
                             cudaMemcpyDeviceToHost));
     for (int64_t a = 0; a < N; a++)
       for (int k = 0; k < nf; k++) feats[a * nf + k] = buf[(size_t)bpos[a] * nf + k];
   } else {
     std::vector<float> buf((size_t)N * nf);
     if (N > 0)
-      FNETG_CUDA(cudaMemcpy(buf.data(), ctx->d_feat.p, sizeof(float) * buf.size(),
+      FNETG_CUDA(copy_sync(ctx, buf.data(), ctx->d_feat.p, sizeof(float) * buf.size(),
                             cudaMemcpyDeviceToHost));
     for (int64_t a = 0; a < N; a++)
       for (int k = 0; k < nf; k++) feats[a * nf + k] = buf[(size_t)bpos[a] * nf + k];
@@ -908,7 +923,7 @@ int fnetg_set_features(fnetg_ctx *ctx, int32_t nf, const double *feats) {
   const int64_t N = ctx->N;
   std::vector<int32_t> bpos(std::max<int64_t>(N, 1));
   if (N > 0)
-    FNETG_CUDA(cudaMemcpy(bpos.data(), ctx->d_bpos.p, sizeof(int32_t) * N, cudaMemcpyDeviceToHost));
+    FNETG_CUDA(copy_sync(ctx, bpos.data(), ctx->d_bpos.p, sizeof(int32_t) * N, cudaMemcpyDeviceToHost));
   const size_t es = ctx->prec == FNETG_FP64 ? 8 : 4;
   FNETG_CUDA(ctx->d_feat.ensure(es * std::max<int64_t>(N, 1) * nf));
   if (ctx->prec == FNETG_FP64) {
@@ -916,13 +931,13 @@ int fnetg_set_features(fnetg_ctx *ctx, int32_t nf, const double *feats) {
     for (int64_t a = 0; a < N; a++)
       for (int k = 0; k < nf; k++) buf[(size_t)bpos[a] * nf + k] = feats[a * nf + k];
     if (N > 0)
-      FNETG_CUDA(cudaMemcpy(ctx->d_feat.p, buf.data(), 8 * buf.size(), cudaMemcpyHostToDevice));
+      FNETG_CUDA(copy_sync(ctx, ctx->d_feat.p, buf.data(), 8 * buf.size(), cudaMemcpyHostToDevice));
   } else {
     std::vector<float> buf((size_t)N * nf);
     for (int64_t a = 0; a < N; a++)
       for (int k = 0; k < nf; k++) buf[(size_t)bpos[a] * nf + k] = (float)feats[a * nf + k];
     if (N > 0)
-      FNETG_CUDA(cudaMemcpy(ctx->d_feat.p, buf.data(), 4 * buf.size(), cudaMemcpyHostToDevice));
+      FNETG_CUDA(copy_sync(ctx, ctx->d_feat.p, buf.data(), 4 * buf.size(), cudaMemcpyHostToDevice));
   }
   ctx->nf = nf;
   ctx->feats_valid = true;
@@ -973,7 +988,7 @@ int fnetg_set_network(fnetg_ctx *ctx, int32_t nspecies, int32_t nlayer, const in
     FNETG_CHECK(std::isfinite(params[q]), FNETG_E_INVALID, "non-finite network parameter");
   FNETG_CUDA(ctx->d_params64.ensure(sizeof(double) * n));
   FNETG_CUDA(ctx->d_params.ensure((ctx->prec == FNETG_FP64 ? 8 : 4) * n));
-  FNETG_CUDA(cudaMemcpy(ctx->d_params64.p, params, sizeof(double) * n, cudaMemcpyHostToDevice));
+  FNETG_CUDA(copy_sync(ctx, ctx->d_params64.p, params, sizeof(double) * n, cudaMemcpyHostToDevice));
   ctx->net_set = true;
   ctx->opt_set = false;
   // the bucket order depends on the species only: features stay valid
@@ -986,7 +1001,7 @@ int fnetg_get_params(fnetg_ctx *ctx, double *params) {
   if (!ctx || !params) return FNETG_E_INVALID;
   FNETG_CHECK(ctx->net_set, FNETG_E_INVALID, "get_params: no network");
   FNETG_CUDA(cudaStreamSynchronize(ctx->stream));
-  FNETG_CUDA(cudaMemcpy(params, ctx->d_params64.p, sizeof(double) * ctx->nsp * ctx->nparams,
+  FNETG_CUDA(copy_sync(ctx, params, ctx->d_params64.p, sizeof(double) * ctx->nsp * ctx->nparams,
                         cudaMemcpyDeviceToHost));
   return FNETG_OK;
 }
@@ -1010,7 +1025,7 @@ int fnetg_predict(fnetg_ctx *ctx, double *atomic_out, double *global_out) {
   const int nout = ctx->dims.back();
   std::vector<double> out((size_t)ctx->N * nout);
   if (ctx->N > 0)
-    FNETG_CUDA(cudaMemcpy(out.data(), ctx->d_out.p, sizeof(double) * out.size(),
+    FNETG_CUDA(copy_sync(ctx, out.data(), ctx->d_out.p, sizeof(double) * out.size(),
                           cudaMemcpyDeviceToHost));
   if (atomic_out) memcpy(atomic_out, out.data(), sizeof(double) * out.size());
   if (global_out) {
@@ -1036,7 +1051,7 @@ int fnetg_jacobian(fnetg_ctx *ctx, double *jac) {
     if (rc) return rc;
     FNETG_CUDA(cudaStreamSynchronize(ctx->stream));
     if (N > 0)
-      FNETG_CUDA(cudaMemcpy(buf.data(), ctx->d_jac.p, sizeof(double) * N * nf,
+      FNETG_CUDA(copy_sync(ctx, buf.data(), ctx->d_jac.p, sizeof(double) * N * nf,
                             cudaMemcpyDeviceToHost));
     for (int64_t a = 0; a < N; a++)
       for (int f = 0; f < nf; f++) jac[(a * nout + o) * nf + f] = buf[a * nf + f];
@@ -1055,7 +1070,7 @@ int fnetg_forces(fnetg_ctx *ctx, double *forces) {
     FNETG_CUDA(cudaStreamSynchronize(ctx->stream));
     const int nout = ctx->dims.back();
     if (ctx->N > 0)
-      FNETG_CUDA(cudaMemcpy(forces, ctx->d_forces.p, sizeof(double) * ctx->N * nout * 3,
+      FNETG_CUDA(copy_sync(ctx, forces, ctx->d_forces.p, sizeof(double) * ctx->N * nout * 3,
                             cudaMemcpyDeviceToHost));
   }
   return FNETG_OK;
@@ -1092,14 +1107,14 @@ int fnetg_set_targets(fnetg_ctx *ctx, int32_t ngt, int32_t nat, const double *gt
   FNETG_CUDA(ctx->d_w.ensure(sizeof(int32_t) * std::max(S, 1)));
   FNETG_CUDA(ctx->d_struct_aw.ensure(sizeof(double) * std::max(S, 1)));
   if (ngt > 0 && S > 0)
-    FNETG_CUDA(cudaMemcpy(ctx->d_gt.p, gt, sizeof(double) * S * ngt, cudaMemcpyHostToDevice));
+    FNETG_CUDA(copy_sync(ctx, ctx->d_gt.p, gt, sizeof(double) * S * ngt, cudaMemcpyHostToDevice));
   if (nat > 0 && N > 0)
-    FNETG_CUDA(cudaMemcpy(ctx->d_at.p, at, sizeof(double) * N * nat, cudaMemcpyHostToDevice));
+    FNETG_CUDA(copy_sync(ctx, ctx->d_at.p, at, sizeof(double) * N * nat, cudaMemcpyHostToDevice));
   if (N > 0)
-    FNETG_CUDA(cudaMemcpy(ctx->d_aw.p, aw.data(), sizeof(double) * N, cudaMemcpyHostToDevice));
+    FNETG_CUDA(copy_sync(ctx, ctx->d_aw.p, aw.data(), sizeof(double) * N, cudaMemcpyHostToDevice));
   if (S > 0) {
-    FNETG_CUDA(cudaMemcpy(ctx->d_w.p, w.data(), sizeof(int32_t) * S, cudaMemcpyHostToDevice));
-    FNETG_CUDA(cudaMemcpy(ctx->d_struct_aw.p, saw.data(), sizeof(double) * S,
+    FNETG_CUDA(copy_sync(ctx, ctx->d_w.p, w.data(), sizeof(int32_t) * S, cudaMemcpyHostToDevice));
+    FNETG_CUDA(copy_sync(ctx, ctx->d_struct_aw.p, saw.data(), sizeof(double) * S,
                           cudaMemcpyHostToDevice));
   }
   ctx->targets_set = true;
@@ -1119,12 +1134,12 @@ int fnetg_train_gradients(fnetg_ctx *ctx, int32_t loss, const int32_t *order, do
   if (rc) return rc;
   FNETG_CUDA(cudaStreamSynchronize(ctx->stream));
   if (grad)
-    FNETG_CUDA(cudaMemcpy(grad, ctx->d_grad64.p, sizeof(double) * ctx->nsp * ctx->nparams,
+    FNETG_CUDA(copy_sync(ctx, grad, ctx->d_grad64.p, sizeof(double) * ctx->nsp * ctx->nparams,
                           cudaMemcpyDeviceToHost));
   if (loss_out)
-    FNETG_CUDA(cudaMemcpy(loss_out, ctx->d_scalars.p, sizeof(double), cudaMemcpyDeviceToHost));
+    FNETG_CUDA(copy_sync(ctx, loss_out, ctx->d_scalars.p, sizeof(double), cudaMemcpyDeviceToHost));
   if (atomic_out && ctx->N > 0)
-    FNETG_CUDA(cudaMemcpy(atomic_out, ctx->d_out.p, sizeof(double) * ctx->N * ctx->dims.back(),
+    FNETG_CUDA(copy_sync(ctx, atomic_out, ctx->d_out.p, sizeof(double) * ctx->N * ctx->dims.back(),
                           cudaMemcpyDeviceToHost));
   return FNETG_OK;
 }
@@ -1142,9 +1157,9 @@ int fnetg_update_prepare(fnetg_ctx *ctx, double *grad, double strength, double a
   int rc = run_update_prepare(ctx, strength, alpha);
   if (rc) return rc;
   FNETG_CUDA(cudaStreamSynchronize(ctx->stream));
-  FNETG_CUDA(cudaMemcpy(grad, ctx->d_grad64.p, sizeof(double) * n, cudaMemcpyDeviceToHost));
+  FNETG_CUDA(copy_sync(ctx, grad, ctx->d_grad64.p, sizeof(double) * n, cudaMemcpyDeviceToHost));
   if (grad_norm)
-    FNETG_CUDA(cudaMemcpy(grad_norm, ctx->d_scalars.as<double>() + 1, sizeof(double),
+    FNETG_CUDA(copy_sync(ctx, grad_norm, ctx->d_scalars.as<double>() + 1, sizeof(double),
                           cudaMemcpyDeviceToHost));
   return FNETG_OK;
 }

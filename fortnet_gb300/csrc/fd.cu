@@ -42,13 +42,13 @@ extern "C" int fnetg_forces_fd(fnetg_ctx *ctx, double delta, double *forces) {
   std::vector<double> ext((size_t)std::max<int64_t>(N, 1) * std::max(next, 1));
   std::vector<double> params((size_t)ctx->nsp * ctx->nparams);
   if (N > 0) {
-    FNETG_CUDA(cudaMemcpy(coords.data(), ctx->d_coords.p, sizeof(double) * 3 * N,
+    FNETG_CUDA(copy_sync(ctx, coords.data(), ctx->d_coords.p, sizeof(double) * 3 * N,
                           cudaMemcpyDeviceToHost));
     if (next > 0)
-      FNETG_CUDA(cudaMemcpy(ext.data(), ctx->d_ext.p, sizeof(double) * N * next,
+      FNETG_CUDA(copy_sync(ctx, ext.data(), ctx->d_ext.p, sizeof(double) * N * next,
                             cudaMemcpyDeviceToHost));
   }
-  FNETG_CUDA(cudaMemcpy(params.data(), ctx->d_params64.p, sizeof(double) * params.size(),
+  FNETG_CUDA(copy_sync(ctx, params.data(), ctx->d_params64.p, sizeof(double) * params.size(),
                         cudaMemcpyDeviceToHost));
   std::memset(forces, 0, sizeof(double) * (size_t)N * nout * 3);
 

@@ -8,6 +8,7 @@
 #include <cstring>
 #include <map>
 #include <string>
+#include <atomic>
 #include <vector>
 
 #include "../../include/fnetg.h"
@@ -57,23 +58,33 @@ struct MFunc {
   int pad;
 };
 
-// Device buffer with grow-only reallocation.
+// Device buffer with grow-only reallocation.  A regrowth allocates 1/8 more than asked, so
+// that slowly growing sizes do not reallocate (cudaFree synchronises the whole device).
+// Allocations made by a host thread are added to *account when the thread has set it.
 struct DBuf {
   void *p = nullptr;
   size_t bytes = 0;
+  inline static thread_local std::atomic<int64_t> *account = nullptr;
   ~DBuf() { release(); }
   void release() {
     if (p) cudaFree(p);
+    if (p && account) *account -= (int64_t)bytes;
     p = nullptr;
     bytes = 0;
   }
   cudaError_t ensure(size_t n) {
     if (n <= bytes && p) return cudaSuccess;
+    const bool regrow = p != nullptr;
     release();
     if (n == 0) n = 16;
+    if (regrow) n += n / 8;
     cudaError_t e = cudaMalloc(&p, n);
-    if (e == cudaSuccess) bytes = n;
-    else p = nullptr;
+    if (e == cudaSuccess) {
+      bytes = n;
+      if (account) *account += (int64_t)n;
+    } else {
+      p = nullptr;
+    }
     return e;
   }
   template <typename T> T *as() const { return static_cast<T *>(p); }
@@ -240,6 +251,18 @@ struct LaunchScope {
 };
 
 inline int ceil_div(int64_t a, int64_t b) { return (int)((a + b - 1) / b); }
+// Raise (never lower) a kernel's dynamic shared-memory limit on the current device.  The
+// limit is per kernel, not per launch: contexts on other host threads launch the same kernel
+// with other sizes, and lowering it under them would make their launches fail.
+cudaError_t raise_smem_limit(const void *kernel, size_t bytes);
+// A copy on the context's stream, waited for: ordered after the context's kernels (the
+// stream does not synchronise with the legacy default stream), and the host buffer may be
+// released on return.  Contexts on other host threads are not waited for.
+inline cudaError_t copy_sync(fnetg_ctx *c, void *dst, const void *src, size_t bytes,
+                             cudaMemcpyKind kind) {
+  cudaError_t e = cudaMemcpyAsync(dst, src, bytes, kind, c->stream);
+  return e == cudaSuccess ? cudaStreamSynchronize(c->stream) : e;
+}
 int num_sms();
 void resolve_profile(fnetg_ctx *c);
 

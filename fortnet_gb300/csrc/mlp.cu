@@ -709,7 +709,7 @@ int launch_variant(fnetg_ctx *ctx, int kind, int v, const Layouts &Lo, MlpArgs<T
   FNETG_CHECK(smem <= 227 * 1024, FNETG_E_UNSUPPORTED, "network too wide for shared memory");
   void *k = mlp_variant<T>(kind, v);
   const int threads = (v & 2) ? 256 : 128;
-  FNETG_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  FNETG_CUDA(raise_smem_limit(k, smem));
   int per_sm = 0;
   FNETG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, threads, smem));
   FNETG_CHECK(per_sm > 0, FNETG_E_UNSUPPORTED, "MLP variant does not fit on an SM");
@@ -763,7 +763,7 @@ int run_mlp(fnetg_ctx *ctx, int kind, const Layouts &Lo, MlpArgs<T> &a, const ch
 template <typename T> int do_params(fnetg_ctx *ctx) {
   const Layouts Lo = make_layouts(ctx);
   FNETG_CUDA(ctx->d_ref_of_compute.ensure(sizeof(int64_t) * std::max<int64_t>(Lo.net.pstride, 1)));
-  FNETG_CUDA(cudaMemcpy(ctx->d_ref_of_compute.p, Lo.ref_of_compute.data(),
+  FNETG_CUDA(copy_sync(ctx, ctx->d_ref_of_compute.p, Lo.ref_of_compute.data(),
                         sizeof(int64_t) * Lo.net.pstride, cudaMemcpyHostToDevice));
   FNETG_CUDA(ctx->d_params.ensure(sizeof(T) * ctx->nsp * Lo.net.pstride));
   dim3 grid(ceil_div(Lo.net.pstride, 256), ctx->nsp);

@@ -334,7 +334,7 @@ __device__ Tile<T> carve_tile(unsigned char *p, const TileArgs<T> &a, bool force
 
 // Warps per CTA for a warp-per-atom kernel whose CTA needs `fixed` + wpb * `per_warp` bytes of
 // dynamic shared memory: the choice among 8, 4, 2, 1 with the most resident warps per SM
-// (ties go to the larger CTA).  Sets the kernel's shared-memory attributes for that choice.
+// (ties go to the larger CTA).  Raises the kernel's shared-memory limit to cover that choice.
 template <typename K>
 inline cudaError_t pick_warps(K kernel, size_t fixed, size_t per_warp, int &wpb, size_t &smem,
                               int &ctas_per_sm) {
@@ -345,7 +345,7 @@ inline cudaError_t pick_warps(K kernel, size_t fixed, size_t per_warp, int &wpb,
   for (int w = 8; w >= 1; w >>= 1) {
     const size_t bytes = fixed + per_warp * (size_t)w;
     if (bytes > 227 * 1024) continue;
-    err = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    err = raise_smem_limit(reinterpret_cast<const void *>(kernel), bytes);
     if (err != cudaSuccess) return err;
     int ctas = 0;
     err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&ctas, kernel, w * 32, bytes);
@@ -360,7 +360,7 @@ inline cudaError_t pick_warps(K kernel, size_t fixed, size_t per_warp, int &wpb,
   wpb = best_w;
   smem = fixed + per_warp * (size_t)best_w;
   ctas_per_sm = std::max(best_ctas, 1);
-  return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  return raise_smem_limit(reinterpret_cast<const void *>(kernel), smem);
 }
 
 // Stage the pair tile of atom i (all lanes), build the ordered species lists.

@@ -12,7 +12,8 @@ pair within 6 Angstrom, in Hartree).
        (168 features), network 168-64-64-1, mini-batches of 256 structures
 * C4 — 5,000 structures of 100-500 atoms, H/C/O, nR = 10, nA = 6 at 6.5 A (66 features),
        network 66-64-64-1, energies and forces
-* C5 — request stream: Poisson arrivals at 2,000 req/s, 16-4,096 atoms (log-uniform)
+* C5 — request stream: Poisson arrivals at 2,000 req/s, 16-4,096 atoms (log-uniform), the
+       C4 model; a pool of distinct structures that the stream cycles through
 """
 
 from __future__ import annotations
@@ -71,7 +72,20 @@ CONFIGS = {
                  (0.01, 2.0), {"zeta": (1.0, 2.0, 4.0), "lambda": (1.0, -1.0),
                                "eta": (0.005, 0.005, 1)},
                  (64, 64), 1004),
+    # request pool of the serving stream: the C4 model and functions, 16-4,096 atoms
+    "C5": Config("C5", 64, (16, 4096), "loguniform", (1, 6, 8), (1.0, 1.0, 1.0), 6.5, 10,
+                 (0.01, 2.0), {"zeta": (1.0, 2.0, 4.0), "lambda": (1.0, -1.0),
+                               "eta": (0.005, 0.005, 1)},
+                 (64, 64), 1005),
 }
+
+C5_RATE = 2000.0  # requests / s (Poisson arrivals)
+
+
+def arrivals(n, rate=C5_RATE, seed=1005):
+    """Arrival times (s) of a Poisson stream of n requests at the given rate."""
+    rng = np.random.default_rng(seed + 7)
+    return np.cumsum(rng.exponential(1.0 / rate, size=n))
 
 
 def base_functions(cfg: Config):
