@@ -76,7 +76,8 @@ def build(force=False, verbose=False, extra=None):
 HOST_DIR = os.path.join(HERE, "host")
 HOST_LIB = os.path.join(OUT_DIR, "libfnetg_host.so")
 HOST_RUN = os.path.join(OUT_DIR, "fnetg_run")
-HOST_SOURCES = ["hdf5lite.cpp", "fnet_host.cpp"]
+HOST_SOURCES = ["hdf5lite.cpp", "fnet_host.cpp", "ipi.cpp"]
+HOST_IPI = os.path.join(OUT_DIR, "fnetg_ipi")
 
 
 def cuda_lib_dir():
@@ -95,13 +96,14 @@ def host_link_flags():
 
 
 def build_host(force=False):
-    """The C++ host layer (libfnetg_host.so) and the fnetg_run driver, on top of libfnetg."""
+    """The C++ host layer (libfnetg_host.so) and the fnetg_run / fnetg_ipi programs, on top of
+    libfnetg."""
     build()
-    srcs = [os.path.join(HOST_DIR, f) for f in HOST_SOURCES + ["fnetg_run.cpp"]]
+    srcs = [os.path.join(HOST_DIR, f) for f in HOST_SOURCES + ["fnetg_run.cpp", "fnetg_ipi.cpp"]]
     hdrs = [os.path.join(HOST_DIR, f) for f in os.listdir(HOST_DIR) if f.endswith(".hpp")]
     newest = max(os.path.getmtime(f) for f in srcs + hdrs + [LIB])
-    if (not force and os.path.exists(HOST_RUN) and os.path.exists(HOST_LIB)
-            and os.path.getmtime(HOST_RUN) >= newest and os.path.getmtime(HOST_LIB) >= newest):
+    outs = [HOST_RUN, HOST_LIB, HOST_IPI]
+    if not force and all(os.path.exists(o) and os.path.getmtime(o) >= newest for o in outs):
         return HOST_LIB
     cmd = (["g++", "-shared", "-o", HOST_LIB + ".tmp"] + host_flags()
            + [os.path.join(HOST_DIR, f) for f in HOST_SOURCES]
@@ -116,6 +118,12 @@ def build_host(force=False):
     if res.returncode != 0:
         raise RuntimeError(f"fnetg_run build failed:\n{res.stdout}\n{res.stderr}")
     os.replace(HOST_RUN + ".tmp", HOST_RUN)
+    cmd = (["g++", "-o", HOST_IPI + ".tmp"] + host_flags()
+           + [os.path.join(HOST_DIR, "fnetg_ipi.cpp")] + host_link_flags())
+    res = subprocess.run(cmd, capture_output=True, text=True)
+    if res.returncode != 0:
+        raise RuntimeError(f"fnetg_ipi build failed:\n{res.stdout}\n{res.stderr}")
+    os.replace(HOST_IPI + ".tmp", HOST_IPI)
     return HOST_LIB
 
 
