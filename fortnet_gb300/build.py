@@ -76,7 +76,7 @@ def build(force=False, verbose=False, extra=None):
 HOST_DIR = os.path.join(HERE, "host")
 HOST_LIB = os.path.join(OUT_DIR, "libfnetg_host.so")
 HOST_RUN = os.path.join(OUT_DIR, "fnetg_run")
-HOST_SOURCES = ["hdf5lite.cpp", "fnet_host.cpp", "ipi.cpp"]
+HOST_SOURCES = ["hdf5lite.cpp", "h5write.cpp", "fnet_host.cpp", "ipi.cpp"]
 HOST_IPI = os.path.join(OUT_DIR, "fnetg_ipi")
 
 

@@ -1,5 +1,6 @@
 // C++ host side over the fnetg C-ABI (see fnet_host.hpp).
 #include "fnet_host.hpp"
+#include "h5write.hpp"
 
 #include <algorithm>
 #include <cctype>
@@ -329,6 +330,128 @@ std::vector<double> forceAnalysisFiniteDiff(Context &ctx, const TBpnn &bpnn, dou
   std::vector<double> f((size_t)ctx.data()->nTotalAtoms() * bpnn.dims.back() * 3, 0.0);
   ctx.check(fnetg_forces_fd(ctx.get(), delta, f.data()));
   return f;
+}
+
+// ---------------------------------------------------------------- writers
+
+void writeNetstat(const std::string &path, const Netstat &ns) {
+  h5w::File f;
+  f.group("netstat");
+  const int ng = (int)ns.gFunctions.size();
+  if (ng > 0) {
+    f.attr_str("netstat/mapping", "type", "acsf");
+    f.attr_i32("netstat/mapping", "nfunctions", {ng});
+    for (int i = 0; i < ng; i++) {
+      const fnetg_gfunc &g = ns.gFunctions[i];
+      if (g.type < 1 || g.type > 5) throw Error(FNETG_E_INVALID, "unknown G-function type");
+      const std::string fp = "netstat/mapping/function" + std::to_string(i + 1);
+      const bool ang = g.type >= 4;
+      f.attr_str(fp, "type", "g" + std::to_string(g.type));
+      f.attr_i32(fp, "atomid", {g.atomid});
+      f.attr_f64(fp, "cutoff", {g.rcut});
+      f.attr_i32(fp, "atomicnumbers", {g.z1, g.z2});
+      f.attr_i32(fp, "tradial", {ang ? 0 : 1});
+      f.attr_i32(fp, "tangular", {ang ? 1 : 0});
+      if (g.type == 2) {
+        f.attr_f64(fp, "eta", {g.eta});
+        f.attr_f64(fp, "rs", {g.rs});
+      } else if (g.type == 3) {
+        f.attr_f64(fp, "kappa", {g.kappa});
+      } else if (ang) {
+        f.attr_f64(fp, "xi", {g.xi});
+        f.attr_f64(fp, "lambda", {g.lambda});
+        f.attr_f64(fp, "eta", {g.eta});
+      }
+    }
+    if (!ns.zPrec.empty()) {
+      if ((int)ns.zPrec.size() != 2 * ng) throw Error(FNETG_E_SHAPE, "z-score statistics size");
+      f.attr_str("netstat/mapping/preconditioning", "type", "zscore");
+      f.dataset_f64("netstat/mapping/preconditioning/means", {(uint64_t)ng},
+                    std::vector<double>(ns.zPrec.begin(), ns.zPrec.begin() + ng));
+      f.dataset_f64("netstat/mapping/preconditioning/variances", {(uint64_t)ng},
+                    std::vector<double>(ns.zPrec.begin() + ng, ns.zPrec.end()));
+    }
+  }
+  if (!ns.extIndices.empty()) {
+    f.attr_i32("netstat/external", "nextfeatures", {(int32_t)ns.extIndices.size()});
+    f.dataset_i32("netstat/external/indices", {ns.extIndices.size()}, ns.extIndices);
+  }
+  const int nsp = (int)ns.atomicNumbers.size();
+  const int L = (int)ns.dims.size();
+  f.attr_i32("netstat/bpnn", "nglobaltargets", {ns.nGlobalTargets});
+  f.attr_i32("netstat/bpnn", "natomictargets", {ns.nAtomicTargets});
+  f.dataset_i32("netstat/bpnn/atomicnumbers", {(uint64_t)nsp}, ns.atomicNumbers);
+  static const char *act_names[] = {"tanh", "sigmoid", "relu", "lrelu", "softplus",
+                                    "bent", "atan", "gaussian", "heaviside", "linear"};
+  if (ns.activation < 0 || ns.activation > 9) throw Error(FNETG_E_INVALID, "activation code");
+  const int64_t np = fnetg_nparams(L, ns.dims.data());
+  if ((int64_t)ns.params.size() != np * nsp) throw Error(FNETG_E_SHAPE, "parameter count");
+  // serialised order (network.F90:397-427): every ww column-major, then every bb
+  std::vector<int64_t> woff(L), boff(L);
+  int64_t ind = 0;
+  for (int l = 0; l < L; l++) {
+    woff[l] = ind;
+    ind += (int64_t)ns.dims[l] * (l < L - 1 ? ns.dims[l + 1] : 1);
+  }
+  for (int l = 0; l < L; l++) {
+    boff[l] = ind;
+    ind += ns.dims[l];
+  }
+  for (int s = 0; s < nsp; s++) {
+    const std::string sp = "netstat/bpnn/" + lower(elementSymbol(ns.atomicNumbers[s])) + "-subnetwork";
+    f.attr_i32(sp, "element", {ns.atomicNumbers[s]});
+    f.attr_i32(sp, "nlayer", {L});
+    f.attr_str(sp, "activation", act_names[ns.activation]);
+    f.dataset_i32(sp + "/topology", {(uint64_t)L}, ns.dims);
+    const double *p = ns.params.data() + (size_t)s * np;
+    for (int l = 0; l + 1 < L; l++) {
+      const std::string lp = sp + "/layer" + std::to_string(l + 1);
+      // ww(l) of shape (dims[l], dims[l+1]) in Fortran order: the file lists (dims[l+1], dims[l])
+      f.dataset_f64(lp + "/weights", {(uint64_t)ns.dims[l + 1], (uint64_t)ns.dims[l]},
+                    std::vector<double>(p + woff[l], p + woff[l] + (int64_t)ns.dims[l] * ns.dims[l + 1]));
+      f.dataset_f64(lp + "/bias", {(uint64_t)ns.dims[l + 1]},
+                    std::vector<double>(p + boff[l + 1], p + boff[l + 1] + ns.dims[l + 1]));
+    }
+  }
+  f.write(path);
+}
+
+void writeFnetout(const std::string &path, const std::string &mode, int nGlobalTargets,
+                  int nAtomicTargets, const std::vector<FnetoutDatapoint> &points) {
+  if (mode != "validate" && mode != "predict")
+    throw Error(FNETG_E_INVALID, "Invalid program running mode selected.");
+  const int nTargets = nGlobalTargets + nAtomicTargets;
+  if (mode == "validate" && nTargets == 0)
+    throw Error(FNETG_E_INVALID, "Validation mode only valid in combination with target data.");
+  const bool tForces = !points.empty() && !points[0].forces.empty();
+  h5w::File f;
+  f.attr_str("fnetout", "mode", mode);
+  f.attr_i32("fnetout/output", "ndatapoints", {(int32_t)points.size()});
+  f.attr_i32("fnetout/output", "tforces", {tForces ? 1 : 0});
+  f.attr_i32("fnetout/output", "nglobaltargets", {nGlobalTargets});
+  f.attr_i32("fnetout/output", "natomictargets", {nAtomicTargets});
+  for (size_t k = 0; k < points.size(); k++) {
+    const FnetoutDatapoint &d = points[k];
+    const std::string dp = "fnetout/output/datapoint" + std::to_string(k + 1);
+    if (nTargets <= 0) throw Error(FNETG_E_SHAPE, "no outputs");
+    const uint64_t nAtom = d.rawPredictions.size() / (uint64_t)nTargets;
+    if (nAtom * (uint64_t)nTargets != d.rawPredictions.size())
+      throw Error(FNETG_E_SHAPE, "raw predictions size");
+    f.group(dp);
+    if (nGlobalTargets > 0) {
+      std::vector<double> g(nGlobalTargets, 0.0);
+      for (uint64_t a = 0; a < nAtom; a++)
+        for (int o = 0; o < nGlobalTargets; o++) g[o] += d.rawPredictions[a * nTargets + o];
+      f.dataset_f64(dp + "/globalpredictions", {(uint64_t)nGlobalTargets}, g);
+      if (mode == "validate")
+        f.dataset_f64(dp + "/globaltargets", {d.globalTargets.size()}, d.globalTargets);
+    }
+    f.dataset_f64(dp + "/rawpredictions", {nAtom, (uint64_t)nTargets}, d.rawPredictions);
+    if (mode == "validate" && nAtomicTargets > 0)
+      f.dataset_f64(dp + "/atomictargets", {nAtom, (uint64_t)nAtomicTargets}, d.atomicTargets);
+    if (tForces) f.dataset_f64(dp + "/forces", {nAtom, 3 * (uint64_t)nTargets}, d.forces);
+  }
+  f.write(path);
 }
 
 }  // namespace fnet

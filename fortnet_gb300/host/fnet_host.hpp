@@ -58,6 +58,22 @@ struct Netstat {
 
 Netstat readNetstat(const std::string &path);
 int32_t activationCode(const std::string &name);
+// The netstat file of a model: createNetstat + writeBpnnHeader (lib_io/netstat.F90:37-60,
+// 312-402), writeExtFeaturesConfig (406-453), TAcsf_toFile (acsf.F90:1759-1906) and the
+// layer parameters of TBpnn_toFile (bpnn.F90:1062-1140).
+void writeNetstat(const std::string &path, const Netstat &ns);
+
+// One structure's results for writeFnetout.
+struct FnetoutDatapoint {
+  std::vector<double> rawPredictions;   // [nAtom][nOut]
+  std::vector<double> forces;           // [nAtom][nOut][3] or empty
+  std::vector<double> globalTargets;    // validate mode: [nGlobalTargets]
+  std::vector<double> atomicTargets;    // validate mode: [nAtom][nAtomicTargets]
+};
+// writeFnetout (lib_io/fnetout.F90:33-158); mode "predict" or "validate".  Global predictions
+// are the per-structure sums of the first nGlobalTargets outputs.
+void writeFnetout(const std::string &path, const std::string &mode, int nGlobalTargets,
+                  int nAtomicTargets, const std::vector<FnetoutDatapoint> &points);
 
 // One GPU context holding a dataset (the program state of fortnet.F90:110-215).
 class Context {

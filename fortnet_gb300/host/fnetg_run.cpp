@@ -7,6 +7,11 @@
 //       predictions, forces).
 //   fnetg_run --dump DATASET [NETSTAT]
 //       read the files only (no GPU) and print what was read as JSON.
+//   fnetg_run --copy-netstat NETSTAT OUT
+//       read a netstat file and write the model it holds to OUT (no GPU).
+//
+// With --fnetout FILE [--mode predict|validate] the run also writes the reference's fnetout
+// file (predictions, forces, and in validate mode the dataset's targets).
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -68,10 +73,14 @@ int dump(const char *dataset, const char *netstat) {
 int run(int argc, char **argv) {
   const char *dataset = argv[1], *netstat = argv[2];
   int32_t prec = FNETG_FP64;
-  std::string forces;
+  std::string forces, fnetout, mode = "predict";
   double delta = 0.0;
   for (int k = 3; k < argc; k++) {
-    if (!std::strcmp(argv[k], "--fp32")) {
+    if (!std::strcmp(argv[k], "--fnetout") && k + 1 < argc) {
+      fnetout = argv[++k];
+    } else if (!std::strcmp(argv[k], "--mode") && k + 1 < argc) {
+      mode = argv[++k];
+    } else if (!std::strcmp(argv[k], "--fp32")) {
       prec = FNETG_FP32;
     } else if (!std::strcmp(argv[k], "--forces") && k + 1 < argc) {
       forces = argv[++k];
@@ -111,12 +120,30 @@ int run(int argc, char **argv) {
   fnet::TBpnn bpnn = fnet::TBpnn::fromNetstat(ns);
   bpnn.load(ctx);
   const fnet::Predicts p = bpnn.predictBatch(ctx);
+  std::vector<double> f;
+  if (forces == "analytical") f = fnet::forceAnalysisAnalytical(ctx, bpnn);
+  if (forces == "fd") f = fnet::forceAnalysisFiniteDiff(ctx, bpnn, delta);
   std::printf("{\n");
   print_array("atomic", p.atomic);
-  if (forces == "analytical") print_array("forces", fnet::forceAnalysisAnalytical(ctx, bpnn));
-  if (forces == "fd") print_array("forces", fnet::forceAnalysisFiniteDiff(ctx, bpnn, delta));
+  if (!f.empty()) print_array("forces", f);
   print_array("global", p.global, true);
   std::printf("}\n");
+  if (!fnetout.empty()) {
+    const int nout = ns.dims.back();
+    std::vector<fnet::FnetoutDatapoint> pts(d.nDatapoints());
+    for (int s = 0; s < d.nDatapoints(); s++) {
+      const int64_t a0 = d.atomOffsets[s], a1 = d.atomOffsets[s + 1];
+      pts[s].rawPredictions.assign(p.atomic.begin() + a0 * nout, p.atomic.begin() + a1 * nout);
+      if (!f.empty()) pts[s].forces.assign(f.begin() + a0 * nout * 3, f.begin() + a1 * nout * 3);
+      if (mode == "validate") {
+        pts[s].globalTargets.assign(d.globalTargets.begin() + (int64_t)s * d.nGlobalTargets,
+                                    d.globalTargets.begin() + (int64_t)(s + 1) * d.nGlobalTargets);
+        pts[s].atomicTargets.assign(d.atomicTargets.begin() + a0 * d.nAtomicTargets,
+                                    d.atomicTargets.begin() + a1 * d.nAtomicTargets);
+      }
+    }
+    fnet::writeFnetout(fnetout, mode, ns.nGlobalTargets, ns.nAtomicTargets, pts);
+  }
   return 0;
 }
 
@@ -125,9 +152,15 @@ int run(int argc, char **argv) {
 int main(int argc, char **argv) {
   try {
     if (argc >= 3 && !std::strcmp(argv[1], "--dump")) return dump(argv[2], argc > 3 ? argv[3] : nullptr);
+    if (argc == 4 && !std::strcmp(argv[1], "--copy-netstat")) {
+      fnet::writeNetstat(argv[3], fnet::readNetstat(argv[2]));
+      return 0;
+    }
     if (argc >= 3) return run(argc, argv);
     std::fprintf(stderr, "usage: fnetg_run DATASET NETSTAT [--fp32] [--forces analytical|fd DELTA]\n"
-                         "       fnetg_run --dump DATASET [NETSTAT]\n");
+                         "                 [--fnetout FILE [--mode predict|validate]]\n"
+                         "       fnetg_run --dump DATASET [NETSTAT]\n"
+                         "       fnetg_run --copy-netstat NETSTAT OUT\n");
     return 2;
   } catch (const fnet::Error &e) {
     std::fprintf(stderr, "fnetg_run: error %d: %s\n", e.code, e.what());
