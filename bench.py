@@ -317,6 +317,10 @@ def serving_leg(args):
     import queue as _queue
 
     sys.setswitchinterval(0.0002)  # the submitter spins before each arrival
+    import gc
+
+    gc.collect()
+    gc.disable()  # no collector pauses in the load generator while the stream runs
     pending = _queue.Queue()
     lat = np.zeros(warm + n)
     done_ns = np.zeros(warm + n, dtype=np.int64)
@@ -343,6 +347,7 @@ def serving_leg(args):
             t, na = srv.submit(an, xyz, lv, arrival_ns=target)
             pending.put((k, t, na))
         th.join()
+        gc.enable()
         st = srv.stats()
     # FP32 service against an FP64 run of the same kernels on the first pool structures
     chk = list(range(min(16, len(reqs))))
@@ -370,6 +375,7 @@ def serving_leg(args):
         "lanes": st["lanes"], "batches": st["batches"],
         "mean_batch_requests": round(st["requests"] / max(st["batches"], 1), 2),
         "max_batch_requests": st["max_batch_requests"], "max_in_flight": st["max_in_flight"],
+        "max_batch_ms": round(1e3 * st["max_batch_s"], 3),
         "device_bytes": st["device_bytes"],
         "fp32_vs_fp64": {"structures": len(chk), "energy_rel": float(f"{e_err:.3g}"),
                          "force_rel_of_max": float(f"{f_err:.3g}")},

@@ -389,14 +389,15 @@ class Rng:
 class _ServerConfig(C.Structure):
     _fields_ = [("precision", C.c_int32), ("device", C.c_int32), ("lanes", C.c_int32),
                 ("pad", C.c_int32), ("max_batch_atoms", C.c_int64),
-                ("hbm_budget_bytes", C.c_int64)]
+                ("hbm_budget_bytes", C.c_int64), ("reserve_bytes", C.c_int64)]
 
 
 class _ServerStats(C.Structure):
     _fields_ = [("requests", C.c_int64), ("batches", C.c_int64), ("atoms", C.c_int64),
                 ("max_batch_atoms", C.c_int64), ("max_batch_requests", C.c_int64),
                 ("device_bytes", C.c_int64), ("batch_cap_atoms", C.c_int64),
-                ("lanes", C.c_int32), ("max_in_flight", C.c_int32), ("busy_s", C.c_double)]
+                ("lanes", C.c_int32), ("max_in_flight", C.c_int32), ("busy_s", C.c_double),
+                ("max_batch_s", C.c_double)]
 
 
 class Server:
@@ -404,10 +405,10 @@ class Server:
     thread, served by continuous batching over ``lanes`` concurrent device batches."""
 
     def __init__(self, atomic_numbers, funcs, zprec, dims, activation, params, precision=FP32,
-                 device=0, lanes=0, max_batch_atoms=0, hbm_budget_bytes=0):
+                 device=0, lanes=0, max_batch_atoms=0, hbm_budget_bytes=0, reserve_bytes=0):
         self.lib = load()
         cfg = _ServerConfig(int(precision), int(device), int(lanes), 0, int(max_batch_atoms),
-                            int(hbm_budget_bytes))
+                            int(hbm_budget_bytes), int(reserve_bytes))
         g = pack(funcs) if not isinstance(funcs, np.ndarray) else funcs
         self.ng = len(g)
         self.dims = [int(d) for d in dims]

@@ -58,16 +58,32 @@ struct MFunc {
   int pad;
 };
 
+// Stream-ordered allocation from a memory pool, for contexts driven by one host thread each
+// (the prediction service's lanes): set per thread through DBuf::pool.
+struct PoolAlloc {
+  cudaMemPool_t pool;
+  cudaStream_t stream;
+};
+
 // Device buffer with grow-only reallocation.  A regrowth allocates 1/8 more than asked, so
-// that slowly growing sizes do not reallocate (cudaFree synchronises the whole device).
-// Allocations made by a host thread are added to *account when the thread has set it.
+// that slowly growing sizes do not reallocate.  Plain allocations use cudaMalloc/cudaFree
+// (which synchronise the whole device); when the allocating thread has set DBuf::pool, the
+// buffer comes from that pool in the order of that stream (no device-wide synchronisation,
+// and no new device mappings while the pool holds enough reserved memory).  Allocations made
+// by a host thread are added to *account when the thread has set it.
 struct DBuf {
   void *p = nullptr;
   size_t bytes = 0;
+  bool pooled = false;
+  cudaStream_t pool_stream = nullptr;
   inline static thread_local std::atomic<int64_t> *account = nullptr;
+  inline static thread_local const PoolAlloc *pool = nullptr;
   ~DBuf() { release(); }
   void release() {
-    if (p) cudaFree(p);
+    if (p) {
+      if (pooled) cudaFreeAsync(p, pool_stream);
+      else cudaFree(p);
+    }
     if (p && account) *account -= (int64_t)bytes;
     p = nullptr;
     bytes = 0;
@@ -78,7 +94,15 @@ struct DBuf {
     release();
     if (n == 0) n = 16;
     if (regrow) n += n / 8;
-    cudaError_t e = cudaMalloc(&p, n);
+    cudaError_t e;
+    if (pool) {
+      e = cudaMallocFromPoolAsync(&p, n, pool->pool, pool->stream);
+      pooled = true;
+      pool_stream = pool->stream;
+    } else {
+      e = cudaMalloc(&p, n);
+      pooled = false;
+    }
     if (e == cudaSuccess) {
       bytes = n;
       if (account) *account += (int64_t)n;

@@ -42,6 +42,7 @@ using RequestPtr = std::shared_ptr<Request>;
 
 struct Lane {
   fnetg_ctx *ctx = nullptr;
+  fnetg::PoolAlloc alloc{};  // the server's pool on this lane's stream
   std::thread th;
   std::atomic<int64_t> dev_bytes{0};  // device memory held by the lane's context
   int64_t peak_atoms = 0;   // largest batch served
@@ -70,6 +71,7 @@ struct fnetg_server {
   int64_t next_ticket = 1;
   bool stop = false;
   std::vector<std::unique_ptr<Lane>> lanes;
+  cudaMemPool_t pool = nullptr;
   std::string err;
   fnetg_server_stats st{};
   int32_t in_flight = 0;
@@ -133,6 +135,7 @@ int run_batch(fnetg_server *s, Lane &ln, std::vector<RequestPtr> &batch) {
 void lane_loop(fnetg_server *s, Lane *ln) {
   cudaSetDevice(s->cfg.device);
   fnetg::DBuf::account = &ln->dev_bytes;
+  fnetg::DBuf::pool = &ln->alloc;
   std::vector<RequestPtr> batch;
   for (;;) {
     int64_t atoms = 0;
@@ -179,11 +182,25 @@ void lane_loop(fnetg_server *s, Lane *ln) {
       s->st.max_batch_atoms = std::max(s->st.max_batch_atoms, atoms);
       s->st.max_batch_requests = std::max<int64_t>(s->st.max_batch_requests, (int64_t)batch.size());
       s->st.busy_s += 1e-9 * (double)(t1 - t0);
+      s->st.max_batch_s = std::max(s->st.max_batch_s, 1e-9 * (double)(t1 - t0));
     }
     s->cv_done.notify_all();
     batch.clear();
   }
   fnetg::DBuf::account = nullptr;
+  fnetg::DBuf::pool = nullptr;
+}
+
+// Frees the lanes' contexts and the pool (after their stream-ordered frees have run).
+void teardown(fnetg_server *s) {
+  for (auto &ln : s->lanes)
+    if (ln->ctx) fnetg_destroy(ln->ctx);
+  s->lanes.clear();
+  if (s->pool) {
+    cudaDeviceSynchronize();
+    cudaMemPoolDestroy(s->pool);
+    s->pool = nullptr;
+  }
 }
 
 }  // namespace
@@ -224,19 +241,46 @@ int fnetg_server_create(fnetg_server **out, const fnetg_server_config *cfg, int3
   s->activation = activation;
   const int64_t np = fnetg_nparams(nlayer, dims);
   s->params.assign(params, params + (size_t)nspecies * np);
+  // one pool for every lane's buffers, keeping what it reserves
+  cudaMemPoolProps props{};
+  props.allocType = cudaMemAllocationTypePinned;
+  props.handleTypes = cudaMemHandleTypeNone;
+  props.location.type = cudaMemLocationTypeDevice;
+  props.location.id = cfg->device;
+  if (cudaMemPoolCreate(&s->pool, &props) != cudaSuccess) return FNETG_E_CUDA;
+  uint64_t keep = ~uint64_t(0);
+  if (cudaMemPoolSetAttribute(s->pool, cudaMemPoolAttrReleaseThreshold, &keep) != cudaSuccess) {
+    teardown(s.get());
+    return FNETG_E_CUDA;
+  }
+  const int64_t reserve = std::min<int64_t>(
+      s->cfg.hbm_budget_bytes,
+      s->cfg.reserve_bytes > 0 ? s->cfg.reserve_bytes : (int64_t)s->cfg.lanes << 29);
   for (int l = 0; l < s->cfg.lanes; l++) {
     std::unique_ptr<Lane> ln(new Lane());
-    fnetg::DBuf::account = &ln->dev_bytes;
     int rc = fnetg_create(&ln->ctx, s->cfg.precision, s->cfg.device);
+    void *stream = nullptr;
+    if (!rc) rc = fnetg_get_stream(ln->ctx, &stream);
+    ln->alloc = fnetg::PoolAlloc{s->pool, static_cast<cudaStream_t>(stream)};
+    if (!rc && l == 0 && reserve > 0) {
+      // reserve the pool's memory once: allocate and free it in stream order
+      void *p = nullptr;
+      if (cudaMallocFromPoolAsync(&p, (size_t)reserve, s->pool, ln->alloc.stream) != cudaSuccess ||
+          cudaFreeAsync(p, ln->alloc.stream) != cudaSuccess ||
+          cudaStreamSynchronize(ln->alloc.stream) != cudaSuccess)
+        rc = FNETG_E_NOMEM;
+    }
+    fnetg::DBuf::account = &ln->dev_bytes;
+    fnetg::DBuf::pool = &ln->alloc;
     if (!rc) rc = fnetg_set_gfunctions(ln->ctx, ng, g);
     if (!rc) rc = fnetg_set_network(ln->ctx, nspecies, nlayer, dims, activation, params);
     fnetg::DBuf::account = nullptr;
+    fnetg::DBuf::pool = nullptr;
+    s->lanes.push_back(std::move(ln));
     if (rc) {
-      if (ln->ctx) fnetg_destroy(ln->ctx);
-      for (auto &o : s->lanes) fnetg_destroy(o->ctx);
+      teardown(s.get());
       return rc;
     }
-    s->lanes.push_back(std::move(ln));
   }
   for (auto &ln : s->lanes) ln->th = std::thread(lane_loop, s.get(), ln.get());
   *out = s.release();
@@ -258,7 +302,7 @@ int fnetg_server_destroy(fnetg_server *srv) {
   srv->cv_done.notify_all();
   for (auto &ln : srv->lanes)
     if (ln->th.joinable()) ln->th.join();
-  for (auto &ln : srv->lanes) fnetg_destroy(ln->ctx);
+  teardown(srv);
   delete srv;
   return FNETG_OK;
 }

@@ -12,6 +12,10 @@
  * arrive while other batches are on the device are admitted by the next free lane, so the
  * lanes' batches overlap on the device.
  *
+ * Device memory of the lanes comes from one stream-ordered memory pool that keeps what it
+ * has reserved: after the first batches no allocation synchronises the device or maps new
+ * memory (both of which stall every lane and, on a coherent CPU-GPU node, the host process).
+ *
  * Admission is by device memory: every lane may hold at most hbm_budget_bytes / lanes of
  * device memory, and a batch takes queued requests in arrival order while its atoms times
  * the measured device bytes per atom stay inside that share (and inside max_batch_atoms).
@@ -42,6 +46,8 @@ typedef struct {
   int32_t pad;
   int64_t max_batch_atoms;  /* atoms per batch (and per request) at most; 0 -> 65536 */
   int64_t hbm_budget_bytes; /* device memory all lanes may hold; 0 -> 80% of free memory */
+  int64_t reserve_bytes;    /* device memory reserved up front in the lanes' memory pool;
+                               0 -> 512 MiB per lane (capped by the budget) */
 } fnetg_server_config;
 
 /* The model: G-functions g[ng] with their z-score statistics zprec[2*ng] (means, then
@@ -88,6 +94,7 @@ typedef struct {
   int32_t lanes;
   int32_t max_in_flight;     /* most batches on the device at once */
   double busy_s;             /* summed batch service time of all lanes */
+  double max_batch_s;        /* longest batch service time */
 } fnetg_server_stats;
 
 int fnetg_server_stats_get(fnetg_server *srv, fnetg_server_stats *out);
