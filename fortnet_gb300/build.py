@@ -76,8 +76,11 @@ def build(force=False, verbose=False, extra=None):
 HOST_DIR = os.path.join(HERE, "host")
 HOST_LIB = os.path.join(OUT_DIR, "libfnetg_host.so")
 HOST_RUN = os.path.join(OUT_DIR, "fnetg_run")
-HOST_SOURCES = ["hdf5lite.cpp", "h5write.cpp", "fnet_host.cpp", "ipi.cpp"]
+HOST_SOURCES = ["hdf5lite.cpp", "h5write.cpp", "fnet_host.cpp", "ipi.cpp", "hsd.cpp", "fnet_input.cpp"]
 HOST_IPI = os.path.join(OUT_DIR, "fnetg_ipi")
+HOST_FNETG = os.path.join(OUT_DIR, "fnetg")
+# programs linked against the host layer: output path -> source
+HOST_PROGRAMS = {HOST_RUN: "fnetg_run.cpp", HOST_IPI: "fnetg_ipi.cpp", HOST_FNETG: "fnetg_main.cpp"}
 
 
 def cuda_lib_dir():
@@ -96,13 +99,13 @@ def host_link_flags():
 
 
 def build_host(force=False):
-    """The C++ host layer (libfnetg_host.so) and the fnetg_run / fnetg_ipi programs, on top of
-    libfnetg."""
+    """The C++ host layer (libfnetg_host.so) and the fnetg, fnetg_run and fnetg_ipi programs,
+    on top of libfnetg."""
     build()
-    srcs = [os.path.join(HOST_DIR, f) for f in HOST_SOURCES + ["fnetg_run.cpp", "fnetg_ipi.cpp"]]
+    srcs = [os.path.join(HOST_DIR, f) for f in HOST_SOURCES + list(HOST_PROGRAMS.values())]
     hdrs = [os.path.join(HOST_DIR, f) for f in os.listdir(HOST_DIR) if f.endswith(".hpp")]
     newest = max(os.path.getmtime(f) for f in srcs + hdrs + [LIB])
-    outs = [HOST_RUN, HOST_LIB, HOST_IPI]
+    outs = [HOST_LIB] + list(HOST_PROGRAMS)
     if not force and all(os.path.exists(o) and os.path.getmtime(o) >= newest for o in outs):
         return HOST_LIB
     cmd = (["g++", "-shared", "-o", HOST_LIB + ".tmp"] + host_flags()
@@ -112,18 +115,18 @@ def build_host(force=False):
     if res.returncode != 0:
         raise RuntimeError(f"host library build failed:\n{res.stdout}\n{res.stderr}")
     os.replace(HOST_LIB + ".tmp", HOST_LIB)
-    cmd = (["g++", "-o", HOST_RUN + ".tmp"] + host_flags()
-           + [os.path.join(HOST_DIR, "fnetg_run.cpp")] + host_link_flags())
-    res = subprocess.run(cmd, capture_output=True, text=True)
-    if res.returncode != 0:
-        raise RuntimeError(f"fnetg_run build failed:\n{res.stdout}\n{res.stderr}")
-    os.replace(HOST_RUN + ".tmp", HOST_RUN)
-    cmd = (["g++", "-o", HOST_IPI + ".tmp"] + host_flags()
-           + [os.path.join(HOST_DIR, "fnetg_ipi.cpp")] + host_link_flags())
-    res = subprocess.run(cmd, capture_output=True, text=True)
-    if res.returncode != 0:
-        raise RuntimeError(f"fnetg_ipi build failed:\n{res.stdout}\n{res.stderr}")
-    os.replace(HOST_IPI + ".tmp", HOST_IPI)
+
+    def link(item):
+        out, src = item
+        cmd = (["g++", "-o", out + ".tmp"] + host_flags() + [os.path.join(HOST_DIR, src)]
+               + host_link_flags())
+        res = subprocess.run(cmd, capture_output=True, text=True)
+        if res.returncode != 0:
+            raise RuntimeError(f"{os.path.basename(out)} build failed:\n{res.stdout}\n{res.stderr}")
+        os.replace(out + ".tmp", out)
+
+    with cf.ThreadPoolExecutor(max_workers=len(HOST_PROGRAMS)) as ex:
+        list(ex.map(link, HOST_PROGRAMS.items()))
     return HOST_LIB
 
 

@@ -416,6 +416,55 @@ void writeNetstat(const std::string &path, const Netstat &ns) {
   f.write(path);
 }
 
+void writeHdfDataset(const std::string &path, const Dataset &d) {
+  h5w::File f;
+  const int S = d.nDatapoints();
+  const std::string ds = "fnetdata/dataset";
+  f.attr_i32(ds, "ndatapoints", {S});
+  f.attr_i32(ds, "nextfeatures", {d.nExtFeatures});
+  f.attr_i32(ds, "withstructures", {1});
+  f.attr_i32(ds, "ntotatoms", {(int32_t)d.nTotalAtoms()});
+  f.dataset_i32(ds + "/atomicnumbers", {d.atomicNumbers.size()}, d.atomicNumbers);
+  f.attr_i32(ds + "/training", "nglobaltargets", {d.nGlobalTargets});
+  f.attr_i32(ds + "/training", "natomictargets", {d.nAtomicTargets});
+  for (int s = 0; s < S; s++) {
+    const int64_t a0 = d.atomOffsets[s], a1 = d.atomOffsets[s + 1];
+    const uint64_t n = (uint64_t)(a1 - a0);
+    const std::string dp = ds + "/datapoint" + std::to_string(s + 1);
+    f.attr_i32(dp, "weight", {d.weights.empty() ? 1 : d.weights[s]});
+    f.dataset_f64(dp + "/atomicweights", {n},
+                  d.atomicWeights.empty() ? std::vector<double>(n, 1.0)
+                                          : std::vector<double>(d.atomicWeights.begin() + a0,
+                                                                d.atomicWeights.begin() + a1));
+    const std::string geo = dp + "/geometry";
+    f.attr_i32(geo, "fractional", {0});
+    f.attr_i32(geo, "periodic", {d.periodic[s] ? 1 : 0});
+    f.dataset_f64(geo + "/coordinates", {n, 3},
+                  std::vector<double>(d.coords.begin() + 3 * a0, d.coords.begin() + 3 * a1));
+    if (d.periodic[s])
+      f.dataset_f64(geo + "/basis", {3, 3},
+                    std::vector<double>(d.latVecs.begin() + 9 * s, d.latVecs.begin() + 9 * (s + 1)));
+    f.dataset_i32(geo + "/localattoatnum", {n},
+                  std::vector<int32_t>(d.localAtToAtNum.begin() + a0, d.localAtToAtNum.begin() + a1));
+    std::vector<int32_t> sp(d.localAtToGlobalSp.begin() + a0, d.localAtToGlobalSp.begin() + a1);
+    for (int32_t &x : sp) x += 1;
+    f.dataset_i32(geo + "/localattoglobalsp", {n}, sp);
+    if (d.nGlobalTargets > 0)
+      f.dataset_f64(dp + "/globaltargets", {(uint64_t)d.nGlobalTargets},
+                    std::vector<double>(d.globalTargets.begin() + (int64_t)s * d.nGlobalTargets,
+                                        d.globalTargets.begin() + (int64_t)(s + 1) * d.nGlobalTargets));
+    if (d.nAtomicTargets > 0)
+      f.dataset_f64(dp + "/atomictargets", {n, (uint64_t)d.nAtomicTargets},
+                    std::vector<double>(d.atomicTargets.begin() + a0 * d.nAtomicTargets,
+                                        d.atomicTargets.begin() + a1 * d.nAtomicTargets));
+    if (d.nExtFeatures > 0)
+      f.dataset_f64(dp + "/extfeatures", {n, (uint64_t)d.nExtFeatures},
+                    std::vector<double>(d.extFeatures.begin() + a0 * d.nExtFeatures,
+                                        d.extFeatures.begin() + a1 * d.nExtFeatures));
+  }
+  f.write(path);
+}
+
 void writeFnetout(const std::string &path, const std::string &mode, int nGlobalTargets,
                   int nAtomicTargets, const std::vector<FnetoutDatapoint> &points) {
   if (mode != "validate" && mode != "predict")

@@ -43,6 +43,9 @@ struct Dataset {
 
 // readHdfDataset (fnetdata.F90:994-1216): geometry, targets, weights, external features.
 Dataset readHdfDataset(const std::string &path);
+// The dataset file layout readHdfDataset reads (cartesian coordinates), for converting data
+// into the fnet format.
+void writeHdfDataset(const std::string &path, const Dataset &d);
 
 // A netstat file: ACSF configuration, z-score statistics and the trained sub-networks.
 struct Netstat {

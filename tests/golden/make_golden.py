@@ -160,7 +160,8 @@ def netstat_arrays(ns, prefix):
 def extract_case(ref_root, case, outdir):
     cdir = os.path.join(ref_root, "test", "prog", "fortnet", case)
     with open(os.path.join(cdir, "fortnet_in.hsd")) as fh:
-        hsd = parse_hsd(fh.read())
+        hsd_text = fh.read()
+    hsd = parse_hsd(hsd_text)
     mode = str(_get(hsd, "Options/Mode", "train")).strip("'\"").lower()
     read_netstat = _yes(_get(hsd, "Options/ReadNetStats"))
     seed = int(_get(hsd, "Options/RandomSeed", "0"))
@@ -246,6 +247,8 @@ def extract_case(ref_root, case, outdir):
         if frc:
             arrays["out_forces"] = np.concatenate(frc)
     arrays["settings"] = np.frombuffer(json.dumps(settings).encode(), dtype=np.uint8)
+    # the input file itself, for running the whole program on the case
+    arrays["hsd"] = np.frombuffer(hsd_text.encode(), dtype=np.uint8)
     fname = case.replace("/", "__") + ".npz"
     np.savez_compressed(os.path.join(outdir, "cases", fname), **arrays)
     return fname, None

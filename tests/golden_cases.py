@@ -61,6 +61,8 @@ def load_case(name) -> Case:
     z = np.load(os.path.join(GOLDEN, "cases", name.replace("/", "__") + ".npz"))
     arrays = {k: z[k] for k in z.files}
     settings = json.loads(bytes(arrays.pop("settings")).decode())
+    if "hsd" in arrays:
+        settings["hsd"] = bytes(arrays.pop("hsd")).decode()
     return Case(name, settings, arrays, load_dataset(settings["dataset"]))
 
 

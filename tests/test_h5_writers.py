@@ -33,15 +33,17 @@ def tool(tmp_path_factory):
     return exe
 
 
-def write_model(path, atomic_numbers, funcs, zprec, dims, activation, nglobal, natomic, params):
-    """The model file read by tests/cpp/h5_writers.cpp."""
+def write_model(path, atomic_numbers, funcs, zprec, dims, activation, nglobal, natomic, params,
+                ext_indices=None):
+    """The model file read by tests/cpp/h5_writers.cpp (zprec None: no z-score statistics)."""
     g = pack(funcs) if len(funcs) else np.zeros(0, dtype=GFUNC_DTYPE)
     with open(path, "wb") as fh:
         fh.write(np.int32(len(atomic_numbers)).tobytes())
         fh.write(np.asarray(atomic_numbers, dtype="<i4").tobytes())
         fh.write(np.int32(len(g)).tobytes())
         fh.write(g.tobytes())
-        if len(g):
+        fh.write(np.int32(0 if zprec is None else 1).tobytes())
+        if zprec is not None:
             fh.write(np.asarray(zprec, dtype="<f8").reshape(-1).tobytes())
         fh.write(np.int32(len(dims)).tobytes())
         fh.write(np.asarray(dims, dtype="<i4").tobytes())
@@ -49,6 +51,9 @@ def write_model(path, atomic_numbers, funcs, zprec, dims, activation, nglobal, n
         fh.write(np.int32(nglobal).tobytes())
         fh.write(np.int32(natomic).tobytes())
         fh.write(np.asarray(params, dtype="<f8").reshape(-1).tobytes())
+        ext = np.zeros(0, dtype="<i4") if ext_indices is None else np.asarray(ext_indices, "<i4")
+        fh.write(np.int32(len(ext)).tobytes())
+        fh.write(ext.tobytes())
 
 
 @pytest.mark.skipif(not NETSTATS, reason="reference netstat files not available")
