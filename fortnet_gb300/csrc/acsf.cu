@@ -46,10 +46,11 @@ __global__ void __launch_bounds__(256) acsf_kernel(TileArgs<T> a) {
     // parts combined by shuffles.  The cutoff table is zero outside a function's class.
     {
       const int S = a.rad_split;
+      const int sh = S == 4 ? 2 : (S == 2 ? 1 : 0);  // S is a power of two: no divisions
       const int items = a.nrad * S;
       for (int base = 0; base < items; base += 32) {
         const int it = base + lane;
-        const int g = it / S, part = it - g * S;
+        const int g = it >> sh, part = it - (g << sh);
         T acc = 0;
         if (it < items) {
           const GDesc d = a.rad[g];
@@ -57,7 +58,7 @@ __global__ void __launch_bounds__(256) acsf_kernel(TileArgs<T> a) {
           const T kappa = P[1], rs = P[2], eta = P[3];
           const uint16_t *lst = d.chan1 >= 0 ? t.lists + d.chan1 * a.cap : nullptr;
           const int n = d.chan1 >= 0 ? t.cnt[d.chan1] : np;
-          const int chunk = ((n + S - 1) / S + 3) & ~3;
+          const int chunk = (((n + S - 1) >> sh) + 3) & ~3;
           const int k0 = min(n, part * chunk), k1 = min(n, k0 + chunk);
           const T *fcr = t.fc + d.rclass * a.cap;
           const T idi = atom_id<T>(a.ext, a.next, d.atomid, i);

@@ -393,8 +393,9 @@ __global__ void __launch_bounds__(256, 3) forces_kernel(TileArgs<T> a) {
       }
     }
     __syncwarp();
-    // ---- scatter: F_j -= w_p, F_i += sum_p w_p (self images cancel)
-    double sx = 0, sy = 0, sz = 0;
+    // ---- scatter: F_j -= w_p, F_i += sum_p w_p (self images cancel).  A lane sums its own
+    // pairs (two or three) in T and the warp sums the lanes in FP64.
+    T lx = 0, ly = 0, lz = 0;
     for (int q = lane; q < np; q += 32) {
       if ((tl.info[q] >> 8) & 1u) continue;
       const V4<T> w = tl.w[q];
@@ -403,10 +404,11 @@ __global__ void __launch_bounds__(256, 3) forces_kernel(TileArgs<T> a) {
       atomicAdd(Fj + 0, -(double)w.x);
       atomicAdd(Fj + 1, -(double)w.y);
       atomicAdd(Fj + 2, -(double)w.z);
-      sx += (double)w.x;
-      sy += (double)w.y;
-      sz += (double)w.z;
+      lx += w.x;
+      ly += w.y;
+      lz += w.z;
     }
+    double sx = (double)lx, sy = (double)ly, sz = (double)lz;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
       sx += __shfl_xor_sync(0xffffffffu, sx, o);
