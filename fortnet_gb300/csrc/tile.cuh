@@ -42,38 +42,22 @@ constexpr bool mono_mult_table_ok() {
 }
 static_assert(mono_mult_table_ok(), "multinomial table");
 
-// Float exp on the FMA/ALU pipes only (the library's range reduction spends conversion
-// instructions, which GB300 issues on its narrow FP64 pipe).  Cody-Waite reduction:
-// n = round(x log2 e) by adding 1.5 * 2^23 (the float sum rounds to an integer; n is read back
-// from the bit pattern), z = x - n ln2 with ln2 split in a 15-bit head (n * head exact) and a
-// tail, e^z from its Taylor series through z^7 (|z| <= ln2 / 2: truncation < 1e-8), and the
-// scaling by 2^n added to the exponent field.  Max error 1.3 ulp on [-86.5, 88.7]; results
-// below exp(-86.5) are flushed to zero.
-__device__ __forceinline__ float exp_cw(float x) {
-  constexpr float kLog2e = 1.44269504088896341f;
-  constexpr float kLn2Hi = 0.693145751953125f;       // ln 2 to 15 significant bits
-  constexpr float kLn2Lo = 1.428606765330187e-06f;   // ln 2 - kLn2Hi
-  constexpr float kRound = 12582912.f;               // 1.5 * 2^23
-  const float xc = fminf(fmaxf(x, -86.5f), 88.7f);
-  const float t = fmaf(xc, kLog2e, kRound);
-  const float n = t - kRound;
-  const int ni = __float_as_int(t) - __float_as_int(kRound);
-  float z = fmaf(-n, kLn2Hi, xc);
-  z = fmaf(-n, kLn2Lo, z);
-  float p = 1.f / 5040.f;
-  p = fmaf(p, z, 1.f / 720.f);
-  p = fmaf(p, z, 1.f / 120.f);
-  p = fmaf(p, z, 1.f / 24.f);
-  p = fmaf(p, z, 1.f / 6.f);
-  p = fmaf(p, z, 0.5f);
-  p = fmaf(p, z, 1.f);
-  p = fmaf(p, z, 1.f);
-  const float r = __int_as_float(__float_as_int(p) + (ni << 23));
-  return x != x ? x : (x < -86.5f ? 0.f : r);
+// Float exp through the hardware base-2 exponential: exp(x) = 2^(x log2 e) with the product
+// x log2 e carried as hi + lo (log2 e split into a float head and tail, the rounding of x * head
+// recovered by an FMA), ex2.approx on hi and the first-order factor 1 + lo ln 2 for the tail.
+// Inputs below -87.3 flush to zero (ftz), as the FP32 kernels need for exp(-eta r^2).
+__device__ __forceinline__ float exp_ex2(float x) {
+  constexpr float kL2eHi = 1.44269502162933349609375f;  // log2 e rounded to float
+  constexpr float kL2eLo = 1.925963033500011e-08f;      // log2 e - kL2eHi
+  const float hi = x * kL2eHi;
+  const float lo = fmaf(x, kL2eLo, fmaf(x, kL2eHi, -hi));
+  float r;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(hi));
+  return fmaf(r * lo, 0.693147180559945309f, r);
 }
 
 template <typename T> __device__ __forceinline__ T m_exp(T x);
-template <> __device__ __forceinline__ float m_exp<float>(float x) { return exp_cw(x); }
+template <> __device__ __forceinline__ float m_exp<float>(float x) { return exp_ex2(x); }
 template <> __device__ __forceinline__ double m_exp<double>(double x) { return exp(x); }
 template <typename T> __device__ __forceinline__ T m_cos(T x);
 template <> __device__ __forceinline__ float m_cos<float>(float x) { return cosf(x); }
