@@ -647,15 +647,17 @@ Layouts make_layouts(fnetg_ctx *ctx) {
 }
 
 // Rows per chunk: the tile's rows, halved until the chunk's buffers (and the staged weights)
-// leave room for two CTAs per SM (or reach four rows).
-template <typename T> int chunk_rows(const NetDesc &n, int tile_rows, bool keep_all, bool sw) {
+// fit the shared-memory budget per CTA (or reach four rows).
+template <typename T>
+int chunk_rows(const NetDesc &n, int tile_rows, bool keep_all, bool sw, size_t budget) {
   int RC = pad4(tile_rows);
-  while (RC > 4 && sizeof(T) * smem_plan(n, RC + 4, keep_all, sw).total > 100 * 1024) RC >>= 1;
+  while (RC > 4 && sizeof(T) * smem_plan(n, RC + 4, keep_all, sw).total > budget) RC >>= 1;
   return RC;
 }
 
 template <typename T> void prepare(fnetg_ctx *ctx, const Layouts &Lo, MlpArgs<T> &a,
-                                   bool keep_all, bool sw, size_t &smem) {
+                                   bool keep_all, bool sw, size_t &smem,
+                                   size_t budget = 100 * 1024) {
   a = MlpArgs<T>{};
   a.net = Lo.net;
   a.params = ctx->d_params.as<T>();
@@ -664,7 +666,7 @@ template <typename T> void prepare(fnetg_ctx *ctx, const Layouts &Lo, MlpArgs<T>
   a.tiles = ctx->d_tiles.as<int4>();
   a.ntiles = ctx->ntiles;
   a.bperm = ctx->d_bperm.as<int32_t>();
-  a.RC = chunk_rows<T>(Lo.net, ctx->tile_rows, keep_all, sw);
+  a.RC = chunk_rows<T>(Lo.net, ctx->tile_rows, keep_all, sw, budget);
   a.RCP = a.RC + 4;
   a.pl = smem_plan(Lo.net, a.RCP, keep_all, sw);
   smem = sizeof(T) * (size_t)a.pl.total;
@@ -672,8 +674,10 @@ template <typename T> void prepare(fnetg_ctx *ctx, const Layouts &Lo, MlpArgs<T>
 
 // ---- launch variants and their selection ----------------------------------------------
 // Variant v: v & 2 -> 256 threads with 4 x 2 register tiles (else 128 threads, 4 x 4);
-// v & 1 -> weights staged in shared memory.  The first launch of a kind for a network
-// shape times every variant that fits and keeps the fastest for the context.
+// v & 1 -> weights staged in shared memory; v & 4 -> chunks sized for four CTAs per SM
+// (50 KB of shared memory) instead of two.  The first launch of a kind for a network
+// shape times every variant that fits (the fastest of three launches each) and keeps the
+// fastest for the context.
 enum MlpKind { kMlpForward = 0, kMlpJacobian = 1, kMlpBackward = 2 };
 
 template <typename T, int OW, bool SW> void *mlp_kernel_ptr(int kind) {
@@ -695,7 +699,7 @@ template <typename T>
 int launch_variant(fnetg_ctx *ctx, int kind, int v, const Layouts &Lo, MlpArgs<T> &a) {
   size_t smem = 0;
   const MlpArgs<T> keep = a;
-  prepare<T>(ctx, Lo, a, kind != kMlpForward, (v & 1) != 0, smem);
+  prepare<T>(ctx, Lo, a, kind != kMlpForward, (v & 1) != 0, smem, (v & 4) ? 50 * 1024 : 100 * 1024);
   // outputs and inputs set by the caller survive the re-preparation
   a.out = keep.out;
   a.delta_out = keep.delta_out;
@@ -707,7 +711,7 @@ int launch_variant(fnetg_ctx *ctx, int kind, int v, const Layouts &Lo, MlpArgs<T
   a.jac64 = keep.jac64;
   a.jacT = keep.jacT;
   FNETG_CHECK(smem <= 227 * 1024, FNETG_E_UNSUPPORTED, "network too wide for shared memory");
-  void *k = mlp_variant<T>(kind, v);
+  void *k = mlp_variant<T>(kind, v & 3);
   const int threads = (v & 2) ? 256 : 128;
   FNETG_CUDA(raise_smem_limit(k, smem));
   int per_sm = 0;
@@ -723,7 +727,7 @@ int launch_variant(fnetg_ctx *ctx, int kind, int v, const Layouts &Lo, MlpArgs<T
 template <typename T> bool variant_fits(fnetg_ctx *ctx, const Layouts &Lo, int kind, int v) {
   MlpArgs<T> a;
   size_t smem = 0;
-  prepare<T>(ctx, Lo, a, kind != kMlpForward, (v & 1) != 0, smem);
+  prepare<T>(ctx, Lo, a, kind != kMlpForward, (v & 1) != 0, smem, (v & 4) ? 50 * 1024 : 100 * 1024);
   return smem <= 227 * 1024 && a.RC >= 16;
 }
 
@@ -738,18 +742,22 @@ int run_mlp(fnetg_ctx *ctx, int kind, const Layouts &Lo, MlpArgs<T> &a, const ch
   int &cfg = ctx->mlp_cfg[pi * 3 + kind];
   if (cfg < 0) {
     float best = 0.f;
-    for (int v = 0; v < 4; v++) {
+    for (int v = 0; v < 8; v++) {
       if (v != 0 && !variant_fits<T>(ctx, Lo, kind, v)) continue;
       MlpArgs<T> b = a;
       int rc = launch_variant<T>(ctx, kind, v, Lo, b);  // warm-up
       if (rc) return rc;
-      FNETG_CUDA(cudaEventRecord(ctx->ev0, ctx->stream));
-      rc = launch_variant<T>(ctx, kind, v, Lo, b);
-      if (rc) return rc;
-      FNETG_CUDA(cudaEventRecord(ctx->ev1, ctx->stream));
-      FNETG_CUDA(cudaEventSynchronize(ctx->ev1));
       float ms = 0.f;
-      FNETG_CUDA(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
+      for (int rep = 0; rep < 3; rep++) {  // the fastest of three launches
+        FNETG_CUDA(cudaEventRecord(ctx->ev0, ctx->stream));
+        rc = launch_variant<T>(ctx, kind, v, Lo, b);
+        if (rc) return rc;
+        FNETG_CUDA(cudaEventRecord(ctx->ev1, ctx->stream));
+        FNETG_CUDA(cudaEventSynchronize(ctx->ev1));
+        float t = 0.f;
+        FNETG_CUDA(cudaEventElapsedTime(&t, ctx->ev0, ctx->ev1));
+        ms = rep == 0 ? t : std::min(ms, t);
+      }
       if (cfg < 0 || ms < best) {
         best = ms;
         cfg = v;
