@@ -18,6 +18,17 @@ namespace fnetg {
 
 namespace {
 
+// Per-CTA copy of the radial descriptors: parameters (kappa, rs, eta) and
+// (list channel, cutoff class, atom id, type | output column << 8).
+template <typename T> struct RadDesc {
+  V4<T> p;
+  int4 m;
+};
+
+template <typename T> __host__ __device__ inline size_t raddesc_bytes(int nrad) {
+  return (sizeof(RadDesc<T>) * (size_t)nrad + 127) / 128 * 128;
+}
+
 template <typename T, int D>
 __global__ void __launch_bounds__(256) acsf_kernel(TileArgs<T> a) {
   extern __shared__ __align__(128) unsigned char smem[];
@@ -26,7 +37,15 @@ __global__ void __launch_bounds__(256) acsf_kernel(TileArgs<T> a) {
   const size_t tb =
       tile_bytes<T>(a.cap, a.nrcls, a.necls, a.nz, a.ncombo, a.n_mono, a.ng, false, a.ngroups > 0,
                     tile_etab(a, false));
-  Tile<T> t = carve_tile<T>(smem + tb * warp, a, false);
+  RadDesc<T> *rd = reinterpret_cast<RadDesc<T> *>(smem);
+  for (int g = threadIdx.x; g < a.nrad; g += blockDim.x) {
+    const GDesc d = a.rad[g];
+    const T *P = a.radp + 8 * g;
+    rd[g] = RadDesc<T>{V4<T>{P[1], P[2], P[3], (T)0},
+                       make_int4(d.chan1, d.rclass, d.atomid, d.type | (d.out << 8))};
+  }
+  __syncthreads();
+  Tile<T> t = carve_tile<T>(smem + raddesc_bytes<T>(a.nrad) + tb * warp, a, false);
   for (int64_t i = (int64_t)blockIdx.x * wpb + warp; i < a.natoms; i += (int64_t)gridDim.x * wpb) {
     const int64_t p0 = a.poff[i];
     const int np = (int)(a.pend[i] - p0);
@@ -53,21 +72,21 @@ __global__ void __launch_bounds__(256) acsf_kernel(TileArgs<T> a) {
         const int g = it >> sh, part = it - (g << sh);
         T acc = 0;
         if (it < items) {
-          const GDesc d = a.rad[g];
-          const T *P = a.radp + 8 * g;
-          const T kappa = P[1], rs = P[2], eta = P[3];
-          const uint16_t *lst = d.chan1 >= 0 ? t.lists + d.chan1 * a.cap : nullptr;
-          const int n = d.chan1 >= 0 ? t.cnt[d.chan1] : np;
+          const RadDesc<T> rdg = rd[g];
+          const T kappa = rdg.p.x, rs = rdg.p.y, eta = rdg.p.z;
+          const int chan1 = rdg.m.x, rclass = rdg.m.y, atomid = rdg.m.z, type = rdg.m.w & 0xff;
+          const uint16_t *lst = chan1 >= 0 ? t.lists + chan1 * a.cap : nullptr;
+          const int n = chan1 >= 0 ? t.cnt[chan1] : np;
           const int chunk = (((n + S - 1) >> sh) + 3) & ~3;
           const int k0 = min(n, part * chunk), k1 = min(n, k0 + chunk);
-          const T *fcr = t.fc + d.rclass * a.cap;
-          const T idi = atom_id<T>(a.ext, a.next, d.atomid, i);
+          const T *fcr = t.fc + rclass * a.cap;
+          const T idi = atom_id<T>(a.ext, a.next, atomid, i);
           auto term = [&](int q) -> T {
             const T r = t.u[q].w;
             T fc = fcr[q];
-            if (d.atomid > 0) fc *= idi * atom_id<T>(a.ext, a.next, d.atomid, t.pj[q]);
-            if (d.type == 1) return fc;
-            if (d.type == 2) {
+            if (atomid > 0) fc *= idi * atom_id<T>(a.ext, a.next, atomid, t.pj[q]);
+            if (type == 1) return fc;
+            if (type == 2) {
               const T x = r - rs;
               return m_exp<T>(-(eta * (x * x))) * fc;
             }
@@ -93,7 +112,7 @@ __global__ void __launch_bounds__(256) acsf_kernel(TileArgs<T> a) {
           acc = (acc0 + acc1) + (acc2 + acc3);
         }
         for (int o = 1; o < S; o <<= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-        if (it < items && part == 0) a.feat[row * a.nf + a.rad[g].out] = acc;
+        if (it < items && part == 0) a.feat[row * a.nf + (rd[g].m.w >> 8)] = acc;
       }
     }
     // ---- integer-xi G5 through moments: lanes over functions
@@ -320,7 +339,8 @@ template <typename T, int D> int launch_acsf_d(fnetg_ctx *ctx, TileArgs<T> &a) {
                     tile_etab(a, false));
   int wpb = 1, per_sm = 1;
   size_t smem = 0;
-  const cudaError_t err = pick_warps(acsf_kernel<T, D>, 0, tb, wpb, smem, per_sm);
+  const cudaError_t err =
+      pick_warps(acsf_kernel<T, D>, raddesc_bytes<T>(a.nrad), tb, wpb, smem, per_sm);
   FNETG_CHECK(err != cudaErrorInvalidValue, FNETG_E_UNSUPPORTED,
               "neighbour tile of one atom exceeds shared memory");
   FNETG_CUDA(err);

@@ -528,6 +528,10 @@ int fnetg_set_gfunctions(fnetg_ctx *ctx, int32_t ng, const fnetg_gfunc *g) {
       ctx->rad_seg[c + 2] = pos;
     }
   }
+  // force kernel fast path: every radial function a G2 without atom id, one cutoff class
+  ctx->rad_fast = ctx->h_rad.empty() ? -1 : ctx->h_rad[0].rclass;
+  for (auto &d : ctx->h_rad)
+    if (d.type != 2 || d.atomid != 0 || d.rclass != ctx->rad_fast) ctx->rad_fast = -1;
   // G5 functions with a small integer xi take the moment form; the rest (G4, other xi) the
   // triplet sweep
   std::vector<GDesc> mom, trip;
@@ -630,6 +634,8 @@ int fnetg_set_gfunctions(fnetg_ctx *ctx, int32_t ng, const fnetg_gfunc *g) {
       epc.insert(epc.end(), ctx->h_mpc.begin() + (size_t)f * (kMaxMomentDegree + 1),
                  ctx->h_mpc.begin() + (size_t)(f + 1) * (kMaxMomentDegree + 1));
     ctx->h_mpc = epc;
+    ctx->n_qgpack = (int)pack.size();
+    ctx->n_qgent = (int)qg_f.size();
     FNETG_CUDA(ctx->d_qgroups.ensure(sizeof(int32_t) * std::max<size_t>(pack.size(), 1)));
     FNETG_CUDA(copy_sync(ctx, ctx->d_qgroups.p, pack.data(), sizeof(int32_t) * pack.size(),
                           cudaMemcpyHostToDevice));

@@ -227,6 +227,23 @@ template <typename T> __host__ __device__ inline size_t radtab_bytes(int nrad) {
   return ((size_t)sizeof(RadEntry<T>) * nrad + 127) / 128 * 128;
 }
 
+__host__ __device__ inline size_t align16(size_t b) { return (b + 15) / 16 * 16; }
+
+// per-CTA copies of the factorised-adjoint tables: the group pack, the combo index and the
+// degree coefficients (read in dependent chains per atom: kept out of global memory)
+template <typename T> __host__ __device__ inline size_t adjtab_bytes(const TileArgs<T> &a) {
+  if (a.ncombo <= 0) return 0;
+  const size_t b = align16(sizeof(int32_t) * a.nqg_pack) +
+                   align16(sizeof(int32_t) * (a.nz + 1) * a.necls) +
+                   align16(sizeof(T) * a.nqg_ent * (kMaxMomentDegree + 1));
+  return (b + 127) / 128 * 128;  // the tiles that follow stay 128-byte aligned
+}
+
+// per-warp radial coefficient table of the fast path: (rs, eta, J, J eta) per function
+template <typename T> __host__ __device__ inline size_t radw_bytes(const TileArgs<T> &a) {
+  return a.rad_fast >= 0 ? (sizeof(V4<T>) * a.nrad + 127) / 128 * 128 : 0;
+}
+
 template <typename T, int D>
 __global__ void __launch_bounds__(256, 3) forces_kernel(TileArgs<T> a) {
   extern __shared__ __align__(128) unsigned char smem[];
@@ -241,8 +258,22 @@ __global__ void __launch_bounds__(256, 3) forces_kernel(TileArgs<T> a) {
     rt[g] = RadEntry<T>{d.type == 3 ? P[1] : P[2], P[3], d.out,
                         d.type | (d.rclass << 4) | (d.atomid << 8)};
   }
+  constexpr int KD = kMaxMomentDegree + 1;
+  unsigned char *adj = smem + radtab_bytes<T>(a.nrad);
+  int32_t *s_qg = reinterpret_cast<int32_t *>(adj);
+  int32_t *s_cidx = reinterpret_cast<int32_t *>(adj + align16(sizeof(int32_t) * a.nqg_pack));
+  T *s_mpc = reinterpret_cast<T *>(adj + align16(sizeof(int32_t) * a.nqg_pack) +
+                                   align16(sizeof(int32_t) * (a.nz + 1) * a.necls));
+  if (a.ncombo > 0) {
+    for (int t = threadIdx.x; t < a.nqg_pack; t += blockDim.x) s_qg[t] = a.qg[t];
+    for (int t = threadIdx.x; t < (a.nz + 1) * a.necls; t += blockDim.x) s_cidx[t] = a.cidx[t];
+    for (int t = threadIdx.x; t < a.nqg_ent * KD; t += blockDim.x) s_mpc[t] = a.mpc[t];
+  }
   __syncthreads();
-  Tile<T> tl = carve_tile<T>(smem + radtab_bytes<T>(a.nrad) + tb * warp, a, true);
+  const size_t fixed = radtab_bytes<T>(a.nrad) + adjtab_bytes<T>(a);
+  unsigned char *mine = smem + fixed + (tb + radw_bytes<T>(a)) * warp;
+  Tile<T> tl = carve_tile<T>(mine, a, true);
+  V4<T> *wt = reinterpret_cast<V4<T> *>(mine + tb);
   // degrees and multinomial weights of this lane's monomials (lane, lane + 32)
   const int mdeg0 = lane < kMaxMono ? kMonoTab[lane][0] + kMonoTab[lane][1] + kMonoTab[lane][2] : 0;
   const int mdeg1 = lane + 32 < kMaxMono
@@ -255,6 +286,53 @@ __global__ void __launch_bounds__(256, 3) forces_kernel(TileArgs<T> a) {
     const int np = (int)(a.pend[i] - p0);
     for (int g = lane; g < a.ng; g += 32) tl.jv[g] = a.J[i * a.nf + g];
     stage_tile<T>(a, tl, i, p0, np, lane, true);
+    if (a.rad_fast >= 0) {
+      // ---- radial, fast path (G2 only, one cutoff class, no atom ids): per pair
+      //   dE/dr = dfc sum_g J_g e_g - 2 fc sum_g J_g eta_g x_g e_g,  x_g = r - rs_g,
+      //   e_g = exp(-eta_g x_g^2), over the all-atom functions and the pair's species' own
+      for (int g = lane; g < a.nrad; g += 32) {
+        const RadEntry<T> re = rt[g];
+        const T J = tl.jv[re.out];
+        wt[g] = V4<T>{re.p0, re.p1, J, J * re.p1};
+      }
+      __syncwarp();
+      const int rcl = a.rad_fast;
+      for (int q = lane; q < np; q += 32) {
+        const uint32_t inf = tl.info[q];
+        const int code = (int)(inf & 0xff);
+        if ((inf >> 8) & 1u) continue;  // self images do not move relative to the centre
+        const T r = tl.u[q].w;
+        T s1a = 0, s1b = 0, s2a = 0, s2b = 0;
+        const int nseg = code < a.nz ? 2 : 1;
+        for (int sg = 0; sg < nseg; sg++) {
+          const int g0 = sg == 0 ? 0 : a.rad_seg[code + 1];
+          const int g1 = sg == 0 ? a.rad_seg[1] : a.rad_seg[code + 2];
+          int g = g0;
+          for (; g + 2 <= g1; g += 2) {
+            const V4<T> w0 = wt[g], w1 = wt[g + 1];
+            const T x0 = r - w0.x, x1 = r - w1.x;
+            const T e0 = m_exp<T>(-(w0.y * (x0 * x0))), e1 = m_exp<T>(-(w1.y * (x1 * x1)));
+            s1a += w0.z * e0;
+            s2a += w0.w * (x0 * e0);
+            s1b += w1.z * e1;
+            s2b += w1.w * (x1 * e1);
+          }
+          if (g < g1) {
+            const V4<T> w0 = wt[g];
+            const T x0 = r - w0.x;
+            const T e0 = m_exp<T>(-(w0.y * (x0 * x0)));
+            s1a += w0.z * e0;
+            s2a += w0.w * (x0 * e0);
+          }
+        }
+        const T fc = tl.fc[rcl * a.cap + q], dfc = tl.dfc[rcl * a.cap + q];
+        const T dsum = dfc * (s1a + s1b) - (T)2 * fc * (s2a + s2b);
+        const V4<T> u = tl.u[q];
+        tl.w[q].x += dsum * u.x;
+        tl.w[q].y += dsum * u.y;
+        tl.w[q].z += dsum * u.z;
+      }
+    } else
     // ---- radial: lanes over pairs, each over the all-atom functions and its species' own
     for (int q = lane; q < np; q += 32) {
       const uint32_t inf = tl.info[q];
@@ -320,23 +398,22 @@ __global__ void __launch_bounds__(256, 3) forces_kernel(TileArgs<T> a) {
       //   h_g(m) = sum_{f in F_g} J_out(f) pc_f(m),
       //   Qc[z][e](alpha) = mult(alpha) sum_{k in {list z, all atoms}} sum_{g of k}
       //                     h_g(|alpha|) M_{ko(g)}(alpha).
-      constexpr int KD = kMaxMomentDegree + 1;
-      const int32_t *qg_off = a.qg, *qg_ko = a.qg + a.ncombo + 1;
+      const int32_t *qg_off = s_qg, *qg_ko = s_qg + a.ncombo + 1;
       const int32_t *qg_eoff = qg_ko + a.nqg, *qg_out = qg_eoff + a.nqg + 1;
       T *H = tl.Q;
       for (int it = lane; it < a.nqg * KD; it += 32) {
         const int g = it / KD, m = it - g * KD;
         T acc = 0;
         for (int e = qg_eoff[g]; e < qg_eoff[g + 1]; e++)
-          acc += tl.jv[qg_out[e]] * a.mpc[e * KD + m];
+          acc += tl.jv[qg_out[e]] * s_mpc[e * KD + m];
         H[it] = acc;
       }
       __syncwarp();
       // this lane's monomials lane and lane + 32 (degree and weight fixed per kernel)
       for (int zz = 0; zz <= a.nz; zz++)
         for (int e = 0; e < a.necls; e++) {
-          const int ks = zz < a.nz ? a.cidx[(zz + 1) * a.necls + e] : -1;
-          const int ka = a.cidx[e];
+          const int ks = zz < a.nz ? s_cidx[(zz + 1) * a.necls + e] : -1;
+          const int ka = s_cidx[e];
           T v0 = 0, v1 = 0;
           for (int side = 0; side < 2; side++) {
             const int k = side == 0 ? ks : ka;
@@ -462,6 +539,9 @@ template <typename T> void fill_tile_args_forces(fnetg_ctx *ctx, TileArgs<T> &a)
   a.qent = ctx->d_qent.as<int32_t>();
   a.qg = ctx->d_qgroups.as<int32_t>();
   a.nqg = ctx->n_qgroups;
+  a.nqg_pack = ctx->n_qgpack;
+  a.nqg_ent = ctx->n_qgent;
+  a.rad_fast = ctx->rad_fast;
   a.mpc = static_cast<const T *>(dbl ? ctx->d_mpc_d.p : ctx->d_mpc_f.p);
   a.combo = ctx->d_combo.as<int32_t>();
   a.ncombo = ctx->n_combo;
@@ -475,10 +555,11 @@ template <typename T, int D> int launch_forces_d(fnetg_ctx *ctx, TileArgs<T> &a,
   const int64_t N = ctx->N;
   const size_t tb = tile_bytes<T>(a.cap, a.nrcls, a.necls, a.nz, a.ncombo, a.n_mono, a.ng, true, a.ngroups > 0,
                     tile_etab(a, true), tile_qwords(a));
-  const size_t rb = radtab_bytes<T>(a.nrad);
+  const size_t fixed = radtab_bytes<T>(a.nrad) + adjtab_bytes<T>(a);
   int wpb = 1, per_sm = 1;
   size_t smem = 0;
-  const cudaError_t err = pick_warps(forces_kernel<T, D>, rb, tb, wpb, smem, per_sm);
+  const cudaError_t err =
+      pick_warps(forces_kernel<T, D>, fixed, tb + radw_bytes<T>(a), wpb, smem, per_sm);
   FNETG_CHECK(err != cudaErrorInvalidValue, FNETG_E_UNSUPPORTED,
               "neighbour tile of one atom exceeds shared memory");
   FNETG_CUDA(err);

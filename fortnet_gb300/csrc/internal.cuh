@@ -214,6 +214,8 @@ struct fnetg_ctx {
   int64_t nparams = 0;
   std::vector<int64_t> woff, boff;
   std::vector<int64_t> h_sp_tile0;  // [nsp+1] first MLP tile of every species
+  int n_qgpack = 0, n_qgent = 0;  // ints of the adjoint group pack, entries of its coefficients
+  int rad_fast = -1;  // every radial function a G2 without atom id in this cutoff class (else -1)
   // MLP launch variants picked by timing on first use, per precision and kernel kind
   // (forward, Jacobian, backward), for the network shape mlp_dims
   int mlp_cfg[6] = {-1, -1, -1, -1, -1, -1};

@@ -182,6 +182,9 @@ template <typename T> struct TileArgs {
   const int32_t *qg;
   int nqg;
   const T *mpc;
+  int nqg_pack, nqg_ent;  // ints of the pack, entries of mpc (both staged per CTA)
+  int rad_fast;           // forces: every radial function a G2 without atom id in this
+                          // cutoff class (per-warp coefficient table), else -1
   // moment cache [natoms][ncombo][n_mono]: written by the ACSF kernel (mom != null), read by
   // the force kernel when mom_cached
   T *mom;
