@@ -29,6 +29,22 @@ template <typename T> __host__ __device__ inline size_t raddesc_bytes(int nrad) 
   return (sizeof(RadDesc<T>) * (size_t)nrad + 127) / 128 * 128;
 }
 
+constexpr int kKD = kMaxMomentDegree + 1;
+
+// Per-CTA tables of the factorised G5 evaluation: combo pairs (int2), functions (pair, output
+// column), degree coefficients pc_f(m) and the multinomial weights of the monomials.
+template <typename T> __host__ __device__ inline size_t g5tab_bytes(const TileArgs<T> &a) {
+  if (a.nmf <= 0) return 0;
+  const size_t b = sizeof(int32_t) * 2 * (size_t)(a.nmpair + a.nmf) +
+                   sizeof(T) * ((size_t)a.nmf * kKD + kMaxMono);
+  return (b + 127) / 128 * 128;
+}
+
+// per-warp degree sums S_p(m) = sum_{|alpha| = m} mult(alpha) M_k1(alpha) M_k2(alpha)
+template <typename T> __host__ __device__ inline size_t g5sum_bytes(const TileArgs<T> &a) {
+  return a.nmf > 0 ? (sizeof(T) * (size_t)a.nmpair * kKD + 127) / 128 * 128 : 0;
+}
+
 template <typename T, int D>
 __global__ void __launch_bounds__(256) acsf_kernel(TileArgs<T> a) {
   extern __shared__ __align__(128) unsigned char smem[];
@@ -44,8 +60,25 @@ __global__ void __launch_bounds__(256) acsf_kernel(TileArgs<T> a) {
     rd[g] = RadDesc<T>{V4<T>{P[1], P[2], P[3], (T)0},
                        make_int4(d.chan1, d.rclass, d.atomid, d.type | (d.out << 8))};
   }
+  // int2 tables first (8-byte aligned from the 128-byte aligned start), then the T tables
+  unsigned char *g5 = smem + raddesc_bytes<T>(a.nrad);
+  int2 *s_pair = reinterpret_cast<int2 *>(g5);
+  int2 *s_mf = s_pair + a.nmpair;
+  T *s_fpc = reinterpret_cast<T *>(s_mf + a.nmf);
+  T *s_mult = s_fpc + (size_t)a.nmf * kKD;
+  if (D > 0 && a.nmf > 0) {
+    for (int t2 = threadIdx.x; t2 < a.nmf * kKD; t2 += blockDim.x) s_fpc[t2] = a.fpc[t2];
+    for (int t2 = threadIdx.x; t2 < kMaxMono; t2 += blockDim.x) s_mult[t2] = (T)kMonoMult[t2];
+    for (int t2 = threadIdx.x; t2 < a.nmpair; t2 += blockDim.x)
+      s_pair[t2] = make_int2(a.mpair[2 * t2], a.mpair[2 * t2 + 1]);
+    for (int t2 = threadIdx.x; t2 < a.nmf; t2 += blockDim.x)
+      s_mf[t2] = make_int2(a.mfunc[t2].pair, a.mfunc[t2].out);
+  }
   __syncthreads();
-  Tile<T> t = carve_tile<T>(smem + raddesc_bytes<T>(a.nrad) + tb * warp, a, false);
+  const size_t fixed = raddesc_bytes<T>(a.nrad) + g5tab_bytes<T>(a);
+  unsigned char *mine = smem + fixed + (tb + g5sum_bytes<T>(a)) * warp;
+  Tile<T> t = carve_tile<T>(mine, a, false);
+  T *S = reinterpret_cast<T *>(mine + tb);
   for (int64_t i = (int64_t)blockIdx.x * wpb + warp; i < a.natoms; i += (int64_t)gridDim.x * wpb) {
     const int64_t p0 = a.poff[i];
     const int np = (int)(a.pend[i] - p0);
@@ -115,14 +148,27 @@ __global__ void __launch_bounds__(256) acsf_kernel(TileArgs<T> a) {
         if (it < items && part == 0) a.feat[row * a.nf + (rd[g].m.w >> 8)] = acc;
       }
     }
-    // ---- integer-xi G5 through moments: lanes over functions
-    for (int f = lane; f < a.nmf; f += 32) {
-      const MFunc mf = a.mfunc[f];
-      const T *cf = a.mcoef + (int64_t)f * a.n_mono;
-      const T *M1 = t.M + mf.k1 * a.n_mono, *M2 = t.M + mf.k2 * a.n_mono;
-      T acc = 0;
-      for (int al = 0; al < a.n_mono; al++) acc += cf[al] * M1[al] * M2[al];
-      a.feat[row * a.nf + mf.out] = acc;
+    // ---- integer-xi G5 through moments, factorised: coef_f(alpha) = mult(alpha) pc_f(|alpha|),
+    // so G_f = sum_m pc_f(m) S_p(m) with the degree sums S_p of the function's combo pair
+    if (D > 0 && a.nmf > 0) {
+      for (int it = lane; it < a.nmpair * kKD; it += 32) {
+        const int p = it / kKD, m = it - p * kKD;
+        const int2 kk = s_pair[p];
+        const T *M1 = t.M + kk.x * a.n_mono, *M2 = t.M + kk.y * a.n_mono;
+        const int a0 = m * (m + 1) * (m + 2) / 6, a1 = min(a.n_mono, (m + 1) * (m + 2) * (m + 3) / 6);
+        T acc = 0;
+        for (int al = a0; al < a1; al++) acc += s_mult[al] * (M1[al] * M2[al]);
+        S[it] = acc;
+      }
+      __syncwarp();
+      for (int f = lane; f < a.nmf; f += 32) {
+        const int2 mf = s_mf[f];
+        const T *pc = s_fpc + f * kKD, *Sp = S + mf.x * kKD;
+        T acc = 0;
+#pragma unroll
+        for (int m = 0; m < kKD; m++) acc += pc[m] * Sp[m];
+        a.feat[row * a.nf + mf.y] = acc;
+      }
     }
     // ---- remaining angular groups: lanes over triplets
     for (int gi = 0; gi < a.ngroups; gi++) {
@@ -320,9 +366,9 @@ template <typename T> void fill_tile_args(fnetg_ctx *ctx, TileArgs<T> &a) {
   a.cap = std::max(32, (ctx->max_pairs + 31) / 32 * 32);
   a.mfunc = ctx->d_mfunc.as<MFunc>();
   a.nmf = (int)ctx->h_mfunc.size();
-  a.mcoef = static_cast<const T *>(dbl ? ctx->d_mcoef.p : ctx->d_mcoef_f.p);
-  a.qoff = ctx->d_qoff.as<int32_t>();
-  a.qent = ctx->d_qent.as<int32_t>();
+  a.mpair = ctx->d_mpair.as<int32_t>();
+  a.nmpair = (int)ctx->h_mpair.size() / 2;
+  a.fpc = static_cast<const T *>(sizeof(T) == 8 ? ctx->d_fpc_d.p : ctx->d_fpc_f.p);
   a.combo = ctx->d_combo.as<int32_t>();
   a.ncombo = ctx->n_combo;
   a.cidx = ctx->d_cidx.as<int32_t>();
@@ -339,8 +385,8 @@ template <typename T, int D> int launch_acsf_d(fnetg_ctx *ctx, TileArgs<T> &a) {
                     tile_etab(a, false));
   int wpb = 1, per_sm = 1;
   size_t smem = 0;
-  const cudaError_t err =
-      pick_warps(acsf_kernel<T, D>, raddesc_bytes<T>(a.nrad), tb, wpb, smem, per_sm);
+  const cudaError_t err = pick_warps(acsf_kernel<T, D>, raddesc_bytes<T>(a.nrad) + g5tab_bytes<T>(a),
+                                     tb + g5sum_bytes<T>(a), wpb, smem, per_sm);
   FNETG_CHECK(err != cudaErrorInvalidValue, FNETG_E_UNSUPPORTED,
               "neighbour tile of one atom exceeds shared memory");
   FNETG_CUDA(err);

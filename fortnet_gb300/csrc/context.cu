@@ -541,7 +541,6 @@ int fnetg_set_gfunctions(fnetg_ctx *ctx, int32_t ng, const fnetg_gfunc *g) {
   }
   ang = trip;
   ctx->h_mfunc.clear();
-  ctx->h_mcoef.clear();
   ctx->h_combo.clear();
   ctx->mom_degree = 0;
   for (auto &d : mom) ctx->mom_degree = std::max(ctx->mom_degree, d.xi_int);
@@ -558,11 +557,6 @@ int fnetg_set_gfunctions(fnetg_ctx *ctx, int32_t ng, const fnetg_gfunc *g) {
     }
     return slot;
   };
-  // monomials ordered by degree, then by descending x and y exponents
-  std::vector<std::array<int, 3>> mono;
-  for (int m = 0; m <= D; m++)
-    for (int a = m; a >= 0; a--)
-      for (int b = m - a; b >= 0; b--) mono.push_back({a, b, m - a - b});
   auto fact = [](int n) {
     double r = 1.0;
     for (int k = 2; k <= n; k++) r *= k;
@@ -574,16 +568,6 @@ int fnetg_set_gfunctions(fnetg_ctx *ctx, int32_t ng, const fnetg_gfunc *g) {
     mf.k2 = combo_of(d.chan2, d.eclass);
     mf.out = d.out;
     ctx->h_mfunc.push_back(mf);
-    for (auto &al : mono) {
-      const int m = al[0] + al[1] + al[2];
-      double c = 0.0;
-      if (m <= d.xi_int) {
-        const double binom = fact(d.xi_int) / (fact(m) * fact(d.xi_int - m));
-        const double w = fact(m) / (fact(al[0]) * fact(al[1]) * fact(al[2]));
-        c = d.pref * binom * std::pow(d.lambda, m) * w;
-      }
-      ctx->h_mcoef.push_back(c);
-    }
   }
   ctx->n_combo = (int)ctx->h_combo.size() / 2;
   // Degree coefficients pc_f(m) = 2^(1-xi) C(xi, m) lambda^m (coef_f(alpha) = pc_f(|alpha|)
@@ -595,6 +579,34 @@ int fnetg_set_gfunctions(fnetg_ctx *ctx, int32_t ng, const fnetg_gfunc *g) {
     for (int m = 0; m <= d.xi_int; m++)
       ctx->h_mpc[f * (kMaxMomentDegree + 1) + m] =
           d.pref * (fact(d.xi_int) / (fact(m) * fact(d.xi_int - m))) * std::pow(d.lambda, m);
+  }
+  ctx->h_fpc = ctx->h_mpc;  // per function (h_mpc is regrouped for the adjoint below)
+  ctx->h_mpair.clear();
+  for (auto &mf : ctx->h_mfunc) {
+    const int lo = std::min(mf.k1, mf.k2), hi = std::max(mf.k1, mf.k2);
+    int pidx = -1;
+    for (size_t q = 0; q + 1 < ctx->h_mpair.size(); q += 2)
+      if (ctx->h_mpair[q] == lo && ctx->h_mpair[q + 1] == hi) pidx = (int)(q / 2);
+    if (pidx < 0) {
+      pidx = (int)ctx->h_mpair.size() / 2;
+      ctx->h_mpair.push_back(lo);
+      ctx->h_mpair.push_back(hi);
+    }
+    mf.pair = pidx;
+  }
+  {
+    FNETG_CUDA(ctx->d_mpair.ensure(sizeof(int32_t) * std::max<size_t>(ctx->h_mpair.size(), 2)));
+    FNETG_CUDA(ctx->d_fpc_d.ensure(sizeof(double) * std::max<size_t>(ctx->h_fpc.size(), 1)));
+    FNETG_CUDA(ctx->d_fpc_f.ensure(sizeof(float) * std::max<size_t>(ctx->h_fpc.size(), 1)));
+    if (!ctx->h_mpair.empty()) {
+      const std::vector<float> pf(ctx->h_fpc.begin(), ctx->h_fpc.end());
+      FNETG_CUDA(copy_sync(ctx, ctx->d_mpair.p, ctx->h_mpair.data(),
+                            sizeof(int32_t) * ctx->h_mpair.size(), cudaMemcpyHostToDevice));
+      FNETG_CUDA(copy_sync(ctx, ctx->d_fpc_d.p, ctx->h_fpc.data(),
+                            sizeof(double) * ctx->h_fpc.size(), cudaMemcpyHostToDevice));
+      FNETG_CUDA(copy_sync(ctx, ctx->d_fpc_f.p, pf.data(), sizeof(float) * pf.size(),
+                            cudaMemcpyHostToDevice));
+    }
   }
   std::vector<int32_t> qg_off(ctx->n_combo + 1, 0), qg_ko, qg_foff(1, 0), qg_f;
   for (int k = 0; k < ctx->n_combo; k++) {
@@ -650,45 +662,12 @@ int fnetg_set_gfunctions(fnetg_ctx *ctx, int32_t ng, const fnetg_gfunc *g) {
     }
   }
   // per-combo list of the moment functions whose Q (adjoint moment) it receives
-  std::vector<int32_t> qoff(ctx->n_combo + 1, 0), qent;
-  for (int k = 0; k < ctx->n_combo; k++) {
-    qoff[k] = (int32_t)qent.size() / 2;
-    for (size_t f = 0; f < ctx->h_mfunc.size(); f++) {
-      const MFunc &mf = ctx->h_mfunc[f];
-      if (mf.k1 == k) {
-        qent.push_back((int32_t)f);
-        qent.push_back(mf.k2);
-      }
-      if (mf.k2 == k) {
-        qent.push_back((int32_t)f);
-        qent.push_back(mf.k1);
-      }
-    }
-  }
-  qoff[ctx->n_combo] = (int32_t)qent.size() / 2;
-  FNETG_CUDA(ctx->d_qoff.ensure(sizeof(int32_t) * (ctx->n_combo + 1)));
-  FNETG_CUDA(ctx->d_qent.ensure(sizeof(int32_t) * std::max<size_t>(qent.size(), 2)));
-  FNETG_CUDA(copy_sync(ctx, ctx->d_qoff.p, qoff.data(), sizeof(int32_t) * qoff.size(),
-                        cudaMemcpyHostToDevice));
-  if (!qent.empty())
-    FNETG_CUDA(copy_sync(ctx, ctx->d_qent.p, qent.data(), sizeof(int32_t) * qent.size(),
-                          cudaMemcpyHostToDevice));
-  {
-    std::vector<float> cf(ctx->h_mcoef.begin(), ctx->h_mcoef.end());
-    FNETG_CUDA(ctx->d_mcoef_f.ensure(sizeof(float) * std::max<size_t>(cf.size(), 1)));
-    if (!cf.empty())
-      FNETG_CUDA(copy_sync(ctx, ctx->d_mcoef_f.p, cf.data(), sizeof(float) * cf.size(),
-                            cudaMemcpyHostToDevice));
-  }
   FNETG_CUDA(ctx->d_mfunc.ensure(sizeof(MFunc) * std::max<size_t>(ctx->h_mfunc.size(), 1)));
-  FNETG_CUDA(ctx->d_mcoef.ensure(sizeof(double) * std::max<size_t>(ctx->h_mcoef.size(), 1)));
   FNETG_CUDA(ctx->d_combo.ensure(sizeof(int32_t) * std::max<size_t>(ctx->h_combo.size(), 2)));
   FNETG_CUDA(ctx->d_cidx.ensure(sizeof(int32_t) * std::max<size_t>(ctx->h_cidx.size(), 1)));
   if (!ctx->h_mfunc.empty()) {
     FNETG_CUDA(copy_sync(ctx, ctx->d_mfunc.p, ctx->h_mfunc.data(), sizeof(MFunc) * ctx->h_mfunc.size(),
                           cudaMemcpyHostToDevice));
-    FNETG_CUDA(copy_sync(ctx, ctx->d_mcoef.p, ctx->h_mcoef.data(),
-                          sizeof(double) * ctx->h_mcoef.size(), cudaMemcpyHostToDevice));
     FNETG_CUDA(copy_sync(ctx, ctx->d_combo.p, ctx->h_combo.data(),
                           sizeof(int32_t) * ctx->h_combo.size(), cudaMemcpyHostToDevice));
   }

@@ -534,9 +534,6 @@ template <typename T> void fill_tile_args_forces(fnetg_ctx *ctx, TileArgs<T> &a)
   a.cap = std::max(32, (ctx->max_pairs + 31) / 32 * 32);
   a.mfunc = ctx->d_mfunc.as<MFunc>();
   a.nmf = (int)ctx->h_mfunc.size();
-  a.mcoef = static_cast<const T *>(dbl ? ctx->d_mcoef.p : ctx->d_mcoef_f.p);
-  a.qoff = ctx->d_qoff.as<int32_t>();
-  a.qent = ctx->d_qent.as<int32_t>();
   a.qg = ctx->d_qgroups.as<int32_t>();
   a.nqg = ctx->n_qgroups;
   a.nqg_pack = ctx->n_qgpack;

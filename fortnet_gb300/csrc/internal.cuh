@@ -55,7 +55,7 @@ constexpr int kMaxMono = 35;  // monomials of degree <= 4 in three variables
 struct MFunc {
   int k1, k2;  // moment combos (list, eta class) of the two neighbour lists
   int out;     // output column
-  int pad;
+  int pair;    // index of the combo pair (min(k1, k2), max(k1, k2)) among the distinct pairs
 };
 
 // Stream-ordered allocation from a memory pool, for contexts driven by one host thread each
@@ -166,16 +166,15 @@ struct fnetg_ctx {
   // moment form of the integer-xi G5 functions
   int mom_degree = 0, n_mono = 0, n_combo = 0;
   std::vector<fnetg::MFunc> h_mfunc;
-  std::vector<double> h_mcoef;      // [nmf][n_mono]
   std::vector<int32_t> h_combo;     // [ncombo][2] (list code or -1 = all, eta class)
   std::vector<int32_t> h_cidx;      // [(nz+1) * necls] combo index, -1 if unused
-  fnetg::DBuf d_mfunc, d_mcoef, d_combo, d_cidx, d_qoff, d_qent;
+  fnetg::DBuf d_mfunc, d_combo, d_cidx;
   std::vector<double> h_mpc;    // [entries][kMaxMomentDegree + 1] degree coefficients of the
                                 // adjoint group entries
   int n_qgroups = 0;            // adjoint partner groups over all combos
   fnetg::DBuf d_qgroups, d_mpc_d, d_mpc_f;
   // kernel parameter copies in both arithmetic widths: [rcut, kappa, rs, eta, lambda, xi, pref, 0]
-  fnetg::DBuf d_radpar_f, d_radpar_d, d_angpar_f, d_angpar_d, d_mcoef_f, d_ecls_eta_f, d_rcls_f;
+  fnetg::DBuf d_radpar_f, d_radpar_d, d_angpar_f, d_angpar_d, d_ecls_eta_f, d_rcls_f;
   fnetg::DBuf d_rad, d_ang, d_groups, d_code, d_ecls_eta, d_ecls_rclass, d_ecls_atomid,
       d_rcls;
 
@@ -215,6 +214,11 @@ struct fnetg_ctx {
   std::vector<int64_t> woff, boff;
   std::vector<int64_t> h_sp_tile0;  // [nsp+1] first MLP tile of every species
   int n_qgpack = 0, n_qgent = 0;  // ints of the adjoint group pack, entries of its coefficients
+  // value kernel: distinct moment-combo pairs (k1 <= k2) of the G5 moment functions and every
+  // function's degree coefficients pc_f(m) (MFunc::pad holds the function's pair)
+  std::vector<int32_t> h_mpair;
+  std::vector<double> h_fpc;
+  fnetg::DBuf d_mpair, d_fpc_d, d_fpc_f;
   int rad_fast = -1;  // every radial function a G2 without atom id in this cutoff class (else -1)
   // MLP launch variants picked by timing on first use, per precision and kernel kind
   // (forward, Jacobian, backward), for the network shape mlp_dims

@@ -169,9 +169,6 @@ template <typename T> struct TileArgs {
   // moment form
   const MFunc *mfunc;
   int nmf;
-  const T *mcoef;         // [nmf][n_mono]
-  const int32_t *qoff;    // [ncombo+1] per-combo adjoint lists
-  const int32_t *qent;    // (function, other combo) pairs
   const int32_t *combo;   // [ncombo][2]
   int ncombo;
   const int32_t *cidx;    // [(nz+1)*necls]
@@ -183,6 +180,11 @@ template <typename T> struct TileArgs {
   int nqg;
   const T *mpc;
   int nqg_pack, nqg_ent;  // ints of the pack, entries of mpc (both staged per CTA)
+  // value kernel, factorised G5: distinct combo pairs [nmpair][2], coefficients
+  // fpc[nmf][kMaxMomentDegree + 1]
+  const int32_t *mpair;
+  int nmpair;
+  const T *fpc;
   int rad_fast;           // forces: every radial function a G2 without atom id in this
                           // cutoff class (per-warp coefficient table), else -1
   // moment cache [natoms][ncombo][n_mono]: written by the ACSF kernel (mom != null), read by
