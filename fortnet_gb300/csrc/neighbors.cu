@@ -178,7 +178,7 @@ template <typename T, bool kFill>
 __global__ void __launch_bounds__(256) nb_kernel(NbArgs a) {
   __shared__ int blk_max;
   __shared__ unsigned long long blk_sum;
-  __shared__ int2 queue_all[kNbWarps][64];
+  __shared__ int2 queue_all[kNbWarps][128];  // up to 31 pending + 64 new accepted
   if (threadIdx.x == 0) {
     blk_max = 0;
     blk_sum = 0;
@@ -221,18 +221,17 @@ __global__ void __launch_bounds__(256) nb_kernel(NbArgs a) {
         }
         if (dd > a.rc2_hi) continue;
       }
-      for (int base = 0; base < tcount; base += 32) {
-        bool ok = false;
-        int jl = 0;
-        float df = 0.f;
-        V4<float> cjf{0.f, 0.f, 0.f, 0.f};
-        if (base + lane < tcount) {
-          jl = il + tstart + base + lane;
+      // candidates 64 at a time, two per lane: the shifted centre is formed once per image
+      const float px = cif.x - ch.x, py = cif.y - ch.y, pz = cif.z - ch.z;
+      auto test = [&](int k, bool &ok, int &jl) {
+        ok = false;
+        jl = 0;
+        if (k < tcount) {
+          jl = il + tstart + k;
           if (jl >= n) jl -= n;
-          cjf = a.cf[a0 + jl];
-          const float e0 = (cjf.x + ch.x) - cif.x, e1 = (cjf.y + ch.y) - cif.y,
-                      e2 = (cjf.z + ch.z) - cif.z;
-          df = e0 * e0 + e1 * e1 + e2 * e2;
+          const V4<float> cjf = a.cf[a0 + jl];
+          const float e0 = cjf.x - px, e1 = cjf.y - py, e2 = cjf.z - pz;
+          const float df = e0 * e0 + e1 * e1 + e2 * e2;
           if (df <= a.rc2_lo) {
             ok = true;
           } else if (df <= a.rc2_hi) {
@@ -241,23 +240,37 @@ __global__ void __launch_bounds__(256) nb_kernel(NbArgs a) {
             ok = exact_pair(a, ci, a0 + jl, img >= im0 ? img : -1, d) <= a.rc2;
           }
         }
-        const unsigned m = __ballot_sync(0xffffffffu, ok);
+      };
+      for (int base = 0; base < tcount; base += 64) {
+        bool ok0, ok1;
+        int j0, j1;
+        test(base + lane, ok0, j0);
+        test(base + 32 + lane, ok1, j1);
+        const unsigned m0 = __ballot_sync(0xffffffffu, ok0), m1 = __ballot_sync(0xffffffffu, ok1);
+        const int n0 = __popc(m0), n1 = __popc(m1);
         if (kFill) {
           // queue the accepted candidates in iterator order; store them 32 at a time
-          if (ok) queue[qn + __popc(m & ((1u << lane) - 1u))] = make_int2(jl, (int)img);
-          qn += __popc(m);
+          const unsigned below = (1u << lane) - 1u;
+          if (ok0) queue[qn + __popc(m0 & below)] = make_int2(j0, (int)img);
+          if (ok1) queue[qn + n0 + __popc(m1 & below)] = make_int2(j1, (int)img);
+          qn += n0 + n1;
           __syncwarp();
-          if (qn >= 32) {
+          while (qn >= 32) {
             const int2 e = queue[lane];
             store_pair<T>(a, ci, cif, cil, i, a0, e.x, e.y, im0, wpos, stored + lane);
+            // move the remaining qn - 32 (< 64) entries to the front: read all, then write
+            const int rem = qn - 32;
+            const int2 v0 = lane < rem ? queue[lane + 32] : make_int2(0, 0);
+            const int2 v1 = lane + 32 < rem ? queue[lane + 64] : make_int2(0, 0);
             __syncwarp();
-            if (lane < qn - 32) queue[lane] = queue[lane + 32];
+            if (lane < rem) queue[lane] = v0;
+            if (lane + 32 < rem) queue[lane + 32] = v1;
             __syncwarp();
             qn -= 32;
             stored += 32;
           }
         }
-        cnt += __popc(m);
+        cnt += n0 + n1;
       }
     }
     if (kFill && lane < qn) {
