@@ -18,8 +18,9 @@ namespace fnetg {
 
 namespace {
 
-// Per-CTA copy of the radial descriptors: parameters (kappa, rs, eta) and
-// (list channel, cutoff class, atom id, type | output column << 8).
+// Per-CTA copy of the radial descriptors in shape order: parameters (kappa, rs, -eta log2 e)
+// and (list-channel bit, cutoff class, atom id, type | output column << 8).  The channel bit
+// is 1 << species code, or bit 31 for the all-atom list.
 template <typename T> struct RadDesc {
   V4<T> p;
   int4 m;
@@ -45,8 +46,94 @@ template <typename T> __host__ __device__ inline size_t g5sum_bytes(const TileAr
   return a.nmf > 0 ? (sizeof(T) * (size_t)a.nmpair * kKD + 127) / 128 * 128 : 0;
 }
 
+template <typename T> struct RvDesc {
+  T rs, c2;       // rs, -eta log2 e
+  uint32_t bits;  // list-channel bit
+};
+
+// List-channel bits of tile pair q: its species and the all-atom list; every list for a self
+// image; none for lanes past the end.
+template <typename T>
+__device__ __forceinline__ uint32_t pair_channels(const Tile<T> &t, int q, bool live) {
+  const uint32_t inf = t.info[q];
+  const int code = (int)(inf & 0xff);
+  return !live ? 0u
+         : ((inf >> 8) & 1u) ? kRvAllChannels
+                             : (0x80000000u | (code < kMaxSpeciesCodes ? 1u << code : 0u));
+}
+
+// One batch of up to 32 radial G2 functions (one cutoff class, no atom ids), lanes over pairs,
+// each function evaluated per pair without branches and added where its list holds the pair.
+// A transposing butterfly returns function f's sum on lane f.
+template <typename T, typename Desc>
+__device__ __forceinline__ T radial_batch(const Tile<T> &t, const T *fcr, int np, int nb, int lane,
+                                          Desc desc) {
+  T acc[32];
+#pragma unroll
+  for (int f = 0; f < 32; f++) acc[f] = 0;
+  for (int q0 = 0; q0 < np; q0 += 32) {
+    const int q = q0 + lane;
+    const bool live = q < np;
+    const int qq = live ? q : q0;
+    const uint32_t cm = pair_channels<T>(t, qq, live);
+    const T r = t.u[qq].w;
+    const T fc = fcr[qq];
+#pragma unroll
+    for (int f = 0; f < 32; f++) {
+      if (f < nb) {
+        const RvDesc<T> d = desc(f);
+        const T x = r - d.rs;
+        const T v = m_exp2<T>(d.c2 * (x * x)) * fc;
+        if (cm & d.bits) acc[f] += v;
+      }
+    }
+  }
+  return transpose_reduce32<T>(acc, lane);
+}
+
+// The grid form of the radial G2 set: every shape (rs, eta) on the same NC list channels (the
+// species expansion of the reference's radial functions).  Batches of 32 / NC shapes x NC
+// channels; a pair evaluates each shape once and adds it to the channels holding it.  Shapes
+// past rv_nshape in the last batch are evaluated and dropped.
+template <typename T, int NC>
+__device__ __forceinline__ void radial_grid(const TileArgs<T> &a, const Tile<T> &t, const T *fcr,
+                                            int np, int lane, int64_t row) {
+  constexpr int SB = 32 / NC;
+#pragma unroll
+  for (int b = 0; b * SB * NC < kRadParam; b++) {
+    if (b * SB < a.rv_nshape) {
+      T acc[32];
+#pragma unroll
+      for (int f = 0; f < 32; f++) acc[f] = 0;
+      for (int q0 = 0; q0 < np; q0 += 32) {
+        const int q = q0 + lane;
+        const bool live = q < np;
+        const int qq = live ? q : q0;
+        const uint32_t cm = pair_channels<T>(t, qq, live);
+        bool in[NC];
+#pragma unroll
+        for (int c = 0; c < NC; c++) in[c] = (cm & a.rv_chan[c]) != 0u;
+        const T r = t.u[qq].w;
+        const T fc = fcr[qq];
+#pragma unroll
+        for (int sh = 0; sh < SB; sh++) {
+          const T x = r - a.rv_rs[b * SB + sh];
+          const T v = m_exp2<T>(a.rv_c2[b * SB + sh] * (x * x)) * fc;
+#pragma unroll
+          for (int c = 0; c < NC; c++)
+            if (in[c]) acc[sh * NC + c] += v;
+        }
+      }
+      const T tot = transpose_reduce32<T>(acc, lane);
+      if (lane < SB * NC && b * SB + lane / NC < a.rv_nshape)
+        a.feat[row * a.nf + a.rv_out[b * SB * NC + lane]] = tot;
+    }
+  }
+}
+
 template <typename T, int D>
-__global__ void __launch_bounds__(256) acsf_kernel(TileArgs<T> a) {
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 1)
+    acsf_kernel(const __grid_constant__ TileArgs<T> a) {
   extern __shared__ __align__(128) unsigned char smem[];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int wpb = blockDim.x >> 5;
@@ -55,10 +142,12 @@ __global__ void __launch_bounds__(256) acsf_kernel(TileArgs<T> a) {
                     tile_etab(a, false));
   RadDesc<T> *rd = reinterpret_cast<RadDesc<T> *>(smem);
   for (int g = threadIdx.x; g < a.nrad; g += blockDim.x) {
-    const GDesc d = a.rad[g];
-    const T *P = a.radp + 8 * g;
-    rd[g] = RadDesc<T>{V4<T>{P[1], P[2], P[3], (T)0},
-                       make_int4(d.chan1, d.rclass, d.atomid, d.type | (d.out << 8))};
+    const int src = a.radv[g];
+    const GDesc d = a.rad[src];
+    const T *P = a.radp + 8 * src;
+    const uint32_t bits = d.chan1 < 0 ? 0x80000000u : (1u << d.chan1);
+    rd[g] = RadDesc<T>{V4<T>{P[1], P[2], -P[3] * (T)kLog2e, (T)0},
+                       make_int4((int)bits, d.rclass, d.atomid, d.type | (d.out << 8))};
   }
   // int2 tables first (8-byte aligned from the 128-byte aligned start), then the T tables
   unsigned char *g5 = smem + raddesc_bytes<T>(a.nrad);
@@ -92,11 +181,46 @@ __global__ void __launch_bounds__(256) acsf_kernel(TileArgs<T> a) {
         for (int k = lane; k < nm; k += 32) dst[k] = t.M[k];
       }
     }
-    // ---- radial functions: items (function, part) over lanes; a function's list is split
-    // into rad_split contiguous parts on adjacent lanes (full lanes when the function count
-    // is not a multiple of 32), each part walked with four independent partial sums, the
-    // parts combined by shuffles.  The cutoff table is zero outside a function's class.
-    {
+    if (a.rad_fast >= 0) {
+      // ---- radial functions, all G2 of one cutoff class without atom ids: lanes over pairs,
+      // the functions in batches of 32 (radial_batch); descriptors from the kernel parameters
+      // when they fit there, else from the per-CTA table
+      const T *fcr = t.fc + a.rad_fast * a.cap;
+      if (a.rv_nc == 1) {
+        radial_grid<T, 1>(a, t, fcr, np, lane, row);
+      } else if (a.rv_nc == 2) {
+        radial_grid<T, 2>(a, t, fcr, np, lane, row);
+      } else if (a.rv_nc == 3) {
+        radial_grid<T, 3>(a, t, fcr, np, lane, row);
+      } else if (a.rv_nc == 4) {
+        radial_grid<T, 4>(a, t, fcr, np, lane, row);
+      } else if (a.rv_param) {
+#pragma unroll
+        for (int b = 0; b < kRadParam / 32; b++) {
+          if (b * 32 < a.nrad) {
+            const int nb = min(32, a.nrad - b * 32);
+            const T tot = radial_batch<T>(t, fcr, np, nb, lane, [&](int f) {
+              return RvDesc<T>{a.rv_rs[b * 32 + f], a.rv_c2[b * 32 + f], a.rv_bits[b * 32 + f]};
+            });
+            if (lane < nb) a.feat[row * a.nf + a.rv_out[b * 32 + lane]] = tot;
+          }
+        }
+      } else {
+        for (int b0 = 0; b0 < a.nrad; b0 += 32) {
+          const int nb = min(32, a.nrad - b0);
+          const RadDesc<T> *rb = rd + b0;
+          const T tot = radial_batch<T>(t, fcr, np, nb, lane, [&](int f) {
+            return RvDesc<T>{rb[f].p.y, rb[f].p.z, (uint32_t)rb[f].m.x};
+          });
+          if (lane < nb) a.feat[row * a.nf + (rb[lane].m.w >> 8)] = tot;
+        }
+      }
+    } else {
+      // ---- radial functions, general: items (function, part) over lanes; a function's list
+      // is split into rad_split contiguous parts on adjacent lanes (full lanes when the
+      // function count is not a multiple of 32), each part walked with four independent
+      // partial sums, the parts combined by shuffles.  The cutoff table is zero outside a
+      // function's class.
       const int S = a.rad_split;
       const int sh = S == 4 ? 2 : (S == 2 ? 1 : 0);  // S is a power of two: no divisions
       const int items = a.nrad * S;
@@ -106,8 +230,10 @@ __global__ void __launch_bounds__(256) acsf_kernel(TileArgs<T> a) {
         T acc = 0;
         if (it < items) {
           const RadDesc<T> rdg = rd[g];
-          const T kappa = rdg.p.x, rs = rdg.p.y, eta = rdg.p.z;
-          const int chan1 = rdg.m.x, rclass = rdg.m.y, atomid = rdg.m.z, type = rdg.m.w & 0xff;
+          const T kappa = rdg.p.x, rs = rdg.p.y, c2 = rdg.p.z;
+          const uint32_t fbit = (uint32_t)rdg.m.x;
+          const int chan1 = fbit == 0x80000000u ? -1 : __ffs((int)fbit) - 1;
+          const int rclass = rdg.m.y, atomid = rdg.m.z, type = rdg.m.w & 15;
           const uint16_t *lst = chan1 >= 0 ? t.lists + chan1 * a.cap : nullptr;
           const int n = chan1 >= 0 ? t.cnt[chan1] : np;
           const int chunk = (((n + S - 1) >> sh) + 3) & ~3;
@@ -121,7 +247,7 @@ __global__ void __launch_bounds__(256) acsf_kernel(TileArgs<T> a) {
             if (type == 1) return fc;
             if (type == 2) {
               const T x = r - rs;
-              return m_exp<T>(-(eta * (x * x))) * fc;
+              return m_exp2<T>(c2 * (x * x)) * fc;
             }
             return m_cos<T>(kappa * r) * fc;
           };
@@ -349,7 +475,56 @@ template <typename T> void fill_tile_args(fnetg_ctx *ctx, TileArgs<T> &a) {
   a.ext = ctx->d_ext.as<double>();
   a.next = ctx->next;
   a.rad = ctx->d_rad.as<GDesc>();
+  a.radv = ctx->d_radv.as<int32_t>();
+  a.rad_fast = ctx->rad_fast;
   a.nrad = (int)ctx->h_rad.size();
+  a.rv_param = a.rv_nc = a.rv_nshape = 0;
+  if (ctx->rad_fast >= 0 && a.nrad <= kRadParam) {
+    a.rv_param = 1;
+    auto chanbit = [](const GDesc &d) { return d.chan1 < 0 ? 0x80000000u : (1u << d.chan1); };
+    for (int g = 0; g < a.nrad; g++) {
+      const GDesc &d = ctx->h_rad[ctx->h_radv[g]];
+      a.rv_rs[g] = (T)d.rs;
+      a.rv_c2[g] = -(T)d.eta * (T)kLog2e;
+      a.rv_bits[g] = chanbit(d);
+      a.rv_out[g] = d.out;
+    }
+    // grid form: the first shape's channel run repeated, shape by shape, with distinct shapes
+    int nc = 0;
+    const GDesc &d0 = ctx->h_rad[ctx->h_radv[0]];
+    while (nc < a.nrad && ctx->h_rad[ctx->h_radv[nc]].rs == d0.rs &&
+           ctx->h_rad[ctx->h_radv[nc]].eta == d0.eta)
+      nc++;
+    bool grid = nc >= 1 && nc <= 4 && a.nrad % nc == 0;
+    for (int g = 0; grid && g < a.nrad; g++) {
+      const GDesc &d = ctx->h_rad[ctx->h_radv[g]];
+      const GDesc &h = ctx->h_rad[ctx->h_radv[g - g % nc]];  // the shape's first function
+      grid = chanbit(d) == chanbit(ctx->h_rad[ctx->h_radv[g % nc]]) && d.rs == h.rs && d.eta == h.eta &&
+             (g % nc != 0 || g == 0 ||
+              d.rs != ctx->h_rad[ctx->h_radv[g - 1]].rs || d.eta != ctx->h_rad[ctx->h_radv[g - 1]].eta);
+    }
+    if (grid) {
+      const int ns = a.nrad / nc, sb = 32 / nc;
+      a.rv_nc = nc;
+      a.rv_nshape = ns;
+      T rs[kRadParam] = {}, c2[kRadParam] = {};
+      int32_t out[kRadParam] = {};
+      for (int sh = 0; sh < ns; sh++) {
+        const GDesc &d = ctx->h_rad[ctx->h_radv[sh * nc]];
+        rs[sh] = (T)d.rs;
+        c2[sh] = -(T)d.eta * (T)kLog2e;
+        // function (shape sh, channel c) sits at lane (sh % sb) * nc + c of batch sh / sb
+        for (int c = 0; c < nc; c++)
+          out[(sh / sb) * sb * nc + (sh % sb) * nc + c] = ctx->h_rad[ctx->h_radv[sh * nc + c]].out;
+      }
+      for (int g = 0; g < kRadParam; g++) {
+        a.rv_rs[g] = rs[g];
+        a.rv_c2[g] = c2[g];
+        a.rv_out[g] = out[g];
+      }
+      for (int c = 0; c < nc; c++) a.rv_chan[c] = chanbit(ctx->h_rad[ctx->h_radv[c]]);
+    }
+  }
   a.ang = ctx->d_ang.as<GDesc>();
   const bool dbl = sizeof(T) == 8;
   a.radp = static_cast<const T *>(dbl ? ctx->d_radpar_d.p : ctx->d_radpar_f.p);
@@ -406,8 +581,8 @@ template <typename T> int launch_acsf(fnetg_ctx *ctx) {
   TileArgs<T> a;
   fill_tile_args<T>(ctx, a);
   FNETG_CHECK(a.cap <= 65535, FNETG_E_UNSUPPORTED, "more than 65535 neighbours of one atom");
-  // radial split: the S in {1, 2, 4} with the fewest lane passes per list element
-  // (ceil(nrad S / 32) / S, ties to the smaller S)
+  // general radial path: the split S in {1, 2, 4} with the fewest lane passes per list
+  // element (ceil(nrad S / 32) / S, ties to the smaller S)
   a.rad_split = 1;
   for (int S = 2; S <= 4; S <<= 1)
     if ((double)ceil_div((int64_t)a.nrad * S, 32) / S <

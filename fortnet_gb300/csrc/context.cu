@@ -1,5 +1,6 @@
 // Context management and the C-ABI entry points of libfnetg.
 #include <algorithm>
+#include <tuple>
 #include <cstdio>
 #include <array>
 #include <set>
@@ -528,6 +529,21 @@ int fnetg_set_gfunctions(fnetg_ctx *ctx, int32_t ng, const fnetg_gfunc *g) {
       ctx->rad_seg[c + 2] = pos;
     }
   }
+  // value kernel order: functions of one shape (type, cutoff class, atom id, rs / eta / kappa)
+  // adjacent, list channels in ascending order within a shape (the order above is stable), so
+  // that a species-expanded set forms a shape x channel grid
+  {
+    const int nr = (int)ctx->h_rad.size();
+    std::vector<int32_t> ord(nr);
+    for (int g = 0; g < nr; g++) ord[g] = g;
+    auto key = [&](int g) {
+      const GDesc &d = ctx->h_rad[g];
+      return std::make_tuple(d.type, d.rclass, d.atomid, d.type == 3 ? d.kappa : 0.0,
+                             d.type == 2 ? d.rs : 0.0, d.type == 2 ? d.eta : 0.0);
+    };
+    std::stable_sort(ord.begin(), ord.end(), [&](int x, int y) { return key(x) < key(y); });
+    ctx->h_radv = ord;
+  }
   // force kernel fast path: every radial function a G2 without atom id, one cutoff class
   ctx->rad_fast = ctx->h_rad.empty() ? -1 : ctx->h_rad[0].rclass;
   for (auto &d : ctx->h_rad)
@@ -568,6 +584,30 @@ int fnetg_set_gfunctions(fnetg_ctx *ctx, int32_t ng, const fnetg_gfunc *g) {
     mf.k2 = combo_of(d.chan2, d.eclass);
     mf.out = d.out;
     ctx->h_mfunc.push_back(mf);
+  }
+  // combos renumbered in (list channel, eta class) order: the moment kernels take runs of one
+  // list's eta classes together
+  {
+    const int nc = (int)ctx->h_combo.size() / 2;
+    std::vector<int> ord(nc), pos(nc);
+    for (int k = 0; k < nc; k++) ord[k] = k;
+    std::sort(ord.begin(), ord.end(), [&](int x, int y) {
+      return std::make_pair(ctx->h_combo[2 * x], ctx->h_combo[2 * x + 1]) <
+             std::make_pair(ctx->h_combo[2 * y], ctx->h_combo[2 * y + 1]);
+    });
+    std::vector<int32_t> sorted(2 * nc);
+    for (int k = 0; k < nc; k++) {
+      pos[ord[k]] = k;
+      sorted[2 * k] = ctx->h_combo[2 * ord[k]];
+      sorted[2 * k + 1] = ctx->h_combo[2 * ord[k] + 1];
+    }
+    ctx->h_combo = sorted;
+    for (auto &mf : ctx->h_mfunc) {
+      mf.k1 = pos[mf.k1];
+      mf.k2 = pos[mf.k2];
+    }
+    for (auto &c : ctx->h_cidx)
+      if (c >= 0) c = pos[c];
   }
   ctx->n_combo = (int)ctx->h_combo.size() / 2;
   // Degree coefficients pc_f(m) = 2^(1-xi) C(xi, m) lambda^m (coef_f(alpha) = pc_f(|alpha|)
@@ -708,9 +748,13 @@ int fnetg_set_gfunctions(fnetg_ctx *ctx, int32_t ng, const fnetg_gfunc *g) {
   FNETG_CUDA(ctx->d_ecls_rclass.ensure(sizeof(int) * kMaxEtaClasses));
   FNETG_CUDA(ctx->d_ecls_atomid.ensure(sizeof(int) * kMaxEtaClasses));
   FNETG_CUDA(ctx->d_rcls.ensure(sizeof(double) * kMaxRcutClasses));
-  if (!ctx->h_rad.empty())
+  FNETG_CUDA(ctx->d_radv.ensure(sizeof(int32_t) * std::max<size_t>(ctx->h_radv.size(), 1)));
+  if (!ctx->h_rad.empty()) {
     FNETG_CUDA(copy_sync(ctx, ctx->d_rad.p, ctx->h_rad.data(), sizeof(GDesc) * ctx->h_rad.size(),
                           cudaMemcpyHostToDevice));
+    FNETG_CUDA(copy_sync(ctx, ctx->d_radv.p, ctx->h_radv.data(),
+                          sizeof(int32_t) * ctx->h_radv.size(), cudaMemcpyHostToDevice));
+  }
   if (!ctx->h_ang.empty())
     FNETG_CUDA(copy_sync(ctx, ctx->d_ang.p, ctx->h_ang.data(), sizeof(GDesc) * ctx->h_ang.size(),
                           cudaMemcpyHostToDevice));

@@ -138,7 +138,7 @@ __device__ __forceinline__ void pair_e_d(const TileArgs<T> &a, const Tile<T> &tl
   const T f = tl.fc[rc * a.cap + q], df = tl.dfc[rc * a.cap + q];
   T ids = (T)1;
   if (aid > 0) ids = atom_id<T>(a.ext, a.next, aid, i) * atom_id<T>(a.ext, a.next, aid, tl.pj[q]);
-  const T ex = m_exp<T>(-(eta * (r * r)));
+  const T ex = m_exp2<T>((-eta * (T)kLog2e) * (r * r));
   E = ex * f * ids;
   Dv = ex * (df - (T)2 * eta * r * f) * ids;
 }
@@ -245,7 +245,8 @@ template <typename T> __host__ __device__ inline size_t radw_bytes(const TileArg
 }
 
 template <typename T, int D>
-__global__ void __launch_bounds__(256, 3) forces_kernel(TileArgs<T> a) {
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 1)
+    forces_kernel(const __grid_constant__ TileArgs<T> a) {
   extern __shared__ __align__(128) unsigned char smem[];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int wpb = blockDim.x >> 5;
@@ -289,11 +290,12 @@ __global__ void __launch_bounds__(256, 3) forces_kernel(TileArgs<T> a) {
     if (a.rad_fast >= 0) {
       // ---- radial, fast path (G2 only, one cutoff class, no atom ids): per pair
       //   dE/dr = dfc sum_g J_g e_g - 2 fc sum_g J_g eta_g x_g e_g,  x_g = r - rs_g,
-      //   e_g = exp(-eta_g x_g^2), over the all-atom functions and the pair's species' own
+      //   e_g = exp(-eta_g x_g^2), over the all-atom functions and the pair's species' own;
+      // the table holds (rs, -eta log2 e, J, J eta)
       for (int g = lane; g < a.nrad; g += 32) {
         const RadEntry<T> re = rt[g];
         const T J = tl.jv[re.out];
-        wt[g] = V4<T>{re.p0, re.p1, J, J * re.p1};
+        wt[g] = V4<T>{re.p0, -re.p1 * (T)kLog2e, J, J * re.p1};
       }
       __syncwarp();
       const int rcl = a.rad_fast;
@@ -311,7 +313,7 @@ __global__ void __launch_bounds__(256, 3) forces_kernel(TileArgs<T> a) {
           for (; g + 2 <= g1; g += 2) {
             const V4<T> w0 = wt[g], w1 = wt[g + 1];
             const T x0 = r - w0.x, x1 = r - w1.x;
-            const T e0 = m_exp<T>(-(w0.y * (x0 * x0))), e1 = m_exp<T>(-(w1.y * (x1 * x1)));
+            const T e0 = m_exp2<T>(w0.y * (x0 * x0)), e1 = m_exp2<T>(w1.y * (x1 * x1));
             s1a += w0.z * e0;
             s2a += w0.w * (x0 * e0);
             s1b += w1.z * e1;
@@ -320,7 +322,7 @@ __global__ void __launch_bounds__(256, 3) forces_kernel(TileArgs<T> a) {
           if (g < g1) {
             const V4<T> w0 = wt[g];
             const T x0 = r - w0.x;
-            const T e0 = m_exp<T>(-(w0.y * (x0 * x0)));
+            const T e0 = m_exp2<T>(w0.y * (x0 * x0));
             s1a += w0.z * e0;
             s2a += w0.w * (x0 * e0);
           }

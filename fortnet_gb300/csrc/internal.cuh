@@ -158,6 +158,8 @@ struct fnetg_ctx {
   std::vector<fnetg::GDesc> h_rad, h_ang;
   std::vector<int> rad_seg;  // [kMaxSpeciesCodes + 2]: all-atom radial functions [0, rad_seg[1]),
                              // species code c in [rad_seg[c + 1], rad_seg[c + 2])
+  std::vector<int32_t> h_radv;  // value-kernel order of h_rad: by shape (type, cutoff class,
+                                // atom id, rs / eta / kappa), then list channel
   std::vector<fnetg::AGroup> h_groups;
   std::vector<double> rcut_classes;
   std::vector<double> ecls_eta;
@@ -175,7 +177,7 @@ struct fnetg_ctx {
   fnetg::DBuf d_qgroups, d_mpc_d, d_mpc_f;
   // kernel parameter copies in both arithmetic widths: [rcut, kappa, rs, eta, lambda, xi, pref, 0]
   fnetg::DBuf d_radpar_f, d_radpar_d, d_angpar_f, d_angpar_d, d_ecls_eta_f, d_rcls_f;
-  fnetg::DBuf d_rad, d_ang, d_groups, d_code, d_ecls_eta, d_ecls_rclass, d_ecls_atomid,
+  fnetg::DBuf d_rad, d_radv, d_ang, d_groups, d_code, d_ecls_eta, d_ecls_rclass, d_ecls_atomid,
       d_rcls;
 
   // neighbour list

@@ -42,6 +42,35 @@ constexpr bool mono_mult_table_ok() {
 }
 static_assert(mono_mult_table_ok(), "multinomial table");
 
+// Each monomial of degree >= 1 as its parent (one exponent lower) times one coordinate, the
+// first of x, y, z with a nonzero exponent.
+struct MonoLinks {
+  int parent[kMaxMono];
+  int axis[kMaxMono];
+};
+constexpr int mono_index(int a, int b, int c) {
+  for (int al = 0; al < kMaxMono; al++)
+    if (kMonoTab[al][0] == a && kMonoTab[al][1] == b && kMonoTab[al][2] == c) return al;
+  return -1;
+}
+constexpr MonoLinks make_mono_links() {
+  MonoLinks l{};
+  for (int al = 1; al < kMaxMono; al++) {
+    const int a = kMonoTab[al][0], b = kMonoTab[al][1], c = kMonoTab[al][2];
+    l.axis[al] = a > 0 ? 0 : (b > 0 ? 1 : 2);
+    l.parent[al] = a > 0 ? mono_index(a - 1, b, c) : (b > 0 ? mono_index(a, b - 1, c) : mono_index(a, b, c - 1));
+  }
+  return l;
+}
+__device__ constexpr MonoLinks kMonoLinks = make_mono_links();
+constexpr bool mono_links_ok() {
+  const MonoLinks l = make_mono_links();
+  for (int al = 1; al < kMaxMono; al++)
+    if (l.parent[al] < 0 || l.parent[al] >= al) return false;
+  return true;
+}
+static_assert(mono_links_ok(), "monomial parents precede their children");
+
 // Float exp through the hardware base-2 exponential: exp(x) = 2^(x log2 e) with the product
 // x log2 e carried as hi + lo (log2 e split into a float head and tail, the rounding of x * head
 // recovered by an FMA), ex2.approx on hi and the first-order factor 1 + lo ln 2 for the tail.
@@ -59,6 +88,17 @@ __device__ __forceinline__ float exp_ex2(float x) {
 template <typename T> __device__ __forceinline__ T m_exp(T x);
 template <> __device__ __forceinline__ float m_exp<float>(float x) { return exp_ex2(x); }
 template <> __device__ __forceinline__ double m_exp<double>(double x) { return exp(x); }
+// 2^x: ex2.approx (flushing results below 2^-126 to zero) for float, exp2 for double.  Callers
+// fold log2 e into their coefficients, exp(-eta x^2) = 2^(-eta log2(e) x^2): the rounding of
+// the folded coefficient is of the size of the rounding of eta x^2 itself.
+template <typename T> __device__ __forceinline__ T m_exp2(T x);
+template <> __device__ __forceinline__ float m_exp2<float>(float x) {
+  float r;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+template <> __device__ __forceinline__ double m_exp2<double>(double x) { return exp2(x); }
+constexpr double kLog2e = 1.44269504088896340736;
 template <typename T> __device__ __forceinline__ T m_cos(T x);
 template <> __device__ __forceinline__ float m_cos<float>(float x) { return cosf(x); }
 template <> __device__ __forceinline__ double m_cos<double>(double x) { return cos(x); }
@@ -100,13 +140,14 @@ template <>
 __device__ __forceinline__ void cutoff_fc<float>(float r, float rc, float &fc, float &dfc) {
   // sin phi = cos theta and cos phi = sin theta for theta = (pi / 2) r / rc: the series run on
   // the smaller of the two angles (<= pi/4), so both ends of [0, rc] keep relative accuracy
-  const float phi = (float)(kPi / 2.0) * ((rc - r) / rc);
-  const float theta = (float)(kPi / 2.0) * (r / rc);
+  const float irc = 1.f / rc;
+  const float phi = (float)(kPi / 2.0) * ((rc - r) * irc);
+  const float theta = (float)(kPi / 2.0) * (r * irc);
   float sm, cm;
   sincos_taylor(fminf(phi, theta), sm, cm);
   const float s = phi <= theta ? sm : cm, c = phi <= theta ? cm : sm;
   fc = s * s;
-  dfc = -((float)kPi / rc) * (s * c);
+  dfc = -((float)kPi * irc) * (s * c);
 }
 
 template <typename T> __device__ __forceinline__ T m_pow(T b, T e);
@@ -138,6 +179,9 @@ template <typename T> __device__ __forceinline__ T int_pow(T base, int n, T e) {
 }
 
 // Everything the per-atom kernels read (one struct for both kernels).
+constexpr int kRadParam = 64;                  // radial descriptors carried as kernel parameters
+constexpr uint32_t kRvAllChannels = 0x800000ffu;  // channel bits of a self image: every list
+
 template <typename T> struct TileArgs {
   int64_t natoms;
   const int64_t *poff;     // pairs of atom i: [poff[i], pend[i])
@@ -153,7 +197,18 @@ template <typename T> struct TileArgs {
   const T *radp;          // [nrad][8] parameters in the kernel's width
   int nrad;
   int rad_seg[kMaxSpeciesCodes + 2];  // radial functions by list channel (see the context)
-  int rad_split;          // value kernel: lanes per radial function (1, 2 or 4)
+  const int32_t *radv;    // value kernel: radial functions in shape order
+  int rad_split;          // value kernel, general radial path: lanes per function (1, 2 or 4)
+  // value kernel, radial fast path with at most kRadParam functions: the descriptors held in
+  // the kernel parameters, read as constant-bank operands by the unrolled loops.  Grid form
+  // (rv_nc > 0: every shape on the same rv_nc list channels): per shape rs and -eta log2 e,
+  // per channel its bit, per function (shape-major) its output column.  Otherwise per function
+  // rs, -eta log2 e, channel bit and output column.
+  int rv_param, rv_nc, rv_nshape;
+  T rv_rs[kRadParam], rv_c2[kRadParam];
+  uint32_t rv_bits[kRadParam];
+  int32_t rv_out[kRadParam];
+  uint32_t rv_chan[kMaxSpeciesCodes + 1];
   const GDesc *ang;       // triplet-sweep functions
   const T *angp;          // [nang][8]
   const AGroup *groups;
@@ -379,7 +434,7 @@ __device__ void stage_tile(const TileArgs<T> &a, Tile<T> &t, int64_t i, int64_t 
       const T eta = a.ecls_eta[e];
       const int aid = a.ecls_atomid[e];
       const int rc = a.ecls_rclass[e];
-      const T ex = m_exp<T>(-(eta * (v.w * v.w)));
+      const T ex = m_exp2<T>((-eta * (T)kLog2e) * (v.w * v.w));
       T ids = (T)1;
       if (aid > 0) ids = atom_id<T>(a.ext, a.next, aid, i) * atom_id<T>(a.ext, a.next, aid, j);
       const T f = t.fc[rc * a.cap + q];
@@ -423,51 +478,69 @@ __device__ __forceinline__ T transpose_reduce32(T *v, int lane) {
   return v[0];
 }
 
-// M_k(alpha) = sum over list(k) of E_e(k)(j) u_j^alpha for every (list, eta class) combo k:
-// lanes over the list's pairs, monomials of degree <= D unrolled, warp reduction per combo.
+// One pass of the moment sums M_k(alpha) = sum over list(k) of E_e(k)(j) u_j^alpha for nk <= 32 / S
+// consecutive combos k0.. of one list (the combos are ordered by list, then eta class).  Lane
+// (group g, slot s) walks the list's pairs s, s + S, ... with the weight of combo k0 + g, the
+// monomials carried as products (child = parent * coordinate); a transposing butterfly over the
+// S slots then leaves C = ceil(NM / S) consecutive sums on each lane.
+template <typename T, int D, int S>
+__device__ __forceinline__ void moment_pass(const TileArgs<T> &a, Tile<T> &t, const uint16_t *lst,
+                                            int n, int k0, int nk, int lane) {
+  constexpr int NM = n_mono_of(D);
+  constexpr int C = (NM + S - 1) / S;
+  constexpr int V = C * S;
+  const int grp = lane / S, slot = lane % S;
+  const bool on = grp < nk;
+  const int e = on ? a.combo[2 * (k0 + grp) + 1] : 0;
+  const T *E = t.E + e * a.cap;
+  T acc[V];
+#pragma unroll
+  for (int al = 0; al < V; al++) acc[al] = 0;
+  for (int kk = slot; kk < n; kk += S) {
+    const int q = lst ? lst[kk] : kk;
+    const V4<T> u = t.u[q];
+    T m[NM];
+    m[0] = on ? E[q] : (T)0;
+#pragma unroll
+    for (int al = 1; al < NM; al++) {
+      const int ax = kMonoLinks.axis[al];
+      m[al] = m[kMonoLinks.parent[al]] * (ax == 0 ? u.x : (ax == 1 ? u.y : u.z));
+    }
+#pragma unroll
+    for (int al = 0; al < NM; al++) acc[al] += m[al];
+  }
+#pragma unroll
+  for (int sh = S / 2, L = V; sh >= 1; sh >>= 1, L >>= 1) {
+    const bool upper = (lane & sh) != 0;
+#pragma unroll
+    for (int k = 0; k < L / 2; k++) {
+      const T send = upper ? acc[k] : acc[k + L / 2];
+      const T keep = upper ? acc[k + L / 2] : acc[k];
+      acc[k] = keep + __shfl_xor_sync(0xffffffffu, send, sh);
+    }
+  }
+  if (on) {
+    T *M = t.M + (k0 + grp) * NM;
+#pragma unroll
+    for (int c = 0; c < C; c++)
+      if (slot * C + c < NM) M[slot * C + c] = acc[c];
+  }
+}
+
+// M_k(alpha) for every (list, eta class) combo k: runs of one list's combos taken up to four
+// at a time (8 slots per combo for three or four, 16 for two, 32 for one).
 template <typename T, int D>
 __device__ void compute_moments(const TileArgs<T> &a, Tile<T> &t, int np, int lane) {
-  constexpr int NM = n_mono_of(D);
-  for (int k = 0; k < a.ncombo; k++) {
-    const int z = a.combo[2 * k], e = a.combo[2 * k + 1];
+  for (int k = 0; k < a.ncombo;) {
+    const int z = a.combo[2 * k];
+    int nk = 1;
+    while (k + nk < a.ncombo && nk < 4 && a.combo[2 * (k + nk)] == z) nk++;
     const uint16_t *lst = z >= 0 ? t.lists + z * a.cap : nullptr;
     const int n = z >= 0 ? t.cnt[z] : np;
-    const T *E = t.E + e * a.cap;
-    T acc[NM > 32 ? NM : 32];
-#pragma unroll
-    for (int al = 0; al < (NM > 32 ? NM : 32); al++) acc[al] = 0;
-    for (int kk = lane; kk < n; kk += 32) {
-      const int q = lst ? lst[kk] : kk;
-      const V4<T> u = t.u[q];
-      const T w = E[q];
-      T px[D + 1], py[D + 1], pz[D + 1];
-      px[0] = py[0] = pz[0] = (T)1;
-#pragma unroll
-      for (int d = 1; d <= D; d++) {
-        px[d] = px[d - 1] * u.x;
-        py[d] = py[d - 1] * u.y;
-        pz[d] = pz[d - 1] * u.z;
-      }
-#pragma unroll
-      for (int al = 0; al < NM; al++)
-        acc[al] += w * (px[kMonoTab[al][0]] * py[kMonoTab[al][1]] * pz[kMonoTab[al][2]]);
-    }
-    T *M = t.M + k * a.n_mono;
-    if (NM >= 32) {
-      const T mine = transpose_reduce32<T>(acc, lane);
-      M[lane] = mine;
-#pragma unroll
-      for (int al = 32; al < NM; al++) {
-        const T sres = warp_sum<T>(acc[al]);
-        if (lane == 0) M[al] = sres;
-      }
-    } else {
-#pragma unroll
-      for (int al = 0; al < NM; al++) {
-        const T sres = warp_sum<T>(acc[al]);
-        if (lane == al) M[al] = sres;
-      }
-    }
+    if (nk == 1) moment_pass<T, D, 32>(a, t, lst, n, k, 1, lane);
+    else if (nk == 2) moment_pass<T, D, 16>(a, t, lst, n, k, 2, lane);
+    else moment_pass<T, D, 8>(a, t, lst, n, k, nk, lane);
+    k += nk;
   }
   __syncwarp();
 }
