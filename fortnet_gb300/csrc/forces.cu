@@ -143,70 +143,60 @@ __device__ __forceinline__ void pair_e_d(const TileArgs<T> &a, const Tile<T> &tl
   Dv = ex * (df - (T)2 * eta * r * f) * ids;
 }
 
-// Per-pair derivative of the moment terms, degree D known at compile time.  Linear in the
-// adjoint moments, so with c_D(alpha) = sum_e D_e Qc_e(alpha) and c_E(alpha) = sum_e E_e Qc_e(alpha)
+// Per-pair derivative of the moment terms, degree D and (for NE > 0) the eta-class count known at
+// compile time.  Linear in the adjoint moments, so with c_D(alpha) = sum_e D_e Qc_e(alpha) and
+// c_E(alpha) = sum_e E_e Qc_e(alpha)
 //   w += P_D(u) u + (grad P_E(u) - (grad P_E(u) . u) u) / r,   P_c(u) = sum_alpha c(alpha) u^alpha.
-// Up to four eta classes are folded inside the unrolled monomial loop (no coefficient arrays
-// stay live); more classes take one polynomial pass per class.
-template <typename T, int D>
+// The monomials are built as products (child = parent * coordinate) and the gradient takes
+// d/dx u^alpha = a u^(alpha - e_x) from the same registers.  NE = 0: any class count, one
+// polynomial pass per class.
+template <typename T, int D, int NE>
 __device__ __forceinline__ void moment_pair_force(const TileArgs<T> &a, Tile<T> &tl, int q,
                                                   int zz, int64_t i) {
   constexpr int NM = n_mono_of(D);
   const V4<T> u = tl.u[q];
   const T r = u.w;
-  T px[D + 1], py[D + 1], pz[D + 1];
-  px[0] = py[0] = pz[0] = (T)1;
+  T m[NM];
+  m[0] = (T)1;
 #pragma unroll
-  for (int d = 1; d <= D; d++) {
-    px[d] = px[d - 1] * u.x;
-    py[d] = py[d - 1] * u.y;
-    pz[d] = pz[d - 1] * u.z;
+  for (int al = 1; al < NM; al++) {
+    const int ax = kMonoLinks.axis[al];
+    m[al] = m[kMonoLinks.parent[al]] * (ax == 0 ? u.x : (ax == 1 ? u.y : u.z));
   }
   T P = 0, gx = 0, gy = 0, gz = 0;
   const T *Qz = tl.Qc + (int64_t)zz * a.necls * NM;
-  if (a.necls <= 4) {
-    T Ee[4], De[4];
+  auto add = [&](int al, T cd, T ce) {
+    P += cd * m[al];
+    const int ea = kMonoTab[al][0], eb = kMonoTab[al][1], ec = kMonoTab[al][2];
+    if (ea > 0) gx += (ea == 1 ? ce : (T)ea * ce) * m[kMonoDown.idx[al][0] < 0 ? 0 : kMonoDown.idx[al][0]];
+    if (eb > 0) gy += (eb == 1 ? ce : (T)eb * ce) * m[kMonoDown.idx[al][1] < 0 ? 0 : kMonoDown.idx[al][1]];
+    if (ec > 0) gz += (ec == 1 ? ce : (T)ec * ce) * m[kMonoDown.idx[al][2] < 0 ? 0 : kMonoDown.idx[al][2]];
+  };
+  if constexpr (NE > 0) {
+    T Ee[NE], De[NE];
 #pragma unroll
-    for (int e = 0; e < 4; e++) {
-      Ee[e] = De[e] = (T)0;
-      if (e < a.necls) pair_e_d<T>(a, tl, q, e, r, i, Ee[e], De[e]);
-    }
+    for (int e = 0; e < NE; e++) pair_e_d<T>(a, tl, q, e, r, i, Ee[e], De[e]);
 #pragma unroll
     for (int al = 0; al < NM; al++) {
       T cd = 0, ce = 0;
 #pragma unroll
-      for (int e = 0; e < 4; e++) {
-        if (e < a.necls) {
-          const T qv = Qz[e * NM + al];
-          cd += De[e] * qv;
-          ce += Ee[e] * qv;
-        }
+      for (int e = 0; e < NE; e++) {
+        const T qv = Qz[e * NM + al];
+        cd += De[e] * qv;
+        ce += Ee[e] * qv;
       }
-      const int ea = kMonoTab[al][0], eb = kMonoTab[al][1], ec = kMonoTab[al][2];
-      P += cd * (px[ea] * py[eb] * pz[ec]);
-      if (ea > 0) gx += ((T)ea * ce) * (px[ea > 0 ? ea - 1 : 0] * py[eb] * pz[ec]);
-      if (eb > 0) gy += ((T)eb * ce) * (px[ea] * py[eb > 0 ? eb - 1 : 0] * pz[ec]);
-      if (ec > 0) gz += ((T)ec * ce) * (px[ea] * py[eb] * pz[ec > 0 ? ec - 1 : 0]);
+      add(al, cd, ce);
     }
   } else {
     for (int e = 0; e < a.necls; e++) {
       T Ev, Dv;
       pair_e_d<T>(a, tl, q, e, r, i, Ev, Dv);
       const T *Qe = Qz + e * NM;
-      T pe = 0, hx = 0, hy = 0, hz = 0;
 #pragma unroll
       for (int al = 0; al < NM; al++) {
         const T qv = Qe[al];
-        const int ea = kMonoTab[al][0], eb = kMonoTab[al][1], ec = kMonoTab[al][2];
-        pe += qv * (px[ea] * py[eb] * pz[ec]);
-        if (ea > 0) hx += ((T)ea * qv) * (px[ea > 0 ? ea - 1 : 0] * py[eb] * pz[ec]);
-        if (eb > 0) hy += ((T)eb * qv) * (px[ea] * py[eb > 0 ? eb - 1 : 0] * pz[ec]);
-        if (ec > 0) hz += ((T)ec * qv) * (px[ea] * py[eb] * pz[ec > 0 ? ec - 1 : 0]);
+        add(al, Dv * qv, Ev * qv);
       }
-      P += Dv * pe;
-      gx += Ev * hx;
-      gy += Ev * hy;
-      gz += Ev * hz;
     }
   }
   const T gu = gx * u.x + gy * u.y + gz * u.z;
@@ -214,6 +204,19 @@ __device__ __forceinline__ void moment_pair_force(const TileArgs<T> &a, Tile<T> 
   tl.w[q].x += P * u.x + ir * (gx - gu * u.x);
   tl.w[q].y += P * u.y + ir * (gy - gu * u.y);
   tl.w[q].z += P * u.z + ir * (gz - gu * u.z);
+}
+
+// All pairs of the tile through moment_pair_force (self images do not move relative to the
+// centre; pairs of a species outside the lists take the all-atom row nz).
+template <typename T, int D, int NE>
+__device__ __forceinline__ void moment_pairs(const TileArgs<T> &a, Tile<T> &tl, int np, int lane,
+                                             int64_t i) {
+  for (int q = lane; q < np; q += 32) {
+    const uint32_t inf = tl.info[q];
+    if ((inf >> 8) & 1u) continue;
+    const int z = (int)(inf & 0xff);
+    moment_pair_force<T, D, NE>(a, tl, q, z < a.nz ? z : a.nz, i);
+  }
 }
 
 // Radial function parameters staged once per CTA: p0 = rs (G2) or kappa (G3), p1 = eta,
@@ -244,8 +247,12 @@ template <typename T> __host__ __device__ inline size_t radw_bytes(const TileArg
   return a.rad_fast >= 0 ? (sizeof(V4<T>) * a.nrad + 127) / 128 * 128 : 0;
 }
 
+// FP32: CTAs of at most 4 warps, 5 per SM (the shared-memory limit of the tiles) at up to 96
+// registers a thread; FP64: up to 8 warps a CTA, registers unbounded.
+template <typename T> constexpr int kForcesThreads = sizeof(T) == 4 ? 128 : 256;
+
 template <typename T, int D>
-__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 1)
+__global__ void __launch_bounds__(kForcesThreads<T>, sizeof(T) == 4 ? 5 : 1)
     forces_kernel(const __grid_constant__ TileArgs<T> a) {
   extern __shared__ __align__(128) unsigned char smem[];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -432,11 +439,13 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 1)
           if (lane + 32 < NM) dst[lane + 32] = mmult1 * v1;
         }
       __syncwarp();
-      for (int q = lane; q < np; q += 32) {
-        const uint32_t inf = tl.info[q];
-        if ((inf >> 8) & 1u) continue;
-        const int z = (int)(inf & 0xff);
-        moment_pair_force<T, (D > 0 ? D : 1)>(a, tl, q, z < a.nz ? z : a.nz, i);
+      constexpr int DD = D > 0 ? D : 1;
+      switch (a.necls) {
+        case 1: moment_pairs<T, DD, 1>(a, tl, np, lane, i); break;
+        case 2: moment_pairs<T, DD, 2>(a, tl, np, lane, i); break;
+        case 3: moment_pairs<T, DD, 3>(a, tl, np, lane, i); break;
+        case 4: moment_pairs<T, DD, 4>(a, tl, np, lane, i); break;
+        default: moment_pairs<T, DD, 0>(a, tl, np, lane, i); break;
       }
     }
     __syncwarp();
@@ -558,7 +567,8 @@ template <typename T, int D> int launch_forces_d(fnetg_ctx *ctx, TileArgs<T> &a,
   int wpb = 1, per_sm = 1;
   size_t smem = 0;
   const cudaError_t err =
-      pick_warps(forces_kernel<T, D>, fixed, tb + radw_bytes<T>(a), wpb, smem, per_sm);
+      pick_warps(forces_kernel<T, D>, fixed, tb + radw_bytes<T>(a), wpb, smem, per_sm,
+                 kForcesThreads<T> / 32);
   FNETG_CHECK(err != cudaErrorInvalidValue, FNETG_E_UNSUPPORTED,
               "neighbour tile of one atom exceeds shared memory");
   FNETG_CUDA(err);

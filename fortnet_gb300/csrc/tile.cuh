@@ -63,6 +63,23 @@ constexpr MonoLinks make_mono_links() {
   return l;
 }
 __device__ constexpr MonoLinks kMonoLinks = make_mono_links();
+
+// Each monomial's derivative partner per coordinate: the index of alpha - e_axis, -1 when that
+// exponent is zero (d/dx u^alpha = a u^(alpha - e_x)).
+struct MonoDown {
+  int idx[kMaxMono][3];
+};
+constexpr MonoDown make_mono_down() {
+  MonoDown d{};
+  for (int al = 0; al < kMaxMono; al++) {
+    const int a = kMonoTab[al][0], b = kMonoTab[al][1], c = kMonoTab[al][2];
+    d.idx[al][0] = a > 0 ? mono_index(a - 1, b, c) : -1;
+    d.idx[al][1] = b > 0 ? mono_index(a, b - 1, c) : -1;
+    d.idx[al][2] = c > 0 ? mono_index(a, b, c - 1) : -1;
+  }
+  return d;
+}
+__device__ constexpr MonoDown kMonoDown = make_mono_down();
 constexpr bool mono_links_ok() {
   const MonoLinks l = make_mono_links();
   for (int al = 1; al < kMaxMono; al++)
@@ -377,16 +394,18 @@ __device__ Tile<T> carve_tile(unsigned char *p, const TileArgs<T> &a, bool force
 }
 
 // Warps per CTA for a warp-per-atom kernel whose CTA needs `fixed` + wpb * `per_warp` bytes of
-// dynamic shared memory: the choice among 8, 4, 2, 1 with the most resident warps per SM
-// (ties go to the larger CTA).  Raises the kernel's shared-memory limit to cover that choice.
+// dynamic shared memory: the choice among 8, 4, 2, 1 (at most max_w, the kernel's launch bound)
+// with the most resident warps per SM (ties go to the larger CTA).  Raises the kernel's
+// shared-memory limit to cover that choice.
 template <typename K>
 inline cudaError_t pick_warps(K kernel, size_t fixed, size_t per_warp, int &wpb, size_t &smem,
-                              int &ctas_per_sm) {
+                              int &ctas_per_sm, int max_w = 8) {
   cudaError_t err = cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
                                          (int)cudaSharedmemCarveoutMaxShared);
   if (err != cudaSuccess) return err;
   int best_w = 0, best_warps = -1, best_ctas = 0;
   for (int w = 8; w >= 1; w >>= 1) {
+    if (w > max_w) continue;
     const size_t bytes = fixed + per_warp * (size_t)w;
     if (bytes > 227 * 1024) continue;
     err = raise_smem_limit(reinterpret_cast<const void *>(kernel), bytes);
