@@ -482,32 +482,40 @@ __global__ void __launch_bounds__(kForcesThreads<T>, sizeof(T) == 4 ? 5 : 1)
     }
     __syncwarp();
     // ---- scatter: F_j -= w_p, F_i += sum_p w_p (self images cancel).  A lane sums its own
-    // pairs (two or three) in T and the warp sums the lanes in FP64.
+    // pairs (two or three) in T and the warp sums the lanes.  FP32: one vector atomic per pair
+    // into the float4 accumulators; FP64: three FP64 atomics.
     T lx = 0, ly = 0, lz = 0;
     for (int q = lane; q < np; q += 32) {
       if ((tl.info[q] >> 8) & 1u) continue;
       const V4<T> w = tl.w[q];
       const int64_t j = tl.pj[q];
-      double *Fj = a.F + (j * a.nout + a.out_index) * 3;
-      atomicAdd(Fj + 0, -(double)w.x);
-      atomicAdd(Fj + 1, -(double)w.y);
-      atomicAdd(Fj + 2, -(double)w.z);
+      if constexpr (sizeof(T) == 4) {
+        atomicAdd(a.F4 + j * a.nout + a.out_index, make_float4(-w.x, -w.y, -w.z, 0.f));
+      } else {
+        double *Fj = a.F + (j * a.nout + a.out_index) * 3;
+        atomicAdd(Fj + 0, -(double)w.x);
+        atomicAdd(Fj + 1, -(double)w.y);
+        atomicAdd(Fj + 2, -(double)w.z);
+      }
       lx += w.x;
       ly += w.y;
       lz += w.z;
     }
-    double sx = (double)lx, sy = (double)ly, sz = (double)lz;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
-      sx += __shfl_xor_sync(0xffffffffu, sx, o);
-      sy += __shfl_xor_sync(0xffffffffu, sy, o);
-      sz += __shfl_xor_sync(0xffffffffu, sz, o);
+      lx += __shfl_xor_sync(0xffffffffu, lx, o);
+      ly += __shfl_xor_sync(0xffffffffu, ly, o);
+      lz += __shfl_xor_sync(0xffffffffu, lz, o);
     }
     if (lane == 0) {
-      double *Fi = a.F + (i * a.nout + a.out_index) * 3;
-      atomicAdd(Fi + 0, sx);
-      atomicAdd(Fi + 1, sy);
-      atomicAdd(Fi + 2, sz);
+      if constexpr (sizeof(T) == 4) {
+        atomicAdd(a.F4 + i * a.nout + a.out_index, make_float4(lx, ly, lz, 0.f));
+      } else {
+        double *Fi = a.F + (i * a.nout + a.out_index) * 3;
+        atomicAdd(Fi + 0, (double)lx);
+        atomicAdd(Fi + 1, (double)ly);
+        atomicAdd(Fi + 2, (double)lz);
+      }
     }
     __syncwarp();
   }
@@ -559,6 +567,16 @@ template <typename T> void fill_tile_args_forces(fnetg_ctx *ctx, TileArgs<T> &a)
   a.ng = (int)ctx->gf.size();
 }
 
+// FP32 force accumulators [N][nout] (float4) into the FP64 force array [N][nout][3]
+__global__ void forces4_to_f64_kernel(const float4 *f4, double *F, int64_t n) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const float4 v = f4[k];
+  F[3 * k + 0] = (double)v.x;
+  F[3 * k + 1] = (double)v.y;
+  F[3 * k + 2] = (double)v.z;
+}
+
 template <typename T, int D> int launch_forces_d(fnetg_ctx *ctx, TileArgs<T> &a, int nout) {
   const int64_t N = ctx->N;
   const size_t tb = tile_bytes<T>(a.cap, a.nrcls, a.necls, a.nz, a.ncombo, a.n_mono, a.ng, true, a.ngroups > 0,
@@ -583,6 +601,13 @@ template <typename T, int D> int launch_forces_d(fnetg_ctx *ctx, TileArgs<T> &a,
     forces_kernel<T, D><<<blocks, wpb * 32, smem, ctx->stream>>>(a);
     FNETG_CUDA(cudaGetLastError());
   }
+  if (sizeof(T) == 4) {
+    const int64_t n = N * nout;
+    LaunchScope ls(ctx, "forces");
+    forces4_to_f64_kernel<<<(int)ceil_div(n, 256), 256, 0, ctx->stream>>>(
+        ctx->d_forces4.as<float4>(), ctx->d_forces.as<double>(), n);
+    FNETG_CUDA(cudaGetLastError());
+  }
   return FNETG_OK;
 }
 
@@ -599,6 +624,11 @@ template <typename T> int launch_forces(fnetg_ctx *ctx) {
   fill_tile_args_forces<T>(ctx, a);
   a.J = ctx->d_jacT.as<T>();
   a.F = ctx->d_forces.as<double>();
+  if (sizeof(T) == 4) {
+    FNETG_CUDA(ctx->d_forces4.ensure(sizeof(float4) * (size_t)N * nout));
+    FNETG_CUDA(cudaMemsetAsync(ctx->d_forces4.p, 0, sizeof(float4) * (size_t)N * nout, ctx->stream));
+    a.F4 = ctx->d_forces4.as<float4>();
+  }
   if (ctx->mom_valid) {
     a.mom = ctx->d_mom.as<T>();
     a.mom_cached = 1;

@@ -233,7 +233,7 @@ struct fnetg_ctx {
   int ngt = 0, nat = 0;
   bool targets_set = false;
   fnetg::DBuf d_gt, d_at, d_aw, d_w, d_out, d_gsum, d_lossgrad, d_losspart, d_gpart, d_grad64,
-      d_order, d_jac, d_jacT, d_forces, d_scalars, d_struct_aw;
+      d_order, d_jac, d_jacT, d_forces, d_forces4, d_scalars, d_struct_aw;
   double sum_weights = 0.0;
 
   // optimiser state (device)

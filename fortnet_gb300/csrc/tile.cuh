@@ -269,7 +269,8 @@ template <typename T> struct TileArgs {
   // forces
   int ng;
   const T *J;
-  double *F;
+  double *F;     // FP64 kernels: [N][nout][3]
+  float4 *F4;    // FP32 kernels: [N][nout] (x, y, z, unused), converted into F afterwards
   int out_index, nout;
 };
 
