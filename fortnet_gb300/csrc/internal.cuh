@@ -197,6 +197,13 @@ struct fnetg_ctx {
   bool pslab = false;
   int64_t pslots = 0;       // allocated pair slots (P when compact)
   int64_t nb_cap_hint = 0;  // per-atom capacity for the next slab build (0: count first)
+  // lattice-point tables of the last build, reused while the lattices, periodic flags, cutoff
+  // and cutoff classes are unchanged (coordinates may move)
+  bool nbimg_valid = false;
+  double nbimg_rcut = 0.0;
+  std::vector<double> nbimg_lat, nbimg_rcls;
+  std::vector<int32_t> nbimg_periodic, nbimg_ranges;
+  double nbimg_shift = 0.0;  // largest translation of an image over all structures
   int64_t nb_hint_n = -1;   // atom count the capacity was measured on
   fnetg::DBuf d_pcount, d_poff, d_pend, d_pj, d_pmeta, d_rij, d_d2, d_scan_tmp, d_maxp, d_rcls2;
 
@@ -227,6 +234,7 @@ struct fnetg_ctx {
   int mlp_cfg[6] = {-1, -1, -1, -1, -1, -1};
   std::vector<int32_t> mlp_dims;
   fnetg::DBuf d_params64, d_params, d_ref_of_compute, d_sp_tile0;
+  std::vector<int64_t> h_ref_of_compute;  // the table last uploaded to d_ref_of_compute
   fnetg::DBuf d_gchunk;  // FP64 gradient sums of tile chunks
 
   // outputs / training

@@ -770,9 +770,14 @@ int run_mlp(fnetg_ctx *ctx, int kind, const Layouts &Lo, MlpArgs<T> &a, const ch
 
 template <typename T> int do_params(fnetg_ctx *ctx) {
   const Layouts Lo = make_layouts(ctx);
-  FNETG_CUDA(ctx->d_ref_of_compute.ensure(sizeof(int64_t) * std::max<int64_t>(Lo.net.pstride, 1)));
-  FNETG_CUDA(copy_sync(ctx, ctx->d_ref_of_compute.p, Lo.ref_of_compute.data(),
-                        sizeof(int64_t) * Lo.net.pstride, cudaMemcpyHostToDevice));
+  // the index table changes with the network shape only: uploaded (and waited for) when it
+  // differs from the one on the device
+  if (Lo.ref_of_compute != ctx->h_ref_of_compute) {
+    FNETG_CUDA(ctx->d_ref_of_compute.ensure(sizeof(int64_t) * std::max<int64_t>(Lo.net.pstride, 1)));
+    FNETG_CUDA(copy_sync(ctx, ctx->d_ref_of_compute.p, Lo.ref_of_compute.data(),
+                          sizeof(int64_t) * Lo.net.pstride, cudaMemcpyHostToDevice));
+    ctx->h_ref_of_compute = Lo.ref_of_compute;
+  }
   FNETG_CUDA(ctx->d_params.ensure(sizeof(T) * ctx->nsp * Lo.net.pstride));
   dim3 grid(ceil_div(Lo.net.pstride, 256), ctx->nsp);
   LaunchScope ls(ctx, "params");

@@ -453,76 +453,104 @@ int run_neighbors(fnetg_ctx *ctx, double rcut) {
   const int64_t N = ctx->N;
   const int S = ctx->S;
   FNETG_CHECK(rcut > 0.0, FNETG_E_INVALID, "neighbour cutoff must be > 0");
-  std::vector<int32_t> ranges((size_t)6 * std::max(S, 1), 0);
-  for (int s = 0; s < S; s++) {
-    if (!ctx->h_periodic[s]) continue;
-    if (fnetg_lattice_ranges(ctx->h_lat.data() + 9 * s, rcut, ranges.data() + 6 * s))
-      return fail(ctx, FNETG_E_GEOMETRY, "dependent lattice vectors");
-    for (int c = 0; c < 6; c++)
-      FNETG_CHECK(std::abs(ranges[6 * s + c]) <= 127, FNETG_E_UNSUPPORTED,
-                  "more than 127 periodic images along a lattice vector");
-  }
-  // lattice points of every structure in the iterator's order (latpointiter.F90:121-174,
-  // origin excluded) with the cell vector matmul(latVecs, n) summed in index order
-  std::vector<int64_t> img_off(S + 1, 0);
-  std::vector<V4<double>> imgs;
-  std::vector<V4<float>> imgs_f;
-  for (int s = 0; s < S; s++) {
-    img_off[s] = (int64_t)imgs.size();
-    if (!ctx->h_periodic[s]) continue;
-    const int32_t *r = ranges.data() + 6 * s;
-    const double *L = ctx->h_lat.data() + 9 * s;
-    for (int n1 = r[0]; n1 <= r[1]; n1++)
-      for (int n2 = r[2]; n2 <= r[3]; n2++)
-        for (int n3 = r[4]; n3 <= r[5]; n3++) {
-          if (n1 == 0 && n2 == 0 && n3 == 0) continue;
-          double cv[3];
-          for (int c = 0; c < 3; c++) {
-            double v = L[c + 0] * (double)n1;
-            v = v + L[c + 3] * (double)n2;
-            v = v + L[c + 6] * (double)n3;
-            cv[c] = v;
+  // the lattice-point tables and the cutoff-class uploads depend on the lattices, periodic
+  // flags, cutoff and cutoff classes only: rebuilt when one of them changed
+  const bool reuse = ctx->nbimg_valid && ctx->nbimg_rcut == rcut && ctx->nbimg_lat == ctx->h_lat &&
+                     ctx->nbimg_periodic == ctx->h_periodic && ctx->nbimg_rcls == ctx->rcut_classes;
+  if (!reuse) {
+    ctx->nbimg_valid = false;
+    std::vector<int32_t> ranges((size_t)6 * std::max(S, 1), 0);
+    for (int s = 0; s < S; s++) {
+      if (!ctx->h_periodic[s]) continue;
+      if (fnetg_lattice_ranges(ctx->h_lat.data() + 9 * s, rcut, ranges.data() + 6 * s))
+        return fail(ctx, FNETG_E_GEOMETRY, "dependent lattice vectors");
+      for (int c = 0; c < 6; c++)
+        FNETG_CHECK(std::abs(ranges[6 * s + c]) <= 127, FNETG_E_UNSUPPORTED,
+                    "more than 127 periodic images along a lattice vector");
+    }
+    // lattice points of every structure in the iterator's order (latpointiter.F90:121-174,
+    // origin excluded) with the cell vector matmul(latVecs, n) summed in index order
+    std::vector<int64_t> img_off(S + 1, 0);
+    std::vector<V4<double>> imgs;
+    std::vector<V4<float>> imgs_f;
+    for (int s = 0; s < S; s++) {
+      img_off[s] = (int64_t)imgs.size();
+      if (!ctx->h_periodic[s]) continue;
+      const int32_t *r = ranges.data() + 6 * s;
+      const double *L = ctx->h_lat.data() + 9 * s;
+      for (int n1 = r[0]; n1 <= r[1]; n1++)
+        for (int n2 = r[2]; n2 <= r[3]; n2++)
+          for (int n3 = r[4]; n3 <= r[5]; n3++) {
+            if (n1 == 0 && n2 == 0 && n3 == 0) continue;
+            double cv[3];
+            for (int c = 0; c < 3; c++) {
+              double v = L[c + 0] * (double)n1;
+              v = v + L[c + 3] * (double)n2;
+              v = v + L[c + 6] * (double)n3;
+              cv[c] = v;
+            }
+            const uint64_t packed = (uint64_t)((uint32_t)(uint8_t)(int8_t)n1 |
+                                               ((uint32_t)(uint8_t)(int8_t)n2 << 8) |
+                                               ((uint32_t)(uint8_t)(int8_t)n3 << 16));
+            double w;
+            std::memcpy(&w, &packed, sizeof w);
+            imgs.push_back(V4<double>{cv[0], cv[1], cv[2], w});
+            float h[3], l[3];
+            for (int c = 0; c < 3; c++) {
+              h[c] = (float)cv[c];
+              l[c] = (float)(cv[c] - (double)h[c]);
+            }
+            float pw;
+            const uint32_t p32 = (uint32_t)packed;
+            std::memcpy(&pw, &p32, sizeof pw);
+            imgs_f.push_back(V4<float>{h[0], h[1], h[2], pw});
+            imgs_f.push_back(V4<float>{l[0], l[1], l[2], 0.f});
           }
-          const uint64_t packed = (uint64_t)((uint32_t)(uint8_t)(int8_t)n1 |
-                                             ((uint32_t)(uint8_t)(int8_t)n2 << 8) |
-                                             ((uint32_t)(uint8_t)(int8_t)n3 << 16));
-          double w;
-          std::memcpy(&w, &packed, sizeof w);
-          imgs.push_back(V4<double>{cv[0], cv[1], cv[2], w});
-          float h[3], l[3];
-          for (int c = 0; c < 3; c++) {
-            h[c] = (float)cv[c];
-            l[c] = (float)(cv[c] - (double)h[c]);
-          }
-          float pw;
-          const uint32_t p32 = (uint32_t)packed;
-          std::memcpy(&pw, &p32, sizeof pw);
-          imgs_f.push_back(V4<float>{h[0], h[1], h[2], pw});
-          imgs_f.push_back(V4<float>{l[0], l[1], l[2], 0.f});
+    }
+    img_off[S] = (int64_t)imgs.size();
+    FNETG_CUDA(ctx->d_img_off.ensure(sizeof(int64_t) * (S + 1)));
+    FNETG_CUDA(ctx->d_imgs.ensure(sizeof(V4<double>) * std::max<size_t>(imgs.size(), 1)));
+    FNETG_CUDA(ctx->d_imgs_f.ensure(sizeof(V4<float>) * std::max<size_t>(imgs_f.size(), 1)));
+    FNETG_CUDA(cudaMemcpyAsync(ctx->d_img_off.p, img_off.data(), sizeof(int64_t) * (S + 1),
+                               cudaMemcpyHostToDevice, ctx->stream));
+    if (!imgs.empty()) {
+      FNETG_CUDA(cudaMemcpyAsync(ctx->d_imgs.p, imgs.data(), sizeof(V4<double>) * imgs.size(),
+                                 cudaMemcpyHostToDevice, ctx->stream));
+      FNETG_CUDA(cudaMemcpyAsync(ctx->d_imgs_f.p, imgs_f.data(), sizeof(V4<float>) * imgs_f.size(),
+                                 cudaMemcpyHostToDevice, ctx->stream));
+    }
+    // cutoff classes must contain the search cutoff's membership for the G-functions
+    FNETG_CUDA(ctx->d_rcls.ensure(sizeof(double) * kMaxRcutClasses));
+    if (!ctx->rcut_classes.empty())
+      FNETG_CUDA(cudaMemcpyAsync(ctx->d_rcls.p, ctx->rcut_classes.data(),
+                                 sizeof(double) * ctx->rcut_classes.size(), cudaMemcpyHostToDevice,
+                                 ctx->stream));
+    // the farthest image translation over all structures
+    double shift_max = 0.0;
+    for (int s = 0; s < S; s++) {
+      double shift = 0.0;
+      if (ctx->h_periodic[s]) {
+        for (int k = 0; k < 3; k++) {
+          const double *col = ctx->h_lat.data() + 9 * s + 3 * k;
+          const double len = std::sqrt(col[0] * col[0] + col[1] * col[1] + col[2] * col[2]);
+          const int nmax = std::max(std::abs(ranges[6 * s + 2 * k]), std::abs(ranges[6 * s + 2 * k + 1]));
+          shift += len * nmax;
         }
-  }
-  img_off[S] = (int64_t)imgs.size();
-  FNETG_CUDA(ctx->d_img_off.ensure(sizeof(int64_t) * (S + 1)));
-  FNETG_CUDA(ctx->d_imgs.ensure(sizeof(V4<double>) * std::max<size_t>(imgs.size(), 1)));
-  FNETG_CUDA(ctx->d_imgs_f.ensure(sizeof(V4<float>) * std::max<size_t>(imgs_f.size(), 1)));
-  FNETG_CUDA(cudaMemcpyAsync(ctx->d_img_off.p, img_off.data(), sizeof(int64_t) * (S + 1),
-                             cudaMemcpyHostToDevice, ctx->stream));
-  if (!imgs.empty()) {
-    FNETG_CUDA(cudaMemcpyAsync(ctx->d_imgs.p, imgs.data(), sizeof(V4<double>) * imgs.size(),
-                               cudaMemcpyHostToDevice, ctx->stream));
-    FNETG_CUDA(cudaMemcpyAsync(ctx->d_imgs_f.p, imgs_f.data(), sizeof(V4<float>) * imgs_f.size(),
-                               cudaMemcpyHostToDevice, ctx->stream));
+      }
+      shift_max = std::max(shift_max, shift);
+    }
+    ctx->nbimg_shift = shift_max;
+    ctx->nbimg_rcut = rcut;
+    ctx->nbimg_lat = ctx->h_lat;
+    ctx->nbimg_periodic = ctx->h_periodic;
+    ctx->nbimg_rcls = ctx->rcut_classes;
+    ctx->nbimg_valid = true;
   }
   FNETG_CUDA(ctx->d_pcount.ensure(sizeof(int64_t) * std::max<int64_t>(N, 1)));
   FNETG_CUDA(ctx->d_poff.ensure(sizeof(int64_t) * (N + 1)));
   FNETG_CUDA(ctx->d_maxp.ensure(sizeof(int) * 4));
   FNETG_CUDA(cudaMemsetAsync(ctx->d_maxp.p, 0, sizeof(int) * 4, ctx->stream));
-  // cutoff classes must contain the search cutoff's membership for the G-functions
-  std::vector<double> rcls = ctx->rcut_classes;
-  FNETG_CUDA(ctx->d_rcls.ensure(sizeof(double) * kMaxRcutClasses));
-  if (!rcls.empty())
-    FNETG_CUDA(cudaMemcpyAsync(ctx->d_rcls.p, rcls.data(), sizeof(double) * rcls.size(),
-                               cudaMemcpyHostToDevice, ctx->stream));
+  const std::vector<double> &rcls = ctx->rcut_classes;
   NbArgs a{};
   a.off = ctx->d_off.as<int64_t>();
   a.astruct = ctx->d_atom_struct.as<int32_t>();
@@ -539,20 +567,7 @@ int run_neighbors(fnetg_ctx *ctx, double rcut) {
   // are at most `reach` in magnitude (box extent plus the farthest image translation); each of
   // the few float roundings of a component difference is below 2^-23 * reach, so the squared
   // distance is off by less than 8 * 2^-23 * reach * rcut + 2^-20 * rcut^2.
-  double reach = 0.0;
-  for (int s = 0; s < S; s++) {
-    double shift = 0.0;
-    if (ctx->h_periodic[s]) {
-      for (int k = 0; k < 3; k++) {
-        const double *col = ctx->h_lat.data() + 9 * s + 3 * k;
-        const double len = std::sqrt(col[0] * col[0] + col[1] * col[1] + col[2] * col[2]);
-        const int nmax = std::max(std::abs(ranges[6 * s + 2 * k]), std::abs(ranges[6 * s + 2 * k + 1]));
-        shift += len * nmax;
-      }
-    }
-    reach = std::max(reach, shift);
-  }
-  reach += ctx->max_extent + rcut;
+  const double reach = ctx->nbimg_shift + ctx->max_extent + rcut;
   auto margin = [&](double rc) { return 16.0 * 1.2e-7 * reach * rc + 1e-6 * rc * rc + 1e-6; };
   a.rc2_lo = (float)(rcut * rcut - margin(rcut));
   a.rc2_hi = (float)(rcut * rcut + margin(rcut));
