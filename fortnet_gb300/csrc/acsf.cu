@@ -531,12 +531,7 @@ template <typename T> void fill_tile_args(fnetg_ctx *ctx, TileArgs<T> &a) {
   a.angp = static_cast<const T *>(dbl ? ctx->d_angpar_d.p : ctx->d_angpar_f.p);
   a.groups = ctx->d_groups.as<AGroup>();
   a.ngroups = (int)ctx->h_groups.size();
-  a.ecls_eta = static_cast<const T *>(dbl ? ctx->d_ecls_eta.p : ctx->d_ecls_eta_f.p);
-  a.ecls_rclass = ctx->d_ecls_rclass.as<int>();
-  a.ecls_atomid = ctx->d_ecls_atomid.as<int>();
-  a.necls = (int)ctx->ecls_eta.size();
-  a.rcls = static_cast<const T *>(dbl ? ctx->d_rcls.p : ctx->d_rcls_f.p);
-  a.nrcls = (int)ctx->rcut_classes.size();
+  fill_class_tables<T>(ctx, a);
   a.nz = (int)ctx->zcodes.size();
   a.cap = std::max(32, (ctx->max_pairs + 31) / 32 * 32);
   a.mfunc = ctx->d_mfunc.as<MFunc>();

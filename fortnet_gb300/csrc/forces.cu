@@ -292,8 +292,14 @@ __global__ void __launch_bounds__(kForcesThreads<T>, sizeof(T) == 4 ? 5 : 1)
   for (int64_t i = (int64_t)blockIdx.x * wpb + warp; i < a.natoms; i += (int64_t)gridDim.x * wpb) {
     const int64_t p0 = a.poff[i];
     const int np = (int)(a.pend[i] - p0);
-    for (int g = lane; g < a.ng; g += 32) tl.jv[g] = a.J[i * a.nf + g];
+    // this atom's dE/dG row and cached moments: asynchronous copies overlapping the staging
+    // (the previous atom's readers finished at the loop's closing warp barrier)
+    async_copy<T>(tl.jv, a.J + i * a.nf, a.ng, lane);
+    if (D > 0 && a.ncombo > 0 && a.mom_cached)
+      async_copy<T>(tl.M, a.mom + i * (a.ncombo * n_mono_of(D > 0 ? D : 1)),
+                    a.ncombo * n_mono_of(D > 0 ? D : 1), lane);
     stage_tile<T>(a, tl, i, p0, np, lane, true);
+    async_copy_wait();
     if (a.rad_fast >= 0) {
       // ---- radial, fast path (G2 only, one cutoff class, no atom ids): per pair
       //   dE/dr = dfc sum_g J_g e_g - 2 fc sum_g J_g eta_g x_g e_g,  x_g = r - rs_g,
@@ -396,9 +402,7 @@ __global__ void __launch_bounds__(kForcesThreads<T>, sizeof(T) == 4 ? 5 : 1)
     if (D > 0 && a.ncombo > 0) {
       constexpr int NM = n_mono_of(D > 0 ? D : 1);
       if (a.mom_cached) {
-        const T *src = a.mom + i * (a.ncombo * NM);
-        for (int k = lane; k < a.ncombo * NM; k += 32) tl.M[k] = src[k];
-        __syncwarp();
+        // copied with the dE/dG row above
       } else {
         compute_moments<T, (D > 0 ? D : 1)>(a, tl, np, lane);
       }
@@ -543,12 +547,7 @@ template <typename T> void fill_tile_args_forces(fnetg_ctx *ctx, TileArgs<T> &a)
   a.angp = static_cast<const T *>(dbl ? ctx->d_angpar_d.p : ctx->d_angpar_f.p);
   a.groups = ctx->d_groups.as<AGroup>();
   a.ngroups = (int)ctx->h_groups.size();
-  a.ecls_eta = static_cast<const T *>(dbl ? ctx->d_ecls_eta.p : ctx->d_ecls_eta_f.p);
-  a.ecls_rclass = ctx->d_ecls_rclass.as<int>();
-  a.ecls_atomid = ctx->d_ecls_atomid.as<int>();
-  a.necls = (int)ctx->ecls_eta.size();
-  a.rcls = static_cast<const T *>(dbl ? ctx->d_rcls.p : ctx->d_rcls_f.p);
-  a.nrcls = (int)ctx->rcut_classes.size();
+  fill_class_tables<T>(ctx, a);
   a.nz = (int)ctx->zcodes.size();
   a.cap = std::max(32, (ctx->max_pairs + 31) / 32 * 32);
   a.mfunc = ctx->d_mfunc.as<MFunc>();

@@ -230,11 +230,12 @@ template <typename T> struct TileArgs {
   const T *angp;          // [nang][8]
   const AGroup *groups;
   int ngroups;
-  const T *ecls_eta;
-  const int *ecls_rclass;
-  const int *ecls_atomid;
+  // eta classes and cutoff classes as kernel parameters (read per pair by the staging)
+  T ecls_eta[kMaxEtaClasses];
+  int ecls_rclass[kMaxEtaClasses];
+  int ecls_atomid[kMaxEtaClasses];
   int necls;
-  const T *rcls;
+  T rcls[kMaxRcutClasses];
   int nrcls;
   int nz;
   int cap;
@@ -394,6 +395,52 @@ __device__ Tile<T> carve_tile(unsigned char *p, const TileArgs<T> &a, bool force
   return t;
 }
 
+// Asynchronous global -> shared copy of n elements (cp.async, lanes striding): 16-byte pieces
+// when both ends are 16-byte aligned and the length a multiple of 16 bytes, else element-sized
+// pieces.  One commit group per call; async_copy_wait completes every group of the lane and
+// synchronises the warp.
+template <typename T>
+__device__ __forceinline__ void async_copy(T *dst, const T *src, int n, int lane) {
+  static_assert(sizeof(T) == 4 || sizeof(T) == 8, "element size");
+  const uintptr_t da = reinterpret_cast<uintptr_t>(dst), sa = reinterpret_cast<uintptr_t>(src);
+  const size_t bytes = sizeof(T) * (size_t)n;
+  if (((da | sa) & 15u) == 0 && (bytes & 15u) == 0) {
+    const int n16 = (int)(bytes / 16);
+    for (int k = lane; k < n16; k += 32) {
+      const unsigned d = (unsigned)__cvta_generic_to_shared(reinterpret_cast<char *>(dst) + 16 * (size_t)k);
+      asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d),
+                   "l"(reinterpret_cast<const char *>(src) + 16 * (size_t)k)
+                   : "memory");
+    }
+  } else {
+    for (int k = lane; k < n; k += 32) {
+      const unsigned d = (unsigned)__cvta_generic_to_shared(dst + k);
+      asm volatile("cp.async.ca.shared.global [%0], [%1], %2;\n" ::"r"(d), "l"(src + k),
+                   "n"((int)sizeof(T))
+                   : "memory");
+    }
+  }
+  asm volatile("cp.async.commit_group;\n" ::: "memory");
+}
+__device__ __forceinline__ void async_copy_wait() {
+  asm volatile("cp.async.wait_all;\n" ::: "memory");
+  __syncwarp();
+}
+
+// The eta-class and cutoff-class tables of the context, in the kernels' width.
+template <typename T> inline void fill_class_tables(const fnetg_ctx *ctx, TileArgs<T> &a) {
+  a.necls = (int)ctx->ecls_eta.size();
+  for (int e = 0; e < kMaxEtaClasses; e++) {
+    const bool on = e < a.necls;
+    a.ecls_eta[e] = on ? (T)ctx->ecls_eta[e] : (T)0;
+    a.ecls_rclass[e] = on ? ctx->ecls_rclass[e] : 0;
+    a.ecls_atomid[e] = on ? ctx->ecls_atomid[e] : 0;
+  }
+  a.nrcls = (int)ctx->rcut_classes.size();
+  for (int c = 0; c < kMaxRcutClasses; c++)
+    a.rcls[c] = c < a.nrcls ? (T)ctx->rcut_classes[c] : (T)0;
+}
+
 // Warps per CTA for a warp-per-atom kernel whose CTA needs `fixed` + wpb * `per_warp` bytes of
 // dynamic shared memory: the choice among 8, 4, 2, 1 (at most max_w, the kernel's launch bound)
 // with the most resident warps per SM (ties go to the larger CTA).  Raises the kernel's
@@ -427,20 +474,19 @@ inline cudaError_t pick_warps(K kernel, size_t fixed, size_t per_warp, int &wpb,
   return raise_smem_limit(reinterpret_cast<const void *>(kernel), smem);
 }
 
-// Stage the pair tile of atom i (all lanes), build the ordered species lists.
+// One pair of the tile: displacement, unit vector, neighbour, flags, cutoff tables and (when
+// the tile keeps them) the eta-class tables.
 template <typename T>
-__device__ void stage_tile(const TileArgs<T> &a, Tile<T> &t, int64_t i, int64_t p0, int np,
-                           int lane, bool forces) {
-  for (int q = lane; q < np; q += 32) {
-    const V4<T> v = a.rij[p0 + q];
+__device__ __forceinline__ void stage_pair(const TileArgs<T> &a, Tile<T> &t, int64_t i, int q,
+                                           const V4<T> v, int32_t j, uint32_t meta, int c,
+                                           bool forces) {
+  {
     if (t.v) t.v[q] = v;
     const T rinv = (T)1 / v.w;
     t.u[q] = V4<T>{v.x * rinv, v.y * rinv, v.z * rinv, v.w};
     if (forces) t.w[q] = V4<T>{0, 0, 0, 0};
-    const int32_t j = a.pj[p0 + q];
     t.pj[q] = j;
-    const uint32_t rmask = a.pmeta[p0 + q] >> 24;
-    const int c = a.code[j];
+    const uint32_t rmask = meta >> 24;
     t.info[q] = (uint32_t)(c & 0xff) | ((uint32_t)(j == i) << 8) | (rmask << 16);
     for (int rc = 0; rc < a.nrcls; rc++) {
       const T rcut = a.rcls[rc];
@@ -462,6 +508,34 @@ __device__ void stage_tile(const TileArgs<T> &a, Tile<T> &t, int64_t i, int64_t 
       if (forces) t.D[e * a.cap + q] = ex * (t.dfc[rc * a.cap + q] - (T)2 * eta * v.w * f) * ids;
     }
   }
+}
+
+// Stage the pair tile of atom i (all lanes), build the ordered species lists.  A lane takes
+// pairs q and q + 32 together: both pair records and both neighbour species are requested
+// before either is used, so the two memory round trips overlap.
+template <typename T>
+__device__ void stage_tile(const TileArgs<T> &a, Tile<T> &t, int64_t i, int64_t p0, int np,
+                           int lane, bool forces) {
+  for (int q0 = 0; q0 < np; q0 += 64) {
+    const int qa = q0 + lane, qb = q0 + 32 + lane;
+    const bool ha = qa < np, hb = qb < np;
+    V4<T> va{}, vb{};
+    int32_t ja = 0, jb = 0;
+    uint32_t ma = 0, mb = 0;
+    if (ha) {
+      va = a.rij[p0 + qa];
+      ja = a.pj[p0 + qa];
+      ma = a.pmeta[p0 + qa];
+    }
+    if (hb) {
+      vb = a.rij[p0 + qb];
+      jb = a.pj[p0 + qb];
+      mb = a.pmeta[p0 + qb];
+    }
+    const int ca = ha ? a.code[ja] : 0, cb = hb ? a.code[jb] : 0;
+    if (ha) stage_pair<T>(a, t, i, qa, va, ja, ma, ca, forces);
+    if (hb) stage_pair<T>(a, t, i, qb, vb, jb, mb, cb, forces);
+  }
   __syncwarp();
   for (int z = 0; z < a.nz; z++) {
     int base = 0;
@@ -480,6 +554,7 @@ __device__ void stage_tile(const TileArgs<T> &a, Tile<T> &t, int64_t i, int64_t 
   }
   __syncwarp();
 }
+
 
 // Sum of v[0..31] over the warp's lanes, returned on lane l for index l: each of the five
 // butterfly steps exchanges half of the remaining values (31 shuffles instead of 160).
