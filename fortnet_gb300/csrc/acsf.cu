@@ -172,7 +172,16 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 1)
     const int64_t p0 = a.poff[i];
     const int np = (int)(a.pend[i] - p0);
     const int64_t row = a.bpos[i];
+    // the next atom of this warp: its pair range requested now, its records prefetched into
+    // L2 once the range has arrived (after the staging)
+    const int64_t inext = i + (int64_t)gridDim.x * wpb;
+    int64_t nx0 = 0, nx1 = 0;
+    if (inext < a.natoms) {
+      nx0 = a.poff[inext];
+      nx1 = a.pend[inext];
+    }
     stage_tile<T>(a, t, i, p0, np, lane, false);
+    prefetch_pairs<T>(a, nx0, nx1, lane);
     if (D > 0 && a.ncombo > 0) {
       compute_moments<T, (D > 0 ? D : 1)>(a, t, np, lane);
       if (a.mom) {

@@ -300,6 +300,7 @@ __global__ void __launch_bounds__(kForcesThreads<T>, sizeof(T) == 4 ? 5 : 1)
                     a.ncombo * n_mono_of(D > 0 ? D : 1), lane);
     stage_tile<T>(a, tl, i, p0, np, lane, true);
     async_copy_wait();
+
     if (a.rad_fast >= 0) {
       // ---- radial, fast path (G2 only, one cutoff class, no atom ids): per pair
       //   dE/dr = dfc sum_g J_g e_g - 2 fc sum_g J_g eta_g x_g e_g,  x_g = r - rs_g,

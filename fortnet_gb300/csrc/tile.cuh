@@ -427,6 +427,25 @@ __device__ __forceinline__ void async_copy_wait() {
   __syncwarp();
 }
 
+// L2 prefetch of [p, p + bytes): one 128-byte line per lane and instruction.
+__device__ __forceinline__ void prefetch_l2(const void *p, size_t bytes, int lane) {
+  const uintptr_t b = reinterpret_cast<uintptr_t>(p);
+  const uintptr_t end = b + bytes;
+  for (uintptr_t l = (b & ~uintptr_t(127)) + 128u * (uintptr_t)lane; l < end; l += 128u * 32u)
+    asm volatile("prefetch.global.L2 [%0];" ::"l"(l));
+}
+
+// Pair records of a later atom [p0, p1) brought into L2 while the current atom is processed.
+template <typename T>
+__device__ __forceinline__ void prefetch_pairs(const TileArgs<T> &a, int64_t p0, int64_t p1,
+                                               int lane) {
+  if (p1 <= p0) return;
+  const size_t n = (size_t)(p1 - p0);
+  prefetch_l2(a.rij + p0, sizeof(V4<T>) * n, lane);
+  prefetch_l2(a.pj + p0, sizeof(int32_t) * n, lane);
+  prefetch_l2(a.pmeta + p0, sizeof(uint32_t) * n, lane);
+}
+
 // The eta-class and cutoff-class tables of the context, in the kernels' width.
 template <typename T> inline void fill_class_tables(const fnetg_ctx *ctx, TileArgs<T> &a) {
   a.necls = (int)ctx->ecls_eta.size();
