@@ -681,6 +681,28 @@ int fnetg_set_gfunctions(fnetg_ctx *ctx, int32_t ng, const fnetg_gfunc *g) {
     pack.insert(pack.end(), qg_ko.begin(), qg_ko.end());
     pack.insert(pack.end(), qg_foff.begin(), qg_foff.end());
     for (int32_t f : qg_f) pack.push_back(ctx->h_mfunc[f].out);
+    // adjoint rows (list channel zz in 0..nz, row nz the all-atom list only; eta class e):
+    // [rows + 1] term offsets, then the terms g | ko << 16 over the groups of the row's own
+    // combo and of the all-atom combo of the same class
+    {
+      const int nrows = (nz + 1) * ne;
+      std::vector<int32_t> roff(1, 0), terms;
+      for (int zz = 0; zz <= nz; zz++)
+        for (int e = 0; e < ne; e++) {
+          const int ks = zz < nz ? ctx->h_cidx[(size_t)(zz + 1) * ne + e] : -1;
+          const int ka = ctx->h_cidx[e];
+          for (int k : {ks, ka}) {
+            if (k < 0) continue;
+            for (int g = qg_off[k]; g < qg_off[k + 1]; g++) terms.push_back(g | (qg_ko[g] << 16));
+          }
+          roff.push_back((int32_t)terms.size());
+        }
+      FNETG_CHECK((int)roff.size() == nrows + 1, FNETG_E_CUDA, "adjoint rows");
+      FNETG_CHECK(qg_ko.size() < 65536 && ctx->n_combo < 32768, FNETG_E_UNSUPPORTED,
+                  "too many moment partner groups");
+      pack.insert(pack.end(), roff.begin(), roff.end());
+      pack.insert(pack.end(), terms.begin(), terms.end());
+    }
     std::vector<double> epc;
     for (int32_t f : qg_f)
       epc.insert(epc.end(), ctx->h_mpc.begin() + (size_t)f * (kMaxMomentDegree + 1),

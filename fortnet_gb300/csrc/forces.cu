@@ -412,37 +412,43 @@ __global__ void __launch_bounds__(kForcesThreads<T>, sizeof(T) == 4 ? 5 : 1)
       //   h_g(m) = sum_{f in F_g} J_out(f) pc_f(m),
       //   Qc[z][e](alpha) = mult(alpha) sum_{k in {list z, all atoms}} sum_{g of k}
       //                     h_g(|alpha|) M_{ko(g)}(alpha).
-      const int32_t *qg_off = s_qg, *qg_ko = s_qg + a.ncombo + 1;
+      const int32_t *qg_ko = s_qg + a.ncombo + 1;
       const int32_t *qg_eoff = qg_ko + a.nqg, *qg_out = qg_eoff + a.nqg + 1;
+      const int32_t *row_off = qg_out + a.nqg_ent, *row_term = row_off + (a.nz + 1) * a.necls + 1;
       T *H = tl.Q;
-      for (int it = lane; it < a.nqg * KD; it += 32) {
-        const int g = it / KD, m = it - g * KD;
-        T acc = 0;
-        for (int e = qg_eoff[g]; e < qg_eoff[g + 1]; e++)
-          acc += tl.jv[qg_out[e]] * s_mpc[e * KD + m];
-        H[it] = acc;
+      // h_g(m) with lanes over groups: an entry's dE/dG weight read once for every degree
+      for (int g = lane; g < a.nqg; g += 32) {
+        T h[KD];
+#pragma unroll
+        for (int m = 0; m < KD; m++) h[m] = 0;
+        const int e1 = qg_eoff[g + 1];
+#pragma unroll 2
+        for (int e = qg_eoff[g]; e < e1; e++) {
+          const T jw = tl.jv[qg_out[e]];
+#pragma unroll
+          for (int m = 0; m < KD; m++) h[m] += jw * s_mpc[e * KD + m];
+        }
+#pragma unroll
+        for (int m = 0; m < KD; m++) H[g * KD + m] = h[m];
       }
       __syncwarp();
-      // this lane's monomials lane and lane + 32 (degree and weight fixed per kernel)
-      for (int zz = 0; zz <= a.nz; zz++)
-        for (int e = 0; e < a.necls; e++) {
-          const int ks = zz < a.nz ? s_cidx[(zz + 1) * a.necls + e] : -1;
-          const int ka = s_cidx[e];
-          T v0 = 0, v1 = 0;
-          for (int side = 0; side < 2; side++) {
-            const int k = side == 0 ? ks : ka;
-            if (k < 0) continue;
-            for (int g = qg_off[k]; g < qg_off[k + 1]; g++) {
-              const T *Mk = tl.M + qg_ko[g] * NM;
-              const T *Hg = H + g * KD;
-              if (lane < NM) v0 += Hg[mdeg0] * Mk[lane];
-              if (lane + 32 < NM) v1 += Hg[mdeg1] * Mk[lane + 32];
-            }
-          }
-          T *dst = tl.Qc + ((int64_t)zz * a.necls + e) * NM;
-          if (lane < NM) dst[lane] = mmult0 * v0;
-          if (lane + 32 < NM) dst[lane + 32] = mmult1 * v1;
+      // Qc rows from their flat term lists (partner group g, partner combo ko); this lane's
+      // monomials lane and lane + 32 (degree and weight fixed per kernel)
+      const int nrows = (a.nz + 1) * a.necls;
+      for (int r = 0; r < nrows; r++) {
+        T v0 = 0, v1 = 0;
+        const int t1 = row_off[r + 1];
+        for (int t = row_off[r]; t < t1; t++) {
+          const int tg = row_term[t];
+          const T *Mk = tl.M + (tg >> 16) * NM;
+          const T *Hg = H + (tg & 0xffff) * KD;
+          if (lane < NM) v0 += Hg[mdeg0] * Mk[lane];
+          if (lane + 32 < NM) v1 += Hg[mdeg1] * Mk[lane + 32];
         }
+        T *dst = tl.Qc + (int64_t)r * NM;
+        if (lane < NM) dst[lane] = mmult0 * v0;
+        if (lane + 32 < NM) dst[lane + 32] = mmult1 * v1;
+      }
       __syncwarp();
       constexpr int DD = D > 0 ? D : 1;
       switch (a.necls) {
