@@ -224,7 +224,7 @@ def run_ours(args):
         ms_step = float(t.item())
     # per-kernel device time inside the timed steps
     fams = ["neighbors", "scan", "acsf", "zscore", "mlp_forward", "mlp_backward",
-            "mlp_jacobian", "forces", "reduce", "loss", "optimizer", "params"]
+            "mlp_jacobian", "forces", "forces_out", "reduce", "loss", "optimizer", "params"]
     prof = {f: ctx.profile_read(f) for f in fams}
     ctx.profile(False)
     value = N * world / (ms_step / 1e3)

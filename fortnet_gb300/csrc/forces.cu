@@ -300,7 +300,6 @@ __global__ void __launch_bounds__(kForcesThreads<T>, sizeof(T) == 4 ? 5 : 1)
                     a.ncombo * n_mono_of(D > 0 ? D : 1), lane);
     stage_tile<T>(a, tl, i, p0, np, lane, true);
     async_copy_wait();
-
     if (a.rad_fast >= 0) {
       // ---- radial, fast path (G2 only, one cutoff class, no atom ids): per pair
       //   dE/dr = dfc sum_g J_g e_g - 2 fc sum_g J_g eta_g x_g e_g,  x_g = r - rs_g,
@@ -609,7 +608,7 @@ template <typename T, int D> int launch_forces_d(fnetg_ctx *ctx, TileArgs<T> &a,
   }
   if (sizeof(T) == 4) {
     const int64_t n = N * nout;
-    LaunchScope ls(ctx, "forces");
+    LaunchScope ls(ctx, "forces_out");
     forces4_to_f64_kernel<<<(int)ceil_div(n, 256), 256, 0, ctx->stream>>>(
         ctx->d_forces4.as<float4>(), ctx->d_forces.as<double>(), n);
     FNETG_CUDA(cudaGetLastError());
