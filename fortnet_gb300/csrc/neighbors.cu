@@ -174,8 +174,9 @@ __device__ __forceinline__ void store_pair(const NbArgs &a, const double *ci, co
   reinterpret_cast<V4<T> *>(a.rij)[q] = v;
 }
 
+// Four CTAs of 256 threads per SM: at most 64 registers a thread (80 unbounded, 3 CTAs)
 template <typename T, bool kFill>
-__global__ void __launch_bounds__(256) nb_kernel(NbArgs a) {
+__global__ void __launch_bounds__(256, 4) nb_kernel(NbArgs a) {
   __shared__ int blk_max;
   __shared__ unsigned long long blk_sum;
   __shared__ int2 queue_all[kNbWarps][128];  // up to 31 pending + 64 new accepted
