@@ -131,14 +131,15 @@ def device_step(ctx, zprec):
 
 
 def e2e_step(ctx, zprec, coords_pinned, out_energy, out_forces):
+    """The step through the public API with host buffers: coordinates uploaded from pinned
+    memory, per-structure energies and all forces downloaded into pinned buffers."""
     ctx.update_coords(coords_pinned)
     ctx.neighbors()
     ctx.acsf(download=False)
     ctx.zscore(zprec=zprec)
     loss, _, _ = ctx.train_iteration("mse")
-    at, gl = ctx.predict()
-    out_energy[:] = gl
-    out_forces[:] = ctx.forces()
+    ctx.predict(atomic=False, out_global=out_energy)
+    ctx.forces(out=out_forces)
     return loss
 
 
@@ -232,8 +233,8 @@ def run_ours(args):
     coords_t = torch.empty((N, 3), dtype=torch.float64, pin_memory=True)
     coords = coords_t.numpy()
     coords[:] = ds.coords
-    energy = np.zeros((ds.nstruct, 1))
-    forces = np.zeros((N, 1, 3))
+    energy = torch.empty((ds.nstruct, 1), dtype=torch.float64, pin_memory=True).numpy()
+    forces = torch.empty((N, 1, 3), dtype=torch.float64, pin_memory=True).numpy()
     for _ in range(2):
         e2e_step(ctx, zprec, coords, energy, forces)
     ctx.synchronize()

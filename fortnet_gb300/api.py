@@ -122,6 +122,12 @@ def _c(a, dtype):
     return None if a is None else np.ascontiguousarray(a, dtype=dtype)
 
 
+def _check_out(a, shape):
+    """A caller-owned output buffer must be C-contiguous float64 of the result's shape."""
+    if a.dtype != np.float64 or not a.flags["C_CONTIGUOUS"] or tuple(a.shape) != tuple(shape):
+        raise ValueError("output buffer must be C-contiguous float64 of shape %s" % (shape,))
+
+
 class Context:
     """One library context: a CUDA stream, device-resident structures, features, network."""
 
@@ -263,10 +269,17 @@ class Context:
         self._check(self.lib.fnetg_get_params(self.h, _p(out)))
         return out
 
-    def predict(self):
+    def predict(self, atomic=True, out_atomic=None, out_global=None):
+        """(atomic outputs [Ntot, nOut] or None, per-structure sums [S, nOut]).  out_atomic /
+        out_global: caller-owned C-contiguous float64 buffers to fill (for example pinned host
+        memory); atomic=False downloads the sums only (summed on the device in atom order)."""
         nout = self.dims[-1]
-        at = np.zeros((self.ntot, nout))
-        gl = np.zeros((self.nstruct, nout))
+        at = None
+        if atomic:
+            at = out_atomic if out_atomic is not None else np.zeros((self.ntot, nout))
+            _check_out(at, (self.ntot, nout))
+        gl = out_global if out_global is not None else np.zeros((self.nstruct, nout))
+        _check_out(gl, (self.nstruct, nout))
         self._check(self.lib.fnetg_predict(self.h, _p(at), _p(gl)))
         return at, gl
 
@@ -277,9 +290,12 @@ class Context:
         self._check(self.lib.fnetg_jacobian(self.h, _p(out)))
         return out
 
-    def forces(self):
+    def forces(self, out=None):
+        """Analytical forces [Ntot, nOut, 3]; out: a caller-owned float64 buffer to fill."""
         nout = self.dims[-1]
-        out = np.zeros((self.ntot, nout, 3))
+        if out is None:
+            out = np.zeros((self.ntot, nout, 3))
+        _check_out(out, (self.ntot, nout, 3))
         self._check(self.lib.fnetg_forces(self.h, _p(out)))
         return out
 

@@ -140,6 +140,20 @@ int fnetg_lattice_ranges(const double *L, double rcut, int32_t *lohi) {
 }
 
 // ---------------------------------------------------------------------------------------
+namespace fnetg {
+// Per-structure sums of the atomic outputs, one thread per (structure, output), atoms in order
+// (the host loop's order and operations: the same FP64 result)
+__global__ void struct_sum_kernel(const double *out, const int64_t *off, int S, int nout,
+                                  double *gsum) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (int64_t)S * nout) return;
+  const int s = (int)(t / nout), o = (int)(t - (int64_t)s * nout);
+  double acc = 0.0;
+  for (int64_t a = off[s]; a < off[s + 1]; a++) acc += out[a * nout + o];
+  gsum[t] = acc;
+}
+}  // namespace fnetg
+
 extern "C" {
 
 int fnetg_abi_version(void) { return FNETG_ABI_VERSION; }
@@ -1072,20 +1086,35 @@ int fnetg_predict(fnetg_ctx *ctx, double *atomic_out, double *global_out) {
   rc = run_predict(ctx);
   if (rc) return rc;
   if (!atomic_out && !global_out) return FNETG_OK;
-  FNETG_CUDA(cudaStreamSynchronize(ctx->stream));
   const int nout = ctx->dims.back();
-  std::vector<double> out((size_t)ctx->N * nout);
-  if (ctx->N > 0)
-    FNETG_CUDA(copy_sync(ctx, out.data(), ctx->d_out.p, sizeof(double) * out.size(),
+  if (atomic_out) {
+    // atomic outputs straight into the caller's buffer; the sums over each structure's atoms
+    // in atom order on the host
+    if (ctx->N > 0)
+      FNETG_CUDA(copy_sync(ctx, atomic_out, ctx->d_out.p, sizeof(double) * ctx->N * nout,
+                            cudaMemcpyDeviceToHost));
+    if (global_out) {
+      for (int s = 0; s < ctx->S; s++)
+        for (int o = 0; o < nout; o++) {
+          double acc = 0.0;
+          for (int64_t a = ctx->h_off[s]; a < ctx->h_off[s + 1]; a++)
+            acc += atomic_out[a * nout + o];
+          global_out[(size_t)s * nout + o] = acc;
+        }
+    }
+    return FNETG_OK;
+  }
+  // sums only: the same atom-order sums on the device, S * nout values downloaded
+  if (ctx->S > 0) {
+    FNETG_CUDA(ctx->d_gsum.ensure(sizeof(double) * ctx->S * nout));
+    {
+      LaunchScope ls(ctx, "struct_sum");
+      struct_sum_kernel<<<ceil_div((int64_t)ctx->S * nout, 128), 128, 0, ctx->stream>>>(
+          ctx->d_out.as<double>(), ctx->d_off.as<int64_t>(), ctx->S, nout, ctx->d_gsum.as<double>());
+      FNETG_CUDA(cudaGetLastError());
+    }
+    FNETG_CUDA(copy_sync(ctx, global_out, ctx->d_gsum.p, sizeof(double) * ctx->S * nout,
                           cudaMemcpyDeviceToHost));
-  if (atomic_out) memcpy(atomic_out, out.data(), sizeof(double) * out.size());
-  if (global_out) {
-    for (int s = 0; s < ctx->S; s++)
-      for (int o = 0; o < nout; o++) {
-        double acc = 0.0;
-        for (int64_t a = ctx->h_off[s]; a < ctx->h_off[s + 1]; a++) acc += out[a * nout + o];
-        global_out[(size_t)s * nout + o] = acc;
-      }
   }
   return FNETG_OK;
 }
