@@ -155,7 +155,9 @@ int fnetg_get_params(fnetg_ctx *ctx, double *params);
 int64_t fnetg_nparams(int32_t nlayer, const int32_t *dims);
 
 /* TBpnn_predictBatch / iPredict (bpnn.F90:1001-1058, 867-900): atomic outputs
- * atomic_out[Ntot*nout]; global_out[S*nout] = per-structure sums (may be NULL). */
+ * atomic_out[Ntot*nout]; global_out[S*nout] = per-structure sums in atom order.  Either may be
+ * NULL; with atomic_out NULL the sums are formed on the device (the same operations in the same
+ * order) and only they are copied.  Pinned host buffers copy at full link bandwidth. */
 int fnetg_predict(fnetg_ctx *ctx, double *atomic_out, double *global_out);
 /* TBpnn_nJacobian / fdevi (bpnn.F90:937-997, network.F90:183-244):
  * jac[a*nout*nf + o*nf + f] = d out_o / d feature_f of atom a. */
