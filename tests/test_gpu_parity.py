@@ -173,6 +173,34 @@ def test_acsf_values_fp64_and_fp32(kind):
     assert np.max(np.abs(g32 - ref) / scale) < 2e-5
 
 
+def radial_g2_set(kind, rcut, zs=(1, 8)):
+    """Radial G2 sets that take each path of the value kernel's radial sums: a shape x channel
+    grid with the all-atom list as one of the channels, per-function parameters that are no
+    grid (shapes differ per species), and more functions than the kernel parameters carry."""
+    g2 = lambda rs, eta, z=0: GFunction("g2", rcut, rs=rs, eta=eta, z1=z)
+    if kind == "grid_all_and_species":
+        shapes = [(0.0, 0.02), (0.0, 0.2), (1.5, 0.3), (2.5, 1.1)]
+        return [g2(rs, eta, z) for rs, eta in shapes for z in (0,) + tuple(zs)]
+    if kind == "not_grid":
+        return ([g2(0.0, 0.1, zs[0]), g2(1.5, 0.3, zs[0]), g2(0.0, 0.2, zs[1])] +
+                [g2(0.5, 0.05), g2(0.0, 0.1, zs[1]), g2(3.0, 0.7, zs[0])])
+    etas = np.geomspace(0.003, 3.0, 70)
+    return [g2(0.0 if k % 3 else 1.0, float(e), 0 if k % 2 else zs[k % 4 // 2])
+            for k, e in enumerate(etas)]
+
+
+@pytest.mark.parametrize("kind", ["grid_all_and_species", "not_grid", "over_64"])
+def test_acsf_radial_paths(kind):
+    ds = small_cell_dataset()
+    funcs = radial_g2_set(kind, 7.0) + [GFunction("g5", 7.0, eta=0.05, lam=-1.0, xi=4.0)]
+    ref = O.acsf(ds, funcs)
+    g64 = acsf_on_gpu(ds, funcs, api.FP64)
+    np.testing.assert_allclose(g64, ref, rtol=1e-11, atol=1e-13)
+    g32 = acsf_on_gpu(ds, funcs, api.FP32)
+    scale = np.maximum(np.abs(ref).max(axis=0), 1e-30)
+    assert np.max(np.abs(g32 - ref) / scale) < 2e-5
+
+
 GOLDEN_PRED = [n for n in G.case_names() if G.load_case(n).settings["mode"] != "train"]
 GOLDEN_TRAIN = [n for n in G.case_names() if G.load_case(n).settings["mode"] == "train"]
 
