@@ -73,3 +73,17 @@ def test_no_gpu_context_creation_fails_cleanly():
     h = C.c_void_p()
     rc = lib.fnetg_create(C.byref(h), 16, 0)  # invalid precision
     assert rc == -1 and not h.value
+
+
+def test_caller_output_buffers_are_checked_on_the_host():
+    """predict/forces accept caller-owned buffers only as C-contiguous float64 of the result's
+    shape (checked before the library is called)."""
+    good = np.zeros((5, 1, 3))
+    api._check_out(good, (5, 1, 3))
+    for bad in (np.zeros((5, 3)), np.zeros((5, 1, 3), dtype=np.float32),
+                np.zeros((5, 1, 6))[:, :, ::2]):
+        try:
+            api._check_out(bad, (5, 1, 3))
+        except ValueError:
+            continue
+        raise AssertionError("accepted %r" % (bad.shape,))
