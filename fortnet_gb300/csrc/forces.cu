@@ -401,11 +401,8 @@ __global__ void __launch_bounds__(kForcesThreads<T>, sizeof(T) == 4 ? 5 : 1)
     // ---- integer-xi G5 through adjoint moments
     if (D > 0 && a.ncombo > 0) {
       constexpr int NM = n_mono_of(D > 0 ? D : 1);
-      if (a.mom_cached) {
-        // copied with the dE/dG row above
-      } else {
-        compute_moments<T, (D > 0 ? D : 1)>(a, tl, np, lane);
-      }
+      // cached moments arrived with the dE/dG row; otherwise they are formed here
+      if (!a.mom_cached) compute_moments<T, (D > 0 ? D : 1)>(a, tl, np, lane);
       // Adjoint moments, factorised: coef_f(alpha) = mult(alpha) pc_f(|alpha|), so for every
       // partner group g (combo k receiving M of combo ko through functions F_g)
       //   h_g(m) = sum_{f in F_g} J_out(f) pc_f(m),
