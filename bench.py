@@ -1,22 +1,28 @@
-"""Benchmark of the ACSF + BPNN hot path on one GB300 (config C2 of the benchmark set).
+"""Benchmark of the ACSF + BPNN hot path on one GB300: the batching configuration C3.
 
-One step = one pass of the hot path over the whole C2 dataset (2,000 periodic structures of
-64-256 atoms, two species, 96 ACSF features, network 96-32-32-1 tanh, FP32):
-  featurise   neighbour search + G2/G5 values + z-score (training statistics)
-  train       one L-BFGS training iteration of the reference's nTrain loop (update with the
-              current gradient incl. line search, then forward + loss + backward + FP64
-              gradient reduction at the new parameters)
-  predict     energies and analytical forces of every atom at the new parameters
-Metric: atoms/s = atoms in the dataset / step time (train+predict).
+Workload (C3): 20,000 periodic structures of 8-2,048 atoms (log-uniform, 7.4 M atoms), three
+species, 168 ACSF features (72 radial + 96 angular after species expansion, cutoff 6 A),
+per-species networks 168-64-64-1 tanh, energy targets.  Features are computed once per run,
+as the reference does (prog/fortnet/prg_fnet/fortnet.F90:840-921), and reported separately.
 
-`value`: inputs resident in HBM, CUDA events on the library's stream around every step,
-L2 flushed (a 256 MiB write) between steps outside the timed events.
-`e2e`: the same step through the public API with host buffers: coordinates copied in, energies
-and forces copied out, inside the timed region.
+One step = one training pass over every structure + the energies of every structure:
+  batched form   one epoch of 256-structure mini-batches: per mini-batch forward, loss,
+                 reverse pass and steepest-descent step, BF16 tensor-core GEMMs with FP32
+                 accumulation, FP64 gradient sums and parameters, replayed as one CUDA graph;
+                 then a tensor-core forward over every structure
+  plain form     one L-BFGS iteration of the reference's nTrain loop on the whole dataset
+                 (FP32 SIMT kernels, FP64 reductions and optimiser state), then a forward over
+                 every structure
+Metric: atoms/s = atoms in the dataset / step time.  `value` is the batched form with inputs
+resident in HBM (L2 flushed between timed steps); `forms` gives both forms and their ratio,
+and their energy errors against an FP64 evaluation of the same parameters.
+`e2e`: the batched step through the public API from host coordinates: coordinates copied in,
+featurisation, feature packing, the epoch and the energies, the loss and the energies copied
+out, all inside the timed region.
 
 --impl reference times the CPU restatement of the reference's own algorithm (the oracle:
-neighbour list rebuilt per atom and G-function, dense dG/dR) with all host threads on a
-bounded sample of the same workload.
+neighbour list rebuilt per atom and G-function, per-atom network evaluation) with all host
+threads on a bounded sample of the same workload: featurise + one L-BFGS iteration + energies.
 """
 
 from __future__ import annotations
@@ -35,9 +41,11 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-METRIC = "atoms/s train+predict (C2: featurise + L-BFGS iteration + energies/forces)"
+METRIC = ("atoms/s train+predict (C3: one training epoch over every structure + energies; "
+          "batched mixed-precision form)")
 UNIT = "atoms/s"
 L2_FLUSH_BYTES = 256 << 20
+BATCH = 256  # structures per mini-batch (C3)
 
 
 def load_peaks():
@@ -100,81 +108,119 @@ class ClockSampler:
                 "samples": len(self.samples)}
 
 
-def setup(cfg_name, nstruct, precision):
+def oracle_params(cfg, dims):
+    """The reference's initial parameters (RANLUX lux 3 normalXavier, as TBpnn_init draws
+    them), from the oracle's restatement."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+
+    return O.Ranlux(cfg.seed).init_bpnn(dims, "tanh", len(cfg.atomic_numbers))
+
+
+def featurise(ctx, zprec=None, weights=None):
+    ctx.neighbors()
+    ctx.acsf(download=False)
+    return ctx.zscore(weights=weights, zprec=zprec)
+
+
+def setup(args):
     from fortnet_gb300 import api, synthetic
 
-    cfg = synthetic.CONFIGS[cfg_name]
-    ds = synthetic.generate(cfg, nstruct=nstruct)
+    cfg = synthetic.CONFIGS[args.config]
+    t0 = time.perf_counter()
+    ds = synthetic.generate(cfg, nstruct=args.nstruct)
+    gen_s = time.perf_counter() - t0
     funcs = synthetic.gfunctions(cfg)
     dims = synthetic.network_dims(cfg)
-    ctx = api.Context(precision)
+    ctx = api.Context(api.FP32)
     ctx.upload(ds)
     ctx.set_species(ds.species)
     ctx.set_gfunctions(funcs)
-    ctx.neighbors()
-    ctx.acsf(download=False)
-    zprec = ctx.zscore(weights=ds.weights)
-    params = api.Rng(cfg.seed).init_params(dims, len(cfg.atomic_numbers))
+    zprec = featurise(ctx, weights=ds.weights)
+    params = oracle_params(cfg, dims)
     ctx.set_network(dims, "tanh", params)
     ctx.set_targets(ds)
     ctx.optimizer_init("lbfgs", 1e-20, 1e-6, 1e4, memory=1000, linemin=True)
-    return ctx, ds, zprec, funcs, dims, params
+    ctx.batch_setup(args.batch)
+    return ctx, ds, zprec, funcs, dims, params, gen_s
 
 
-def device_step(ctx, zprec):
-    ctx.neighbors()
-    ctx.acsf(download=False)
-    ctx.zscore(zprec=zprec)
+def plain_step(ctx):
+    """The plain FP32 form: one full-batch L-BFGS iteration + energies of every atom."""
     ctx.train_iteration("mse")
     ctx.lib.fnetg_predict(ctx.h, None, None)
-    ctx.lib.fnetg_forces(ctx.h, None)
 
 
-def e2e_step(ctx, zprec, coords_pinned, out_energy, out_forces):
-    """The step through the public API with host buffers: coordinates uploaded from pinned
-    memory, per-structure energies and all forces downloaded into pinned buffers."""
+def batched_step(ctx, lr):
+    """The batched mixed-precision form: one epoch of mini-batch steps + every energy."""
+    ctx.batch_epoch("mse", lr, args_maxdisp(), want_loss=False)
+    ctx.lib.fnetg_batch_predict(ctx.h, None, None)
+
+
+def args_maxdisp():
+    return 1e4
+
+
+def e2e_step(ctx, zprec, coords_pinned, out_energy, out_loss, lr):
+    """The batched step through the public API from host coordinates: coordinates uploaded
+    from pinned memory, featurisation and feature packing, the epoch, the energies; the loss
+    and the per-structure energies downloaded into pinned buffers."""
     ctx.update_coords(coords_pinned)
-    ctx.neighbors()
-    ctx.acsf(download=False)
-    ctx.zscore(zprec=zprec)
-    loss, _, _ = ctx.train_iteration("mse")
-    ctx.predict(atomic=False, out_global=out_energy)
-    ctx.forces(out=out_forces)
-    return loss
+    featurise(ctx, zprec=zprec)
+    ctx.batch_setup(BATCH)
+    ctx.lib.fnetg_batch_epoch(ctx.h, 0, lr, args_maxdisp(), out_loss.ctypes.data)
+    ctx.batch_predict(atomic=False, out_global=out_energy)
 
 
-def algorithmic_bytes(ctx, ds, funcs, dims):
-    """Bytes each kernel family must move per launch (see DESIGN: roofline)."""
-    N, S = ds.ntot, ds.nstruct
-    P = ctx.neighbors()
-    nf = dims[0]
-    fp = 4
-    return {
-        # positions (24 B double + 16 B float) per candidate atom read once per image-visited
-        # structure is L1/L2 traffic; HBM: per atom coords + pair records written
-        "neighbors": N * (24 + 16 + 8) + P * (4 + 4 + 16 + 8),
-        # pair records in, feature rows out
-        "acsf": P * (16 + 4 + 4) + N * (8 + 4) + P * 1 + N * nf * fp,
-        "forces": P * (16 + 4 + 4) + N * nf * fp + N * 8 + P * 24,
-        "mlp_forward": N * nf * fp + N * 8,
-        "mlp_backward": N * nf * fp + N * 8,
-        "mlp_jacobian": N * nf * fp + N * nf * fp,
-        "zscore": 2 * N * (nf - 0) * fp,
-    }
+def timed(ctx, fn, steps, stream, flush, torch):
+    """CUDA-event time of each step on the library's stream, L2 flushed between steps."""
+    times = []
+    for _ in range(steps):
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        fn()
+        e1.record(stream)
+        e1.synchronize()
+        times.append(e0.elapsed_time(e1))
+    return times
 
 
-def profiled_traffic(kernel, config, natoms):
-    """DRAM bytes per launch of `kernel` from the committed ncu summary of this configuration
-    (bytes per atom measured on a small capture of the same workload, scaled by atoms)."""
-    path = os.path.join(ROOT, "profiles", f"{kernel}_kernel_{config}.md")
-    if not os.path.exists(path):
-        return None, None
-    with open(path) as fh:
-        for line in fh:
-            if line.startswith("dram_bytes_per_atom:"):
-                per_atom = float(line.split(":", 1)[1])
-                return int(per_atom * natoms), os.path.relpath(path, ROOT)
-    return None, None
+def energy_errors(ctx, ds, funcs, zprec, dims, nsample=64):
+    """Per-structure energy errors of both forms against an FP64 evaluation of the same
+    parameters, on the first structures of the dataset."""
+    from fortnet_gb300 import api
+
+    params = ctx.params()
+    _, e_tc = ctx.batch_predict(atomic=False)
+    ctx.lib.fnetg_batch_sync_params(ctx.h)
+    _, e_32 = ctx.predict(atomic=False)
+    k = min(nsample, ds.nstruct)
+    sub_off = ds.atom_offsets[:k + 1]
+    from fortnet_gb300.fnetdata import Dataset
+
+    n = int(sub_off[-1])
+    sub = Dataset(atom_offsets=sub_off, coords=ds.coords[:n], atnum=ds.atnum[:n],
+                  species=ds.species[:n], periodic=ds.periodic[:k], latvecs=ds.latvecs[:k],
+                  atomic_numbers=ds.atomic_numbers, weights=ds.weights[:k],
+                  atomic_weights=ds.atomic_weights[:n], global_targets=ds.global_targets[:k],
+                  atomic_targets=ds.atomic_targets[:n])
+    with api.Context(api.FP64) as c:
+        c.upload(sub)
+        c.set_species(sub.species)
+        c.set_gfunctions(funcs)
+        c.acsf(download=False)
+        c.zscore(zprec=zprec)
+        c.set_network(dims, "tanh", params)
+        _, e_64 = c.predict(atomic=False)
+    ref = np.abs(e_64[:k, 0])
+    return {"structures": k,
+            "plain_fp32_energy_rel": float(f"{np.max(np.abs(e_32[:k, 0] - e_64[:k, 0]) / ref):.3g}"),
+            "batched_bf16_energy_rel": float(f"{np.max(np.abs(e_tc[:k, 0] - e_64[:k, 0]) / ref):.3g}"),
+            "batched_bf16_energy_rel_median":
+                float(f"{np.median(np.abs(e_tc[:k, 0] - e_64[:k, 0]) / ref):.3g}")}
 
 
 def run_ours(args):
@@ -191,31 +237,36 @@ def run_ours(args):
     import torch
 
     torch.cuda.set_device(local)
-    precision = api.FP32
-    ctx, ds, zprec, funcs, dims, params = setup(args.config, args.nstruct, precision)
+    ctx, ds, zprec, funcs, dims, params, gen_s = setup(args)
     stream = torch.cuda.ExternalStream(ctx.stream())
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
     N = ds.ntot
+    lr = args.lr
+    # one-time featurisation (the reference computes features once per run), timed alone
+    ctx.synchronize()
+    ctx.profile(True)
+    ctx.profile_reset()
+    feat_ms = float(np.mean(timed(ctx, lambda: featurise(ctx, zprec=zprec), 2, stream, flush,
+                                  torch)))
+    feat_prof = {f: ctx.profile_read(f) for f in ("neighbors", "scan", "acsf", "zscore")}
+    ctx.profile(False)
+    ctx.batch_setup(args.batch)
+    # plain FP32 form
     for _ in range(args.warmup):
-        device_step(ctx, zprec)
+        plain_step(ctx)
+    ctx.synchronize()
+    plain_ms = float(np.mean(timed(ctx, lambda: plain_step(ctx), args.plain_steps, stream, flush,
+                                   torch)))
+    # batched mixed-precision form (the headline): warm-up captures the epoch graph and
+    # runs the autotuner
+    for _ in range(args.warmup):
+        batched_step(ctx, lr)
     ctx.synchronize()
     if dist:
         dist.barrier()
-    ctx.profile(True)
-    ctx.profile_reset()
     launches0 = ctx.launch_count()
-    times = []
     with ClockSampler(local) as clk:
-        for _ in range(args.steps):
-            flush.fill_(1.0)
-            torch.cuda.synchronize()
-            e0 = torch.cuda.Event(enable_timing=True)
-            e1 = torch.cuda.Event(enable_timing=True)
-            e0.record(stream)
-            device_step(ctx, zprec)
-            e1.record(stream)
-            e1.synchronize()
-            times.append(e0.elapsed_time(e1))
+        times = timed(ctx, lambda: batched_step(ctx, lr), args.steps, stream, flush, torch)
     torch.cuda.synchronize()
     launches = ctx.launch_count() - launches0
     ms_step = float(np.mean(times))
@@ -223,67 +274,113 @@ def run_ours(args):
         t = torch.tensor([ms_step], dtype=torch.float64)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms_step = float(t.item())
-    # per-kernel device time inside the timed steps
-    fams = ["neighbors", "scan", "acsf", "zscore", "mlp_forward", "mlp_backward",
-            "mlp_jacobian", "forces", "forces_out", "reduce", "loss", "optimizer", "params"]
+    value = N * world / (ms_step / 1e3)
+    # per-kernel device times of one batched step, launched eagerly with CUDA events (the
+    # profiled epoch runs the same kernels without the graph)
+    ctx.profile(True)
+    ctx.profile_reset()
+    batched_step(ctx, lr)
+    ctx.synchronize()
+    fams = ["tc_forward", "tc_train", "tc_reduce", "tc_update", "tc_pack", "loss"]
     prof = {f: ctx.profile_read(f) for f in fams}
     ctx.profile(False)
-    value = N * world / (ms_step / 1e3)
+    info = ctx.batch_info()
+    errs = energy_errors(ctx, ds, funcs, zprec, dims)
     # ---- end to end through the public API with host buffers (pinned)
-    coords_t = torch.empty((N, 3), dtype=torch.float64, pin_memory=True)
-    coords = coords_t.numpy()
+    coords = torch.empty((N, 3), dtype=torch.float64, pin_memory=True).numpy()
     coords[:] = ds.coords
     energy = torch.empty((ds.nstruct, 1), dtype=torch.float64, pin_memory=True).numpy()
-    forces = torch.empty((N, 1, 3), dtype=torch.float64, pin_memory=True).numpy()
+    loss = torch.empty(1, dtype=torch.float64, pin_memory=True).numpy()
     for _ in range(2):
-        e2e_step(ctx, zprec, coords, energy, forces)
+        e2e_step(ctx, zprec, coords, energy, loss, lr)
     ctx.synchronize()
     t0 = time.perf_counter()
     esteps = max(2, min(args.steps, 5))
     for _ in range(esteps):
-        e2e_step(ctx, zprec, coords, energy, forces)
+        e2e_step(ctx, zprec, coords, energy, loss, lr)
     ctx.synchronize()
     e2e_ms = (time.perf_counter() - t0) * 1e3 / esteps
     h2d = coords.nbytes
-    d2h = energy.nbytes + forces.nbytes + 8
-    # ---- roofline of the dominant kernel family
-    hbm, _, peak_kind = load_peaks()
-    bytes_alg = algorithmic_bytes(ctx, ds, funcs, dims)
+    d2h = energy.nbytes + loss.nbytes
+    # ---- roofline of the dominant kernel of the step (tensor pipe: algorithmic FLOPs)
+    hbm, bf16_peak, peak_kind = load_peaks()
+    nf, h1, h2 = dims[0], dims[1], dims[2]
+    fwd_flop = 2 * (nf * h1 + h1 * h2 + h2)          # per atom, one forward
+    train_flop = 2 * fwd_flop + 2 * h1 * h2            # forward again, delta_1, weight gradients
+    flop = {"tc_forward": fwd_flop, "tc_train": train_flop}
     dom = max((f for f in fams if prof[f][1] > 0), key=lambda f: prof[f][0])
     dom_ms = prof[dom][0] / max(prof[dom][1], 1)
-    per_launch_bytes = bytes_alg.get(dom, 0) / max(1, prof[dom][1] / args.steps)
-    achieved = per_launch_bytes / (dom_ms / 1e3) / 1e9 if dom_ms > 0 else 0.0
+    atoms_per_launch = N / max(1, prof[dom][1] - (1 if dom == "tc_forward" else 0)) \
+        if dom != "tc_forward" else None
+    roof = {"kernel": dom, "launch_ms": round(dom_ms, 5)}
+    if dom in flop:
+        # tc_train runs once per mini-batch over its atoms; tc_forward once per mini-batch and
+        # once over every atom (prediction)
+        nl = prof[dom][1]
+        atoms_total = N * (2 if dom == "tc_forward" else 1)
+        tflops = atoms_total * flop[dom] / (prof[dom][0] / 1e3) / 1e12
+        roof.update({"bound": "tensor", "achieved": round(tflops, 2), "peak": bf16_peak,
+                     "unit": "TFLOP/s", "frac": round(tflops / bf16_peak, 4),
+                     "algorithmic_flop_per_launch": int(atoms_total * flop[dom] / nl),
+                     "peak_source": peak_kind})
+    kx = 2 * (((nf + 1) + 15) // 16 * 16)  # BF16 feature bytes per atom row
     traffic, traffic_src = profiled_traffic(dom, args.config, N)
+    roof["traffic"] = traffic
+    roof["traffic_source"] = traffic_src
     out = {
         "metric": METRIC, "value": round(value, 1), "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_step, 3),
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-        "data": "synthetic (seeded C2 generator: dense-liquid cells, Morse targets)",
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "bf16",
+        "data": "synthetic (seeded C3 generator: dense-liquid cells, Morse energy targets)",
         "config": {"workload": f"{args.config}: {ds.nstruct} structures, {N} atoms, "
-                               f"{dims[0]} features, net {'-'.join(map(str, dims))}, L-BFGS",
+                               f"{dims[0]} features, net {'-'.join(map(str, dims))}, mini-batches "
+                               f"of {args.batch} structures ({info['batches']} per epoch, "
+                               f"{info['tiles']} tiles of 128 atoms)",
                    "l2": "flushed between timed steps (256 MiB write)",
                    "parallelism": "replicas" if world > 1 else "single GPU"},
+        "forms": {
+            "batched_bf16": {"atoms_per_s": round(value / world, 1), "ms_per_step": round(ms_step, 3)},
+            "plain_fp32": {"atoms_per_s": round(N / (plain_ms / 1e3), 1),
+                           "ms_per_step": round(plain_ms, 3)},
+            "ratio": round(plain_ms / ms_step, 2),
+            "errors_vs_fp64": errs,
+            "featurise_ms": round(feat_ms, 2),
+            "featurise_atoms_per_s": round(N / (feat_ms / 1e3), 1),
+            "featurise_kernels_ms": {f: round(v[0] / 2, 3) for f, v in feat_prof.items() if v[1]},
+            "dataset_generation_s": round(gen_s, 1),
+        },
         "e2e": {"value": round(N / (e2e_ms / 1e3), 1), "unit": UNIT,
                 "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
         "gpu_launches": int(launches),
-        "roofline": {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1),
-                     "peak": hbm, "unit": "GB/s", "frac": round(achieved / hbm, 4),
-                     "traffic": traffic, "traffic_source": traffic_src,
-                     "algorithmic_bytes": int(per_launch_bytes), "peak_source": peak_kind},
-        "kernels_ms_per_step": {f: round(prof[f][0] / args.steps, 4) for f in fams
-                                if prof[f][1] > 0},
+        "roofline": roof,
+        "kernels_ms_per_step": {f: round(prof[f][0], 4) for f in fams if prof[f][1] > 0},
+        "kernel_launches_per_step": {f: int(prof[f][1]) for f in fams if prof[f][1] > 0},
+        "autotuned_ctas": {"forward": info["ctas_forward"], "train": info["ctas_train"]},
         "clocks": clk.summary(),
     }
     if args.serve_requests > 0 and rank == 0:
         ctx.close()
         out["serving"] = serving_leg(args)
     if not args.no_cpu_baseline and rank == 0 and world == 1:
-        out["cpu_baseline"] = cpu_baseline(args, sample_structs=args.cpu_sample, threads=1)
+        out["cpu_baseline"] = cpu_baseline(args, threads=1)
     if rank == 0:
         print(json.dumps(out))
     if dist:
         dist.barrier()
         dist.destroy_process_group()
+
+
+def profiled_traffic(kernel, config, natoms):
+    """DRAM bytes per launch of `kernel` from the committed ncu summary of this configuration
+    (bytes per atom measured on a small capture of the same workload, scaled by atoms)."""
+    path = os.path.join(ROOT, "profiles", f"{kernel}_kernel_{config}.md")
+    if not os.path.exists(path):
+        return None, None
+    with open(path) as fh:
+        for line in fh:
+            if line.startswith("dram_bytes_per_launch:"):
+                return int(float(line.split(":", 1)[1])), os.path.relpath(path, ROOT)
+    return None, None
 
 
 def serving_leg(args):
@@ -385,7 +482,9 @@ def serving_leg(args):
 
 
 def cpu_step(ds, funcs, dims, params, zprec, nthreads):
-    """The same step on the oracle (the reference's algorithm restated on the CPU)."""
+    """The same step on the oracle (the reference's algorithm restated on the CPU, with the
+    reference's loop structure): featurise, one L-BFGS iteration of the full-batch loop
+    (gradient, update, gradient at the new parameters), energies of every structure."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
 
@@ -397,30 +496,51 @@ def cpu_step(ds, funcs, dims, params, zprec, nthreads):
                      for s in range(params.shape[0])])
     dd, _ = O.train_gradients(dims, "tanh", newp, feats, ds)
     out = O.predict(dims, "tanh", newp, feats, ds.species)
-    jac = O.jacobian(dims, "tanh", newp, feats, ds.species)
-    O.forces(ds, funcs, zprec, jac, nthreads=nthreads)
-    return out
+    return np.add.reduceat(out[:, 0], ds.atom_offsets[:-1])
 
 
-def cpu_baseline(args, sample_structs, threads):
-    from fortnet_gb300 import api, synthetic
+def cpu_sample(args, max_atoms, nstruct):
+    """A bounded sample of the workload: the first `nstruct` structures of at most `max_atoms`
+    atoms, in dataset order (the oracle's featurisation costs O(atoms^2) per structure)."""
+    from fortnet_gb300 import synthetic
 
     cfg = synthetic.CONFIGS[args.config]
-    ds = synthetic.generate(cfg, nstruct=sample_structs)
-    funcs = synthetic.gfunctions(cfg)
-    dims = synthetic.network_dims(cfg)
-    params = api.Rng(cfg.seed).init_params(dims, len(cfg.atomic_numbers))
+    ds = synthetic.generate(cfg, nstruct=max(8 * nstruct, 64), workers=1)
+    n = np.diff(ds.atom_offsets)
+    idx = [int(s) for s in np.flatnonzero(n <= max_atoms)][:nstruct]
+    from fortnet_gb300.fnetdata import Dataset
+
+    off = ds.atom_offsets
+    rows = np.concatenate([np.arange(off[s], off[s + 1]) for s in idx])
+    noff = np.concatenate([[0], np.cumsum([off[s + 1] - off[s] for s in idx])]).astype(np.int64)
+    sub = Dataset(atom_offsets=noff, coords=np.ascontiguousarray(ds.coords[rows]),
+                  atnum=ds.atnum[rows], species=ds.species[rows], periodic=ds.periodic[idx],
+                  latvecs=np.ascontiguousarray(ds.latvecs[idx]), atomic_numbers=ds.atomic_numbers,
+                  weights=ds.weights[idx], atomic_weights=ds.atomic_weights[rows],
+                  global_targets=np.ascontiguousarray(ds.global_targets[idx]),
+                  atomic_targets=ds.atomic_targets[rows])
+    return cfg, sub
+
+
+def cpu_baseline(args, threads):
+    from fortnet_gb300 import synthetic
+
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
 
+    cfg, ds = cpu_sample(args, args.cpu_max_atoms, args.cpu_sample)
+    funcs = synthetic.gfunctions(cfg)
+    dims = synthetic.network_dims(cfg)
+    params = O.Ranlux(cfg.seed).init_bpnn(dims, "tanh", len(cfg.atomic_numbers))
     zprec = O.zscore_stats(O.acsf(ds, funcs, mode=1), ds)
     t0 = time.perf_counter()
     cpu_step(ds, funcs, dims, params, zprec, threads)
     dt = time.perf_counter() - t0
     return {"value": round(ds.ntot / dt, 2), "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"{ds.nstruct} C2 structures ({ds.ntot} atoms), one step; the oracle "
-                      f"restates the reference loop structure (per-(atom, G) neighbour rebuild, "
-                      f"dense dG/dR)", "seconds": round(dt, 2)}
+            "sample": f"{ds.nstruct} {args.config} structures of <= {args.cpu_max_atoms} atoms "
+                      f"({ds.ntot} atoms), one step: featurise + one L-BFGS iteration + energies; "
+                      f"the oracle restates the reference loop structure (per-(atom, G) "
+                      f"neighbour rebuild, per-atom network evaluation)", "seconds": round(dt, 2)}
 
 
 def run_reference(args):
@@ -428,18 +548,18 @@ def run_reference(args):
     if rank != 0:
         return
     threads = os.cpu_count() or 1
-    from fortnet_gb300 import api, synthetic
+    # only the oracle's library is loaded on this arm (the synthetic generator is numpy)
+    from fortnet_gb300 import synthetic
 
-    cfg = synthetic.CONFIGS[args.config]
-    ds = synthetic.generate(cfg, nstruct=args.ref_sample)
-    funcs = synthetic.gfunctions(cfg)
-    dims = synthetic.network_dims(cfg)
-    params = api.Rng(cfg.seed).init_params(dims, len(cfg.atomic_numbers))
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
 
+    cfg, ds = cpu_sample(args, args.cpu_max_atoms, args.ref_sample)
+    funcs = synthetic.gfunctions(cfg)
+    dims = synthetic.network_dims(cfg)
+    params = O.Ranlux(cfg.seed).init_bpnn(dims, "tanh", len(cfg.atomic_numbers))
     zprec = O.zscore_stats(O.acsf(ds, funcs, mode=1, nthreads=threads), ds)
-    for _ in range(args.warmup if args.warmup < 1 else 1):
+    for _ in range(min(args.warmup, 1)):
         cpu_step(ds, funcs, dims, params, zprec, threads)
     times = []
     for _ in range(args.steps):
@@ -452,12 +572,14 @@ def run_reference(args):
         "impl": "reference", "metric": METRIC, "value": round(v, 2), "unit": UNIT, "n_gpus": 0,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(dt * 1e3, 1),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-        "data": "synthetic (seeded C2 generator)",
-        "config": {"workload": f"{args.config} sample: {ds.nstruct} structures, {ds.ntot} atoms"},
+        "data": f"synthetic (seeded {args.config} generator)",
+        "config": {"workload": f"{args.config} sample: {ds.nstruct} structures of <= "
+                               f"{args.cpu_max_atoms} atoms, {ds.ntot} atoms; featurise + one "
+                               f"L-BFGS iteration + energies"},
         "cpu_baseline": {"value": round(v, 2), "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": f"{ds.nstruct} C2 structures per step (oracle restatement of "
-                                   f"the reference algorithm; the Fortran program cannot be "
-                                   f"built here)"},
+                         "sample": f"{ds.nstruct} {args.config} structures per step (oracle "
+                                   f"restatement of the reference algorithm; the Fortran program "
+                                   f"cannot be built here)"},
         "e2e": {"value": round(v, 2), "unit": UNIT, "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }))
@@ -469,10 +591,15 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--config", default="C2")
+    ap.add_argument("--config", default="C3")
     ap.add_argument("--nstruct", type=int, default=None)
+    ap.add_argument("--batch", type=int, default=BATCH, help="structures per mini-batch")
+    ap.add_argument("--lr", type=float, default=1e-6,
+                    help="learning rate of the mini-batch steepest descent")
+    ap.add_argument("--plain-steps", type=int, default=5)
     ap.add_argument("--cpu-sample", type=int, default=4)
-    ap.add_argument("--ref-sample", type=int, default=32)
+    ap.add_argument("--cpu-max-atoms", type=int, default=128)
+    ap.add_argument("--ref-sample", type=int, default=12)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--serve-requests", type=int, default=20000,
                     help="requests of the C5 serving stream (0: skip the serving leg)")

@@ -97,6 +97,16 @@ def load(build_if_missing=True):
         "fnetg_profile_reset": (C.c_int, [vp]),
         "fnetg_launch_count": (i64, [vp]),
         "fnetg_synchronize": (C.c_int, [vp]),
+        "fnetg_features_jvp": (C.c_int, [vp, vp, vp]),
+        "fnetg_set_force_targets": (C.c_int, [vp, dbl, vp]),
+        "fnetg_last_losses": (C.c_int, [vp, C.POINTER(dbl), C.POINTER(dbl)]),
+        "fnetg_batch_setup": (C.c_int, [vp, i32]),
+        "fnetg_batch_info": (C.c_int, [vp, C.POINTER(i32), C.POINTER(i64), C.POINTER(i32),
+                                       C.POINTER(i32)]),
+        "fnetg_batch_gradients": (C.c_int, [vp, i32, i32, vp, vp]),
+        "fnetg_batch_epoch": (C.c_int, [vp, i32, dbl, dbl, vp]),
+        "fnetg_batch_predict": (C.c_int, [vp, vp, vp]),
+        "fnetg_batch_sync_params": (C.c_int, [vp]),
         "fnetg_server_create": (C.c_int, [C.POINTER(vp), vp, i32, vp, i32, vp, vp, i32, vp, i32,
                                           vp]),
         "fnetg_server_destroy": (C.c_int, [vp]),
@@ -123,9 +133,12 @@ def _c(a, dtype):
 
 
 def _check_out(a, shape):
-    """A caller-owned output buffer must be C-contiguous float64 of the result's shape."""
-    if a.dtype != np.float64 or not a.flags["C_CONTIGUOUS"] or tuple(a.shape) != tuple(shape):
-        raise ValueError("output buffer must be C-contiguous float64 of shape %s" % (shape,))
+    """A caller-owned output buffer must be writeable, C-contiguous float64 of the result's
+    shape (the library writes through its raw pointer)."""
+    if (a.dtype != np.float64 or not a.flags["C_CONTIGUOUS"] or not a.flags["WRITEABLE"]
+            or tuple(a.shape) != tuple(shape)):
+        raise ValueError("output buffer must be writeable, C-contiguous float64 of shape %s"
+                         % (shape,))
 
 
 class Context:
@@ -306,7 +319,27 @@ class Context:
         self._check(self.lib.fnetg_forces_fd(self.h, float(delta), _p(out)))
         return out
 
+    def features_jvp(self, w):
+        """Derivative of every atom's standardised inputs along per-atom vectors w [Ntot, 3]:
+        [Ntot, nf] (the dense dG/dR of calculatePrime contracted with w)."""
+        wv = _c(w, np.float64).reshape(self.ntot, 3)
+        nf = C.c_int32()
+        self._check(self.lib.fnetg_get_features(self.h, None, C.byref(nf)))
+        out = np.zeros((self.ntot, nf.value))
+        self._check(self.lib.fnetg_features_jvp(self.h, _p(wv), _p(out)))
+        return out
+
     # -- training ----------------------------------------------------------------------
+    def set_force_targets(self, weight, forces=None):
+        """Force term weight / (3 Ntot) sum |F - F*|^2 in the training loss (0: off)."""
+        f = None if forces is None else _c(forces, np.float64).reshape(self.ntot, 3)
+        self._check(self.lib.fnetg_set_force_targets(self.h, float(weight), _p(f)))
+
+    def last_losses(self):
+        le, lf = C.c_double(), C.c_double()
+        self._check(self.lib.fnetg_last_losses(self.h, C.byref(le), C.byref(lf)))
+        return le.value, lf.value
+
     def set_targets(self, ds):
         gt = _c(ds.global_targets, np.float64)
         at = _c(ds.atomic_targets, np.float64)
@@ -344,6 +377,45 @@ class Context:
         self._check(self.lib.fnetg_train_iteration(self.h, LOSS[loss], strength, alpha, _p(o),
                                                    C.byref(lv), C.byref(gn), C.byref(conv)))
         return lv.value, gn.value, bool(conv.value)
+
+    # -- batched mixed-precision form (include/fnetg_batch.h) ---------------------------
+    def batch_setup(self, batch_structures=256):
+        """Mini-batches of consecutive structures, BF16 feature tiles and weight images for the
+        tensor-core kernels (after features, z-score, network and targets are set)."""
+        self._check(self.lib.fnetg_batch_setup(self.h, int(batch_structures)))
+        self._batch_off = None
+
+    def batch_info(self):
+        nb, nt, cf, ct = C.c_int32(), C.c_int64(), C.c_int32(), C.c_int32()
+        self._check(self.lib.fnetg_batch_info(self.h, C.byref(nb), C.byref(nt), C.byref(cf),
+                                              C.byref(ct)))
+        return {"batches": nb.value, "tiles": nt.value, "ctas_forward": cf.value,
+                "ctas_train": ct.value}
+
+    def batch_gradients(self, batch, loss="mse", natoms=None):
+        """Raw gradient [nSpecies, nParams] of one mini-batch and its atoms' outputs (natoms:
+        the mini-batch's atom count, to size the output; None skips the outputs)."""
+        grad = np.zeros((self.nspecies, self.nparams))
+        at = None if natoms is None else np.zeros(natoms)
+        self._check(self.lib.fnetg_batch_gradients(self.h, int(batch), LOSS[loss], _p(grad),
+                                                   _p(at)))
+        return grad, at
+
+    def batch_epoch(self, loss="mse", learning_rate=0.01, max_disp=1e4, want_loss=True):
+        lv = np.zeros(1)
+        self._check(self.lib.fnetg_batch_epoch(self.h, LOSS[loss], float(learning_rate),
+                                               float(max_disp), _p(lv) if want_loss else None))
+        return float(lv[0]) if want_loss else None
+
+    def batch_predict(self, atomic=True, out_global=None):
+        at = np.zeros(self.ntot) if atomic else None
+        gl = out_global if out_global is not None else np.zeros((self.nstruct, 1))
+        _check_out(gl, (self.nstruct, 1))
+        self._check(self.lib.fnetg_batch_predict(self.h, _p(at), _p(gl)))
+        return at, gl
+
+    def batch_sync_params(self):
+        self._check(self.lib.fnetg_batch_sync_params(self.h))
 
     # -- plumbing ----------------------------------------------------------------------
     def stream(self):

@@ -17,7 +17,8 @@ CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libfnetg.so")
 SOURCES = ["context.cu", "neighbors.cu", "acsf.cu", "mlp.cu", "forces.cu", "train.cu", "rng.cu",
-           "noalloc.cu", "fd.cu", "serve.cu"]
+           "noalloc.cu", "fd.cu", "serve.cu", "batch.cu", "jvp.cu",
+           "forceloss.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

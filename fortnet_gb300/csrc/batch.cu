@@ -1,0 +1,940 @@
+// Batched mixed-precision form of the training and prediction passes (TBpnn_nTrain's epoch,
+// lib_nn/bpnn.F90:147-390, with its gradient TBpnn_updateGradients 394-481 / sysTrain 610-704,
+// and TBpnn_predictBatch 1001-1058), on Blackwell tensor cores.
+//
+// The dataset is cut into mini-batches of consecutive structures.  Inside a mini-batch the
+// atoms of every species form 128-row tiles (zero rows pad each species' last tile).  The
+// z-scored features of every tile are stored once, as BF16, already in the operand layout of
+// tcgen05.mma (tc.cuh: core matrices, no swizzle), with a constant-1 column after the last
+// feature that carries the first layer's bias through the GEMM.  One persistent kernel per
+// stage walks a tile range with one CTA per SM:
+//   * a bulk copy (cp.async.bulk, mbarrier completion) brings a tile's 128 x K0 features into
+//     shared memory, and the species' packed BF16 weights when the species changes;
+//   * layer GEMMs run as tcgen05.mma kind::f16 (BF16 x BF16, FP32 accumulators in TMEM, 128
+//     lanes = 128 atoms); a thread owns one atom: tcgen05.ld brings its row of accumulators
+//     into registers, tanh and the output layer (a 64-wide dot) run there, and the BF16
+//     activations go back to shared memory as the next GEMM's operand;
+//   * training adds the reverse pass: delta_2 in registers, delta_1 = (W_1 delta_2) * f'
+//     as another GEMM, and the weight gradients X^T delta_1, a_1^T delta_2, a_2^T delta_3 as
+//     GEMMs over the tile's rows (MN-major operands, the same buffers), accumulated in TMEM
+//     over all tiles of the CTA and written once per CTA and species (FP32).
+// The per-CTA gradient partials are summed in FP64 in a fixed order; the update is the
+// reference's steepest descent (steepdesc.F90:126-204) on the FP64 master parameters,
+// applied per mini-batch.  A whole epoch (every mini-batch: forward, loss, reverse pass,
+// reduction, update) is captured once as a CUDA graph and replayed.  Launch shapes (CTAs per
+// stage) are chosen by timing candidates on first use and kept per network shape.
+//
+// Supported networks: two hidden tanh layers of equal padded width 16, 32 or 64 (at most 64
+// units each), one linear output, at most 239 inputs.
+#include <cuda_bf16.h>
+
+#include <algorithm>
+#include <map>
+#include <mutex>
+#include <tuple>
+
+#include "internal.cuh"
+#include "tc.cuh"
+
+namespace fnetg {
+
+__global__ void struct_sum_kernel(const double *out, const int64_t *off, int S, int nout,
+                                  double *gsum);
+int launch_loss_range(fnetg_ctx *ctx, int s0, int count, int loss);
+int launch_loss_reduce(fnetg_ctx *ctx);
+
+namespace {
+
+constexpr int kRows = 128;          // atoms per tile (MMA M, TMEM lanes)
+constexpr int kThreads = 128;       // one thread per atom of the tile
+constexpr uint32_t kTmemCols = 512;
+// TMEM column regions
+constexpr uint32_t kColFwd = 0;     // layer pre-activations / reverse-pass GEMM (<= 64 columns)
+constexpr uint32_t kColG0 = 128;    // first-layer weight gradient, two 128-input M tiles
+constexpr uint32_t kColG1 = 256;    // second-layer weight gradient
+constexpr uint32_t kColG2 = 384;    // output-layer weight gradient (16 columns)
+
+__host__ __device__ inline int rup(int x, int m) { return (x + m - 1) / m * m; }
+
+struct TcNet {
+  int nf, H1, H2;                    // real widths
+  int K0p, K1p, K2p, nmt0;           // padded GEMM K of the three layers, M tiles of X^T delta
+  uint32_t x_bytes;                  // one tile of packed features
+  uint32_t w_bytes;                  // one species' weight block
+  uint32_t off_w1f, off_w1b, off_w2; // offsets inside the weight block
+  // shared-memory plan (bytes)
+  uint32_t sm_x, sm_a1, sm_a2, sm_d2, sm_d1, sm_d3, sm_w, sm_total;
+  // reference layout of one species' parameters (network.F90:397-427)
+  int64_t nparams, woff0, woff1, woff2, woff3, boff1, boff2, boff3;
+};
+
+template <int HP> TcNet make_net(fnetg_ctx *ctx) {
+  TcNet n{};
+  n.nf = ctx->dims[0];
+  n.H1 = ctx->dims[1];
+  n.H2 = ctx->dims[2];
+  n.K0p = rup(n.nf + 1, 16);
+  n.K1p = rup(n.H1 + 1, 16);
+  n.K2p = rup(n.H2 + 1, 16);
+  n.nmt0 = (n.K0p + kRows - 1) / kRows;
+  n.x_bytes = (uint32_t)kRows * n.K0p * 2;
+  const uint32_t w0 = (uint32_t)HP * n.K0p * 2, w1f = (uint32_t)HP * n.K1p * 2,
+                 w1b = (uint32_t)HP * HP * 2, w2 = (uint32_t)(HP + 4) * 4;
+  n.off_w1f = w0;
+  n.off_w1b = w0 + w1f;
+  n.off_w2 = w0 + w1f + w1b;
+  n.w_bytes = (uint32_t)rup((int)(w0 + w1f + w1b + w2), 16);
+  uint32_t o = 0;
+  n.sm_x = o;
+  o += n.x_bytes;
+  n.sm_a1 = o;  // 128 columns: the MN-major M tile of a_1^T delta_2 reads them all
+  o += kRows * kRows * 2;
+  n.sm_a2 = o;
+  o += kRows * kRows * 2;
+  n.sm_d2 = o;
+  o += kRows * HP * 2;
+  n.sm_d1 = o;
+  o += kRows * HP * 2;
+  n.sm_d3 = o;
+  o += kRows * 16 * 2;
+  n.sm_w = o;
+  o += n.w_bytes;
+  n.sm_total = o;
+  n.nparams = ctx->nparams;
+  n.woff0 = ctx->woff[0];
+  n.woff1 = ctx->woff[1];
+  n.woff2 = ctx->woff[2];
+  n.woff3 = ctx->woff[3];
+  n.boff1 = ctx->boff[1];
+  n.boff2 = ctx->boff[2];
+  n.boff3 = ctx->boff[3];
+  return n;
+}
+
+struct TcArgs {
+  TcNet net;
+  const unsigned char *x;     // packed feature tiles
+  const unsigned char *w;     // packed weights [nsp][w_bytes]
+  const int32_t *tile_sp;     // species of every tile
+  const int32_t *tile_atoms;  // [ntiles * 128] atom of every row, -1 = padding
+  int64_t t0, t1;             // tile range of the launch
+  double *out;                // [N] atomic outputs (forward)
+  const double *delta;        // [N] scaled loss gradients of the outputs (training)
+  float *gpart;               // [gridDim.x][nsp][nparams] gradient partials (training)
+  int32_t *gflag;             // [gridDim.x][nsp] partial written
+  int nsp;
+  int *err;                   // set to 1 when a bounded wait gave up
+};
+
+__device__ __forceinline__ float tanh_fast(float x) {
+  float y;
+  asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+
+__device__ __forceinline__ uint32_t pack2(float a, float b) {
+  const __nv_bfloat162 p = __floats2bfloat162_rn(a, b);
+  return *reinterpret_cast<const uint32_t *>(&p);
+}
+__device__ __forceinline__ void st8(unsigned char *base, uint32_t off, const float *v) {
+  *reinterpret_cast<uint4 *>(base + off) =
+      make_uint4(pack2(v[0], v[1]), pack2(v[2], v[3]), pack2(v[4], v[5]), pack2(v[6], v[7]));
+}
+
+// every thread polls; the outcome is made uniform across the CTA
+__device__ __forceinline__ bool wait_all(uint64_t *mb, uint32_t parity) {
+  const bool ok = tc::mbar_wait(mb, parity);
+  return __syncthreads_and(ok ? 1 : 0) != 0;
+}
+
+// Row r's activations of one hidden layer to shared memory as BF16 (core layout, 128 rows):
+// columns [0, HP) from v, then the constant-1 column at index H and zeros up to Kp.
+template <int HP>
+__device__ __forceinline__ void store_act(unsigned char *buf, int r, float (&v)[HP], int H,
+                                          int Kp) {
+#pragma unroll
+  for (int c = 0; c < HP; c++)
+    if (c == H) v[c] = 1.f;  // unrolled compare: the array stays in registers
+#pragma unroll
+  for (int c = 0; c < HP; c += 8) st8(buf, tc::core_off(r, c, kRows), v + c);
+  if (H >= HP) {
+    float e[8] = {1.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    st8(buf, tc::core_off(r, HP, kRows), e);
+    float z[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    for (int c = HP + 8; c < Kp; c += 8) st8(buf, tc::core_off(r, c, kRows), z);
+  }
+}
+
+// MODE 0: forward (atomic outputs).  MODE 1: forward + reverse pass + weight gradients.
+template <int HP, int MODE>
+__global__ void __launch_bounds__(kThreads, 1) tc_mlp_kernel(TcArgs a) {
+  extern __shared__ __align__(1024) unsigned char sm[];
+  __shared__ uint64_t mb_load, mb_mma;
+  __shared__ uint32_t tmem_base;
+  const TcNet &n = a.net;
+  const int tid = threadIdx.x, warp = tid >> 5;
+  unsigned char *X = sm + n.sm_x, *A1 = sm + n.sm_a1, *A2 = sm + n.sm_a2, *D2 = sm + n.sm_d2,
+                *D1 = sm + n.sm_d1, *D3 = sm + n.sm_d3, *W = sm + n.sm_w;
+  const float *w2 = reinterpret_cast<const float *>(W + n.off_w2);
+  if (tid == 0) {
+    tc::mbar_init(&mb_load, 1);
+    tc::mbar_init(&mb_mma, 1);
+    tc::mbar_fence_init();
+  }
+  if (warp == 0) tc::tmem_alloc(&tmem_base, kTmemCols);
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tm = tmem_base;
+  const uint32_t lane_off = (uint32_t)(warp * 32) << 16;
+  const uint32_t sX = tc::smem_u32(X), sA1 = tc::smem_u32(A1), sA2 = tc::smem_u32(A2),
+                 sD2 = tc::smem_u32(D2), sD1 = tc::smem_u32(D1), sD3 = tc::smem_u32(D3),
+                 sW = tc::smem_u32(W);
+  // K-major operands (tc.cuh): lbo = 16 * rows, sbo = 128; MN-major: lbo = 128, sbo = 16 * rows
+  const uint32_t id_h = tc::idesc_bf16(kRows, HP, 0, 0);
+  const uint32_t id_g = tc::idesc_bf16(kRows, HP, 1, 1);
+  const uint32_t id_g2 = tc::idesc_bf16(kRows, 16, 1, 1);
+  uint32_t ph_load = 0, ph_mma = 0;
+  const int64_t nt = a.t1 - a.t0;
+  const int64_t my0 = a.t0 + nt * blockIdx.x / gridDim.x;
+  const int64_t my1 = a.t0 + nt * (blockIdx.x + 1) / gridDim.x;
+  int cur_sp = -1;
+  bool gacc = false;  // the TMEM gradient accumulators hold data of cur_sp
+  uint64_t touched = 0;
+  bool failed = false;
+
+  // gradient accumulators of cur_sp -> this CTA's partial slot (reference parameter order)
+  auto flush = [&]() {
+    float *gp = a.gpart + ((int64_t)blockIdx.x * a.nsp + cur_sp) * n.nparams;
+    for (int mt = 0; mt < n.nmt0; mt++) {
+      const int k = mt * kRows + tid;  // input feature (k == nf: the bias column)
+#pragma unroll
+      for (int c0 = 0; c0 < HP; c0 += 16) {
+        float v[16];
+        tc::tmem_ld16(tm + lane_off + kColG0 + mt * HP + c0, v);
+        tc::tmem_wait_ld();
+#pragma unroll
+        for (int q = 0; q < 16; q++) {
+          const int j = c0 + q;
+          if (j < n.H1 && k < n.nf) gp[n.woff0 + k + (int64_t)n.nf * j] = v[q];
+          else if (j < n.H1 && k == n.nf) gp[n.boff1 + j] = v[q];
+        }
+      }
+    }
+#pragma unroll
+    for (int c0 = 0; c0 < HP; c0 += 16) {
+      float v[16];
+      tc::tmem_ld16(tm + lane_off + kColG1 + c0, v);
+      tc::tmem_wait_ld();
+#pragma unroll
+      for (int q = 0; q < 16; q++) {
+        const int i = c0 + q;
+        if (i < n.H2 && tid < n.H1) gp[n.woff1 + tid + (int64_t)n.H1 * i] = v[q];
+        else if (i < n.H2 && tid == n.H1) gp[n.boff2 + i] = v[q];
+      }
+    }
+    {
+      float v[16];
+      tc::tmem_ld16(tm + lane_off + kColG2, v);
+      tc::tmem_wait_ld();
+      if (tid < n.H2) gp[n.woff2 + tid] = v[0];
+      else if (tid == n.H2) gp[n.boff3] = v[0];
+    }
+    touched |= 1ull << cur_sp;
+  };
+
+  for (int64_t t = my0; t < my1; t++) {
+    const int sp = a.tile_sp[t];
+    const bool new_sp = sp != cur_sp;
+    if (MODE == 1 && new_sp && gacc) {
+      flush();
+      gacc = false;
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    if (tid == 0) {
+      tc::mbar_expect_tx(&mb_load, n.x_bytes + (new_sp ? n.w_bytes : 0u));
+      tc::bulk_g2s(X, a.x + t * (int64_t)n.x_bytes, n.x_bytes, &mb_load);
+      if (new_sp) tc::bulk_g2s(W, a.w + (int64_t)sp * n.w_bytes, n.w_bytes, &mb_load);
+    }
+    cur_sp = sp;
+    const int row = tid;
+    const int atom = a.tile_atoms[t * kRows + row];
+    const float delta3 = (MODE == 1 && atom >= 0) ? (float)a.delta[atom] : 0.f;
+    if (!wait_all(&mb_load, ph_load)) {
+      tc::mbar_wait(&mb_load, ph_load);  // the copies in flight, once more with a limit
+      failed = true;
+      break;
+    }
+    ph_load ^= 1;
+    // ---- layer 1: Z1 = X W0 (+ bias through the constant column)
+    if (tid == 0) {
+      tc::fence_after_sync();
+      for (int ks = 0; ks < n.K0p / 16; ks++)
+        tc::mma_bf16(tm + kColFwd, tc::smem_desc(sX + ks * 2 * 16 * kRows, 16 * kRows, 128),
+                     tc::smem_desc(sW + ks * 2 * 16 * HP, 16 * HP, 128), id_h, ks > 0);
+      tc::mma_commit(&mb_mma);
+    }
+    if (!wait_all(&mb_mma, ph_mma)) { failed = true; break; }
+    ph_mma ^= 1;
+    tc::fence_after_sync();
+    float f1[HP];
+    {
+      float v[HP];
+#pragma unroll
+      for (int c0 = 0; c0 < HP; c0 += 16) {
+        float z[16];
+        tc::tmem_ld16(tm + lane_off + kColFwd + c0, z);
+        tc::tmem_wait_ld();
+#pragma unroll
+        for (int q = 0; q < 16; q++) {
+          const float th = tanh_fast(z[q]);
+          v[c0 + q] = th;
+          f1[c0 + q] = 1.f - th * th;
+        }
+      }
+      store_act<HP>(A1, row, v, n.H1, n.K1p);
+    }
+    tc::fence_async_smem();
+    tc::fence_before_sync();
+    __syncthreads();
+    // ---- layer 2: Z2 = A1 W1 (+ bias)
+    if (tid == 0) {
+      tc::fence_after_sync();
+      for (int ks = 0; ks < n.K1p / 16; ks++)
+        tc::mma_bf16(tm + kColFwd, tc::smem_desc(sA1 + ks * 2 * 16 * kRows, 16 * kRows, 128),
+                     tc::smem_desc(sW + n.off_w1f + ks * 2 * 16 * HP, 16 * HP, 128), id_h,
+                     ks > 0);
+      tc::mma_commit(&mb_mma);
+    }
+    if (!wait_all(&mb_mma, ph_mma)) { failed = true; break; }
+    ph_mma ^= 1;
+    tc::fence_after_sync();
+    {
+      float y = w2[HP];  // output bias
+      float av[HP], dv[HP];
+#pragma unroll
+      for (int c0 = 0; c0 < HP; c0 += 16) {
+        float z[16];
+        tc::tmem_ld16(tm + lane_off + kColFwd + c0, z);
+        tc::tmem_wait_ld();
+#pragma unroll
+        for (int q = 0; q < 16; q++) {
+          const float th = tanh_fast(z[q]);
+          const float wq = w2[c0 + q];
+          y = fmaf(th, wq, y);
+          av[c0 + q] = th;
+          dv[c0 + q] = delta3 * wq * (1.f - th * th);
+        }
+      }
+      if (MODE == 0) {
+        if (atom >= 0) a.out[atom] = (double)y;
+      } else {
+        store_act<HP>(A2, row, av, n.H2, n.K2p);
+#pragma unroll
+        for (int c = 0; c < HP; c += 8) st8(D2, tc::core_off(row, c, kRows), dv + c);
+        float d3[8] = {delta3, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+        float z8[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+        st8(D3, tc::core_off(row, 0, kRows), d3);
+        st8(D3, tc::core_off(row, 8, kRows), z8);
+      }
+    }
+    if (MODE == 0) continue;
+    tc::fence_async_smem();
+    tc::fence_before_sync();
+    __syncthreads();
+    // ---- reverse pass: P = delta_2 W1^T; G1 += A1^T delta_2; G2 += A2^T delta_3
+    if (tid == 0) {
+      tc::fence_after_sync();
+      for (int ks = 0; ks < HP / 16; ks++)
+        tc::mma_bf16(tm + kColFwd, tc::smem_desc(sD2 + ks * 2 * 16 * kRows, 16 * kRows, 128),
+                     tc::smem_desc(sW + n.off_w1b + ks * 2 * 16 * HP, 16 * HP, 128), id_h,
+                     ks > 0);
+      for (int ks = 0; ks < kRows / 16; ks++) {
+        tc::mma_bf16(tm + kColG1, tc::smem_desc(sA1 + ks * 256, 128, 16 * kRows),
+                     tc::smem_desc(sD2 + ks * 256, 128, 16 * kRows), id_g, gacc || ks > 0);
+        tc::mma_bf16(tm + kColG2, tc::smem_desc(sA2 + ks * 256, 128, 16 * kRows),
+                     tc::smem_desc(sD3 + ks * 256, 128, 16 * kRows), id_g2, gacc || ks > 0);
+      }
+      tc::mma_commit(&mb_mma);
+    }
+    if (!wait_all(&mb_mma, ph_mma)) { failed = true; break; }
+    ph_mma ^= 1;
+    tc::fence_after_sync();
+    {
+      float dv[HP];
+#pragma unroll
+      for (int c0 = 0; c0 < HP; c0 += 16) {
+        float z[16];
+        tc::tmem_ld16(tm + lane_off + kColFwd + c0, z);
+        tc::tmem_wait_ld();
+#pragma unroll
+        for (int q = 0; q < 16; q++) dv[c0 + q] = z[q] * f1[c0 + q];
+      }
+#pragma unroll
+      for (int c = 0; c < HP; c += 8) st8(D1, tc::core_off(row, c, kRows), dv + c);
+    }
+    tc::fence_async_smem();
+    tc::fence_before_sync();
+    __syncthreads();
+    // ---- G0 += X^T delta_1 (input features in M tiles of 128)
+    if (tid == 0) {
+      tc::fence_after_sync();
+      for (int mt = 0; mt < n.nmt0; mt++)
+        for (int ks = 0; ks < kRows / 16; ks++)
+          tc::mma_bf16(tm + kColG0 + mt * HP,
+                       tc::smem_desc(sX + mt * 16 * 16 * kRows + ks * 256, 128, 16 * kRows),
+                       tc::smem_desc(sD1 + ks * 256, 128, 16 * kRows), id_g, gacc || ks > 0);
+      tc::mma_commit(&mb_mma);
+    }
+    if (!wait_all(&mb_mma, ph_mma)) { failed = true; break; }
+    ph_mma ^= 1;
+    tc::fence_after_sync();
+    gacc = true;
+  }
+  if (MODE == 1 && !failed) {
+    if (gacc) flush();
+    if (tid < a.nsp) a.gflag[(int64_t)blockIdx.x * a.nsp + tid] = (int)((touched >> tid) & 1);
+  }
+  if (failed && tid == 0) atomicExch(a.err, 1);
+  tc::fence_before_sync();
+  __syncthreads();
+  if (warp == 0) tc::tmem_dealloc(tm, kTmemCols);
+}
+
+// ---- packing kernels ---------------------------------------------------------------------
+// Features of every tile row (z-scored, bucketed rows of the context) -> BF16 core layout,
+// constant 1 in column nf for real atoms; padding rows all zero.
+template <typename T>
+__global__ void pack_x_kernel(const T *feat, const int32_t *bpos, int nf, int K0p,
+                              const int32_t *tile_atoms, int64_t ntiles, uint32_t x_bytes,
+                              unsigned char *x) {
+  const int groups = K0p / 8;
+  const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= ntiles * kRows * groups) return;
+  const int g = (int)(q % groups);
+  const int64_t tr = q / groups;
+  const int64_t t = tr / kRows;
+  const int r = (int)(tr % kRows);
+  const int atom = tile_atoms[tr];
+  float v[8];
+#pragma unroll
+  for (int c = 0; c < 8; c++) {
+    const int k = g * 8 + c;
+    float x0 = 0.f;
+    if (atom >= 0) {
+      if (k < nf) x0 = (float)feat[(int64_t)bpos[atom] * nf + k];
+      else if (k == nf) x0 = 1.f;
+    }
+    v[c] = x0;
+  }
+  st8(x + t * (int64_t)x_bytes, tc::core_off(r, g * 8, kRows), v);
+}
+
+// FP64 master parameters (reference order) -> per-species BF16 weight images + FP32 output
+// layer: W0 image rows = first hidden units, columns = inputs (+ bias column nf); W1 forward
+// image rows = second hidden units, columns = first (+ bias column H1); W1 reverse image rows =
+// first hidden units, columns = second; then w2[HP], b3 as floats.
+template <int HP>
+__global__ void pack_w_kernel(const double *p64, TcNet n, unsigned char *w) {
+  const int s = blockIdx.y;
+  const double *p = p64 + (int64_t)s * n.nparams;
+  unsigned char *blk = w + (int64_t)s * n.w_bytes;
+  const int e0 = HP * n.K0p, e1 = HP * n.K1p, e2 = HP * HP;
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < e0 + e1 + e2 + HP + 1;
+       q += gridDim.x * blockDim.x) {
+    if (q < e0) {
+      const int u = q / n.K0p, k = q % n.K0p;
+      double v = 0.0;
+      if (u < n.H1) v = k < n.nf ? p[n.woff0 + k + (int64_t)n.nf * u] : (k == n.nf ? p[n.boff1 + u] : 0.0);
+      *reinterpret_cast<__nv_bfloat16 *>(blk + tc::core_off(u, k, HP)) = __float2bfloat16_rn((float)v);
+    } else if (q < e0 + e1) {
+      const int r = q - e0, i = r / n.K1p, j = r % n.K1p;
+      double v = 0.0;
+      if (i < n.H2) v = j < n.H1 ? p[n.woff1 + j + (int64_t)n.H1 * i] : (j == n.H1 ? p[n.boff2 + i] : 0.0);
+      *reinterpret_cast<__nv_bfloat16 *>(blk + n.off_w1f + tc::core_off(i, j, HP)) =
+          __float2bfloat16_rn((float)v);
+    } else if (q < e0 + e1 + e2) {
+      const int r = q - e0 - e1, j = r / HP, i = r % HP;
+      const double v = (j < n.H1 && i < n.H2) ? p[n.woff1 + j + (int64_t)n.H1 * i] : 0.0;
+      *reinterpret_cast<__nv_bfloat16 *>(blk + n.off_w1b + tc::core_off(j, i, HP)) =
+          __float2bfloat16_rn((float)v);
+    } else {
+      const int i = q - e0 - e1 - e2;  // i < HP: output weights, i == HP: output bias
+      float *tail = reinterpret_cast<float *>(blk + n.off_w2);
+      tail[i] = i < HP ? (i < n.H2 ? (float)p[n.woff2 + i] : 0.f) : (float)p[n.boff3];
+    }
+  }
+}
+
+// FP64 sums of the per-CTA partials in CTA order (deterministic); parameters no kernel
+// produces (the unused output-layer ww(d_L, 1) and the input-layer biases) are zero.
+__global__ void tc_reduce_kernel(const float *gpart, const int32_t *gflag, int nblk, int nsp,
+                                 TcNet n, double *grad64) {
+  const int s = blockIdx.y;
+  const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= n.nparams) return;
+  const bool produced = q < n.woff3 || q >= n.boff1;
+  double acc = 0.0;
+  if (produced)
+    for (int b = 0; b < nblk; b++)
+      if (gflag[b * nsp + s]) acc += (double)gpart[((int64_t)b * nsp + s) * n.nparams + q];
+  grad64[(int64_t)s * n.nparams + q] = acc;
+}
+
+// Steepest descent of one sub-network with the mini-batch gradient (steepdesc.F90:126-204 after
+// TBpnn_update's normalisation bpnn.F90:751-766, no regularisation): d = -lr g / sum(w), scaled
+// to the maximal displacement when its largest component exceeds it.
+__global__ void tc_sd_kernel(double *params, const double *grad, int64_t np, double inv_sumw,
+                             double lr, double maxdisp) {
+  __shared__ double sh[512];
+  const int s = blockIdx.x;
+  double *x = params + (int64_t)s * np;
+  const double *g = grad + (int64_t)s * np;
+  double mx = 0.0;
+  for (int64_t q = threadIdx.x; q < np; q += blockDim.x)
+    mx = fmax(mx, fabs(-1.0 * lr * (g[q] * inv_sumw)));
+  sh[threadIdx.x] = mx;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if ((int)threadIdx.x < o) sh[threadIdx.x] = fmax(sh[threadIdx.x], sh[threadIdx.x + o]);
+    __syncthreads();
+  }
+  mx = sh[0];
+  for (int64_t q = threadIdx.x; q < np; q += blockDim.x) {
+    const double d = -1.0 * lr * (g[q] * inv_sumw);
+    x[q] = mx <= maxdisp ? x[q] + d : x[q] + (maxdisp / mx) * d;
+  }
+}
+
+// ---- autotuned launch shapes, kept per network shape for the process ----------------------
+std::mutex g_tune_mu;
+std::map<std::tuple<int, int, int, int, int>, int> g_tune;  // (mode, nf, H1, H2, tiles/batch) -> CTAs
+
+}  // namespace
+
+struct BatchState {
+  int B = 0, nbatch = 0, HP = 0;
+  int64_t ntiles = 0;
+  TcNet net{};
+  std::vector<int64_t> tile0;  // [nbatch + 1] first tile of every mini-batch
+  std::vector<int32_t> s0;     // [nbatch + 1] first structure of every mini-batch
+  std::vector<double> sumw;    // [nbatch] datapoint weights of every mini-batch
+  DBuf d_tile_sp, d_tile_atoms, d_x, d_w, d_gpart, d_gflag, d_err;
+  int grid_fwd = 0, grid_train = 0;
+  // what the tile plan was built for
+  int plan_S = -1, plan_nsp = 0;
+  int64_t plan_N = -1;
+  std::vector<int32_t> plan_dims, plan_species;
+  // captured epoch
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  double g_lr = -1.0, g_maxdisp = -1.0;
+  int g_loss = -1;
+  int64_t g_launches = 0;
+  void drop_graph() {
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+    exec = nullptr;
+    graph = nullptr;
+  }
+  ~BatchState() { drop_graph(); }
+};
+
+void batch_free(BatchState *b) { delete b; }
+
+namespace {
+
+template <int HP> void *tc_kernel(int mode) {
+  return mode == 0 ? (void *)tc_mlp_kernel<HP, 0> : (void *)tc_mlp_kernel<HP, 1>;
+}
+void *tc_kernel_hp(int hp, int mode) {
+  switch (hp) {
+    case 16: return tc_kernel<16>(mode);
+    case 32: return tc_kernel<32>(mode);
+    default: return tc_kernel<64>(mode);
+  }
+}
+
+int launch_tc(fnetg_ctx *ctx, int mode, int64_t t0, int64_t t1, int grid) {
+  BatchState &b = *ctx->batch;
+  if (t1 <= t0) return FNETG_OK;
+  TcArgs a{};
+  a.net = b.net;
+  a.x = b.d_x.as<unsigned char>();
+  a.w = b.d_w.as<unsigned char>();
+  a.tile_sp = b.d_tile_sp.as<int32_t>();
+  a.tile_atoms = b.d_tile_atoms.as<int32_t>();
+  a.t0 = t0;
+  a.t1 = t1;
+  a.out = ctx->d_out.as<double>();
+  a.delta = ctx->d_lossgrad.as<double>();
+  a.gpart = b.d_gpart.as<float>();
+  a.gflag = b.d_gflag.as<int32_t>();
+  a.nsp = ctx->nsp;
+  a.err = b.d_err.as<int>();
+  grid = (int)std::max<int64_t>(1, std::min<int64_t>(grid, t1 - t0));
+  void *k = tc_kernel_hp(b.HP, mode);
+  FNETG_CUDA(raise_smem_limit(k, b.net.sm_total));
+  void *args[] = {&a};
+  LaunchScope ls(ctx, mode == 0 ? "tc_forward" : "tc_train");
+  FNETG_CUDA(cudaLaunchKernel(k, dim3(grid), dim3(kThreads), args, b.net.sm_total, ctx->stream));
+  return FNETG_OK;
+}
+
+int launch_pack_w(fnetg_ctx *ctx) {
+  BatchState &b = *ctx->batch;
+  dim3 grid(64, ctx->nsp);
+  LaunchScope ls(ctx, "tc_pack");
+  switch (b.HP) {
+    case 16: pack_w_kernel<16><<<grid, 256, 0, ctx->stream>>>(ctx->d_params64.as<double>(), b.net, b.d_w.as<unsigned char>()); break;
+    case 32: pack_w_kernel<32><<<grid, 256, 0, ctx->stream>>>(ctx->d_params64.as<double>(), b.net, b.d_w.as<unsigned char>()); break;
+    default: pack_w_kernel<64><<<grid, 256, 0, ctx->stream>>>(ctx->d_params64.as<double>(), b.net, b.d_w.as<unsigned char>()); break;
+  }
+  FNETG_CUDA(cudaGetLastError());
+  return FNETG_OK;
+}
+
+// one mini-batch: forward, loss (the reference's loss gradients per atom), reverse pass with
+// weight gradients, FP64 reduction; with update: steepest descent and the new BF16 weights
+int batch_step(fnetg_ctx *ctx, int k, int loss, bool update, double lr, double maxdisp) {
+  BatchState &b = *ctx->batch;
+  int rc = launch_tc(ctx, 0, b.tile0[k], b.tile0[k + 1], b.grid_fwd);
+  if (rc) return rc;
+  rc = launch_loss_range(ctx, b.s0[k], b.s0[k + 1] - b.s0[k], loss);
+  if (rc) return rc;
+  rc = launch_tc(ctx, 1, b.tile0[k], b.tile0[k + 1], b.grid_train);
+  if (rc) return rc;
+  const int nblk = (int)std::max<int64_t>(1, std::min<int64_t>(b.grid_train, b.tile0[k + 1] - b.tile0[k]));
+  {
+    dim3 grid(ceil_div(b.net.nparams, 256), ctx->nsp);
+    LaunchScope ls(ctx, "tc_reduce");
+    tc_reduce_kernel<<<grid, 256, 0, ctx->stream>>>(b.d_gpart.as<float>(), b.d_gflag.as<int32_t>(),
+                                                     nblk, ctx->nsp, b.net,
+                                                     ctx->d_grad64.as<double>());
+    FNETG_CUDA(cudaGetLastError());
+  }
+  if (!update) return FNETG_OK;
+  {
+    LaunchScope ls(ctx, "tc_update");
+    tc_sd_kernel<<<ctx->nsp, 512, 0, ctx->stream>>>(ctx->d_params64.as<double>(),
+                                                    ctx->d_grad64.as<double>(), b.net.nparams,
+                                                    1.0 / b.sumw[k], lr, maxdisp);
+    FNETG_CUDA(cudaGetLastError());
+  }
+  return launch_pack_w(ctx);
+}
+
+int check_err(fnetg_ctx *ctx) {
+  int e = 0;
+  FNETG_CUDA(cudaMemcpyAsync(&e, ctx->batch->d_err.p, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  FNETG_CUDA(cudaStreamSynchronize(ctx->stream));
+  FNETG_CHECK(e == 0, FNETG_E_TIMEOUT, "tensor-core kernel: a bounded wait gave up");
+  return FNETG_OK;
+}
+
+// Time the candidate CTA counts of one stage on mini-batch 0 and keep the fastest.
+int autotune(fnetg_ctx *ctx, int mode, int loss) {
+  BatchState &b = *ctx->batch;
+  const int64_t tiles = b.tile0[1] - b.tile0[0];
+  const auto key = std::make_tuple(mode, b.net.nf, b.net.H1, b.net.H2, (int)tiles);
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = g_tune.find(key);
+    if (it != g_tune.end()) {
+      (mode == 0 ? b.grid_fwd : b.grid_train) = it->second;
+      return FNETG_OK;
+    }
+  }
+  const int sms = num_sms();
+  std::vector<int> cand = {sms, sms / 2, (int)((tiles + 3) / 4), (int)((tiles + 5) / 6),
+                           (int)((tiles + 7) / 8)};
+  int best = sms;
+  float best_ms = 1e30f;
+  if (mode == 1) {  // the reverse pass reads the forward's loss gradients
+    int rc = launch_tc(ctx, 0, b.tile0[0], b.tile0[1], sms);
+    if (rc) return rc;
+    rc = launch_loss_range(ctx, b.s0[0], b.s0[1] - b.s0[0], loss);
+    if (rc) return rc;
+  }
+  for (int g : cand) {
+    if (g < 1 || g > sms) continue;
+    float ms = 0.f;
+    for (int rep = 0; rep < 3; rep++) {
+      FNETG_CUDA(cudaEventRecord(ctx->ev0, ctx->stream));
+      int rc = launch_tc(ctx, mode, b.tile0[0], b.tile0[1], g);
+      if (rc) return rc;
+      FNETG_CUDA(cudaEventRecord(ctx->ev1, ctx->stream));
+      FNETG_CUDA(cudaEventSynchronize(ctx->ev1));
+      float t = 0.f;
+      FNETG_CUDA(cudaEventElapsedTime(&t, ctx->ev0, ctx->ev1));
+      ms = rep == 0 ? t : std::min(ms, t);
+    }
+    if (ms < best_ms) {
+      best_ms = ms;
+      best = g;
+    }
+  }
+  int rc = check_err(ctx);
+  if (rc) return rc;
+  (mode == 0 ? b.grid_fwd : b.grid_train) = best;
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  g_tune[key] = best;
+  return FNETG_OK;
+}
+
+int ensure_tuned(fnetg_ctx *ctx, int loss) {
+  BatchState &b = *ctx->batch;
+  if (b.grid_fwd <= 0) {
+    int rc = autotune(ctx, 0, loss);
+    if (rc) return rc;
+  }
+  if (b.grid_train <= 0) {
+    int rc = autotune(ctx, 1, loss);
+    if (rc) return rc;
+  }
+  return FNETG_OK;
+}
+
+template <typename T>
+int pack_features(fnetg_ctx *ctx) {
+  BatchState &b = *ctx->batch;
+  const int64_t total = b.ntiles * kRows * (b.net.K0p / 8);
+  LaunchScope ls(ctx, "tc_pack");
+  pack_x_kernel<T><<<ceil_div(total, 256), 256, 0, ctx->stream>>>(
+      ctx->d_feat.as<T>(), ctx->d_bpos.as<int32_t>(), b.net.nf, b.net.K0p,
+      b.d_tile_atoms.as<int32_t>(), b.ntiles, b.net.x_bytes, b.d_x.as<unsigned char>());
+  FNETG_CUDA(cudaGetLastError());
+  return FNETG_OK;
+}
+
+}  // namespace
+}  // namespace fnetg
+
+using namespace fnetg;
+
+extern "C" {
+
+int fnetg_batch_setup(fnetg_ctx *ctx, int32_t batch_structures) {
+  if (!ctx) return FNETG_E_INVALID;
+  FNETG_CHECK(batch_structures >= 1, FNETG_E_INVALID, "batch_setup: batch size must be >= 1");
+  FNETG_CHECK(ctx->net_set, FNETG_E_INVALID, "batch_setup: no network");
+  FNETG_CHECK(ctx->feats_valid, FNETG_E_INVALID, "batch_setup: no features computed");
+  FNETG_CHECK(ctx->targets_set, FNETG_E_INVALID, "batch_setup: no targets");
+  FNETG_CHECK(ctx->nf == ctx->dims[0], FNETG_E_SHAPE, "batch_setup: network input width");
+  FNETG_CHECK(ctx->nlayer == 4 && ctx->dims[3] == 1 && ctx->act == FNETG_ACT_TANH &&
+                  ctx->ngt == 1 && ctx->nat == 0,
+              FNETG_E_UNSUPPORTED,
+              "batch_setup: the tensor-core form takes two tanh hidden layers, one output and "
+              "one global target");
+  const int H = std::max(ctx->dims[1], ctx->dims[2]);
+  FNETG_CHECK(H <= 64 && ctx->dims[0] + 1 <= 2 * kRows - 16, FNETG_E_UNSUPPORTED,
+              "batch_setup: hidden layers of at most 64 units and at most 239 inputs");
+  FNETG_CHECK(ctx->nsp <= 64, FNETG_E_UNSUPPORTED, "batch_setup: at most 64 sub-networks");
+  if (!ctx->batch) ctx->batch = new BatchState();
+  BatchState &b = *ctx->batch;
+  if (b.B == batch_structures && b.plan_S == ctx->S && b.plan_N == ctx->N &&
+      b.plan_dims == ctx->dims && b.plan_nsp == ctx->nsp && b.plan_species == ctx->h_species) {
+    // same structures, species, network shape and batch size: the tile plan, the graph and the
+    // tuned launch shapes stay; only the features and weights are packed again
+    int rc = ctx->prec == FNETG_FP64 ? pack_features<double>(ctx) : pack_features<float>(ctx);
+    if (rc) return rc;
+    return launch_pack_w(ctx);
+  }
+  b.drop_graph();
+  b.plan_S = -1;
+  b.HP = H <= 16 ? 16 : (H <= 32 ? 32 : 64);
+  b.net = b.HP == 16 ? make_net<16>(ctx) : (b.HP == 32 ? make_net<32>(ctx) : make_net<64>(ctx));
+  FNETG_CHECK(b.net.sm_total <= 227 * 1024, FNETG_E_UNSUPPORTED,
+              "batch_setup: tile buffers exceed shared memory");
+  b.B = batch_structures;
+  const int S = ctx->S;
+  b.nbatch = (S + b.B - 1) / b.B;
+  b.tile0.assign(1, 0);
+  b.s0.assign(1, 0);
+  b.sumw.clear();
+  std::vector<int32_t> tsp, tatoms;
+  std::vector<int32_t> w(S, 1);
+  if (S > 0) FNETG_CUDA(copy_sync(ctx, w.data(), ctx->d_w.p, sizeof(int32_t) * S, cudaMemcpyDeviceToHost));
+  std::vector<std::vector<int32_t>> rows(ctx->nsp);
+  for (int k = 0; k < b.nbatch; k++) {
+    const int sa = k * b.B, se = std::min(S, sa + b.B);
+    double sw = 0.0;
+    for (int s = sa; s < se; s++) sw += (double)w[s];
+    for (auto &r : rows) r.clear();
+    for (int64_t at = ctx->h_off[sa]; at < ctx->h_off[se]; at++)
+      rows[ctx->h_species[at]].push_back((int32_t)at);
+    for (int sp = 0; sp < ctx->nsp; sp++)
+      for (size_t r0 = 0; r0 < rows[sp].size(); r0 += kRows) {
+        tsp.push_back(sp);
+        for (int r = 0; r < kRows; r++)
+          tatoms.push_back(r0 + r < rows[sp].size() ? rows[sp][r0 + r] : -1);
+      }
+    b.tile0.push_back((int64_t)tsp.size());
+    b.s0.push_back(se);
+    b.sumw.push_back(sw);
+    FNETG_CHECK(sw > 0.0, FNETG_E_INVALID, "batch_setup: a mini-batch has zero total weight");
+  }
+  b.ntiles = (int64_t)tsp.size();
+  FNETG_CHECK(b.ntiles > 0, FNETG_E_INVALID, "batch_setup: no atoms");
+  FNETG_CUDA(b.d_tile_sp.ensure(sizeof(int32_t) * b.ntiles));
+  FNETG_CUDA(b.d_tile_atoms.ensure(sizeof(int32_t) * b.ntiles * kRows));
+  FNETG_CUDA(copy_sync(ctx, b.d_tile_sp.p, tsp.data(), sizeof(int32_t) * b.ntiles, cudaMemcpyHostToDevice));
+  FNETG_CUDA(copy_sync(ctx, b.d_tile_atoms.p, tatoms.data(), sizeof(int32_t) * tatoms.size(),
+                        cudaMemcpyHostToDevice));
+  FNETG_CUDA(b.d_x.ensure((size_t)b.ntiles * b.net.x_bytes));
+  FNETG_CUDA(b.d_w.ensure((size_t)ctx->nsp * b.net.w_bytes));
+  const int maxgrid = num_sms();
+  FNETG_CUDA(b.d_gpart.ensure(sizeof(float) * (size_t)maxgrid * ctx->nsp * b.net.nparams));
+  FNETG_CUDA(b.d_gflag.ensure(sizeof(int32_t) * (size_t)maxgrid * ctx->nsp));
+  FNETG_CUDA(b.d_err.ensure(sizeof(int)));
+  FNETG_CUDA(cudaMemsetAsync(b.d_err.p, 0, sizeof(int), ctx->stream));
+  FNETG_CUDA(ctx->d_out.ensure(sizeof(double) * std::max<int64_t>(ctx->N, 1)));
+  FNETG_CUDA(ctx->d_lossgrad.ensure(sizeof(double) * std::max<int64_t>(ctx->N, 1)));
+  FNETG_CUDA(ctx->d_losspart.ensure(sizeof(double) * 2 * std::max(S, 1)));
+  FNETG_CUDA(ctx->d_scalars.ensure(sizeof(double) * 16));
+  FNETG_CUDA(ctx->d_grad64.ensure(sizeof(double) * ctx->nsp * ctx->nparams));
+  int rc = ctx->prec == FNETG_FP64 ? pack_features<double>(ctx) : pack_features<float>(ctx);
+  if (rc) return rc;
+  rc = launch_pack_w(ctx);
+  if (rc) return rc;
+  b.grid_fwd = b.grid_train = 0;
+  b.plan_S = ctx->S;
+  b.plan_N = ctx->N;
+  b.plan_dims = ctx->dims;
+  b.plan_nsp = ctx->nsp;
+  b.plan_species = ctx->h_species;
+  FNETG_CUDA(cudaStreamSynchronize(ctx->stream));
+  return FNETG_OK;
+}
+
+int fnetg_batch_info(fnetg_ctx *ctx, int32_t *nbatch, int64_t *ntiles, int32_t *ctas_forward,
+                     int32_t *ctas_train) {
+  if (!ctx || !ctx->batch) return FNETG_E_INVALID;
+  if (nbatch) *nbatch = ctx->batch->nbatch;
+  if (ntiles) *ntiles = ctx->batch->ntiles;
+  if (ctas_forward) *ctas_forward = ctx->batch->grid_fwd;
+  if (ctas_train) *ctas_train = ctx->batch->grid_train;
+  return FNETG_OK;
+}
+
+int fnetg_batch_gradients(fnetg_ctx *ctx, int32_t batch, int32_t loss, double *grad,
+                          double *atomic_out) {
+  if (!ctx || !ctx->batch) return FNETG_E_INVALID;
+  BatchState &b = *ctx->batch;
+  FNETG_CHECK(batch >= 0 && batch < b.nbatch, FNETG_E_INVALID, "batch_gradients: batch index");
+  FNETG_CHECK(loss >= 0 && loss <= 3, FNETG_E_INVALID, "loss code");
+  int rc = ensure_tuned(ctx, loss);
+  if (rc) return rc;
+  rc = batch_step(ctx, batch, loss, false, 0.0, 0.0);
+  if (rc) return rc;
+  rc = check_err(ctx);
+  if (rc) return rc;
+  if (grad)
+    FNETG_CUDA(copy_sync(ctx, grad, ctx->d_grad64.p, sizeof(double) * ctx->nsp * ctx->nparams,
+                          cudaMemcpyDeviceToHost));
+  if (atomic_out) {
+    const int64_t a0 = ctx->h_off[b.s0[batch]], a1 = ctx->h_off[b.s0[batch + 1]];
+    if (a1 > a0)
+      FNETG_CUDA(copy_sync(ctx, atomic_out, ctx->d_out.as<double>() + a0,
+                            sizeof(double) * (a1 - a0), cudaMemcpyDeviceToHost));
+  }
+  return FNETG_OK;
+}
+
+int fnetg_batch_epoch(fnetg_ctx *ctx, int32_t loss, double learning_rate, double max_disp,
+                      double *loss_out) {
+  if (!ctx || !ctx->batch) return FNETG_E_INVALID;
+  BatchState &b = *ctx->batch;
+  FNETG_CHECK(loss >= 0 && loss <= 3, FNETG_E_INVALID, "loss code");
+  FNETG_CHECK(learning_rate > 0.0 && max_disp > 0.0, FNETG_E_INVALID,
+              "batch_epoch: learning rate and maximal displacement must be > 0");
+  int rc = ensure_tuned(ctx, loss);
+  if (rc) return rc;
+  if (ctx->prof) {
+    // per-kernel timing requested: the same launches eagerly, each with its CUDA events
+    for (int k = 0; k < b.nbatch; k++) {
+      rc = batch_step(ctx, k, loss, true, learning_rate, max_disp);
+      if (rc) return rc;
+    }
+    rc = launch_loss_reduce(ctx);
+    if (rc) return rc;
+    if (loss_out) {
+      FNETG_CUDA(cudaMemcpyAsync(loss_out, ctx->d_scalars.p, sizeof(double),
+                                 cudaMemcpyDeviceToHost, ctx->stream));
+      return check_err(ctx);
+    }
+    return FNETG_OK;
+  }
+  if (!b.exec || b.g_lr != learning_rate || b.g_maxdisp != max_disp || b.g_loss != loss) {
+    b.drop_graph();
+    // capture every mini-batch step and the epoch loss as one graph (no timing events inside)
+    const bool prof = ctx->prof;
+    ctx->prof = false;
+    const int64_t l0 = ctx->launches;
+    FNETG_CUDA(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+    int crc = FNETG_OK;
+    for (int k = 0; k < b.nbatch && crc == FNETG_OK; k++)
+      crc = batch_step(ctx, k, loss, true, learning_rate, max_disp);
+    if (crc == FNETG_OK) crc = launch_loss_reduce(ctx);
+    cudaGraph_t g = nullptr;
+    const cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
+    ctx->prof = prof;
+    b.g_launches = ctx->launches - l0;
+    ctx->launches = l0;
+    if (crc) {
+      if (g) cudaGraphDestroy(g);
+      return crc;
+    }
+    FNETG_CUDA(e);
+    b.graph = g;
+    FNETG_CUDA(cudaGraphInstantiate(&b.exec, b.graph, 0));
+    b.g_lr = learning_rate;
+    b.g_maxdisp = max_disp;
+    b.g_loss = loss;
+  }
+  {
+    LaunchScope ls(ctx, "tc_epoch");
+    FNETG_CUDA(cudaGraphLaunch(b.exec, ctx->stream));
+  }
+  ctx->launches += b.g_launches - 1;
+  if (loss_out) {
+    FNETG_CUDA(cudaMemcpyAsync(loss_out, ctx->d_scalars.p, sizeof(double), cudaMemcpyDeviceToHost,
+                               ctx->stream));
+    return check_err(ctx);
+  }
+  return FNETG_OK;
+}
+
+int fnetg_batch_predict(fnetg_ctx *ctx, double *atomic_out, double *global_out) {
+  if (!ctx || !ctx->batch) return FNETG_E_INVALID;
+  BatchState &b = *ctx->batch;
+  int rc = ensure_tuned(ctx, 0);
+  if (rc) return rc;
+  rc = launch_tc(ctx, 0, 0, b.ntiles, num_sms());
+  if (rc) return rc;
+  if (global_out && ctx->S > 0) {
+    FNETG_CUDA(ctx->d_gsum.ensure(sizeof(double) * ctx->S));
+    LaunchScope ls(ctx, "struct_sum");
+    struct_sum_kernel<<<ceil_div(ctx->S, 128), 128, 0, ctx->stream>>>(
+        ctx->d_out.as<double>(), ctx->d_off.as<int64_t>(), ctx->S, 1, ctx->d_gsum.as<double>());
+    FNETG_CUDA(cudaGetLastError());
+  }
+  if (atomic_out && ctx->N > 0)
+    FNETG_CUDA(cudaMemcpyAsync(atomic_out, ctx->d_out.p, sizeof(double) * ctx->N,
+                               cudaMemcpyDeviceToHost, ctx->stream));
+  if (global_out && ctx->S > 0)
+    FNETG_CUDA(cudaMemcpyAsync(global_out, ctx->d_gsum.p, sizeof(double) * ctx->S,
+                               cudaMemcpyDeviceToHost, ctx->stream));
+  if (atomic_out || global_out) return check_err(ctx);
+  return FNETG_OK;
+}
+
+int fnetg_batch_sync_params(fnetg_ctx *ctx) {
+  if (!ctx || !ctx->batch) return FNETG_E_INVALID;
+  int rc = launch_pack_w(ctx);
+  if (rc) return rc;
+  return run_params_to_compute(ctx);
+}
+
+}  // extern "C"

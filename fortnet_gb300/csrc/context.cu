@@ -190,6 +190,7 @@ int fnetg_destroy(fnetg_ctx *ctx) {
   for (auto e : ctx->ev_free) cudaEventDestroy(e);
   if (ctx->ev0) cudaEventDestroy(ctx->ev0);
   if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+  if (ctx->batch) fnetg::batch_free(ctx->batch);
   cudaStream_t s = ctx->stream;
   delete ctx;  // DBuf destructors free device memory
   if (s) cudaStreamDestroy(s);

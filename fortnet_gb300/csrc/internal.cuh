@@ -124,6 +124,10 @@ struct PendingLaunch {
   cudaEvent_t e0, e1;
 };
 
+// state of the batched mixed-precision form (batch.cu)
+struct BatchState;
+void batch_free(BatchState *b);
+
 }  // namespace fnetg
 
 struct fnetg_ctx {
@@ -255,6 +259,16 @@ struct fnetg_ctx {
   fnetg::DBuf d_xnew, d_conv;
   void *h_pinned = nullptr;  // small pinned staging area for scalars
 
+  // force-loss training: weight c of c / (3 N) sum |F - F*|^2 (0 = energies only), FP64
+  // target forces [N][3], the loss's force gradient w [N][3], feature tangents u [N][nf],
+  // per-tile gradient partials
+  double fl_weight = 0.0;
+  fnetg::DBuf d_fl_target, d_fl_w, d_fl_u, d_fl_part, d_fl_gpart;
+
+  // batched mixed-precision form: mini-batch tiles, packed BF16 features and weights, the
+  // captured epoch (owned; freed with the context)
+  fnetg::BatchState *batch = nullptr;
+
   // profiling
   bool prof = false;
   std::map<std::string, fnetg::ProfEntry> prof_tab;
@@ -318,6 +332,8 @@ int run_predict(fnetg_ctx *ctx);
 int run_jacobian(fnetg_ctx *ctx, int out_index, void *dst);
 int run_forces(fnetg_ctx *ctx);
 int run_train_gradients(fnetg_ctx *ctx, int loss, const int32_t *order, bool need_predict);
+int run_force_gradients(fnetg_ctx *ctx, int loss);
+int run_features_jvp(fnetg_ctx *ctx, const void *d_w, void *d_u);
 int run_update_prepare(fnetg_ctx *ctx, double strength, double alpha);
 int run_optimizer_step(fnetg_ctx *ctx);
 int run_params_to_compute(fnetg_ctx *ctx);

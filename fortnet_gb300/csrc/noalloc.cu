@@ -13,6 +13,7 @@
 // scratch array has to start at zero.  The array is shared by every call on a device:
 // overlapping calls (other streams, other contexts on the same device) race on it.
 #include <algorithm>
+#include <atomic>
 
 #include "internal.cuh"
 
@@ -67,10 +68,11 @@ __global__ void zfinish_na_kernel(const double *part, int nparts, int ng, double
   out[f] = is_std ? sqrt(acc / den) : acc / den;
 }
 
-// Scratch address per device, looked up once with that device current (two host threads
-// making their first call at the same time both store the same address).
+// Scratch address per device, looked up once with that device current.  Host threads making
+// their first call on a device at the same time may both look it up; they store the same
+// value, and the atomic entries make that well defined.
 constexpr int kMaxDevices = 64;
-double *g_scratch_addr[kMaxDevices] = {};
+std::atomic<double *> g_scratch_addr[kMaxDevices] = {};
 
 template <typename T>
 int run_stats(fnetg_ctx *ctx, const int32_t *d_weights, double *d_zprec, double *scratch) {
@@ -104,6 +106,8 @@ extern "C" int fnetg_acsf_zscore_stats_noalloc(fnetg_ctx *ctx, const int32_t *d_
                                                double *d_zprec) {
   if (!ctx || !d_zprec) return FNETG_E_INVALID;
   FNETG_CHECK(ctx->feats_valid, FNETG_E_INVALID, "zscore_stats_noalloc: no features computed");
+  FNETG_CHECK(!ctx->zprec_valid, FNETG_E_INVALID,
+              "zscore_stats_noalloc: the features are already standardised (fnetg_acsf_zscore)");
   const int ng = (int)ctx->gf.size();
   FNETG_CHECK(ng >= 1 && ng <= kMaxCols, FNETG_E_UNSUPPORTED,
               "zscore_stats_noalloc: the number of ACSF columns must lie in [1, 4095]");
@@ -118,11 +122,11 @@ extern "C" int fnetg_acsf_zscore_stats_noalloc(fnetg_ctx *ctx, const int32_t *d_
     ~Restore() { cudaSetDevice(dev); }
   } restore{prev};
   FNETG_CUDA(cudaSetDevice(ctx->device));
-  double *scratch = g_scratch_addr[ctx->device];
+  double *scratch = g_scratch_addr[ctx->device].load(std::memory_order_relaxed);
   if (!scratch) {
     // first call on this device: resolve the scratch array's address
     FNETG_CUDA(cudaGetSymbolAddress((void **)&scratch, g_zscore_scratch));
-    g_scratch_addr[ctx->device] = scratch;
+    g_scratch_addr[ctx->device].store(scratch, std::memory_order_relaxed);
   }
   return ctx->prec == FNETG_FP64 ? run_stats<double>(ctx, d_weights, d_zprec, scratch)
                                  : run_stats<float>(ctx, d_weights, d_zprec, scratch);

@@ -683,6 +683,7 @@ __global__ void lbfgs_reset_kernel(double *state, size_t stride, const double *p
 
 int run_train_gradients(fnetg_ctx *ctx, int loss, const int32_t *order, bool need_predict) {
   (void)order;  // only the accumulation order changes with the reference's shuffle
+  if (ctx->fl_weight > 0.0) return run_force_gradients(ctx, loss);  // energy + force loss
   const int64_t N = ctx->N;
   const int S = ctx->S;
   const int nout = ctx->dims.back();
@@ -721,6 +722,40 @@ int run_train_gradients(fnetg_ctx *ctx, int loss, const int32_t *order, bool nee
     FNETG_CUDA(cudaGetLastError());
   }
   return run_mlp_backward(ctx);
+}
+
+// The loss kernel over structures [s0, s0 + count) only (a mini-batch): their atoms' scaled
+// output gradients and their per-structure loss parts.
+int launch_loss_range(fnetg_ctx *ctx, int s0, int count, int loss) {
+  if (count <= 0) return FNETG_OK;
+  LossArgs a{};
+  a.S = count;
+  a.off = ctx->d_off.as<int64_t>() + s0;
+  a.out = ctx->d_out.as<double>();
+  a.nout = ctx->dims.back();
+  a.ngt = ctx->ngt;
+  a.nat = ctx->nat;
+  a.gt = ctx->d_gt.as<double>() + (int64_t)s0 * ctx->ngt;
+  a.at = ctx->d_at.as<double>();
+  a.aw = ctx->d_aw.as<double>();
+  a.saw = ctx->d_struct_aw.as<double>() + s0;
+  a.w = ctx->d_w.as<int32_t>() + s0;
+  a.loss = loss;
+  a.delta = ctx->d_lossgrad.as<double>();
+  a.part = ctx->d_losspart.as<double>() + 2 * (int64_t)s0;
+  LaunchScope ls(ctx, "loss");
+  loss_kernel<<<ceil_div(count, 8), 256, 0, ctx->stream>>>(a);
+  FNETG_CUDA(cudaGetLastError());
+  return FNETG_OK;
+}
+
+// dataset loss from the per-structure parts of every structure
+int launch_loss_reduce(fnetg_ctx *ctx) {
+  LaunchScope ls(ctx, "loss");
+  loss_reduce_kernel<<<1, 1024, 0, ctx->stream>>>(ctx->d_losspart.as<double>(), ctx->S,
+                                                   ctx->d_scalars.as<double>());
+  FNETG_CUDA(cudaGetLastError());
+  return FNETG_OK;
 }
 
 int run_update_prepare(fnetg_ctx *ctx, double strength, double alpha) {

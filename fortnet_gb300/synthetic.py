@@ -19,6 +19,7 @@ pair within 6 Angstrom, in Hartree).
 from __future__ import annotations
 
 import math
+import os
 from dataclasses import dataclass
 
 import numpy as np
@@ -158,6 +159,47 @@ def _fcc(rng, jitter=0.05, a=4.05, reps=2):
     return frac * L + rng.normal(0.0, jitter, size=frac.shape), L
 
 
+def _morse_pairs(pos_A, species, L, cut):
+    """Every (atom, periodic image of an atom) pair within cut (A): centre index, neighbour
+    index, displacement centre - neighbour image (A), distance, Morse (D, a, r0)."""
+    from scipy.spatial import cKDTree
+
+    n = len(pos_A)
+    k = int(math.ceil(cut / L))
+    rng_k = np.arange(-k, k + 1)
+    shifts = np.stack(np.meshgrid(rng_k, rng_k, rng_k, indexing="ij"), -1).reshape(-1, 3) * L
+    ghosts = (pos_A[None, :, :] + shifts[:, None, :]).reshape(-1, 3)
+    gidx = np.tile(np.arange(n), len(shifts))
+    tree = cKDTree(ghosts)
+    pairs = tree.query_ball_point(pos_A, r=cut)
+    ii = np.repeat(np.arange(n), [len(p) for p in pairs])
+    gg = np.concatenate([np.asarray(p, dtype=np.int64) for p in pairs]) if n else np.zeros(0, int)
+    jj = gidx[gg]
+    d = pos_A[ii] - ghosts[gg]
+    r = np.sqrt(np.einsum("ij,ij->i", d, d))
+    keep = r > 1e-12  # drop the atom itself
+    ii, jj, d, r = ii[keep], jj[keep], d[keep], r[keep]
+    si, sj = species[ii], species[jj]
+    lo, hi = np.minimum(si, sj), np.maximum(si, sj)
+    D = np.zeros(len(r))
+    A = np.zeros(len(r))
+    R0 = np.zeros(len(r))
+    for (a, b), (dv, av, rv) in MORSE.items():
+        m = (lo == a) & (hi == b)
+        D[m], A[m], R0[m] = dv, av, rv
+    return ii, jj, d, r, D, A, R0
+
+
+def morse_forces(pos_A, species, L, cut=MORSE_CUT):
+    """Forces -dE/dr of morse_energy on every atom, Hartree / Bohr [n, 3]."""
+    ii, jj, d, r, D, A, R0 = _morse_pairs(pos_A, species, L, cut)
+    x = np.exp(-A * (r - R0))
+    dedr = 2.0 * A * D * x * (1.0 - x)  # d/dr of D (x^2 - 2x), eV / A
+    F = np.zeros_like(pos_A)
+    np.add.at(F, ii, -(dedr / r)[:, None] * d)
+    return F * EV__HARTREE / AA__BOHR
+
+
 def morse_energy(pos_A, species, L, cut=MORSE_CUT):
     """Total Morse energy (Hartree) over unique pairs of all periodic images, r <= cut (A)."""
     from scipy.spatial import cKDTree
@@ -189,34 +231,58 @@ def morse_energy(pos_A, species, L, cut=MORSE_CUT):
     return 0.5 * float(np.sum(D * (x * x - 2.0 * x))) * EV__HARTREE
 
 
-def generate(cfg: Config | str, nstruct=None, seed=None, targets=True) -> Dataset:
-    """Generate (the first nstruct structures of) a configuration's dataset."""
-    if isinstance(cfg, str):
-        cfg = CONFIGS[cfg]
-    rng = np.random.default_rng(cfg.seed if seed is None else seed)
-    S = cfg.nstruct if nstruct is None else nstruct
-    nat = _natoms(cfg, rng, cfg.nstruct)[:S]
+def _structure(cfg: Config, seed: int, s: int, n: int, targets: bool, forces: bool = False):
+    """Structure s of a configuration: its own random stream (seeded by (seed, s)), so that
+    structures can be generated in any order and in parallel."""
+    rng = np.random.default_rng([seed, s])
     nsp = len(cfg.atomic_numbers)
     ratios = np.asarray(cfg.ratios, dtype=np.float64) / np.sum(cfg.ratios)
-    coords, atnum, species, lat, gt = [], [], [], [], []
-    for s in range(S):
-        if cfg.fcc:
-            pos, L = _fcc(rng)
-            n = len(pos)
-        else:
-            n = int(nat[s])
-            L = (n / DENSITY) ** (1.0 / 3.0)
-            pos = _rsa_box(n, L, rng)
-        counts = np.floor(ratios * n).astype(int)
-        counts[-1] = n - counts[:-1].sum()
-        sp = np.repeat(np.arange(nsp), counts)
-        rng.shuffle(sp)
-        coords.append(pos * AA__BOHR)
-        atnum.append(np.asarray(cfg.atomic_numbers, dtype=np.int32)[sp])
-        species.append(sp.astype(np.int32))
-        Lb = L * AA__BOHR
-        lat.append(np.array([Lb, 0, 0, 0, Lb, 0, 0, 0, Lb], dtype=np.float64))
-        gt.append([morse_energy(pos, sp, L) if targets else 0.0])
+    if cfg.fcc:
+        pos, L = _fcc(rng)
+        n = len(pos)
+    else:
+        L = (n / DENSITY) ** (1.0 / 3.0)
+        pos = _rsa_box(n, L, rng)
+    counts = np.floor(ratios * n).astype(int)
+    counts[-1] = n - counts[:-1].sum()
+    sp = np.repeat(np.arange(nsp), counts)
+    rng.shuffle(sp)
+    e = morse_energy(pos, sp, L) if targets else 0.0
+    f = morse_forces(pos, sp, L) if forces else None
+    return pos * AA__BOHR, sp.astype(np.int32), L * AA__BOHR, e, f
+
+
+def _structure_job(job):
+    return _structure(*job)
+
+
+def generate(cfg: Config | str, nstruct=None, seed=None, targets=True, workers=None,
+             forces=False) -> Dataset:
+    """Generate (the first nstruct structures of) a configuration's dataset.  Large requests are
+    spread over a process pool (spawned, so it is safe after CUDA initialisation); the result
+    does not depend on the number of workers.  forces=True adds the Morse forces (Hartree /
+    Bohr) as meta["forces"] [Ntot, 3]."""
+    if isinstance(cfg, str):
+        cfg = CONFIGS[cfg]
+    seed = cfg.seed if seed is None else seed
+    rng = np.random.default_rng(seed)
+    S = cfg.nstruct if nstruct is None else nstruct
+    nat = _natoms(cfg, rng, cfg.nstruct)[:S]
+    jobs = [(cfg, seed, s, int(nat[s]), targets, forces) for s in range(S)]
+    if workers is None:
+        workers = min(os.cpu_count() or 1, 32) if S >= 1000 else 1
+    if workers > 1:
+        import multiprocessing as mp
+
+        with mp.get_context("spawn").Pool(workers) as pool:
+            res = pool.map(_structure_job, jobs, chunksize=max(1, S // (8 * workers)))
+    else:
+        res = [_structure_job(j) for j in jobs]
+    coords = [r[0] for r in res]
+    species = [r[1] for r in res]
+    atnum = [np.asarray(cfg.atomic_numbers, dtype=np.int32)[r[1]] for r in res]
+    lat = [np.array([r[2], 0, 0, 0, r[2], 0, 0, 0, r[2]], dtype=np.float64) for r in res]
+    gt = [[r[3]] for r in res]
     off = np.zeros(S + 1, dtype=np.int64)
     off[1:] = np.cumsum([len(c) for c in coords])
     ntot = int(off[-1])
@@ -232,5 +298,6 @@ def generate(cfg: Config | str, nstruct=None, seed=None, targets=True) -> Datase
         atomic_weights=np.ones(ntot),
         global_targets=np.asarray(gt, dtype=np.float64).reshape(S, 1),
         atomic_targets=np.zeros((ntot, 0)),
-        meta={"config": cfg.name},
+        meta={"config": cfg.name,
+              **({"forces": np.concatenate([r[4] for r in res])} if forces else {})},
     )

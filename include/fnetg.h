@@ -132,7 +132,10 @@ int fnetg_acsf_zscore(fnetg_ctx *ctx, const int32_t *weights, double *zprec, int
  * library, weights are read from device memory (d_weights: int32 [nstruct], or NULL for unit
  * weights) and the result goes to d_zprec (device, double [2 * nG]: means, then deviations).
  * Asynchronous on the context's stream; the features are not modified.  Limits: 1 <= nG <=
- * 4095 (FNETG_E_UNSUPPORTED beyond).  The first call on a device looks up the scratch array's
+ * 4095 (FNETG_E_UNSUPPORTED beyond).  Features already standardised by fnetg_acsf_zscore are
+ * refused (FNETG_E_INVALID).  The weights are not checked on the host: a zero weight total
+ * gives non-finite statistics (0/0), and negative weights give meaningless ones.
+ * The first call on a device looks up the scratch array's
  * address (make it before any stream capture).  The scratch array is shared per device:
  * calls that overlap in time (other streams or contexts on the same device) race, so
  * serialise them. */
@@ -174,6 +177,15 @@ int fnetg_forces(fnetg_ctx *ctx, double *forces);
  * fnetg_acsf_zscore call.  Runs the copies through the device pipeline in batches. */
 int fnetg_forces_fd(fnetg_ctx *ctx, double delta, double *forces);
 
+/* Matrix-free dG/dR: the derivative of every atom's standardised network inputs (z-score of
+ * the last fnetg_acsf_zscore call) along per-atom vectors w[Ntot*3],
+ *   u[a*nf + g] = sum_b sum_c d x_a[g] / d r_b[c] * w[3b + c],
+ * i.e. TAcsf_calculatePrime's dense [3, nF, N, N] derivative (acsf.F90:643-717, gFuncGrad
+ * 1496-1670) contracted with w, without storing it (physical derivative: every periodic image
+ * contributes).  Columns of external features are 0.  G1, G2, G3 and G5 without atom ids;
+ * at most 256 neighbours per atom (FNETG_E_UNSUPPORTED otherwise). */
+int fnetg_features_jvp(fnetg_ctx *ctx, const double *w, double *u);
+
 /* ---------------------------------------------------------------- training */
 /* Targets and weights of TDataset (fnetdata.F90:58-130). gt[S*ngt], at[Ntot*nat],
  * atomic_w[Ntot] (NULL = 1), weights[S] (NULL = 1). */
@@ -185,6 +197,17 @@ int fnetg_set_targets(fnetg_ctx *ctx, int32_t ngt, int32_t nat, const double *gt
  * changes the accumulation order, as the reference's shuffle does.  Outputs may be NULL. */
 int fnetg_train_gradients(fnetg_ctx *ctx, int32_t loss, const int32_t *order, double *grad,
                           double *loss_out, double *atomic_out);
+/* No counterpart in the reference (it trains on energies only): adds a force term to the
+ * training loss, L = L_E + weight / (3 Ntot) sum_a |F_a - F*_a|^2, with F the analytical forces
+ * of fnetg_forces and F*[Ntot*3] the target forces.  fnetg_train_gradients and
+ * fnetg_train_iteration then return the gradient of L (the energy part in the reference's raw
+ * convention, the force part multiplied by the summed datapoint weights, so that the update's
+ * normalisation leaves exactly dL_F/dtheta) and L as the loss.  Needs the neighbour list,
+ * z-scored features and tanh networks with one output.  weight = 0 switches the term off. */
+int fnetg_set_force_targets(fnetg_ctx *ctx, double weight, const double *forces);
+/* The energy and force parts of the last loss evaluated with a force term (loss_forces = 0
+ * without one). */
+int fnetg_last_losses(fnetg_ctx *ctx, double *loss_energy, double *loss_forces);
 /* TBpnn_update preamble (bpnn.F90:751-766): elastic-net term, 1/sum(weights) and norm2 of
  * a gradient matrix grad[nspecies*nparams] in place (host buffer, FP64 on the device). */
 int fnetg_update_prepare(fnetg_ctx *ctx, double *grad, double regu_strength, double regu_alpha,

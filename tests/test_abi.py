@@ -76,12 +76,15 @@ def test_no_gpu_context_creation_fails_cleanly():
 
 
 def test_caller_output_buffers_are_checked_on_the_host():
-    """predict/forces accept caller-owned buffers only as C-contiguous float64 of the result's
-    shape (checked before the library is called)."""
+    """predict/forces accept caller-owned buffers only as writeable, C-contiguous float64 of
+    the result's shape (checked before the library is called)."""
     good = np.zeros((5, 1, 3))
     api._check_out(good, (5, 1, 3))
+    readonly = np.zeros((5, 1, 3))
+    readonly.flags.writeable = False
+    frombuf = np.frombuffer(bytes(5 * 3 * 8), dtype=np.float64).reshape(5, 1, 3)
     for bad in (np.zeros((5, 3)), np.zeros((5, 1, 3), dtype=np.float32),
-                np.zeros((5, 1, 6))[:, :, ::2]):
+                np.zeros((5, 1, 6))[:, :, ::2], readonly, frombuf):
         try:
             api._check_out(bad, (5, 1, 3))
         except ValueError:

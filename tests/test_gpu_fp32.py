@@ -1,0 +1,200 @@
+"""The FP32 plain form (the one the benchmark times) against the FP64 oracle, per structure
+and per result: loss, weight gradient and L-BFGS steps of training, energies and forces of
+prediction, on the benchmark's own configurations (C1, samples of C2 and C3, including C3's
+cells smaller than the cutoff).
+
+Tolerances (the benchmark spec's numbers for the plain form, stated per structure):
+  * energies: |E32 - E64| <= 1e-5 |E64| for every structure;
+  * forces: max |F32 - F64| <= 1e-4 max |F64| over every structure's atoms and components;
+  * loss: relative 1e-5;
+  * weight gradient: ||g32 - g64|| <= 1e-4 ||g64|| per sub-network, and every component
+    within 1e-4 of the sub-network's largest;
+  * L-BFGS (memory 1000, line search): after each of the first iterations the parameters'
+    displacement from the start agrees within 1e-3 of its norm (the line search's secant
+    steps divide differences of directional derivatives, which amplifies the gradient's
+    rounding).
+Every test prints the errors it measured.
+"""
+
+import numpy as np
+import pytest
+
+import oracle as O
+from fortnet_gb300 import api, synthetic
+
+pytestmark = pytest.mark.gpu
+
+
+def _prepare(cfg_name, nstruct=None, pick=None):
+    cfg = synthetic.CONFIGS[cfg_name]
+    ds = synthetic.generate(cfg, nstruct=nstruct)
+    if pick is not None:
+        ds = subset(ds, pick(ds))
+    funcs = synthetic.gfunctions(cfg)
+    dims = synthetic.network_dims(cfg)
+    params = O.Ranlux(cfg.seed).init_bpnn(dims, "tanh", len(cfg.atomic_numbers))
+    return cfg, ds, funcs, dims, params
+
+
+def subset(ds, idx):
+    """The structures idx (in that order) of a dataset."""
+    from fortnet_gb300.fnetdata import Dataset
+
+    off = ds.atom_offsets
+    rows = np.concatenate([np.arange(off[s], off[s + 1]) for s in idx])
+    counts = [off[s + 1] - off[s] for s in idx]
+    noff = np.concatenate([[0], np.cumsum(counts)]).astype(np.int64)
+    return Dataset(atom_offsets=noff, coords=np.ascontiguousarray(ds.coords[rows]),
+                   atnum=ds.atnum[rows], species=ds.species[rows],
+                   periodic=ds.periodic[idx], latvecs=np.ascontiguousarray(ds.latvecs[idx]),
+                   atomic_numbers=ds.atomic_numbers, weights=ds.weights[idx],
+                   atomic_weights=ds.atomic_weights[rows],
+                   global_targets=np.ascontiguousarray(ds.global_targets[idx]),
+                   atomic_targets=ds.atomic_targets[rows], meta=ds.meta)
+
+
+def per_structure_errors(ds, pred32, pred64, F32=None, F64=None):
+    """Largest per-structure relative energy error and relative force error (max norm of the
+    structure's force error over the max norm of its forces)."""
+    off = ds.atom_offsets
+    e32 = np.add.reduceat(pred32[:, 0], off[:-1])
+    e64 = np.add.reduceat(pred64[:, 0], off[:-1])
+    e_err = float(np.max(np.abs(e32 - e64) / np.abs(e64)))
+    f_err = None
+    if F32 is not None:
+        F32 = F32.reshape(ds.ntot, -1)
+        F64 = F64.reshape(ds.ntot, -1)
+        f_err = max(float(np.max(np.abs(F32[off[s]:off[s + 1]] - F64[off[s]:off[s + 1]]))
+                          / np.max(np.abs(F64[off[s]:off[s + 1]]))) for s in range(ds.nstruct))
+    return e_err, f_err
+
+
+def _fp32_ctx(ds, funcs, zprec, dims, params):
+    ctx = api.Context(api.FP32)
+    ctx.upload(ds)
+    ctx.set_species(ds.species)
+    ctx.set_gfunctions(funcs)
+    ctx.acsf(download=False)
+    ctx.zscore(zprec=zprec)
+    ctx.set_network(dims, "tanh", params)
+    return ctx
+
+
+@pytest.mark.parametrize("cfg_name,nstruct", [("C1", 64), ("C2", 48)])
+def test_fp32_loss_and_gradient_match_fp64_oracle(cfg_name, nstruct):
+    """TBpnn_updateGradients / sysTrain (bpnn.F90:394-481, 610-704) and msLoss (loss.F90:512-579)
+    in the FP32 context against the FP64 oracle on the same inputs."""
+    cfg, ds, funcs, dims, params = _prepare(cfg_name, nstruct)
+    vals = O.acsf(ds, funcs)
+    zprec = O.zscore_stats(vals, ds)
+    feats = O.zscore_apply(vals, zprec)
+    dd, pred = O.train_gradients(dims, "tanh", params, feats, ds)
+    loss_ref = O.loss("mse", pred, ds, 1, 0)
+    with _fp32_ctx(ds, funcs, zprec, dims, params) as ctx:
+        ctx.set_targets(ds)
+        grad, loss, at = ctx.train_gradients("mse")
+    e_err, _ = per_structure_errors(ds, at, pred)
+    l_err = abs(loss - loss_ref) / abs(loss_ref)
+    g_norm = [float(np.linalg.norm(grad[s] - dd[s]) / np.linalg.norm(dd[s]))
+              for s in range(dd.shape[0])]
+    g_comp = [float(np.max(np.abs(grad[s] - dd[s])) / np.max(np.abs(dd[s])))
+              for s in range(dd.shape[0])]
+    print(f"{cfg_name} FP32 vs FP64: energy {e_err:.2e}, loss {l_err:.2e}, gradient norm-wise "
+          f"{max(g_norm):.2e}, gradient component {max(g_comp):.2e}")
+    assert e_err <= 1e-5
+    assert l_err <= 1e-5
+    assert max(g_norm) <= 1e-4
+    assert max(g_comp) <= 1e-4
+
+
+def test_fp32_lbfgs_iterations_match_fp64_oracle():
+    """The reference's default optimiser (L-BFGS, memory 1000, line search; lbfgs.F90:283-488,
+    linemin.F90:221-391) driven by the FP32 gradients, against the FP64 oracle."""
+    cfg, ds, funcs, dims, params0 = _prepare("C2", 48)
+    vals = O.acsf(ds, funcs)
+    zprec = O.zscore_stats(vals, ds)
+    feats = O.zscore_apply(vals, zprec)
+    nsp = params0.shape[0]
+    opts = [O.Lbfgs(params0[s], 1e-20, 1e-6, 1e4, 1000, True, False) for s in range(nsp)]
+    params = params0.copy()
+    dd, _ = O.train_gradients(dims, "tanh", params, feats, ds)
+    hist = []
+    niter = 5
+    for _ in range(niter):
+        g, _ = O.update_prepare(dims, "tanh", params, dd, 0.0, 0.0, float(ds.weights.sum()))
+        params = np.stack([opts[s].next(0.0, g[s])[0] for s in range(nsp)])
+        dd, _ = O.train_gradients(dims, "tanh", params, feats, ds)
+        hist.append(params.copy())
+    errs = []
+    with _fp32_ctx(ds, funcs, zprec, dims, params0) as ctx:
+        ctx.set_targets(ds)
+        ctx.optimizer_init("lbfgs", 1e-20, 1e-6, 1e4, memory=1000, linemin=True)
+        for it in range(niter):
+            ctx.train_iteration("mse")
+            p = ctx.params()
+            disp = np.linalg.norm(hist[it] - params0)
+            errs.append(float(np.linalg.norm(p - hist[it]) / max(disp, 1e-300)))
+    print("C2 FP32 L-BFGS displacement error per iteration: " + ", ".join(f"{e:.2e}" for e in errs))
+    assert max(errs) <= 1e-3
+
+
+def test_fp32_c2_energies_and_forces_per_structure():
+    """Prediction with analytical forces (predictBatch, forceAnalysis_analytical) on C2 cells:
+    every structure's energy and forces against the FP64 oracle (physical derivative: C2's
+    smaller cells see repeated images)."""
+    cfg, ds, funcs, dims, params = _prepare("C2", 12)
+    vals = O.acsf(ds, funcs)
+    zprec = O.zscore_stats(vals, ds)
+    feats = O.zscore_apply(vals, zprec)
+    pred = O.predict(dims, "tanh", params, feats, ds.species)
+    jac = O.jacobian(dims, "tanh", params, feats, ds.species)
+    F = O.forces(ds, funcs, zprec, jac, physical=True)
+    with _fp32_ctx(ds, funcs, zprec, dims, params) as ctx:
+        p32, _ = ctx.predict()
+        F32 = ctx.forces()
+    e_err, f_err = per_structure_errors(ds, p32, pred, F32, F)
+    print(f"C2 FP32 per structure: energy {e_err:.2e}, forces {f_err:.2e}")
+    assert e_err <= 1e-5
+    assert f_err <= 1e-4
+
+
+def test_fp32_c3_sample_with_cells_below_the_cutoff():
+    """C3 structures of at most 64 atoms (cubic cells of 4.95-9.8 A against a 6 A cutoff: self
+    images and repeated images): pair sets bit-exact, ACSF within 2e-5 of each function's
+    scale, energies and forces per structure against the FP64 oracle."""
+    def small(ds):
+        n = np.diff(ds.atom_offsets)
+        return [int(s) for s in np.flatnonzero(n <= 64)[:10]]
+
+    cfg, ds, funcs, dims, params = _prepare("C3", 60, pick=small)
+    Ls = ds.latvecs[:, 0] / synthetic.AA__BOHR
+    assert Ls.min() < cfg.rcut, "the sample must contain cells smaller than the cutoff"
+    rc = cfg.rcut * synthetic.AA__BOHR
+    ref_nb = O.neighbours(ds, rc)
+    vals = O.acsf(ds, funcs)
+    zprec = O.zscore_stats(vals, ds)
+    feats = O.zscore_apply(vals, zprec)
+    pred = O.predict(dims, "tanh", params, feats, ds.species)
+    jac = O.jacobian(dims, "tanh", params, feats, ds.species)
+    F = O.forces(ds, funcs, zprec, jac, physical=True)
+    with api.Context(api.FP32) as ctx:
+        ctx.upload(ds)
+        ctx.neighbors(rc)
+        nb = ctx.get_neighbors()
+        ctx.set_species(ds.species)
+        ctx.set_gfunctions(funcs)
+        v32 = ctx.acsf()
+        ctx.zscore(zprec=zprec)
+        ctx.set_network(dims, "tanh", params)
+        p32, _ = ctx.predict()
+        F32 = ctx.forces()
+    for k in range(4):
+        np.testing.assert_array_equal(nb[k], ref_nb[k])
+    scale = np.maximum(np.abs(vals).max(axis=0), 1e-30)
+    v_err = float(np.max(np.abs(v32 - vals) / scale))
+    e_err, f_err = per_structure_errors(ds, p32, pred, F32, F)
+    print(f"C3 sample ({ds.nstruct} structures, L {Ls.min():.2f}-{Ls.max():.2f} A): ACSF "
+          f"{v_err:.2e} of scale, energy {e_err:.2e}, forces {f_err:.2e}")
+    assert v_err <= 2e-5
+    assert e_err <= 1e-5
+    assert f_err <= 1e-4

@@ -230,20 +230,32 @@ def normwise(x, ref):
 
 
 def test_golden_prediction_fp32_tolerances():
-    """FP32 plain form: energies within 1e-5, forces within 1e-4 (norm-wise relative)."""
+    """FP32 plain form on every golden prediction case, per structure: each structure's summed
+    outputs within 1e-5 of the golden value (relative, per output), and each structure's
+    analytical forces within 1e-4 of its largest golden force component."""
+    worst_e, worst_f = 0.0, 0.0
     for name in GOLDEN_PRED:
         case = G.load_case(name)
         pred, forces = gpu_flows.prediction(case, api.FP32)
         ref = case.arrays["out_rawpredictions"]
         ds = case.ds
-        e = np.add.reduceat(pred, ds.atom_offsets[:-1], axis=0)
-        er = np.add.reduceat(ref, ds.atom_offsets[:-1], axis=0)
-        assert normwise(e, er) < 1e-5, name
+        off = ds.atom_offsets
+        e = np.add.reduceat(pred, off[:-1], axis=0)
+        er = np.add.reduceat(ref, off[:-1], axis=0)
+        e_err = float(np.max(np.abs(e - er) / np.abs(er)))
+        worst_e = max(worst_e, e_err)
+        assert e_err <= 1e-5, (name, e_err)
         # finite differences divide the FP32 rounding of the energies by 2 delta: their force
         # tolerance does not apply to the FP32 form (the FP64 test checks them)
         if forces is not None and case.settings.get("forces") == "analytical":
+            f = forces.reshape(forces.shape[0], -1)
             fr = case.arrays["out_forces"]
-            assert normwise(forces.reshape(forces.shape[0], -1), fr) < 1e-4, name
+            for s in range(ds.nstruct):
+                fs, frs = f[off[s]:off[s + 1]], fr[off[s]:off[s + 1]]
+                f_err = float(np.max(np.abs(fs - frs)) / np.max(np.abs(frs)))
+                worst_f = max(worst_f, f_err)
+                assert f_err <= 1e-4, (name, s, f_err)
+    print(f"golden FP32 per structure: energy {worst_e:.2e}, forces {worst_f:.2e}")
 
 
 def oracle_energy_forces(ds, funcs, zprec, dims, act, params, sp, physical=True):

@@ -14,7 +14,7 @@ from fortnet_gb300 import api, build as B, hdf5lite, netstat
 from fortnet_gb300.gfunctions import GFUNC_DTYPE, GFunction, pack
 from h5tree import assert_same_tree
 
-REF = os.environ.get("FORTNET_REFERENCE", "/root/reference")
+from conftest import REFERENCE as REF
 NETSTATS = sorted(glob.glob(os.path.join(REF, "test", "prog", "fortnet", "**", "*fortnet.hdf5"),
                             recursive=True))
 FNETOUTS = sorted(glob.glob(os.path.join(REF, "test", "prog", "fortnet", "**", "_fnetout.hdf5"),

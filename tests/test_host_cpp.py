@@ -14,7 +14,7 @@ from fortnet_gb300 import build as B
 from fortnet_gb300 import fnetdata, netstat
 from fortnet_gb300.gfunctions import TYPE_CODES
 
-REF = os.environ.get("FORTNET_REFERENCE", "/root/reference")
+from conftest import REFERENCE as REF
 DATASETS = sorted(glob.glob(os.path.join(REF, "test", "prog", "fortnet", "datasets", "*.hdf5")))
 NETSTATS = sorted(glob.glob(os.path.join(REF, "test", "prog", "fortnet", "prediction", "**",
                                          "fortnet.hdf5"), recursive=True))

@@ -67,3 +67,71 @@ def test_noalloc_stats_rejects_missing_features():
         ctx.set_gfunctions(synthetic.gfunctions(cfg))
         d_z = torch.zeros(2 * 96, dtype=torch.float64, device="cuda")
         assert _lib_fn(ctx)(ctx.h, None, d_z.data_ptr()) == -1  # FNETG_E_INVALID
+
+
+def _wide_ctx(ng, nstruct=3):
+    """A context whose network inputs are ng uploaded columns (G2 functions set only to fix
+    the column count; the features themselves come from fnetg_set_features)."""
+    from fortnet_gb300.gfunctions import GFunction
+
+    cfg = synthetic.CONFIGS["C2"]
+    ds = synthetic.generate(cfg, nstruct=nstruct, targets=False)
+    funcs = [GFunction("g2", 8.0, eta=0.01 + 1e-4 * k) for k in range(ng)]
+    ctx = api.Context(api.FP64)
+    ctx.upload(ds)
+    ctx.set_species(ds.species)
+    ctx.set_gfunctions(funcs)
+    feats = np.random.default_rng(ng).normal(3.0, 0.5, size=(ds.ntot, ng))
+    ctx.set_features(feats)
+    return ctx, ds
+
+
+def test_noalloc_stats_at_the_column_limit():
+    """nG = 4095, the largest the fixed scratch array takes: at most 32 chunks of 4096 partial
+    columns, so with ~9,600 atoms every chunk holds more than the minimum 256 atoms.  It matches
+    the allocating path; nG = 4096 is refused with FNETG_E_UNSUPPORTED."""
+    torch = pytest.importorskip("torch")
+    ctx, ds = _wide_ctx(4095, nstruct=60)
+    assert ds.ntot > 32 * 256
+    with ctx:
+        d_z = torch.full((2 * 4095,), float("nan"), dtype=torch.float64, device="cuda")
+        torch.cuda.synchronize()
+        rc = _lib_fn(ctx)(ctx.h, None, d_z.data_ptr())
+        assert rc == 0, ctx.lib.fnetg_last_error(ctx.h)
+        ctx.synchronize()
+        got = d_z.cpu().numpy().reshape(2, 4095)
+        ref = ctx.zscore()
+    np.testing.assert_allclose(got, ref, rtol=1e-13, atol=0.0)
+    ctx, _ = _wide_ctx(4096, nstruct=1)
+    with ctx:
+        d_z = torch.zeros(2 * 4096, dtype=torch.float64, device="cuda")
+        assert _lib_fn(ctx)(ctx.h, None, d_z.data_ptr()) == -7  # FNETG_E_UNSUPPORTED
+
+
+def test_noalloc_stats_refuse_standardised_features():
+    """After fnetg_acsf_zscore the device features are standardised; the statistics of the
+    raw features can no longer be formed and the call is refused (FNETG_E_INVALID)."""
+    torch = pytest.importorskip("torch")
+    cfg = synthetic.CONFIGS["C2"]
+    ds = synthetic.generate(cfg, nstruct=4, targets=False)
+    funcs = synthetic.gfunctions(cfg)
+    with _features_ctx(api.FP32, ds, funcs) as ctx:
+        ctx.zscore()
+        d_z = torch.zeros(2 * len(funcs), dtype=torch.float64, device="cuda")
+        assert _lib_fn(ctx)(ctx.h, None, d_z.data_ptr()) == -1
+
+
+def test_noalloc_stats_zero_weight_total_is_not_finite():
+    """The weights are read on the device and not checked: an all-zero weight vector gives the
+    documented non-finite statistics (0/0) instead of an error code."""
+    torch = pytest.importorskip("torch")
+    cfg = synthetic.CONFIGS["C2"]
+    ds = synthetic.generate(cfg, nstruct=4, targets=False)
+    funcs = synthetic.gfunctions(cfg)
+    with _features_ctx(api.FP64, ds, funcs) as ctx:
+        d_w = torch.zeros(ds.nstruct, dtype=torch.int32, device="cuda")
+        d_z = torch.zeros(2 * len(funcs), dtype=torch.float64, device="cuda")
+        torch.cuda.synchronize()
+        assert _lib_fn(ctx)(ctx.h, d_w.data_ptr(), d_z.data_ptr()) == 0
+        ctx.synchronize()
+        assert not np.any(np.isfinite(d_z.cpu().numpy()))
