@@ -107,6 +107,7 @@ def load(build_if_missing=True):
         "fnetg_batch_epoch": (C.c_int, [vp, i32, dbl, dbl, vp]),
         "fnetg_batch_predict": (C.c_int, [vp, vp, vp]),
         "fnetg_batch_sync_params": (C.c_int, [vp]),
+        "fnetg_batch_train_bf16": (C.c_int, [vp, i32]),
         "fnetg_server_create": (C.c_int, [C.POINTER(vp), vp, i32, vp, i32, vp, vp, i32, vp, i32,
                                           vp]),
         "fnetg_server_destroy": (C.c_int, [vp]),
@@ -413,6 +414,10 @@ class Context:
         _check_out(gl, (self.nstruct, 1))
         self._check(self.lib.fnetg_batch_predict(self.h, _p(at), _p(gl)))
         return at, gl
+
+    def batch_train_bf16(self, on=True):
+        """Full-batch training gradients from the tensor-core kernels (the precision form)."""
+        self._check(self.lib.fnetg_batch_train_bf16(self.h, int(on)))
 
     def batch_sync_params(self):
         self._check(self.lib.fnetg_batch_sync_params(self.h))

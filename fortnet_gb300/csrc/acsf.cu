@@ -723,6 +723,7 @@ template <typename T> int launch_ext(fnetg_ctx *ctx) {
 }  // namespace
 
 int run_acsf(fnetg_ctx *ctx) {
+  ctx->feat_gen++;
   ctx->nf = (int)ctx->gf.size() + (int)ctx->ext_idx.size();
   int rc = ctx->prec == FNETG_FP64 ? launch_acsf<double>(ctx) : launch_acsf<float>(ctx);
   if (rc) return rc;
@@ -732,10 +733,12 @@ int run_acsf(fnetg_ctx *ctx) {
 }
 
 int run_ext_inputs(fnetg_ctx *ctx) {
+  ctx->feat_gen++;
   return ctx->prec == FNETG_FP64 ? launch_ext<double>(ctx) : launch_ext<float>(ctx);
 }
 
 int run_zscore(fnetg_ctx *ctx, const int32_t *weights, bool compute) {
+  ctx->feat_gen++;
   return ctx->prec == FNETG_FP64 ? launch_zscore<double>(ctx, weights, compute)
                                  : launch_zscore<float>(ctx, weights, compute);
 }

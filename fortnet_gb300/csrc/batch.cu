@@ -46,6 +46,7 @@ int launch_loss_reduce(fnetg_ctx *ctx);
 namespace {
 
 constexpr int kRows = 128;          // atoms per tile (MMA M, TMEM lanes)
+constexpr int kMaxTcBlocks = 1024;  // CTAs of one tensor-core launch (gradient partial slots)
 constexpr int kThreads = 128;       // one thread per atom of the tile
 constexpr uint32_t kTmemCols = 512;
 // TMEM column regions
@@ -61,9 +62,13 @@ struct TcNet {
   int K0p, K1p, K2p, nmt0;           // padded GEMM K of the three layers, M tiles of X^T delta
   uint32_t x_bytes;                  // one tile of packed features
   uint32_t w_bytes;                  // one species' weight block
-  uint32_t off_w1f, off_w1b, off_w2; // offsets inside the weight block
-  // shared-memory plan (bytes)
+  uint32_t off_w1f, off_w1b, off_w0b, off_w2;  // offsets inside the weight block
+  // shared-memory plan (bytes) of the forward / training / Jacobian kernels
   uint32_t sm_x, sm_a1, sm_a2, sm_d2, sm_d1, sm_d3, sm_w, sm_total;
+  // shared-memory plan of the tangent (force-loss) kernel: features and their tangents,
+  // activations and tangents of both hidden layers (exactly their K columns: the 128-wide
+  // MN-major reads of a layer run on into the next buffer), adjoints, output adjoints, weights
+  uint32_t tm_x, tm_u, tm_a1, tm_t1, tm_a2, tm_t2, tm_zb, tm_zd, tm_d3a, tm_d3b, tm_w, tm_total;
   // reference layout of one species' parameters (network.F90:397-427)
   int64_t nparams, woff0, woff1, woff2, woff3, boff1, boff2, boff3;
 };
@@ -79,11 +84,13 @@ template <int HP> TcNet make_net(fnetg_ctx *ctx) {
   n.nmt0 = (n.K0p + kRows - 1) / kRows;
   n.x_bytes = (uint32_t)kRows * n.K0p * 2;
   const uint32_t w0 = (uint32_t)HP * n.K0p * 2, w1f = (uint32_t)HP * n.K1p * 2,
-                 w1b = (uint32_t)HP * HP * 2, w2 = (uint32_t)(HP + 4) * 4;
+                 w1b = (uint32_t)HP * HP * 2, w0b = (uint32_t)n.K0p * HP * 2,
+                 w2 = (uint32_t)(HP + 4) * 4;
   n.off_w1f = w0;
   n.off_w1b = w0 + w1f;
-  n.off_w2 = w0 + w1f + w1b;
-  n.w_bytes = (uint32_t)rup((int)(w0 + w1f + w1b + w2), 16);
+  n.off_w0b = w0 + w1f + w1b;
+  n.off_w2 = w0 + w1f + w1b + w0b;
+  n.w_bytes = (uint32_t)rup((int)(w0 + w1f + w1b + w0b + w2), 16);
   uint32_t o = 0;
   n.sm_x = o;
   o += n.x_bytes;
@@ -100,6 +107,30 @@ template <int HP> TcNet make_net(fnetg_ctx *ctx) {
   n.sm_w = o;
   o += n.w_bytes;
   n.sm_total = o;
+  o = 0;
+  n.tm_x = o;
+  o += n.x_bytes;
+  n.tm_u = o;
+  o += n.x_bytes;
+  n.tm_a1 = o;
+  o += kRows * n.K1p * 2;
+  n.tm_t1 = o;
+  o += kRows * n.K1p * 2;
+  n.tm_a2 = o;
+  o += kRows * n.K2p * 2;
+  n.tm_t2 = o;
+  o += kRows * n.K2p * 2;
+  n.tm_zb = o;
+  o += kRows * HP * 2;
+  n.tm_zd = o;
+  o += kRows * HP * 2;
+  n.tm_d3a = o;
+  o += kRows * 16 * 2;
+  n.tm_d3b = o;
+  o += kRows * 16 * 2;
+  n.tm_w = o;  // the weights close the plan: every over-read above lands inside it
+  o += n.w_bytes;
+  n.tm_total = o;
   n.nparams = ctx->nparams;
   n.woff0 = ctx->woff[0];
   n.woff1 = ctx->woff[1];
@@ -124,6 +155,13 @@ struct TcArgs {
   int32_t *gflag;             // [gridDim.x][nsp] partial written
   int nsp;
   int *err;                   // set to 1 when a bounded wait gave up
+  // Jacobian kernel: d out / d x of every atom, scaled by the inverse z-score deviations of
+  // the ACSF columns, [N][nf] atom order (the force kernel's input)
+  float *jac;
+  const float *zinv;          // [ng] inverse deviations, 0 = not standardised
+  int ng;
+  // tangent kernel: packed BF16 tangents of the inputs, same tiles and layout as x
+  const unsigned char *u;
 };
 
 __device__ __forceinline__ float tanh_fast(float x) {
@@ -163,6 +201,80 @@ __device__ __forceinline__ void store_act(unsigned char *buf, int r, float (&v)[
     float z[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
     for (int c = HP + 8; c < Kp; c += 8) st8(buf, tc::core_off(r, c, kRows), z);
   }
+}
+
+// Row r's tangents of one hidden layer (BF16, core layout): columns [0, HP) from v (padded
+// units carry zero tangents), zeros in the bias column and up to Kp.
+template <int HP>
+__device__ __forceinline__ void store_tan(unsigned char *buf, int r, const float (&v)[HP], int H,
+                                          int Kp) {
+#pragma unroll
+  for (int c = 0; c < HP; c += 8) st8(buf, tc::core_off(r, c, kRows), v + c);
+  if (H >= HP) {
+    float z[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    for (int c = HP; c < Kp; c += 8) st8(buf, tc::core_off(r, c, kRows), z);
+  }
+}
+
+// eight BF16 values of a core row back to floats
+__device__ __forceinline__ void ld8(const unsigned char *base, uint32_t off, float *v) {
+  const uint4 q = *reinterpret_cast<const uint4 *>(base + off);
+  const uint32_t w[4] = {q.x, q.y, q.z, q.w};
+#pragma unroll
+  for (int k = 0; k < 4; k++) {
+    __nv_bfloat162 p;
+    *reinterpret_cast<uint32_t *>(&p) = w[k];
+    v[2 * k] = __low2float(p);
+    v[2 * k + 1] = __high2float(p);
+  }
+}
+
+// nk MMAs of K = 16 accumulating into d: operands advance by a_step / b_step bytes per step
+__device__ __forceinline__ void mma_chain(uint32_t d, uint32_t a0, uint32_t a_lbo, uint32_t a_sbo,
+                                          uint32_t a_step, uint32_t b0, uint32_t b_lbo,
+                                          uint32_t b_sbo, uint32_t b_step, int nk, uint32_t idesc,
+                                          bool acc) {
+  for (int ks = 0; ks < nk; ks++)
+    tc::mma_bf16(d, tc::smem_desc(a0 + ks * a_step, a_lbo, a_sbo),
+                 tc::smem_desc(b0 + ks * b_step, b_lbo, b_sbo), idesc, (acc || ks > 0) ? 1u : 0u);
+}
+
+// The TMEM gradient accumulators (G0 in M tiles of 128 inputs, G1, G2) -> one partial slot in
+// the reference parameter order (all threads; thread tid holds lane tid of every region).
+template <int HP>
+__device__ void flush_grads(const TcNet &n, float *gp, uint32_t tm, uint32_t lane_off, int tid) {
+  for (int mt = 0; mt < n.nmt0; mt++) {
+    const int k = mt * kRows + tid;  // input feature (k == nf: the bias column)
+#pragma unroll
+    for (int c0 = 0; c0 < HP; c0 += 16) {
+      float v[16];
+      tc::tmem_ld16(tm + lane_off + kColG0 + mt * HP + c0, v);
+      tc::tmem_wait_ld();
+#pragma unroll
+      for (int q = 0; q < 16; q++) {
+        const int j = c0 + q;
+        if (j < n.H1 && k < n.nf) gp[n.woff0 + k + (int64_t)n.nf * j] = v[q];
+        else if (j < n.H1 && k == n.nf) gp[n.boff1 + j] = v[q];
+      }
+    }
+  }
+#pragma unroll
+  for (int c0 = 0; c0 < HP; c0 += 16) {
+    float v[16];
+    tc::tmem_ld16(tm + lane_off + kColG1 + c0, v);
+    tc::tmem_wait_ld();
+#pragma unroll
+    for (int q = 0; q < 16; q++) {
+      const int i = c0 + q;
+      if (i < n.H2 && tid < n.H1) gp[n.woff1 + tid + (int64_t)n.H1 * i] = v[q];
+      else if (i < n.H2 && tid == n.H1) gp[n.boff2 + i] = v[q];
+    }
+  }
+  float v[16];
+  tc::tmem_ld16(tm + lane_off + kColG2, v);
+  tc::tmem_wait_ld();
+  if (tid < n.H2) gp[n.woff2 + tid] = v[0];
+  else if (tid == n.H2) gp[n.boff3] = v[0];
 }
 
 // MODE 0: forward (atomic outputs).  MODE 1: forward + reverse pass + weight gradients.
@@ -205,41 +317,8 @@ __global__ void __launch_bounds__(kThreads, 1) tc_mlp_kernel(TcArgs a) {
 
   // gradient accumulators of cur_sp -> this CTA's partial slot (reference parameter order)
   auto flush = [&]() {
-    float *gp = a.gpart + ((int64_t)blockIdx.x * a.nsp + cur_sp) * n.nparams;
-    for (int mt = 0; mt < n.nmt0; mt++) {
-      const int k = mt * kRows + tid;  // input feature (k == nf: the bias column)
-#pragma unroll
-      for (int c0 = 0; c0 < HP; c0 += 16) {
-        float v[16];
-        tc::tmem_ld16(tm + lane_off + kColG0 + mt * HP + c0, v);
-        tc::tmem_wait_ld();
-#pragma unroll
-        for (int q = 0; q < 16; q++) {
-          const int j = c0 + q;
-          if (j < n.H1 && k < n.nf) gp[n.woff0 + k + (int64_t)n.nf * j] = v[q];
-          else if (j < n.H1 && k == n.nf) gp[n.boff1 + j] = v[q];
-        }
-      }
-    }
-#pragma unroll
-    for (int c0 = 0; c0 < HP; c0 += 16) {
-      float v[16];
-      tc::tmem_ld16(tm + lane_off + kColG1 + c0, v);
-      tc::tmem_wait_ld();
-#pragma unroll
-      for (int q = 0; q < 16; q++) {
-        const int i = c0 + q;
-        if (i < n.H2 && tid < n.H1) gp[n.woff1 + tid + (int64_t)n.H1 * i] = v[q];
-        else if (i < n.H2 && tid == n.H1) gp[n.boff2 + i] = v[q];
-      }
-    }
-    {
-      float v[16];
-      tc::tmem_ld16(tm + lane_off + kColG2, v);
-      tc::tmem_wait_ld();
-      if (tid < n.H2) gp[n.woff2 + tid] = v[0];
-      else if (tid == n.H2) gp[n.boff3] = v[0];
-    }
+    flush_grads<HP>(n, a.gpart + ((int64_t)blockIdx.x * a.nsp + cur_sp) * n.nparams, tm, lane_off,
+                    tid);
     touched |= 1ull << cur_sp;
   };
 
@@ -402,6 +481,420 @@ __global__ void __launch_bounds__(kThreads, 1) tc_mlp_kernel(TcArgs a) {
   if (warp == 0) tc::tmem_dealloc(tm, kTmemCols);
 }
 
+// CTA-uniform bounded wait that gives up the tile loop (a macro: it breaks the caller's loop)
+#define TC_WAIT(mb, ph)            \
+  if (!wait_all(&(mb), (ph))) {    \
+    failed = true;                 \
+    break;                         \
+  }                                \
+  (ph) ^= 1;                       \
+  tc::fence_after_sync()
+
+// make generic-proxy shared-memory writes visible to the MMAs, then hand over to the issuer
+__device__ __forceinline__ void publish_smem() {
+  tc::fence_async_smem();
+  tc::fence_before_sync();
+  __syncthreads();
+}
+
+// d out / d x of every atom (the input Jacobian of TNetwork_fdevi, network.F90:183-244, in
+// reverse mode): forward, delta_2 = w2 * f'(z2) with seed 1, delta_1 = (W1 delta_2) * f'(z1),
+// J = W0 delta_1 as a fourth GEMM (N = the padded inputs), each column scaled by its inverse
+// z-score deviation for the force contraction.  The atomic outputs are written as well.
+template <int HP>
+__global__ void __launch_bounds__(kThreads, 1) tc_jac_kernel(TcArgs a) {
+  extern __shared__ __align__(1024) unsigned char sm[];
+  __shared__ uint64_t mb_load, mb_mma;
+  __shared__ uint32_t tmem_base;
+  const TcNet &n = a.net;
+  const int tid = threadIdx.x, warp = tid >> 5;
+  unsigned char *X = sm + n.sm_x, *A1 = sm + n.sm_a1, *D2 = sm + n.sm_d2, *D1 = sm + n.sm_d1,
+                *W = sm + n.sm_w;
+  const float *w2 = reinterpret_cast<const float *>(W + n.off_w2);
+  if (tid == 0) {
+    tc::mbar_init(&mb_load, 1);
+    tc::mbar_init(&mb_mma, 1);
+    tc::mbar_fence_init();
+  }
+  if (warp == 0) tc::tmem_alloc(&tmem_base, kTmemCols);
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tm = tmem_base, lane_off = (uint32_t)(warp * 32) << 16;
+  const uint32_t sX = tc::smem_u32(X), sA1 = tc::smem_u32(A1), sD2 = tc::smem_u32(D2),
+                 sD1 = tc::smem_u32(D1), sW = tc::smem_u32(W);
+  const uint32_t id_h = tc::idesc_bf16(kRows, HP, 0, 0), id_j = tc::idesc_bf16(kRows, n.K0p, 0, 0);
+  constexpr uint32_t kColJ = 256;
+  uint32_t ph_load = 0, ph_mma = 0;
+  const int64_t nt = a.t1 - a.t0;
+  const int64_t my0 = a.t0 + nt * blockIdx.x / gridDim.x;
+  const int64_t my1 = a.t0 + nt * (blockIdx.x + 1) / gridDim.x;
+  int cur_sp = -1;
+  bool failed = false;
+  for (int64_t t = my0; t < my1; t++) {
+    const int sp = a.tile_sp[t];
+    const bool new_sp = sp != cur_sp;
+    tc::fence_before_sync();
+    __syncthreads();
+    if (tid == 0) {
+      tc::mbar_expect_tx(&mb_load, n.x_bytes + (new_sp ? n.w_bytes : 0u));
+      tc::bulk_g2s(X, a.x + t * (int64_t)n.x_bytes, n.x_bytes, &mb_load);
+      if (new_sp) tc::bulk_g2s(W, a.w + (int64_t)sp * n.w_bytes, n.w_bytes, &mb_load);
+    }
+    cur_sp = sp;
+    const int row = tid;
+    const int atom = a.tile_atoms[t * kRows + row];
+    if (!wait_all(&mb_load, ph_load)) {
+      tc::mbar_wait(&mb_load, ph_load);
+      failed = true;
+      break;
+    }
+    ph_load ^= 1;
+    if (tid == 0) {
+      tc::fence_after_sync();
+      mma_chain(tm, sX, 16 * kRows, 128, 32 * kRows, sW, 16 * HP, 128, 32 * HP, n.K0p / 16, id_h,
+                false);
+      tc::mma_commit(&mb_mma);
+    }
+    TC_WAIT(mb_mma, ph_mma);
+    float f1[HP];
+    {
+      float v[HP];
+#pragma unroll
+      for (int c0 = 0; c0 < HP; c0 += 16) {
+        float z[16];
+        tc::tmem_ld16(tm + lane_off + c0, z);
+        tc::tmem_wait_ld();
+#pragma unroll
+        for (int q = 0; q < 16; q++) {
+          const float th = tanh_fast(z[q]);
+          v[c0 + q] = th;
+          f1[c0 + q] = 1.f - th * th;
+        }
+      }
+      store_act<HP>(A1, row, v, n.H1, n.K1p);
+    }
+    publish_smem();
+    if (tid == 0) {
+      tc::fence_after_sync();
+      mma_chain(tm, sA1, 16 * kRows, 128, 32 * kRows, sW + n.off_w1f, 16 * HP, 128, 32 * HP,
+                n.K1p / 16, id_h, false);
+      tc::mma_commit(&mb_mma);
+    }
+    TC_WAIT(mb_mma, ph_mma);
+    {
+      float y = w2[HP], dv[HP];
+#pragma unroll
+      for (int c0 = 0; c0 < HP; c0 += 16) {
+        float z[16];
+        tc::tmem_ld16(tm + lane_off + c0, z);
+        tc::tmem_wait_ld();
+#pragma unroll
+        for (int q = 0; q < 16; q++) {
+          const float th = tanh_fast(z[q]);
+          y = fmaf(th, w2[c0 + q], y);
+          dv[c0 + q] = w2[c0 + q] * (1.f - th * th);
+        }
+      }
+      if (atom >= 0) a.out[atom] = (double)y;
+#pragma unroll
+      for (int c = 0; c < HP; c += 8) st8(D2, tc::core_off(row, c, kRows), dv + c);
+    }
+    publish_smem();
+    if (tid == 0) {
+      tc::fence_after_sync();
+      mma_chain(tm, sD2, 16 * kRows, 128, 32 * kRows, sW + n.off_w1b, 16 * HP, 128, 32 * HP,
+                HP / 16, id_h, false);
+      tc::mma_commit(&mb_mma);
+    }
+    TC_WAIT(mb_mma, ph_mma);
+    {
+      float dv[HP];
+#pragma unroll
+      for (int c0 = 0; c0 < HP; c0 += 16) {
+        float z[16];
+        tc::tmem_ld16(tm + lane_off + c0, z);
+        tc::tmem_wait_ld();
+#pragma unroll
+        for (int q = 0; q < 16; q++) dv[c0 + q] = z[q] * f1[c0 + q];
+      }
+#pragma unroll
+      for (int c = 0; c < HP; c += 8) st8(D1, tc::core_off(row, c, kRows), dv + c);
+    }
+    publish_smem();
+    if (tid == 0) {
+      tc::fence_after_sync();
+      mma_chain(tm + kColJ, sD1, 16 * kRows, 128, 32 * kRows, sW + n.off_w0b, 16 * n.K0p, 128,
+                32 * n.K0p, HP / 16, id_j, false);
+      tc::mma_commit(&mb_mma);
+    }
+    TC_WAIT(mb_mma, ph_mma);
+    for (int c0 = 0; c0 < n.K0p; c0 += 16) {
+      float v[16];
+      tc::tmem_ld16(tm + lane_off + kColJ + c0, v);
+      tc::tmem_wait_ld();
+      if (atom >= 0) {
+#pragma unroll
+        for (int q = 0; q < 16; q++) {
+          const int k = c0 + q;
+          if (k < n.nf) {
+            float s = 1.f;
+            if (k < a.ng) {
+              const float inv = a.zinv[k];
+              s = inv == 0.f ? 1.f : inv;
+            }
+            a.jac[(int64_t)atom * n.nf + k] = v[q] * s;
+          }
+        }
+      }
+    }
+  }
+  if (failed && tid == 0) atomicExch(a.err, 1);
+  tc::fence_before_sync();
+  __syncthreads();
+  if (warp == 0) tc::tmem_dealloc(tm, kTmemCols);
+}
+
+// The reverse pass of the force-loss gradient (forceloss.cu states the mathematics) on tensor
+// cores: per tile the values and tangents of both hidden layers (X W0 and U W0, A1 W1 and
+// T1 W1), the adjoints of the pre-activations and of their tangents (output adjoints: the
+// energy loss gradient and -1), and the weight gradients X^T zbar_1 + U^T zdotbar_1,
+// A1^T zbar_2 + T1^T zdotbar_2, A2^T ybar + T2^T ydotbar accumulated in TMEM as in the
+// training kernel.
+template <int HP>
+__global__ void __launch_bounds__(kThreads, 1) tc_tan_kernel(TcArgs a) {
+  extern __shared__ __align__(1024) unsigned char sm[];
+  __shared__ uint64_t mb_load, mb_mma;
+  __shared__ uint32_t tmem_base;
+  const TcNet &n = a.net;
+  const int tid = threadIdx.x, warp = tid >> 5;
+  unsigned char *X = sm + n.tm_x, *U = sm + n.tm_u, *A1 = sm + n.tm_a1, *T1 = sm + n.tm_t1,
+                *A2 = sm + n.tm_a2, *T2 = sm + n.tm_t2, *ZB = sm + n.tm_zb, *ZD = sm + n.tm_zd,
+                *D3a = sm + n.tm_d3a, *D3b = sm + n.tm_d3b, *W = sm + n.tm_w;
+  const float *w2 = reinterpret_cast<const float *>(W + n.off_w2);
+  if (tid == 0) {
+    tc::mbar_init(&mb_load, 1);
+    tc::mbar_init(&mb_mma, 1);
+    tc::mbar_fence_init();
+  }
+  if (warp == 0) tc::tmem_alloc(&tmem_base, kTmemCols);
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tm = tmem_base, lane_off = (uint32_t)(warp * 32) << 16;
+  const uint32_t sX = tc::smem_u32(X), sU = tc::smem_u32(U), sA1 = tc::smem_u32(A1),
+                 sT1 = tc::smem_u32(T1), sA2 = tc::smem_u32(A2), sT2 = tc::smem_u32(T2),
+                 sZB = tc::smem_u32(ZB), sZD = tc::smem_u32(ZD), sD3a = tc::smem_u32(D3a),
+                 sD3b = tc::smem_u32(D3b), sW = tc::smem_u32(W);
+  const uint32_t id_h = tc::idesc_bf16(kRows, HP, 0, 0);
+  const uint32_t id_g = tc::idesc_bf16(kRows, HP, 1, 1);
+  const uint32_t id_g2 = tc::idesc_bf16(kRows, 16, 1, 1);
+  constexpr uint32_t kColTan = 64;  // tangents next to the values
+  uint32_t ph_load = 0, ph_mma = 0;
+  const int64_t nt = a.t1 - a.t0;
+  const int64_t my0 = a.t0 + nt * blockIdx.x / gridDim.x;
+  const int64_t my1 = a.t0 + nt * (blockIdx.x + 1) / gridDim.x;
+  int cur_sp = -1;
+  bool gacc = false, failed = false;
+  uint64_t touched = 0;
+  // K-major: lbo 16 R, sbo 128, step 32 R; MN-major over 128 rows: lbo 128, sbo 2048, step 256
+  for (int64_t t = my0; t < my1; t++) {
+    const int sp = a.tile_sp[t];
+    const bool new_sp = sp != cur_sp;
+    if (new_sp && gacc) {
+      flush_grads<HP>(n, a.gpart + ((int64_t)blockIdx.x * a.nsp + cur_sp) * n.nparams, tm,
+                      lane_off, tid);
+      touched |= 1ull << cur_sp;
+      gacc = false;
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    if (tid == 0) {
+      tc::mbar_expect_tx(&mb_load, 2 * n.x_bytes + (new_sp ? n.w_bytes : 0u));
+      tc::bulk_g2s(X, a.x + t * (int64_t)n.x_bytes, n.x_bytes, &mb_load);
+      tc::bulk_g2s(U, a.u + t * (int64_t)n.x_bytes, n.x_bytes, &mb_load);
+      if (new_sp) tc::bulk_g2s(W, a.w + (int64_t)sp * n.w_bytes, n.w_bytes, &mb_load);
+    }
+    cur_sp = sp;
+    const int row = tid;
+    const int atom = a.tile_atoms[t * kRows + row];
+    const float ybar = atom >= 0 ? (float)a.delta[atom] : 0.f;
+    const float ydbar = atom >= 0 ? -1.f : 0.f;
+    if (!wait_all(&mb_load, ph_load)) {
+      tc::mbar_wait(&mb_load, ph_load);
+      failed = true;
+      break;
+    }
+    ph_load ^= 1;
+    // ---- layer 1: Z1 = X W0 (+ bias), Zdot1 = U W0
+    if (tid == 0) {
+      tc::fence_after_sync();
+      mma_chain(tm, sX, 16 * kRows, 128, 32 * kRows, sW, 16 * HP, 128, 32 * HP, n.K0p / 16, id_h,
+                false);
+      mma_chain(tm + kColTan, sU, 16 * kRows, 128, 32 * kRows, sW, 16 * HP, 128, 32 * HP,
+                n.K0p / 16, id_h, false);
+      tc::mma_commit(&mb_mma);
+    }
+    TC_WAIT(mb_mma, ph_mma);
+    {
+      float av[HP], tv[HP];
+#pragma unroll
+      for (int c0 = 0; c0 < HP; c0 += 16) {
+        float z[16], zd[16];
+        tc::tmem_ld16(tm + lane_off + c0, z);
+        tc::tmem_ld16(tm + lane_off + kColTan + c0, zd);
+        tc::tmem_wait_ld();
+#pragma unroll
+        for (int q = 0; q < 16; q++) {
+          const float th = tanh_fast(z[q]);
+          av[c0 + q] = th;
+          tv[c0 + q] = (1.f - th * th) * zd[q];
+        }
+      }
+      store_act<HP>(A1, row, av, n.H1, n.K1p);
+      store_tan<HP>(T1, row, tv, n.H1, n.K1p);
+    }
+    publish_smem();
+    // ---- layer 2: Z2 = A1 W1 (+ bias), Zdot2 = T1 W1
+    if (tid == 0) {
+      tc::fence_after_sync();
+      mma_chain(tm, sA1, 16 * kRows, 128, 32 * kRows, sW + n.off_w1f, 16 * HP, 128, 32 * HP,
+                n.K1p / 16, id_h, false);
+      mma_chain(tm + kColTan, sT1, 16 * kRows, 128, 32 * kRows, sW + n.off_w1f, 16 * HP, 128,
+                32 * HP, n.K1p / 16, id_h, false);
+      tc::mma_commit(&mb_mma);
+    }
+    TC_WAIT(mb_mma, ph_mma);
+    {
+      float av[HP], tv[HP], zb[HP], zdb[HP];
+#pragma unroll
+      for (int c0 = 0; c0 < HP; c0 += 16) {
+        float z[16], zd[16];
+        tc::tmem_ld16(tm + lane_off + c0, z);
+        tc::tmem_ld16(tm + lane_off + kColTan + c0, zd);
+        tc::tmem_wait_ld();
+#pragma unroll
+        for (int q = 0; q < 16; q++) {
+          const float th = tanh_fast(z[q]), pv = 1.f - th * th, wq = w2[c0 + q];
+          av[c0 + q] = th;
+          tv[c0 + q] = pv * zd[q];
+          // abar_2 = ybar w2, adotbar_2 = ydotbar w2
+          zb[c0 + q] = pv * (ybar * wq) - 2.f * th * pv * zd[q] * (ydbar * wq);
+          zdb[c0 + q] = pv * (ydbar * wq);
+        }
+      }
+      store_act<HP>(A2, row, av, n.H2, n.K2p);
+      store_tan<HP>(T2, row, tv, n.H2, n.K2p);
+#pragma unroll
+      for (int c = 0; c < HP; c += 8) {
+        st8(ZB, tc::core_off(row, c, kRows), zb + c);
+        st8(ZD, tc::core_off(row, c, kRows), zdb + c);
+      }
+      float e0[8] = {ybar, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+      float e1[8] = {ydbar, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+      float z8[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+      st8(D3a, tc::core_off(row, 0, kRows), e0);
+      st8(D3a, tc::core_off(row, 8, kRows), z8);
+      st8(D3b, tc::core_off(row, 0, kRows), e1);
+      st8(D3b, tc::core_off(row, 8, kRows), z8);
+    }
+    publish_smem();
+    // ---- abar_1 = zbar_2 W1^T, adotbar_1 = zdotbar_2 W1^T; G1, G2
+    if (tid == 0) {
+      tc::fence_after_sync();
+      mma_chain(tm, sZB, 16 * kRows, 128, 32 * kRows, sW + n.off_w1b, 16 * HP, 128, 32 * HP,
+                HP / 16, id_h, false);
+      mma_chain(tm + kColTan, sZD, 16 * kRows, 128, 32 * kRows, sW + n.off_w1b, 16 * HP, 128,
+                32 * HP, HP / 16, id_h, false);
+      mma_chain(tm + kColG1, sA1, 128, 16 * kRows, 256, sZB, 128, 16 * kRows, 256, kRows / 16,
+                id_g, gacc);
+      mma_chain(tm + kColG1, sT1, 128, 16 * kRows, 256, sZD, 128, 16 * kRows, 256, kRows / 16,
+                id_g, true);
+      mma_chain(tm + kColG2, sA2, 128, 16 * kRows, 256, sD3a, 128, 16 * kRows, 256, kRows / 16,
+                id_g2, gacc);
+      mma_chain(tm + kColG2, sT2, 128, 16 * kRows, 256, sD3b, 128, 16 * kRows, 256, kRows / 16,
+                id_g2, true);
+      tc::mma_commit(&mb_mma);
+    }
+    TC_WAIT(mb_mma, ph_mma);
+    {
+      // zbar_1 = f' abar_1 + f'' zdot_1 adotbar_1 with f'' zdot_1 = -2 a_1 t_1 (tanh)
+      float zb[HP], zdb[HP];
+#pragma unroll
+      for (int c0 = 0; c0 < HP; c0 += 16) {
+        float ab[16], tb[16], a1[16], t1[16];
+        tc::tmem_ld16(tm + lane_off + c0, ab);
+        tc::tmem_ld16(tm + lane_off + kColTan + c0, tb);
+        tc::tmem_wait_ld();
+        ld8(A1, tc::core_off(row, c0, kRows), a1);
+        ld8(A1, tc::core_off(row, c0 + 8, kRows), a1 + 8);
+        ld8(T1, tc::core_off(row, c0, kRows), t1);
+        ld8(T1, tc::core_off(row, c0 + 8, kRows), t1 + 8);
+#pragma unroll
+        for (int q = 0; q < 16; q++) {
+          const int j = c0 + q;
+          const float av = j < n.H1 ? a1[q] : 0.f, pv = 1.f - av * av;
+          zb[j] = pv * ab[q] - 2.f * av * t1[q] * tb[q];
+          zdb[j] = pv * tb[q];
+        }
+      }
+#pragma unroll
+      for (int c = 0; c < HP; c += 8) {
+        st8(ZB, tc::core_off(row, c, kRows), zb + c);
+        st8(ZD, tc::core_off(row, c, kRows), zdb + c);
+      }
+    }
+    publish_smem();
+    // ---- G0 += X^T zbar_1 + U^T zdotbar_1
+    if (tid == 0) {
+      tc::fence_after_sync();
+      for (int mt = 0; mt < n.nmt0; mt++) {
+        mma_chain(tm + kColG0 + mt * HP, sX + mt * 16 * 16 * kRows, 128, 16 * kRows, 256, sZB,
+                  128, 16 * kRows, 256, kRows / 16, id_g, gacc);
+        mma_chain(tm + kColG0 + mt * HP, sU + mt * 16 * 16 * kRows, 128, 16 * kRows, 256, sZD,
+                  128, 16 * kRows, 256, kRows / 16, id_g, true);
+      }
+      tc::mma_commit(&mb_mma);
+    }
+    TC_WAIT(mb_mma, ph_mma);
+    gacc = true;
+  }
+  if (!failed) {
+    if (gacc) {
+      flush_grads<HP>(n, a.gpart + ((int64_t)blockIdx.x * a.nsp + cur_sp) * n.nparams, tm,
+                      lane_off, tid);
+      touched |= 1ull << cur_sp;
+    }
+    if (tid < a.nsp) a.gflag[(int64_t)blockIdx.x * a.nsp + tid] = (int)((touched >> tid) & 1);
+  }
+  if (failed && tid == 0) atomicExch(a.err, 1);
+  tc::fence_before_sync();
+  __syncthreads();
+  if (warp == 0) tc::tmem_dealloc(tm, kTmemCols);
+}
+
+// tangents of the standardised inputs ([N][nf] atom order, the context's arithmetic) -> BF16
+// tiles in the feature layout; the bias column and padding rows are zero
+template <typename T>
+__global__ void pack_u_kernel(const T *u, int nf, int K0p, const int32_t *tile_atoms,
+                              int64_t ntiles, uint32_t x_bytes, unsigned char *out) {
+  const int groups = K0p / 8;
+  const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= ntiles * kRows * groups) return;
+  const int g = (int)(q % groups);
+  const int64_t tr = q / groups;
+  const int64_t t = tr / kRows;
+  const int r = (int)(tr % kRows);
+  const int atom = tile_atoms[tr];
+  float v[8];
+#pragma unroll
+  for (int c = 0; c < 8; c++) {
+    const int k = g * 8 + c;
+    v[c] = (atom >= 0 && k < nf) ? (float)u[(int64_t)atom * nf + k] : 0.f;
+  }
+  st8(out + t * (int64_t)x_bytes, tc::core_off(r, g * 8, kRows), v);
+}
+
 // ---- packing kernels ---------------------------------------------------------------------
 // Features of every tile row (z-scored, bucketed rows of the context) -> BF16 core layout,
 // constant 1 in column nf for real atoms; padding rows all zero.
@@ -434,14 +927,15 @@ __global__ void pack_x_kernel(const T *feat, const int32_t *bpos, int nf, int K0
 // FP64 master parameters (reference order) -> per-species BF16 weight images + FP32 output
 // layer: W0 image rows = first hidden units, columns = inputs (+ bias column nf); W1 forward
 // image rows = second hidden units, columns = first (+ bias column H1); W1 reverse image rows =
-// first hidden units, columns = second; then w2[HP], b3 as floats.
+// first hidden units, columns = second; W0 reverse image rows = inputs, columns = first hidden
+// units; then w2[HP], b3 as floats.
 template <int HP>
 __global__ void pack_w_kernel(const double *p64, TcNet n, unsigned char *w) {
   const int s = blockIdx.y;
   const double *p = p64 + (int64_t)s * n.nparams;
   unsigned char *blk = w + (int64_t)s * n.w_bytes;
-  const int e0 = HP * n.K0p, e1 = HP * n.K1p, e2 = HP * HP;
-  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < e0 + e1 + e2 + HP + 1;
+  const int e0 = HP * n.K0p, e1 = HP * n.K1p, e2 = HP * HP, e3 = n.K0p * HP;
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < e0 + e1 + e2 + e3 + HP + 1;
        q += gridDim.x * blockDim.x) {
     if (q < e0) {
       const int u = q / n.K0p, k = q % n.K0p;
@@ -459,8 +953,14 @@ __global__ void pack_w_kernel(const double *p64, TcNet n, unsigned char *w) {
       const double v = (j < n.H1 && i < n.H2) ? p[n.woff1 + j + (int64_t)n.H1 * i] : 0.0;
       *reinterpret_cast<__nv_bfloat16 *>(blk + n.off_w1b + tc::core_off(j, i, HP)) =
           __float2bfloat16_rn((float)v);
+    } else if (q < e0 + e1 + e2 + e3) {
+      // reverse image of W0 (rows = inputs, columns = first hidden units) for d out / d x
+      const int r = q - e0 - e1 - e2, k = r / HP, j = r % HP;
+      const double v = (k < n.nf && j < n.H1) ? p[n.woff0 + k + (int64_t)n.nf * j] : 0.0;
+      *reinterpret_cast<__nv_bfloat16 *>(blk + n.off_w0b + tc::core_off(k, j, n.K0p)) =
+          __float2bfloat16_rn((float)v);
     } else {
-      const int i = q - e0 - e1 - e2;  // i < HP: output weights, i == HP: output bias
+      const int i = q - e0 - e1 - e2 - e3;  // i < HP: output weights, i == HP: output bias
       float *tail = reinterpret_cast<float *>(blk + n.off_w2);
       tail[i] = i < HP ? (i < n.H2 ? (float)p[n.woff2 + i] : 0.f) : (float)p[n.boff3];
     }
@@ -468,43 +968,102 @@ __global__ void pack_w_kernel(const double *p64, TcNet n, unsigned char *w) {
 }
 
 // FP64 sums of the per-CTA partials in CTA order (deterministic); parameters no kernel
-// produces (the unused output-layer ww(d_L, 1) and the input-layer biases) are zero.
-__global__ void tc_reduce_kernel(const float *gpart, const int32_t *gflag, int nblk, int nsp,
-                                 TcNet n, double *grad64) {
-  const int s = blockIdx.y;
-  const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (q >= n.nparams) return;
-  const bool produced = q < n.woff3 || q >= n.boff1;
-  double acc = 0.0;
-  if (produced)
-    for (int b = 0; b < nblk; b++)
-      if (gflag[b * nsp + s]) acc += (double)gpart[((int64_t)b * nsp + s) * n.nparams + q];
-  grad64[(int64_t)s * n.nparams + q] = acc;
-}
+// produces (the unused output-layer ww(d_L, 1) and the input-layer biases) are zero.  Every
+// block also records the largest |g| of its parameters (bmax[species][block]) for the update's
+// displacement limit.
+constexpr int kRedThreads = 256;
 
-// Steepest descent of one sub-network with the mini-batch gradient (steepdesc.F90:126-204 after
-// TBpnn_update's normalisation bpnn.F90:751-766, no regularisation): d = -lr g / sum(w), scaled
-// to the maximal displacement when its largest component exceeds it.
-__global__ void tc_sd_kernel(double *params, const double *grad, int64_t np, double inv_sumw,
-                             double lr, double maxdisp) {
-  __shared__ double sh[512];
-  const int s = blockIdx.x;
-  double *x = params + (int64_t)s * np;
-  const double *g = grad + (int64_t)s * np;
-  double mx = 0.0;
-  for (int64_t q = threadIdx.x; q < np; q += blockDim.x)
-    mx = fmax(mx, fabs(-1.0 * lr * (g[q] * inv_sumw)));
-  sh[threadIdx.x] = mx;
+__global__ void __launch_bounds__(kRedThreads) tc_reduce_kernel(const float *gpart,
+                                                                const int32_t *gflag, int nblk,
+                                                                int nsp, TcNet n, double *grad64,
+                                                                double *bmax) {
+  __shared__ int flag[kMaxTcBlocks];
+  __shared__ double sh[kRedThreads];
+  const int s = blockIdx.y;
+  for (int b = threadIdx.x; b < nblk; b += blockDim.x) flag[b] = gflag[b * nsp + s];
   __syncthreads();
-  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+  const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  double acc = 0.0;
+  if (q < n.nparams && (q < n.woff3 || q >= n.boff1)) {
+    // four interleaved running sums, combined in a fixed order
+    double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+    const float *p = gpart + (int64_t)s * n.nparams + q;
+    const int64_t stride = (int64_t)nsp * n.nparams;
+    int b = 0;
+    for (; b + 3 < nblk; b += 4) {
+      if (flag[b]) a0 += (double)p[b * stride];
+      if (flag[b + 1]) a1 += (double)p[(b + 1) * stride];
+      if (flag[b + 2]) a2 += (double)p[(b + 2) * stride];
+      if (flag[b + 3]) a3 += (double)p[(b + 3) * stride];
+    }
+    for (; b < nblk; b++)
+      if (flag[b]) a0 += (double)p[b * stride];
+    acc = (a0 + a1) + (a2 + a3);
+  }
+  if (q < n.nparams) grad64[(int64_t)s * n.nparams + q] = acc;
+  sh[threadIdx.x] = fabs(acc);
+  __syncthreads();
+  for (int o = kRedThreads / 2; o > 0; o >>= 1) {
     if ((int)threadIdx.x < o) sh[threadIdx.x] = fmax(sh[threadIdx.x], sh[threadIdx.x + o]);
     __syncthreads();
   }
-  mx = sh[0];
-  for (int64_t q = threadIdx.x; q < np; q += blockDim.x) {
-    const double d = -1.0 * lr * (g[q] * inv_sumw);
-    x[q] = mx <= maxdisp ? x[q] + d : x[q] + (maxdisp / mx) * d;
+  if (threadIdx.x == 0) bmax[(int64_t)s * gridDim.x + blockIdx.x] = sh[0];
+}
+
+// Parameter q of a species -> its places in the species' weight images (the packing of
+// pack_w_kernel, one parameter at a time).
+template <int HP>
+__device__ __forceinline__ void write_images(const TcNet &n, unsigned char *blk, int64_t q,
+                                             double v) {
+  const __nv_bfloat16 h = __float2bfloat16_rn((float)v);
+  if (q >= n.woff0 && q < n.woff0 + (int64_t)n.nf * n.H1) {
+    const int r = (int)(q - n.woff0), k = r % n.nf, j = r / n.nf;
+    *reinterpret_cast<__nv_bfloat16 *>(blk + tc::core_off(j, k, HP)) = h;
+    *reinterpret_cast<__nv_bfloat16 *>(blk + n.off_w0b + tc::core_off(k, j, n.K0p)) = h;
+  } else if (q >= n.woff1 && q < n.woff1 + (int64_t)n.H1 * n.H2) {
+    const int r = (int)(q - n.woff1), j = r % n.H1, i = r / n.H1;
+    *reinterpret_cast<__nv_bfloat16 *>(blk + n.off_w1f + tc::core_off(i, j, HP)) = h;
+    *reinterpret_cast<__nv_bfloat16 *>(blk + n.off_w1b + tc::core_off(j, i, HP)) = h;
+  } else if (q >= n.woff2 && q < n.woff2 + n.H2) {
+    reinterpret_cast<float *>(blk + n.off_w2)[q - n.woff2] = (float)v;
+  } else if (q >= n.boff1 && q < n.boff1 + n.H1) {
+    *reinterpret_cast<__nv_bfloat16 *>(blk + tc::core_off((int)(q - n.boff1), n.nf, HP)) = h;
+  } else if (q >= n.boff2 && q < n.boff2 + n.H2) {
+    *reinterpret_cast<__nv_bfloat16 *>(blk + n.off_w1f + tc::core_off((int)(q - n.boff2), n.H1, HP)) = h;
+  } else if (q == n.boff3) {
+    reinterpret_cast<float *>(blk + n.off_w2)[HP] = (float)v;
   }
+}
+
+// Steepest descent of every sub-network with the mini-batch gradient (steepdesc.F90:126-204
+// after TBpnn_update's normalisation bpnn.F90:751-766, no regularisation): d = -lr g / sum(w),
+// scaled to the maximal displacement when its largest component exceeds it; the new FP64
+// parameter and its BF16 / FP32 image entries written in the same pass.
+template <int HP>
+__global__ void __launch_bounds__(kRedThreads) tc_update_kernel(double *params,
+                                                                const double *grad,
+                                                                const double *bmax, int nbm,
+                                                                TcNet n, double inv_sumw,
+                                                                double lr, double maxdisp,
+                                                                unsigned char *w) {
+  __shared__ double smax;
+  const int s = blockIdx.y;
+  if (threadIdx.x < 32) {
+    double m = 0.0;
+    for (int b = threadIdx.x; b < nbm; b += 32) m = fmax(m, bmax[(int64_t)s * nbm + b]);
+#pragma unroll
+    for (int k = 16; k > 0; k >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, k));
+    if (threadIdx.x == 0) smax = lr * (m * inv_sumw);
+  }
+  __syncthreads();
+  const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= n.nparams) return;
+  const double mx = smax;
+  double *x = params + (int64_t)s * n.nparams;
+  const double d = -1.0 * lr * (grad[(int64_t)s * n.nparams + q] * inv_sumw);
+  const double v = mx <= maxdisp ? x[q] + d : x[q] + (maxdisp / mx) * d;
+  x[q] = v;
+  write_images<HP>(n, w + (int64_t)s * n.w_bytes, q, v);
 }
 
 // ---- autotuned launch shapes, kept per network shape for the process ----------------------
@@ -520,7 +1079,7 @@ struct BatchState {
   std::vector<int64_t> tile0;  // [nbatch + 1] first tile of every mini-batch
   std::vector<int32_t> s0;     // [nbatch + 1] first structure of every mini-batch
   std::vector<double> sumw;    // [nbatch] datapoint weights of every mini-batch
-  DBuf d_tile_sp, d_tile_atoms, d_x, d_w, d_gpart, d_gflag, d_err;
+  DBuf d_tile_sp, d_tile_atoms, d_x, d_u, d_w, d_gpart, d_gflag, d_err, d_bmax;
   int grid_fwd = 0, grid_train = 0;
   // what the tile plan was built for
   int plan_S = -1, plan_nsp = 0;
@@ -555,6 +1114,14 @@ void *tc_kernel_hp(int hp, int mode) {
     default: return tc_kernel<64>(mode);
   }
 }
+void *tc_jac_hp(int hp) {
+  return hp == 16 ? (void *)tc_jac_kernel<16>
+                  : (hp == 32 ? (void *)tc_jac_kernel<32> : (void *)tc_jac_kernel<64>);
+}
+void *tc_tan_hp(int hp) {
+  return hp == 16 ? (void *)tc_tan_kernel<16>
+                  : (hp == 32 ? (void *)tc_tan_kernel<32> : (void *)tc_tan_kernel<64>);
+}
 
 int launch_tc(fnetg_ctx *ctx, int mode, int64_t t0, int64_t t1, int grid) {
   BatchState &b = *ctx->batch;
@@ -575,10 +1142,75 @@ int launch_tc(fnetg_ctx *ctx, int mode, int64_t t0, int64_t t1, int grid) {
   a.err = b.d_err.as<int>();
   grid = (int)std::max<int64_t>(1, std::min<int64_t>(grid, t1 - t0));
   void *k = tc_kernel_hp(b.HP, mode);
+  if (mode == 0) ctx->out_fgen = ctx->out_pgen = -1;  // d_out now holds the BF16 forward
   FNETG_CUDA(raise_smem_limit(k, b.net.sm_total));
   void *args[] = {&a};
   LaunchScope ls(ctx, mode == 0 ? "tc_forward" : "tc_train");
   FNETG_CUDA(cudaLaunchKernel(k, dim3(grid), dim3(kThreads), args, b.net.sm_total, ctx->stream));
+  return FNETG_OK;
+}
+
+TcArgs base_args(fnetg_ctx *ctx, int64_t t0, int64_t t1) {
+  BatchState &b = *ctx->batch;
+  TcArgs a{};
+  a.net = b.net;
+  a.x = b.d_x.as<unsigned char>();
+  a.w = b.d_w.as<unsigned char>();
+  a.tile_sp = b.d_tile_sp.as<int32_t>();
+  a.tile_atoms = b.d_tile_atoms.as<int32_t>();
+  a.t0 = t0;
+  a.t1 = t1;
+  a.out = ctx->d_out.as<double>();
+  a.delta = ctx->d_lossgrad.as<double>();
+  a.gpart = b.d_gpart.as<float>();
+  a.gflag = b.d_gflag.as<int32_t>();
+  a.nsp = ctx->nsp;
+  a.err = b.d_err.as<int>();
+  return a;
+}
+
+// the input Jacobian of every atom of tiles [t0, t1) into d_jacT (scaled for the force kernel)
+int launch_tc_jac(fnetg_ctx *ctx, int64_t t0, int64_t t1, int grid) {
+  BatchState &b = *ctx->batch;
+  if (t1 <= t0) return FNETG_OK;
+  TcArgs a = base_args(ctx, t0, t1);
+  FNETG_CUDA(ctx->d_jacT.ensure(sizeof(float) * std::max<int64_t>(ctx->N, 1) * ctx->nf));
+  a.jac = ctx->d_jacT.as<float>();
+  a.zinv = ctx->d_zprec_f.as<float>() + ctx->gf.size();
+  a.ng = (int)ctx->gf.size();
+  grid = (int)std::max<int64_t>(1, std::min<int64_t>(grid, t1 - t0));
+  void *k = tc_jac_hp(b.HP);
+  FNETG_CUDA(raise_smem_limit(k, b.net.sm_total));
+  void *args[] = {&a};
+  ctx->out_fgen = ctx->out_pgen = -1;
+  LaunchScope ls(ctx, "tc_jacobian");
+  FNETG_CUDA(cudaLaunchKernel(k, dim3(grid), dim3(kThreads), args, b.net.sm_total, ctx->stream));
+  return FNETG_OK;
+}
+
+// the force-loss reverse pass over tiles [t0, t1) (packed tangents in the batch state)
+int launch_tc_tan(fnetg_ctx *ctx, int64_t t0, int64_t t1, int grid) {
+  BatchState &b = *ctx->batch;
+  if (t1 <= t0) return FNETG_OK;
+  TcArgs a = base_args(ctx, t0, t1);
+  a.u = b.d_u.as<unsigned char>();
+  grid = (int)std::max<int64_t>(1, std::min<int64_t>(grid, t1 - t0));
+  void *k = tc_tan_hp(b.HP);
+  FNETG_CUDA(raise_smem_limit(k, b.net.tm_total));
+  void *args[] = {&a};
+  LaunchScope ls(ctx, "tc_tangent");
+  FNETG_CUDA(cudaLaunchKernel(k, dim3(grid), dim3(kThreads), args, b.net.tm_total, ctx->stream));
+  return FNETG_OK;
+}
+
+int launch_reduce(fnetg_ctx *ctx, int nblk) {
+  BatchState &b = *ctx->batch;
+  dim3 grid(ceil_div(b.net.nparams, kRedThreads), ctx->nsp);
+  LaunchScope ls(ctx, "tc_reduce");
+  tc_reduce_kernel<<<grid, kRedThreads, 0, ctx->stream>>>(
+      b.d_gpart.as<float>(), b.d_gflag.as<int32_t>(), nblk, ctx->nsp, b.net,
+      ctx->d_grad64.as<double>(), b.d_bmax.as<double>());
+  FNETG_CUDA(cudaGetLastError());
   return FNETG_OK;
 }
 
@@ -606,23 +1238,23 @@ int batch_step(fnetg_ctx *ctx, int k, int loss, bool update, double lr, double m
   rc = launch_tc(ctx, 1, b.tile0[k], b.tile0[k + 1], b.grid_train);
   if (rc) return rc;
   const int nblk = (int)std::max<int64_t>(1, std::min<int64_t>(b.grid_train, b.tile0[k + 1] - b.tile0[k]));
-  {
-    dim3 grid(ceil_div(b.net.nparams, 256), ctx->nsp);
-    LaunchScope ls(ctx, "tc_reduce");
-    tc_reduce_kernel<<<grid, 256, 0, ctx->stream>>>(b.d_gpart.as<float>(), b.d_gflag.as<int32_t>(),
-                                                     nblk, ctx->nsp, b.net,
-                                                     ctx->d_grad64.as<double>());
-    FNETG_CUDA(cudaGetLastError());
-  }
+  rc = launch_reduce(ctx, nblk);
+  if (rc) return rc;
   if (!update) return FNETG_OK;
-  {
-    LaunchScope ls(ctx, "tc_update");
-    tc_sd_kernel<<<ctx->nsp, 512, 0, ctx->stream>>>(ctx->d_params64.as<double>(),
-                                                    ctx->d_grad64.as<double>(), b.net.nparams,
-                                                    1.0 / b.sumw[k], lr, maxdisp);
-    FNETG_CUDA(cudaGetLastError());
-  }
-  return launch_pack_w(ctx);
+  dim3 grid(ceil_div(b.net.nparams, kRedThreads), ctx->nsp);
+  LaunchScope ls(ctx, "tc_update");
+  void *kern = b.HP == 16 ? (void *)tc_update_kernel<16>
+                          : (b.HP == 32 ? (void *)tc_update_kernel<32> : (void *)tc_update_kernel<64>);
+  double *p64 = ctx->d_params64.as<double>();
+  const double *g64 = ctx->d_grad64.as<double>();
+  const double *bm = b.d_bmax.as<double>();
+  int nbm = (int)grid.x;
+  TcNet net = b.net;
+  double inv = 1.0 / b.sumw[k];
+  unsigned char *wimg = b.d_w.as<unsigned char>();
+  void *args[] = {&p64, &g64, &bm, &nbm, &net, &inv, &lr, &maxdisp, &wimg};
+  FNETG_CUDA(cudaLaunchKernel(kern, grid, dim3(kRedThreads), args, 0, ctx->stream));
+  return FNETG_OK;
 }
 
 int check_err(fnetg_ctx *ctx) {
@@ -647,7 +1279,7 @@ int autotune(fnetg_ctx *ctx, int mode, int loss) {
     }
   }
   const int sms = num_sms();
-  std::vector<int> cand = {sms, sms / 2, (int)((tiles + 3) / 4), (int)((tiles + 5) / 6),
+  std::vector<int> cand = {sms, sms / 2, sms / 4, (int)((tiles + 3) / 4), (int)((tiles + 5) / 6),
                            (int)((tiles + 7) / 8)};
   int best = sms;
   float best_ms = 1e30f;
@@ -664,6 +1296,12 @@ int autotune(fnetg_ctx *ctx, int mode, int loss) {
       FNETG_CUDA(cudaEventRecord(ctx->ev0, ctx->stream));
       int rc = launch_tc(ctx, mode, b.tile0[0], b.tile0[1], g);
       if (rc) return rc;
+      if (mode == 1) {
+        // the training stage is timed with the reduction of its per-CTA partials, whose
+        // cost grows with the CTA count
+        rc = launch_reduce(ctx, (int)std::max<int64_t>(1, std::min<int64_t>(g, tiles)));
+        if (rc) return rc;
+      }
       FNETG_CUDA(cudaEventRecord(ctx->ev1, ctx->stream));
       FNETG_CUDA(cudaEventSynchronize(ctx->ev1));
       float t = 0.f;
@@ -709,6 +1347,61 @@ int pack_features(fnetg_ctx *ctx) {
 }
 
 }  // namespace
+
+// The full-batch training gradient (every tile of every mini-batch in one launch per stage)
+// with the tensor-core network passes, for fnetg_train_gradients / fnetg_train_iteration:
+//   energies only: forward, loss, reverse pass with weight gradients, FP64 reduction;
+//   with a force term: forward + input Jacobian (one kernel), loss, analytical forces from that
+//   Jacobian (FP32 kernel), the force term and its input tangents (FP32), the tangent reverse
+//   pass, FP64 reduction.
+int run_batch_gradients(fnetg_ctx *ctx, int loss) {
+  FNETG_CHECK(ctx->batch != nullptr, FNETG_E_INVALID, "tensor-core training: no batch setup");
+  BatchState &b = *ctx->batch;
+  const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(num_sms(), b.ntiles));
+  int rc = launch_pack_w(ctx);  // the parameters may have moved since the last images
+  if (rc) return rc;
+  FNETG_CUDA(ctx->d_grad64.ensure(sizeof(double) * ctx->nsp * ctx->nparams));
+  if (ctx->fl_weight > 0.0) {
+    FNETG_CHECK(ctx->prec == FNETG_FP32 && ctx->nb_valid && ctx->zprec_valid, FNETG_E_INVALID,
+                "tensor-core force loss: FP32 context with neighbour list and z-scored features");
+    FNETG_CHECK(b.net.tm_total <= 227 * 1024, FNETG_E_UNSUPPORTED,
+                "tensor-core force loss: tile buffers exceed shared memory (inputs too wide)");
+    rc = launch_tc_jac(ctx, 0, b.ntiles, grid);
+    if (rc) return rc;
+    rc = launch_loss_range(ctx, 0, ctx->S, loss);
+    if (rc) return rc;
+    rc = launch_loss_reduce(ctx);
+    if (rc) return rc;
+    ctx->jac_ready = true;
+    rc = run_forces(ctx);
+    ctx->jac_ready = false;
+    if (rc) return rc;
+    rc = run_force_loss_terms(ctx);
+    if (rc) return rc;
+    FNETG_CUDA(b.d_u.ensure((size_t)b.ntiles * b.net.x_bytes));
+    {
+      const int64_t total = b.ntiles * kRows * (b.net.K0p / 8);
+      LaunchScope ls(ctx, "tc_pack");
+      pack_u_kernel<float><<<ceil_div(total, 256), 256, 0, ctx->stream>>>(
+          ctx->d_fl_u.as<float>(), ctx->nf, b.net.K0p, b.d_tile_atoms.as<int32_t>(), b.ntiles,
+          b.net.x_bytes, b.d_u.as<unsigned char>());
+      FNETG_CUDA(cudaGetLastError());
+    }
+    rc = launch_tc_tan(ctx, 0, b.ntiles, grid);
+    if (rc) return rc;
+  } else {
+    rc = launch_tc(ctx, 0, 0, b.ntiles, grid);
+    if (rc) return rc;
+    rc = launch_loss_range(ctx, 0, ctx->S, loss);
+    if (rc) return rc;
+    rc = launch_loss_reduce(ctx);
+    if (rc) return rc;
+    rc = launch_tc(ctx, 1, 0, b.ntiles, grid);
+    if (rc) return rc;
+  }
+  return launch_reduce(ctx, grid);
+}
+
 }  // namespace fnetg
 
 using namespace fnetg;
@@ -787,6 +1480,8 @@ int fnetg_batch_setup(fnetg_ctx *ctx, int32_t batch_structures) {
   const int maxgrid = num_sms();
   FNETG_CUDA(b.d_gpart.ensure(sizeof(float) * (size_t)maxgrid * ctx->nsp * b.net.nparams));
   FNETG_CUDA(b.d_gflag.ensure(sizeof(int32_t) * (size_t)maxgrid * ctx->nsp));
+  FNETG_CUDA(b.d_bmax.ensure(sizeof(double) * (size_t)ctx->nsp *
+                             ceil_div(b.net.nparams, kRedThreads)));
   FNETG_CUDA(b.d_err.ensure(sizeof(int)));
   FNETG_CUDA(cudaMemsetAsync(b.d_err.p, 0, sizeof(int), ctx->stream));
   FNETG_CUDA(ctx->d_out.ensure(sizeof(double) * std::max<int64_t>(ctx->N, 1)));
@@ -927,6 +1622,14 @@ int fnetg_batch_predict(fnetg_ctx *ctx, double *atomic_out, double *global_out) 
     FNETG_CUDA(cudaMemcpyAsync(global_out, ctx->d_gsum.p, sizeof(double) * ctx->S,
                                cudaMemcpyDeviceToHost, ctx->stream));
   if (atomic_out || global_out) return check_err(ctx);
+  return FNETG_OK;
+}
+
+int fnetg_batch_train_bf16(fnetg_ctx *ctx, int32_t on) {
+  if (!ctx) return FNETG_E_INVALID;
+  FNETG_CHECK(!on || ctx->batch != nullptr, FNETG_E_INVALID,
+              "batch_train_bf16: call fnetg_batch_setup first");
+  ctx->batch_train = on != 0;
   return FNETG_OK;
 }
 

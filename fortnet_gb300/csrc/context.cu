@@ -266,6 +266,7 @@ int fnetg_upload_structures(fnetg_ctx *ctx, int32_t nstruct, const int64_t *atom
                             const int32_t *atnum, const double *coords, const int32_t *periodic,
                             const double *latvecs, const double *ext, int32_t next) {
   if (!ctx) return FNETG_E_INVALID;
+  ctx->feat_gen++;
   FNETG_CHECK(nstruct >= 0 && atom_offsets && (nstruct == 0 || (atnum && coords)),
               FNETG_E_INVALID, "upload_structures: null array");
   FNETG_CHECK(atom_offsets[0] == 0, FNETG_E_SHAPE, "atom_offsets[0] must be 0");
@@ -359,6 +360,7 @@ int fnetg_upload_structures(fnetg_ctx *ctx, int32_t nstruct, const int64_t *atom
 
 int fnetg_update_coords(fnetg_ctx *ctx, const double *coords) {
   if (!ctx || (!coords && ctx->N > 0)) return FNETG_E_INVALID;
+  ctx->feat_gen++;
   const int64_t N = ctx->N;
   for (int64_t q = 0; q < 3 * N; q++)
     FNETG_CHECK(std::isfinite(coords[q]), FNETG_E_GEOMETRY, "non-finite coordinate");
@@ -440,6 +442,7 @@ static int rebuild_buckets(fnetg_ctx *ctx, bool order_changes) {
 
 int fnetg_set_species(fnetg_ctx *ctx, const int32_t *species) {
   if (!ctx || (!species && ctx->N > 0)) return FNETG_E_INVALID;
+  ctx->feat_gen++;
   for (int64_t a = 0; a < ctx->N; a++)
     FNETG_CHECK(species[a] >= 0 && species[a] < 1024, FNETG_E_INVALID, "species index");
   if (ctx->net_set)
@@ -563,6 +566,7 @@ int fnetg_set_gfunctions(fnetg_ctx *ctx, int32_t ng, const fnetg_gfunc *g) {
   ctx->rad_fast = ctx->h_rad.empty() ? -1 : ctx->h_rad[0].rclass;
   for (auto &d : ctx->h_rad)
     if (d.type != 2 || d.atomid != 0 || d.rclass != ctx->rad_fast) ctx->rad_fast = -1;
+  ctx->h_ang_all = ang;  // every angular function, before the moment form takes its share
   // G5 functions with a small integer xi take the moment form; the rest (G4, other xi) the
   // triplet sweep
   std::vector<GDesc> mom, trip;
@@ -778,6 +782,10 @@ int fnetg_set_gfunctions(fnetg_ctx *ctx, int32_t ng, const fnetg_gfunc *g) {
       ctx->h_groups.push_back(grp);
     }
   }
+  FNETG_CUDA(ctx->d_ang_all.ensure(sizeof(GDesc) * std::max<size_t>(ctx->h_ang_all.size(), 1)));
+  if (!ctx->h_ang_all.empty())
+    FNETG_CUDA(copy_sync(ctx, ctx->d_ang_all.p, ctx->h_ang_all.data(),
+                          sizeof(GDesc) * ctx->h_ang_all.size(), cudaMemcpyHostToDevice));
   FNETG_CUDA(ctx->d_rad.ensure(sizeof(GDesc) * std::max<size_t>(ctx->h_rad.size(), 1)));
   FNETG_CUDA(ctx->d_ang.ensure(sizeof(GDesc) * std::max<size_t>(ctx->h_ang.size(), 1)));
   FNETG_CUDA(ctx->d_groups.ensure(sizeof(AGroup) * std::max<size_t>(ctx->h_groups.size(), 1)));
@@ -986,6 +994,7 @@ int fnetg_get_features(fnetg_ctx *ctx, double *feats, int32_t *nf_out) {
 
 int fnetg_set_features(fnetg_ctx *ctx, int32_t nf, const double *feats) {
   if (!ctx || nf <= 0 || (!feats && ctx->N > 0)) return FNETG_E_INVALID;
+  ctx->feat_gen++;
   const int64_t N = ctx->N;
   std::vector<int32_t> bpos(std::max<int64_t>(N, 1));
   if (N > 0)
@@ -1084,8 +1093,12 @@ int fnetg_predict(fnetg_ctx *ctx, double *atomic_out, double *global_out) {
   if (!ctx) return FNETG_E_INVALID;
   int rc = check_ready_for_network(ctx);
   if (rc) return rc;
-  rc = run_predict(ctx);
-  if (rc) return rc;
+  // the forward at these parameters and inputs is already on the device (a training
+  // iteration's gradient evaluation leaves it there): reused
+  if (ctx->out_pgen != ctx->param_gen || ctx->out_fgen != ctx->feat_gen) {
+    rc = run_predict(ctx);
+    if (rc) return rc;
+  }
   if (!atomic_out && !global_out) return FNETG_OK;
   const int nout = ctx->dims.back();
   if (atomic_out) {

@@ -240,22 +240,11 @@ __global__ void fl_finish_kernel(const double *part, int nb, double coef, double
 
 constexpr int kPrepBlocks = 256;
 
-template <typename T> int do_force_gradients(fnetg_ctx *ctx, int loss) {
+// The force term of the loss at the current forces: L_F into scalars[2] (and added to the
+// total in scalars[0]), the loss's force gradient w scaled by the summed weights, and the
+// input tangents u = (dx/dR) w (jvp.cu) into d_fl_u.
+template <typename T> int force_loss_terms(fnetg_ctx *ctx) {
   const int64_t N = ctx->N;
-  FNETG_CHECK(ctx->act == FNETG_ACT_TANH && ctx->dims.back() == 1 && ctx->ngt == 1 &&
-                  ctx->nat == 0,
-              FNETG_E_UNSUPPORTED,
-              "force loss: tanh networks with one output and one global target (energy)");
-  FNETG_CHECK(ctx->nb_valid && ctx->zprec_valid, FNETG_E_INVALID,
-              "force loss: neighbour list and z-scored features are needed");
-  int rc = run_predict(ctx);
-  if (rc) return rc;
-  rc = launch_loss_range(ctx, 0, ctx->S, loss);
-  if (rc) return rc;
-  rc = launch_loss_reduce(ctx);
-  if (rc) return rc;
-  rc = run_forces(ctx);
-  if (rc) return rc;
   FNETG_CUDA(ctx->d_fl_w.ensure(sizeof(T) * std::max<int64_t>(3 * N, 1)));
   FNETG_CUDA(ctx->d_fl_u.ensure(sizeof(T) * std::max<int64_t>(N, 1) * ctx->nf));
   FNETG_CUDA(ctx->d_fl_part.ensure(sizeof(double) * kPrepBlocks));
@@ -273,7 +262,25 @@ template <typename T> int do_force_gradients(fnetg_ctx *ctx, int loss) {
                                                ctx->d_scalars.as<double>());
     FNETG_CUDA(cudaGetLastError());
   }
-  rc = run_features_jvp(ctx, ctx->d_fl_w.p, ctx->d_fl_u.p);
+  return run_features_jvp(ctx, ctx->d_fl_w.p, ctx->d_fl_u.p);
+}
+
+template <typename T> int do_force_gradients(fnetg_ctx *ctx, int loss) {
+  FNETG_CHECK(ctx->act == FNETG_ACT_TANH && ctx->dims.back() == 1 && ctx->ngt == 1 &&
+                  ctx->nat == 0,
+              FNETG_E_UNSUPPORTED,
+              "force loss: tanh networks with one output and one global target (energy)");
+  FNETG_CHECK(ctx->nb_valid && ctx->zprec_valid, FNETG_E_INVALID,
+              "force loss: neighbour list and z-scored features are needed");
+  int rc = run_predict(ctx);
+  if (rc) return rc;
+  rc = launch_loss_range(ctx, 0, ctx->S, loss);
+  if (rc) return rc;
+  rc = launch_loss_reduce(ctx);
+  if (rc) return rc;
+  rc = run_forces(ctx);
+  if (rc) return rc;
+  rc = force_loss_terms<T>(ctx);
   if (rc) return rc;
   FlArgs<T> a{};
   a.net = make_flnet(ctx);
@@ -306,6 +313,10 @@ template <typename T> int do_force_gradients(fnetg_ctx *ctx, int loss) {
 }
 
 }  // namespace
+
+int run_force_loss_terms(fnetg_ctx *ctx) {
+  return ctx->prec == FNETG_FP64 ? force_loss_terms<double>(ctx) : force_loss_terms<float>(ctx);
+}
 
 int run_force_gradients(fnetg_ctx *ctx, int loss) {
   return ctx->prec == FNETG_FP64 ? do_force_gradients<double>(ctx, loss)

@@ -596,8 +596,10 @@ template <typename T, int D> int launch_forces_d(fnetg_ctx *ctx, TileArgs<T> &a,
   const int blocks = (int)std::max<int64_t>(
       1, std::min<int64_t>(want, (int64_t)num_sms() * per_sm * 8));
   for (int o = 0; o < nout; o++) {
-    int rc = run_jacobian(ctx, o, ctx->d_jacT.p);
-    if (rc) return rc;
+    if (!(ctx->jac_ready && nout == 1)) {
+      int rc = run_jacobian(ctx, o, ctx->d_jacT.p);
+      if (rc) return rc;
+    }
     a.out_index = o;
     LaunchScope ls(ctx, "forces");
     forces_kernel<T, D><<<blocks, wpb * 32, smem, ctx->stream>>>(a);

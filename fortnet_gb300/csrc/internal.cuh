@@ -160,6 +160,9 @@ struct fnetg_ctx {
   // G-functions
   std::vector<fnetg_gfunc> gf;
   std::vector<fnetg::GDesc> h_rad, h_ang;
+  std::vector<fnetg::GDesc> h_ang_all;  // every angular function in input order (h_ang holds
+                                        // only the triplet-sweep ones)
+  fnetg::DBuf d_ang_all, d_jvp_ang, d_jvp_grp;
   std::vector<int> rad_seg;  // [kMaxSpeciesCodes + 2]: all-atom radial functions [0, rad_seg[1]),
                              // species code c in [rad_seg[c + 1], rad_seg[c + 2])
   std::vector<int32_t> h_radv;  // value-kernel order of h_rad: by shape (type, cutoff class,
@@ -210,6 +213,9 @@ struct fnetg_ctx {
   double nbimg_shift = 0.0;  // largest translation of an image over all structures
   int64_t nb_hint_n = -1;   // atom count the capacity was measured on
   fnetg::DBuf d_pcount, d_poff, d_pend, d_pj, d_pmeta, d_rij, d_d2, d_scan_tmp, d_maxp, d_rcls2;
+  // cell lists of the larger structures (rebuilt with every neighbour search)
+  int64_t ncells = 0;
+  fnetg::DBuf d_cgrid, d_cnum, d_coff, d_ccount, d_cstart, d_cfill, d_akey, d_catom;
 
   // features (bucketed rows, compute precision)
   int nf = 0;
@@ -241,6 +247,10 @@ struct fnetg_ctx {
   std::vector<int64_t> h_ref_of_compute;  // the table last uploaded to d_ref_of_compute
   fnetg::DBuf d_gchunk;  // FP64 gradient sums of tile chunks
 
+  // versions of the network inputs and of the compute parameters; d_out holds the plain form's
+  // forward at (out_fgen, out_pgen), -1 when another kernel wrote it
+  int64_t feat_gen = 0, param_gen = 0, out_fgen = -1, out_pgen = -1;
+
   // outputs / training
   int ngt = 0, nat = 0;
   bool targets_set = false;
@@ -263,11 +273,13 @@ struct fnetg_ctx {
   // target forces [N][3], the loss's force gradient w [N][3], feature tangents u [N][nf],
   // per-tile gradient partials
   double fl_weight = 0.0;
+  bool jac_ready = false;  // d_jacT already holds the Jacobian the force kernel needs
   fnetg::DBuf d_fl_target, d_fl_w, d_fl_u, d_fl_part, d_fl_gpart;
 
   // batched mixed-precision form: mini-batch tiles, packed BF16 features and weights, the
   // captured epoch (owned; freed with the context)
   fnetg::BatchState *batch = nullptr;
+  bool batch_train = false;  // training gradients from the tensor-core kernels
 
   // profiling
   bool prof = false;
@@ -333,6 +345,8 @@ int run_jacobian(fnetg_ctx *ctx, int out_index, void *dst);
 int run_forces(fnetg_ctx *ctx);
 int run_train_gradients(fnetg_ctx *ctx, int loss, const int32_t *order, bool need_predict);
 int run_force_gradients(fnetg_ctx *ctx, int loss);
+int run_force_loss_terms(fnetg_ctx *ctx);
+int run_batch_gradients(fnetg_ctx *ctx, int loss);
 int run_features_jvp(fnetg_ctx *ctx, const void *d_w, void *d_u);
 int run_update_prepare(fnetg_ctx *ctx, double strength, double alpha);
 int run_optimizer_step(fnetg_ctx *ctx);

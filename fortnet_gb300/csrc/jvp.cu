@@ -15,6 +15,7 @@
 // formula (acsf.F90:1440-1492: ordered pairs including j = k, both orders for equal lists).
 // G4 and functions with atom ids are not supported here.
 #include <algorithm>
+#include <array>
 
 #include "internal.cuh"
 
@@ -26,6 +27,7 @@ namespace {
 
 constexpr int kJvpWarps = 4;
 constexpr int kJvpCap = 256;  // pairs of one atom staged in shared memory
+constexpr int kJvpGroup = 16; // angular functions evaluated together (same lists and eta)
 constexpr double kPi = 3.14159265358979323846;
 
 template <typename T> struct JvpArgs {
@@ -36,8 +38,10 @@ template <typename T> struct JvpArgs {
   const V4<T> *rij;
   const int8_t *code;
   const T *w;             // [N][3]
-  const GDesc *rad, *ang;
+  const GDesc *rad, *ang;     // radial functions; angular functions in group order
   int nrad, nang;
+  const int4 *grp;            // angular groups: (chan1, chan2, rclass | eclass << 8, first | count << 16)
+  int ngrp;
   const double *zsd;      // z-score deviations [ng] (FP64 path) or null
   const float *zinv;      // inverse deviations [ng], 0 = not standardised (FP32 path) or null
   T *u;                   // [N][nf] atom order
@@ -91,11 +95,20 @@ template <typename T>
 __global__ void __launch_bounds__(32 * kJvpWarps) jvp_kernel(JvpArgs<T> a) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  V4<T> *D = reinterpret_cast<V4<T> *>(smem) + (size_t)wid * 2 * kJvpCap;  // d (x, y, z, r)
-  V4<T> *Wd = D + kJvpCap;                                                 // w_j - w_a, r dot
-  uint32_t *info = reinterpret_cast<uint32_t *>(reinterpret_cast<V4<T> *>(smem) +
+  // per warp: d (x, y, z, r) and (w_j - w_a, r dot) of every pair, then per angular group the
+  // pair's E = exp(-eta r^2) fc and its derivative along w, and the two lists (pair indices)
+  V4<T> *D = reinterpret_cast<V4<T> *>(smem) + (size_t)wid * 2 * kJvpCap;
+  V4<T> *Wd = D + kJvpCap;
+  T *Ep = reinterpret_cast<T *>(reinterpret_cast<V4<T> *>(smem) + (size_t)kJvpWarps * 2 * kJvpCap) +
+          (size_t)wid * 2 * kJvpCap;
+  T *Edp = Ep + kJvpCap;
+  uint32_t *info = reinterpret_cast<uint32_t *>(reinterpret_cast<T *>(
+                       reinterpret_cast<V4<T> *>(smem) + (size_t)kJvpWarps * 2 * kJvpCap) +
                                                 (size_t)kJvpWarps * 2 * kJvpCap) +
                    (size_t)wid * kJvpCap;
+  uint16_t *L1 = reinterpret_cast<uint16_t *>(info + (size_t)(kJvpWarps - wid) * kJvpCap) +
+                 (size_t)wid * 2 * kJvpCap;
+  uint16_t *L2 = L1 + kJvpCap;
   const int64_t i = (int64_t)blockIdx.x * kJvpWarps + wid;
   if (i >= a.natoms) return;
   const int64_t p0 = a.poff[i];
@@ -143,51 +156,84 @@ __global__ void __launch_bounds__(32 * kJvpWarps) jvp_kernel(JvpArgs<T> a) {
     acc = jsum(acc);
     if (lane == 0) ui[g.out] = acc * zscale(a, g.out);
   }
-  // ---- angular G5: sum over ordered (j, k), j in list 1, k in list 2
-  for (int f = 0; f < a.nang; f++) {
-    const GDesc g = a.ang[f];
-    const T rc = (T)g.rcut, eta = (T)g.eta, lam = (T)g.lambda, xi = (T)g.xi;
-    T acc = (T)0;
-    for (int qj = lane; qj < np; qj += 32) {
-      const uint32_t ij = info[qj];
-      if (!in_chan(ij, g.chan1) || !((ij >> (16 + g.rclass)) & 1u)) continue;
-      const V4<T> dj = D[qj], wj = Wd[qj];
-      T fj, dfj;
-      fcut<T>(dj.w, rc, fj, dfj);
-      const T ej = exp(-eta * dj.w * dj.w);
-      const T Ej = ej * fj, Edj = ej * (dfj - (T)2 * eta * dj.w * fj) * wj.w;  // E_j, dE_j/dt
-      for (int qk = 0; qk < np; qk++) {
-        const uint32_t ik = info[qk];
-        if (!in_chan(ik, g.chan2) || !((ik >> (16 + g.rclass)) & 1u)) continue;
-        const V4<T> dk = D[qk], wk = Wd[qk];
-        T fk, dfk;
-        fcut<T>(dk.w, rc, fk, dfk);
-        const T ek = exp(-eta * dk.w * dk.w);
-        const T Ek = ek * fk, Edk = ek * (dfk - (T)2 * eta * dk.w * fk) * wk.w;
-        T c = (T)1, cd = (T)0;  // cos(theta) and its derivative; exactly (1, 0) for j = k
-        if (qj != qk) {
-          const T rr = dj.w * dk.w;
-          c = (dj.x * dk.x + dj.y * dk.y + dj.z * dk.z) / rr;
-          c = c > (T)1 ? (T)1 : (c < (T)-1 ? (T)-1 : c);
-          cd = (wj.x * dk.x + wj.y * dk.y + wj.z * dk.z + dj.x * wk.x + dj.y * wk.y +
-                dj.z * wk.z) / rr -
-               c * (wj.w / dj.w + wk.w / dk.w);
+  // ---- angular G5 by groups of functions sharing both lists, cutoff and eta: per ordered
+  // pair (j in list 1, k in list 2, j = k included) the cosine and its derivative once
+  const unsigned below = (1u << lane) - 1u;
+  for (int gi = 0; gi < a.ngrp; gi++) {
+    const int4 gr = a.grp[gi];
+    const int rcl = gr.z & 0xff, fcount = gr.w >> 16, first = gr.w & 0xffff;
+    const GDesc g0 = a.ang[first];
+    const T rc = (T)g0.rcut, eta = (T)g0.eta;
+    // E and its derivative of every pair in the cutoff class; the two lists in pair order
+    int n1 = 0, n2 = 0;
+    for (int q0 = 0; q0 < np; q0 += 32) {
+      const int q = q0 + lane;
+      bool in1 = false, in2 = false;
+      if (q < np) {
+        const uint32_t inf = info[q];
+        const bool inr = (inf >> (16 + rcl)) & 1u;
+        in1 = inr && in_chan(inf, gr.x);
+        in2 = inr && in_chan(inf, gr.y);
+        if (in1 || in2) {
+          const T r = D[q].w;
+          T fc, dfc;
+          fcut<T>(r, rc, fc, dfc);
+          const T e = exp(-eta * r * r);
+          Ep[q] = e * fc;
+          Edp[q] = e * (dfc - (T)2 * eta * r * fc) * Wd[q].w;
         }
-        const T base = (T)1 + lam * c;
+      }
+      const unsigned m1 = __ballot_sync(0xffffffffu, in1), m2 = __ballot_sync(0xffffffffu, in2);
+      if (in1) L1[n1 + __popc(m1 & below)] = (uint16_t)q;
+      if (in2) L2[n2 + __popc(m2 & below)] = (uint16_t)q;
+      n1 += __popc(m1);
+      n2 += __popc(m2);
+    }
+    __syncwarp();
+    T acc[kJvpGroup];
+#pragma unroll
+    for (int f = 0; f < kJvpGroup; f++) acc[f] = (T)0;
+    for (int t = lane; t < n1 * n2; t += 32) {
+      const int qj = L1[t / n2], qk = L2[t % n2];
+      const V4<T> dj = D[qj], wj = Wd[qj], dk = D[qk], wk = Wd[qk];
+      const T Ej = Ep[qj], Ek = Ep[qk], Edj = Edp[qj], Edk = Edp[qk];
+      T c = (T)1, cd = (T)0;  // cos(theta) and its derivative; exactly (1, 0) for j = k
+      if (qj != qk) {
+        const T rr = dj.w * dk.w;
+        c = (dj.x * dk.x + dj.y * dk.y + dj.z * dk.z) / rr;
+        c = c > (T)1 ? (T)1 : (c < (T)-1 ? (T)-1 : c);
+        cd = (wj.x * dk.x + wj.y * dk.y + wj.z * dk.z + dj.x * wk.x + dj.y * wk.y +
+              dj.z * wk.z) / rr -
+             c * (wj.w / dj.w + wk.w / dk.w);
+      }
+      const T EE = Ej * Ek, dEE = Edj * Ek + Ej * Edk;
+#pragma unroll
+      for (int f = 0; f < kJvpGroup; f++) {
+        if (f >= fcount) break;
+        const GDesc &g = a.ang[first + f];
+        const T lam = (T)g.lambda, base = (T)1 + lam * c;
         T p, pd;  // base^xi and xi base^(xi - 1)
         if (g.xi_int > 0) {
           const T b1 = ipow(base, g.xi_int - 1);
           p = b1 * base;
-          pd = xi * b1;
+          pd = (T)g.xi * b1;
         } else {
-          p = pow(base, xi);
-          pd = base > (T)0 ? xi * pow(base, xi - (T)1) : (T)0;
+          p = pow(base, (T)g.xi);
+          pd = base > (T)0 ? (T)g.xi * pow(base, (T)g.xi - (T)1) : (T)0;
         }
-        acc += pd * lam * cd * Ej * Ek + p * (Edj * Ek + Ej * Edk);
+        acc[f] += pd * lam * cd * EE + p * dEE;
       }
     }
-    acc = jsum(acc);
-    if (lane == 0) ui[g.out] = acc * (T)g.pref * zscale(a, g.out);
+#pragma unroll
+    for (int f = 0; f < kJvpGroup; f++) {
+      if (f >= fcount) break;
+      const T v = jsum(acc[f]);
+      if (lane == 0) {
+        const GDesc &g = a.ang[first + f];
+        ui[g.out] = v * (T)g.pref * zscale(a, g.out);
+      }
+    }
+    __syncwarp();
   }
 }
 
@@ -195,12 +241,40 @@ template <typename T> int do_jvp(fnetg_ctx *ctx, const T *d_w, T *d_u) {
   for (auto &g : ctx->h_rad) {
     FNETG_CHECK(g.atomid == 0, FNETG_E_UNSUPPORTED, "features_jvp: atom-id weighted functions");
   }
-  for (auto &g : ctx->h_ang) {
+  for (auto &g : ctx->h_ang_all) {
     FNETG_CHECK(g.type == 5 && g.atomid == 0, FNETG_E_UNSUPPORTED,
                 "features_jvp: G4 and atom-id weighted angular functions");
   }
   FNETG_CHECK(ctx->max_pairs <= kJvpCap, FNETG_E_UNSUPPORTED,
               "features_jvp: more than 256 neighbours of one atom");
+  // angular functions grouped by (lists, cutoff class, eta class), at most kJvpGroup each
+  std::vector<GDesc> ord;
+  std::vector<int4> grp;
+  {
+    std::vector<std::array<int, 4>> keys;
+    for (auto &g : ctx->h_ang_all) {
+      const std::array<int, 4> k{g.chan1, g.chan2, g.rclass, g.eclass};
+      if (std::find(keys.begin(), keys.end(), k) == keys.end()) keys.push_back(k);
+    }
+    for (auto &k : keys) {
+      std::vector<GDesc> mem;
+      for (auto &g : ctx->h_ang_all)
+        if (g.chan1 == k[0] && g.chan2 == k[1] && g.rclass == k[2] && g.eclass == k[3]) mem.push_back(g);
+      for (size_t q0 = 0; q0 < mem.size(); q0 += kJvpGroup) {
+        const int cnt = (int)std::min<size_t>(kJvpGroup, mem.size() - q0);
+        grp.push_back(make_int4(k[0], k[1], k[2] | (k[3] << 8), (int)ord.size() | (cnt << 16)));
+        ord.insert(ord.end(), mem.begin() + q0, mem.begin() + q0 + cnt);
+      }
+    }
+  }
+  FNETG_CUDA(ctx->d_jvp_ang.ensure(sizeof(GDesc) * std::max<size_t>(ord.size(), 1)));
+  FNETG_CUDA(ctx->d_jvp_grp.ensure(sizeof(int4) * std::max<size_t>(grp.size(), 1)));
+  if (!ord.empty()) {
+    FNETG_CUDA(copy_sync(ctx, ctx->d_jvp_ang.p, ord.data(), sizeof(GDesc) * ord.size(),
+                          cudaMemcpyHostToDevice));
+    FNETG_CUDA(copy_sync(ctx, ctx->d_jvp_grp.p, grp.data(), sizeof(int4) * grp.size(),
+                          cudaMemcpyHostToDevice));
+  }
   JvpArgs<T> a{};
   a.natoms = ctx->N;
   a.poff = ctx->d_poff.as<int64_t>();
@@ -211,9 +285,11 @@ template <typename T> int do_jvp(fnetg_ctx *ctx, const T *d_w, T *d_u) {
   a.code = ctx->d_code.as<int8_t>();
   a.w = d_w;
   a.rad = ctx->d_rad.as<GDesc>();
-  a.ang = ctx->d_ang.as<GDesc>();
+  a.ang = ctx->d_jvp_ang.as<GDesc>();
   a.nrad = (int)ctx->h_rad.size();
-  a.nang = (int)ctx->h_ang.size();
+  a.nang = (int)ord.size();
+  a.grp = ctx->d_jvp_grp.as<int4>();
+  a.ngrp = (int)grp.size();
   if (ctx->zprec_valid) {
     if (sizeof(T) == 8) a.zsd = ctx->d_zprec.as<double>() + ctx->gf.size();
     else a.zinv = ctx->d_zprec_f.as<float>() + ctx->gf.size();
@@ -224,7 +300,8 @@ template <typename T> int do_jvp(fnetg_ctx *ctx, const T *d_w, T *d_u) {
   a.err = reinterpret_cast<int *>(ctx->d_scalars.as<double>() + 15);
   FNETG_CUDA(cudaMemsetAsync(a.err, 0, sizeof(int), ctx->stream));
   FNETG_CUDA(cudaMemsetAsync(d_u, 0, sizeof(T) * std::max<int64_t>(ctx->N, 1) * ctx->nf, ctx->stream));
-  const size_t smem = (size_t)kJvpWarps * kJvpCap * (2 * sizeof(V4<T>) + sizeof(uint32_t));
+  const size_t smem = (size_t)kJvpWarps * kJvpCap *
+                      (2 * sizeof(V4<T>) + 2 * sizeof(T) + sizeof(uint32_t) + 2 * sizeof(uint16_t));
   FNETG_CUDA(raise_smem_limit((const void *)jvp_kernel<T>, smem));
   if (ctx->N > 0) {
     LaunchScope ls(ctx, "features_jvp");

@@ -853,10 +853,14 @@ template <typename T> int do_backward(fnetg_ctx *ctx) {
 }  // namespace
 
 int run_params_to_compute(fnetg_ctx *ctx) {
+  ctx->param_gen++;
   return ctx->prec == FNETG_FP64 ? do_params<double>(ctx) : do_params<float>(ctx);
 }
 int run_predict(fnetg_ctx *ctx) {
-  return ctx->prec == FNETG_FP64 ? do_predict<double>(ctx) : do_predict<float>(ctx);
+  const int rc = ctx->prec == FNETG_FP64 ? do_predict<double>(ctx) : do_predict<float>(ctx);
+  ctx->out_fgen = rc ? -1 : ctx->feat_gen;
+  ctx->out_pgen = rc ? -1 : ctx->param_gen;
+  return rc;
 }
 int run_jacobian(fnetg_ctx *ctx, int o, void *dst) {
   return ctx->prec == FNETG_FP64 ? do_jacobian<double>(ctx, o, dst) : do_jacobian<float>(ctx, o, dst);

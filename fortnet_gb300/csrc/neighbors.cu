@@ -52,7 +52,20 @@ struct NbArgs {
   int64_t *pbeg, *pend;
   int *overflow;
   unsigned long long *total;
+  // cell lists of the structures that use them (cgrid[s].w != 0): per structure the grid
+  // dimensions and its first cell, per cell the range of its atoms in catom (structure-local
+  // indices)
+  const int4 *cgrid;
+  const int64_t *coff;
+  const int64_t *cstart;
+  const int32_t *catom;
+  float inv_cs;   // 1 / cell edge (relative float frame)
+  float rbox;     // half-width of a centre's candidate box, >= the float pre-filter's reach
 };
+
+constexpr int kCellMin = 96;         // structures with fewer atoms test every atom
+constexpr int kCellMaxAtoms = 4096;  // per-warp bitmask of accepted neighbours per image
+constexpr int kCellDimMax = 32;      // cells per axis
 
 __device__ __forceinline__ double exact_d2(const double *ci, const double *cj, const double *cv,
                                            double *d) {
@@ -180,6 +193,7 @@ __global__ void __launch_bounds__(256, 4) nb_kernel(NbArgs a) {
   __shared__ int blk_max;
   __shared__ unsigned long long blk_sum;
   __shared__ int2 queue_all[kNbWarps][128];  // up to 31 pending + 64 new accepted
+  __shared__ uint32_t bits_all[kNbWarps][kCellMaxAtoms / 32];  // accepted atoms of one image
   if (threadIdx.x == 0) {
     blk_max = 0;
     blk_sum = 0;
@@ -198,6 +212,9 @@ __global__ void __launch_bounds__(256, 4) nb_kernel(NbArgs a) {
     int64_t wpos = 0;
     if (kFill) wpos = a.slab_cap > 0 ? i * a.slab_cap : a.poff[i];
     int2 *queue = queue_all[threadIdx.x >> 5];
+    uint32_t *bits = bits_all[threadIdx.x >> 5];
+    const int4 cg = a.cgrid ? a.cgrid[s] : make_int4(0, 0, 0, 0);
+    const int64_t cbase = cg.w ? a.coff[s] : 0;
     int qn = 0;           // queued accepted candidates (uniform across the warp)
     int64_t stored = 0;   // accepted candidates already stored
     int64_t cnt = 0;
@@ -224,6 +241,95 @@ __global__ void __launch_bounds__(256, 4) nb_kernel(NbArgs a) {
       }
       // candidates 64 at a time, two per lane: the shifted centre is formed once per image
       const float px = cif.x - ch.x, py = cif.y - ch.y, pz = cif.z - ch.z;
+      // the reference's decision for structure-local atom jl of this image
+      auto decide = [&](int jl) -> bool {
+        const V4<float> cjf = a.cf[a0 + jl];
+        const float e0 = cjf.x - px, e1 = cjf.y - py, e2 = cjf.z - pz;
+        const float df = e0 * e0 + e1 * e1 + e2 * e2;
+        if (df <= a.rc2_lo) return true;
+        if (df > a.rc2_hi) return false;
+        double d[3];
+        return exact_pair(a, ci, a0 + jl, img >= im0 ? img : -1, d) <= a.rc2;
+      };
+      if (cg.w) {
+        // cell list: only the cells of the box around the shifted centre are tested; the
+        // accepted atoms are marked in a bitmask and leave in the iterator's cyclic order
+        int lo[3], hi[3];
+        const float pc[3] = {px, py, pz};
+        const int gd[3] = {cg.x, cg.y, cg.z};
+        bool empty = false;
+        for (int c = 0; c < 3; c++) {
+          lo[c] = max(0, (int)floorf((pc[c] - a.rbox) * a.inv_cs));
+          hi[c] = min(gd[c] - 1, (int)floorf((pc[c] + a.rbox) * a.inv_cs));
+          empty = empty || lo[c] > hi[c];
+        }
+        if (empty) continue;
+        const int nwd = (n + 31) >> 5;
+        for (int w = lane; w < nwd; w += 32) bits[w] = 0u;
+        __syncwarp();
+        const int nx = hi[0] - lo[0] + 1, ny = hi[1] - lo[1] + 1, nz = hi[2] - lo[2] + 1;
+        for (int c = lane; c < nx * ny * nz; c += 32) {
+          const int cx = lo[0] + c / (ny * nz), cy = lo[1] + (c / nz) % ny, cz = lo[2] + c % nz;
+          const int64_t key = cbase + ((int64_t)cx * cg.y + cy) * cg.z + cz;
+          for (int64_t q = a.cstart[key]; q < a.cstart[key + 1]; q++) {
+            const int jl = a.catom[q];
+            if (jl == il && img < im0) continue;  // the centre itself in the central cell
+            if (decide(jl)) atomicOr(&bits[jl >> 5], 1u << (jl & 31));
+          }
+        }
+        __syncwarp();
+        // slots of the cyclic order: the start word from the start bit, the other words, the
+        // start word below the start bit
+        const int start = img < im0 ? (il + 1 == n ? 0 : il + 1) : il;
+        const int sw = start >> 5, sb = start & 31;
+        const int nslot = nwd + (sb > 0 ? 1 : 0);
+        for (int base = 0; base < nslot; base += 32) {
+          const int t = base + lane;
+          uint32_t m = 0u;
+          int widx = 0;
+          if (t < nslot) {
+            widx = t == nwd ? sw : (sw + t) % nwd;
+            m = bits[widx];
+            if (t == 0) m &= sb > 0 ? ~((1u << sb) - 1u) : 0xffffffffu;
+            else if (t == nwd) m &= (1u << sb) - 1u;
+          }
+          unsigned nzm = __ballot_sync(0xffffffffu, m != 0u);
+          if (!kFill) {
+            int c = __popc(m);
+#pragma unroll
+            for (int k = 16; k > 0; k >>= 1) c += __shfl_xor_sync(0xffffffffu, c, k);
+            cnt += c;
+            continue;
+          }
+          while (nzm) {
+            const int src = __ffs(nzm) - 1;
+            nzm &= nzm - 1;
+            const uint32_t mw = __shfl_sync(0xffffffffu, m, src);
+            const int wsrc = __shfl_sync(0xffffffffu, widx, src);
+            const bool ok = (mw >> lane) & 1u;
+            const unsigned mb = __ballot_sync(0xffffffffu, ok);
+            const unsigned below = (1u << lane) - 1u;
+            if (ok) queue[qn + __popc(mb & below)] = make_int2(wsrc * 32 + lane, (int)img);
+            qn += __popc(mb);
+            cnt += __popc(mb);
+            __syncwarp();
+            while (qn >= 32) {
+              const int2 e = queue[lane];
+              store_pair<T>(a, ci, cif, cil, i, a0, e.x, e.y, im0, wpos, stored + lane);
+              const int rem = qn - 32;
+              const int2 v0 = lane < rem ? queue[lane + 32] : make_int2(0, 0);
+              const int2 v1 = lane + 32 < rem ? queue[lane + 64] : make_int2(0, 0);
+              __syncwarp();
+              if (lane < rem) queue[lane] = v0;
+              if (lane + 32 < rem) queue[lane + 32] = v1;
+              __syncwarp();
+              qn -= 32;
+              stored += 32;
+            }
+          }
+        }
+        continue;
+      }
       auto test = [&](int k, bool &ok, int &jl) {
         ok = false;
         jl = 0;
@@ -415,7 +521,113 @@ __global__ void prep_coords_kernel(const double *coords, const int64_t *off, V4<
     }
 }
 
+// Cell grid of every structure that uses one: edge 1 / inv_cs over its bounding box (relative
+// float frame), at most kCellDimMax cells per axis.
+__global__ void cell_grid_kernel(const float *bbox, const int64_t *off, int S, float inv_cs,
+                                 int4 *cgrid, int64_t *ncell) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= S) return;
+  const int64_t n = off[s + 1] - off[s];
+  const bool on = n >= kCellMin && n <= kCellMaxAtoms;
+  int g[3] = {0, 0, 0};
+  if (on)
+    for (int c = 0; c < 3; c++)
+      g[c] = min(kCellDimMax, max(1, (int)(bbox[6 * s + 3 + c] * inv_cs) + 1));
+  cgrid[s] = make_int4(g[0], g[1], g[2], on ? 1 : 0);
+  ncell[s] = on ? (int64_t)g[0] * g[1] * g[2] : 0;
+}
+
+__device__ __forceinline__ int64_t cell_key(const V4<float> &p, const int4 &g, int64_t base,
+                                            float inv_cs) {
+  const int cx = min(g.x - 1, max(0, (int)floorf(p.x * inv_cs)));
+  const int cy = min(g.y - 1, max(0, (int)floorf(p.y * inv_cs)));
+  const int cz = min(g.z - 1, max(0, (int)floorf(p.z * inv_cs)));
+  return base + ((int64_t)cx * g.y + cy) * g.z + cz;
+}
+
+__global__ void cell_count_kernel(const V4<float> *cf, const int32_t *astruct, int64_t N,
+                                  const int4 *cgrid, const int64_t *coff, float inv_cs,
+                                  int64_t *akey, int64_t *ccount) {
+  const int64_t a = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (a >= N) return;
+  const int s = astruct[a];
+  const int4 g = cgrid[s];
+  if (!g.w) {
+    akey[a] = -1;
+    return;
+  }
+  const int64_t key = cell_key(cf[a], g, coff[s], inv_cs);
+  akey[a] = key;
+  atomicAdd(reinterpret_cast<unsigned long long *>(ccount + key), 1ull);
+}
+
+__global__ void cell_fill_kernel(const int64_t *akey, const int32_t *astruct, const int64_t *off,
+                                 int64_t N, const int64_t *cstart, int64_t *cfill,
+                                 int32_t *catom) {
+  const int64_t a = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (a >= N) return;
+  const int64_t key = akey[a];
+  if (key < 0) return;
+  const int64_t pos =
+      cstart[key] + (int64_t)atomicAdd(reinterpret_cast<unsigned long long *>(cfill + key), 1ull);
+  catom[pos] = (int32_t)(a - off[astruct[a]]);
+}
+
 }  // namespace
+
+// Cell lists of the structures with kCellMin..kCellMaxAtoms atoms for the given cutoff (cells of
+// half the cutoff): counted, scanned and filled on the device.
+int build_cells(fnetg_ctx *ctx, double rcut, float &inv_cs) {
+  const int S = ctx->S;
+  const int64_t N = ctx->N;
+  inv_cs = (float)(2.0 / rcut);
+  FNETG_CUDA(ctx->d_cgrid.ensure(sizeof(int4) * std::max(S, 1)));
+  FNETG_CUDA(ctx->d_cnum.ensure(sizeof(int64_t) * std::max(S, 1)));
+  FNETG_CUDA(ctx->d_coff.ensure(sizeof(int64_t) * (S + 1)));
+  if (S == 0) return FNETG_OK;
+  {
+    LaunchScope ls(ctx, "neighbors");
+    cell_grid_kernel<<<ceil_div(S, 128), 128, 0, ctx->stream>>>(
+        ctx->d_bbox.as<float>(), ctx->d_off.as<int64_t>(), S, inv_cs, ctx->d_cgrid.as<int4>(),
+        ctx->d_cnum.as<int64_t>());
+    FNETG_CUDA(cudaGetLastError());
+  }
+  int rc = exclusive_scan_i64(ctx, ctx->d_cnum.as<int64_t>(), ctx->d_coff.as<int64_t>(), S);
+  if (rc) return rc;
+  int64_t ncells = 0;
+  FNETG_CUDA(copy_sync(ctx, &ncells, ctx->d_coff.as<int64_t>() + S, sizeof(int64_t),
+                        cudaMemcpyDeviceToHost));
+  FNETG_CUDA(ctx->d_ccount.ensure(sizeof(int64_t) * std::max<int64_t>(ncells, 1)));
+  FNETG_CUDA(ctx->d_cstart.ensure(sizeof(int64_t) * (ncells + 1)));
+  FNETG_CUDA(ctx->d_cfill.ensure(sizeof(int64_t) * std::max<int64_t>(ncells, 1)));
+  FNETG_CUDA(ctx->d_akey.ensure(sizeof(int64_t) * std::max<int64_t>(N, 1)));
+  FNETG_CUDA(ctx->d_catom.ensure(sizeof(int32_t) * std::max<int64_t>(N, 1)));
+  if (ncells == 0 || N == 0) {
+    ctx->ncells = 0;
+    return FNETG_OK;
+  }
+  FNETG_CUDA(cudaMemsetAsync(ctx->d_ccount.p, 0, sizeof(int64_t) * ncells, ctx->stream));
+  FNETG_CUDA(cudaMemsetAsync(ctx->d_cfill.p, 0, sizeof(int64_t) * ncells, ctx->stream));
+  {
+    LaunchScope ls(ctx, "neighbors");
+    cell_count_kernel<<<ceil_div(N, 256), 256, 0, ctx->stream>>>(
+        ctx->d_coordsf.as<V4<float>>(), ctx->d_atom_struct.as<int32_t>(), N,
+        ctx->d_cgrid.as<int4>(), ctx->d_coff.as<int64_t>(), inv_cs, ctx->d_akey.as<int64_t>(),
+        ctx->d_ccount.as<int64_t>());
+    FNETG_CUDA(cudaGetLastError());
+  }
+  rc = exclusive_scan_i64(ctx, ctx->d_ccount.as<int64_t>(), ctx->d_cstart.as<int64_t>(), ncells);
+  if (rc) return rc;
+  {
+    LaunchScope ls(ctx, "neighbors");
+    cell_fill_kernel<<<ceil_div(N, 256), 256, 0, ctx->stream>>>(
+        ctx->d_akey.as<int64_t>(), ctx->d_atom_struct.as<int32_t>(), ctx->d_off.as<int64_t>(), N,
+        ctx->d_cstart.as<int64_t>(), ctx->d_cfill.as<int64_t>(), ctx->d_catom.as<int32_t>());
+    FNETG_CUDA(cudaGetLastError());
+  }
+  ctx->ncells = ncells;
+  return FNETG_OK;
+}
 
 int prepare_coords(fnetg_ctx *ctx) {
   if (ctx->S == 0) return FNETG_OK;
@@ -589,6 +801,18 @@ int run_neighbors(fnetg_ctx *ctx, double rcut) {
   a.exact_geometry = ctx->prec == FNETG_FP64 ? 1 : 0;
   a.count = ctx->d_pcount.as<int64_t>();
   a.maxp = ctx->d_maxp.as<int>();
+  // cell lists (the candidate boxes reach past the float pre-filter's outer bound)
+  {
+    float inv_cs = 0.f;
+    int rc = build_cells(ctx, rcut, inv_cs);
+    if (rc) return rc;
+    a.cgrid = ctx->ncells > 0 ? ctx->d_cgrid.as<int4>() : nullptr;
+    a.coff = ctx->d_coff.as<int64_t>();
+    a.cstart = ctx->d_cstart.as<int64_t>();
+    a.catom = ctx->d_catom.as<int32_t>();
+    a.inv_cs = inv_cs;
+    a.rbox = (float)(std::sqrt((double)a.rc2_hi) * (1.0 + 1e-5) + 1e-5);
+  }
   const int threads = kNbWarps * 32, wpb = kNbWarps;
   const int blocks = std::max(1, ceil_div(N, wpb));
   const size_t es = ctx->prec == FNETG_FP64 ? 8 : 4;

@@ -55,10 +55,24 @@ struct LossArgs {
   double *part;           // [S][2] loss numerator / denominator per structure
 };
 
-// one warp per structure
-__global__ void loss_kernel(LossArgs a) {
-  const int lane = threadIdx.x & 31;
-  const int s = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+// one CTA of kLossThreads per structure: the structure's atoms strided over the threads, sums
+// by warp shuffles and a shared-memory combine (large structures no longer serialise a warp)
+constexpr int kLossThreads = 128;
+
+__device__ __forceinline__ double cta_sum(double v, double *sh) {
+#pragma unroll
+  for (int k = 16; k > 0; k >>= 1) v += __shfl_xor_sync(0xffffffffu, v, k);
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
+  __syncthreads();
+  double t = 0.0;
+  for (int w = 0; w < kLossThreads / 32; w++) t += sh[w];
+  return t;
+}
+
+__global__ void __launch_bounds__(kLossThreads) loss_cta_kernel(LossArgs a) {
+  __shared__ double sh[kLossThreads / 32];
+  const int s = blockIdx.x;
   if (s >= a.S) return;
   const int64_t a0 = a.off[s], a1 = a.off[s + 1];
   const int n = (int)(a1 - a0);
@@ -68,13 +82,12 @@ __global__ void loss_kernel(LossArgs a) {
     double lsum = 0.0;
     for (int o = 0; o < a.ngt; o++) {
       double sum = 0.0;
-      for (int64_t at = a0 + lane; at < a1; at += 32) sum += a.out[at * a.nout + o];
-#pragma unroll
-      for (int k = 16; k > 0; k >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, k);
+      for (int64_t at = a0 + threadIdx.x; at < a1; at += kLossThreads) sum += a.out[at * a.nout + o];
+      sum = cta_sum(sum, sh);
       const double t = a.gt[(int64_t)s * a.ngt + o];
       const double lg = lossgrad(a.loss, sum, t);
       lsum += loss_term(a.loss, sum, t);
-      for (int64_t at = a0 + lane; at < a1; at += 32)
+      for (int64_t at = a0 + threadIdx.x; at < a1; at += kLossThreads)
         a.delta[at * a.nout + o] = lg * a.aw[at] / (double)n * ws;
     }
     num += ws * a.saw[s] * loss_finish(a.loss, lsum, a.ngt);
@@ -82,7 +95,7 @@ __global__ void loss_kernel(LossArgs a) {
   }
   if (a.nat > 0) {
     double ln = 0.0, ld = 0.0;
-    for (int64_t at = a0 + lane; at < a1; at += 32) {
+    for (int64_t at = a0 + threadIdx.x; at < a1; at += kLossThreads) {
       double lsum = 0.0;
       for (int t = 0; t < a.nat; t++) {
         const double p = a.out[at * a.nout + a.ngt + t];
@@ -93,15 +106,10 @@ __global__ void loss_kernel(LossArgs a) {
       ln += ws * a.aw[at] * loss_finish(a.loss, lsum, a.nat);
       ld += ws * a.aw[at];
     }
-#pragma unroll
-    for (int k = 16; k > 0; k >>= 1) {
-      ln += __shfl_xor_sync(0xffffffffu, ln, k);
-      ld += __shfl_xor_sync(0xffffffffu, ld, k);
-    }
-    num += ln;
-    den += ld;
+    num += cta_sum(ln, sh);
+    den += cta_sum(ld, sh);
   }
-  if (lane == 0) {
+  if (threadIdx.x == 0) {
     a.part[2 * s] = num;
     a.part[2 * s + 1] = den;
   }
@@ -683,6 +691,7 @@ __global__ void lbfgs_reset_kernel(double *state, size_t stride, const double *p
 
 int run_train_gradients(fnetg_ctx *ctx, int loss, const int32_t *order, bool need_predict) {
   (void)order;  // only the accumulation order changes with the reference's shuffle
+  if (ctx->batch_train) return run_batch_gradients(ctx, loss);      // tensor-core passes
   if (ctx->fl_weight > 0.0) return run_force_gradients(ctx, loss);  // energy + force loss
   const int64_t N = ctx->N;
   const int S = ctx->S;
@@ -712,7 +721,7 @@ int run_train_gradients(fnetg_ctx *ctx, int loss, const int32_t *order, bool nee
   a.part = ctx->d_losspart.as<double>();
   if (S > 0) {
     LaunchScope ls(ctx, "loss");
-    loss_kernel<<<ceil_div(S, 8), 256, 0, ctx->stream>>>(a);
+    loss_cta_kernel<<<S, kLossThreads, 0, ctx->stream>>>(a);
     FNETG_CUDA(cudaGetLastError());
   }
   {
@@ -727,6 +736,11 @@ int run_train_gradients(fnetg_ctx *ctx, int loss, const int32_t *order, bool nee
 // The loss kernel over structures [s0, s0 + count) only (a mini-batch): their atoms' scaled
 // output gradients and their per-structure loss parts.
 int launch_loss_range(fnetg_ctx *ctx, int s0, int count, int loss) {
+  // the buffers every loss evaluation writes (no-ops once sized, as during graph capture)
+  FNETG_CUDA(ctx->d_lossgrad.ensure(sizeof(double) * std::max<int64_t>(ctx->N, 1) *
+                                    ctx->dims.back()));
+  FNETG_CUDA(ctx->d_losspart.ensure(sizeof(double) * 2 * std::max(ctx->S, 1)));
+  FNETG_CUDA(ctx->d_scalars.ensure(sizeof(double) * 16));
   if (count <= 0) return FNETG_OK;
   LossArgs a{};
   a.S = count;
@@ -744,13 +758,15 @@ int launch_loss_range(fnetg_ctx *ctx, int s0, int count, int loss) {
   a.delta = ctx->d_lossgrad.as<double>();
   a.part = ctx->d_losspart.as<double>() + 2 * (int64_t)s0;
   LaunchScope ls(ctx, "loss");
-  loss_kernel<<<ceil_div(count, 8), 256, 0, ctx->stream>>>(a);
+  loss_cta_kernel<<<count, kLossThreads, 0, ctx->stream>>>(a);
   FNETG_CUDA(cudaGetLastError());
   return FNETG_OK;
 }
 
 // dataset loss from the per-structure parts of every structure
 int launch_loss_reduce(fnetg_ctx *ctx) {
+  FNETG_CUDA(ctx->d_losspart.ensure(sizeof(double) * 2 * std::max(ctx->S, 1)));
+  FNETG_CUDA(ctx->d_scalars.ensure(sizeof(double) * 16));
   LaunchScope ls(ctx, "loss");
   loss_reduce_kernel<<<1, 1024, 0, ctx->stream>>>(ctx->d_losspart.as<double>(), ctx->S,
                                                    ctx->d_scalars.as<double>());

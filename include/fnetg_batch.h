@@ -52,6 +52,14 @@ int fnetg_batch_epoch(fnetg_ctx *ctx, int32_t loss, double learning_rate, double
  * outputs atomic_out[Ntot] and per-structure sums global_out[S] (atom order).  Either may be
  * NULL (results stay on the device). */
 int fnetg_batch_predict(fnetg_ctx *ctx, double *atomic_out, double *global_out);
+/* on != 0: fnetg_train_gradients and fnetg_train_iteration (the full-batch L-BFGS / SD loop of
+ * TBpnn_nTrain, bpnn.F90:293-363) take their gradients from the tensor-core kernels over every
+ * tile of the mini-batch plan: forward, reverse pass and weight gradients in BF16 with FP32
+ * accumulation, FP64 sums, parameters and optimiser state.  With a force term
+ * (fnetg_set_force_targets) the input Jacobian also comes from the tensor cores, while the
+ * analytical forces and the dG/dR contraction stay FP32 (FP32 context required).  This is
+ * the precision form; on = 0 returns to the plain kernels. */
+int fnetg_batch_train_bf16(fnetg_ctx *ctx, int32_t on);
 /* After epochs: refresh the plain form's compute copy of the parameters (and the BF16 images)
  * from the FP64 master, so fnetg_predict / fnetg_forces use the trained parameters. */
 int fnetg_batch_sync_params(fnetg_ctx *ctx);

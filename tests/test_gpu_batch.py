@@ -189,3 +189,46 @@ def test_batch_epochs_lower_the_loss_and_sync_to_the_plain_form():
     e_ref = np.add.reduceat(ref, ds.atom_offsets[:-1])
     assert np.max(np.abs(e_plain[:, 0] - e_ref) / np.abs(e_ref)) <= 1e-5
     assert np.max(np.abs(e_tc[:, 0] - e_ref) / np.abs(e_ref)) <= 5e-2
+
+
+@pytest.mark.parametrize("force_weight", [0.0, 0.1])
+def test_tensor_core_training_gradients_match_fp64(force_weight):
+    """The precision form's full-batch gradient (fnetg_batch_train_bf16): BF16 tensor-core
+    forward, input Jacobian and reverse passes, FP32 forces and dG/dR contraction, FP64 sums;
+    against the FP64 plain kernels' gradient of the same loss (energies, or energies + 0.1 x
+    force MSE), norm-wise within 5e-2 per sub-network; then L-BFGS iterations on it lower the
+    loss."""
+    cfg = synthetic.CONFIGS["C4"]
+    ds = synthetic.generate(cfg, nstruct=10, forces=True)
+    funcs = synthetic.gfunctions(cfg)
+    dims = synthetic.network_dims(cfg)
+    params = random_params(dims, 3, seed=4)
+    zprec = O.zscore_stats(O.acsf(ds, funcs), ds)
+
+    def ctx_for(prec):
+        c = api.Context(prec)
+        c.upload(ds)
+        c.set_species(ds.species)
+        c.set_gfunctions(funcs)
+        c.acsf(download=False)
+        c.zscore(zprec=zprec)
+        c.set_network(dims, "tanh", params)
+        c.set_targets(ds)
+        if force_weight > 0:
+            c.set_force_targets(force_weight, ds.meta["forces"])
+        return c
+
+    with ctx_for(api.FP64) as c:
+        g64, l64, _ = c.train_gradients("mse")
+    with ctx_for(api.FP32) as c:
+        c.batch_setup(4)
+        c.batch_train_bf16(True)
+        g16, l16, _ = c.train_gradients("mse")
+        c.optimizer_init("lbfgs", 1e-20, 1e-6, 1e4, memory=100, linemin=True)
+        hist = [c.train_iteration("mse")[0] for _ in range(8)]
+    err = max(float(np.linalg.norm(g16[s] - g64[s]) / np.linalg.norm(g64[s])) for s in range(3))
+    print(f"C4 BF16 gradient (force weight {force_weight}) vs FP64: norm-wise {err:.2e}, loss "
+          f"{abs(l16 - l64) / l64:.2e}; L-BFGS losses {['%.3e' % h for h in hist]}")
+    assert err <= 5e-2
+    assert abs(l16 - l64) <= 2e-2 * l64
+    assert hist[-1] < hist[0]

@@ -102,6 +102,18 @@ def test_neighbor_pairs_bit_exact_synthetic_c2():
 
 
 @pytest.mark.parametrize("precision", [api.FP32, api.FP64])
+def test_neighbor_pairs_bit_exact_c3_cell_lists(precision):
+    """C3's structures of 96-2,048 atoms take the cell-list search (cells of half the cutoff,
+    accepted atoms emitted in the iterator's cyclic order); the smaller ones, down to cells below
+    the cutoff, scan every atom.  Pair sets, order, images and distances equal the oracle's."""
+    ds = synthetic.generate("C3", nstruct=30)
+    n = np.diff(ds.atom_offsets)
+    assert n.max() >= 1000 and (n < 96).any() and (n >= 96).sum() >= 5
+    rc = synthetic.CONFIGS["C3"].rcut / 0.529177249
+    assert check_neighbors(ds, rc, precision) > 100000
+
+
+@pytest.mark.parametrize("precision", [api.FP32, api.FP64])
 def test_neighbor_rebuilds_slab_and_overflow(precision):
     """A rebuild of the same dataset finds, counts and stores pairs in one slab pass; a denser
     geometry overflows the per-atom capacity and falls back to the counted build.  Pair sets
@@ -230,9 +242,12 @@ def normwise(x, ref):
 
 
 def test_golden_prediction_fp32_tolerances():
-    """FP32 plain form on every golden prediction case, per structure: each structure's summed
-    outputs within 1e-5 of the golden value (relative, per output), and each structure's
-    analytical forces within 1e-4 of its largest golden force component."""
+    """FP32 plain form on every golden prediction case, per structure and output: the summed
+    outputs within 1e-5 of the larger of the golden sum and the sum of the golden atomic
+    output magnitudes (some trained outputs sum to ~1e-6 from terms of ~0.2, where a relative
+    error of the sum means nothing), and each structure's analytical forces within 1e-4 of its
+    largest golden force component; norm-wise over each case, 1e-5 (energies) and 1e-4
+    (forces)."""
     worst_e, worst_f = 0.0, 0.0
     for name in GOLDEN_PRED:
         case = G.load_case(name)
@@ -242,17 +257,20 @@ def test_golden_prediction_fp32_tolerances():
         off = ds.atom_offsets
         e = np.add.reduceat(pred, off[:-1], axis=0)
         er = np.add.reduceat(ref, off[:-1], axis=0)
-        e_err = float(np.max(np.abs(e - er) / np.abs(er)))
+        mag = np.add.reduceat(np.abs(ref), off[:-1], axis=0)
+        e_err = float(np.max(np.abs(e - er) / np.maximum(np.abs(er), mag)))
         worst_e = max(worst_e, e_err)
         assert e_err <= 1e-5, (name, e_err)
+        assert normwise(e, er) < 1e-5, name
         # finite differences divide the FP32 rounding of the energies by 2 delta: their force
         # tolerance does not apply to the FP32 form (the FP64 test checks them)
         if forces is not None and case.settings.get("forces") == "analytical":
             f = forces.reshape(forces.shape[0], -1)
             fr = case.arrays["out_forces"]
+            assert normwise(f, fr) < 1e-4, name
             for s in range(ds.nstruct):
                 fs, frs = f[off[s]:off[s + 1]], fr[off[s]:off[s + 1]]
-                f_err = float(np.max(np.abs(fs - frs)) / np.max(np.abs(frs)))
+                f_err = float(np.max(np.abs(fs - frs)) / (np.max(np.abs(frs)) or np.abs(fr).max()))
                 worst_f = max(worst_f, f_err)
                 assert f_err <= 1e-4, (name, s, f_err)
     print(f"golden FP32 per structure: energy {worst_e:.2e}, forces {worst_f:.2e}")
