@@ -395,17 +395,18 @@ def profiled_traffic(kernel, config, natoms):
 
 
 def c4_model(args):
-    """The C4 model of the serving stream: 66-64-64-1 tanh networks trained from the
-    reference's initial parameters (RANLUX normalXavier) with the precision form's loss,
-    energies + 0.1 x force MSE against Morse targets, by L-BFGS on a C4 training sample.
-    Returns the parameters, the training sample's z-score statistics and the training record."""
+    """The C4 model of the serving stream: 66-64-64-1 tanh networks trained with the precision
+    form's loss, energies + 0.1 x force MSE against Morse targets, by L-BFGS on a C4 training
+    sample, from well-conditioned initial weights (N(0, 1/fan_in)); the reference's
+    normalXavier draw saturates the tanh units and stays saturated through training.  Returns
+    the parameters, the training sample's z-score statistics and the training record."""
     from fortnet_gb300 import api, synthetic
 
     cfg = synthetic.CONFIGS["C4"]
     ds = synthetic.generate(cfg, nstruct=args.model_structs, forces=True)
     funcs = synthetic.gfunctions(cfg)
     dims = synthetic.network_dims(cfg)
-    params = oracle_params(cfg, dims)
+    params = synthetic.normal_params(dims, len(cfg.atomic_numbers), cfg.seed)
     with api.Context(api.FP32) as c:
         c.upload(ds)
         c.set_species(ds.species)
@@ -424,7 +425,8 @@ def c4_model(args):
         last = c.last_losses()
         secs = time.perf_counter() - t0
         params = c.params()
-    rec = {"structures": ds.nstruct, "atoms": ds.ntot, "iterations": args.model_iters,
+    rec = {"init": "N(0, 1/fan_in) weights, N(0, 0.01) biases (seed 1004)",
+           "structures": ds.nstruct, "atoms": ds.ntot, "iterations": args.model_iters,
            "loss_energy": [float(f"{first[0]:.4g}"), float(f"{last[0]:.4g}")],
            "loss_forces": [float(f"{first[1]:.4g}"), float(f"{last[1]:.4g}")],
            "seconds": round(secs, 2)}
@@ -435,8 +437,10 @@ def precision_leg(args):
     """The precision form on C4 (5,000 structures of 100-500 atoms, three species, 66 features,
     66-64-64-1 tanh, cutoff 6.5 A): training iterations of the loss energies + 0.1 x force MSE
     (forward, analytical forces, dG/dR contraction, reverse pass with tangents, FP64 gradient
-    reduction, L-BFGS with FP64 state), FP32 kernels; atoms/s per iteration, and the FP32
-    results' errors against an FP64 run of the same kernels (energies, forces, gradient)."""
+    reduction, L-BFGS with FP64 state) with the network passes in FP32 SIMT kernels and on the
+    tensor cores (BF16 operands, FP32 accumulation); atoms/s per iteration, and the results'
+    errors against an FP64 run of the same kernels (energies, forces, gradient).  Initial
+    weights N(0, 1/fan_in) (the served C4 model's)."""
     from fortnet_gb300 import api, synthetic
     from fortnet_gb300.fnetdata import Dataset
 
@@ -444,38 +448,43 @@ def precision_leg(args):
     ds = synthetic.generate(cfg, nstruct=args.c4_structs, forces=True)
     funcs = synthetic.gfunctions(cfg)
     dims = synthetic.network_dims(cfg)
-    params = oracle_params(cfg, dims)
+    params = synthetic.normal_params(dims, len(cfg.atomic_numbers), cfg.seed)
     out = {"workload": f"C4: {ds.nstruct} structures, {ds.ntot} atoms, {dims[0]} features, net "
                        f"{'-'.join(map(str, dims))}, loss E + 0.1 F-MSE, L-BFGS"}
-    with api.Context(api.FP32) as c:
-        c.upload(ds)
-        c.set_species(ds.species)
-        c.set_gfunctions(funcs)
-        zprec = featurise(c, weights=ds.weights)
-        c.set_network(dims, "tanh", params)
-        c.set_targets(ds)
-        c.set_force_targets(0.1, ds.meta["forces"])
-        c.optimizer_init("lbfgs", 1e-20, 1e-6, 1e4, memory=1000, linemin=True)
-        for _ in range(2):
-            c.train_iteration("mse")
-        c.synchronize()
-        c.profile(True)
-        c.profile_reset()
-        t0 = time.perf_counter()
-        for _ in range(args.c4_iters):
-            c.train_iteration("mse")
-        c.synchronize()
-        dt = (time.perf_counter() - t0) / args.c4_iters
-        fams = ["mlp_forward", "mlp_jacobian", "forces", "features_jvp", "force_loss_backward",
-                "force_loss", "loss", "reduce", "optimizer", "params"]
-        prof = {f: c.profile_read(f) for f in fams}
-        c.profile(False)
-        params_now = c.params()
-        out.update({"atoms_per_s": round(ds.ntot / dt, 1), "ms_per_iteration": round(dt * 1e3, 3),
-                    "iterations": args.c4_iters,
-                    "kernels_ms_per_iteration": {f: round(v[0] / args.c4_iters, 4)
-                                                 for f, v in prof.items() if v[1]},
-                    "losses": dict(zip(("energy", "forces"), c.last_losses()))})
+    fams = ["mlp_forward", "mlp_jacobian", "forces", "features_jvp", "force_loss_backward",
+            "force_loss", "loss", "reduce", "optimizer", "params", "tc_jacobian", "tc_tangent",
+            "tc_reduce", "tc_pack"]
+    for form in ("plain_fp32", "bf16_tensor_cores"):
+        with api.Context(api.FP32) as c:
+            c.upload(ds)
+            c.set_species(ds.species)
+            c.set_gfunctions(funcs)
+            zprec = featurise(c, weights=ds.weights)
+            c.set_network(dims, "tanh", params)
+            c.set_targets(ds)
+            c.set_force_targets(0.1, ds.meta["forces"])
+            if form == "bf16_tensor_cores":
+                c.batch_setup(args.batch)
+                c.batch_train_bf16(True)
+            c.optimizer_init("lbfgs", 1e-20, 1e-6, 1e4, memory=1000, linemin=True)
+            for _ in range(2):
+                c.train_iteration("mse")
+            c.synchronize()
+            c.profile(True)
+            c.profile_reset()
+            t0 = time.perf_counter()
+            for _ in range(args.c4_iters):
+                c.train_iteration("mse")
+            c.synchronize()
+            dt = (time.perf_counter() - t0) / args.c4_iters
+            prof = {f: c.profile_read(f) for f in fams}
+            c.profile(False)
+            params_now = c.params()
+            out[form] = {"atoms_per_s": round(ds.ntot / dt, 1),
+                         "ms_per_iteration": round(dt * 1e3, 3), "iterations": args.c4_iters,
+                         "kernels_ms_per_iteration": {f: round(v[0] / args.c4_iters, 4)
+                                                      for f, v in prof.items() if v[1]},
+                         "losses": dict(zip(("energy", "forces"), c.last_losses()))}
     # FP32 against FP64 on the first structures, same parameters
     k = min(32, ds.nstruct)
     n = int(ds.atom_offsets[k])
@@ -507,7 +516,22 @@ def precision_leg(args):
                 for s in range(g64.shape[0]))
     out["errors_fp32_vs_fp64"] = {
         "structures": k, "energy_rel": float(f"{np.max(np.abs(e32 - e64) / np.abs(e64)):.3g}"),
-        "force_rel_of_max": float(f"{f_err:.3g}"), "gradient_rel": float(f"{g_err:.3g}")}
+        "force_rel_of_max": float(f"{f_err:.3g}"), "gradient_rel": float(f"{g_err:.3g}"),
+        "parameters": "after the timed tensor-core iterations"}
+    # the tensor-core gradient against the FP64 one at the same parameters
+    with api.Context(api.FP32) as c:
+        c.upload(sub)
+        c.set_species(sub.species)
+        c.set_gfunctions(funcs)
+        featurise(c, zprec=zprec)
+        c.set_network(dims, "tanh", params_now)
+        c.set_targets(sub)
+        c.set_force_targets(0.1, ds.meta["forces"][:n])
+        c.batch_setup(min(args.batch, k))
+        c.batch_train_bf16(True)
+        g16, _, _ = c.train_gradients("mse")
+    out["errors_bf16_vs_fp64"] = {
+        "structures": k, "gradient_rel": float(f"{max(float(np.linalg.norm(g16[s] - g64[s]) / np.linalg.norm(g64[s])) for s in range(g64.shape[0])):.3g}")}
     return out
 
 
@@ -726,7 +750,7 @@ def main():
     ap.add_argument("--serve-lanes", type=int, default=3)
     ap.add_argument("--model-structs", type=int, default=96,
                     help="C4 structures the served model is trained on")
-    ap.add_argument("--model-iters", type=int, default=150)
+    ap.add_argument("--model-iters", type=int, default=600)
     ap.add_argument("--c4-structs", type=int, default=5000)
     ap.add_argument("--c4-iters", type=int, default=3,
                     help="timed force-loss training iterations on C4 (0: skip the leg)")

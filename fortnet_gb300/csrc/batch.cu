@@ -61,10 +61,17 @@ struct TcNet {
   int nf, H1, H2;                    // real widths
   int K0p, K1p, K2p, nmt0;           // padded GEMM K of the three layers, M tiles of X^T delta
   uint32_t x_bytes;                  // one tile of packed features
-  uint32_t w_bytes;                  // one species' weight block
+  // one species' weight block: W0 | W1 forward | w2, b3 | W1 reverse | W0 reverse; the
+  // forward pass loads the first w_bytes0, training and the tangent pass w_bytes1, the
+  // Jacobian all w_bytes
+  uint32_t w_bytes, w_bytes0, w_bytes1;
   uint32_t off_w1f, off_w1b, off_w0b, off_w2;  // offsets inside the weight block
-  // shared-memory plan (bytes) of the forward / training / Jacobian kernels
-  uint32_t sm_x, sm_a1, sm_a2, sm_d2, sm_d1, sm_d3, sm_w, sm_total;
+  // shared-memory plan (bytes) of the training kernel (and of the Jacobian kernel, whose
+  // weights end at jm_total)
+  uint32_t sm_x, sm_a1, sm_a2, sm_d2, sm_d1, sm_d3, sm_w, sm_total, jm_total;
+  // shared-memory plan of the forward kernel: features, first activations, the weights it
+  // reads; small enough for two CTAs per SM
+  uint32_t fm_x, fm_a1, fm_w, fm_total;
   // shared-memory plan of the tangent (force-loss) kernel: features and their tangents,
   // activations and tangents of both hidden layers (exactly their K columns: the 128-wide
   // MN-major reads of a layer run on into the next buffer), adjoints, output adjoints, weights
@@ -87,10 +94,12 @@ template <int HP> TcNet make_net(fnetg_ctx *ctx) {
                  w1b = (uint32_t)HP * HP * 2, w0b = (uint32_t)n.K0p * HP * 2,
                  w2 = (uint32_t)(HP + 4) * 4;
   n.off_w1f = w0;
-  n.off_w1b = w0 + w1f;
-  n.off_w0b = w0 + w1f + w1b;
-  n.off_w2 = w0 + w1f + w1b + w0b;
-  n.w_bytes = (uint32_t)rup((int)(w0 + w1f + w1b + w0b + w2), 16);
+  n.off_w2 = w0 + w1f;
+  n.off_w1b = n.off_w2 + w2;
+  n.off_w0b = n.off_w1b + w1b;
+  n.w_bytes0 = n.off_w1b;  // multiples of 16: (HP + 4) * 4 and every image are
+  n.w_bytes1 = n.off_w0b;
+  n.w_bytes = n.off_w0b + w0b;
   uint32_t o = 0;
   n.sm_x = o;
   o += n.x_bytes;
@@ -105,8 +114,16 @@ template <int HP> TcNet make_net(fnetg_ctx *ctx) {
   n.sm_d3 = o;
   o += kRows * 16 * 2;
   n.sm_w = o;
-  o += n.w_bytes;
-  n.sm_total = o;
+  n.sm_total = o + n.w_bytes1;
+  n.jm_total = o + n.w_bytes;
+  o = 0;
+  n.fm_x = o;
+  o += n.x_bytes;
+  n.fm_a1 = o;  // exactly K1p columns: only the K-major reads of the second layer
+  o += kRows * n.K1p * 2;
+  n.fm_w = o;
+  o += n.w_bytes0;
+  n.fm_total = o;
   o = 0;
   n.tm_x = o;
   o += n.x_bytes;
@@ -129,7 +146,7 @@ template <int HP> TcNet make_net(fnetg_ctx *ctx) {
   n.tm_d3b = o;
   o += kRows * 16 * 2;
   n.tm_w = o;  // the weights close the plan: every over-read above lands inside it
-  o += n.w_bytes;
+  o += n.w_bytes1;
   n.tm_total = o;
   n.nparams = ctx->nparams;
   n.woff0 = ctx->woff[0];
@@ -285,15 +302,19 @@ __global__ void __launch_bounds__(kThreads, 1) tc_mlp_kernel(TcArgs a) {
   __shared__ uint32_t tmem_base;
   const TcNet &n = a.net;
   const int tid = threadIdx.x, warp = tid >> 5;
-  unsigned char *X = sm + n.sm_x, *A1 = sm + n.sm_a1, *A2 = sm + n.sm_a2, *D2 = sm + n.sm_d2,
-                *D1 = sm + n.sm_d1, *D3 = sm + n.sm_d3, *W = sm + n.sm_w;
+  // the forward pass uses its own compact plan (two CTAs per SM) and 64 TMEM columns
+  constexpr uint32_t kCols = MODE == 0 ? 64u : kTmemCols;
+  const uint32_t wload = MODE == 0 ? n.w_bytes0 : n.w_bytes1;
+  unsigned char *X = sm + (MODE == 0 ? n.fm_x : n.sm_x), *A1 = sm + (MODE == 0 ? n.fm_a1 : n.sm_a1),
+                *A2 = sm + n.sm_a2, *D2 = sm + n.sm_d2, *D1 = sm + n.sm_d1, *D3 = sm + n.sm_d3,
+                *W = sm + (MODE == 0 ? n.fm_w : n.sm_w);
   const float *w2 = reinterpret_cast<const float *>(W + n.off_w2);
   if (tid == 0) {
     tc::mbar_init(&mb_load, 1);
     tc::mbar_init(&mb_mma, 1);
     tc::mbar_fence_init();
   }
-  if (warp == 0) tc::tmem_alloc(&tmem_base, kTmemCols);
+  if (warp == 0) tc::tmem_alloc(&tmem_base, kCols);
   tc::fence_before_sync();
   __syncthreads();
   tc::fence_after_sync();
@@ -332,9 +353,9 @@ __global__ void __launch_bounds__(kThreads, 1) tc_mlp_kernel(TcArgs a) {
     tc::fence_before_sync();
     __syncthreads();
     if (tid == 0) {
-      tc::mbar_expect_tx(&mb_load, n.x_bytes + (new_sp ? n.w_bytes : 0u));
+      tc::mbar_expect_tx(&mb_load, n.x_bytes + (new_sp ? wload : 0u));
       tc::bulk_g2s(X, a.x + t * (int64_t)n.x_bytes, n.x_bytes, &mb_load);
-      if (new_sp) tc::bulk_g2s(W, a.w + (int64_t)sp * n.w_bytes, n.w_bytes, &mb_load);
+      if (new_sp) tc::bulk_g2s(W, a.w + (int64_t)sp * n.w_bytes, wload, &mb_load);
     }
     cur_sp = sp;
     const int row = tid;
@@ -478,7 +499,7 @@ __global__ void __launch_bounds__(kThreads, 1) tc_mlp_kernel(TcArgs a) {
   if (failed && tid == 0) atomicExch(a.err, 1);
   tc::fence_before_sync();
   __syncthreads();
-  if (warp == 0) tc::tmem_dealloc(tm, kTmemCols);
+  if (warp == 0) tc::tmem_dealloc(tm, kCols);
 }
 
 // CTA-uniform bounded wait that gives up the tile loop (a macro: it breaks the caller's loop)
@@ -710,10 +731,10 @@ __global__ void __launch_bounds__(kThreads, 1) tc_tan_kernel(TcArgs a) {
     tc::fence_before_sync();
     __syncthreads();
     if (tid == 0) {
-      tc::mbar_expect_tx(&mb_load, 2 * n.x_bytes + (new_sp ? n.w_bytes : 0u));
+      tc::mbar_expect_tx(&mb_load, 2 * n.x_bytes + (new_sp ? n.w_bytes1 : 0u));
       tc::bulk_g2s(X, a.x + t * (int64_t)n.x_bytes, n.x_bytes, &mb_load);
       tc::bulk_g2s(U, a.u + t * (int64_t)n.x_bytes, n.x_bytes, &mb_load);
-      if (new_sp) tc::bulk_g2s(W, a.w + (int64_t)sp * n.w_bytes, n.w_bytes, &mb_load);
+      if (new_sp) tc::bulk_g2s(W, a.w + (int64_t)sp * n.w_bytes, n.w_bytes1, &mb_load);
     }
     cur_sp = sp;
     const int row = tid;
@@ -972,42 +993,48 @@ __global__ void pack_w_kernel(const double *p64, TcNet n, unsigned char *w) {
 // block also records the largest |g| of its parameters (bmax[species][block]) for the update's
 // displacement limit.
 constexpr int kRedThreads = 256;
+constexpr int kRedSplit = 8;  // threads sharing one parameter's CTA loop
 
 __global__ void __launch_bounds__(kRedThreads) tc_reduce_kernel(const float *gpart,
                                                                 const int32_t *gflag, int nblk,
                                                                 int nsp, TcNet n, double *grad64,
                                                                 double *bmax) {
   __shared__ int flag[kMaxTcBlocks];
-  __shared__ double sh[kRedThreads];
+  __shared__ double part[kRedSplit][kRedThreads / kRedSplit];
+  __shared__ double sh[kRedThreads / kRedSplit];
   const int s = blockIdx.y;
   for (int b = threadIdx.x; b < nblk; b += blockDim.x) flag[b] = gflag[b * nsp + s];
   __syncthreads();
-  const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  // thread (r, k): parameter q = block * 32 + k, CTAs b = r, r + 8, ... (independent loads in
+  // flight across the eight threads); the eight partial sums combined in r order
+  constexpr int kq = kRedThreads / kRedSplit;
+  const int k = threadIdx.x % kq, r = threadIdx.x / kq;
+  const int64_t q = (int64_t)blockIdx.x * kq + k;
   double acc = 0.0;
   if (q < n.nparams && (q < n.woff3 || q >= n.boff1)) {
-    // four interleaved running sums, combined in a fixed order
-    double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
     const float *p = gpart + (int64_t)s * n.nparams + q;
     const int64_t stride = (int64_t)nsp * n.nparams;
-    int b = 0;
-    for (; b + 3 < nblk; b += 4) {
-      if (flag[b]) a0 += (double)p[b * stride];
-      if (flag[b + 1]) a1 += (double)p[(b + 1) * stride];
-      if (flag[b + 2]) a2 += (double)p[(b + 2) * stride];
-      if (flag[b + 3]) a3 += (double)p[(b + 3) * stride];
-    }
-    for (; b < nblk; b++)
-      if (flag[b]) a0 += (double)p[b * stride];
-    acc = (a0 + a1) + (a2 + a3);
+    for (int b = r; b < nblk; b += kRedSplit)
+      if (flag[b]) acc += (double)p[b * stride];
   }
-  if (q < n.nparams) grad64[(int64_t)s * n.nparams + q] = acc;
-  sh[threadIdx.x] = fabs(acc);
+  part[r][k] = acc;
   __syncthreads();
-  for (int o = kRedThreads / 2; o > 0; o >>= 1) {
-    if ((int)threadIdx.x < o) sh[threadIdx.x] = fmax(sh[threadIdx.x], sh[threadIdx.x + o]);
-    __syncthreads();
+  if (threadIdx.x < kq) {
+    double t = 0.0;
+#pragma unroll
+    for (int rr = 0; rr < kRedSplit; rr++) t += part[rr][threadIdx.x];
+    const int64_t qq = (int64_t)blockIdx.x * kq + threadIdx.x;
+    if (qq < n.nparams) grad64[(int64_t)s * n.nparams + qq] = t;
+    sh[threadIdx.x] = fabs(t);
   }
-  if (threadIdx.x == 0) bmax[(int64_t)s * gridDim.x + blockIdx.x] = sh[0];
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    double m = 0.0;
+    for (int t = threadIdx.x; t < kq; t += 32) m = fmax(m, sh[t]);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if (threadIdx.x == 0) bmax[(int64_t)s * gridDim.x + blockIdx.x] = m;
+  }
 }
 
 // Parameter q of a species -> its places in the species' weight images (the packing of
@@ -1143,10 +1170,11 @@ int launch_tc(fnetg_ctx *ctx, int mode, int64_t t0, int64_t t1, int grid) {
   grid = (int)std::max<int64_t>(1, std::min<int64_t>(grid, t1 - t0));
   void *k = tc_kernel_hp(b.HP, mode);
   if (mode == 0) ctx->out_fgen = ctx->out_pgen = -1;  // d_out now holds the BF16 forward
-  FNETG_CUDA(raise_smem_limit(k, b.net.sm_total));
+  const uint32_t smem = mode == 0 ? b.net.fm_total : b.net.sm_total;
+  FNETG_CUDA(raise_smem_limit(k, smem));
   void *args[] = {&a};
   LaunchScope ls(ctx, mode == 0 ? "tc_forward" : "tc_train");
-  FNETG_CUDA(cudaLaunchKernel(k, dim3(grid), dim3(kThreads), args, b.net.sm_total, ctx->stream));
+  FNETG_CUDA(cudaLaunchKernel(k, dim3(grid), dim3(kThreads), args, smem, ctx->stream));
   return FNETG_OK;
 }
 
@@ -1180,11 +1208,11 @@ int launch_tc_jac(fnetg_ctx *ctx, int64_t t0, int64_t t1, int grid) {
   a.ng = (int)ctx->gf.size();
   grid = (int)std::max<int64_t>(1, std::min<int64_t>(grid, t1 - t0));
   void *k = tc_jac_hp(b.HP);
-  FNETG_CUDA(raise_smem_limit(k, b.net.sm_total));
+  FNETG_CUDA(raise_smem_limit(k, b.net.jm_total));
   void *args[] = {&a};
   ctx->out_fgen = ctx->out_pgen = -1;
   LaunchScope ls(ctx, "tc_jacobian");
-  FNETG_CUDA(cudaLaunchKernel(k, dim3(grid), dim3(kThreads), args, b.net.sm_total, ctx->stream));
+  FNETG_CUDA(cudaLaunchKernel(k, dim3(grid), dim3(kThreads), args, b.net.jm_total, ctx->stream));
   return FNETG_OK;
 }
 
@@ -1205,7 +1233,7 @@ int launch_tc_tan(fnetg_ctx *ctx, int64_t t0, int64_t t1, int grid) {
 
 int launch_reduce(fnetg_ctx *ctx, int nblk) {
   BatchState &b = *ctx->batch;
-  dim3 grid(ceil_div(b.net.nparams, kRedThreads), ctx->nsp);
+  dim3 grid(ceil_div(b.net.nparams, kRedThreads / kRedSplit), ctx->nsp);
   LaunchScope ls(ctx, "tc_reduce");
   tc_reduce_kernel<<<grid, kRedThreads, 0, ctx->stream>>>(
       b.d_gpart.as<float>(), b.d_gflag.as<int32_t>(), nblk, ctx->nsp, b.net,
@@ -1248,7 +1276,7 @@ int batch_step(fnetg_ctx *ctx, int k, int loss, bool update, double lr, double m
   double *p64 = ctx->d_params64.as<double>();
   const double *g64 = ctx->d_grad64.as<double>();
   const double *bm = b.d_bmax.as<double>();
-  int nbm = (int)grid.x;
+  int nbm = ceil_div(b.net.nparams, kRedThreads / kRedSplit);
   TcNet net = b.net;
   double inv = 1.0 / b.sumw[k];
   unsigned char *wimg = b.d_w.as<unsigned char>();
@@ -1279,8 +1307,11 @@ int autotune(fnetg_ctx *ctx, int mode, int loss) {
     }
   }
   const int sms = num_sms();
+  // the forward kernel's plan fits two CTAs on an SM; the training kernel's one
+  const int gmax = mode == 0 ? 2 * sms : sms;
   std::vector<int> cand = {sms, sms / 2, sms / 4, (int)((tiles + 3) / 4), (int)((tiles + 5) / 6),
                            (int)((tiles + 7) / 8)};
+  if (mode == 0) cand.insert(cand.begin(), {2 * sms, (int)((tiles + 1) / 2)});
   int best = sms;
   float best_ms = 1e30f;
   if (mode == 1) {  // the reverse pass reads the forward's loss gradients
@@ -1290,7 +1321,7 @@ int autotune(fnetg_ctx *ctx, int mode, int loss) {
     if (rc) return rc;
   }
   for (int g : cand) {
-    if (g < 1 || g > sms) continue;
+    if (g < 1 || g > gmax) continue;
     float ms = 0.f;
     for (int rep = 0; rep < 3; rep++) {
       FNETG_CUDA(cudaEventRecord(ctx->ev0, ctx->stream));
@@ -1390,7 +1421,7 @@ int run_batch_gradients(fnetg_ctx *ctx, int loss) {
     rc = launch_tc_tan(ctx, 0, b.ntiles, grid);
     if (rc) return rc;
   } else {
-    rc = launch_tc(ctx, 0, 0, b.ntiles, grid);
+    rc = launch_tc(ctx, 0, 0, b.ntiles, 2 * num_sms());  // two forward CTAs fit on an SM
     if (rc) return rc;
     rc = launch_loss_range(ctx, 0, ctx->S, loss);
     if (rc) return rc;
@@ -1438,7 +1469,7 @@ int fnetg_batch_setup(fnetg_ctx *ctx, int32_t batch_structures) {
   b.plan_S = -1;
   b.HP = H <= 16 ? 16 : (H <= 32 ? 32 : 64);
   b.net = b.HP == 16 ? make_net<16>(ctx) : (b.HP == 32 ? make_net<32>(ctx) : make_net<64>(ctx));
-  FNETG_CHECK(b.net.sm_total <= 227 * 1024, FNETG_E_UNSUPPORTED,
+  FNETG_CHECK(b.net.jm_total <= 227 * 1024, FNETG_E_UNSUPPORTED,
               "batch_setup: tile buffers exceed shared memory");
   b.B = batch_structures;
   const int S = ctx->S;
@@ -1481,7 +1512,7 @@ int fnetg_batch_setup(fnetg_ctx *ctx, int32_t batch_structures) {
   FNETG_CUDA(b.d_gpart.ensure(sizeof(float) * (size_t)maxgrid * ctx->nsp * b.net.nparams));
   FNETG_CUDA(b.d_gflag.ensure(sizeof(int32_t) * (size_t)maxgrid * ctx->nsp));
   FNETG_CUDA(b.d_bmax.ensure(sizeof(double) * (size_t)ctx->nsp *
-                             ceil_div(b.net.nparams, kRedThreads)));
+                             ceil_div(b.net.nparams, kRedThreads / kRedSplit)));
   FNETG_CUDA(b.d_err.ensure(sizeof(int)));
   FNETG_CUDA(cudaMemsetAsync(b.d_err.p, 0, sizeof(int), ctx->stream));
   FNETG_CUDA(ctx->d_out.ensure(sizeof(double) * std::max<int64_t>(ctx->N, 1)));
@@ -1606,7 +1637,7 @@ int fnetg_batch_predict(fnetg_ctx *ctx, double *atomic_out, double *global_out) 
   BatchState &b = *ctx->batch;
   int rc = ensure_tuned(ctx, 0);
   if (rc) return rc;
-  rc = launch_tc(ctx, 0, 0, b.ntiles, num_sms());
+  rc = launch_tc(ctx, 0, 0, b.ntiles, 2 * num_sms());
   if (rc) return rc;
   if (global_out && ctx->S > 0) {
     FNETG_CUDA(ctx->d_gsum.ensure(sizeof(double) * ctx->S));

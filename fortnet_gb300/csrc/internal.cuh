@@ -215,7 +215,7 @@ struct fnetg_ctx {
   fnetg::DBuf d_pcount, d_poff, d_pend, d_pj, d_pmeta, d_rij, d_d2, d_scan_tmp, d_maxp, d_rcls2;
   // cell lists of the larger structures (rebuilt with every neighbour search)
   int64_t ncells = 0;
-  fnetg::DBuf d_cgrid, d_cnum, d_coff, d_ccount, d_cstart, d_cfill, d_akey, d_catom;
+  fnetg::DBuf d_cgrid, d_cnum, d_coff, d_ccount, d_cstart, d_cfill, d_akey, d_cpos;
 
   // features (bucketed rows, compute precision)
   int nf = 0;

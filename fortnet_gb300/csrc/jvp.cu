@@ -28,6 +28,7 @@ namespace {
 constexpr int kJvpWarps = 4;
 constexpr int kJvpCap = 256;  // pairs of one atom staged in shared memory
 constexpr int kJvpGroup = 16; // angular functions evaluated together (same lists and eta)
+constexpr int kJvpMaxXi = 4;  // integer xi of the shared-power path
 constexpr double kPi = 3.14159265358979323846;
 
 template <typename T> struct JvpArgs {
@@ -193,6 +194,24 @@ __global__ void __launch_bounds__(32 * kJvpWarps) jvp_kernel(JvpArgs<T> a) {
     T acc[kJvpGroup];
 #pragma unroll
     for (int f = 0; f < kJvpGroup; f++) acc[f] = (T)0;
+    // the group's functions in registers: lambda = +-1 with integer xi <= kJvpMaxXi take the
+    // powers of (1 +- cos) computed once per pair of neighbours
+    T lamf[kJvpGroup], xif[kJvpGroup];
+    int xin[kJvpGroup];
+    bool fast = true;
+#pragma unroll
+    for (int f = 0; f < kJvpGroup; f++) {
+      lamf[f] = (T)0;
+      xif[f] = (T)1;
+      xin[f] = 1;
+      if (f < fcount) {
+        const GDesc &g = a.ang[first + f];
+        lamf[f] = (T)g.lambda;
+        xif[f] = (T)g.xi;
+        xin[f] = g.xi_int;
+        fast = fast && g.xi_int >= 1 && g.xi_int <= kJvpMaxXi && (g.lambda == 1.0 || g.lambda == -1.0);
+      }
+    }
     for (int t = lane; t < n1 * n2; t += 32) {
       const int qj = L1[t / n2], qk = L2[t % n2];
       const V4<T> dj = D[qj], wj = Wd[qj], dk = D[qk], wk = Wd[qk];
@@ -207,21 +226,42 @@ __global__ void __launch_bounds__(32 * kJvpWarps) jvp_kernel(JvpArgs<T> a) {
              c * (wj.w / dj.w + wk.w / dk.w);
       }
       const T EE = Ej * Ek, dEE = Edj * Ek + Ej * Edk;
+      if (fast) {
+        T pp[kJvpMaxXi + 1], pm[kJvpMaxXi + 1];  // (1 + c)^m, (1 - c)^m
+        pp[0] = pm[0] = (T)1;
 #pragma unroll
-      for (int f = 0; f < kJvpGroup; f++) {
-        if (f >= fcount) break;
-        const GDesc &g = a.ang[first + f];
-        const T lam = (T)g.lambda, base = (T)1 + lam * c;
-        T p, pd;  // base^xi and xi base^(xi - 1)
-        if (g.xi_int > 0) {
-          const T b1 = ipow(base, g.xi_int - 1);
-          p = b1 * base;
-          pd = (T)g.xi * b1;
-        } else {
-          p = pow(base, (T)g.xi);
-          pd = base > (T)0 ? (T)g.xi * pow(base, (T)g.xi - (T)1) : (T)0;
+        for (int m = 1; m <= kJvpMaxXi; m++) {
+          pp[m] = pp[m - 1] * ((T)1 + c);
+          pm[m] = pm[m - 1] * ((T)1 - c);
         }
-        acc[f] += pd * lam * cd * EE + p * dEE;
+#pragma unroll
+        for (int f = 0; f < kJvpGroup; f++) {
+          if (f >= fcount) break;
+          T p = (T)0, b1 = (T)0;
+#pragma unroll
+          for (int m = 1; m <= kJvpMaxXi; m++)
+            if (m == xin[f]) {
+              p = lamf[f] > (T)0 ? pp[m] : pm[m];
+              b1 = lamf[f] > (T)0 ? pp[m - 1] : pm[m - 1];
+            }
+          acc[f] += xif[f] * b1 * lamf[f] * cd * EE + p * dEE;
+        }
+      } else {
+#pragma unroll
+        for (int f = 0; f < kJvpGroup; f++) {
+          if (f >= fcount) break;
+          const T lam = lamf[f], base = (T)1 + lam * c;
+          T p, pd;  // base^xi and xi base^(xi - 1)
+          if (xin[f] > 0) {
+            const T b1 = ipow(base, xin[f] - 1);
+            p = b1 * base;
+            pd = xif[f] * b1;
+          } else {
+            p = pow(base, xif[f]);
+            pd = base > (T)0 ? xif[f] * pow(base, xif[f] - (T)1) : (T)0;
+          }
+          acc[f] += pd * lam * cd * EE + p * dEE;
+        }
       }
     }
 #pragma unroll

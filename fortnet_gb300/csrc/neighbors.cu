@@ -58,7 +58,7 @@ struct NbArgs {
   const int4 *cgrid;
   const int64_t *coff;
   const int64_t *cstart;
-  const int32_t *catom;
+  const V4<float> *cpos;  // per cell slot: relative float position, w = structure-local index
   float inv_cs;   // 1 / cell edge (relative float frame)
   float rbox;     // half-width of a centre's candidate box, >= the float pre-filter's reach
 };
@@ -242,8 +242,7 @@ __global__ void __launch_bounds__(256, 4) nb_kernel(NbArgs a) {
       // candidates 64 at a time, two per lane: the shifted centre is formed once per image
       const float px = cif.x - ch.x, py = cif.y - ch.y, pz = cif.z - ch.z;
       // the reference's decision for structure-local atom jl of this image
-      auto decide = [&](int jl) -> bool {
-        const V4<float> cjf = a.cf[a0 + jl];
+      auto decide = [&](int jl, const V4<float> &cjf) -> bool {
         const float e0 = cjf.x - px, e1 = cjf.y - py, e2 = cjf.z - pz;
         const float df = e0 * e0 + e1 * e1 + e2 * e2;
         if (df <= a.rc2_lo) return true;
@@ -271,10 +270,18 @@ __global__ void __launch_bounds__(256, 4) nb_kernel(NbArgs a) {
         for (int c = lane; c < nx * ny * nz; c += 32) {
           const int cx = lo[0] + c / (ny * nz), cy = lo[1] + (c / nz) % ny, cz = lo[2] + c % nz;
           const int64_t key = cbase + ((int64_t)cx * cg.y + cy) * cg.z + cz;
-          for (int64_t q = a.cstart[key]; q < a.cstart[key + 1]; q++) {
-            const int jl = a.catom[q];
-            if (jl == il && img < im0) continue;  // the centre itself in the central cell
-            if (decide(jl)) atomicOr(&bits[jl >> 5], 1u << (jl & 31));
+          const int64_t q0 = a.cstart[key], q1 = a.cstart[key + 1];
+          // the cell's atoms are stored contiguously with their positions: two at a time, both
+          // loads issued before either test
+          for (int64_t q = q0; q < q1; q += 2) {
+            const V4<float> pa = a.cpos[q];
+            const bool two = q + 1 < q1;
+            const V4<float> pb = two ? a.cpos[q + 1] : pa;
+            const int ja = (int)__float_as_int(pa.w), jb = (int)__float_as_int(pb.w);
+            if (!(ja == il && img < im0) && decide(ja, pa))
+              atomicOr(&bits[ja >> 5], 1u << (ja & 31));
+            if (two && !(jb == il && img < im0) && decide(jb, pb))
+              atomicOr(&bits[jb >> 5], 1u << (jb & 31));
           }
         }
         __syncwarp();
@@ -563,14 +570,16 @@ __global__ void cell_count_kernel(const V4<float> *cf, const int32_t *astruct, i
 
 __global__ void cell_fill_kernel(const int64_t *akey, const int32_t *astruct, const int64_t *off,
                                  int64_t N, const int64_t *cstart, int64_t *cfill,
-                                 int32_t *catom) {
+                                 const V4<float> *cf, V4<float> *cpos) {
   const int64_t a = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (a >= N) return;
   const int64_t key = akey[a];
   if (key < 0) return;
   const int64_t pos =
       cstart[key] + (int64_t)atomicAdd(reinterpret_cast<unsigned long long *>(cfill + key), 1ull);
-  catom[pos] = (int32_t)(a - off[astruct[a]]);
+  V4<float> p = cf[a];
+  p.w = __int_as_float((int)(a - off[astruct[a]]));
+  cpos[pos] = p;
 }
 
 }  // namespace
@@ -601,7 +610,7 @@ int build_cells(fnetg_ctx *ctx, double rcut, float &inv_cs) {
   FNETG_CUDA(ctx->d_cstart.ensure(sizeof(int64_t) * (ncells + 1)));
   FNETG_CUDA(ctx->d_cfill.ensure(sizeof(int64_t) * std::max<int64_t>(ncells, 1)));
   FNETG_CUDA(ctx->d_akey.ensure(sizeof(int64_t) * std::max<int64_t>(N, 1)));
-  FNETG_CUDA(ctx->d_catom.ensure(sizeof(int32_t) * std::max<int64_t>(N, 1)));
+  FNETG_CUDA(ctx->d_cpos.ensure(sizeof(V4<float>) * std::max<int64_t>(N, 1)));
   if (ncells == 0 || N == 0) {
     ctx->ncells = 0;
     return FNETG_OK;
@@ -622,7 +631,8 @@ int build_cells(fnetg_ctx *ctx, double rcut, float &inv_cs) {
     LaunchScope ls(ctx, "neighbors");
     cell_fill_kernel<<<ceil_div(N, 256), 256, 0, ctx->stream>>>(
         ctx->d_akey.as<int64_t>(), ctx->d_atom_struct.as<int32_t>(), ctx->d_off.as<int64_t>(), N,
-        ctx->d_cstart.as<int64_t>(), ctx->d_cfill.as<int64_t>(), ctx->d_catom.as<int32_t>());
+        ctx->d_cstart.as<int64_t>(), ctx->d_cfill.as<int64_t>(), ctx->d_coordsf.as<V4<float>>(),
+        ctx->d_cpos.as<V4<float>>());
     FNETG_CUDA(cudaGetLastError());
   }
   ctx->ncells = ncells;
@@ -809,7 +819,7 @@ int run_neighbors(fnetg_ctx *ctx, double rcut) {
     a.cgrid = ctx->ncells > 0 ? ctx->d_cgrid.as<int4>() : nullptr;
     a.coff = ctx->d_coff.as<int64_t>();
     a.cstart = ctx->d_cstart.as<int64_t>();
-    a.catom = ctx->d_catom.as<int32_t>();
+    a.cpos = ctx->d_cpos.as<V4<float>>();
     a.inv_cs = inv_cs;
     a.rbox = (float)(std::sqrt((double)a.rc2_hi) * (1.0 + 1e-5) + 1e-5);
   }

@@ -112,6 +112,35 @@ def network_dims(cfg: Config):
     return [len(gfunctions(cfg))] + list(cfg.hidden) + [1]
 
 
+def param_layout(dims):
+    """Offsets of the reference's parameter order (network.F90:397-427): every layer's weight
+    matrix column-major (the output layer's ww(d_L, 1) included), then every layer's biases."""
+    woff, boff, ind = [], [], 0
+    for l in range(len(dims)):
+        woff.append(ind)
+        ind += dims[l] * (dims[l + 1] if l < len(dims) - 1 else 1)
+    for l in range(len(dims)):
+        boff.append(ind)
+        ind += dims[l]
+    return woff, boff, ind
+
+
+def normal_params(dims, nspecies, seed):
+    """Well-conditioned synthetic networks in the reference order: weights N(0, 1/fan_in),
+    biases N(0, 0.1^2), the unused entries (ww(d_L, 1), input-layer biases) zero.  Unlike the
+    reference's normalXavier draw (all weights positive Gaussian pdf values), these keep the
+    tanh units of z-scored inputs out of saturation."""
+    rng = np.random.default_rng(seed)
+    woff, boff, n = param_layout(dims)
+    p = np.zeros((nspecies, n))
+    for s in range(nspecies):
+        for l in range(len(dims) - 1):
+            k = dims[l] * dims[l + 1]
+            p[s, woff[l]:woff[l] + k] = rng.normal(0, 1 / np.sqrt(dims[l]), size=k)
+            p[s, boff[l + 1]:boff[l + 1] + dims[l + 1]] = rng.normal(0, 0.1, size=dims[l + 1])
+    return p
+
+
 def _natoms(cfg, rng, n):
     lo, hi = cfg.natoms
     if cfg.dist == "fixed":

@@ -31,29 +31,11 @@ def bf16(x):
 
 
 def layout(dims):
-    """Offsets of the reference parameter order (network.F90:397-427)."""
-    woff, boff, ind = [], [], 0
-    for l in range(len(dims)):
-        woff.append(ind)
-        ind += dims[l] * (dims[l + 1] if l < len(dims) - 1 else 1)
-    for l in range(len(dims)):
-        boff.append(ind)
-        ind += dims[l]
-    return woff, boff, ind
+    return synthetic.param_layout(dims)
 
 
 def random_params(dims, nsp, seed):
-    """Unsaturated random networks: weights N(0, 1/fan_in), biases N(0, 0.1^2); the unused
-    entries (output ww(d_L,1), input-layer biases) zero."""
-    rng = np.random.default_rng(seed)
-    woff, boff, n = layout(dims)
-    p = np.zeros((nsp, n))
-    for s in range(nsp):
-        for l in range(len(dims) - 1):
-            k = dims[l] * dims[l + 1]
-            p[s, woff[l]:woff[l] + k] = rng.normal(0, 1 / np.sqrt(dims[l]), size=k)
-            p[s, boff[l + 1]:boff[l + 1] + dims[l + 1]] = rng.normal(0, 0.1, size=dims[l + 1])
-    return p
+    return synthetic.normal_params(dims, nsp, seed)
 
 
 def unpack(p, dims):

@@ -91,33 +91,30 @@ def test_alone_mixed_and_context_agree(pool, precision):
             np.testing.assert_allclose(f, f_ref[a:b], rtol=0.0, atol=ftol * fscale)
 
 
-@pytest.mark.parametrize("precision,scale", [(api.FP64, 1.0), (api.FP64, 0.1), (api.FP32, 0.1)])
-def test_matches_oracle_on_small_requests(precision, scale):
+@pytest.mark.parametrize("precision,kind", [(api.FP64, "reference_init"), (api.FP64, "normal"),
+                                            (api.FP32, "normal")])
+def test_matches_oracle_on_small_requests(precision, kind):
     """Service against the FP64 oracle on small cells (L < rc: self images).
 
     FP64: energies to 1e-10 relative, forces to 1e-9 of the largest component.
-    FP32 (initial weights scaled by 0.1; unscaled, the reference's normalXavier draw
-    saturates the tanh units on z-scored inputs and makes forces ill-conditioned):
-    energies to 1e-5 of the summed magnitudes of the atomic outputs (the random network's
-    atomic outputs have mixed signs and their sums cancel by up to 15x), forces to 3e-4 of
-    the largest component.  These bounds are set by the model's conditioning, not by the
-    kernels: z-score deviations down to 1.6e-3 with mean/deviation ratios up to 7.7 turn the
-    FP32 rounding of the ACSF values (5e-6 in standardised units) into energy changes of
-    3.6e-5 of the sum and force changes of 8.4e-5 of the largest component when the oracle
-    alone is fed features perturbed that much; each feature's own force term is computed to
-    better than 1e-6 of its size."""
+    FP32, on a well-conditioned network (weights N(0, 1/fan_in), biases N(0, 0.01)): energies to
+    1e-5 relative, forces to 1e-4 of the largest component, the benchmark spec's numbers.  (The
+    reference's normalXavier draw, all weights positive, saturates the tanh units on z-scored
+    inputs; FP32 rounding of the ACSF values is then amplified past these bounds whatever the
+    kernels do, which the FP64 case with that draw covers instead.)"""
     cfg = synthetic.Config("small", 6, (16, 40), "uniform", C5.atomic_numbers, C5.ratios,
                            C5.rcut, C5.n_g2, C5.g2_eta, C5.g5, C5.hidden, 77)
     ds = synthetic.generate(cfg, targets=False)
     funcs, dims, params = model(11)
-    params = params * scale
+    if kind == "normal":
+        params = synthetic.normal_params(dims, len(C5.atomic_numbers), 11)
     vals = O.acsf(ds, funcs)
     zprec = O.zscore_stats(vals, ds)
     feats = O.zscore_apply(vals, zprec)
     atomic = O.predict(dims, "tanh", params, feats, ds.species)
     jac = O.jacobian(dims, "tanh", params, feats, ds.species)
     f_orc = O.forces(ds, funcs, zprec, jac, physical=True).reshape(ds.ntot, -1, 3)
-    e_tol, f_tol = (1e-10, 1e-9) if precision == api.FP64 else (1e-5, 3e-4)
+    e_tol, f_tol = (1e-10, 1e-9) if precision == api.FP64 else (1e-5, 1e-4)
     with api.Server(C5.atomic_numbers, funcs, zprec, dims, "tanh", params,
                     precision=precision, lanes=2) as srv:
         tickets = [srv.submit(an, xyz, lat) for an, xyz, lat in requests(ds)]
@@ -125,8 +122,7 @@ def test_matches_oracle_on_small_requests(precision, scale):
     for s in range(ds.nstruct):
         a, b = ds.atom_offsets[s], ds.atom_offsets[s + 1]
         e_orc = float(np.sum(atomic[a:b]))
-        e_scale = abs(e_orc) if precision == api.FP64 else float(np.sum(np.abs(atomic[a:b])))
-        assert abs(got[s][0][0] - e_orc) <= e_tol * e_scale
+        assert abs(got[s][0][0] - e_orc) <= e_tol * abs(e_orc)
         fmax = float(np.max(np.abs(f_orc[a:b])))
         assert np.max(np.abs(got[s][1] - f_orc[a:b])) <= f_tol * fmax + 1e-12
 
