@@ -366,10 +366,12 @@ def run_ours(args):
         "autotuned_ctas": {"forward": info["ctas_forward"], "train": info["ctas_train"]},
         "clocks": clk.summary(),
     }
-    if rank == 0 and (args.c4_iters > 0 or args.serve_requests > 0):
+    if rank == 0 and (args.c4_iters > 0 or args.serve_requests > 0 or not args.no_lbfgs):
         ctx.close()
     if args.c4_iters > 0 and rank == 0:
         out["precision_c4"] = precision_leg(args)
+    if not args.no_lbfgs and rank == 0:
+        out["lbfgs_full_history"] = lbfgs_leg(args)
     if args.serve_requests > 0 and rank == 0:
         out["serving"] = serving_leg(args)
     if not args.no_cpu_baseline and rank == 0 and world == 1:
@@ -532,6 +534,62 @@ def precision_leg(args):
         g16, _, _ = c.train_gradients("mse")
     out["errors_bf16_vs_fp64"] = {
         "structures": k, "gradient_rel": float(f"{max(float(np.linalg.norm(g16[s] - g64[s]) / np.linalg.norm(g64[s])) for s in range(g64.shape[0])):.3g}")}
+    return out
+
+
+def lbfgs_leg(args):
+    """L-BFGS at full history (memory 1000, the reference's default): the optimiser's cost per
+    iteration on the C3 networks (three sub-networks of 15,041 parameters) once every one of
+    the 1,000 history slots holds a pair, against its cost with 10 slots.  The iterations run
+    the full training step on a 64-structure C3 sample, without line search and with the
+    quasi-Newton step capped at the maximal displacement, so that every iteration adds a pair;
+    the optimiser's launches (gradient preparation, history update, inner products,
+    recursion, combination, step) are timed with CUDA events over 20 iterations."""
+    from fortnet_gb300 import api, synthetic
+
+    cfg = synthetic.CONFIGS["C3"]
+    ds = synthetic.generate(cfg, nstruct=64)
+    funcs = synthetic.gfunctions(cfg)
+    dims = synthetic.network_dims(cfg)
+    params = synthetic.normal_params(dims, len(cfg.atomic_numbers), cfg.seed)
+    out = {"memory": 1000, "parameters_per_species": None, "species": len(cfg.atomic_numbers)}
+    with api.Context(api.FP32) as c:
+        c.upload(ds)
+        c.set_species(ds.species)
+        c.set_gfunctions(funcs)
+        featurise(c, weights=ds.weights)
+        c.set_network(dims, "tanh", params)
+        c.set_targets(ds)
+        out["parameters_per_species"] = int(c.params().shape[1])
+        c.optimizer_init("lbfgs", 1e-30, 1e-6, 0.05, memory=1000, linemin=False,
+                         qn_max_disp=True)
+
+        def measure(iters=20):
+            c.synchronize()
+            c.profile(True)
+            c.profile_reset()
+            for _ in range(iters):
+                c.train_iteration("mse")
+            c.synchronize()
+            ms, n = c.profile_read("optimizer")
+            c.profile(False)
+            return round(ms / iters, 4)
+
+        for _ in range(10):
+            c.train_iteration("mse")
+        out["ms_per_iteration_10_slots"] = measure()
+        t0 = time.perf_counter()
+        filled = 30
+        while filled < 1000 + 30 and time.perf_counter() - t0 < 600:
+            for _ in range(100):
+                c.train_iteration("mse")
+            c.synchronize()
+            filled += 100
+        out["ms_per_iteration_1000_slots"] = measure()
+        out["iterations_before_timing"] = filled
+        out["slots_written"] = min(1000, filled)
+        out["fill_seconds"] = round(time.perf_counter() - t0, 2)
+        out["loss"] = float(f"{c.last_losses()[0]:.4g}")
     return out
 
 
@@ -743,6 +801,8 @@ def main():
     ap.add_argument("--cpu-max-atoms", type=int, default=128)
     ap.add_argument("--ref-sample", type=int, default=12)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-lbfgs", action="store_true",
+                    help="skip the L-BFGS full-history measurement")
     ap.add_argument("--serve-requests", type=int, default=20000,
                     help="requests of the C5 serving stream (0: skip the serving leg)")
     ap.add_argument("--serve-warmup", type=int, default=1000)

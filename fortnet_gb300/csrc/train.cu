@@ -215,17 +215,25 @@ __global__ void sd_kernel(double *params, const double *grad, int64_t np, SdStat
 // ---------------------------------------------------------------- L-BFGS + line minimiser
 // state layout per species (doubles): vectors xx, xold, gg, dir, x0, d0, dxt, qq (n each),
 // ss, yy (mem*n each), rho, alph (mem each), scalars (32)
+// ss, yy (mem*n each), rho, alph (mem each), scalars (32); then the inner products of the
+// L-BFGS direction (Gram form): sy[a][b] = s_a.y_b, syt[b][a] = s_a.y_b, yg[a][b] = y_a.y_b
+// (mem*mem each), ps[a] = s_a.g, py[a] = y_a.g, the direction's coefficients cs, cy (mem each)
+// and kLbSplit partial sums of the direction (n each)
 enum {
   SC_ITER = 0, SC_STATE, SC_IITER, SC_CONV, SC_XX0, SC_XX1, SC_DX0, SC_DX1, SC_XCUR, SC_MAXX,
-  SC_FIRST, SC_CONVERGED, SC_NS = 32
+  SC_FIRST, SC_CONVERGED, SC_PHASE, SC_NE, SC_USED, SC_GAMMA, SC_NS = 32
 };
+constexpr int kLbSplit = 8;         // slot groups of the direction's combination
+constexpr int kLbMaxMem = 8192;     // history slots the Gram-form recursion holds in shared memory
 
 struct LbView {
   double *xx, *xold, *gg, *dir, *x0, *d0, *dxt, *qq, *ss, *yy, *rho, *alph, *sc;
+  double *sy, *syt, *yg, *ps, *py, *cs, *cy, *part;
 };
 
 __host__ __device__ inline size_t lb_stride(int64_t n, int mem) {
-  return (size_t)8 * n + (size_t)2 * mem * n + (size_t)2 * mem + SC_NS;
+  return (size_t)8 * n + (size_t)2 * mem * n + (size_t)2 * mem + SC_NS +
+         (size_t)3 * mem * mem + (size_t)4 * mem + (size_t)kLbSplit * n;
 }
 
 __device__ LbView lb_view(double *base, int64_t n, int mem) {
@@ -243,7 +251,15 @@ __device__ LbView lb_view(double *base, int64_t n, int mem) {
   v.yy = p; p += (size_t)mem * n;
   v.rho = p; p += mem;
   v.alph = p; p += mem;
-  v.sc = p;
+  v.sc = p; p += SC_NS;
+  v.sy = p; p += (size_t)mem * mem;
+  v.syt = p; p += (size_t)mem * mem;
+  v.yg = p; p += (size_t)mem * mem;
+  v.ps = p; p += mem;
+  v.py = p; p += mem;
+  v.cs = p; p += mem;
+  v.cy = p; p += mem;
+  v.part = p;
   return v;
 }
 
@@ -273,20 +289,36 @@ __device__ void bcopy(double *dst, const double *src, int64_t n) {
   __syncthreads();
 }
 
-// TLbfgs_calcDirection (lbfgs.F90:387-488); slots never written hold zeros and are skipped
-// (they leave qq and dir bit-identical)
-__device__ void lb_direction(LbView &v, const LbParams &P, const double *xx, const double *g,
-                             double *sh) {
+// TLbfgs_calcDirection (lbfgs.F90:387-488) in Gram form.  The two-loop recursion
+//   loop 1 (newest to oldest): alpha_k = rho_k s_k.q,  q -= alpha_k y_k       (q = g at start)
+//   r = gamma q;  loop 2 (oldest to newest): beta_l = rho_l y_l.r,  r += (alpha_l - beta_l) s_l
+//   dir = -r
+// keeps q and r as combinations of g and the stored pairs, so every inner product it takes is
+// a combination of s_a.g, y_a.g, s_a.y_b and y_a.y_b.  Those are kept per slot pair and
+// refreshed for the newest slot only; both loops become triangular solves over scalars (the
+// serial chains of 2 x memory full-length dot products are gone), and dir is formed once as
+// -gamma g + sum_a cs_a s_a + cy_a y_a.  Same arithmetic in exact terms; rounding differs by
+// the order of the sums.  Slots never written are skipped (in the reference they have
+// rho = 0 and change nothing).
+//
+// Stage 1 (lbfgs_pre_kernel, one CTA per species): convergence, the line minimiser, and the
+// history update s_ne = x - x_old, y_ne = g - g_old.  SC_PHASE tells the later stages what
+// to do: 0 nothing (converged or inside a line search), 1 a Gram-form direction, 2 the first
+// direction -g.
+__device__ void lb_history(LbView &v, const LbParams &P, const double *xx, const double *g) {
   const int64_t n = P.n;
   const int mem = P.mem;
-  int iter = (int)v.sc[SC_ITER];
+  const int iter = (int)v.sc[SC_ITER];
   if (iter == 0) {
     for (int64_t q = threadIdx.x; q < n; q += blockDim.x) {
       v.gg[q] = g[q];
       v.dir[q] = -g[q];
     }
     __syncthreads();
-    if (threadIdx.x == 0) v.sc[SC_ITER] = 1;
+    if (threadIdx.x == 0) {
+      v.sc[SC_ITER] = 1;
+      v.sc[SC_PHASE] = 2;
+    }
     __syncthreads();
     return;
   }
@@ -295,51 +327,35 @@ __device__ void lb_direction(LbView &v, const LbParams &P, const double *xx, con
   for (int64_t q = threadIdx.x; q < n; q += blockDim.x) {
     s[q] = xx[q] - v.xold[q];
     y[q] = g[q] - v.gg[q];
-  }
-  __syncthreads();
-  const double beta = bdot(y, s, n, sh);
-  if (threadIdx.x == 0) v.rho[ne] = 1.0 / fmax(fabs(beta), kEps);
-  for (int64_t q = threadIdx.x; q < n; q += blockDim.x) {
     v.xold[q] = xx[q];
     v.gg[q] = g[q];
   }
   __syncthreads();
-  double diag;
-  if (iter == 1) {
-    diag = 1.0;
-  } else {
-    const double yy2 = bdot(y, y, n, sh);
-    diag = bdot(s, y, n, sh) / fmax(yy2, kEps);
+  if (threadIdx.x == 0) {
+    v.sc[SC_NE] = ne;
+    v.sc[SC_USED] = iter < mem ? iter : mem;
+    v.sc[SC_PHASE] = 1;
   }
-  const int used = iter < mem ? iter : mem;  // slots holding history
-  bcopy(v.qq, g, n);
-  for (int m = 0; m < mem; m++) {
-    const int ii = ((ne - m) % mem + mem) % mem;
-    if (m >= used) break;
-    const double al = v.rho[ii] * bdot(v.ss + (size_t)ii * n, v.qq, n, sh);
-    if (threadIdx.x == 0) v.alph[ii] = al;
-    for (int64_t q = threadIdx.x; q < n; q += blockDim.x) v.qq[q] = v.qq[q] - al * v.yy[(size_t)ii * n + q];
-    __syncthreads();
-  }
-  for (int64_t q = threadIdx.x; q < n; q += blockDim.x) v.dir[q] = diag * v.qq[q];
-  __syncthreads();
-  const int oldest = (ne + 1) % mem;
-  for (int m = 0; m < mem; m++) {
-    const int ii = (oldest + m) % mem;
-    // the reference visits every slot; unwritten slots (rho == 0) change nothing
-    const bool written = used >= mem || (ii <= ne && ii > ne - used);
-    if (!written) continue;
-    const double b = v.rho[ii] * bdot(v.yy + (size_t)ii * n, v.dir, n, sh);
-    const double al = v.alph[ii];
-    for (int64_t q = threadIdx.x; q < n; q += blockDim.x)
-      v.dir[q] = v.dir[q] + v.ss[(size_t)ii * n + q] * (al - b);
-    __syncthreads();
-  }
-  for (int64_t q = threadIdx.x; q < n; q += blockDim.x) v.dir[q] = -v.dir[q];
-  __syncthreads();
-  if (threadIdx.x == 0) v.sc[SC_ITER] = iter + 1;
   __syncthreads();
 }
+
+// Stage 2 (lbfgs_gram_kernel): the inner products that involve the newest pair or the new
+// gradient, for every written slot a: s_a.y_ne, y_a.y_ne, s_a.g, y_a.g.  kGramSlots slots per
+// CTA share the loads of y_ne and g.
+constexpr int kGramSlots = 4;
+constexpr int kGramThreads = 256;
+
+// Stage 3 (lbfgs_recur_kernel, one CTA per species): the two loops as blocked triangular
+// solves.  Loop-1 order k = 0..used-1 runs newest to oldest (slot ne - k), loop-2 order
+// l = 0..used-1 oldest to newest (slot ne - used + 1 + l).  Each block of 32 rows is solved by
+// one warp from a staged diagonal block; the rows below it are updated by all threads.
+constexpr int kRecThreads = 512;
+constexpr int kRecBlock = 32;
+
+// Stage 4 (lbfgs_combine_kernel): kLbSplit partial sums of sum_a cs_a s_a + cy_a y_a over
+// slot groups; stage 5 (lbfgs_post_kernel) adds them in a fixed order to -gamma g and runs the
+// line minimiser's reset / first step, or the plain step.
+constexpr int kCombThreads = 128;
 
 // TLineMin reset (linemin.F90:141-176)
 __device__ void lm_reset(LbView &v, const LbParams &P, const double *x0, const double *d0,
@@ -493,9 +509,10 @@ __device__ bool lm_next(LbView &v, const LbParams &P, double fu, const double *d
   return false;
 }
 
-// TLbfgs_next (lbfgs.F90:283-359); params holds xNew on exit
-__global__ void lbfgs_kernel(double *state, size_t stride, double *params, const double *grad,
-                             LbParams P, int *conv_flags) {
+// TLbfgs_next (lbfgs.F90:283-359) in five launches (stages above); params holds xNew once
+// stage 5 ran.
+__global__ void lbfgs_pre_kernel(double *state, size_t stride, double *params, const double *grad,
+                                 LbParams P, int *conv_flags) {
   __shared__ double sh[kOptThreads];
   const int s = blockIdx.x;
   LbView v = lb_view(state + (size_t)s * stride, P.n, P.mem);
@@ -503,6 +520,7 @@ __global__ void lbfgs_kernel(double *state, size_t stride, double *params, const
   double *xnew = params + (size_t)s * P.n;
   const int64_t n = P.n;
   const double fx = 0.0;  // the reference passes a loss value that the line minimiser only stores
+  if (threadIdx.x == 0) v.sc[SC_PHASE] = 0;
   const double gmax = bmaxabs(dx, n, sh);
   if (gmax < P.tol) {
     if (threadIdx.x == 0) conv_flags[s] = 1;
@@ -520,7 +538,229 @@ __global__ void lbfgs_kernel(double *state, size_t stride, double *params, const
       return;
     }
   }
-  lb_direction(v, P, v.xx, v.dxt, sh);
+  lb_history(v, P, v.xx, v.dxt);
+}
+
+__global__ void __launch_bounds__(kGramThreads) lbfgs_gram_kernel(double *state, size_t stride,
+                                                                  LbParams P) {
+  __shared__ double red[kGramThreads / 32][4 * kGramSlots];
+  LbView v = lb_view(state + (size_t)blockIdx.y * stride, P.n, P.mem);
+  if ((int)v.sc[SC_PHASE] != 1) return;
+  const int64_t n = P.n;
+  const int mem = P.mem;
+  const int ne = (int)v.sc[SC_NE], used = (int)v.sc[SC_USED];
+  const int k0 = blockIdx.x * kGramSlots;
+  if (k0 >= used) return;
+  const int nk = min(kGramSlots, used - k0);
+  int slot[kGramSlots];
+#pragma unroll
+  for (int i = 0; i < kGramSlots; i++) slot[i] = ((ne - (k0 + min(i, nk - 1))) % mem + mem) % mem;
+  const double *yn = v.yy + (size_t)ne * n, *g = v.dxt;
+  double acc[4 * kGramSlots];
+#pragma unroll
+  for (int i = 0; i < 4 * kGramSlots; i++) acc[i] = 0.0;
+  for (int64_t q = threadIdx.x; q < n; q += kGramThreads) {
+    const double a = yn[q], b = g[q];
+#pragma unroll
+    for (int i = 0; i < kGramSlots; i++) {
+      const double sv = v.ss[(size_t)slot[i] * n + q], yv = v.yy[(size_t)slot[i] * n + q];
+      acc[4 * i + 0] = fma(sv, a, acc[4 * i + 0]);
+      acc[4 * i + 1] = fma(yv, a, acc[4 * i + 1]);
+      acc[4 * i + 2] = fma(sv, b, acc[4 * i + 2]);
+      acc[4 * i + 3] = fma(yv, b, acc[4 * i + 3]);
+    }
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int i = 0; i < 4 * kGramSlots; i++) {
+    double t = acc[i];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+    if (lane == 0) red[warp][i] = t;
+  }
+  __syncthreads();
+  if (threadIdx.x < 4 * kGramSlots) {
+    const int i = threadIdx.x >> 2, c = threadIdx.x & 3;
+    if (i < nk) {
+      double t = 0.0;
+      for (int w = 0; w < kGramThreads / 32; w++) t += red[w][threadIdx.x];
+      const int sa = ((ne - (k0 + i)) % mem + mem) % mem;
+      if (c == 0) {
+        v.sy[(size_t)sa * mem + ne] = t;
+        v.syt[(size_t)ne * mem + sa] = t;
+        if (sa == ne) v.rho[ne] = 1.0 / fmax(fabs(t), kEps);
+      } else if (c == 1) {
+        v.yg[(size_t)sa * mem + ne] = t;
+        v.yg[(size_t)ne * mem + sa] = t;
+      } else if (c == 2) {
+        v.ps[sa] = t;
+      } else {
+        v.py[sa] = t;
+      }
+    }
+  }
+}
+
+__global__ void __launch_bounds__(kRecThreads) lbfgs_recur_kernel(double *state, size_t stride,
+                                                                  LbParams P) {
+  extern __shared__ double rs[];  // A[mem] (loop 1), C[mem] (loop 2), R[mem] (rho by k)
+  __shared__ double D[kRecBlock][kRecBlock];
+  __shared__ double s_gamma;
+  LbView v = lb_view(state + (size_t)blockIdx.x * stride, P.n, P.mem);
+  if ((int)v.sc[SC_PHASE] != 1) return;
+  const int mem = P.mem;
+  const int ne = (int)v.sc[SC_NE], used = (int)v.sc[SC_USED];
+  double *A = rs, *C = rs + mem, *R = rs + 2 * mem;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  // loop-1 order k -> slot; loop-2 order l is loop-1 order used - 1 - l
+  auto slot1 = [&](int k) { return ((ne - k) % mem + mem) % mem; };
+  for (int k = tid; k < used; k += kRecThreads) {
+    const int sk = slot1(k);
+    R[k] = v.rho[sk];
+    A[k] = v.ps[sk];
+  }
+  if (tid == 0) {
+    const int iter = (int)v.sc[SC_ITER];
+    s_gamma = iter == 1 ? 1.0
+                        : v.sy[(size_t)ne * mem + ne] / fmax(v.yg[(size_t)ne * mem + ne], kEps);
+  }
+  __syncthreads();
+  // ---- loop 1: A[k] = s_k.g - sum_{j<k} alpha_j s_k.y_j;  alpha_k = rho_k A[k]
+  for (int jb = 0; jb < used; jb += kRecBlock) {
+    const int nb = min(kRecBlock, used - jb);
+    for (int e = tid; e < kRecBlock * kRecBlock; e += kRecThreads) {
+      const int jj = e / kRecBlock, i = e % kRecBlock;
+      D[jj][i] = (jj < nb && i < nb && i > jj)
+                     ? v.syt[(size_t)slot1(jb + jj) * mem + slot1(jb + i)] : 0.0;
+    }
+    __syncthreads();
+    if (warp == 0) {
+      const int k = jb + lane;
+      const double rk = lane < nb ? R[k] : 0.0;
+      double b = lane < nb ? A[k] : 0.0;
+      for (int jj = 0; jj < nb; jj++) {
+        const double aj = __shfl_sync(0xffffffffu, rk * b, jj);  // row jj is final
+        if (lane > jj) b = fma(-aj, D[jj][lane], b);
+      }
+      if (lane < nb) A[k] = rk * b;  // alpha_k
+    }
+    __syncthreads();
+    for (int k = jb + nb + tid; k < used; k += kRecThreads) {
+      const int sk = slot1(k);
+      double acc = 0.0;
+#pragma unroll 8
+      for (int jj = 0; jj < nb; jj++)
+        acc = fma(A[jb + jj], v.syt[(size_t)slot1(jb + jj) * mem + sk], acc);
+      A[k] -= acc;
+    }
+    __syncthreads();
+  }
+  const double gamma = s_gamma;
+  // ---- r = gamma q: C[l] = gamma (y_l.g - sum_j alpha_j y_l.y_j)
+  for (int l = tid; l < used; l += kRecThreads) {
+    const int sl = slot1(used - 1 - l);
+    double acc = 0.0;
+#pragma unroll 4
+    for (int k = 0; k < used; k++) acc = fma(A[k], v.yg[(size_t)slot1(k) * mem + sl], acc);
+    C[l] = gamma * (v.py[sl] - acc);
+  }
+  __syncthreads();
+  // ---- loop 2: C[l] = y_l.r before step l; delta_l = alpha_l - rho_l C[l];
+  //      C[l'] += delta_l s_l.y_l' for the later rows l'
+  for (int jb = 0; jb < used; jb += kRecBlock) {
+    const int nb = min(kRecBlock, used - jb);
+    for (int e = tid; e < kRecBlock * kRecBlock; e += kRecThreads) {
+      const int jj = e / kRecBlock, i = e % kRecBlock;
+      D[jj][i] = (jj < nb && i < nb && i > jj)
+                     ? v.sy[(size_t)slot1(used - 1 - (jb + jj)) * mem + slot1(used - 1 - (jb + i))]
+                     : 0.0;
+    }
+    __syncthreads();
+    if (warp == 0) {
+      const int l = jb + lane;
+      const int k = used - 1 - l;
+      const double rl = lane < nb ? R[k] : 0.0, al = lane < nb ? A[k] : 0.0;
+      double c = lane < nb ? C[l] : 0.0;
+      for (int jj = 0; jj < nb; jj++) {
+        const double dj = __shfl_sync(0xffffffffu, al - rl * c, jj);  // row jj is final
+        if (lane > jj) c = fma(dj, D[jj][lane], c);
+      }
+      if (lane < nb) C[l] = al - rl * c;  // delta_l
+    }
+    __syncthreads();
+    for (int l = jb + nb + tid; l < used; l += kRecThreads) {
+      const int sl = slot1(used - 1 - l);
+      double acc = 0.0;
+#pragma unroll 8
+      for (int jj = 0; jj < nb; jj++)
+        acc = fma(C[jb + jj], v.sy[(size_t)slot1(used - 1 - (jb + jj)) * mem + sl], acc);
+      C[l] += acc;
+    }
+    __syncthreads();
+  }
+  // ---- dir = -r = -gamma g + gamma sum alpha_k y_k - sum delta_l s_l
+  for (int k = tid; k < used; k += kRecThreads) {
+    const int sk = slot1(k);
+    v.cy[sk] = gamma * A[k];
+    v.cs[sk] = -C[used - 1 - k];
+    v.alph[sk] = A[k];
+  }
+  if (tid == 0) v.sc[SC_GAMMA] = gamma;
+}
+
+__global__ void __launch_bounds__(kCombThreads) lbfgs_combine_kernel(double *state, size_t stride,
+                                                                     LbParams P) {
+  __shared__ double cf[2 * (kLbMaxMem / kLbSplit + 1)];
+  __shared__ int sl[kLbMaxMem / kLbSplit + 1];
+  LbView v = lb_view(state + (size_t)blockIdx.y * stride, P.n, P.mem);
+  if ((int)v.sc[SC_PHASE] != 1) return;
+  const int64_t n = P.n;
+  const int mem = P.mem;
+  const int ne = (int)v.sc[SC_NE], used = (int)v.sc[SC_USED];
+  const int z = blockIdx.z;
+  const int k0 = (int)((int64_t)used * z / kLbSplit), k1 = (int)((int64_t)used * (z + 1) / kLbSplit);
+  for (int k = k0 + threadIdx.x; k < k1; k += kCombThreads) {
+    const int sk = ((ne - k) % mem + mem) % mem;
+    sl[k - k0] = sk;
+    cf[2 * (k - k0)] = v.cs[sk];
+    cf[2 * (k - k0) + 1] = v.cy[sk];
+  }
+  __syncthreads();
+  const int64_t q = (int64_t)blockIdx.x * kCombThreads + threadIdx.x;
+  if (q >= n) return;
+  double acc = 0.0;
+#pragma unroll 4
+  for (int k = 0; k < k1 - k0; k++) {
+    const size_t o = (size_t)sl[k] * n + q;
+    acc = fma(cf[2 * k], v.ss[o], acc);
+    acc = fma(cf[2 * k + 1], v.yy[o], acc);
+  }
+  v.part[(size_t)z * n + q] = acc;
+}
+
+__global__ void lbfgs_post_kernel(double *state, size_t stride, double *params, const double *grad,
+                                  LbParams P) {
+  __shared__ double sh[kOptThreads];
+  const int s = blockIdx.x;
+  LbView v = lb_view(state + (size_t)s * stride, P.n, P.mem);
+  const int phase = (int)v.sc[SC_PHASE];
+  if (phase == 0) return;
+  const double *dx = grad + (size_t)s * P.n;
+  double *xnew = params + (size_t)s * P.n;
+  const int64_t n = P.n;
+  const double fx = 0.0;
+  if (phase == 1) {
+    const double gamma = v.sc[SC_GAMMA];
+    for (int64_t q = threadIdx.x; q < n; q += blockDim.x) {
+      double d = -gamma * v.dxt[q];
+#pragma unroll
+      for (int z = 0; z < kLbSplit; z++) d += v.part[(size_t)z * n + q];
+      v.dir[q] = d;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) v.sc[SC_ITER] = v.sc[SC_ITER] + 1;
+    __syncthreads();
+  }
   if (P.linesearch) {
     lm_reset(v, P, v.xx, v.dir, 1.0, sh);
     lm_next(v, P, fx, dx, v.xx, sh);
@@ -536,6 +776,7 @@ __global__ void lbfgs_kernel(double *state, size_t stride, double *params, const
     __syncthreads();
   }
   bcopy(xnew, v.xx, n);
+  if (threadIdx.x == 0) v.sc[SC_PHASE] = 0;
 }
 
 // ---------------------------------------------------------------- conjugate gradients
@@ -674,12 +915,11 @@ __global__ void fire_reset_kernel(double *state, size_t stride, int64_t n, doubl
   v.sc[SC_XX1] = 0.1 * dt_max;
 }
 
+// after the whole state block was zeroed
 __global__ void lbfgs_reset_kernel(double *state, size_t stride, const double *params,
                                    int64_t n, int mem) {
   const int s = blockIdx.x;
   double *base = state + (size_t)s * stride;
-  for (size_t q = threadIdx.x; q < stride; q += blockDim.x) base[q] = 0.0;
-  __syncthreads();
   LbView v = lb_view(base, n, mem);
   for (int64_t q = threadIdx.x; q < n; q += blockDim.x) {
     v.xx[q] = params[(size_t)s * n + q];
@@ -816,10 +1056,22 @@ int run_optimizer_step(fnetg_ctx *ctx) {
   } else {
     LbParams P{ctx->nparams, ctx->opt_mem, ctx->opt_threshold, ctx->opt_max_disp,
                ctx->opt_linemin, ctx->opt_qn ? ctx->opt_max_disp : -1.0, ctx->opt_threshold};
+    double *st = ctx->d_opt.as<double>();
+    const size_t stride = ctx->opt_stride;
+    const int mem = ctx->opt_mem;
+    const size_t rec_smem = sizeof(double) * 3 * (size_t)mem;
+    FNETG_CUDA(raise_smem_limit((const void *)lbfgs_recur_kernel, rec_smem));
     LaunchScope ls(ctx, "optimizer");
-    lbfgs_kernel<<<ctx->nsp, kOptThreads, 0, ctx->stream>>>(
-        ctx->d_opt.as<double>(), ctx->opt_stride, ctx->d_params64.as<double>(),
-        ctx->d_grad64.as<double>(), P, conv);
+    lbfgs_pre_kernel<<<ctx->nsp, kOptThreads, 0, ctx->stream>>>(
+        st, stride, ctx->d_params64.as<double>(), ctx->d_grad64.as<double>(), P, conv);
+    lbfgs_gram_kernel<<<dim3(ceil_div(mem, kGramSlots), ctx->nsp), kGramThreads, 0,
+                        ctx->stream>>>(st, stride, P);
+    lbfgs_recur_kernel<<<ctx->nsp, kRecThreads, rec_smem, ctx->stream>>>(st, stride, P);
+    lbfgs_combine_kernel<<<dim3((unsigned)ceil_div(ctx->nparams, (int64_t)kCombThreads),
+                                ctx->nsp, kLbSplit),
+                           kCombThreads, 0, ctx->stream>>>(st, stride, P);
+    lbfgs_post_kernel<<<ctx->nsp, kOptThreads, 0, ctx->stream>>>(
+        st, stride, ctx->d_params64.as<double>(), ctx->d_grad64.as<double>(), P);
   }
   FNETG_CUDA(cudaGetLastError());
   return run_params_to_compute(ctx);
@@ -854,8 +1106,12 @@ int fnetg_optimizer_init(fnetg_ctx *ctx, int32_t kind, double threshold, double 
   if (kind != FNETG_OPT_SD) {
     // L-BFGS, CG and FIRE keep their state in the L-BFGS block layout (mem = 1 for CG/FIRE)
     const int mem = kind == FNETG_OPT_LBFGS ? ctx->opt_mem : 1;
+    FNETG_CHECK(mem <= kLbMaxMem, FNETG_E_UNSUPPORTED,
+                "optimizer_init: L-BFGS memory above 8192 slots");
     ctx->opt_stride = lb_stride(ctx->nparams, mem);
     FNETG_CUDA(ctx->d_opt.ensure(sizeof(double) * ctx->opt_stride * ctx->nsp));
+    FNETG_CUDA(cudaMemsetAsync(ctx->d_opt.p, 0, sizeof(double) * ctx->opt_stride * ctx->nsp,
+                               ctx->stream));
     LaunchScope ls(ctx, "optimizer");
     lbfgs_reset_kernel<<<ctx->nsp, kOptThreads, 0, ctx->stream>>>(
         ctx->d_opt.as<double>(), ctx->opt_stride, ctx->d_params64.as<double>(), ctx->nparams,

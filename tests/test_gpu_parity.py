@@ -372,6 +372,51 @@ def test_c2_energies_fp32_within_1e5_of_fp64_oracle():
     assert normwise(glob, e_ref) < 1e-5
 
 
+@pytest.mark.parametrize("memory,linemin,niter", [(3, False, 24), (4, True, 40)])
+def test_lbfgs_history_wraps_like_the_oracle(memory, linemin, niter):
+    """L-BFGS past its memory: the history ring buffer is overwritten several times
+    (lbfgs.F90:387-488), every direction from the Gram-form recursion; parameters after each
+    iteration against the oracle's two-loop recursion (rounding differs in the order of the
+    sums only)."""
+    cfg = synthetic.CONFIGS["C1"]
+    ds = synthetic.generate(cfg, nstruct=12)
+    funcs = synthetic.gfunctions(cfg)
+    dims = synthetic.network_dims(cfg)
+    params0 = O.Ranlux(6).init_bpnn(dims, "tanh", 1)
+    vals = O.acsf(ds, funcs)
+    zprec = O.zscore_stats(vals, ds)
+    feats = O.zscore_apply(vals, zprec)
+    # without the line search the quasi-Newton step is capped at the maximal displacement
+    opt = O.Lbfgs(params0[0], 1e-30, 1e-6, 0.2, memory, linemin, not linemin)
+    params = params0.copy()
+    dd, _ = O.train_gradients(dims, "tanh", params, feats, ds)
+    ref_hist = []
+    for _ in range(niter):
+        g, _ = O.update_prepare(dims, "tanh", params, dd, 0.0, 0.0, float(ds.weights.sum()))
+        params = opt.next(0.0, g[0])[0][None, :]
+        dd, _ = O.train_gradients(dims, "tanh", params, feats, ds)
+        ref_hist.append(params.copy())
+    worst = 0.0
+    with api.Context(api.FP64) as ctx:
+        ctx.upload(ds)
+        ctx.set_species(ds.species)
+        ctx.set_gfunctions(funcs)
+        ctx.acsf(download=False)
+        ctx.zscore(zprec=zprec)
+        ctx.set_network(dims, "tanh", params0)
+        ctx.set_targets(ds)
+        ctx.optimizer_init("lbfgs", 1e-30, 1e-6, 0.2, memory=memory, linemin=linemin,
+                           qn_max_disp=not linemin)
+        for it in range(niter):
+            ctx.train_iteration("mse")
+            p = ctx.params()
+            worst = max(worst, float(np.max(np.abs(p - ref_hist[it]))
+                                     / np.max(np.abs(ref_hist[it] - params0))))
+            np.testing.assert_allclose(p, ref_hist[it], rtol=1e-7, atol=1e-9)
+    print(f"L-BFGS memory {memory}, line search {linemin}, {niter} iterations: worst parameter "
+          f"difference {worst:.2e} of the displacement")
+
+
 @pytest.mark.parametrize("optimizer", ["sd", "lbfgs", "cg", "fire"])
 def test_training_iterations_match_oracle(optimizer):
     """Several full training iterations (gradient, update, optimiser incl. line search)."""
