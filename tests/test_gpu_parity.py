@@ -241,13 +241,43 @@ def normwise(x, ref):
     return float(np.linalg.norm(np.asarray(x) - ref) / max(np.linalg.norm(ref), 1e-300))
 
 
+ACT_NP = {"tanh": np.tanh, "sigmoid": lambda z: 1.0 / (1.0 + np.exp(-z)),
+          "relu": lambda z: np.maximum(z, 0.0), "lrelu": lambda z: np.where(z > 0, z, 0.01 * z),
+          "softplus": lambda z: np.log1p(np.exp(z)),
+          "bent": lambda z: (np.sqrt(z * z + 1.0) - 1.0) / 2.0 + z, "atan": np.arctan,
+          "gaussian": lambda z: np.exp(-z * z), "heaviside": lambda z: (z > 0).astype(float),
+          "linear": lambda z: z}
+
+
+def output_term_magnitudes(dims, act, params, feats, sp):
+    """Per atom and output, |b| + sum_j |w_j a_j| of the output layer (FP64): the size of the
+    terms the output is summed from, which sets the scale of any output's rounding error."""
+    woff, boff, _ = synthetic.param_layout(dims)
+    f = ACT_NP[act]
+    out = np.zeros((feats.shape[0], dims[-1]))
+    for s in np.unique(sp):
+        m = sp == s
+        a = feats[m]
+        p = params[s]
+        for l in range(len(dims) - 1):
+            W = p[woff[l]:woff[l] + dims[l] * dims[l + 1]].reshape(dims[l + 1], dims[l]).T
+            b = p[boff[l + 1]:boff[l + 1] + dims[l + 1]]
+            if l == len(dims) - 2:
+                out[m] = np.abs(a) @ np.abs(W) + np.abs(b)
+            else:
+                a = f(a @ W + b)
+    return out
+
+
 def test_golden_prediction_fp32_tolerances():
     """FP32 plain form on every golden prediction case (the reference's trained networks):
     norm-wise over each case 1e-5 (summed outputs) and 1e-4 (analytical forces), the north
-    star's numbers; per structure and output, the summed outputs within 1e-4 of the larger of
-    the golden sum and the sum of the golden atomic output magnitudes (some trained outputs sum
-    to ~1e-6 from terms of ~0.2), and the forces within 5e-4 of the structure's largest
-    component.  The worst values are printed."""
+    star's numbers; per structure and output, the summed outputs within 1e-5 and the forces
+    within 1e-4 of the structure's largest component.  A structure's output sum is compared
+    relative to the larger of |sum|, sum |o_i| and the sum of the output layers' term
+    magnitudes |b| + sum |w a| (FP64): some trained outputs are ~5e-4 differences of terms of
+    ~4.5 (one ulp of FP32 on the terms is then ~5e-4 of the output), so their own size is not
+    the scale of a rounding error.  The worst values are printed."""
     worst_e, worst_f, worst_en, worst_fn = 0.0, 0.0, 0.0, 0.0
     for name in GOLDEN_PRED:
         case = G.load_case(name)
@@ -255,9 +285,17 @@ def test_golden_prediction_fp32_tolerances():
         ref = case.arrays["out_rawpredictions"]
         ds = case.ds
         off = ds.atom_offsets
+        inp = case.net("in_")
+        vals = O.acsf(ds, inp["gfuncs"]) if inp["gfuncs"] else None
+        if vals is not None and inp["zprec"] is not None:
+            vals = O.zscore_apply(vals, inp["zprec"])
+        feats = G.assemble_features(vals, ds, inp["ext_indices"])
+        sp = G.species_index(ds, inp["atomic_numbers"])
+        terms = output_term_magnitudes(inp["dims"], inp["activation"], inp["params"], feats, sp)
         e = np.add.reduceat(pred, off[:-1], axis=0)
         er = np.add.reduceat(ref, off[:-1], axis=0)
-        mag = np.add.reduceat(np.abs(ref), off[:-1], axis=0)
+        mag = np.maximum(np.add.reduceat(np.abs(ref), off[:-1], axis=0),
+                         np.add.reduceat(terms, off[:-1], axis=0))
         worst_e = max(worst_e, float(np.max(np.abs(e - er) / np.maximum(np.abs(er), mag))))
         worst_en = max(worst_en, normwise(e, er))
         # finite differences divide the FP32 rounding of the energies by 2 delta: their force
@@ -273,7 +311,7 @@ def test_golden_prediction_fp32_tolerances():
     print(f"golden FP32: per structure energy {worst_e:.2e}, forces {worst_f:.2e}; norm-wise "
           f"energy {worst_en:.2e}, forces {worst_fn:.2e}")
     assert worst_en < 1e-5 and worst_fn < 1e-4
-    assert worst_e <= 1e-4 and worst_f <= 5e-4
+    assert worst_e <= 1e-5 and worst_f <= 1e-4
 
 
 def oracle_energy_forces(ds, funcs, zprec, dims, act, params, sp, physical=True):
