@@ -46,9 +46,21 @@ def library_path():
     return _build.LIB
 
 
-def load(build_if_missing=True):
-    """Load libfnetg.so (building it first if it is missing and nvcc is available)."""
+_others = {}  # other builds of the library (the bounds-checked one), by path
+
+
+def load(build_if_missing=True, path=None):
+    """Load libfnetg.so (building it first if it is missing and nvcc is available); path
+    selects another build of the library, for example the bounds-checked one
+    (fortnet_gb300.build.build(checks=True))."""
     global _lib
+    if path is not None and os.path.abspath(path) != os.path.abspath(_build.LIB):
+        path = os.path.abspath(path)
+        if path not in _others:
+            if not os.path.exists(path):
+                raise FnetgError(-7, f"{path} missing")
+            _others[path] = _bind(C.CDLL(path))
+        return _others[path]
     if _lib is not None:
         return _lib
     path = _build.LIB
@@ -56,7 +68,12 @@ def load(build_if_missing=True):
         if not build_if_missing:
             raise FnetgError(-7, f"{path} missing; build it with fortnet_gb300.build.build()")
         _build.build()
-    L = C.CDLL(path)
+    _lib = _bind(C.CDLL(path))
+    return _lib
+
+
+def _bind(L):
+    """Argument and result types of every entry point."""
     vp, i32, i64, dbl = C.c_void_p, C.c_int32, C.c_int64, C.c_double
     sig = {
         "fnetg_create": (C.c_int, [C.POINTER(vp), i32, i32]),
@@ -97,6 +114,7 @@ def load(build_if_missing=True):
         "fnetg_profile_reset": (C.c_int, [vp]),
         "fnetg_launch_count": (i64, [vp]),
         "fnetg_synchronize": (C.c_int, [vp]),
+        "fnetg_check_status": (C.c_int, [vp, C.POINTER(i32)]),
         "fnetg_features_jvp": (C.c_int, [vp, vp, vp]),
         "fnetg_set_force_targets": (C.c_int, [vp, dbl, vp]),
         "fnetg_last_losses": (C.c_int, [vp, C.POINTER(dbl), C.POINTER(dbl)]),
@@ -121,7 +139,6 @@ def load(build_if_missing=True):
         fn = getattr(L, name)
         fn.restype = res
         fn.argtypes = args
-    _lib = L
     return L
 
 
@@ -145,8 +162,8 @@ def _check_out(a, shape):
 class Context:
     """One library context: a CUDA stream, device-resident structures, features, network."""
 
-    def __init__(self, precision=FP32, device=0):
-        self.lib = load()
+    def __init__(self, precision=FP32, device=0, library=None):
+        self.lib = load(path=library)
         h = C.c_void_p()
         rc = self.lib.fnetg_create(C.byref(h), int(precision), int(device))
         if rc != 0:
@@ -423,6 +440,13 @@ class Context:
         self._check(self.lib.fnetg_batch_sync_params(self.h))
 
     # -- plumbing ----------------------------------------------------------------------
+    def check_status(self):
+        """The first failed index check of the bounds-checked build since the last call
+        (file code x 100000 + line), 0 if none; always 0 for the default build."""
+        site = C.c_int32()
+        self._check(self.lib.fnetg_check_status(self.h, C.byref(site)))
+        return site.value
+
     def stream(self):
         s = C.c_void_p()
         self._check(self.lib.fnetg_get_stream(self.h, C.byref(s)))

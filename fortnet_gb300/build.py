@@ -16,6 +16,9 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libfnetg.so")
+# the bounds-checked build (every index guard compiled in; slower, for tests)
+CHECKS_DIR = os.path.join(OUT_DIR, "checks")
+CHECKS_LIB = os.path.join(CHECKS_DIR, "libfnetg.so")
 SOURCES = ["context.cu", "neighbors.cu", "acsf.cu", "mlp.cu", "forces.cu", "train.cu", "rng.cu",
            "noalloc.cu", "fd.cu", "serve.cu", "batch.cu", "jvp.cu",
            "forceloss.cu"]
@@ -34,8 +37,8 @@ def common_flags():
                    "-Xcompiler", "-fPIC,-ffp-contract=off,-O2", "-I", os.path.join(HERE, "..", "include")]
 
 
-def _compile(src, extra):
-    obj = os.path.join(OUT_DIR, os.path.splitext(src)[0] + ".o")
+def _compile(src, extra, out_dir=OUT_DIR):
+    obj = os.path.join(out_dir, os.path.splitext(src)[0] + ".o")
     cmd = [nvcc_path(), "-c", os.path.join(CSRC, src), "-o", obj] + common_flags() + extra
     res = subprocess.run(cmd, capture_output=True, text=True)
     if res.returncode != 0:
@@ -43,35 +46,37 @@ def _compile(src, extra):
     return obj, res.stderr
 
 
-def _stale():
-    if not os.path.exists(LIB):
+def _stale(lib=LIB):
+    if not os.path.exists(lib):
         return True
-    t = os.path.getmtime(LIB)
+    t = os.path.getmtime(lib)
     deps = [os.path.join(CSRC, f) for f in os.listdir(CSRC)] + [
         os.path.join(HERE, "..", "include", "fnetg.h"), os.path.abspath(__file__)]
     return any(os.path.getmtime(d) > t for d in deps if os.path.exists(d))
 
 
-def build(force=False, verbose=False, extra=None):
-    """Compile and link the library; returns its path."""
-    if not force and not _stale():
-        return LIB
-    os.makedirs(OUT_DIR, exist_ok=True)
-    extra = list(extra or [])
+def build(force=False, verbose=False, extra=None, checks=False):
+    """Compile and link the library; returns its path.  checks=True builds the bounds-checked
+    library (-DFNETG_CHECKS) into _build/checks/ instead."""
+    lib, out_dir = (CHECKS_LIB, CHECKS_DIR) if checks else (LIB, OUT_DIR)
+    if not force and not _stale(lib):
+        return lib
+    os.makedirs(out_dir, exist_ok=True)
+    extra = list(extra or []) + (["-DFNETG_CHECKS"] if checks else [])
     with cf.ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
-        results = list(ex.map(lambda s: _compile(s, extra), SOURCES))
+        results = list(ex.map(lambda s: _compile(s, extra, out_dir), SOURCES))
     if verbose:
         for _, err in results:
             if err.strip():
                 print(err, file=sys.stderr)
     objs = [o for o, _ in results]
-    tmp = LIB + ".tmp"
+    tmp = lib + ".tmp"
     cmd = [nvcc_path(), "-shared", "-o", tmp] + objs + ARCH + ["-lcudart"]
     res = subprocess.run(cmd, capture_output=True, text=True)
     if res.returncode != 0:
         raise RuntimeError(f"link failed:\n{res.stdout}\n{res.stderr}")
-    os.replace(tmp, LIB)
-    return LIB
+    os.replace(tmp, lib)
+    return lib
 
 
 HOST_DIR = os.path.join(HERE, "host")

@@ -10,6 +10,7 @@
 // (acsf.F90:1480-1488) into O(N_nb) moments.  G4 and other xi run a lanes-over-triplets sweep
 // for a group of up to 32 functions sharing two lists, with exp(-eta r^2) fc(r) tabulated per
 // pair and eta class.
+#define FNETG_FILE_CODE 2  // site codes of the bounds-checked build
 #include <algorithm>
 
 #include "tile.cuh"
@@ -172,6 +173,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 1)
     const int64_t p0 = a.poff[i];
     const int np = (int)(a.pend[i] - p0);
     const int64_t row = a.bpos[i];
+    if (!FNETG_GUARD(np >= 0 && np <= a.cap && row >= 0 && row < a.natoms)) continue;
     // the next atom of this warp: its pair range requested now, its records prefetched into
     // L2 once the range has arrived (after the staging)
     const int64_t inext = i + (int64_t)gridDim.x * wpb;
@@ -742,5 +744,7 @@ int run_zscore(fnetg_ctx *ctx, const int32_t *weights, bool compute) {
   return ctx->prec == FNETG_FP64 ? launch_zscore<double>(ctx, weights, compute)
                                  : launch_zscore<float>(ctx, weights, compute);
 }
+
+FNETG_CHECK_READER(check_site_acsf)
 
 }  // namespace fnetg

@@ -26,6 +26,7 @@
 //
 // Supported networks: two hidden tanh layers of equal padded width 16, 32 or 64 (at most 64
 // units each), one linear output, at most 239 inputs.
+#define FNETG_FILE_CODE 5  // site codes of the bounds-checked build
 #include <cuda_bf16.h>
 
 #include <algorithm>
@@ -179,7 +180,15 @@ struct TcArgs {
   int ng;
   // tangent kernel: packed BF16 tangents of the inputs, same tiles and layout as x
   const unsigned char *u;
+  int64_t natoms;             // atoms of the context (bounds-checked build)
 };
+
+// A tile row's atom; in the bounds-checked build an index outside the context's atoms is
+// recorded and the row treated as padding.
+__device__ __forceinline__ int tile_atom(const int32_t *tile_atoms, int64_t k, int64_t natoms) {
+  const int v = tile_atoms[k];
+  return (v < 0 || FNETG_GUARD(v < natoms)) ? v : -1;
+}
 
 __device__ __forceinline__ float tanh_fast(float x) {
   float y;
@@ -359,7 +368,7 @@ __global__ void __launch_bounds__(kThreads, 1) tc_mlp_kernel(TcArgs a) {
     }
     cur_sp = sp;
     const int row = tid;
-    const int atom = a.tile_atoms[t * kRows + row];
+    const int atom = tile_atom(a.tile_atoms, t * kRows + row, a.natoms);
     const float delta3 = (MODE == 1 && atom >= 0) ? (float)a.delta[atom] : 0.f;
     if (!wait_all(&mb_load, ph_load)) {
       tc::mbar_wait(&mb_load, ph_load);  // the copies in flight, once more with a limit
@@ -564,7 +573,7 @@ __global__ void __launch_bounds__(kThreads, 1) tc_jac_kernel(TcArgs a) {
     }
     cur_sp = sp;
     const int row = tid;
-    const int atom = a.tile_atoms[t * kRows + row];
+    const int atom = tile_atom(a.tile_atoms, t * kRows + row, a.natoms);
     if (!wait_all(&mb_load, ph_load)) {
       tc::mbar_wait(&mb_load, ph_load);
       failed = true;
@@ -738,7 +747,7 @@ __global__ void __launch_bounds__(kThreads, 1) tc_tan_kernel(TcArgs a) {
     }
     cur_sp = sp;
     const int row = tid;
-    const int atom = a.tile_atoms[t * kRows + row];
+    const int atom = tile_atom(a.tile_atoms, t * kRows + row, a.natoms);
     const float ybar = atom >= 0 ? (float)a.delta[atom] : 0.f;
     const float ydbar = atom >= 0 ? -1.f : 0.f;
     if (!wait_all(&mb_load, ph_load)) {
@@ -898,7 +907,8 @@ __global__ void __launch_bounds__(kThreads, 1) tc_tan_kernel(TcArgs a) {
 // tiles in the feature layout; the bias column and padding rows are zero
 template <typename T>
 __global__ void pack_u_kernel(const T *u, int nf, int K0p, const int32_t *tile_atoms,
-                              int64_t ntiles, uint32_t x_bytes, unsigned char *out) {
+                              int64_t ntiles, uint32_t x_bytes, unsigned char *out,
+                              int64_t natoms) {
   const int groups = K0p / 8;
   const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= ntiles * kRows * groups) return;
@@ -906,7 +916,7 @@ __global__ void pack_u_kernel(const T *u, int nf, int K0p, const int32_t *tile_a
   const int64_t tr = q / groups;
   const int64_t t = tr / kRows;
   const int r = (int)(tr % kRows);
-  const int atom = tile_atoms[tr];
+  const int atom = tile_atom(tile_atoms, tr, natoms);
   float v[8];
 #pragma unroll
   for (int c = 0; c < 8; c++) {
@@ -922,7 +932,7 @@ __global__ void pack_u_kernel(const T *u, int nf, int K0p, const int32_t *tile_a
 template <typename T>
 __global__ void pack_x_kernel(const T *feat, const int32_t *bpos, int nf, int K0p,
                               const int32_t *tile_atoms, int64_t ntiles, uint32_t x_bytes,
-                              unsigned char *x) {
+                              unsigned char *x, int64_t natoms) {
   const int groups = K0p / 8;
   const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= ntiles * kRows * groups) return;
@@ -930,7 +940,7 @@ __global__ void pack_x_kernel(const T *feat, const int32_t *bpos, int nf, int K0
   const int64_t tr = q / groups;
   const int64_t t = tr / kRows;
   const int r = (int)(tr % kRows);
-  const int atom = tile_atoms[tr];
+  const int atom = tile_atom(tile_atoms, tr, natoms);
   float v[8];
 #pragma unroll
   for (int c = 0; c < 8; c++) {
@@ -1159,6 +1169,7 @@ int launch_tc(fnetg_ctx *ctx, int mode, int64_t t0, int64_t t1, int grid) {
   a.w = b.d_w.as<unsigned char>();
   a.tile_sp = b.d_tile_sp.as<int32_t>();
   a.tile_atoms = b.d_tile_atoms.as<int32_t>();
+  a.natoms = ctx->N;
   a.t0 = t0;
   a.t1 = t1;
   a.out = ctx->d_out.as<double>();
@@ -1186,6 +1197,7 @@ TcArgs base_args(fnetg_ctx *ctx, int64_t t0, int64_t t1) {
   a.w = b.d_w.as<unsigned char>();
   a.tile_sp = b.d_tile_sp.as<int32_t>();
   a.tile_atoms = b.d_tile_atoms.as<int32_t>();
+  a.natoms = ctx->N;
   a.t0 = t0;
   a.t1 = t1;
   a.out = ctx->d_out.as<double>();
@@ -1372,7 +1384,7 @@ int pack_features(fnetg_ctx *ctx) {
   LaunchScope ls(ctx, "tc_pack");
   pack_x_kernel<T><<<ceil_div(total, 256), 256, 0, ctx->stream>>>(
       ctx->d_feat.as<T>(), ctx->d_bpos.as<int32_t>(), b.net.nf, b.net.K0p,
-      b.d_tile_atoms.as<int32_t>(), b.ntiles, b.net.x_bytes, b.d_x.as<unsigned char>());
+      b.d_tile_atoms.as<int32_t>(), b.ntiles, b.net.x_bytes, b.d_x.as<unsigned char>(), ctx->N);
   FNETG_CUDA(cudaGetLastError());
   return FNETG_OK;
 }
@@ -1415,7 +1427,7 @@ int run_batch_gradients(fnetg_ctx *ctx, int loss) {
       LaunchScope ls(ctx, "tc_pack");
       pack_u_kernel<float><<<ceil_div(total, 256), 256, 0, ctx->stream>>>(
           ctx->d_fl_u.as<float>(), ctx->nf, b.net.K0p, b.d_tile_atoms.as<int32_t>(), b.ntiles,
-          b.net.x_bytes, b.d_u.as<unsigned char>());
+          b.net.x_bytes, b.d_u.as<unsigned char>(), ctx->N);
       FNETG_CUDA(cudaGetLastError());
     }
     rc = launch_tc_tan(ctx, 0, b.ntiles, grid);
@@ -1432,6 +1444,8 @@ int run_batch_gradients(fnetg_ctx *ctx, int loss) {
   }
   return launch_reduce(ctx, grid);
 }
+
+FNETG_CHECK_READER(check_site_batch)
 
 }  // namespace fnetg
 

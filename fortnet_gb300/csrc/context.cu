@@ -211,6 +211,19 @@ int fnetg_synchronize(fnetg_ctx *ctx) {
   return FNETG_OK;
 }
 
+int fnetg_check_status(fnetg_ctx *ctx, int32_t *site) {
+  if (!ctx || !site) return FNETG_E_INVALID;
+  FNETG_CUDA(cudaStreamSynchronize(ctx->stream));
+  int first = 0;
+  for (int v : {check_site_neighbors(), check_site_acsf(), check_site_forces(), check_site_mlp(),
+                check_site_batch(), check_site_jvp()}) {
+    FNETG_CHECK(v >= 0, FNETG_E_CUDA, "check_status: reading a check word failed");
+    if (first == 0) first = v;
+  }
+  *site = first;
+  return FNETG_OK;
+}
+
 int fnetg_profile_enable(fnetg_ctx *ctx, int32_t enable) {
   if (!ctx) return FNETG_E_INVALID;
   ctx->prof = enable != 0;

@@ -13,6 +13,7 @@
 //                    accumulation.
 // Forces are scattered as F_j -= w_p, F_i += w_p with FP64 atomics; every periodic image
 // contributes its own derivative (physical forces), self images cancel.
+#define FNETG_FILE_CODE 3  // site codes of the bounds-checked build
 #include <algorithm>
 
 #include "tile.cuh"
@@ -292,6 +293,7 @@ __global__ void __launch_bounds__(kForcesThreads<T>, sizeof(T) == 4 ? 5 : 1)
   for (int64_t i = (int64_t)blockIdx.x * wpb + warp; i < a.natoms; i += (int64_t)gridDim.x * wpb) {
     const int64_t p0 = a.poff[i];
     const int np = (int)(a.pend[i] - p0);
+    if (!FNETG_GUARD(np >= 0 && np <= a.cap)) continue;
     // this atom's dE/dG row and cached moments: asynchronous copies overlapping the staging
     // (the previous atom's readers finished at the loop's closing warp barrier)
     async_copy<T>(tl.jv, a.J + i * a.nf, a.ng, lane);
@@ -496,6 +498,7 @@ __global__ void __launch_bounds__(kForcesThreads<T>, sizeof(T) == 4 ? 5 : 1)
       if ((tl.info[q] >> 8) & 1u) continue;
       const V4<T> w = tl.w[q];
       const int64_t j = tl.pj[q];
+      if (!FNETG_GUARD(j >= 0 && j < a.natoms)) continue;
       if constexpr (sizeof(T) == 4) {
         atomicAdd(a.F4 + j * a.nout + a.out_index, make_float4(-w.x, -w.y, -w.z, 0.f));
       } else {
@@ -652,5 +655,7 @@ template <typename T> int launch_forces(fnetg_ctx *ctx) {
 int run_forces(fnetg_ctx *ctx) {
   return ctx->prec == FNETG_FP64 ? launch_forces<double>(ctx) : launch_forces<float>(ctx);
 }
+
+FNETG_CHECK_READER(check_site_forces)
 
 }  // namespace fnetg

@@ -16,6 +16,33 @@
 namespace fnetg {
 
 // ---------------------------------------------------------------------------------------
+// Index checks of the bounds-checked build (compiled with -DFNETG_CHECKS, a separate library):
+// FNETG_GUARD(ok) records the first failing site (file code x 100000 + line) in the word of
+// its translation unit and evaluates to ok, so that the guarded access is skipped; the
+// default build compiles every guard to `true`.  fnetg_check_status reads and clears the
+// words of every translation unit.
+#ifdef FNETG_CHECKS
+static __device__ int g_fnetg_check_site;
+__device__ __forceinline__ bool fnetg_guard(bool ok, int site) {
+  if (!ok) atomicCAS(&g_fnetg_check_site, 0, site);
+  return ok;
+}
+#define FNETG_GUARD(ok) ::fnetg::fnetg_guard((ok), FNETG_FILE_CODE * 100000 + __LINE__)
+// host reader of this translation unit's word (read and cleared)
+#define FNETG_CHECK_READER(fn)                                                \
+  int fn() {                                                                  \
+    int v = 0, z = 0;                                                         \
+    if (cudaMemcpyFromSymbol(&v, g_fnetg_check_site, sizeof(int)) != cudaSuccess) return -1; \
+    if (cudaMemcpyToSymbol(g_fnetg_check_site, &z, sizeof(int)) != cudaSuccess) return -1;   \
+    return v;                                                                 \
+  }
+#else
+#define FNETG_GUARD(ok) true
+#define FNETG_CHECK_READER(fn) \
+  int fn() { return 0; }
+#endif
+
+// ---------------------------------------------------------------------------------------
 // small vector types with explicit alignment (the deprecated double4 is avoided)
 template <typename T> struct __align__(4 * sizeof(T)) V4 { T x, y, z, w; };
 
@@ -352,5 +379,12 @@ int run_update_prepare(fnetg_ctx *ctx, double strength, double alpha);
 int run_optimizer_step(fnetg_ctx *ctx);
 int run_params_to_compute(fnetg_ctx *ctx);
 int exclusive_scan_i64(fnetg_ctx *ctx, const int64_t *in, int64_t *out, int64_t n);
+// check words of the bounds-checked build (0 = no failed check; always 0 in the default build)
+int check_site_neighbors();
+int check_site_acsf();
+int check_site_forces();
+int check_site_mlp();
+int check_site_batch();
+int check_site_jvp();
 
 }  // namespace fnetg

@@ -24,6 +24,7 @@
 // (dM_k1 M_k2 + M_k1 dM_k2) with the moments themselves from the value kernel's cache.  That
 // kernel (jvp_tile_kernel) also takes the radial functions; the triplet kernel (jvp_kernel)
 // then runs only for the angular functions outside the moment form.
+#define FNETG_FILE_CODE 6  // site codes of the bounds-checked build
 #include <algorithm>
 #include <array>
 
@@ -515,7 +516,7 @@ __global__ void __launch_bounds__(32 * kJtWarps) jvp_tile_kernel(JtArgs<T> a) {
       acc += dg * Wd[q].w;
     }
     acc = jsum(acc);
-    if (lane == 0) ui[g.out] = acc * jt_zscale(a, g.out);
+    if (lane == 0 && FNETG_GUARD(g.out >= 0 && g.out < a.nf)) ui[g.out] = acc * jt_zscale(a, g.out);
   }
   if (a.nmf == 0) return;
   // ---- moments (from the cache when it holds them) and their tangents
@@ -560,7 +561,7 @@ __global__ void __launch_bounds__(32 * kJtWarps) jvp_tile_kernel(JtArgs<T> a) {
     T acc = 0;
 #pragma unroll
     for (int m = 0; m < kJtKD; m++) acc += pc[m] * S[m];
-    ui[mf.out] = acc * jt_zscale(a, mf.out);
+    if (FNETG_GUARD(mf.out >= 0 && mf.out < a.nf)) ui[mf.out] = acc * jt_zscale(a, mf.out);
   }
 }
 
@@ -707,6 +708,8 @@ int run_features_jvp(fnetg_ctx *ctx, const void *d_w, void *d_u) {
              ? do_jvp<double>(ctx, static_cast<const double *>(d_w), static_cast<double *>(d_u))
              : do_jvp<float>(ctx, static_cast<const float *>(d_w), static_cast<float *>(d_u));
 }
+
+FNETG_CHECK_READER(check_site_jvp)
 
 }  // namespace fnetg
 

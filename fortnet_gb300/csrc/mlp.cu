@@ -11,6 +11,7 @@
 // layout pads every weight row to a multiple of four (zeros) and stores W ([d_in][d_out])
 // for the forward pass and W^T ([d_out][d_in]) for the backward pass.  Per-tile
 // weight-gradient partials are reduced across tiles in FP64.
+#define FNETG_FILE_CODE 4  // site codes of the bounds-checked build
 #include <algorithm>
 
 #include "internal.cuh"
@@ -366,6 +367,7 @@ template <typename T> struct MlpArgs {
   int64_t ntiles;         // CTAs loop over the tiles in steps of gridDim.x
   const int32_t *bperm;   // row -> atom
   int RC, RCP;            // rows per chunk, padded row stride of the shared buffers
+  int64_t natoms;         // rows of feat / atoms of out (bounds-checked build)
   SmemPlan pl;            // shared-memory offsets (kernel parameter: indexed without local copies)
   double *out;            // [N][nout] atom order (forward)
   // backward
@@ -387,7 +389,8 @@ __device__ void load_features(const MlpArgs<T> &a, int64_t row0, int nrows, T *X
   const int nf = a.nf, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
   for (int r = threadIdx.x >> 5; r < a.RC; r += nw)
     for (int k = lane; k < nf; k += 32)
-      X[(int64_t)k * a.RCP + r] = r < nrows ? a.feat[(row0 + r) * nf + k] : (T)0;
+      X[(int64_t)k * a.RCP + r] =
+          r < nrows && FNETG_GUARD(row0 + r < a.natoms) ? a.feat[(row0 + r) * nf + k] : (T)0;
 }
 
 template <int OW> constexpr int mlp_threads() { return OW == 4 ? 128 : 256; }
@@ -437,6 +440,7 @@ __global__ void __launch_bounds__(mlp_threads<OW>()) mlp_forward_kernel(MlpArgs<
       }
       for (int r = threadIdx.x; r < nrows; r += blockDim.x) {
         const int64_t atom = a.bperm[row0 + r];
+        if (!FNETG_GUARD(row0 + r < a.natoms && atom >= 0 && atom < a.natoms)) continue;
         for (int o = 0; o < nout; o++) a.out[atom * nout + o] = (double)in[(int64_t)o * a.RCP + r];
       }
       __syncthreads();
@@ -499,6 +503,7 @@ __global__ void __launch_bounds__(mlp_threads<OW>()) mlp_jacobian_kernel(MlpArgs
         for (int k = lane; k < nf; k += 32) {
           const T v = J[(int64_t)k * a.RCP + r];
           const int64_t atom = a.bperm[row0 + r];
+          if (!FNETG_GUARD(row0 + r < a.natoms && atom >= 0 && atom < a.natoms)) continue;
           if (a.jac64) a.jac64[atom * nf + k] = (double)v;
           if (a.jacT) {
             T s = v;
@@ -666,6 +671,7 @@ template <typename T> void prepare(fnetg_ctx *ctx, const Layouts &Lo, MlpArgs<T>
   a.tiles = ctx->d_tiles.as<int4>();
   a.ntiles = ctx->ntiles;
   a.bperm = ctx->d_bperm.as<int32_t>();
+  a.natoms = ctx->N;
   a.RC = chunk_rows<T>(Lo.net, ctx->tile_rows, keep_all, sw, budget);
   a.RCP = a.RC + 4;
   a.pl = smem_plan(Lo.net, a.RCP, keep_all, sw);
@@ -868,5 +874,7 @@ int run_jacobian(fnetg_ctx *ctx, int o, void *dst) {
 int run_mlp_backward(fnetg_ctx *ctx) {
   return ctx->prec == FNETG_FP64 ? do_backward<double>(ctx) : do_backward<float>(ctx);
 }
+
+FNETG_CHECK_READER(check_site_mlp)
 
 }  // namespace fnetg

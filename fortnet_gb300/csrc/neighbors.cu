@@ -10,6 +10,7 @@
 // (nc = c_j + L n, d = c_i - nc, d2 = (d0^2 + d1^2) + d2^2, d2 <= rc^2) with every
 // operation rounded separately (no FMA contraction).  A ballot keeps the accepted pairs in
 // iterator order, so the fill pass reproduces the reference's neighbour order exactly.
+#define FNETG_FILE_CODE 1  // site codes of the bounds-checked build
 #include <algorithm>
 
 #include "internal.cuh"
@@ -59,6 +60,7 @@ struct NbArgs {
   const int64_t *coff;
   const int64_t *cstart;
   const V4<float> *cpos;  // per cell slot: relative float position, w = structure-local index
+  int64_t nslots;  // pair slots of pj / pmeta / rij (bounds-checked build)
   float inv_cs;   // 1 / cell edge (relative float frame)
   float rbox;     // half-width of a centre's candidate box, >= the float pre-filter's reach
 };
@@ -137,6 +139,7 @@ __device__ __forceinline__ void store_pair(const NbArgs &a, const double *ci, co
   const int64_t img = img_i;
   const int64_t j = a0 + jl;
   const int64_t q = wpos + rank;
+  if (!FNETG_GUARD(q >= 0 && q < a.nslots && jl >= 0)) return;
   V4<float> ch{0.f, 0.f, 0.f, 0.f}, cvl{0.f, 0.f, 0.f, 0.f};
   uint32_t packed = 0;
   if (img >= im0) {
@@ -278,9 +281,10 @@ __global__ void __launch_bounds__(256, 4) nb_kernel(NbArgs a) {
             const bool two = q + 1 < q1;
             const V4<float> pb = two ? a.cpos[q + 1] : pa;
             const int ja = (int)__float_as_int(pa.w), jb = (int)__float_as_int(pb.w);
-            if (!(ja == il && img < im0) && decide(ja, pa))
+            if (!(ja == il && img < im0) && decide(ja, pa) && FNETG_GUARD(ja >= 0 && ja < n))
               atomicOr(&bits[ja >> 5], 1u << (ja & 31));
-            if (two && !(jb == il && img < im0) && decide(jb, pb))
+            if (two && !(jb == il && img < im0) && decide(jb, pb) &&
+                FNETG_GUARD(jb >= 0 && jb < n))
               atomicOr(&bits[jb >> 5], 1u << (jb & 31));
           }
         }
@@ -316,7 +320,8 @@ __global__ void __launch_bounds__(256, 4) nb_kernel(NbArgs a) {
             const bool ok = (mw >> lane) & 1u;
             const unsigned mb = __ballot_sync(0xffffffffu, ok);
             const unsigned below = (1u << lane) - 1u;
-            if (ok) queue[qn + __popc(mb & below)] = make_int2(wsrc * 32 + lane, (int)img);
+            if (ok && FNETG_GUARD(qn + __popc(mb & below) < 128))
+              queue[qn + __popc(mb & below)] = make_int2(wsrc * 32 + lane, (int)img);
             qn += __popc(mb);
             cnt += __popc(mb);
             __syncwarp();
@@ -365,8 +370,10 @@ __global__ void __launch_bounds__(256, 4) nb_kernel(NbArgs a) {
         if (kFill) {
           // queue the accepted candidates in iterator order; store them 32 at a time
           const unsigned below = (1u << lane) - 1u;
-          if (ok0) queue[qn + __popc(m0 & below)] = make_int2(j0, (int)img);
-          if (ok1) queue[qn + n0 + __popc(m1 & below)] = make_int2(j1, (int)img);
+          if (ok0 && FNETG_GUARD(qn + __popc(m0 & below) < 128))
+            queue[qn + __popc(m0 & below)] = make_int2(j0, (int)img);
+          if (ok1 && FNETG_GUARD(qn + n0 + __popc(m1 & below) < 128))
+            queue[qn + n0 + __popc(m1 & below)] = make_int2(j1, (int)img);
           qn += n0 + n1;
           __syncwarp();
           while (qn >= 32) {
@@ -836,6 +843,7 @@ int run_neighbors(fnetg_ctx *ctx, double rcut) {
     FNETG_CUDA(ctx->d_rij.ensure(4 * es * slots));
     FNETG_CUDA(ctx->d_pend.ensure(sizeof(int64_t) * N));
     a.slab_cap = cap;
+    a.nslots = slots;
     a.poff = nullptr;
     a.pbeg = ctx->d_poff.as<int64_t>();
     a.pend = ctx->d_pend.as<int64_t>();
@@ -896,6 +904,7 @@ int run_neighbors(fnetg_ctx *ctx, double rcut) {
   FNETG_CUDA(ctx->d_pmeta.ensure(sizeof(uint32_t) * std::max<int64_t>(P, 1)));
   FNETG_CUDA(ctx->d_rij.ensure(4 * es * std::max<int64_t>(P, 1)));
   a.poff = ctx->d_poff.as<int64_t>();
+  a.nslots = P;
   a.pj = ctx->d_pj.as<int32_t>();
   a.pmeta = ctx->d_pmeta.as<uint32_t>();
   a.rij = ctx->d_rij.p;
@@ -942,5 +951,7 @@ int pair_d2(fnetg_ctx *ctx) {
   ctx->d2_valid = true;
   return FNETG_OK;
 }
+
+FNETG_CHECK_READER(check_site_neighbors)
 
 }  // namespace fnetg

@@ -566,7 +566,8 @@ __device__ void stage_tile(const TileArgs<T> &a, Tile<T> &t, int64_t i, int64_t 
         in = ((int)(inf & 0xff) == z) || ((inf >> 8) & 1u);
       }
       const unsigned m = __ballot_sync(0xffffffffu, in);
-      if (in) t.lists[z * a.cap + base + __popc(m & ((1u << lane) - 1u))] = (uint16_t)q;
+      if (in && FNETG_GUARD(base + __popc(m & ((1u << lane) - 1u)) < a.cap))
+        t.lists[z * a.cap + base + __popc(m & ((1u << lane) - 1u))] = (uint16_t)q;
       base += __popc(m);
     }
     if (lane == 0) t.cnt[z] = base;

@@ -252,6 +252,12 @@ int fnetg_profile_reset(fnetg_ctx *ctx);
 /* Total kernel launches of the context since creation (or the last reset). */
 int64_t fnetg_launch_count(fnetg_ctx *ctx);
 int fnetg_synchronize(fnetg_ctx *ctx);
+/* Bounds-checked build only (the library compiled with -DFNETG_CHECKS): after synchronising
+ * the context's stream, *site receives the first failed index check since the last call
+ * (file code x 100000 + source line; the access it guarded was skipped) and the record is
+ * cleared; 0 = every check passed.  The default build has no checks and always gives 0.  No
+ * counterpart in the reference (its debug builds check array bounds with -fcheck=all). */
+int fnetg_check_status(fnetg_ctx *ctx, int32_t *site);
 
 #ifdef __cplusplus
 }
