@@ -215,25 +215,27 @@ __global__ void sd_kernel(double *params, const double *grad, int64_t np, SdStat
 // ---------------------------------------------------------------- L-BFGS + line minimiser
 // state layout per species (doubles): vectors xx, xold, gg, dir, x0, d0, dxt, qq (n each),
 // ss, yy (mem*n each), rho, alph (mem each), scalars (32)
-// ss, yy (mem*n each), rho, alph (mem each), scalars (32); then the inner products of the
-// L-BFGS direction (Gram form): sy[a][b] = s_a.y_b, syt[b][a] = s_a.y_b, yg[a][b] = y_a.y_b
-// (mem*mem each), ps[a] = s_a.g, py[a] = y_a.g, the direction's coefficients cs, cy (mem each)
-// and kLbSplit partial sums of the direction (n each)
+// ss, yy (mem*n each), rho, alph (mem each), scalars (32); then the compact form of the
+// L-BFGS direction: rinv[a][b] = (R^-1)_ab and rinvt[b][a] = (R^-1)_ab for the upper-triangular
+// R_ab = s_a.y_b (a older than b), R_aa = max(|s_a.y_a|, eps); syt[b][a] = s_a.y_b (the column
+// of the newest pair), yg[a][b] = y_a.y_b (mem*mem each); ps[a] = s_a.g, py[a] = y_a.g, the
+// direction's coefficients cs, cy and the intermediate v3 (mem each), and kLbSplit partial sums
+// of the direction (n each).  alph holds v1 = R^-1 S^T g.
 enum {
   SC_ITER = 0, SC_STATE, SC_IITER, SC_CONV, SC_XX0, SC_XX1, SC_DX0, SC_DX1, SC_XCUR, SC_MAXX,
   SC_FIRST, SC_CONVERGED, SC_PHASE, SC_NE, SC_USED, SC_GAMMA, SC_NS = 32
 };
 constexpr int kLbSplit = 8;         // slot groups of the direction's combination
-constexpr int kLbMaxMem = 8192;     // history slots the Gram-form recursion holds in shared memory
+constexpr int kLbMaxMem = 8192;     // history slots (the combination stages a slot group)
 
 struct LbView {
   double *xx, *xold, *gg, *dir, *x0, *d0, *dxt, *qq, *ss, *yy, *rho, *alph, *sc;
-  double *sy, *syt, *yg, *ps, *py, *cs, *cy, *part;
+  double *rinv, *syt, *yg, *rinvt, *ps, *py, *cs, *cy, *v3, *part;
 };
 
 __host__ __device__ inline size_t lb_stride(int64_t n, int mem) {
   return (size_t)8 * n + (size_t)2 * mem * n + (size_t)2 * mem + SC_NS +
-         (size_t)3 * mem * mem + (size_t)4 * mem + (size_t)kLbSplit * n;
+         (size_t)4 * mem * mem + (size_t)5 * mem + (size_t)kLbSplit * n;
 }
 
 __device__ LbView lb_view(double *base, int64_t n, int mem) {
@@ -252,13 +254,15 @@ __device__ LbView lb_view(double *base, int64_t n, int mem) {
   v.rho = p; p += mem;
   v.alph = p; p += mem;
   v.sc = p; p += SC_NS;
-  v.sy = p; p += (size_t)mem * mem;
+  v.rinv = p; p += (size_t)mem * mem;
   v.syt = p; p += (size_t)mem * mem;
   v.yg = p; p += (size_t)mem * mem;
+  v.rinvt = p; p += (size_t)mem * mem;
   v.ps = p; p += mem;
   v.py = p; p += mem;
   v.cs = p; p += mem;
   v.cy = p; p += mem;
+  v.v3 = p; p += mem;
   v.part = p;
   return v;
 }
@@ -289,22 +293,26 @@ __device__ void bcopy(double *dst, const double *src, int64_t n) {
   __syncthreads();
 }
 
-// TLbfgs_calcDirection (lbfgs.F90:387-488) in Gram form.  The two-loop recursion
-//   loop 1 (newest to oldest): alpha_k = rho_k s_k.q,  q -= alpha_k y_k       (q = g at start)
-//   r = gamma q;  loop 2 (oldest to newest): beta_l = rho_l y_l.r,  r += (alpha_l - beta_l) s_l
-//   dir = -r
-// keeps q and r as combinations of g and the stored pairs, so every inner product it takes is
-// a combination of s_a.g, y_a.g, s_a.y_b and y_a.y_b.  Those are kept per slot pair and
-// refreshed for the newest slot only; both loops become triangular solves over scalars (the
-// serial chains of 2 x memory full-length dot products are gone), and dir is formed once as
-// -gamma g + sum_a cs_a s_a + cy_a y_a.  Same arithmetic in exact terms; rounding differs by
-// the order of the sums.  Slots never written are skipped (in the reference they have
-// rho = 0 and change nothing).
+// TLbfgs_calcDirection (lbfgs.F90:387-488) in the compact form of the L-BFGS inverse Hessian
+// (Byrd, Nocedal and Schnabel, Math. Program. 63 (1994), eq. 3.7): with the stored pairs as the
+// columns of S and Y (oldest first), R the upper triangle of S^T Y with the diagonal
+// 1 / rho_a = max(|s_a.y_a|, eps) of the reference's rho, D = diag(1 / rho) and gamma the
+// initial diagonal, the two-loop recursion's direction is
+//   dir = -H g = -gamma g - S p + gamma Y v1,
+//   v1 = R^-1 S^T g,   p = R^-T ((D + gamma Y^T Y) v1 - gamma Y^T g).
+// Same arithmetic in exact terms (the recursion is this product written as loops); rounding
+// differs by the order of the sums.  The serial chains of the recursion (2 x memory dependent
+// dot products over all parameters) become matrix-vector products over memory x memory
+// matrices that spread over the whole GPU.  R^-1 is kept from one direction to the next: when
+// the oldest pair leaves the ring buffer, the inverse of the remaining trailing block of R is
+// the trailing block of R^-1; a new pair adds the column -R^-1 c rho_new (c_a = s_a.y_new) and
+// the diagonal rho_new.  Slots never written are skipped (the reference's rho = 0 for them
+// changes nothing).
 //
 // Stage 1 (lbfgs_pre_kernel, one CTA per species): convergence, the line minimiser, and the
 // history update s_ne = x - x_old, y_ne = g - g_old.  SC_PHASE tells the later stages what
-// to do: 0 nothing (converged or inside a line search), 1 a Gram-form direction, 2 the first
-// direction -g.
+// to do: 0 nothing (converged or inside a line search), 1 a compact-form direction, 2 the
+// first direction -g.
 __device__ void lb_history(LbView &v, const LbParams &P, const double *xx, const double *g) {
   const int64_t n = P.n;
   const int mem = P.mem;
@@ -345,15 +353,14 @@ __device__ void lb_history(LbView &v, const LbParams &P, const double *xx, const
 constexpr int kGramSlots = 4;
 constexpr int kGramThreads = 256;
 
-// Stage 3 (lbfgs_recur_kernel, one CTA per species): the two loops as blocked triangular
-// solves.  Loop-1 order k = 0..used-1 runs newest to oldest (slot ne - k), loop-2 order
-// l = 0..used-1 oldest to newest (slot ne - used + 1 + l).  Each block of 32 rows is solved by
-// one warp from a staged diagonal block; the rows below it are updated by all threads.
-constexpr int kRecThreads = 512;
-constexpr int kRecBlock = 32;
+// Stages 3-6 (lbfgs_rinv_kernel, lbfgs_v1_kernel, lbfgs_v2_kernel, lbfgs_p_kernel): the new
+// column of R^-1 and gamma, v1, v3 = (D + gamma Y^T Y) v1 - gamma Y^T g, p = R^-T v3 and the
+// coefficients; a warp per row of the memory x memory matrices, rows in age order
+// (k = 0 oldest .. used - 1 newest, slot ne - (used - 1 - k)).
+constexpr int kGemvWarps = 8;
 
-// Stage 4 (lbfgs_combine_kernel): kLbSplit partial sums of sum_a cs_a s_a + cy_a y_a over
-// slot groups; stage 5 (lbfgs_post_kernel) adds them in a fixed order to -gamma g and runs the
+// Stage 7 (lbfgs_combine_kernel): kLbSplit partial sums of sum_a cs_a s_a + cy_a y_a over
+// slot groups; stage 8 (lbfgs_post_kernel) adds them in a fixed order to -gamma g and runs the
 // line minimiser's reset / first step, or the plain step.
 constexpr int kCombThreads = 128;
 
@@ -586,7 +593,6 @@ __global__ void __launch_bounds__(kGramThreads) lbfgs_gram_kernel(double *state,
       for (int w = 0; w < kGramThreads / 32; w++) t += red[w][threadIdx.x];
       const int sa = ((ne - (k0 + i)) % mem + mem) % mem;
       if (c == 0) {
-        v.sy[(size_t)sa * mem + ne] = t;
         v.syt[(size_t)ne * mem + sa] = t;
         if (sa == ne) v.rho[ne] = 1.0 / fmax(fabs(t), kEps);
       } else if (c == 1) {
@@ -601,111 +607,102 @@ __global__ void __launch_bounds__(kGramThreads) lbfgs_gram_kernel(double *state,
   }
 }
 
-__global__ void __launch_bounds__(kRecThreads) lbfgs_recur_kernel(double *state, size_t stride,
-                                                                  LbParams P) {
-  extern __shared__ double rs[];  // A[mem] (loop 1), C[mem] (loop 2), R[mem] (rho by k)
-  __shared__ double D[kRecBlock][kRecBlock];
-  __shared__ double s_gamma;
-  LbView v = lb_view(state + (size_t)blockIdx.x * stride, P.n, P.mem);
+// slot of age k (0 = oldest) among `used` written slots ending at ne
+__device__ __forceinline__ int age_slot(int k, int ne, int used, int mem) {
+  const int s = ne - (used - 1 - k);
+  return s < 0 ? s + mem : s;
+}
+
+// sum over ages kb in [k0, k1) of row[slot(kb)] * x(kb), lanes over kb, on every lane
+template <typename F>
+__device__ __forceinline__ double warp_row_dot(const double *row, int k0, int k1, int ne, int used,
+                                               int mem, F x) {
+  double acc = 0.0;
+  for (int kb = k0 + (threadIdx.x & 31); kb < k1; kb += 32)
+    acc = fma(row[age_slot(kb, ne, used, mem)], x(kb), acc);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  return acc;
+}
+
+// new column of R^-1 (rows older than the newest pair) and its diagonal; gamma
+__global__ void __launch_bounds__(32 * kGemvWarps) lbfgs_rinv_kernel(double *state, size_t stride,
+                                                                     LbParams P) {
+  LbView v = lb_view(state + (size_t)blockIdx.y * stride, P.n, P.mem);
   if ((int)v.sc[SC_PHASE] != 1) return;
-  const int mem = P.mem;
-  const int ne = (int)v.sc[SC_NE], used = (int)v.sc[SC_USED];
-  double *A = rs, *C = rs + mem, *R = rs + 2 * mem;
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  // loop-1 order k -> slot; loop-2 order l is loop-1 order used - 1 - l
-  auto slot1 = [&](int k) { return ((ne - k) % mem + mem) % mem; };
-  for (int k = tid; k < used; k += kRecThreads) {
-    const int sk = slot1(k);
-    R[k] = v.rho[sk];
-    A[k] = v.ps[sk];
-  }
-  if (tid == 0) {
-    const int iter = (int)v.sc[SC_ITER];
-    s_gamma = iter == 1 ? 1.0
-                        : v.sy[(size_t)ne * mem + ne] / fmax(v.yg[(size_t)ne * mem + ne], kEps);
-  }
-  __syncthreads();
-  // ---- loop 1: A[k] = s_k.g - sum_{j<k} alpha_j s_k.y_j;  alpha_k = rho_k A[k]
-  for (int jb = 0; jb < used; jb += kRecBlock) {
-    const int nb = min(kRecBlock, used - jb);
-    for (int e = tid; e < kRecBlock * kRecBlock; e += kRecThreads) {
-      const int jj = e / kRecBlock, i = e % kRecBlock;
-      D[jj][i] = (jj < nb && i < nb && i > jj)
-                     ? v.syt[(size_t)slot1(jb + jj) * mem + slot1(jb + i)] : 0.0;
+  const int mem = P.mem, ne = (int)v.sc[SC_NE], used = (int)v.sc[SC_USED];
+  const int ka = blockIdx.x * kGemvWarps + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+  if (ka >= used) return;
+  const double rho_ne = v.rho[ne];
+  if (ka == used - 1) {
+    if (lane == 0) {
+      v.rinv[(size_t)ne * mem + ne] = rho_ne;
+      v.rinvt[(size_t)ne * mem + ne] = rho_ne;
+      const int iter = (int)v.sc[SC_ITER];
+      v.sc[SC_GAMMA] = iter == 1 ? 1.0
+                                 : v.syt[(size_t)ne * mem + ne] /
+                                       fmax(v.yg[(size_t)ne * mem + ne], kEps);
     }
-    __syncthreads();
-    if (warp == 0) {
-      const int k = jb + lane;
-      const double rk = lane < nb ? R[k] : 0.0;
-      double b = lane < nb ? A[k] : 0.0;
-      for (int jj = 0; jj < nb; jj++) {
-        const double aj = __shfl_sync(0xffffffffu, rk * b, jj);  // row jj is final
-        if (lane > jj) b = fma(-aj, D[jj][lane], b);
-      }
-      if (lane < nb) A[k] = rk * b;  // alpha_k
-    }
-    __syncthreads();
-    for (int k = jb + nb + tid; k < used; k += kRecThreads) {
-      const int sk = slot1(k);
-      double acc = 0.0;
-#pragma unroll 8
-      for (int jj = 0; jj < nb; jj++)
-        acc = fma(A[jb + jj], v.syt[(size_t)slot1(jb + jj) * mem + sk], acc);
-      A[k] -= acc;
-    }
-    __syncthreads();
+    return;
   }
-  const double gamma = s_gamma;
-  // ---- r = gamma q: C[l] = gamma (y_l.g - sum_j alpha_j y_l.y_j)
-  for (int l = tid; l < used; l += kRecThreads) {
-    const int sl = slot1(used - 1 - l);
-    double acc = 0.0;
-#pragma unroll 4
-    for (int k = 0; k < used; k++) acc = fma(A[k], v.yg[(size_t)slot1(k) * mem + sl], acc);
-    C[l] = gamma * (v.py[sl] - acc);
+  const int sa = age_slot(ka, ne, used, mem);
+  const double *c = v.syt + (size_t)ne * mem;  // c[b] = s_b . y_ne
+  const double t = warp_row_dot(v.rinv + (size_t)sa * mem, ka, used - 1, ne, used, mem,
+                                [&](int kb) { return c[age_slot(kb, ne, used, mem)]; });
+  if (lane == 0) {
+    const double x = -t * rho_ne;
+    v.rinv[(size_t)sa * mem + ne] = x;
+    v.rinvt[(size_t)ne * mem + sa] = x;
   }
-  __syncthreads();
-  // ---- loop 2: C[l] = y_l.r before step l; delta_l = alpha_l - rho_l C[l];
-  //      C[l'] += delta_l s_l.y_l' for the later rows l'
-  for (int jb = 0; jb < used; jb += kRecBlock) {
-    const int nb = min(kRecBlock, used - jb);
-    for (int e = tid; e < kRecBlock * kRecBlock; e += kRecThreads) {
-      const int jj = e / kRecBlock, i = e % kRecBlock;
-      D[jj][i] = (jj < nb && i < nb && i > jj)
-                     ? v.sy[(size_t)slot1(used - 1 - (jb + jj)) * mem + slot1(used - 1 - (jb + i))]
-                     : 0.0;
-    }
-    __syncthreads();
-    if (warp == 0) {
-      const int l = jb + lane;
-      const int k = used - 1 - l;
-      const double rl = lane < nb ? R[k] : 0.0, al = lane < nb ? A[k] : 0.0;
-      double c = lane < nb ? C[l] : 0.0;
-      for (int jj = 0; jj < nb; jj++) {
-        const double dj = __shfl_sync(0xffffffffu, al - rl * c, jj);  // row jj is final
-        if (lane > jj) c = fma(dj, D[jj][lane], c);
-      }
-      if (lane < nb) C[l] = al - rl * c;  // delta_l
-    }
-    __syncthreads();
-    for (int l = jb + nb + tid; l < used; l += kRecThreads) {
-      const int sl = slot1(used - 1 - l);
-      double acc = 0.0;
-#pragma unroll 8
-      for (int jj = 0; jj < nb; jj++)
-        acc = fma(C[jb + jj], v.sy[(size_t)slot1(used - 1 - (jb + jj)) * mem + sl], acc);
-      C[l] += acc;
-    }
-    __syncthreads();
+}
+
+// v1 = R^-1 (S^T g), kept in alph (by slot)
+__global__ void __launch_bounds__(32 * kGemvWarps) lbfgs_v1_kernel(double *state, size_t stride,
+                                                                   LbParams P) {
+  LbView v = lb_view(state + (size_t)blockIdx.y * stride, P.n, P.mem);
+  if ((int)v.sc[SC_PHASE] != 1) return;
+  const int mem = P.mem, ne = (int)v.sc[SC_NE], used = (int)v.sc[SC_USED];
+  const int ka = blockIdx.x * kGemvWarps + (threadIdx.x >> 5);
+  if (ka >= used) return;
+  const int sa = age_slot(ka, ne, used, mem);
+  const double t = warp_row_dot(v.rinv + (size_t)sa * mem, ka, used, ne, used, mem,
+                                [&](int kb) { return v.ps[age_slot(kb, ne, used, mem)]; });
+  if ((threadIdx.x & 31) == 0) v.alph[sa] = t;
+}
+
+// v3 = D v1 + gamma (Y^T Y) v1 - gamma Y^T g
+__global__ void __launch_bounds__(32 * kGemvWarps) lbfgs_v2_kernel(double *state, size_t stride,
+                                                                   LbParams P) {
+  LbView v = lb_view(state + (size_t)blockIdx.y * stride, P.n, P.mem);
+  if ((int)v.sc[SC_PHASE] != 1) return;
+  const int mem = P.mem, ne = (int)v.sc[SC_NE], used = (int)v.sc[SC_USED];
+  const int ka = blockIdx.x * kGemvWarps + (threadIdx.x >> 5);
+  if (ka >= used) return;
+  const int sa = age_slot(ka, ne, used, mem);
+  const double gamma = v.sc[SC_GAMMA];
+  const double t = warp_row_dot(v.yg + (size_t)sa * mem, 0, used, ne, used, mem,
+                                [&](int kb) { return v.alph[age_slot(kb, ne, used, mem)]; });
+  if ((threadIdx.x & 31) == 0) {
+    const double d = fmax(fabs(v.syt[(size_t)sa * mem + sa]), kEps);
+    v.v3[sa] = d * v.alph[sa] + gamma * t - gamma * v.py[sa];
   }
-  // ---- dir = -r = -gamma g + gamma sum alpha_k y_k - sum delta_l s_l
-  for (int k = tid; k < used; k += kRecThreads) {
-    const int sk = slot1(k);
-    v.cy[sk] = gamma * A[k];
-    v.cs[sk] = -C[used - 1 - k];
-    v.alph[sk] = A[k];
+}
+
+// p = R^-T v3; the direction's coefficients cs = -p, cy = gamma v1
+__global__ void __launch_bounds__(32 * kGemvWarps) lbfgs_p_kernel(double *state, size_t stride,
+                                                                  LbParams P) {
+  LbView v = lb_view(state + (size_t)blockIdx.y * stride, P.n, P.mem);
+  if ((int)v.sc[SC_PHASE] != 1) return;
+  const int mem = P.mem, ne = (int)v.sc[SC_NE], used = (int)v.sc[SC_USED];
+  const int kb = blockIdx.x * kGemvWarps + (threadIdx.x >> 5);
+  if (kb >= used) return;
+  const int sb = age_slot(kb, ne, used, mem);
+  const double t = warp_row_dot(v.rinvt + (size_t)sb * mem, 0, kb + 1, ne, used, mem,
+                                [&](int ka) { return v.v3[age_slot(ka, ne, used, mem)]; });
+  if ((threadIdx.x & 31) == 0) {
+    v.cs[sb] = -t;
+    v.cy[sb] = v.sc[SC_GAMMA] * v.alph[sb];
   }
-  if (tid == 0) v.sc[SC_GAMMA] = gamma;
 }
 
 __global__ void __launch_bounds__(kCombThreads) lbfgs_combine_kernel(double *state, size_t stride,
@@ -1059,14 +1056,16 @@ int run_optimizer_step(fnetg_ctx *ctx) {
     double *st = ctx->d_opt.as<double>();
     const size_t stride = ctx->opt_stride;
     const int mem = ctx->opt_mem;
-    const size_t rec_smem = sizeof(double) * 3 * (size_t)mem;
-    FNETG_CUDA(raise_smem_limit((const void *)lbfgs_recur_kernel, rec_smem));
+    const dim3 gemv(ceil_div(mem, kGemvWarps), ctx->nsp);
     LaunchScope ls(ctx, "optimizer");
     lbfgs_pre_kernel<<<ctx->nsp, kOptThreads, 0, ctx->stream>>>(
         st, stride, ctx->d_params64.as<double>(), ctx->d_grad64.as<double>(), P, conv);
     lbfgs_gram_kernel<<<dim3(ceil_div(mem, kGramSlots), ctx->nsp), kGramThreads, 0,
                         ctx->stream>>>(st, stride, P);
-    lbfgs_recur_kernel<<<ctx->nsp, kRecThreads, rec_smem, ctx->stream>>>(st, stride, P);
+    lbfgs_rinv_kernel<<<gemv, 32 * kGemvWarps, 0, ctx->stream>>>(st, stride, P);
+    lbfgs_v1_kernel<<<gemv, 32 * kGemvWarps, 0, ctx->stream>>>(st, stride, P);
+    lbfgs_v2_kernel<<<gemv, 32 * kGemvWarps, 0, ctx->stream>>>(st, stride, P);
+    lbfgs_p_kernel<<<gemv, 32 * kGemvWarps, 0, ctx->stream>>>(st, stride, P);
     lbfgs_combine_kernel<<<dim3((unsigned)ceil_div(ctx->nparams, (int64_t)kCombThreads),
                                 ctx->nsp, kLbSplit),
                            kCombThreads, 0, ctx->stream>>>(st, stride, P);

@@ -256,7 +256,7 @@ int fnetg_synchronize(fnetg_ctx *ctx);
  * the context's stream, *site receives the first failed index check since the last call
  * (file code x 100000 + source line; the access it guarded was skipped) and the record is
  * cleared; 0 = every check passed.  The default build has no checks and always gives 0.  No
- * counterpart in the reference (its debug builds check array bounds with -fcheck=all). */
+ * counterpart in the reference beyond its debug builds' -fbounds-check (sys/gnu.cmake:33). */
 int fnetg_check_status(fnetg_ctx *ctx, int32_t *site);
 
 #ifdef __cplusplus
