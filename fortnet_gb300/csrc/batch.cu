@@ -68,8 +68,12 @@ struct TcNet {
   uint32_t w_bytes, w_bytes0, w_bytes1;
   uint32_t off_w1f, off_w1b, off_w0b, off_w2;  // offsets inside the weight block
   // shared-memory plan (bytes) of the training kernel (and of the Jacobian kernel, whose
-  // weights end at jm_total)
-  uint32_t sm_x, sm_a1, sm_a2, sm_d2, sm_d1, sm_d3, sm_w, sm_total, jm_total;
+  // weights end at jm_total): features | activations of both layers (exactly their K columns:
+  // the 128-wide MN-major reads of the weight-gradient products run on into the next buffer) |
+  // adjoints | weights | second feature buffer (the next tile's features, loaded while the
+  // current tile computes; prefetch = 0 where it does not fit)
+  uint32_t sm_x, sm_a1, sm_a2, sm_d2, sm_d1, sm_d3, sm_w, sm_x1, sm_total, jm_total;
+  int prefetch;
   // shared-memory plan of the forward kernel: features, first activations, the weights it
   // reads; small enough for two CTAs per SM
   uint32_t fm_x, fm_a1, fm_w, fm_total;
@@ -104,10 +108,10 @@ template <int HP> TcNet make_net(fnetg_ctx *ctx) {
   uint32_t o = 0;
   n.sm_x = o;
   o += n.x_bytes;
-  n.sm_a1 = o;  // 128 columns: the MN-major M tile of a_1^T delta_2 reads them all
-  o += kRows * kRows * 2;
+  n.sm_a1 = o;
+  o += kRows * n.K1p * 2;
   n.sm_a2 = o;
-  o += kRows * kRows * 2;
+  o += kRows * n.K2p * 2;
   n.sm_d2 = o;
   o += kRows * HP * 2;
   n.sm_d1 = o;
@@ -115,8 +119,15 @@ template <int HP> TcNet make_net(fnetg_ctx *ctx) {
   n.sm_d3 = o;
   o += kRows * 16 * 2;
   n.sm_w = o;
-  n.sm_total = o + n.w_bytes1;
+  n.sm_x1 = o + n.w_bytes1;
   n.jm_total = o + n.w_bytes;
+  {
+    // the 128-column reads of a_1 and a_2 stay inside the allocation
+    const uint32_t reach = std::max(n.sm_a1, n.sm_a2) + kRows * kRows * 2;
+    const uint32_t with_x1 = std::max(n.sm_x1 + n.x_bytes, reach);
+    n.prefetch = with_x1 <= 227u * 1024u - 1024u ? 1 : 0;
+    n.sm_total = n.prefetch ? with_x1 : std::max(n.sm_x1, reach);
+  }
   o = 0;
   n.fm_x = o;
   o += n.x_bytes;
@@ -307,7 +318,7 @@ __device__ void flush_grads(const TcNet &n, float *gp, uint32_t tm, uint32_t lan
 template <int HP, int MODE>
 __global__ void __launch_bounds__(kThreads, 1) tc_mlp_kernel(TcArgs a) {
   extern __shared__ __align__(1024) unsigned char sm[];
-  __shared__ uint64_t mb_load, mb_mma;
+  __shared__ uint64_t mb_load, mb_mma, mb_x[2];
   __shared__ uint32_t tmem_base;
   const TcNet &n = a.net;
   const int tid = threadIdx.x, warp = tid >> 5;
@@ -317,10 +328,16 @@ __global__ void __launch_bounds__(kThreads, 1) tc_mlp_kernel(TcArgs a) {
   unsigned char *X = sm + (MODE == 0 ? n.fm_x : n.sm_x), *A1 = sm + (MODE == 0 ? n.fm_a1 : n.sm_a1),
                 *A2 = sm + n.sm_a2, *D2 = sm + n.sm_d2, *D1 = sm + n.sm_d1, *D3 = sm + n.sm_d3,
                 *W = sm + (MODE == 0 ? n.fm_w : n.sm_w);
+  // training: the next tile's features are requested into the other buffer while the current
+  // tile computes (mb_x[b] counts buffer b's copy; mb_load the weights)
+  const bool pf = MODE == 1 && n.prefetch;
+  unsigned char *const Xb0 = X, *const Xb1 = sm + n.sm_x1;
   const float *w2 = reinterpret_cast<const float *>(W + n.off_w2);
   if (tid == 0) {
     tc::mbar_init(&mb_load, 1);
     tc::mbar_init(&mb_mma, 1);
+    tc::mbar_init(&mb_x[0], 1);
+    tc::mbar_init(&mb_x[1], 1);
     tc::mbar_fence_init();
   }
   if (warp == 0) tc::tmem_alloc(&tmem_base, kCols);
@@ -329,14 +346,15 @@ __global__ void __launch_bounds__(kThreads, 1) tc_mlp_kernel(TcArgs a) {
   tc::fence_after_sync();
   const uint32_t tm = tmem_base;
   const uint32_t lane_off = (uint32_t)(warp * 32) << 16;
-  const uint32_t sX = tc::smem_u32(X), sA1 = tc::smem_u32(A1), sA2 = tc::smem_u32(A2),
+  const uint32_t sA1 = tc::smem_u32(A1), sA2 = tc::smem_u32(A2),
                  sD2 = tc::smem_u32(D2), sD1 = tc::smem_u32(D1), sD3 = tc::smem_u32(D3),
                  sW = tc::smem_u32(W);
   // K-major operands (tc.cuh): lbo = 16 * rows, sbo = 128; MN-major: lbo = 128, sbo = 16 * rows
   const uint32_t id_h = tc::idesc_bf16(kRows, HP, 0, 0);
   const uint32_t id_g = tc::idesc_bf16(kRows, HP, 1, 1);
   const uint32_t id_g2 = tc::idesc_bf16(kRows, 16, 1, 1);
-  uint32_t ph_load = 0, ph_mma = 0;
+  uint32_t ph_load = 0, ph_mma = 0, ph_x0 = 0, ph_x1 = 0;
+  bool pend_x0 = false, pend_x1 = false, pend_w = false;  // copies requested, not yet waited for
   const int64_t nt = a.t1 - a.t0;
   const int64_t my0 = a.t0 + nt * blockIdx.x / gridDim.x;
   const int64_t my1 = a.t0 + nt * (blockIdx.x + 1) / gridDim.x;
@@ -344,6 +362,7 @@ __global__ void __launch_bounds__(kThreads, 1) tc_mlp_kernel(TcArgs a) {
   bool gacc = false;  // the TMEM gradient accumulators hold data of cur_sp
   uint64_t touched = 0;
   bool failed = false;
+  int buf = 0;
 
   // gradient accumulators of cur_sp -> this CTA's partial slot (reference parameter order)
   auto flush = [&]() {
@@ -351,7 +370,20 @@ __global__ void __launch_bounds__(kThreads, 1) tc_mlp_kernel(TcArgs a) {
                     tid);
     touched |= 1ull << cur_sp;
   };
+  // after a wait gave up: the copies still in flight, each once more with a limit
+  auto drain = [&]() {
+    if (pend_w) tc::mbar_wait(&mb_load, ph_load);
+    if (pend_x0) tc::mbar_wait(&mb_x[0], ph_x0);
+    if (pend_x1) tc::mbar_wait(&mb_x[1], ph_x1);
+  };
 
+  if (pf && my0 < my1) {
+    if (tid == 0) {
+      tc::mbar_expect_tx(&mb_x[0], n.x_bytes);
+      tc::bulk_g2s(Xb0, a.x + my0 * (int64_t)n.x_bytes, n.x_bytes, &mb_x[0]);
+    }
+    pend_x0 = true;
+  }
   for (int64_t t = my0; t < my1; t++) {
     const int sp = a.tile_sp[t];
     const bool new_sp = sp != cur_sp;
@@ -361,21 +393,54 @@ __global__ void __launch_bounds__(kThreads, 1) tc_mlp_kernel(TcArgs a) {
     }
     tc::fence_before_sync();
     __syncthreads();
+    const bool more = pf && t + 1 < my1;
     if (tid == 0) {
-      tc::mbar_expect_tx(&mb_load, n.x_bytes + (new_sp ? wload : 0u));
-      tc::bulk_g2s(X, a.x + t * (int64_t)n.x_bytes, n.x_bytes, &mb_load);
-      if (new_sp) tc::bulk_g2s(W, a.w + (int64_t)sp * n.w_bytes, wload, &mb_load);
+      if (pf) {
+        if (new_sp) {
+          tc::mbar_expect_tx(&mb_load, wload);
+          tc::bulk_g2s(W, a.w + (int64_t)sp * n.w_bytes, wload, &mb_load);
+        }
+        // the other buffer's last reader (the previous tile's last MMA) has completed
+        if (more) {
+          tc::mbar_expect_tx(&mb_x[buf ^ 1], n.x_bytes);
+          tc::bulk_g2s(buf ? Xb0 : Xb1, a.x + (t + 1) * (int64_t)n.x_bytes, n.x_bytes,
+                       &mb_x[buf ^ 1]);
+        }
+      } else {
+        tc::mbar_expect_tx(&mb_load, n.x_bytes + (new_sp ? wload : 0u));
+        tc::bulk_g2s(X, a.x + t * (int64_t)n.x_bytes, n.x_bytes, &mb_load);
+        if (new_sp) tc::bulk_g2s(W, a.w + (int64_t)sp * n.w_bytes, wload, &mb_load);
+      }
+    }
+    if (pf) {
+      pend_w = new_sp;
+      if (more) (buf ? pend_x0 : pend_x1) = true;
+    } else {
+      pend_w = true;
     }
     cur_sp = sp;
     const int row = tid;
     const int atom = tile_atom(a.tile_atoms, t * kRows + row, a.natoms);
     const float delta3 = (MODE == 1 && atom >= 0) ? (float)a.delta[atom] : 0.f;
-    if (!wait_all(&mb_load, ph_load)) {
-      tc::mbar_wait(&mb_load, ph_load);  // the copies in flight, once more with a limit
-      failed = true;
-      break;
+    if (pf) {
+      if (!wait_all(&mb_x[buf], buf ? ph_x1 : ph_x0)) {
+        drain();
+        failed = true;
+        break;
+      }
+      (buf ? ph_x1 : ph_x0) ^= 1;
+      (buf ? pend_x1 : pend_x0) = false;
     }
-    ph_load ^= 1;
+    if (pend_w) {
+      if (!wait_all(&mb_load, ph_load)) {
+        drain();
+        failed = true;
+        break;
+      }
+      ph_load ^= 1;
+      pend_w = false;
+    }
+    const uint32_t sX = tc::smem_u32(pf && buf ? Xb1 : Xb0);
     // ---- layer 1: Z1 = X W0 (+ bias through the constant column)
     if (tid == 0) {
       tc::fence_after_sync();
@@ -384,7 +449,7 @@ __global__ void __launch_bounds__(kThreads, 1) tc_mlp_kernel(TcArgs a) {
                      tc::smem_desc(sW + ks * 2 * 16 * HP, 16 * HP, 128), id_h, ks > 0);
       tc::mma_commit(&mb_mma);
     }
-    if (!wait_all(&mb_mma, ph_mma)) { failed = true; break; }
+    if (!wait_all(&mb_mma, ph_mma)) { drain(); failed = true; break; }
     ph_mma ^= 1;
     tc::fence_after_sync();
     float f1[HP];
@@ -416,7 +481,7 @@ __global__ void __launch_bounds__(kThreads, 1) tc_mlp_kernel(TcArgs a) {
                      ks > 0);
       tc::mma_commit(&mb_mma);
     }
-    if (!wait_all(&mb_mma, ph_mma)) { failed = true; break; }
+    if (!wait_all(&mb_mma, ph_mma)) { drain(); failed = true; break; }
     ph_mma ^= 1;
     tc::fence_after_sync();
     {
@@ -467,7 +532,7 @@ __global__ void __launch_bounds__(kThreads, 1) tc_mlp_kernel(TcArgs a) {
       }
       tc::mma_commit(&mb_mma);
     }
-    if (!wait_all(&mb_mma, ph_mma)) { failed = true; break; }
+    if (!wait_all(&mb_mma, ph_mma)) { drain(); failed = true; break; }
     ph_mma ^= 1;
     tc::fence_after_sync();
     {
@@ -496,10 +561,11 @@ __global__ void __launch_bounds__(kThreads, 1) tc_mlp_kernel(TcArgs a) {
                        tc::smem_desc(sD1 + ks * 256, 128, 16 * kRows), id_g, gacc || ks > 0);
       tc::mma_commit(&mb_mma);
     }
-    if (!wait_all(&mb_mma, ph_mma)) { failed = true; break; }
+    if (!wait_all(&mb_mma, ph_mma)) { drain(); failed = true; break; }
     ph_mma ^= 1;
     tc::fence_after_sync();
     gacc = true;
+    if (pf) buf ^= 1;
   }
   if (MODE == 1 && !failed) {
     if (gacc) flush();
@@ -1024,7 +1090,18 @@ __global__ void __launch_bounds__(kRedThreads) tc_reduce_kernel(const float *gpa
   if (q < n.nparams && (q < n.woff3 || q >= n.boff1)) {
     const float *p = gpart + (int64_t)s * n.nparams + q;
     const int64_t stride = (int64_t)nsp * n.nparams;
-    for (int b = r; b < nblk; b += kRedSplit)
+    // four CTAs' partials requested together (a partial a CTA did not write is loaded but not
+    // added), summed in CTA order
+    int b = r;
+    for (; b + 3 * kRedSplit < nblk; b += 4 * kRedSplit) {
+      const float v0 = p[b * stride], v1 = p[(b + kRedSplit) * stride],
+                  v2 = p[(b + 2 * kRedSplit) * stride], v3 = p[(b + 3 * kRedSplit) * stride];
+      if (flag[b]) acc += (double)v0;
+      if (flag[b + kRedSplit]) acc += (double)v1;
+      if (flag[b + 2 * kRedSplit]) acc += (double)v2;
+      if (flag[b + 3 * kRedSplit]) acc += (double)v3;
+    }
+    for (; b < nblk; b += kRedSplit)
       if (flag[b]) acc += (double)p[b * stride];
   }
   part[r][k] = acc;

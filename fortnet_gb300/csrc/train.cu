@@ -81,9 +81,18 @@ __global__ void __launch_bounds__(kLossThreads) loss_cta_kernel(LossArgs a) {
   if (a.ngt > 0) {
     double lsum = 0.0;
     for (int o = 0; o < a.ngt; o++) {
-      double sum = 0.0;
-      for (int64_t at = a0 + threadIdx.x; at < a1; at += kLossThreads) sum += a.out[at * a.nout + o];
-      sum = cta_sum(sum, sh);
+      // four outputs requested together per thread (large structures: 2,048 atoms are 16 per
+      // thread), partial sums combined in a fixed order
+      double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
+      int64_t at = a0 + threadIdx.x;
+      for (; at + 3 * kLossThreads < a1; at += 4 * kLossThreads) {
+        s0 += a.out[at * a.nout + o];
+        s1 += a.out[(at + kLossThreads) * a.nout + o];
+        s2 += a.out[(at + 2 * kLossThreads) * a.nout + o];
+        s3 += a.out[(at + 3 * kLossThreads) * a.nout + o];
+      }
+      for (; at < a1; at += kLossThreads) s0 += a.out[at * a.nout + o];
+      double sum = cta_sum((s0 + s1) + (s2 + s3), sh);
       const double t = a.gt[(int64_t)s * a.ngt + o];
       const double lg = lossgrad(a.loss, sum, t);
       lsum += loss_term(a.loss, sum, t);
