@@ -688,8 +688,10 @@ def serving_leg(args):
     """The C5 serving stream through the public service API (include/fnetg_serve.h): Poisson
     arrivals at 2,000 req/s, each request one three-species periodic structure of 16-4,096
     atoms (log-uniform) drawn from a pool of distinct structures, energies + forces of the
-    trained C4 model (66-64-64-1, FP32 kernels).  Latency = completion - scheduled arrival, so a
-    late submission counts against the service."""
+    trained C4 model (66-64-64-1): once with the plain FP32 kernels, once with the network
+    passes on the tensor cores (BF16 forward and input Jacobian, FP32 ACSF and forces).
+    Latency = completion - scheduled arrival, so a late submission counts against the
+    service."""
     from fortnet_gb300 import api, synthetic
 
     cfg = synthetic.CONFIGS["C5"]
@@ -703,73 +705,111 @@ def serving_leg(args):
     warm, n = args.serve_warmup, args.serve_requests
     arr = synthetic.arrivals(warm + n, seed=cfg.seed)
     pick = np.random.default_rng(cfg.seed + 11).integers(0, len(reqs), size=warm + n)
+    import gc
     import queue as _queue
 
     sys.setswitchinterval(0.0002)  # the submitter spins before each arrival
-    import gc
 
-    gc.collect()
-    gc.disable()  # no collector pauses in the load generator while the stream runs
-    pending = _queue.Queue()
-    lat = np.zeros(warm + n)
-    done_ns = np.zeros(warm + n, dtype=np.int64)
-    with api.Server(cfg.atomic_numbers, funcs, zprec, dims, "tanh", params, precision=api.FP32,
-                    lanes=args.serve_lanes) as srv:
-        def waiter():
-            for _ in range(warm + n):
-                k, t, na = pending.get()
-                _, _, lat[k] = srv.wait(t, na, timeout=120.0)
-                done_ns[k] = srv.clock_ns()
+    def stream(tensor_cores):
+        gc.collect()
+        gc.disable()  # no collector pauses in the load generator while the stream runs
+        pending = _queue.Queue()
+        lat = np.zeros(warm + n)
+        done_ns = np.zeros(warm + n, dtype=np.int64)
+        with api.Server(cfg.atomic_numbers, funcs, zprec, dims, "tanh", params,
+                        precision=api.FP32, lanes=args.serve_lanes,
+                        tensor_cores=tensor_cores) as srv:
+            def waiter():
+                for _ in range(warm + n):
+                    k, t, na = pending.get()
+                    _, _, lat[k] = srv.wait(t, na, timeout=120.0)
+                    done_ns[k] = srv.clock_ns()
 
-        th = threading.Thread(target=waiter)
-        th.start()
-        t0 = srv.clock_ns() + 50_000_000
-        for k in range(warm + n):
-            target = t0 + int(arr[k] * 1e9)
-            while True:
-                dt = target - srv.clock_ns()
-                if dt <= 0:
-                    break
-                if dt > 300_000:
-                    time.sleep((dt - 200_000) / 1e9)
-            an, xyz, lv = reqs[pick[k]]
-            t, na = srv.submit(an, xyz, lv, arrival_ns=target)
-            pending.put((k, t, na))
-        th.join()
-        gc.enable()
-        st = srv.stats()
-    # FP32 service against an FP64 run of the same kernels on the first pool structures
+            th = threading.Thread(target=waiter)
+            th.start()
+            t0 = srv.clock_ns() + 50_000_000
+            for k in range(warm + n):
+                target = t0 + int(arr[k] * 1e9)
+                while True:
+                    dt = target - srv.clock_ns()
+                    if dt <= 0:
+                        break
+                    if dt > 300_000:
+                        time.sleep((dt - 200_000) / 1e9)
+                an, xyz, lv = reqs[pick[k]]
+                t, na = srv.submit(an, xyz, lv, arrival_ns=target)
+                pending.put((k, t, na))
+            th.join()
+            gc.enable()
+            st = srv.stats()
+        meas = lat[warm:]
+        atoms = int(sum(len(reqs[pick[k]][0]) for k in range(warm, warm + n)))
+        span = (done_ns[warm:].max() - (t0 + int(arr[warm] * 1e9))) / 1e9
+        return {
+            "p50_ms": round(float(np.percentile(meas, 50)), 3),
+            "p99_ms": round(float(np.percentile(meas, 99)), 3),
+            "mean_ms": round(float(np.mean(meas)), 3), "max_ms": round(float(np.max(meas)), 3),
+            "atoms_per_s": round(atoms / span, 1),
+            "offered_atoms_per_s": round(atoms / (arr[-1] - arr[warm]), 1),
+            "lanes": st["lanes"], "batches": st["batches"],
+            "mean_batch_requests": round(st["requests"] / max(st["batches"], 1), 2),
+            "max_batch_requests": st["max_batch_requests"], "max_in_flight": st["max_in_flight"],
+            "max_batch_ms": round(1e3 * st["max_batch_s"], 3),
+            "device_bytes": st["device_bytes"]}
+
+    plain = stream(False)
+    tc = stream(True)
+    # both services against an FP64 run of the plain kernels on the first pool structures;
+    # energies relative to sum_i |o_i| of the FP64 atomic outputs
     chk = list(range(min(16, len(reqs))))
     res = {}
-    for prec in (api.FP32, api.FP64):
+    for key, prec, tcores in (("fp32", api.FP32, False), ("bf16", api.FP32, True),
+                              ("fp64", api.FP64, False)):
         with api.Server(cfg.atomic_numbers, funcs, zprec, dims, "tanh", params, precision=prec,
-                        lanes=1) as s2:
+                        lanes=1, tensor_cores=tcores) as s2:
             ts = [s2.submit(*reqs[k]) for k in chk]
-            res[prec] = [s2.wait(t, na, timeout=120.0) for t, na in ts]
-    e_err = max(abs(a[0][0] - b[0][0]) / abs(b[0][0]) for a, b in zip(res[api.FP32], res[api.FP64]))
-    f_err = max(float(np.max(np.abs(a[1] - b[1])) / np.max(np.abs(b[1])))
-                for a, b in zip(res[api.FP32], res[api.FP64]))
-    meas = lat[warm:]
-    atoms = int(sum(len(reqs[pick[k]][0]) for k in range(warm, warm + n)))
-    span = (done_ns[warm:].max() - (t0 + int(arr[warm] * 1e9))) / 1e9
+            res[key] = [s2.wait(t, na, timeout=120.0) for t, na in ts]
+    sub = first_structures(pool, len(chk))
+    with api.Context(api.FP64) as c:
+        c.upload(sub)
+        c.set_species(sub.species)
+        c.set_gfunctions(funcs)
+        c.acsf(download=False)
+        c.zscore(zprec=zprec)
+        c.set_network(dims, "tanh", params)
+        at64, _ = c.predict(atomic=True)
+    mag = np.add.reduceat(np.abs(at64[:, 0]), sub.atom_offsets[:-1])
+
+    def errs(key):
+        e = max(abs(a[0][0] - b[0][0]) / m for a, b, m in zip(res[key], res["fp64"], mag))
+        f = max(float(np.max(np.abs(a[1] - b[1])) / np.max(np.abs(b[1])))
+                for a, b in zip(res[key], res["fp64"]))
+        return {"structures": len(chk), "energy_rel": float(f"{e:.3g}"),
+                "energy_metric": "|E - E64| / sum_i |o_i,64|", "force_rel_of_max": float(f"{f:.3g}")}
+
     return {
         "workload": f"C5: Poisson {synthetic.C5_RATE:.0f} req/s, 16-4096 atoms log-uniform "
                     f"(pool of {pool.nstruct} structures), model 66-64-64-1 tanh, energies + forces",
         "requests": n, "warmup_requests": warm, "dtype": "f32",
-        "p50_ms": round(float(np.percentile(meas, 50)), 3),
-        "p99_ms": round(float(np.percentile(meas, 99)), 3),
-        "mean_ms": round(float(np.mean(meas)), 3), "max_ms": round(float(np.max(meas)), 3),
-        "atoms_per_s": round(atoms / span, 1),
-        "offered_atoms_per_s": round(atoms / (arr[-1] - arr[warm]), 1),
-        "lanes": st["lanes"], "batches": st["batches"],
-        "mean_batch_requests": round(st["requests"] / max(st["batches"], 1), 2),
-        "max_batch_requests": st["max_batch_requests"], "max_in_flight": st["max_in_flight"],
-        "max_batch_ms": round(1e3 * st["max_batch_s"], 3),
-        "device_bytes": st["device_bytes"],
-        "fp32_vs_fp64": {"structures": len(chk), "energy_rel": float(f"{e_err:.3g}"),
-                         "force_rel_of_max": float(f"{f_err:.3g}")},
+        **plain,
+        "fp32_vs_fp64": errs("fp32"),
+        "tensor_cores": {"dtype": "bf16 network passes, f32 ACSF and forces", **tc,
+                         "vs_fp64": errs("bf16")},
         "model": model_rec,
     }
+
+
+def first_structures(ds, k):
+    """The first k structures of a dataset."""
+    from fortnet_gb300.fnetdata import Dataset
+
+    off = ds.atom_offsets[:k + 1]
+    n = int(off[-1])
+    return Dataset(atom_offsets=off, coords=ds.coords[:n], atnum=ds.atnum[:n],
+                   species=ds.species[:n], periodic=ds.periodic[:k], latvecs=ds.latvecs[:k],
+                   atomic_numbers=ds.atomic_numbers, weights=ds.weights[:k],
+                   atomic_weights=ds.atomic_weights[:n], global_targets=ds.global_targets[:k],
+                   atomic_targets=ds.atomic_targets[:n])
 
 
 def cpu_step(ds, funcs, dims, params, zprec, nthreads):

@@ -126,6 +126,7 @@ def _bind(L):
         "fnetg_batch_predict": (C.c_int, [vp, vp, vp]),
         "fnetg_batch_sync_params": (C.c_int, [vp]),
         "fnetg_batch_train_bf16": (C.c_int, [vp, i32]),
+        "fnetg_batch_forces": (C.c_int, [vp, vp, vp]),
         "fnetg_server_create": (C.c_int, [C.POINTER(vp), vp, i32, vp, i32, vp, vp, i32, vp, i32,
                                           vp]),
         "fnetg_server_destroy": (C.c_int, [vp]),
@@ -432,6 +433,15 @@ class Context:
         self._check(self.lib.fnetg_batch_predict(self.h, _p(at), _p(gl)))
         return at, gl
 
+    def batch_forces(self, out_global=None, out_forces=None):
+        """Energies [S, 1] and forces [N, 1, 3] with the network passes on the tensor cores."""
+        gl = out_global if out_global is not None else np.zeros((self.nstruct, 1))
+        _check_out(gl, (self.nstruct, 1))
+        fo = out_forces if out_forces is not None else np.zeros((self.ntot, 1, 3))
+        _check_out(fo, (self.ntot, 1, 3))
+        self._check(self.lib.fnetg_batch_forces(self.h, _p(gl), _p(fo)))
+        return gl, fo
+
     def batch_train_bf16(self, on=True):
         """Full-batch training gradients from the tensor-core kernels (the precision form)."""
         self._check(self.lib.fnetg_batch_train_bf16(self.h, int(on)))
@@ -505,7 +515,7 @@ class Rng:
 
 class _ServerConfig(C.Structure):
     _fields_ = [("precision", C.c_int32), ("device", C.c_int32), ("lanes", C.c_int32),
-                ("pad", C.c_int32), ("max_batch_atoms", C.c_int64),
+                ("tensor_cores", C.c_int32), ("max_batch_atoms", C.c_int64),
                 ("hbm_budget_bytes", C.c_int64), ("reserve_bytes", C.c_int64)]
 
 
@@ -522,10 +532,11 @@ class Server:
     thread, served by continuous batching over ``lanes`` concurrent device batches."""
 
     def __init__(self, atomic_numbers, funcs, zprec, dims, activation, params, precision=FP32,
-                 device=0, lanes=0, max_batch_atoms=0, hbm_budget_bytes=0, reserve_bytes=0):
+                 device=0, lanes=0, max_batch_atoms=0, hbm_budget_bytes=0, reserve_bytes=0,
+                 tensor_cores=False):
         self.lib = load()
-        cfg = _ServerConfig(int(precision), int(device), int(lanes), 0, int(max_batch_atoms),
-                            int(hbm_budget_bytes), int(reserve_bytes))
+        cfg = _ServerConfig(int(precision), int(device), int(lanes), int(bool(tensor_cores)),
+                            int(max_batch_atoms), int(hbm_budget_bytes), int(reserve_bytes))
         g = pack(funcs) if not isinstance(funcs, np.ndarray) else funcs
         self.ng = len(g)
         self.dims = [int(d) for d in dims]

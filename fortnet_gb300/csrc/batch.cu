@@ -122,9 +122,15 @@ template <int HP> TcNet make_net(fnetg_ctx *ctx) {
   n.sm_x1 = o + n.w_bytes1;
   n.jm_total = o + n.w_bytes;
   {
-    // the 128-column reads of a_1 and a_2 stay inside the allocation
-    const uint32_t reach = std::max(n.sm_a1, n.sm_a2) + kRows * kRows * 2;
-    const uint32_t with_x1 = std::max(n.sm_x1 + n.x_bytes, reach);
+    // The MN-major operand reads run past a buffer's own columns: 128 columns of a_1 and a_2
+    // (the M tile of a^T delta), nmt0 x 128 columns of a feature buffer (the M tiles of
+    // X^T delta_1).  Every such read stays inside the allocation: the first feature buffer and
+    // the activations are followed by other buffers; the second feature buffer closes the plan,
+    // so the plan is extended by its over-read.
+    const uint32_t mt_bytes = (uint32_t)n.nmt0 * kRows * kRows * 2;
+    const uint32_t reach = std::max({n.sm_a1 + kRows * kRows * 2, n.sm_a2 + kRows * kRows * 2,
+                                     n.sm_x + mt_bytes});
+    const uint32_t with_x1 = std::max({n.sm_x1 + n.x_bytes, n.sm_x1 + mt_bytes, reach});
     n.prefetch = with_x1 <= 227u * 1024u - 1024u ? 1 : 0;
     n.sm_total = n.prefetch ? with_x1 : std::max(n.sm_x1, reach);
   }
@@ -1535,13 +1541,12 @@ int fnetg_batch_setup(fnetg_ctx *ctx, int32_t batch_structures) {
   FNETG_CHECK(batch_structures >= 1, FNETG_E_INVALID, "batch_setup: batch size must be >= 1");
   FNETG_CHECK(ctx->net_set, FNETG_E_INVALID, "batch_setup: no network");
   FNETG_CHECK(ctx->feats_valid, FNETG_E_INVALID, "batch_setup: no features computed");
-  FNETG_CHECK(ctx->targets_set, FNETG_E_INVALID, "batch_setup: no targets");
   FNETG_CHECK(ctx->nf == ctx->dims[0], FNETG_E_SHAPE, "batch_setup: network input width");
   FNETG_CHECK(ctx->nlayer == 4 && ctx->dims[3] == 1 && ctx->act == FNETG_ACT_TANH &&
-                  ctx->ngt == 1 && ctx->nat == 0,
+                  (!ctx->targets_set || (ctx->ngt == 1 && ctx->nat == 0)),
               FNETG_E_UNSUPPORTED,
               "batch_setup: the tensor-core form takes two tanh hidden layers, one output and "
-              "one global target");
+              "(for training) one global target");
   const int H = std::max(ctx->dims[1], ctx->dims[2]);
   FNETG_CHECK(H <= 64 && ctx->dims[0] + 1 <= 2 * kRows - 16, FNETG_E_UNSUPPORTED,
               "batch_setup: hidden layers of at most 64 units and at most 239 inputs");
@@ -1569,8 +1574,9 @@ int fnetg_batch_setup(fnetg_ctx *ctx, int32_t batch_structures) {
   b.s0.assign(1, 0);
   b.sumw.clear();
   std::vector<int32_t> tsp, tatoms;
-  std::vector<int32_t> w(S, 1);
-  if (S > 0) FNETG_CUDA(copy_sync(ctx, w.data(), ctx->d_w.p, sizeof(int32_t) * S, cudaMemcpyDeviceToHost));
+  std::vector<int32_t> w(S, 1);  // datapoint weights (1 for predictions without targets)
+  if (S > 0 && ctx->targets_set)
+    FNETG_CUDA(copy_sync(ctx, w.data(), ctx->d_w.p, sizeof(int32_t) * S, cudaMemcpyDeviceToHost));
   std::vector<std::vector<int32_t>> rows(ctx->nsp);
   for (int k = 0; k < b.nbatch; k++) {
     const int sa = k * b.B, se = std::min(S, sa + b.B);
@@ -1638,6 +1644,7 @@ int fnetg_batch_info(fnetg_ctx *ctx, int32_t *nbatch, int64_t *ntiles, int32_t *
 int fnetg_batch_gradients(fnetg_ctx *ctx, int32_t batch, int32_t loss, double *grad,
                           double *atomic_out) {
   if (!ctx || !ctx->batch) return FNETG_E_INVALID;
+  FNETG_CHECK(ctx->targets_set, FNETG_E_INVALID, "batch_gradients: no targets");
   BatchState &b = *ctx->batch;
   FNETG_CHECK(batch >= 0 && batch < b.nbatch, FNETG_E_INVALID, "batch_gradients: batch index");
   FNETG_CHECK(loss >= 0 && loss <= 3, FNETG_E_INVALID, "loss code");
@@ -1662,6 +1669,7 @@ int fnetg_batch_gradients(fnetg_ctx *ctx, int32_t batch, int32_t loss, double *g
 int fnetg_batch_epoch(fnetg_ctx *ctx, int32_t loss, double learning_rate, double max_disp,
                       double *loss_out) {
   if (!ctx || !ctx->batch) return FNETG_E_INVALID;
+  FNETG_CHECK(ctx->targets_set, FNETG_E_INVALID, "batch_epoch: no targets");
   BatchState &b = *ctx->batch;
   FNETG_CHECK(loss >= 0 && loss <= 3, FNETG_E_INVALID, "loss code");
   FNETG_CHECK(learning_rate > 0.0 && max_disp > 0.0, FNETG_E_INVALID,
@@ -1744,6 +1752,39 @@ int fnetg_batch_predict(fnetg_ctx *ctx, double *atomic_out, double *global_out) 
     FNETG_CUDA(cudaMemcpyAsync(global_out, ctx->d_gsum.p, sizeof(double) * ctx->S,
                                cudaMemcpyDeviceToHost, ctx->stream));
   if (atomic_out || global_out) return check_err(ctx);
+  return FNETG_OK;
+}
+
+int fnetg_batch_forces(fnetg_ctx *ctx, double *global_out, double *forces_out) {
+  if (!ctx || !ctx->batch) return FNETG_E_INVALID;
+  BatchState &b = *ctx->batch;
+  FNETG_CHECK(ctx->prec == FNETG_FP32 && ctx->nb_valid && ctx->zprec_valid, FNETG_E_INVALID,
+              "batch_forces: FP32 context with neighbour list and z-scored features");
+  FNETG_CHECK(b.plan_S == ctx->S && b.plan_N == ctx->N, FNETG_E_INVALID,
+              "batch_forces: the structures changed since fnetg_batch_setup");
+  // forward and input Jacobian of every tile in one launch (a CTA per tile up to the SM count)
+  int rc = launch_tc_jac(ctx, 0, b.ntiles, (int)std::min<int64_t>(num_sms(), b.ntiles));
+  if (rc) return rc;
+  ctx->jac_ready = true;
+  rc = run_forces(ctx);
+  ctx->jac_ready = false;
+  if (rc) return rc;
+  rc = check_err(ctx);
+  if (rc) return rc;
+  if (global_out && ctx->S > 0) {
+    FNETG_CUDA(ctx->d_gsum.ensure(sizeof(double) * ctx->S));
+    {
+      LaunchScope ls(ctx, "struct_sum");
+      struct_sum_kernel<<<ceil_div(ctx->S, 128), 128, 0, ctx->stream>>>(
+          ctx->d_out.as<double>(), ctx->d_off.as<int64_t>(), ctx->S, 1, ctx->d_gsum.as<double>());
+      FNETG_CUDA(cudaGetLastError());
+    }
+    FNETG_CUDA(copy_sync(ctx, global_out, ctx->d_gsum.p, sizeof(double) * ctx->S,
+                          cudaMemcpyDeviceToHost));
+  }
+  if (forces_out && ctx->N > 0)
+    FNETG_CUDA(copy_sync(ctx, forces_out, ctx->d_forces.p, sizeof(double) * ctx->N * 3,
+                          cudaMemcpyDeviceToHost));
   return FNETG_OK;
 }
 

@@ -17,6 +17,7 @@
 #include <unordered_map>
 #include <vector>
 
+#include "fnetg_batch.h"
 #include "fnetg_serve.h"
 #include "internal.cuh"
 
@@ -120,8 +121,14 @@ int run_batch(fnetg_server *s, Lane &ln, std::vector<RequestPtr> &batch) {
   if (!rc) rc = fnetg_acsf_zscore(ctx, nullptr, s->zprec.data(), 0);
   ln.global.resize((size_t)S * nout);
   ln.forces.resize((size_t)N * nout * 3);
-  if (!rc) rc = fnetg_predict(ctx, nullptr, ln.global.data());
-  if (!rc) rc = fnetg_forces(ctx, ln.forces.data());
+  if (s->cfg.tensor_cores) {
+    // the batch as one mini-batch of species tiles; forward and Jacobian on the tensor cores
+    if (!rc) rc = fnetg_batch_setup(ctx, S);
+    if (!rc) rc = fnetg_batch_forces(ctx, ln.global.data(), ln.forces.data());
+  } else {
+    if (!rc) rc = fnetg_predict(ctx, nullptr, ln.global.data());
+    if (!rc) rc = fnetg_forces(ctx, ln.forces.data());
+  }
   if (rc) return rc;
   for (int k = 0; k < S; k++) {
     Request &r = *batch[k];
@@ -222,6 +229,10 @@ int fnetg_server_create(fnetg_server **out, const fnetg_server_config *cfg, int3
   if (nspecies < 1 || ng < 1 || nlayer < 2 || dims[0] != ng) return FNETG_E_SHAPE;
   if (cfg->lanes < 0 || cfg->lanes > 16 || cfg->max_batch_atoms < 0 || cfg->hbm_budget_bytes < 0)
     return FNETG_E_INVALID;
+  if (cfg->tensor_cores &&
+      (cfg->precision != FNETG_FP32 || nlayer != 4 || dims[3] != 1 ||
+       activation != FNETG_ACT_TANH || std::max(dims[1], dims[2]) > 64 || dims[0] > 239))
+    return FNETG_E_UNSUPPORTED;
   std::unique_ptr<fnetg_server> s(new fnetg_server());
   s->cfg = *cfg;
   if (s->cfg.lanes == 0) s->cfg.lanes = 3;

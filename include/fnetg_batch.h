@@ -26,7 +26,8 @@ extern "C" {
 
 /* Mini-batches of batch_structures consecutive structures (the last may be smaller).  Packs the
  * current (z-scored) features of every mini-batch into species tiles of 128 atoms as BF16, and
- * the current parameters as BF16 weight images.  The mini-batch loop replaces the full-batch
+ * the current parameters as BF16 weight images.  Targets are needed by the training calls
+ * below, not by the setup.  The mini-batch loop replaces the full-batch
  * loop of TBpnn_nTrain (prog/fortnet/lib_nn/bpnn.F90:293-363). */
 int fnetg_batch_setup(fnetg_ctx *ctx, int32_t batch_structures);
 /* Mini-batch count, tile count and the CTA counts the autotuner chose (0 before the first
@@ -52,6 +53,14 @@ int fnetg_batch_epoch(fnetg_ctx *ctx, int32_t loss, double learning_rate, double
  * outputs atomic_out[Ntot] and per-structure sums global_out[S] (atom order).  Either may be
  * NULL (results stay on the device). */
 int fnetg_batch_predict(fnetg_ctx *ctx, double *atomic_out, double *global_out);
+/* Energies and analytical forces of every structure with the network passes on the tensor
+ * cores: one launch computes every atom's output and input Jacobian (BF16 operands, FP32
+ * accumulation; TNetwork_fdevi, network.F90:183-244, in reverse mode), and the FP32 force
+ * kernel contracts it with dG/dR (forceAnalysis_analytical, lib_analysis/forces.F90:317-425).
+ * FP32 context with z-scored features, after fnetg_batch_setup for the current structures
+ * (targets are not needed).  global_out[S] (may be NULL) receives the per-structure sums in
+ * atom order, forces_out[N*3] (may be NULL) the forces in the layout of fnetg_forces. */
+int fnetg_batch_forces(fnetg_ctx *ctx, double *global_out, double *forces_out);
 /* on != 0: fnetg_train_gradients and fnetg_train_iteration (the full-batch L-BFGS / SD loop of
  * TBpnn_nTrain, bpnn.F90:293-363) take their gradients from the tensor-core kernels over every
  * tile of the mini-batch plan: forward, reverse pass and weight gradients in BF16 with FP32

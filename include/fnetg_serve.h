@@ -43,7 +43,10 @@ typedef struct {
   int32_t precision;        /* FNETG_FP32 or FNETG_FP64: arithmetic of ACSF, network, forces */
   int32_t device;           /* CUDA device ordinal */
   int32_t lanes;            /* batches in flight at once; 0 -> 3 */
-  int32_t pad;
+  int32_t tensor_cores;     /* 1: the network passes (forward and input Jacobian) in BF16 on the
+                               tensor cores (fnetg_batch_forces); FP32 precision and networks of
+                               two tanh hidden layers of at most 64 units, one output, at most
+                               239 inputs.  0: the plain kernels */
   int64_t max_batch_atoms;  /* atoms per batch (and per request) at most; 0 -> 65536 */
   int64_t hbm_budget_bytes; /* device memory all lanes may hold; 0 -> 80% of free memory */
   int64_t reserve_bytes;    /* device memory reserved up front in the lanes' memory pool;

@@ -127,6 +127,48 @@ def test_matches_oracle_on_small_requests(precision, kind):
         assert np.max(np.abs(got[s][1] - f_orc[a:b])) <= f_tol * fmax + 1e-12
 
 
+def test_tensor_core_lanes_alone_mixed_and_against_fp64(pool):
+    """Lanes with the network passes on the tensor cores (fnetg_batch_forces: BF16 forward and
+    input Jacobian, FP32 ACSF and force contraction) on a well-conditioned C4-shaped model:
+    every request alone and in a mixed batch gives the same energy (a row's arithmetic does not
+    depend on the tile it sits in) and forces within the FP32 accumulation order (1e-6 of the
+    largest component); against the FP64 plain service the BF16 rounding of the network inputs,
+    weights and activations is within 2e-2 of sum_i |o_i| on energies and 5e-2 of the largest
+    component on forces (printed)."""
+    ds, funcs, dims, _, zprec = pool
+    params = synthetic.normal_params(dims, len(C5.atomic_numbers), 13)
+    reqs = requests(ds)
+    with api.Server(C5.atomic_numbers, funcs, zprec, dims, "tanh", params,
+                    precision=api.FP64, lanes=2) as srv:
+        ref = [srv.wait(*srv.submit(an, xyz, lat), timeout=60.0) for an, xyz, lat in reqs]
+    with api.Server(C5.atomic_numbers, funcs, zprec, dims, "tanh", params,
+                    precision=api.FP32, lanes=3, tensor_cores=True) as srv:
+        alone = [srv.wait(*srv.submit(an, xyz, lat), timeout=60.0) for an, xyz, lat in reqs]
+        tickets = [srv.submit(an, xyz, lat) for an, xyz, lat in reqs]
+        mixed = [srv.wait(t, n, timeout=60.0) for t, n in tickets]
+    # sum_i |o_i| of every structure from an FP64 context
+    with api.Context(api.FP64) as ctx:
+        ctx.upload(ds)
+        ctx.set_species(ds.species)
+        ctx.set_gfunctions(funcs)
+        ctx.acsf(download=False)
+        ctx.zscore(zprec=zprec)
+        ctx.set_network(dims, "tanh", params)
+        at, _ = ctx.predict()
+    worst_e = worst_f = 0.0
+    for s in range(ds.nstruct):
+        a, b = ds.atom_offsets[s], ds.atom_offsets[s + 1]
+        fscale = float(np.max(np.abs(ref[s][1])))
+        np.testing.assert_allclose(mixed[s][0], alone[s][0], rtol=1e-12, atol=0.0)
+        np.testing.assert_allclose(mixed[s][1], alone[s][1], rtol=0.0, atol=1e-6 * fscale)
+        mag = float(np.sum(np.abs(at[a:b])))
+        worst_e = max(worst_e, abs(alone[s][0][0] - ref[s][0][0]) / mag)
+        worst_f = max(worst_f, float(np.max(np.abs(alone[s][1] - ref[s][1]))) / fscale)
+    print(f"tensor-core lanes vs FP64 service: energies {worst_e:.2e} of sum |o_i|, forces "
+          f"{worst_f:.2e} of the largest component")
+    assert worst_e <= 2e-2 and worst_f <= 5e-2
+
+
 def test_requests_queued_behind_a_batch_are_batched_together(pool):
     ds, funcs, dims, params, zprec = pool
     reqs = requests(ds)
