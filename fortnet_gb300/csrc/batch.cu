@@ -105,13 +105,16 @@ template <int HP> TcNet make_net(fnetg_ctx *ctx) {
   n.w_bytes0 = n.off_w1b;  // multiples of 16: (HP + 4) * 4 and every image are
   n.w_bytes1 = n.off_w0b;
   n.w_bytes = n.off_w0b + w0b;
+  // stored columns of a hidden layer's activations: the GEMM's K extent, and at least the HP
+  // columns the epilogues write (K1p < HP when H1 < H2)
+  const uint32_t k1s = (uint32_t)std::max(n.K1p, HP), k2s = (uint32_t)std::max(n.K2p, HP);
   uint32_t o = 0;
   n.sm_x = o;
   o += n.x_bytes;
   n.sm_a1 = o;
-  o += kRows * n.K1p * 2;
+  o += kRows * k1s * 2;
   n.sm_a2 = o;
-  o += kRows * n.K2p * 2;
+  o += kRows * k2s * 2;
   n.sm_d2 = o;
   o += kRows * HP * 2;
   n.sm_d1 = o;
@@ -137,8 +140,8 @@ template <int HP> TcNet make_net(fnetg_ctx *ctx) {
   o = 0;
   n.fm_x = o;
   o += n.x_bytes;
-  n.fm_a1 = o;  // exactly K1p columns: only the K-major reads of the second layer
-  o += kRows * n.K1p * 2;
+  n.fm_a1 = o;  // only the K-major reads of the second layer
+  o += kRows * k1s * 2;
   n.fm_w = o;
   o += n.w_bytes0;
   n.fm_total = o;
@@ -148,13 +151,13 @@ template <int HP> TcNet make_net(fnetg_ctx *ctx) {
   n.tm_u = o;
   o += n.x_bytes;
   n.tm_a1 = o;
-  o += kRows * n.K1p * 2;
+  o += kRows * k1s * 2;
   n.tm_t1 = o;
-  o += kRows * n.K1p * 2;
+  o += kRows * k1s * 2;
   n.tm_a2 = o;
-  o += kRows * n.K2p * 2;
+  o += kRows * k2s * 2;
   n.tm_t2 = o;
-  o += kRows * n.K2p * 2;
+  o += kRows * k2s * 2;
   n.tm_zb = o;
   o += kRows * HP * 2;
   n.tm_zd = o;
@@ -163,9 +166,15 @@ template <int HP> TcNet make_net(fnetg_ctx *ctx) {
   o += kRows * 16 * 2;
   n.tm_d3b = o;
   o += kRows * 16 * 2;
-  n.tm_w = o;  // the weights close the plan: every over-read above lands inside it
+  n.tm_w = o;
   o += n.w_bytes1;
-  n.tm_total = o;
+  {
+    // the transposed-operand reads (128 columns of an activation or tangent buffer, nmt0 x 128
+    // of a feature or feature-tangent buffer) stay inside the allocation
+    const uint32_t mt_bytes = (uint32_t)n.nmt0 * kRows * kRows * 2, m1 = kRows * kRows * 2;
+    n.tm_total = std::max({o, n.tm_x + mt_bytes, n.tm_u + mt_bytes, n.tm_a1 + m1, n.tm_t1 + m1,
+                           n.tm_a2 + m1, n.tm_t2 + m1});
+  }
   n.nparams = ctx->nparams;
   n.woff0 = ctx->woff[0];
   n.woff1 = ctx->woff[1];
@@ -320,14 +329,76 @@ __device__ void flush_grads(const TcNet &n, float *gp, uint32_t tm, uint32_t lan
   else if (tid == n.H2) gp[n.boff3] = v[0];
 }
 
+// Row r's activations of one hidden layer, the CH columns [c0, c0 + CH) of one half of the
+// row (BF16, core layout): the constant-1 column at index H when it falls in this half; the
+// half holding column HP also writes the constant column and the zero padding up to Kp when
+// H == HP.
+template <int HP, int CH>
+__device__ __forceinline__ void store_act_half(unsigned char *buf, int r, float (&v)[CH], int c0,
+                                               int H, int Kp) {
+#pragma unroll
+  for (int c = 0; c < CH; c++)
+    if (c0 + c == H) v[c] = 1.f;  // unrolled compare: the array stays in registers
+#pragma unroll
+  for (int c = 0; c < CH; c += 8) st8(buf, tc::core_off(r, c0 + c, kRows), v + c);
+  if (H >= HP && c0 + CH == HP) {
+    float e[8] = {1.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    st8(buf, tc::core_off(r, HP, kRows), e);
+    float z[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    for (int c = HP + 8; c < Kp; c += 8) st8(buf, tc::core_off(r, c, kRows), z);
+  }
+}
+
+// Gradient accumulators -> one CTA's partial slot (reference parameter order); thread (row,
+// half) writes the columns of its half.
+template <int HP>
+__device__ void flush_grads_half(const TcNet &n, float *gp, uint32_t tm, uint32_t lane_off,
+                                 int row, int half) {
+  constexpr int CH = HP / 2;
+  const int c0 = half * CH;
+  for (int mt = 0; mt < n.nmt0; mt++) {
+    const int k = mt * kRows + row;  // input feature (k == nf: the bias column)
+    float v[CH];
+    tc::tmem_ld_cols<CH>(tm + lane_off + kColG0 + mt * HP + c0, v);
+#pragma unroll
+    for (int q = 0; q < CH; q++) {
+      const int j = c0 + q;
+      if (j < n.H1 && k < n.nf) gp[n.woff0 + k + (int64_t)n.nf * j] = v[q];
+      else if (j < n.H1 && k == n.nf) gp[n.boff1 + j] = v[q];
+    }
+  }
+  {
+    float v[CH];
+    tc::tmem_ld_cols<CH>(tm + lane_off + kColG1 + c0, v);
+#pragma unroll
+    for (int q = 0; q < CH; q++) {
+      const int i = c0 + q;
+      if (i < n.H2 && row < n.H1) gp[n.woff1 + row + (int64_t)n.H1 * i] = v[q];
+      else if (i < n.H2 && row == n.H1) gp[n.boff2 + i] = v[q];
+    }
+  }
+  if (half == 0) {  // whole warps: the TMEM load is warp-collective
+    float v[8];
+    tc::tmem_ld_cols<8>(tm + lane_off + kColG2, v);
+    if (row < n.H2) gp[n.woff2 + row] = v[0];
+    else if (row == n.H2) gp[n.boff3] = v[0];
+  }
+}
+
 // MODE 0: forward (atomic outputs).  MODE 1: forward + reverse pass + weight gradients.
+// Two threads per atom row: warps w and w + 4 read the same TMEM lane quarter and split the
+// hidden units of every epilogue (CH = HP / 2 columns each), so each scheduler runs two warps.
+constexpr int kMlpThreads = 2 * kRows;
 template <int HP, int MODE>
-__global__ void __launch_bounds__(kThreads, 1) tc_mlp_kernel(TcArgs a) {
+__global__ void __launch_bounds__(kMlpThreads, MODE == 0 ? 2 : 1) tc_mlp_kernel(TcArgs a) {
+  constexpr int CH = HP / 2;
   extern __shared__ __align__(1024) unsigned char sm[];
   __shared__ uint64_t mb_load, mb_mma, mb_x[2];
   __shared__ uint32_t tmem_base;
+  __shared__ float ypart[kRows];
   const TcNet &n = a.net;
   const int tid = threadIdx.x, warp = tid >> 5;
+  const int row = tid & (kRows - 1), half = tid >> 7, c0 = half * CH;
   // the forward pass uses its own compact plan (two CTAs per SM) and 64 TMEM columns
   constexpr uint32_t kCols = MODE == 0 ? 64u : kTmemCols;
   const uint32_t wload = MODE == 0 ? n.w_bytes0 : n.w_bytes1;
@@ -351,7 +422,7 @@ __global__ void __launch_bounds__(kThreads, 1) tc_mlp_kernel(TcArgs a) {
   __syncthreads();
   tc::fence_after_sync();
   const uint32_t tm = tmem_base;
-  const uint32_t lane_off = (uint32_t)(warp * 32) << 16;
+  const uint32_t lane_off = (uint32_t)((warp & 3) * 32) << 16;
   const uint32_t sA1 = tc::smem_u32(A1), sA2 = tc::smem_u32(A2),
                  sD2 = tc::smem_u32(D2), sD1 = tc::smem_u32(D1), sD3 = tc::smem_u32(D3),
                  sW = tc::smem_u32(W);
@@ -372,8 +443,8 @@ __global__ void __launch_bounds__(kThreads, 1) tc_mlp_kernel(TcArgs a) {
 
   // gradient accumulators of cur_sp -> this CTA's partial slot (reference parameter order)
   auto flush = [&]() {
-    flush_grads<HP>(n, a.gpart + ((int64_t)blockIdx.x * a.nsp + cur_sp) * n.nparams, tm, lane_off,
-                    tid);
+    flush_grads_half<HP>(n, a.gpart + ((int64_t)blockIdx.x * a.nsp + cur_sp) * n.nparams, tm,
+                         lane_off, row, half);
     touched |= 1ull << cur_sp;
   };
   // after a wait gave up: the copies still in flight, each once more with a limit
@@ -425,7 +496,6 @@ __global__ void __launch_bounds__(kThreads, 1) tc_mlp_kernel(TcArgs a) {
       pend_w = true;
     }
     cur_sp = sp;
-    const int row = tid;
     const int atom = tile_atom(a.tile_atoms, t * kRows + row, a.natoms);
     const float delta3 = (MODE == 1 && atom >= 0) ? (float)a.delta[atom] : 0.f;
     if (pf) {
@@ -458,22 +528,17 @@ __global__ void __launch_bounds__(kThreads, 1) tc_mlp_kernel(TcArgs a) {
     if (!wait_all(&mb_mma, ph_mma)) { drain(); failed = true; break; }
     ph_mma ^= 1;
     tc::fence_after_sync();
-    float f1[HP];
+    float f1[CH];
     {
-      float v[HP];
+      float v[CH];
+      tc::tmem_ld_cols<CH>(tm + lane_off + kColFwd + c0, v);
 #pragma unroll
-      for (int c0 = 0; c0 < HP; c0 += 16) {
-        float z[16];
-        tc::tmem_ld16(tm + lane_off + kColFwd + c0, z);
-        tc::tmem_wait_ld();
-#pragma unroll
-        for (int q = 0; q < 16; q++) {
-          const float th = tanh_fast(z[q]);
-          v[c0 + q] = th;
-          f1[c0 + q] = 1.f - th * th;
-        }
+      for (int q = 0; q < CH; q++) {
+        const float th = tanh_fast(v[q]);
+        v[q] = th;
+        f1[q] = 1.f - th * th;
       }
-      store_act<HP>(A1, row, v, n.H1, n.K1p);
+      store_act_half<HP, CH>(A1, row, v, c0, n.H1, n.K1p);
     }
     tc::fence_async_smem();
     tc::fence_before_sync();
@@ -491,32 +556,32 @@ __global__ void __launch_bounds__(kThreads, 1) tc_mlp_kernel(TcArgs a) {
     ph_mma ^= 1;
     tc::fence_after_sync();
     {
-      float y = w2[HP];  // output bias
-      float av[HP], dv[HP];
+      float y = 0.f;  // this half's share of w2 . a2
+      float av[CH], dv[CH];
+      tc::tmem_ld_cols<CH>(tm + lane_off + kColFwd + c0, av);
 #pragma unroll
-      for (int c0 = 0; c0 < HP; c0 += 16) {
-        float z[16];
-        tc::tmem_ld16(tm + lane_off + kColFwd + c0, z);
-        tc::tmem_wait_ld();
-#pragma unroll
-        for (int q = 0; q < 16; q++) {
-          const float th = tanh_fast(z[q]);
-          const float wq = w2[c0 + q];
-          y = fmaf(th, wq, y);
-          av[c0 + q] = th;
-          dv[c0 + q] = delta3 * wq * (1.f - th * th);
-        }
+      for (int q = 0; q < CH; q++) {
+        const float th = tanh_fast(av[q]);
+        const float wq = w2[c0 + q];
+        y = fmaf(th, wq, y);
+        av[q] = th;
+        dv[q] = delta3 * wq * (1.f - th * th);
       }
       if (MODE == 0) {
-        if (atom >= 0) a.out[atom] = (double)y;
+        // output = b3 + both halves' shares, added in a fixed order
+        if (half == 1) ypart[row] = y;
+        __syncthreads();
+        if (half == 0 && atom >= 0) a.out[atom] = (double)(w2[HP] + (y + ypart[row]));
       } else {
-        store_act<HP>(A2, row, av, n.H2, n.K2p);
+        store_act_half<HP, CH>(A2, row, av, c0, n.H2, n.K2p);
 #pragma unroll
-        for (int c = 0; c < HP; c += 8) st8(D2, tc::core_off(row, c, kRows), dv + c);
-        float d3[8] = {delta3, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-        float z8[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-        st8(D3, tc::core_off(row, 0, kRows), d3);
-        st8(D3, tc::core_off(row, 8, kRows), z8);
+        for (int c = 0; c < CH; c += 8) st8(D2, tc::core_off(row, c0 + c, kRows), dv + c);
+        if (half == 0) {
+          float d3[8] = {delta3, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+          float z8[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+          st8(D3, tc::core_off(row, 0, kRows), d3);
+          st8(D3, tc::core_off(row, 8, kRows), z8);
+        }
       }
     }
     if (MODE == 0) continue;
@@ -542,17 +607,12 @@ __global__ void __launch_bounds__(kThreads, 1) tc_mlp_kernel(TcArgs a) {
     ph_mma ^= 1;
     tc::fence_after_sync();
     {
-      float dv[HP];
+      float dv[CH];
+      tc::tmem_ld_cols<CH>(tm + lane_off + kColFwd + c0, dv);
 #pragma unroll
-      for (int c0 = 0; c0 < HP; c0 += 16) {
-        float z[16];
-        tc::tmem_ld16(tm + lane_off + kColFwd + c0, z);
-        tc::tmem_wait_ld();
+      for (int q = 0; q < CH; q++) dv[q] *= f1[q];
 #pragma unroll
-        for (int q = 0; q < 16; q++) dv[c0 + q] = z[q] * f1[c0 + q];
-      }
-#pragma unroll
-      for (int c = 0; c < HP; c += 8) st8(D1, tc::core_off(row, c, kRows), dv + c);
+      for (int c = 0; c < CH; c += 8) st8(D1, tc::core_off(row, c0 + c, kRows), dv + c);
     }
     tc::fence_async_smem();
     tc::fence_before_sync();
@@ -1268,7 +1328,7 @@ int launch_tc(fnetg_ctx *ctx, int mode, int64_t t0, int64_t t1, int grid) {
   FNETG_CUDA(raise_smem_limit(k, smem));
   void *args[] = {&a};
   LaunchScope ls(ctx, mode == 0 ? "tc_forward" : "tc_train");
-  FNETG_CUDA(cudaLaunchKernel(k, dim3(grid), dim3(kThreads), args, smem, ctx->stream));
+  FNETG_CUDA(cudaLaunchKernel(k, dim3(grid), dim3(kMlpThreads), args, smem, ctx->stream));
   return FNETG_OK;
 }
 

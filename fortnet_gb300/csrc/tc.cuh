@@ -107,6 +107,28 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
 #pragma unroll
   for (int k = 0; k < 16; k++) v[k] = __uint_as_float(r[k]);
 }
+__device__ __forceinline__ void tmem_ld8(uint32_t taddr, float (&v)[8]) {
+  uint32_t r[8];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];\n"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7])
+      : "r"(taddr));
+#pragma unroll
+  for (int k = 0; k < 8; k++) v[k] = __uint_as_float(r[k]);
+}
+// CH consecutive accumulator columns of this warp's lanes (CH = 8, 16 or 32), one wait
+template <int CH> __device__ __forceinline__ void tmem_ld_cols(uint32_t taddr, float (&v)[CH]) {
+  static_assert(CH == 8 || CH % 16 == 0, "column count");
+  if constexpr (CH == 8) {
+    tmem_ld8(taddr, v);
+  } else {
+#pragma unroll
+    for (int c0 = 0; c0 < CH; c0 += 16)
+      tmem_ld16(taddr + c0, *reinterpret_cast<float(*)[16]>(&v[c0]));
+  }
+  asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+}
 __device__ __forceinline__ void tmem_wait_ld() {
   asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
 }
