@@ -1141,14 +1141,28 @@ __global__ void __launch_bounds__(kRedThreads) tc_reduce_kernel(const float *gpa
                                                                 const int32_t *gflag, int nblk,
                                                                 int nsp, TcNet n, double *grad64,
                                                                 double *bmax) {
-  __shared__ int flag[kMaxTcBlocks];
+  __shared__ int list[kMaxTcBlocks];  // the CTAs that wrote a partial of this species, in order
+  __shared__ int nlist;
   __shared__ double part[kRedSplit][kRedThreads / kRedSplit];
   __shared__ double sh[kRedThreads / kRedSplit];
   const int s = blockIdx.y;
-  for (int b = threadIdx.x; b < nblk; b += blockDim.x) flag[b] = gflag[b * nsp + s];
+  if (threadIdx.x < 32) {
+    // compact the written partials (tiles are sorted by species, so a species' CTAs form a
+    // short run): ballots over the flags, in CTA order
+    int cnt = 0;
+    for (int b0 = 0; b0 < nblk; b0 += 32) {
+      const int b = b0 + threadIdx.x;
+      const bool on = b < nblk && gflag[b * nsp + s] != 0;
+      const unsigned m = __ballot_sync(0xffffffffu, on);
+      if (on) list[cnt + __popc(m & ((1u << threadIdx.x) - 1u))] = b;
+      cnt += __popc(m);
+    }
+    if (threadIdx.x == 0) nlist = cnt;
+  }
   __syncthreads();
-  // thread (r, k): parameter q = block * 32 + k, CTAs b = r, r + 8, ... (independent loads in
-  // flight across the eight threads); the eight partial sums combined in r order
+  const int nl = nlist;
+  // thread (r, k): parameter q = block * 32 + k, partials r, r + 8, ... of the list (loads
+  // requested four at a time); the eight partial sums combined in r order
   constexpr int kq = kRedThreads / kRedSplit;
   const int k = threadIdx.x % kq, r = threadIdx.x / kq;
   const int64_t q = (int64_t)blockIdx.x * kq + k;
@@ -1156,19 +1170,16 @@ __global__ void __launch_bounds__(kRedThreads) tc_reduce_kernel(const float *gpa
   if (q < n.nparams && (q < n.woff3 || q >= n.boff1)) {
     const float *p = gpart + (int64_t)s * n.nparams + q;
     const int64_t stride = (int64_t)nsp * n.nparams;
-    // four CTAs' partials requested together (a partial a CTA did not write is loaded but not
-    // added), summed in CTA order
-    int b = r;
-    for (; b + 3 * kRedSplit < nblk; b += 4 * kRedSplit) {
-      const float v0 = p[b * stride], v1 = p[(b + kRedSplit) * stride],
-                  v2 = p[(b + 2 * kRedSplit) * stride], v3 = p[(b + 3 * kRedSplit) * stride];
-      if (flag[b]) acc += (double)v0;
-      if (flag[b + kRedSplit]) acc += (double)v1;
-      if (flag[b + 2 * kRedSplit]) acc += (double)v2;
-      if (flag[b + 3 * kRedSplit]) acc += (double)v3;
+    int i = r;
+    for (; i + 3 * kRedSplit < nl; i += 4 * kRedSplit) {
+      const float v0 = p[list[i] * stride], v1 = p[list[i + kRedSplit] * stride],
+                  v2 = p[list[i + 2 * kRedSplit] * stride], v3 = p[list[i + 3 * kRedSplit] * stride];
+      acc += (double)v0;
+      acc += (double)v1;
+      acc += (double)v2;
+      acc += (double)v3;
     }
-    for (; b < nblk; b += kRedSplit)
-      if (flag[b]) acc += (double)p[b * stride];
+    for (; i < nl; i += kRedSplit) acc += (double)p[list[i] * stride];
   }
   part[r][k] = acc;
   __syncthreads();

@@ -96,8 +96,18 @@ __global__ void __launch_bounds__(kLossThreads) loss_cta_kernel(LossArgs a) {
       const double t = a.gt[(int64_t)s * a.ngt + o];
       const double lg = lossgrad(a.loss, sum, t);
       lsum += loss_term(a.loss, sum, t);
-      for (int64_t at = a0 + threadIdx.x; at < a1; at += kLossThreads)
-        a.delta[at * a.nout + o] = lg * a.aw[at] / (double)n * ws;
+      // atomic weights of four atoms loaded before their four stores (the stores could alias
+      // the loads as far as the compiler knows)
+      at = a0 + threadIdx.x;
+      for (; at + 3 * kLossThreads < a1; at += 4 * kLossThreads) {
+        const double w0 = a.aw[at], w1 = a.aw[at + kLossThreads],
+                     w2 = a.aw[at + 2 * kLossThreads], w3 = a.aw[at + 3 * kLossThreads];
+        a.delta[at * a.nout + o] = lg * w0 / (double)n * ws;
+        a.delta[(at + kLossThreads) * a.nout + o] = lg * w1 / (double)n * ws;
+        a.delta[(at + 2 * kLossThreads) * a.nout + o] = lg * w2 / (double)n * ws;
+        a.delta[(at + 3 * kLossThreads) * a.nout + o] = lg * w3 / (double)n * ws;
+      }
+      for (; at < a1; at += kLossThreads) a.delta[at * a.nout + o] = lg * a.aw[at] / (double)n * ws;
     }
     num += ws * a.saw[s] * loss_finish(a.loss, lsum, a.ngt);
     den += ws * a.saw[s];
