@@ -269,13 +269,15 @@ __global__ void __launch_bounds__(256, 4) nb_kernel(NbArgs a) {
         const int nwd = (n + 31) >> 5;
         for (int w = lane; w < nwd; w += 32) bits[w] = 0u;
         __syncwarp();
-        const int nx = hi[0] - lo[0] + 1, ny = hi[1] - lo[1] + 1, nz = hi[2] - lo[2] + 1;
-        for (int c = lane; c < nx * ny * nz; c += 32) {
-          const int cx = lo[0] + c / (ny * nz), cy = lo[1] + (c / nz) % ny, cz = lo[2] + c % nz;
-          const int64_t key = cbase + ((int64_t)cx * cg.y + cy) * cg.z + cz;
-          const int64_t q0 = a.cstart[key], q1 = a.cstart[key + 1];
-          // the cell's atoms are stored contiguously with their positions: two at a time, both
-          // loads issued before either test
+        // lanes over the (x, y) columns of the box: the cells lo[2]..hi[2] of a column are
+        // consecutive in the cell order, so a column's atoms are one contiguous run
+        const int nx = hi[0] - lo[0] + 1, ny = hi[1] - lo[1] + 1;
+        for (int c = lane; c < nx * ny; c += 32) {
+          const int cx = lo[0] + c / ny, cy = lo[1] + c % ny;
+          const int64_t kcol = cbase + ((int64_t)cx * cg.y + cy) * cg.z;
+          const int64_t q0 = a.cstart[kcol + lo[2]], q1 = a.cstart[kcol + hi[2] + 1];
+          // the column's atoms are stored contiguously with their positions: two at a time,
+          // both loads issued before either test
           for (int64_t q = q0; q < q1; q += 2) {
             const V4<float> pa = a.cpos[q];
             const bool two = q + 1 < q1;
@@ -304,7 +306,6 @@ __global__ void __launch_bounds__(256, 4) nb_kernel(NbArgs a) {
             if (t == 0) m &= sb > 0 ? ~((1u << sb) - 1u) : 0xffffffffu;
             else if (t == nwd) m &= (1u << sb) - 1u;
           }
-          unsigned nzm = __ballot_sync(0xffffffffu, m != 0u);
           if (!kFill) {
             int c = __popc(m);
 #pragma unroll
@@ -312,33 +313,25 @@ __global__ void __launch_bounds__(256, 4) nb_kernel(NbArgs a) {
             cnt += c;
             continue;
           }
-          while (nzm) {
-            const int src = __ffs(nzm) - 1;
-            nzm &= nzm - 1;
-            const uint32_t mw = __shfl_sync(0xffffffffu, m, src);
-            const int wsrc = __shfl_sync(0xffffffffu, widx, src);
-            const bool ok = (mw >> lane) & 1u;
-            const unsigned mb = __ballot_sync(0xffffffffu, ok);
-            const unsigned below = (1u << lane) - 1u;
-            if (ok && FNETG_GUARD(qn + __popc(mb & below) < 128))
-              queue[qn + __popc(mb & below)] = make_int2(wsrc * 32 + lane, (int)img);
-            qn += __popc(mb);
-            cnt += __popc(mb);
-            __syncwarp();
-            while (qn >= 32) {
-              const int2 e = queue[lane];
-              store_pair<T>(a, ci, cif, cil, i, a0, e.x, e.y, im0, wpos, stored + lane);
-              const int rem = qn - 32;
-              const int2 v0 = lane < rem ? queue[lane + 32] : make_int2(0, 0);
-              const int2 v1 = lane + 32 < rem ? queue[lane + 64] : make_int2(0, 0);
-              __syncwarp();
-              if (lane < rem) queue[lane] = v0;
-              if (lane + 32 < rem) queue[lane + 32] = v1;
-              __syncwarp();
-              qn -= 32;
-              stored += 32;
-            }
+          // ranks of the accepted atoms in the cyclic order: the slots' popcounts scanned over
+          // the lanes; each lane stores its own slot's pairs (structures on the cell path use
+          // it for every image, so nothing is queued)
+          const int pc = __popc(m);
+          int off = pc;
+#pragma unroll
+          for (int k = 1; k < 32; k <<= 1) {
+            const int v = __shfl_up_sync(0xffffffffu, off, k);
+            if (lane >= k) off += v;
           }
+          const int total = __shfl_sync(0xffffffffu, off, 31);
+          off -= pc;
+          for (uint32_t mm = m; mm; mm &= mm - 1u) {
+            const int bit = __ffs(mm) - 1;
+            store_pair<T>(a, ci, cif, cil, i, a0, widx * 32 + bit, (int)img, im0, wpos, stored + off);
+            off++;
+          }
+          stored += total;
+          cnt += total;
         }
         continue;
       }
