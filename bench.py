@@ -118,9 +118,43 @@ def oracle_params(cfg, dims):
 
 
 def featurise(ctx, zprec=None, weights=None):
-    ctx.neighbors()
+    ctx.npairs = ctx.neighbors()
     ctx.acsf(download=False)
     return ctx.zscore(weights=weights, zprec=zprec)
+
+
+def acsf_op_counts(funcs, species_frac):
+    """Algorithmic work of the ACSF value pass in the moment form, from the G-function list:
+    (FP32 operations per pair, per atom; ex2 operations per pair; bytes per pair, per atom).
+    Per pair: the cutoff (one sine, 4 operations), every radial G2 whose list holds the pair
+    (x = r - rs, x^2, the scale, the exponential, times fc, the sum: 5 operations and one ex2;
+    a resolved function holds its species' share of the pairs), per angular eta class
+    E = exp(-eta r^2) fc (2 operations, one ex2) and the 35 moment products and sums of degree
+    <= 4 (70 operations), plus the 34 products building the monomials once.  Per atom: per
+    (channel pair, eta class) the degree sums over the 35 monomials (3 operations each), per G5
+    function the combination of its five degree sums (10).  HBM: the pair record (displacement
+    and distance 16 B, neighbour 4 B, image and class 4 B) per pair; per atom the features (4 B
+    each) and the moment cache (35 FP32 per list and eta class)."""
+    rad = [f for f in funcs if f.radial]
+    ang = [f for f in funcs if f.angular]
+    def frac(z):
+        return 1.0 if z == 0 else species_frac.get(z, 0.0)
+
+    per_pair = 4.0 + sum(5.0 * frac(f.z1) for f in rad)
+    ex2_pair = 1.0 + sum(frac(f.z1) for f in rad)
+    per_atom = 0.0
+    mom_bytes = 0.0
+    if ang:
+        etas = sorted({f.eta for f in ang})
+        lists = sorted({f.z1 for f in ang} | {f.z2 for f in ang})
+        chpairs = sorted({(min(f.z1, f.z2), max(f.z1, f.z2)) for f in ang})
+        # a pair enters its species' list (and the all-atom list when one is used)
+        share = sum(frac(z) for z in lists)
+        per_pair += 34.0 + len(etas) * share * (2.0 + 70.0)
+        ex2_pair += len(etas) * share
+        per_atom = len(chpairs) * len(etas) * 35 * 3.0 + len(ang) * 10.0
+        mom_bytes = 4.0 * 35 * len(lists) * len(etas)
+    return per_pair, per_atom, ex2_pair, 24.0, 4.0 * len(funcs) + mom_bytes
 
 
 def setup(args):
@@ -231,6 +265,46 @@ def energy_errors(ctx, ds, funcs, zprec, dims, nsample=64):
             "plain_fp32": stats(e_32), "batched_bf16": stats(e_tc)}
 
 
+def featurise_roofline(ctx, ds, funcs, feat_prof, nfeat=2):
+    """Rooflines of the featurisation stages, from their CUDA-event times over nfeat
+    featurisations: the ACSF value pass against the device's measured FP32 and ex2 rates and
+    HBM bandwidth, the neighbour search (its kernels together) against HBM (its pair records
+    written once: 24 B per pair, plus positions read and cell-sorted)."""
+    fp32_peak, ex2_peak = ctx.probe_peaks()
+    hbm, _, peak_kind = load_peaks()
+    N, P = ds.ntot, float(ctx.npairs)
+    zs, cnt = np.unique(ds.atnum, return_counts=True)
+    frac = {int(z): float(c) / N for z, c in zip(zs, cnt)}
+    fpp, fpa, epp, bpp, bpa = acsf_op_counts(funcs, frac)
+    out = {"pairs": int(P), "peaks": {"fp32_tflops": round(fp32_peak, 1),
+                                      "ex2_tops": round(ex2_peak, 2), "hbm_gbs": hbm,
+                                      "source": "fnetg_probe_peaks (FMA and ex2 loops, CUDA "
+                                                "events) and MEASURED_PEAKS.json " + peak_kind}}
+    ms, n = feat_prof["acsf"]
+    if n:
+        sec = ms / nfeat / 1e3
+        fl = (P * fpp + N * fpa) / sec / 1e12
+        ex = P * epp / sec / 1e12
+        gb = (P * bpp + N * bpa) / sec / 1e9
+        out["acsf"] = {"ms": round(ms / nfeat, 3),
+                       "flop_per_pair": round(fpp, 1), "flop_per_atom": round(fpa, 1),
+                       "ex2_per_pair": round(epp, 2),
+                       "fp32": {"achieved": round(fl, 2), "peak": round(fp32_peak, 1),
+                                "unit": "TFLOP/s", "frac": round(fl / fp32_peak, 4)},
+                       "ex2": {"achieved": round(ex, 3), "peak": round(ex2_peak, 2),
+                               "unit": "Top/s", "frac": round(ex / ex2_peak, 4)},
+                       "hbm": {"achieved": round(gb, 1), "peak": hbm, "unit": "GB/s",
+                               "frac": round(gb / hbm, 4)}}
+    ms, n = feat_prof["neighbors"]
+    if n:
+        sec = ms / nfeat / 1e3
+        gb = (P * 24.0 + N * 32.0) / sec / 1e9
+        out["neighbors"] = {"ms": round(ms / nfeat, 3), "bytes_per_pair": 24,
+                            "hbm": {"achieved": round(gb, 1), "peak": hbm, "unit": "GB/s",
+                                    "frac": round(gb / hbm, 4)}}
+    return out
+
+
 def run_ours(args):
     from fortnet_gb300 import api
 
@@ -258,6 +332,7 @@ def run_ours(args):
                                   torch)))
     feat_prof = {f: ctx.profile_read(f) for f in ("neighbors", "scan", "acsf", "zscore")}
     ctx.profile(False)
+    feat_roof = featurise_roofline(ctx, ds, funcs, feat_prof)
     ctx.batch_setup(args.batch)
     # plain FP32 form, then the batched mixed-precision form (the headline); the warm-up of
     # the batched form captures the epoch graph and runs the autotuner.  The clock sampler
@@ -365,6 +440,7 @@ def run_ours(args):
             "featurise_ms": round(feat_ms, 2),
             "featurise_atoms_per_s": round(N / (feat_ms / 1e3), 1),
             "featurise_kernels_ms": {f: round(v[0] / 2, 3) for f, v in feat_prof.items() if v[1]},
+            "featurise_roofline": feat_roof,
             "dataset_generation_s": round(gen_s, 1),
         },
         "accuracy": accuracy,

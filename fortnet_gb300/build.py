@@ -21,7 +21,7 @@ CHECKS_DIR = os.path.join(OUT_DIR, "checks")
 CHECKS_LIB = os.path.join(CHECKS_DIR, "libfnetg.so")
 SOURCES = ["context.cu", "neighbors.cu", "acsf.cu", "mlp.cu", "forces.cu", "train.cu", "rng.cu",
            "noalloc.cu", "fd.cu", "serve.cu", "batch.cu", "jvp.cu",
-           "forceloss.cu"]
+           "forceloss.cu", "probe.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -291,9 +291,17 @@ __device__ __forceinline__ void mma_chain(uint32_t d, uint32_t a0, uint32_t a_lb
                  tc::smem_desc(b0 + ks * b_step, b_lbo, b_sbo), idesc, (acc || ks > 0) ? 1u : 0u);
 }
 
+// One gradient partial: stored, or added to what the same CTA stored for the species before
+// (a launch over several mini-batches meets a species once per mini-batch).  A template flag,
+// so that a plain flush issues no load of the old partial.
+template <bool ADD> __device__ __forceinline__ void put_grad(float *p, float v) {
+  if (ADD) *p += v;
+  else *p = v;
+}
+
 // The TMEM gradient accumulators (G0 in M tiles of 128 inputs, G1, G2) -> one partial slot in
 // the reference parameter order (all threads; thread tid holds lane tid of every region).
-template <int HP>
+template <int HP, bool ADD>
 __device__ void flush_grads(const TcNet &n, float *gp, uint32_t tm, uint32_t lane_off, int tid) {
   for (int mt = 0; mt < n.nmt0; mt++) {
     const int k = mt * kRows + tid;  // input feature (k == nf: the bias column)
@@ -305,8 +313,8 @@ __device__ void flush_grads(const TcNet &n, float *gp, uint32_t tm, uint32_t lan
 #pragma unroll
       for (int q = 0; q < 16; q++) {
         const int j = c0 + q;
-        if (j < n.H1 && k < n.nf) gp[n.woff0 + k + (int64_t)n.nf * j] = v[q];
-        else if (j < n.H1 && k == n.nf) gp[n.boff1 + j] = v[q];
+        if (j < n.H1 && k < n.nf) put_grad<ADD>(gp + n.woff0 + k + (int64_t)n.nf * j, v[q]);
+        else if (j < n.H1 && k == n.nf) put_grad<ADD>(gp + n.boff1 + j, v[q]);
       }
     }
   }
@@ -318,15 +326,15 @@ __device__ void flush_grads(const TcNet &n, float *gp, uint32_t tm, uint32_t lan
 #pragma unroll
     for (int q = 0; q < 16; q++) {
       const int i = c0 + q;
-      if (i < n.H2 && tid < n.H1) gp[n.woff1 + tid + (int64_t)n.H1 * i] = v[q];
-      else if (i < n.H2 && tid == n.H1) gp[n.boff2 + i] = v[q];
+      if (i < n.H2 && tid < n.H1) put_grad<ADD>(gp + n.woff1 + tid + (int64_t)n.H1 * i, v[q]);
+      else if (i < n.H2 && tid == n.H1) put_grad<ADD>(gp + n.boff2 + i, v[q]);
     }
   }
   float v[16];
   tc::tmem_ld16(tm + lane_off + kColG2, v);
   tc::tmem_wait_ld();
-  if (tid < n.H2) gp[n.woff2 + tid] = v[0];
-  else if (tid == n.H2) gp[n.boff3] = v[0];
+  if (tid < n.H2) put_grad<ADD>(gp + n.woff2 + tid, v[0]);
+  else if (tid == n.H2) put_grad<ADD>(gp + n.boff3, v[0]);
 }
 
 // Row r's activations of one hidden layer, the CH columns [c0, c0 + CH) of one half of the
@@ -351,7 +359,7 @@ __device__ __forceinline__ void store_act_half(unsigned char *buf, int r, float 
 
 // Gradient accumulators -> one CTA's partial slot (reference parameter order); thread (row,
 // half) writes the columns of its half.
-template <int HP>
+template <int HP, bool ADD>
 __device__ void flush_grads_half(const TcNet &n, float *gp, uint32_t tm, uint32_t lane_off,
                                  int row, int half) {
   constexpr int CH = HP / 2;
@@ -363,8 +371,8 @@ __device__ void flush_grads_half(const TcNet &n, float *gp, uint32_t tm, uint32_
 #pragma unroll
     for (int q = 0; q < CH; q++) {
       const int j = c0 + q;
-      if (j < n.H1 && k < n.nf) gp[n.woff0 + k + (int64_t)n.nf * j] = v[q];
-      else if (j < n.H1 && k == n.nf) gp[n.boff1 + j] = v[q];
+      if (j < n.H1 && k < n.nf) put_grad<ADD>(gp + n.woff0 + k + (int64_t)n.nf * j, v[q]);
+      else if (j < n.H1 && k == n.nf) put_grad<ADD>(gp + n.boff1 + j, v[q]);
     }
   }
   {
@@ -373,15 +381,15 @@ __device__ void flush_grads_half(const TcNet &n, float *gp, uint32_t tm, uint32_
 #pragma unroll
     for (int q = 0; q < CH; q++) {
       const int i = c0 + q;
-      if (i < n.H2 && row < n.H1) gp[n.woff1 + row + (int64_t)n.H1 * i] = v[q];
-      else if (i < n.H2 && row == n.H1) gp[n.boff2 + i] = v[q];
+      if (i < n.H2 && row < n.H1) put_grad<ADD>(gp + n.woff1 + row + (int64_t)n.H1 * i, v[q]);
+      else if (i < n.H2 && row == n.H1) put_grad<ADD>(gp + n.boff2 + i, v[q]);
     }
   }
   if (half == 0) {  // whole warps: the TMEM load is warp-collective
     float v[8];
     tc::tmem_ld_cols<8>(tm + lane_off + kColG2, v);
-    if (row < n.H2) gp[n.woff2 + row] = v[0];
-    else if (row == n.H2) gp[n.boff3] = v[0];
+    if (row < n.H2) put_grad<ADD>(gp + n.woff2 + row, v[0]);
+    else if (row == n.H2) put_grad<ADD>(gp + n.boff3, v[0]);
   }
 }
 
@@ -440,11 +448,38 @@ __global__ void __launch_bounds__(kMlpThreads, MODE == 0 ? 2 : 1) tc_mlp_kernel(
   uint64_t touched = 0;
   bool failed = false;
   int buf = 0;
+  // With the feature prefetch, a tile's input-layer weight gradient G0 += X^T delta_1 is issued
+  // after the next tile's first-layer MMAs (so it runs under that tile's epilogue instead of
+  // ahead of it); until then it is pending with its feature buffer and accumulate flag.
+  bool g0_pend = false, g0_acc = false;
+  uint32_t g0_x = 0;
 
+  // G0 += X^T delta_1 over the input features in M tiles of 128 (issuing thread only)
+  auto issue_g0 = [&](uint32_t sx, bool acc) {
+    for (int mt = 0; mt < n.nmt0; mt++)
+      for (int ks = 0; ks < kRows / 16; ks++)
+        tc::mma_bf16(tm + kColG0 + mt * HP,
+                     tc::smem_desc(sx + mt * 16 * 16 * kRows + ks * 256, 128, 16 * kRows),
+                     tc::smem_desc(sD1 + ks * 256, 128, 16 * kRows), id_g, acc || ks > 0);
+  };
+  // every MMA issued so far (a pending G0 first) has completed: the TMEM accumulators are final
+  auto settle = [&]() -> bool {
+    if (tid == 0) {
+      tc::fence_after_sync();
+      if (g0_pend) issue_g0(g0_x, g0_acc);
+      tc::mma_commit(&mb_mma);
+    }
+    g0_pend = false;
+    if (!wait_all(&mb_mma, ph_mma)) return false;
+    ph_mma ^= 1;
+    tc::fence_after_sync();
+    return true;
+  };
   // gradient accumulators of cur_sp -> this CTA's partial slot (reference parameter order)
   auto flush = [&]() {
-    flush_grads_half<HP>(n, a.gpart + ((int64_t)blockIdx.x * a.nsp + cur_sp) * n.nparams, tm,
-                         lane_off, row, half);
+    float *gp = a.gpart + ((int64_t)blockIdx.x * a.nsp + cur_sp) * n.nparams;
+    if ((touched >> cur_sp) & 1) flush_grads_half<HP, true>(n, gp, tm, lane_off, row, half);
+    else flush_grads_half<HP, false>(n, gp, tm, lane_off, row, half);
     touched |= 1ull << cur_sp;
   };
   // after a wait gave up: the copies still in flight, each once more with a limit
@@ -465,6 +500,11 @@ __global__ void __launch_bounds__(kMlpThreads, MODE == 0 ? 2 : 1) tc_mlp_kernel(
     const int sp = a.tile_sp[t];
     const bool new_sp = sp != cur_sp;
     if (MODE == 1 && new_sp && gacc) {
+      if (!settle()) {
+        drain();
+        failed = true;
+        break;
+      }
       flush();
       gacc = false;
     }
@@ -473,15 +513,12 @@ __global__ void __launch_bounds__(kMlpThreads, MODE == 0 ? 2 : 1) tc_mlp_kernel(
     const bool more = pf && t + 1 < my1;
     if (tid == 0) {
       if (pf) {
+        // the weights' last readers (the previous species' layer and reverse MMAs) completed
+        // before the flush; the next tile's features are requested after this tile's second
+        // layer (below), once the other buffer's last reader has completed
         if (new_sp) {
           tc::mbar_expect_tx(&mb_load, wload);
           tc::bulk_g2s(W, a.w + (int64_t)sp * n.w_bytes, wload, &mb_load);
-        }
-        // the other buffer's last reader (the previous tile's last MMA) has completed
-        if (more) {
-          tc::mbar_expect_tx(&mb_x[buf ^ 1], n.x_bytes);
-          tc::bulk_g2s(buf ? Xb0 : Xb1, a.x + (t + 1) * (int64_t)n.x_bytes, n.x_bytes,
-                       &mb_x[buf ^ 1]);
         }
       } else {
         tc::mbar_expect_tx(&mb_load, n.x_bytes + (new_sp ? wload : 0u));
@@ -491,7 +528,6 @@ __global__ void __launch_bounds__(kMlpThreads, MODE == 0 ? 2 : 1) tc_mlp_kernel(
     }
     if (pf) {
       pend_w = new_sp;
-      if (more) (buf ? pend_x0 : pend_x1) = true;
     } else {
       pend_w = true;
     }
@@ -524,7 +560,11 @@ __global__ void __launch_bounds__(kMlpThreads, MODE == 0 ? 2 : 1) tc_mlp_kernel(
         tc::mma_bf16(tm + kColFwd, tc::smem_desc(sX + ks * 2 * 16 * kRows, 16 * kRows, 128),
                      tc::smem_desc(sW + ks * 2 * 16 * HP, 16 * HP, 128), id_h, ks > 0);
       tc::mma_commit(&mb_mma);
+      // the previous tile's G0 after this commit: it runs under this tile's epilogue and is
+      // covered by the second layer's commit
+      if (MODE == 1 && g0_pend) issue_g0(g0_x, g0_acc);
     }
+    g0_pend = false;
     if (!wait_all(&mb_mma, ph_mma)) { drain(); failed = true; break; }
     ph_mma ^= 1;
     tc::fence_after_sync();
@@ -555,6 +595,16 @@ __global__ void __launch_bounds__(kMlpThreads, MODE == 0 ? 2 : 1) tc_mlp_kernel(
     if (!wait_all(&mb_mma, ph_mma)) { drain(); failed = true; break; }
     ph_mma ^= 1;
     tc::fence_after_sync();
+    if (more) {
+      // the other feature buffer's last reader, the previous tile's G0, has completed (this
+      // commit covers it): the next tile's features go there
+      if (tid == 0) {
+        tc::mbar_expect_tx(&mb_x[buf ^ 1], n.x_bytes);
+        tc::bulk_g2s(buf ? Xb0 : Xb1, a.x + (t + 1) * (int64_t)n.x_bytes, n.x_bytes,
+                     &mb_x[buf ^ 1]);
+      }
+      (buf ? pend_x0 : pend_x1) = true;
+    }
     {
       float y = 0.f;  // this half's share of w2 . a2
       float av[CH], dv[CH];
@@ -588,20 +638,22 @@ __global__ void __launch_bounds__(kMlpThreads, MODE == 0 ? 2 : 1) tc_mlp_kernel(
     tc::fence_async_smem();
     tc::fence_before_sync();
     __syncthreads();
-    // ---- reverse pass: P = delta_2 W1^T; G1 += A1^T delta_2; G2 += A2^T delta_3
+    // ---- reverse pass: P = delta_2 W1^T; G1 += A1^T delta_2; G2 += A2^T delta_3.  The
+    // commit covers P only: the weight-gradient products run under the epilogue, and the next
+    // commit (the next tile's first layer, or a flush) covers them before their operands change
     if (tid == 0) {
       tc::fence_after_sync();
       for (int ks = 0; ks < HP / 16; ks++)
         tc::mma_bf16(tm + kColFwd, tc::smem_desc(sD2 + ks * 2 * 16 * kRows, 16 * kRows, 128),
                      tc::smem_desc(sW + n.off_w1b + ks * 2 * 16 * HP, 16 * HP, 128), id_h,
                      ks > 0);
+      tc::mma_commit(&mb_mma);
       for (int ks = 0; ks < kRows / 16; ks++) {
         tc::mma_bf16(tm + kColG1, tc::smem_desc(sA1 + ks * 256, 128, 16 * kRows),
                      tc::smem_desc(sD2 + ks * 256, 128, 16 * kRows), id_g, gacc || ks > 0);
         tc::mma_bf16(tm + kColG2, tc::smem_desc(sA2 + ks * 256, 128, 16 * kRows),
                      tc::smem_desc(sD3 + ks * 256, 128, 16 * kRows), id_g2, gacc || ks > 0);
       }
-      tc::mma_commit(&mb_mma);
     }
     if (!wait_all(&mb_mma, ph_mma)) { drain(); failed = true; break; }
     ph_mma ^= 1;
@@ -617,25 +669,33 @@ __global__ void __launch_bounds__(kMlpThreads, MODE == 0 ? 2 : 1) tc_mlp_kernel(
     tc::fence_async_smem();
     tc::fence_before_sync();
     __syncthreads();
-    // ---- G0 += X^T delta_1 (input features in M tiles of 128)
-    if (tid == 0) {
+    // ---- G0 += X^T delta_1 (input features in M tiles of 128): with the prefetch it waits
+    // for the next tile's first layer (or a flush); without it, the next tile's features
+    // overwrite this buffer, so it runs now
+    if (pf) {
+      g0_pend = true;
+      g0_acc = gacc;
+      g0_x = sX;
+    } else {
+      if (tid == 0) {
+        tc::fence_after_sync();
+        issue_g0(sX, gacc);
+        tc::mma_commit(&mb_mma);
+      }
+      if (!wait_all(&mb_mma, ph_mma)) { drain(); failed = true; break; }
+      ph_mma ^= 1;
       tc::fence_after_sync();
-      for (int mt = 0; mt < n.nmt0; mt++)
-        for (int ks = 0; ks < kRows / 16; ks++)
-          tc::mma_bf16(tm + kColG0 + mt * HP,
-                       tc::smem_desc(sX + mt * 16 * 16 * kRows + ks * 256, 128, 16 * kRows),
-                       tc::smem_desc(sD1 + ks * 256, 128, 16 * kRows), id_g, gacc || ks > 0);
-      tc::mma_commit(&mb_mma);
     }
-    if (!wait_all(&mb_mma, ph_mma)) { drain(); failed = true; break; }
-    ph_mma ^= 1;
-    tc::fence_after_sync();
     gacc = true;
     if (pf) buf ^= 1;
   }
   if (MODE == 1 && !failed) {
-    if (gacc) flush();
-    if (tid < a.nsp) a.gflag[(int64_t)blockIdx.x * a.nsp + tid] = (int)((touched >> tid) & 1);
+    if (gacc) {
+      if (settle()) flush();
+      else failed = true;
+    }
+    if (!failed && tid < a.nsp)
+      a.gflag[(int64_t)blockIdx.x * a.nsp + tid] = (int)((touched >> tid) & 1);
   }
   if (failed && tid == 0) atomicExch(a.err, 1);
   tc::fence_before_sync();
@@ -859,13 +919,18 @@ __global__ void __launch_bounds__(kThreads, 1) tc_tan_kernel(TcArgs a) {
   int cur_sp = -1;
   bool gacc = false, failed = false;
   uint64_t touched = 0;
+  // gradient accumulators of species sp -> this CTA's partial slot (added to an earlier one)
+  auto flush_tan = [&](int sp) {
+    float *gp = a.gpart + ((int64_t)blockIdx.x * a.nsp + sp) * n.nparams;
+    if ((touched >> sp) & 1) flush_grads<HP, true>(n, gp, tm, lane_off, tid);
+    else flush_grads<HP, false>(n, gp, tm, lane_off, tid);
+  };
   // K-major: lbo 16 R, sbo 128, step 32 R; MN-major over 128 rows: lbo 128, sbo 2048, step 256
   for (int64_t t = my0; t < my1; t++) {
     const int sp = a.tile_sp[t];
     const bool new_sp = sp != cur_sp;
     if (new_sp && gacc) {
-      flush_grads<HP>(n, a.gpart + ((int64_t)blockIdx.x * a.nsp + cur_sp) * n.nparams, tm,
-                      lane_off, tid);
+      flush_tan(cur_sp);
       touched |= 1ull << cur_sp;
       gacc = false;
     }
@@ -1023,8 +1088,7 @@ __global__ void __launch_bounds__(kThreads, 1) tc_tan_kernel(TcArgs a) {
   }
   if (!failed) {
     if (gacc) {
-      flush_grads<HP>(n, a.gpart + ((int64_t)blockIdx.x * a.nsp + cur_sp) * n.nparams, tm,
-                      lane_off, tid);
+      flush_tan(cur_sp);
       touched |= 1ull << cur_sp;
     }
     if (tid < a.nsp) a.gflag[(int64_t)blockIdx.x * a.nsp + tid] = (int)((touched >> tid) & 1);
@@ -1137,24 +1201,37 @@ __global__ void pack_w_kernel(const double *p64, TcNet n, unsigned char *w) {
 constexpr int kRedThreads = 256;
 constexpr int kRedSplit = 8;  // threads sharing one parameter's CTA loop
 
+// hi + lo += v exactly up to the rounding of lo (Knuth's TwoSum on the FP32 pipe): the sums of
+// FP32 partials keep 48 significant bits, more than the FP64 pipe (a 64th of the FP32 rate on
+// this GPU) would be needed for, in a fixed order
+__device__ __forceinline__ void df_add(float &hi, float &lo, float v) {
+  const float s = __fadd_rn(hi, v);
+  const float bb = __fsub_rn(s, hi);
+  lo = __fadd_rn(lo, __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(v, bb)));
+  hi = s;
+}
+
 __global__ void __launch_bounds__(kRedThreads) tc_reduce_kernel(const float *gpart,
                                                                 const int32_t *gflag, int nblk,
                                                                 int nsp, TcNet n, double *grad64,
                                                                 double *bmax) {
   __shared__ int list[kMaxTcBlocks];  // the CTAs that wrote a partial of this species, in order
+  __shared__ unsigned char on[kMaxTcBlocks];
   __shared__ int nlist;
-  __shared__ double part[kRedSplit][kRedThreads / kRedSplit];
+  __shared__ float2 part[kRedSplit][kRedThreads / kRedSplit];
   __shared__ double sh[kRedThreads / kRedSplit];
   const int s = blockIdx.y;
+  // the flags of every CTA, read by all threads at once (one round of loads), then compacted
+  // by one warp in CTA order (tiles are sorted by species, so a species' CTAs form a short run)
+  for (int b = threadIdx.x; b < nblk; b += kRedThreads) on[b] = gflag[b * nsp + s] != 0;
+  __syncthreads();
   if (threadIdx.x < 32) {
-    // compact the written partials (tiles are sorted by species, so a species' CTAs form a
-    // short run): ballots over the flags, in CTA order
     int cnt = 0;
     for (int b0 = 0; b0 < nblk; b0 += 32) {
       const int b = b0 + threadIdx.x;
-      const bool on = b < nblk && gflag[b * nsp + s] != 0;
-      const unsigned m = __ballot_sync(0xffffffffu, on);
-      if (on) list[cnt + __popc(m & ((1u << threadIdx.x) - 1u))] = b;
+      const bool f = b < nblk && on[b];
+      const unsigned m = __ballot_sync(0xffffffffu, f);
+      if (f) list[cnt + __popc(m & ((1u << threadIdx.x) - 1u))] = b;
       cnt += __popc(m);
     }
     if (threadIdx.x == 0) nlist = cnt;
@@ -1166,7 +1243,7 @@ __global__ void __launch_bounds__(kRedThreads) tc_reduce_kernel(const float *gpa
   constexpr int kq = kRedThreads / kRedSplit;
   const int k = threadIdx.x % kq, r = threadIdx.x / kq;
   const int64_t q = (int64_t)blockIdx.x * kq + k;
-  double acc = 0.0;
+  float hi = 0.f, lo = 0.f;
   if (q < n.nparams && (q < n.woff3 || q >= n.boff1)) {
     const float *p = gpart + (int64_t)s * n.nparams + q;
     const int64_t stride = (int64_t)nsp * n.nparams;
@@ -1174,19 +1251,24 @@ __global__ void __launch_bounds__(kRedThreads) tc_reduce_kernel(const float *gpa
     for (; i + 3 * kRedSplit < nl; i += 4 * kRedSplit) {
       const float v0 = p[list[i] * stride], v1 = p[list[i + kRedSplit] * stride],
                   v2 = p[list[i + 2 * kRedSplit] * stride], v3 = p[list[i + 3 * kRedSplit] * stride];
-      acc += (double)v0;
-      acc += (double)v1;
-      acc += (double)v2;
-      acc += (double)v3;
+      df_add(hi, lo, v0);
+      df_add(hi, lo, v1);
+      df_add(hi, lo, v2);
+      df_add(hi, lo, v3);
     }
-    for (; i < nl; i += kRedSplit) acc += (double)p[list[i] * stride];
+    for (; i < nl; i += kRedSplit) df_add(hi, lo, p[list[i] * stride]);
   }
-  part[r][k] = acc;
+  part[r][k] = make_float2(hi, lo);
   __syncthreads();
   if (threadIdx.x < kq) {
-    double t = 0.0;
+    float th = 0.f, tl = 0.f;
 #pragma unroll
-    for (int rr = 0; rr < kRedSplit; rr++) t += part[rr][threadIdx.x];
+    for (int rr = 0; rr < kRedSplit; rr++) {
+      const float2 v = part[rr][threadIdx.x];
+      df_add(th, tl, v.x);
+      tl = __fadd_rn(tl, v.y);
+    }
+    const double t = (double)th + (double)tl;
     const int64_t qq = (int64_t)blockIdx.x * kq + threadIdx.x;
     if (qq < n.nparams) grad64[(int64_t)s * n.nparams + qq] = t;
     sh[threadIdx.x] = fabs(t);
@@ -1237,22 +1319,33 @@ __global__ void __launch_bounds__(kRedThreads) tc_update_kernel(double *params,
                                                                 TcNet n, double inv_sumw,
                                                                 double lr, double maxdisp,
                                                                 unsigned char *w) {
-  __shared__ double smax;
+  __shared__ double smax, sscale;
+  __shared__ double wmax[kRedThreads / 32];
   const int s = blockIdx.y;
-  if (threadIdx.x < 32) {
+  {
+    // the species' largest gradient component from the reduction's block maxima: every
+    // thread's share loaded at once, then warp and block maxima
     double m = 0.0;
-    for (int b = threadIdx.x; b < nbm; b += 32) m = fmax(m, bmax[(int64_t)s * nbm + b]);
+    for (int b = threadIdx.x; b < nbm; b += kRedThreads) m = fmax(m, bmax[(int64_t)s * nbm + b]);
 #pragma unroll
     for (int k = 16; k > 0; k >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, k));
-    if (threadIdx.x == 0) smax = lr * (m * inv_sumw);
+    if ((threadIdx.x & 31) == 0) wmax[threadIdx.x >> 5] = m;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double t = 0.0;
+      for (int w = 0; w < kRedThreads / 32; w++) t = fmax(t, wmax[w]);
+      smax = lr * (t * inv_sumw);
+      // the displacement's scale, one division per CTA (1 when within the limit: x + 1 d
+      // equals x + d)
+      sscale = smax <= maxdisp ? 1.0 : maxdisp / smax;
+    }
   }
   __syncthreads();
   const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= n.nparams) return;
-  const double mx = smax;
   double *x = params + (int64_t)s * n.nparams;
   const double d = -1.0 * lr * (grad[(int64_t)s * n.nparams + q] * inv_sumw);
-  const double v = mx <= maxdisp ? x[q] + d : x[q] + (maxdisp / mx) * d;
+  const double v = x[q] + sscale * d;
   x[q] = v;
   write_images<HP>(n, w + (int64_t)s * n.w_bytes, q, v);
 }

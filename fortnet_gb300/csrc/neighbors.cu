@@ -223,168 +223,180 @@ __global__ void __launch_bounds__(256, 4) nb_kernel(NbArgs a) {
     int64_t cnt = 0;
     const float *bb = a.bbox + 6 * s;
     const int64_t im0 = a.img_off[s], im1 = a.img_off[s + 1];
-    // image -1 is the central cell, then the lattice points of the table (n1 outer .. n3 inner)
-    for (int64_t img = im0 - 1; img < im1; img++) {
-      V4<float> ch{0.f, 0.f, 0.f, 0.f};
-      int tstart = 1, tcount = n - 1;
-      if (img >= im0) {
-        ch = a.imgf[2 * img];
-        tstart = 0;
-        tcount = n;
-        // skip the image when the shifted bounding box is out of reach
+    // image -1 is the central cell, then the lattice points of the table (n1 outer .. n3 inner).
+    // The images are tested 32 at a time, one per lane, against the reach of the structure's
+    // shifted bounding box; the warp then walks the reachable ones in order.
+    for (int64_t ibase = im0 - 1; ibase < im1; ibase += 32) {
+      bool reach = false;
+      const int64_t mine = ibase + lane;
+      if (mine < im0) {
+        reach = true;
+      } else if (mine < im1) {
+        const V4<float> chm = a.imgf[2 * mine];
         const float p[3] = {cif.x, cif.y, cif.z};
-        const float cvf[3] = {ch.x, ch.y, ch.z};
+        const float cvf[3] = {chm.x, chm.y, chm.z};
         float dd = 0.f;
         for (int c = 0; c < 3; c++) {
           const float lo = bb[c] + cvf[c], hi = bb[3 + c] + cvf[c];
           const float e = p[c] < lo ? lo - p[c] : (p[c] > hi ? p[c] - hi : 0.f);
           dd += e * e;
         }
-        if (dd > a.rc2_hi) continue;
+        reach = !(dd > a.rc2_hi);
       }
-      // candidates 64 at a time, two per lane: the shifted centre is formed once per image
-      const float px = cif.x - ch.x, py = cif.y - ch.y, pz = cif.z - ch.z;
-      // the reference's decision for structure-local atom jl of this image
-      auto decide = [&](int jl, const V4<float> &cjf) -> bool {
-        const float e0 = cjf.x - px, e1 = cjf.y - py, e2 = cjf.z - pz;
-        const float df = e0 * e0 + e1 * e1 + e2 * e2;
-        if (df <= a.rc2_lo) return true;
-        if (df > a.rc2_hi) return false;
-        double d[3];
-        return exact_pair(a, ci, a0 + jl, img >= im0 ? img : -1, d) <= a.rc2;
-      };
-      if (cg.w) {
-        // cell list: only the cells of the box around the shifted centre are tested; the
-        // accepted atoms are marked in a bitmask and leave in the iterator's cyclic order
-        int lo[3], hi[3];
-        const float pc[3] = {px, py, pz};
-        const int gd[3] = {cg.x, cg.y, cg.z};
-        bool empty = false;
-        for (int c = 0; c < 3; c++) {
-          lo[c] = max(0, (int)floorf((pc[c] - a.rbox) * a.inv_cs));
-          hi[c] = min(gd[c] - 1, (int)floorf((pc[c] + a.rbox) * a.inv_cs));
-          empty = empty || lo[c] > hi[c];
+      for (unsigned pend = __ballot_sync(0xffffffffu, reach); pend; pend &= pend - 1u) {
+        const int64_t img = ibase + (__ffs(pend) - 1);
+        V4<float> ch{0.f, 0.f, 0.f, 0.f};
+        int tstart = 1, tcount = n - 1;
+        if (img >= im0) {
+          ch = a.imgf[2 * img];
+          tstart = 0;
+          tcount = n;
         }
-        if (empty) continue;
-        const int nwd = (n + 31) >> 5;
-        for (int w = lane; w < nwd; w += 32) bits[w] = 0u;
-        __syncwarp();
-        // lanes over the (x, y) columns of the box: the cells lo[2]..hi[2] of a column are
-        // consecutive in the cell order, so a column's atoms are one contiguous run
-        const int nx = hi[0] - lo[0] + 1, ny = hi[1] - lo[1] + 1;
-        for (int c = lane; c < nx * ny; c += 32) {
-          const int cx = lo[0] + c / ny, cy = lo[1] + c % ny;
-          const int64_t kcol = cbase + ((int64_t)cx * cg.y + cy) * cg.z;
-          const int64_t q0 = a.cstart[kcol + lo[2]], q1 = a.cstart[kcol + hi[2] + 1];
-          // the column's atoms are stored contiguously with their positions: two at a time,
-          // both loads issued before either test
-          for (int64_t q = q0; q < q1; q += 2) {
-            const V4<float> pa = a.cpos[q];
-            const bool two = q + 1 < q1;
-            const V4<float> pb = two ? a.cpos[q + 1] : pa;
-            const int ja = (int)__float_as_int(pa.w), jb = (int)__float_as_int(pb.w);
-            if (!(ja == il && img < im0) && decide(ja, pa) && FNETG_GUARD(ja >= 0 && ja < n))
-              atomicOr(&bits[ja >> 5], 1u << (ja & 31));
-            if (two && !(jb == il && img < im0) && decide(jb, pb) &&
-                FNETG_GUARD(jb >= 0 && jb < n))
-              atomicOr(&bits[jb >> 5], 1u << (jb & 31));
-          }
-        }
-        __syncwarp();
-        // slots of the cyclic order: the start word from the start bit, the other words, the
-        // start word below the start bit
-        const int start = img < im0 ? (il + 1 == n ? 0 : il + 1) : il;
-        const int sw = start >> 5, sb = start & 31;
-        const int nslot = nwd + (sb > 0 ? 1 : 0);
-        for (int base = 0; base < nslot; base += 32) {
-          const int t = base + lane;
-          uint32_t m = 0u;
-          int widx = 0;
-          if (t < nslot) {
-            widx = t == nwd ? sw : (sw + t) % nwd;
-            m = bits[widx];
-            if (t == 0) m &= sb > 0 ? ~((1u << sb) - 1u) : 0xffffffffu;
-            else if (t == nwd) m &= (1u << sb) - 1u;
-          }
-          if (!kFill) {
-            int c = __popc(m);
-#pragma unroll
-            for (int k = 16; k > 0; k >>= 1) c += __shfl_xor_sync(0xffffffffu, c, k);
-            cnt += c;
-            continue;
-          }
-          // ranks of the accepted atoms in the cyclic order: the slots' popcounts scanned over
-          // the lanes; each lane stores its own slot's pairs (structures on the cell path use
-          // it for every image, so nothing is queued)
-          const int pc = __popc(m);
-          int off = pc;
-#pragma unroll
-          for (int k = 1; k < 32; k <<= 1) {
-            const int v = __shfl_up_sync(0xffffffffu, off, k);
-            if (lane >= k) off += v;
-          }
-          const int total = __shfl_sync(0xffffffffu, off, 31);
-          off -= pc;
-          for (uint32_t mm = m; mm; mm &= mm - 1u) {
-            const int bit = __ffs(mm) - 1;
-            store_pair<T>(a, ci, cif, cil, i, a0, widx * 32 + bit, (int)img, im0, wpos, stored + off);
-            off++;
-          }
-          stored += total;
-          cnt += total;
-        }
-        continue;
-      }
-      auto test = [&](int k, bool &ok, int &jl) {
-        ok = false;
-        jl = 0;
-        if (k < tcount) {
-          jl = il + tstart + k;
-          if (jl >= n) jl -= n;
-          const V4<float> cjf = a.cf[a0 + jl];
+        // candidates 64 at a time, two per lane: the shifted centre is formed once per image
+        const float px = cif.x - ch.x, py = cif.y - ch.y, pz = cif.z - ch.z;
+        // the reference's decision for structure-local atom jl of this image
+        auto decide = [&](int jl, const V4<float> &cjf) -> bool {
           const float e0 = cjf.x - px, e1 = cjf.y - py, e2 = cjf.z - pz;
           const float df = e0 * e0 + e1 * e1 + e2 * e2;
-          if (df <= a.rc2_lo) {
-            ok = true;
-          } else if (df <= a.rc2_hi) {
-            // within the float error bound of the cutoff: the reference's FP64 decision
-            double d[3];
-            ok = exact_pair(a, ci, a0 + jl, img >= im0 ? img : -1, d) <= a.rc2;
+          if (df <= a.rc2_lo) return true;
+          if (df > a.rc2_hi) return false;
+          double d[3];
+          return exact_pair(a, ci, a0 + jl, img >= im0 ? img : -1, d) <= a.rc2;
+        };
+        if (cg.w) {
+          // cell list: only the cells of the box around the shifted centre are tested; the
+          // accepted atoms are marked in a bitmask and leave in the iterator's cyclic order
+          int lo[3], hi[3];
+          const float pc[3] = {px, py, pz};
+          const int gd[3] = {cg.x, cg.y, cg.z};
+          bool empty = false;
+          for (int c = 0; c < 3; c++) {
+            lo[c] = max(0, (int)floorf((pc[c] - a.rbox) * a.inv_cs));
+            hi[c] = min(gd[c] - 1, (int)floorf((pc[c] + a.rbox) * a.inv_cs));
+            empty = empty || lo[c] > hi[c];
           }
-        }
-      };
-      for (int base = 0; base < tcount; base += 64) {
-        bool ok0, ok1;
-        int j0, j1;
-        test(base + lane, ok0, j0);
-        test(base + 32 + lane, ok1, j1);
-        const unsigned m0 = __ballot_sync(0xffffffffu, ok0), m1 = __ballot_sync(0xffffffffu, ok1);
-        const int n0 = __popc(m0), n1 = __popc(m1);
-        if (kFill) {
-          // queue the accepted candidates in iterator order; store them 32 at a time
-          const unsigned below = (1u << lane) - 1u;
-          if (ok0 && FNETG_GUARD(qn + __popc(m0 & below) < 128))
-            queue[qn + __popc(m0 & below)] = make_int2(j0, (int)img);
-          if (ok1 && FNETG_GUARD(qn + n0 + __popc(m1 & below) < 128))
-            queue[qn + n0 + __popc(m1 & below)] = make_int2(j1, (int)img);
-          qn += n0 + n1;
+          if (empty) continue;
+          const int nwd = (n + 31) >> 5;
+          for (int w = lane; w < nwd; w += 32) bits[w] = 0u;
           __syncwarp();
-          while (qn >= 32) {
-            const int2 e = queue[lane];
-            store_pair<T>(a, ci, cif, cil, i, a0, e.x, e.y, im0, wpos, stored + lane);
-            // move the remaining qn - 32 (< 64) entries to the front: read all, then write
-            const int rem = qn - 32;
-            const int2 v0 = lane < rem ? queue[lane + 32] : make_int2(0, 0);
-            const int2 v1 = lane + 32 < rem ? queue[lane + 64] : make_int2(0, 0);
-            __syncwarp();
-            if (lane < rem) queue[lane] = v0;
-            if (lane + 32 < rem) queue[lane + 32] = v1;
-            __syncwarp();
-            qn -= 32;
-            stored += 32;
+          // lanes over the (x, y) columns of the box: the cells lo[2]..hi[2] of a column are
+          // consecutive in the cell order, so a column's atoms are one contiguous run
+          const int nx = hi[0] - lo[0] + 1, ny = hi[1] - lo[1] + 1;
+          for (int c = lane; c < nx * ny; c += 32) {
+            const int cx = lo[0] + c / ny, cy = lo[1] + c % ny;
+            const int64_t kcol = cbase + ((int64_t)cx * cg.y + cy) * cg.z;
+            const int64_t q0 = a.cstart[kcol + lo[2]], q1 = a.cstart[kcol + hi[2] + 1];
+            // the column's atoms are stored contiguously with their positions: two at a time,
+            // both loads issued before either test
+            for (int64_t q = q0; q < q1; q += 2) {
+              const V4<float> pa = a.cpos[q];
+              const bool two = q + 1 < q1;
+              const V4<float> pb = two ? a.cpos[q + 1] : pa;
+              const int ja = (int)__float_as_int(pa.w), jb = (int)__float_as_int(pb.w);
+              if (!(ja == il && img < im0) && decide(ja, pa) && FNETG_GUARD(ja >= 0 && ja < n))
+                atomicOr(&bits[ja >> 5], 1u << (ja & 31));
+              if (two && !(jb == il && img < im0) && decide(jb, pb) &&
+                  FNETG_GUARD(jb >= 0 && jb < n))
+                atomicOr(&bits[jb >> 5], 1u << (jb & 31));
+            }
           }
+          __syncwarp();
+          // slots of the cyclic order: the start word from the start bit, the other words, the
+          // start word below the start bit
+          const int start = img < im0 ? (il + 1 == n ? 0 : il + 1) : il;
+          const int sw = start >> 5, sb = start & 31;
+          const int nslot = nwd + (sb > 0 ? 1 : 0);
+          for (int base = 0; base < nslot; base += 32) {
+            const int t = base + lane;
+            uint32_t m = 0u;
+            int widx = 0;
+            if (t < nslot) {
+              widx = t == nwd ? sw : (sw + t) % nwd;
+              m = bits[widx];
+              if (t == 0) m &= sb > 0 ? ~((1u << sb) - 1u) : 0xffffffffu;
+              else if (t == nwd) m &= (1u << sb) - 1u;
+            }
+            if (!kFill) {
+              int c = __popc(m);
+  #pragma unroll
+              for (int k = 16; k > 0; k >>= 1) c += __shfl_xor_sync(0xffffffffu, c, k);
+              cnt += c;
+              continue;
+            }
+            // ranks of the accepted atoms in the cyclic order: the slots' popcounts scanned over
+            // the lanes; each lane stores its own slot's pairs (structures on the cell path use
+            // it for every image, so nothing is queued)
+            const int pc = __popc(m);
+            int off = pc;
+  #pragma unroll
+            for (int k = 1; k < 32; k <<= 1) {
+              const int v = __shfl_up_sync(0xffffffffu, off, k);
+              if (lane >= k) off += v;
+            }
+            const int total = __shfl_sync(0xffffffffu, off, 31);
+            off -= pc;
+            for (uint32_t mm = m; mm; mm &= mm - 1u) {
+              const int bit = __ffs(mm) - 1;
+              store_pair<T>(a, ci, cif, cil, i, a0, widx * 32 + bit, (int)img, im0, wpos,
+                            stored + off);
+              off++;
+            }
+            stored += total;
+            cnt += total;
+          }
+          continue;
         }
-        cnt += n0 + n1;
+        auto test = [&](int k, bool &ok, int &jl) {
+          ok = false;
+          jl = 0;
+          if (k < tcount) {
+            jl = il + tstart + k;
+            if (jl >= n) jl -= n;
+            const V4<float> cjf = a.cf[a0 + jl];
+            const float e0 = cjf.x - px, e1 = cjf.y - py, e2 = cjf.z - pz;
+            const float df = e0 * e0 + e1 * e1 + e2 * e2;
+            if (df <= a.rc2_lo) {
+              ok = true;
+            } else if (df <= a.rc2_hi) {
+              // within the float error bound of the cutoff: the reference's FP64 decision
+              double d[3];
+              ok = exact_pair(a, ci, a0 + jl, img >= im0 ? img : -1, d) <= a.rc2;
+            }
+          }
+        };
+        for (int base = 0; base < tcount; base += 64) {
+          bool ok0, ok1;
+          int j0, j1;
+          test(base + lane, ok0, j0);
+          test(base + 32 + lane, ok1, j1);
+          const unsigned m0 = __ballot_sync(0xffffffffu, ok0), m1 = __ballot_sync(0xffffffffu, ok1);
+          const int n0 = __popc(m0), n1 = __popc(m1);
+          if (kFill) {
+            // queue the accepted candidates in iterator order; store them 32 at a time
+            const unsigned below = (1u << lane) - 1u;
+            if (ok0 && FNETG_GUARD(qn + __popc(m0 & below) < 128))
+              queue[qn + __popc(m0 & below)] = make_int2(j0, (int)img);
+            if (ok1 && FNETG_GUARD(qn + n0 + __popc(m1 & below) < 128))
+              queue[qn + n0 + __popc(m1 & below)] = make_int2(j1, (int)img);
+            qn += n0 + n1;
+            __syncwarp();
+            while (qn >= 32) {
+              const int2 e = queue[lane];
+              store_pair<T>(a, ci, cif, cil, i, a0, e.x, e.y, im0, wpos, stored + lane);
+              // move the remaining qn - 32 (< 64) entries to the front: read all, then write
+              const int rem = qn - 32;
+              const int2 v0 = lane < rem ? queue[lane + 32] : make_int2(0, 0);
+              const int2 v1 = lane + 32 < rem ? queue[lane + 64] : make_int2(0, 0);
+              __syncwarp();
+              if (lane < rem) queue[lane] = v0;
+              if (lane + 32 < rem) queue[lane + 32] = v1;
+              __syncwarp();
+              qn -= 32;
+              stored += 32;
+            }
+          }
+          cnt += n0 + n1;
+        }
       }
     }
     if (kFill && lane < qn) {

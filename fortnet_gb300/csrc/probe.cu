@@ -1,0 +1,97 @@
+// Issue-rate probes of the two pipes the featurisation and force kernels run on: FP32 fused
+// multiply-adds and the special-function unit's base-2 exponential (ex2.approx, the MUFU op
+// the Gaussians of the ACSF and force kernels use).  Each probe keeps every SM busy with
+// independent dependency chains, is timed with CUDA events on the context's stream, and gives
+// the device's sustained rate: the denominators of the compute rooflines of those kernels.
+#include "internal.cuh"
+
+namespace fnetg {
+
+namespace {
+
+constexpr int kProbeThreads = 256;
+constexpr int kChains = 8;  // independent chains per thread (covers the pipes' latency)
+
+__global__ void __launch_bounds__(kProbeThreads) fma_probe_kernel(int iters, float seed,
+                                                                  float *sink) {
+  float x[kChains];
+#pragma unroll
+  for (int c = 0; c < kChains; c++) x[c] = seed + (float)(threadIdx.x + c);
+  const float m = 0.999999f, b = 1e-7f;
+  for (int k = 0; k < iters; k++) {
+#pragma unroll
+    for (int r = 0; r < 16; r++) {
+#pragma unroll
+      for (int c = 0; c < kChains; c++) x[c] = fmaf(x[c], m, b);
+    }
+  }
+  float s = 0.f;
+#pragma unroll
+  for (int c = 0; c < kChains; c++) s += x[c];
+  if (s == 1234.5f) sink[0] = s;  // keeps the chains alive (a store within the buffer)
+}
+
+__global__ void __launch_bounds__(kProbeThreads) ex2_probe_kernel(int iters, float seed,
+                                                                  float *sink) {
+  float x[kChains];
+#pragma unroll
+  for (int c = 0; c < kChains; c++) x[c] = -1e-3f * (seed + (float)(threadIdx.x + c));
+  for (int k = 0; k < iters; k++) {
+#pragma unroll
+    for (int r = 0; r < 16; r++) {
+#pragma unroll
+      for (int c = 0; c < kChains; c++) {
+        float y;
+        asm volatile("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x[c]));
+        x[c] = -y;  // stays in (-1, 0): the next exponential is in (0.5, 1)
+      }
+    }
+  }
+  float s = 0.f;
+#pragma unroll
+  for (int c = 0; c < kChains; c++) s += x[c];
+  if (s == 1234.5f) sink[0] = s;
+}
+
+}  // namespace
+
+}  // namespace fnetg
+
+using namespace fnetg;
+
+extern "C" int fnetg_probe_peaks(fnetg_ctx *ctx, double *fp32_tflops, double *ex2_tops) {
+  if (!ctx) return FNETG_E_INVALID;
+  const int sms = num_sms();
+  const int grid = sms * 8;  // eight 256-thread CTAs per SM
+  // about a quarter of a second per launch at the nominal rates (128 FMA and 16 ex2 per clock
+  // and SM)
+  const int iters_of[2] = {256, 32};
+  FNETG_CUDA(ctx->d_scalars.ensure(sizeof(double) * 16));
+  float *sink = reinterpret_cast<float *>(ctx->d_scalars.p);
+  double best[2] = {0.0, 0.0};
+  for (int kind = 0; kind < 2; kind++) {
+    const int iters = iters_of[kind];
+    // threads x iterations x unrolled steps x chains
+    const double ops = (double)grid * kProbeThreads * iters * 16.0 * kChains;
+    for (int rep = 0; rep < 4; rep++) {  // the first repetition warms up
+      FNETG_CUDA(cudaEventRecord(ctx->ev0, ctx->stream));
+      if (kind == 0)
+        fma_probe_kernel<<<grid, kProbeThreads, 0, ctx->stream>>>(iters, 1.f, sink);
+      else
+        ex2_probe_kernel<<<grid, kProbeThreads, 0, ctx->stream>>>(iters, 1.f, sink);
+      FNETG_CUDA(cudaGetLastError());
+      FNETG_CUDA(cudaEventRecord(ctx->ev1, ctx->stream));
+      FNETG_CUDA(cudaEventSynchronize(ctx->ev1));
+      float ms = 0.f;
+      FNETG_CUDA(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
+      if (rep > 0 && ms > 0.f) {
+        // an FMA is two FLOPs; an ex2 one operation
+        const double rate = ops * (kind == 0 ? 2.0 : 1.0) / (ms * 1e-3) / 1e12;
+        best[kind] = std::max(best[kind], rate);
+      }
+    }
+  }
+  if (fp32_tflops) *fp32_tflops = best[0];
+  if (ex2_tops) *ex2_tops = best[1];
+  return FNETG_OK;
+}

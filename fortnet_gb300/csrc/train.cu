@@ -96,18 +96,21 @@ __global__ void __launch_bounds__(kLossThreads) loss_cta_kernel(LossArgs a) {
       const double t = a.gt[(int64_t)s * a.ngt + o];
       const double lg = lossgrad(a.loss, sum, t);
       lsum += loss_term(a.loss, sum, t);
+      // the structure's factor of every atom's output gradient, lg / n * ws (lg w / n ws for
+      // atomic weight w; equal to it for w = 1): one FP64 division per structure, not per atom
+      const double g = lg / (double)n * ws;
       // atomic weights of four atoms loaded before their four stores (the stores could alias
       // the loads as far as the compiler knows)
       at = a0 + threadIdx.x;
       for (; at + 3 * kLossThreads < a1; at += 4 * kLossThreads) {
         const double w0 = a.aw[at], w1 = a.aw[at + kLossThreads],
                      w2 = a.aw[at + 2 * kLossThreads], w3 = a.aw[at + 3 * kLossThreads];
-        a.delta[at * a.nout + o] = lg * w0 / (double)n * ws;
-        a.delta[(at + kLossThreads) * a.nout + o] = lg * w1 / (double)n * ws;
-        a.delta[(at + 2 * kLossThreads) * a.nout + o] = lg * w2 / (double)n * ws;
-        a.delta[(at + 3 * kLossThreads) * a.nout + o] = lg * w3 / (double)n * ws;
+        a.delta[at * a.nout + o] = g * w0;
+        a.delta[(at + kLossThreads) * a.nout + o] = g * w1;
+        a.delta[(at + 2 * kLossThreads) * a.nout + o] = g * w2;
+        a.delta[(at + 3 * kLossThreads) * a.nout + o] = g * w3;
       }
-      for (; at < a1; at += kLossThreads) a.delta[at * a.nout + o] = lg * a.aw[at] / (double)n * ws;
+      for (; at < a1; at += kLossThreads) a.delta[at * a.nout + o] = g * a.aw[at];
     }
     num += ws * a.saw[s] * loss_finish(a.loss, lsum, a.ngt);
     den += ws * a.saw[s];

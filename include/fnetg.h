@@ -258,6 +258,12 @@ int fnetg_synchronize(fnetg_ctx *ctx);
  * cleared; 0 = every check passed.  The default build has no checks and always gives 0.  No
  * counterpart in the reference beyond its debug builds' -fbounds-check (sys/gnu.cmake:33). */
 int fnetg_check_status(fnetg_ctx *ctx, int32_t *site);
+/* Sustained issue rates of the device, measured on the context's stream with CUDA events:
+ * FP32 fused multiply-adds (TFLOP/s, two FLOPs each) and the special-function unit's ex2
+ * (10^12 operations/s).  Self-written loops of independent dependency chains over every SM,
+ * about one second in total.  The compute-roofline denominators of the featurisation and force
+ * kernels; no counterpart in the reference. */
+int fnetg_probe_peaks(fnetg_ctx *ctx, double *fp32_tflops, double *ex2_tops);
 
 #ifdef __cplusplus
 }

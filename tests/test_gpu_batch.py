@@ -214,3 +214,58 @@ def test_tensor_core_training_gradients_match_fp64(force_weight):
     assert err <= 5e-2
     assert abs(l16 - l64) <= 2e-2 * l64
     assert hist[-1] < hist[0]
+
+
+@pytest.mark.parametrize("force_weight", [0.0, 0.1])
+def test_full_batch_gradient_over_many_small_mini_batches(force_weight):
+    """A full-batch tensor-core launch over a plan of many small mini-batches: with two
+    structures per mini-batch (a handful of tiles each) and about 600 tiles over one CTA per SM,
+    most CTAs meet a species again after other species, in the next mini-batch, and must add to
+    the gradient partial they stored for it before.  Energy loss: equal to the sum of the
+    per-mini-batch gradients (the same BF16 tile arithmetic, FP32 sums grouped differently:
+    norm-wise 1e-4); with the force term: within 5e-2 of the FP64 plain kernels, as on few
+    tiles."""
+    cfg = synthetic.CONFIGS["C4"]
+    ds = synthetic.generate(cfg, nstruct=200, forces=force_weight > 0)
+    funcs = synthetic.gfunctions(cfg)
+    dims = synthetic.network_dims(cfg)
+    params = random_params(dims, 3, seed=5)
+
+    def ctx_for(prec, zprec=None):
+        c = api.Context(prec)
+        c.upload(ds)
+        c.set_species(ds.species)
+        c.set_gfunctions(funcs)
+        c.acsf(download=False)
+        z = c.zscore(zprec=zprec)
+        c.set_network(dims, "tanh", params)
+        c.set_targets(ds)
+        if force_weight > 0:
+            c.set_force_targets(force_weight, ds.meta["forces"])
+        return c, z
+
+    c, zprec = ctx_for(api.FP64)
+    with c:
+        g64, _, _ = c.train_gradients("mse")
+    c, _ = ctx_for(api.FP32, zprec)
+    with c:
+        c.batch_setup(2)
+        info = c.batch_info()
+        nbatch, ntiles = info["batches"], info["tiles"]
+        assert ntiles >= 4 * 152 and nbatch == 100
+        c.batch_train_bf16(True)
+        g16, _, _ = c.train_gradients("mse")
+        if force_weight == 0:
+            gsum = np.zeros_like(g16)
+            for k in range(nbatch):
+                gsum += c.batch_gradients(k)[0]
+    err64 = max(float(np.linalg.norm(g16[s] - g64[s]) / np.linalg.norm(g64[s]))
+                for s in range(3))
+    msg = f"full-batch BF16 gradient over {ntiles} tiles vs FP64: {err64:.2e}"
+    if force_weight == 0:
+        errsum = max(float(np.linalg.norm(g16[s] - gsum[s]) / np.linalg.norm(gsum[s]))
+                     for s in range(3))
+        msg += f"; vs the sum of {nbatch} mini-batch gradients: {errsum:.2e}"
+        assert errsum <= 1e-4
+    print(msg)
+    assert err64 <= 5e-2
