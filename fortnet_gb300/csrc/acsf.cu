@@ -34,11 +34,11 @@ template <typename T> __host__ __device__ inline size_t raddesc_bytes(int nrad) 
 constexpr int kKD = kMaxMomentDegree + 1;
 
 // Per-CTA tables of the factorised G5 evaluation: combo pairs (int2), functions (pair, output
-// column), degree coefficients pc_f(m) and the multinomial weights of the monomials.
+// column) and degree coefficients pc_f(m).
 template <typename T> __host__ __device__ inline size_t g5tab_bytes(const TileArgs<T> &a) {
   if (a.nmf <= 0) return 0;
   const size_t b = sizeof(int32_t) * 2 * (size_t)(a.nmpair + a.nmf) +
-                   sizeof(T) * ((size_t)a.nmf * kKD + kMaxMono);
+                   sizeof(T) * (size_t)a.nmf * kKD;
   return (b + 127) / 128 * 128;
 }
 
@@ -92,42 +92,62 @@ __device__ __forceinline__ T radial_batch(const Tile<T> &t, const T *fcr, int np
   return transpose_reduce32<T>(acc, lane);
 }
 
-// The grid form of the radial G2 set: every shape (rs, eta) on the same NC list channels (the
-// species expansion of the reference's radial functions).  Batches of 32 / NC shapes x NC
-// channels; a pair evaluates each shape once and adds it to the channels holding it.  Shapes
-// past rv_nshape in the last batch are evaluated and dropped.
-template <typename T, int NC>
-__device__ __forceinline__ void radial_grid(const TileArgs<T> &a, const Tile<T> &t, const T *fcr,
-                                            int np, int lane, int64_t row) {
-  constexpr int SB = 32 / NC;
+// The grid form of the radial G2 set: every shape (rs, eta) on the same rv_nc list channels
+// (the species expansion of the reference's radial functions), output column of (shape sh,
+// channel c) at rv_out[sh * rv_nc + c].  Walked list by list: for channel c, lane (group g,
+// slot s) sums shapes g SPG .. g SPG + SPG - 1 over the channel list's pairs s, s + S, ...
+// (S slots, 32 / S groups); a transposing butterfly over the slots leaves shape g SPG + s on
+// lane (g, s).  Each (pair, shape) term of a channel is evaluated once and added without
+// predication, and the per-lane shape parameters stay in registers.  Needs
+// rv_nshape <= 32 / S x SPG.
+template <typename T, int S, int SPG>
+__device__ __forceinline__ void radial_lists(const TileArgs<T> &a, const Tile<T> &t, const T *fcr,
+                                             int np, int lane, int64_t row) {
+  constexpr int C = (SPG + S - 1) / S;
+  constexpr int V = C * S;
+  const int grp = lane / S, slot = lane % S;
+  const int nc = a.rv_nc, ns = a.rv_nshape;
+  T rs[SPG], c2[SPG];
 #pragma unroll
-  for (int b = 0; b * SB * NC < kRadParam; b++) {
-    if (b * SB < a.rv_nshape) {
-      T acc[32];
+  for (int k = 0; k < SPG; k++) {
+    const int sh = min(grp * SPG + k, ns - 1);  // lanes past the last shape repeat it, unused
+    rs[k] = a.rv_rs[sh];
+    c2[k] = a.rv_c2[sh];
+  }
+  for (int c = 0; c < nc; c++) {
+    const uint32_t bits = a.rv_chan[c];
+    const bool all = bits == 0x80000000u;  // the all-atom list: every pair of the tile
+    const int z = all ? 0 : __ffs((int)bits) - 1;
+    const uint16_t *lst = all ? nullptr : t.lists + z * a.cap;
+    const int n = all ? np : t.cnt[z];
+    T acc[V];
 #pragma unroll
-      for (int f = 0; f < 32; f++) acc[f] = 0;
-      for (int q0 = 0; q0 < np; q0 += 32) {
-        const int q = q0 + lane;
-        const bool live = q < np;
-        const int qq = live ? q : q0;
-        const uint32_t cm = pair_channels<T>(t, qq, live);
-        bool in[NC];
+    for (int v = 0; v < V; v++) acc[v] = 0;
+    for (int k = slot; k < n; k += S) {
+      const int q = lst ? lst[k] : k;
+      const T r = t.u[q].w;
+      const T fc = fcr[q];
 #pragma unroll
-        for (int c = 0; c < NC; c++) in[c] = (cm & a.rv_chan[c]) != 0u;
-        const T r = t.u[qq].w;
-        const T fc = fcr[qq];
-#pragma unroll
-        for (int sh = 0; sh < SB; sh++) {
-          const T x = r - a.rv_rs[b * SB + sh];
-          const T v = m_exp2<T>(a.rv_c2[b * SB + sh] * (x * x)) * fc;
-#pragma unroll
-          for (int c = 0; c < NC; c++)
-            if (in[c]) acc[sh * NC + c] += v;
-        }
+      for (int kk = 0; kk < SPG; kk++) {
+        const T x = r - rs[kk];
+        acc[kk] += m_exp2<T>(c2[kk] * (x * x)) * fc;
       }
-      const T tot = transpose_reduce32<T>(acc, lane);
-      if (lane < SB * NC && b * SB + lane / NC < a.rv_nshape)
-        a.feat[row * a.nf + a.rv_out[b * SB * NC + lane]] = tot;
+    }
+#pragma unroll
+    for (int sh = S / 2, L = V; sh >= 1; sh >>= 1, L >>= 1) {
+      const bool upper = (lane & sh) != 0;
+#pragma unroll
+      for (int k = 0; k < L / 2; k++) {
+        const T send = upper ? acc[k] : acc[k + L / 2];
+        const T keep = upper ? acc[k + L / 2] : acc[k];
+        acc[k] = keep + __shfl_xor_sync(0xffffffffu, send, sh);
+      }
+    }
+#pragma unroll
+    for (int cc = 0; cc < C; cc++) {
+      const int k = slot * C + cc, shp = grp * SPG + k;
+      if (k < SPG && shp < ns)
+        a.feat[row * a.nf + a.rv_out[shp * nc + c]] = acc[cc];
     }
   }
 }
@@ -155,10 +175,8 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 1)
   int2 *s_pair = reinterpret_cast<int2 *>(g5);
   int2 *s_mf = s_pair + a.nmpair;
   T *s_fpc = reinterpret_cast<T *>(s_mf + a.nmf);
-  T *s_mult = s_fpc + (size_t)a.nmf * kKD;
   if (D > 0 && a.nmf > 0) {
     for (int t2 = threadIdx.x; t2 < a.nmf * kKD; t2 += blockDim.x) s_fpc[t2] = a.fpc[t2];
-    for (int t2 = threadIdx.x; t2 < kMaxMono; t2 += blockDim.x) s_mult[t2] = (T)kMonoMult[t2];
     for (int t2 = threadIdx.x; t2 < a.nmpair; t2 += blockDim.x)
       s_pair[t2] = make_int2(a.mpair[2 * t2], a.mpair[2 * t2 + 1]);
     for (int t2 = threadIdx.x; t2 < a.nmf; t2 += blockDim.x)
@@ -197,16 +215,14 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 1)
       // the functions in batches of 32 (radial_batch); descriptors from the kernel parameters
       // when they fit there, else from the per-CTA table
       const T *fcr = t.fc + a.rad_fast * a.cap;
-      if (a.rv_nc == 1) {
-        radial_grid<T, 1>(a, t, fcr, np, lane, row);
-      } else if (a.rv_nc == 2) {
-        radial_grid<T, 2>(a, t, fcr, np, lane, row);
-      } else if (a.rv_nc == 3) {
-        radial_grid<T, 3>(a, t, fcr, np, lane, row);
-      } else if (a.rv_nc == 4) {
-        radial_grid<T, 4>(a, t, fcr, np, lane, row);
+      if (a.rv_nc > 0 && a.rv_nshape <= 12) {
+        radial_lists<T, 8, 3>(a, t, fcr, np, lane, row);
+      } else if (a.rv_nc > 0 && a.rv_nshape <= 24) {
+        radial_lists<T, 4, 3>(a, t, fcr, np, lane, row);
+      } else if (a.rv_nc > 0) {
+        radial_lists<T, 4, 4>(a, t, fcr, np, lane, row);
       } else if (a.rv_param) {
-#pragma unroll
+#pragma unroll 1
         for (int b = 0; b < kRadParam / 32; b++) {
           if (b * 32 < a.nrad) {
             const int nb = min(32, a.nrad - b * 32);
@@ -288,14 +304,22 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 1)
     // ---- integer-xi G5 through moments, factorised: coef_f(alpha) = mult(alpha) pc_f(|alpha|),
     // so G_f = sum_m pc_f(m) S_p(m) with the degree sums S_p of the function's combo pair
     if (D > 0 && a.nmf > 0) {
-      for (int it = lane; it < a.nmpair * kKD; it += 32) {
-        const int p = it / kKD, m = it - p * kKD;
+      // one combo pair per lane: its monomials unrolled, each added to its degree's sum with
+      // the multinomial weight as a constant (the same order within a degree as a loop over
+      // the degree's monomials)
+      constexpr int NM = n_mono_of(D > 0 ? D : 1);
+      for (int p = lane; p < a.nmpair; p += 32) {
         const int2 kk = s_pair[p];
-        const T *M1 = t.M + kk.x * a.n_mono, *M2 = t.M + kk.y * a.n_mono;
-        const int a0 = m * (m + 1) * (m + 2) / 6, a1 = min(a.n_mono, (m + 1) * (m + 2) * (m + 3) / 6);
-        T acc = 0;
-        for (int al = a0; al < a1; al++) acc += s_mult[al] * (M1[al] * M2[al]);
-        S[it] = acc;
+        const T *M1 = t.M + kk.x * NM, *M2 = t.M + kk.y * NM;
+        T sm[kKD];
+#pragma unroll
+        for (int m = 0; m < kKD; m++) sm[m] = 0;
+#pragma unroll
+        for (int al = 0; al < NM; al++)
+          sm[kMonoTab[al][0] + kMonoTab[al][1] + kMonoTab[al][2]] +=
+              (T)kMonoMult[al] * (M1[al] * M2[al]);
+#pragma unroll
+        for (int m = 0; m < kKD; m++) S[p * kKD + m] = sm[m];
       }
       __syncwarp();
       for (int f = lane; f < a.nmf; f += 32) {
@@ -518,13 +542,14 @@ template <typename T> void fill_tile_args(fnetg_ctx *ctx, TileArgs<T> &a) {
       a.rv_bits[g] = chanbit(d);
       a.rv_out[g] = d.out;
     }
-    // grid form: the first shape's channel run repeated, shape by shape, with distinct shapes
+    // grid form: the first shape's channel run repeated, shape by shape, with distinct shapes;
+    // at most 32 shapes (the list-by-list walk's lanes)
     int nc = 0;
     const GDesc &d0 = ctx->h_rad[ctx->h_radv[0]];
     while (nc < a.nrad && ctx->h_rad[ctx->h_radv[nc]].rs == d0.rs &&
            ctx->h_rad[ctx->h_radv[nc]].eta == d0.eta)
       nc++;
-    bool grid = nc >= 1 && nc <= 4 && a.nrad % nc == 0;
+    bool grid = nc >= 1 && nc <= kMaxSpeciesCodes + 1 && a.nrad % nc == 0 && a.nrad / nc <= 32;
     for (int g = 0; grid && g < a.nrad; g++) {
       const GDesc &d = ctx->h_rad[ctx->h_radv[g]];
       const GDesc &h = ctx->h_rad[ctx->h_radv[g - g % nc]];  // the shape's first function
@@ -533,7 +558,7 @@ template <typename T> void fill_tile_args(fnetg_ctx *ctx, TileArgs<T> &a) {
               d.rs != ctx->h_rad[ctx->h_radv[g - 1]].rs || d.eta != ctx->h_rad[ctx->h_radv[g - 1]].eta);
     }
     if (grid) {
-      const int ns = a.nrad / nc, sb = 32 / nc;
+      const int ns = a.nrad / nc;
       a.rv_nc = nc;
       a.rv_nshape = ns;
       T rs[kRadParam] = {}, c2[kRadParam] = {};
@@ -542,9 +567,7 @@ template <typename T> void fill_tile_args(fnetg_ctx *ctx, TileArgs<T> &a) {
         const GDesc &d = ctx->h_rad[ctx->h_radv[sh * nc]];
         rs[sh] = (T)d.rs;
         c2[sh] = -(T)d.eta * (T)kLog2e;
-        // function (shape sh, channel c) sits at lane (sh % sb) * nc + c of batch sh / sb
-        for (int c = 0; c < nc; c++)
-          out[(sh / sb) * sb * nc + (sh % sb) * nc + c] = ctx->h_rad[ctx->h_radv[sh * nc + c]].out;
+        for (int c = 0; c < nc; c++) out[sh * nc + c] = ctx->h_rad[ctx->h_radv[sh * nc + c]].out;
       }
       for (int g = 0; g < kRadParam; g++) {
         a.rv_rs[g] = rs[g];

@@ -128,6 +128,7 @@ __device__ __forceinline__ float disp_df(float ah, float al, float bh, float bl,
 }
 
 constexpr int kNbWarps = 8;  // warps per CTA of the neighbour kernel
+constexpr int kNbQueue = 128;  // ring of accepted pairs per warp (a power of two)
 
 // Store accepted pair (centre i, structure-local neighbour jl, image img or im0 - 1 for the
 // central cell) as the rank-th pair of atom i, at wpos + rank (within the slab capacity).
@@ -195,7 +196,7 @@ template <typename T, bool kFill>
 __global__ void __launch_bounds__(256, 4) nb_kernel(NbArgs a) {
   __shared__ int blk_max;
   __shared__ unsigned long long blk_sum;
-  __shared__ int2 queue_all[kNbWarps][128];  // up to 31 pending + 64 new accepted
+  __shared__ int2 queue_all[kNbWarps][kNbQueue];  // accepted pairs waiting to be stored
   __shared__ uint32_t bits_all[kNbWarps][kCellMaxAtoms / 32];  // accepted atoms of one image
   if (threadIdx.x == 0) {
     blk_max = 0;
@@ -218,11 +219,20 @@ __global__ void __launch_bounds__(256, 4) nb_kernel(NbArgs a) {
     uint32_t *bits = bits_all[threadIdx.x >> 5];
     const int4 cg = a.cgrid ? a.cgrid[s] : make_int4(0, 0, 0, 0);
     const int64_t cbase = cg.w ? a.coff[s] : 0;
-    int qn = 0;           // queued accepted candidates (uniform across the warp)
+    int qh = 0, qn = 0;   // head and length of the ring of queued pairs (uniform)
     int64_t stored = 0;   // accepted candidates already stored
     int64_t cnt = 0;
     const float *bb = a.bbox + 6 * s;
     const int64_t im0 = a.img_off[s], im1 = a.img_off[s + 1];
+    // the ring's first 32 pairs stored by the 32 lanes, at consecutive slots
+    auto drain32 = [&]() {
+      const int2 e = queue[(qh + lane) & (kNbQueue - 1)];
+      store_pair<T>(a, ci, cif, cil, i, a0, e.x, e.y, im0, wpos, stored + lane);
+      __syncwarp();
+      qh = (qh + 32) & (kNbQueue - 1);
+      qn -= 32;
+      stored += 32;
+    };
     // image -1 is the central cell, then the lattice points of the table (n1 outer .. n3 inner).
     // The images are tested 32 at a time, one per lane, against the reach of the structure's
     // shifted bounding box; the warp then walks the reachable ones in order.
@@ -318,30 +328,45 @@ __global__ void __launch_bounds__(256, 4) nb_kernel(NbArgs a) {
             }
             if (!kFill) {
               int c = __popc(m);
-  #pragma unroll
+#pragma unroll
               for (int k = 16; k > 0; k >>= 1) c += __shfl_xor_sync(0xffffffffu, c, k);
               cnt += c;
               continue;
             }
             // ranks of the accepted atoms in the cyclic order: the slots' popcounts scanned over
-            // the lanes; each lane stores its own slot's pairs (structures on the cell path use
-            // it for every image, so nothing is queued)
+            // the lanes; the pairs join the ring in that order and leave it 32 at a time
             const int pc = __popc(m);
             int off = pc;
-  #pragma unroll
+#pragma unroll
             for (int k = 1; k < 32; k <<= 1) {
               const int v = __shfl_up_sync(0xffffffffu, off, k);
               if (lane >= k) off += v;
             }
             const int total = __shfl_sync(0xffffffffu, off, 31);
             off -= pc;
-            for (uint32_t mm = m; mm; mm &= mm - 1u) {
-              const int bit = __ffs(mm) - 1;
-              store_pair<T>(a, ci, cif, cil, i, a0, widx * 32 + bit, (int)img, im0, wpos,
-                            stored + off);
-              off++;
+            if (qn + total <= kNbQueue) {
+              int pos = qh + qn + off;
+              for (uint32_t mm = m; mm; mm &= mm - 1u)
+                queue[(pos++) & (kNbQueue - 1)] = make_int2(widx * 32 + __ffs(mm) - 1, (int)img);
+              qn += total;
+              __syncwarp();
+              while (qn >= 32) drain32();
+            } else {
+              // more than the ring holds: the ring's pairs first, then this round's directly
+              for (int k = lane; k < qn; k += 32) {
+                const int2 e = queue[(qh + k) & (kNbQueue - 1)];
+                store_pair<T>(a, ci, cif, cil, i, a0, e.x, e.y, im0, wpos, stored + k);
+              }
+              __syncwarp();
+              stored += qn;
+              qh = qn = 0;
+              for (uint32_t mm = m; mm; mm &= mm - 1u) {
+                store_pair<T>(a, ci, cif, cil, i, a0, widx * 32 + __ffs(mm) - 1, (int)img, im0,
+                              wpos, stored + off);
+                off++;
+              }
+              stored += total;
             }
-            stored += total;
             cnt += total;
           }
           continue;
@@ -373,34 +398,23 @@ __global__ void __launch_bounds__(256, 4) nb_kernel(NbArgs a) {
           const int n0 = __popc(m0), n1 = __popc(m1);
           if (kFill) {
             // queue the accepted candidates in iterator order; store them 32 at a time
+            // (at most 31 waiting + 64 new: within the ring)
             const unsigned below = (1u << lane) - 1u;
-            if (ok0 && FNETG_GUARD(qn + __popc(m0 & below) < 128))
-              queue[qn + __popc(m0 & below)] = make_int2(j0, (int)img);
-            if (ok1 && FNETG_GUARD(qn + n0 + __popc(m1 & below) < 128))
-              queue[qn + n0 + __popc(m1 & below)] = make_int2(j1, (int)img);
+            const int r0 = qn + __popc(m0 & below), r1 = qn + n0 + __popc(m1 & below);
+            if (ok0 && FNETG_GUARD(r0 < kNbQueue))
+              queue[(qh + r0) & (kNbQueue - 1)] = make_int2(j0, (int)img);
+            if (ok1 && FNETG_GUARD(r1 < kNbQueue))
+              queue[(qh + r1) & (kNbQueue - 1)] = make_int2(j1, (int)img);
             qn += n0 + n1;
             __syncwarp();
-            while (qn >= 32) {
-              const int2 e = queue[lane];
-              store_pair<T>(a, ci, cif, cil, i, a0, e.x, e.y, im0, wpos, stored + lane);
-              // move the remaining qn - 32 (< 64) entries to the front: read all, then write
-              const int rem = qn - 32;
-              const int2 v0 = lane < rem ? queue[lane + 32] : make_int2(0, 0);
-              const int2 v1 = lane + 32 < rem ? queue[lane + 64] : make_int2(0, 0);
-              __syncwarp();
-              if (lane < rem) queue[lane] = v0;
-              if (lane + 32 < rem) queue[lane + 32] = v1;
-              __syncwarp();
-              qn -= 32;
-              stored += 32;
-            }
+            while (qn >= 32) drain32();
           }
           cnt += n0 + n1;
         }
       }
     }
     if (kFill && lane < qn) {
-      const int2 e = queue[lane];
+      const int2 e = queue[(qh + lane) & (kNbQueue - 1)];
       store_pair<T>(a, ci, cif, cil, i, a0, e.x, e.y, im0, wpos, stored + lane);
     }
     if ((!kFill || a.slab_cap > 0) && lane == 0) {

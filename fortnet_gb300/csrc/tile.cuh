@@ -196,7 +196,7 @@ template <typename T> __device__ __forceinline__ T int_pow(T base, int n, T e) {
 }
 
 // Everything the per-atom kernels read (one struct for both kernels).
-constexpr int kRadParam = 64;                  // radial descriptors carried as kernel parameters
+constexpr int kRadParam = 128;                 // radial descriptors carried as kernel parameters
 constexpr uint32_t kRvAllChannels = 0x800000ffu;  // channel bits of a self image: every list
 
 template <typename T> struct TileArgs {
@@ -217,10 +217,10 @@ template <typename T> struct TileArgs {
   const int32_t *radv;    // value kernel: radial functions in shape order
   int rad_split;          // value kernel, general radial path: lanes per function (1, 2 or 4)
   // value kernel, radial fast path with at most kRadParam functions: the descriptors held in
-  // the kernel parameters, read as constant-bank operands by the unrolled loops.  Grid form
-  // (rv_nc > 0: every shape on the same rv_nc list channels): per shape rs and -eta log2 e,
-  // per channel its bit, per function (shape-major) its output column.  Otherwise per function
-  // rs, -eta log2 e, channel bit and output column.
+  // the kernel parameters.  Grid form (rv_nc > 0: every shape, at most 32, on the same rv_nc
+  // list channels): per shape rs and -eta log2 e, per channel its bit, per function (shape sh,
+  // channel c) its output column at sh * rv_nc + c.  Otherwise per function rs, -eta log2 e,
+  // channel bit and output column.
   int rv_param, rv_nc, rv_nshape;
   T rv_rs[kRadParam], rv_c2[kRadParam];
   uint32_t rv_bits[kRadParam];

@@ -415,11 +415,16 @@ def test_lbfgs_history_wraps_like_the_oracle(memory, linemin, niter):
     """L-BFGS past its memory: the history ring buffer is overwritten several times
     (lbfgs.F90:387-488), every direction from the compact form of the inverse Hessian;
     parameters after each iteration against the oracle's two-loop recursion (rounding differs
-    in the order of the sums only), rtol 1e-7.  With the line minimiser (linemin.F90:221-391)
-    the search stalls on nearly identical points before its 10-step limit, where the secant or
-    bisection choice turns on the last bits of the projected derivative: a single trial point
-    may then differ before the search returns to the same minimum, so at most two of the
-    iterations may miss the bound, and the last one may not."""
+    in the order of the sums only), rtol 1e-7.  Without the line search both run on the same
+    standardised features (the GPU's own, downloaded): forty quasi-Newton iterations amplify a
+    rounding difference of the inputs by about 10^4, so features that agree to the last bits
+    (the ACSF value tests) would still decide the bound.  With the line minimiser
+    (linemin.F90:221-391) the search stalls on nearly identical points before its 10-step
+    limit, where the secant or bisection choice turns on the last bits of the projected
+    derivative: a single trial point may then differ before the search returns to the same
+    minimum, so at most two of the iterations may miss the bound, and the last one may not.
+    That case runs on the oracle's features, on which the choices agree (on the GPU's they
+    part at a stalled search and rejoin later, to 5e-16, several times in forty iterations)."""
     cfg = synthetic.CONFIGS["C1"]
     ds = synthetic.generate(cfg, nstruct=12)
     funcs = synthetic.gfunctions(cfg)
@@ -428,6 +433,16 @@ def test_lbfgs_history_wraps_like_the_oracle(memory, linemin, niter):
     vals = O.acsf(ds, funcs)
     zprec = O.zscore_stats(vals, ds)
     feats = O.zscore_apply(vals, zprec)
+    if not linemin:
+        with api.Context(api.FP64) as ctx:
+            ctx.upload(ds)
+            ctx.set_species(ds.species)
+            ctx.set_gfunctions(funcs)
+            ctx.acsf(download=False)
+            ctx.zscore(zprec=zprec)
+            gpu_feats = ctx.features()
+        assert np.allclose(gpu_feats, feats, rtol=1e-9, atol=1e-10)
+        feats = gpu_feats
     # without the line search the quasi-Newton step is capped at the maximal displacement
     opt = O.Lbfgs(params0[0], 1e-30, 1e-6, 0.2, memory, linemin, not linemin)
     params = params0.copy()
@@ -443,8 +458,7 @@ def test_lbfgs_history_wraps_like_the_oracle(memory, linemin, niter):
         ctx.upload(ds)
         ctx.set_species(ds.species)
         ctx.set_gfunctions(funcs)
-        ctx.acsf(download=False)
-        ctx.zscore(zprec=zprec)
+        ctx.set_features(feats)
         ctx.set_network(dims, "tanh", params0)
         ctx.set_targets(ds)
         ctx.optimizer_init("lbfgs", 1e-30, 1e-6, 0.2, memory=memory, linemin=linemin,
