@@ -270,14 +270,15 @@ def featurise_roofline(ctx, ds, funcs, feat_prof, nfeat=2):
     featurisations: the ACSF value pass against the device's measured FP32 and ex2 rates and
     HBM bandwidth, the neighbour search (its kernels together) against HBM (its pair records
     written once: 24 B per pair, plus positions read and cell-sorted)."""
-    fp32_peak, ex2_peak = ctx.probe_peaks()
+    fp32_peak, ex2_peak, fp64_peak = ctx.probe_peaks()
     hbm, _, peak_kind = load_peaks()
     N, P = ds.ntot, float(ctx.npairs)
     zs, cnt = np.unique(ds.atnum, return_counts=True)
     frac = {int(z): float(c) / N for z, c in zip(zs, cnt)}
     fpp, fpa, epp, bpp, bpa = acsf_op_counts(funcs, frac)
     out = {"pairs": int(P), "peaks": {"fp32_tflops": round(fp32_peak, 1),
-                                      "ex2_tops": round(ex2_peak, 2), "hbm_gbs": hbm,
+                                      "ex2_tops": round(ex2_peak, 2),
+                                      "fp64_tflops": round(fp64_peak, 3), "hbm_gbs": hbm,
                                       "source": "fnetg_probe_peaks (FMA and ex2 loops, CUDA "
                                                 "events) and MEASURED_PEAKS.json " + peak_kind}}
     ms, n = feat_prof["acsf"]
@@ -755,6 +756,22 @@ def lbfgs_leg(args):
         out["ms_per_iteration_1000_slots"] = measure()
         out["iterations_before_timing"] = filled
         out["slots_written"] = min(1000, filled)
+        # the history's FP64 work per iteration at memory m and n parameters per sub-network:
+        # the new pair against every slot (S^T y, Y^T y, S^T g, Y^T g: 4 m n FMAs), the
+        # combination over S and Y (2 m n) and the m x m matrix-vector products (about 4 m^2),
+        # against the device's measured FP64 FMA rate; the time is the increase from 10 to
+        # 1,000 slots
+        _, _, fp64 = c.probe_peaks()
+        n, m, nsp = out["parameters_per_species"], 1000, out["species"]
+        dm = m - 10
+        flop = 2.0 * nsp * (6.0 * dm * n + 4.0 * (m * m - 100))
+        dt = (out["ms_per_iteration_1000_slots"] - out["ms_per_iteration_10_slots"]) / 1e3
+        if dt > 0:
+            out["history_fp64"] = {"achieved": round(flop / dt / 1e12, 3),
+                                   "peak": round(fp64, 3), "unit": "TFLOP/s",
+                                   "frac": round(flop / dt / 1e12 / fp64, 3),
+                                   "bound": "fp64 (the GPU's FP64 rate is 1/64 of its FP32 "
+                                            "rate; the history is kept in FP64)"}
         out["fill_seconds"] = round(time.perf_counter() - t0, 2)
         out["loss"] = float(f"{c.last_losses()[0]:.4g}")
     return out

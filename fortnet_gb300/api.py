@@ -115,7 +115,8 @@ def _bind(L):
         "fnetg_launch_count": (i64, [vp]),
         "fnetg_synchronize": (C.c_int, [vp]),
         "fnetg_check_status": (C.c_int, [vp, C.POINTER(i32)]),
-        "fnetg_probe_peaks": (C.c_int, [vp, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
+        "fnetg_probe_peaks": (C.c_int, [vp, C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                        C.POINTER(C.c_double)]),
         "fnetg_features_jvp": (C.c_int, [vp, vp, vp]),
         "fnetg_set_force_targets": (C.c_int, [vp, dbl, vp]),
         "fnetg_last_losses": (C.c_int, [vp, C.POINTER(dbl), C.POINTER(dbl)]),
@@ -459,10 +460,11 @@ class Context:
         return site.value
 
     def probe_peaks(self):
-        """Measured FP32 FMA rate (TFLOP/s) and ex2 rate (10^12 op/s) of the device."""
-        f, e = C.c_double(), C.c_double()
-        self._check(self.lib.fnetg_probe_peaks(self.h, C.byref(f), C.byref(e)))
-        return f.value, e.value
+        """Measured FP32 FMA rate (TFLOP/s), ex2 rate (10^12 op/s) and FP64 FMA rate (TFLOP/s)
+        of the device."""
+        f, e, d = C.c_double(), C.c_double(), C.c_double()
+        self._check(self.lib.fnetg_probe_peaks(self.h, C.byref(f), C.byref(e), C.byref(d)))
+        return f.value, e.value, d.value
 
     def stream(self):
         s = C.c_void_p()

@@ -496,8 +496,19 @@ __global__ void __launch_bounds__(kMlpThreads, MODE == 0 ? 2 : 1) tc_mlp_kernel(
     }
     pend_x0 = true;
   }
+  // the tile's species, its rows' atoms and loss gradients are requested one tile ahead (the
+  // gradient once the atom has arrived, half a tile later), off the tile's critical path
+  int sp_next = my0 < my1 ? a.tile_sp[my0] : 0;
+  int atom_next = my0 < my1 ? tile_atom(a.tile_atoms, my0 * kRows + row, a.natoms) : -1;
+  float d3_next = (MODE == 1 && atom_next >= 0) ? (float)a.delta[atom_next] : 0.f;
   for (int64_t t = my0; t < my1; t++) {
-    const int sp = a.tile_sp[t];
+    const int sp = sp_next;
+    const int atom = atom_next;
+    const float delta3 = d3_next;
+    if (t + 1 < my1) {
+      sp_next = a.tile_sp[t + 1];
+      atom_next = tile_atom(a.tile_atoms, (t + 1) * kRows + row, a.natoms);
+    }
     const bool new_sp = sp != cur_sp;
     if (MODE == 1 && new_sp && gacc) {
       if (!settle()) {
@@ -532,8 +543,6 @@ __global__ void __launch_bounds__(kMlpThreads, MODE == 0 ? 2 : 1) tc_mlp_kernel(
       pend_w = true;
     }
     cur_sp = sp;
-    const int atom = tile_atom(a.tile_atoms, t * kRows + row, a.natoms);
-    const float delta3 = (MODE == 1 && atom >= 0) ? (float)a.delta[atom] : 0.f;
     if (pf) {
       if (!wait_all(&mb_x[buf], buf ? ph_x1 : ph_x0)) {
         drain();
@@ -568,6 +577,7 @@ __global__ void __launch_bounds__(kMlpThreads, MODE == 0 ? 2 : 1) tc_mlp_kernel(
     if (!wait_all(&mb_mma, ph_mma)) { drain(); failed = true; break; }
     ph_mma ^= 1;
     tc::fence_after_sync();
+    if (MODE == 1 && t + 1 < my1) d3_next = atom_next >= 0 ? (float)a.delta[atom_next] : 0.f;
     float f1[CH];
     {
       float v[CH];

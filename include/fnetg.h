@@ -259,11 +259,13 @@ int fnetg_synchronize(fnetg_ctx *ctx);
  * counterpart in the reference beyond its debug builds' -fbounds-check (sys/gnu.cmake:33). */
 int fnetg_check_status(fnetg_ctx *ctx, int32_t *site);
 /* Sustained issue rates of the device, measured on the context's stream with CUDA events:
- * FP32 fused multiply-adds (TFLOP/s, two FLOPs each) and the special-function unit's ex2
- * (10^12 operations/s).  Self-written loops of independent dependency chains over every SM,
- * about one second in total.  The compute-roofline denominators of the featurisation and force
- * kernels; no counterpart in the reference. */
-int fnetg_probe_peaks(fnetg_ctx *ctx, double *fp32_tflops, double *ex2_tops);
+ * FP32 fused multiply-adds (TFLOP/s, two FLOPs each), the special-function unit's ex2
+ * (10^12 operations/s) and FP64 fused multiply-adds (TFLOP/s).  Self-written loops of
+ * independent dependency chains over every SM, about two seconds in total.  The
+ * compute-roofline denominators of the featurisation, force and optimiser kernels; no
+ * counterpart in the reference.  Any output pointer may be NULL. */
+int fnetg_probe_peaks(fnetg_ctx *ctx, double *fp32_tflops, double *ex2_tops,
+                      double *fp64_tflops);
 
 #ifdef __cplusplus
 }
