@@ -375,26 +375,23 @@ int fnetg_update_coords(fnetg_ctx *ctx, const double *coords) {
   if (!ctx || (!coords && ctx->N > 0)) return FNETG_E_INVALID;
   ctx->feat_gen++;
   const int64_t N = ctx->N;
-  for (int64_t q = 0; q < 3 * N; q++)
-    FNETG_CHECK(std::isfinite(coords[q]), FNETG_E_GEOMETRY, "non-finite coordinate");
-  if (N > 0)
-    FNETG_CUDA(cudaMemcpyAsync(ctx->d_coords.p, coords, sizeof(double) * 3 * N,
+  // the new coordinates land in a staging buffer; the device checks them and measures the
+  // structures' extents (no pass over them on the host), and only checked coordinates replace
+  // the context's: a refused update leaves the context as it was
+  double ext = 0.0;
+  if (N > 0) {
+    FNETG_CUDA(ctx->d_coords_in.ensure(sizeof(double) * 3 * N));
+    FNETG_CUDA(cudaMemcpyAsync(ctx->d_coords_in.p, coords, sizeof(double) * 3 * N,
                                cudaMemcpyHostToDevice, ctx->stream));
+    bool bad = false;
+    int rc = coords_summary(ctx, ctx->d_coords_in.as<double>(), &ext, &bad);
+    if (rc) return rc;
+    FNETG_CHECK(!bad, FNETG_E_GEOMETRY, "non-finite coordinate");
+    FNETG_CUDA(cudaMemcpyAsync(ctx->d_coords.p, ctx->d_coords_in.p, sizeof(double) * 3 * N,
+                               cudaMemcpyDeviceToDevice, ctx->stream));
+  }
   int rc = prepare_coords(ctx);
   if (rc) return rc;
-  double ext = 0.0;
-  for (int s = 0; s < ctx->S; s++) {
-    double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
-    for (int64_t a = ctx->h_off[s]; a < ctx->h_off[s + 1]; a++)
-      for (int c = 0; c < 3; c++) {
-        lo[c] = std::min(lo[c], coords[3 * a + c]);
-        hi[c] = std::max(hi[c], coords[3 * a + c]);
-      }
-    if (ctx->h_off[s + 1] > ctx->h_off[s])
-      ext = std::max(ext, std::sqrt((hi[0] - lo[0]) * (hi[0] - lo[0]) +
-                                    (hi[1] - lo[1]) * (hi[1] - lo[1]) +
-                                    (hi[2] - lo[2]) * (hi[2] - lo[2])));
-  }
   ctx->max_extent = ext;
   invalidate_geometry(ctx);
   return FNETG_OK;

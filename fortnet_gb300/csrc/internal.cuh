@@ -171,9 +171,10 @@ struct fnetg_ctx {
   std::vector<double> h_lat;
   int32_t next = 0;
   // d_coordsf: [2N] float coordinates relative to the structure's box corner, high parts then
-  // the low parts (coordinate - high part)
+  // the low parts (coordinate - high part); d_coords_in: coordinates of fnetg_update_coords
+  // until they are checked
   fnetg::DBuf d_off, d_atom_struct, d_coords, d_coordsf, d_atnum, d_lat, d_ranges, d_bbox,
-      d_ext, d_periodic;
+      d_ext, d_periodic, d_coords_in;
 
   // species (sub-network index per atom) and bucketing
   bool species_set = false;
@@ -359,9 +360,37 @@ inline cudaError_t copy_sync(fnetg_ctx *c, void *dst, const void *src, size_t by
 int num_sms();
 void resolve_profile(fnetg_ctx *c);
 
+// Loss functions of lib_common/loss.F90 (217-721) for one prediction p and target t: the
+// gradient of the loss term, the term, and the term sums turned into the loss value.
+__device__ __forceinline__ double lossgrad(int loss, double p, double t) {
+  switch (loss) {
+    case FNETG_LOSS_RMS: return (p - t) / sqrt((p - t) * (p - t));
+    case FNETG_LOSS_MAE: return (p - t) / fabs(p - t);
+    case FNETG_LOSS_MAPE: return 100.0 * (p - t) / (t * t * fabs(p / t - 1.0));
+    default: return 2.0 * (p - t);
+  }
+}
+__device__ __forceinline__ double loss_term(int loss, double p, double t) {
+  switch (loss) {
+    case FNETG_LOSS_MAE: return fabs(t - p);
+    case FNETG_LOSS_MAPE: return fabs((t - p) / t);
+    default: return (t - p) * (t - p);
+  }
+}
+__device__ __forceinline__ double loss_finish(int loss, double sum, int n) {
+  switch (loss) {
+    case FNETG_LOSS_RMS: return sqrt(sum / (double)n);
+    case FNETG_LOSS_MAPE: return 100.0 * sum / (double)n;
+    default: return sum / (double)n;
+  }
+}
+
 // kernels' host entry points (one per translation unit)
 int run_neighbors(fnetg_ctx *ctx, double rcut);
 int prepare_coords(fnetg_ctx *ctx);
+// Largest structure bounding-box diagonal of the device coordinates d_xyz [N][3] and whether
+// any of them is not finite (one reduction on the device, 16 bytes read back, synchronous).
+int coords_summary(fnetg_ctx *ctx, const double *d_xyz, double *max_extent, bool *nonfinite);
 int pair_d2(fnetg_ctx *ctx);
 const int64_t *pair_end(fnetg_ctx *ctx);  // device end offsets of every atom's pairs
 int run_acsf(fnetg_ctx *ctx);

@@ -12,6 +12,7 @@
 // iterator order, so the fill pass reproduces the reference's neighbour order exactly.
 #define FNETG_FILE_CODE 1  // site codes of the bounds-checked build
 #include <algorithm>
+#include <cstring>
 
 #include "internal.cuh"
 
@@ -554,6 +555,52 @@ __global__ void prep_coords_kernel(const double *coords, const int64_t *off, V4<
     }
 }
 
+// Per structure: the FP64 bounding-box diagonal sqrt((hi - lo)_x^2 + (hi - lo)_y^2 +
+// (hi - lo)_z^2), in that operation order, into a running maximum (the bits of a non-negative
+// double order like the value), and a flag for any coordinate that is not finite.
+__global__ void coords_summary_kernel(const double *coords, const int64_t *off, int S,
+                                      unsigned long long *max_bits, int *nonfinite) {
+  __shared__ double lo[3][256], hi[3][256];
+  __shared__ int bad;
+  const int s = blockIdx.x;
+  if (s >= S) return;
+  if (threadIdx.x == 0) bad = 0;
+  __syncthreads();
+  const int64_t a0 = off[s], a1 = off[s + 1];
+  double l[3] = {1e300, 1e300, 1e300}, h[3] = {-1e300, -1e300, -1e300};
+  bool fin = true;
+  for (int64_t a = a0 + threadIdx.x; a < a1; a += blockDim.x)
+    for (int c = 0; c < 3; c++) {
+      const double x = coords[3 * a + c];
+      fin = fin && isfinite(x);
+      l[c] = fmin(l[c], x);
+      h[c] = fmax(h[c], x);
+    }
+  if (!fin) atomicOr(&bad, 1);
+  for (int c = 0; c < 3; c++) {
+    lo[c][threadIdx.x] = l[c];
+    hi[c][threadIdx.x] = h[c];
+  }
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o)
+      for (int c = 0; c < 3; c++) {
+        lo[c][threadIdx.x] = fmin(lo[c][threadIdx.x], lo[c][threadIdx.x + o]);
+        hi[c][threadIdx.x] = fmax(hi[c][threadIdx.x], hi[c][threadIdx.x + o]);
+      }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    if (bad) atomicOr(nonfinite, 1);
+    if (a1 > a0) {
+      const double d0 = hi[0][0] - lo[0][0], d1 = hi[1][0] - lo[1][0], d2 = hi[2][0] - lo[2][0];
+      const double e =
+          sqrt(__dadd_rn(__dadd_rn(__dmul_rn(d0, d0), __dmul_rn(d1, d1)), __dmul_rn(d2, d2)));
+      atomicMax(max_bits, (unsigned long long)__double_as_longlong(e));
+    }
+  }
+}
+
 // Cell grid of every structure that uses one: edge 1 / inv_cs over its bounding box (relative
 // float frame), at most kCellDimMax cells per axis.
 __global__ void cell_grid_kernel(const float *bbox, const int64_t *off, int S, float inv_cs,
@@ -673,6 +720,27 @@ int prepare_coords(fnetg_ctx *ctx) {
       ctx->d_coordsf.as<V4<float>>() + std::max<int64_t>(ctx->N, 1), ctx->d_bbox.as<float>(),
       ctx->S);
   FNETG_CUDA(cudaGetLastError());
+  return FNETG_OK;
+}
+
+int coords_summary(fnetg_ctx *ctx, const double *d_xyz, double *max_extent, bool *nonfinite) {
+  *max_extent = 0.0;
+  *nonfinite = false;
+  if (ctx->S == 0 || ctx->N == 0) return FNETG_OK;
+  FNETG_CUDA(ctx->d_scalars.ensure(sizeof(double) * 16));
+  unsigned long long *acc = reinterpret_cast<unsigned long long *>(ctx->d_scalars.p) + 8;
+  FNETG_CUDA(cudaMemsetAsync(acc, 0, 16, ctx->stream));
+  {
+    LaunchScope ls(ctx, "coords");
+    coords_summary_kernel<<<ctx->S, 256, 0, ctx->stream>>>(
+        d_xyz, ctx->d_off.as<int64_t>(), ctx->S, acc, reinterpret_cast<int *>(acc + 1));
+    FNETG_CUDA(cudaGetLastError());
+  }
+  unsigned long long h[2] = {0, 0};
+  FNETG_CUDA(cudaMemcpyAsync(h, acc, 16, cudaMemcpyDeviceToHost, ctx->stream));
+  FNETG_CUDA(cudaStreamSynchronize(ctx->stream));
+  std::memcpy(max_extent, &h[0], sizeof(double));
+  *nonfinite = (h[1] & 0xffffffffull) != 0;
   return FNETG_OK;
 }
 

@@ -18,31 +18,6 @@ constexpr double kEps = 2.220446049250313e-16;        // epsilon(1.0_dp)
 constexpr double kGoldenMeanP1 = 1.6180339887498949;  // lib_dftbp/constants.F90:131
 constexpr int kOptThreads = 512;
 
-__device__ __forceinline__ double lossgrad(int loss, double p, double t) {
-  switch (loss) {
-    case FNETG_LOSS_RMS: return (p - t) / sqrt((p - t) * (p - t));
-    case FNETG_LOSS_MAE: return (p - t) / fabs(p - t);
-    case FNETG_LOSS_MAPE: return 100.0 * (p - t) / (t * t * fabs(p / t - 1.0));
-    default: return 2.0 * (p - t);
-  }
-}
-
-// simple losses accumulate these two sums; finish() turns them into the loss value
-__device__ __forceinline__ double loss_term(int loss, double p, double t) {
-  switch (loss) {
-    case FNETG_LOSS_MAE: return fabs(t - p);
-    case FNETG_LOSS_MAPE: return fabs((t - p) / t);
-    default: return (t - p) * (t - p);
-  }
-}
-__device__ __forceinline__ double loss_finish(int loss, double sum, int n) {
-  switch (loss) {
-    case FNETG_LOSS_RMS: return sqrt(sum / (double)n);
-    case FNETG_LOSS_MAPE: return 100.0 * sum / (double)n;
-    default: return sum / (double)n;
-  }
-}
-
 struct LossArgs {
   int S;
   const int64_t *off;

@@ -2,6 +2,8 @@
 atom-order sums bit for bit, and caller-owned (pinned) output buffers receive exactly what
 freshly allocated ones do."""
 
+import dataclasses
+
 import numpy as np
 import pytest
 import torch
@@ -62,3 +64,37 @@ def sum_in_order(v):
     for x in v:
         acc += float(x)
     return acc
+
+
+def test_update_coords_refuses_non_finite_and_keeps_the_context():
+    """fnetg_update_coords checks the new coordinates on the device before they replace the
+    context's: a NaN is refused with FNETG_E_GEOMETRY and the previous geometry (and its pair
+    list) stays; finite moved coordinates are taken."""
+    cfg = synthetic.CONFIGS["C2"]
+    ds = synthetic.generate(cfg, nstruct=6, targets=False)
+    with api.Context(api.FP32) as ctx:
+        ctx.upload(ds)
+        ctx.set_species(ds.species)
+        ctx.set_gfunctions(synthetic.gfunctions(cfg))
+        p0 = ctx.neighbors()
+        off0, j0, _, _ = ctx.get_neighbors()
+        bad = ds.coords.copy()
+        bad[len(bad) // 2, 1] = np.nan
+        with pytest.raises(api.FnetgError) as err:
+            ctx.update_coords(bad)
+        assert err.value.code == -6
+        assert ctx.neighbors() == p0
+        off1, j1, _, _ = ctx.get_neighbors()
+        assert np.array_equal(off0, off1) and np.array_equal(j0, j1)
+        moved = ds.coords * 1.05
+        ctx.update_coords(moved)
+        ctx.neighbors()
+        off2, j2, _, _ = ctx.get_neighbors()
+    fresh = dataclasses.replace(ds, coords=moved)
+    with api.Context(api.FP32) as ctx:
+        ctx.upload(fresh)
+        ctx.set_species(ds.species)
+        ctx.set_gfunctions(synthetic.gfunctions(cfg))
+        ctx.neighbors()
+        off3, j3, _, _ = ctx.get_neighbors()
+    assert np.array_equal(off2, off3) and np.array_equal(j2, j3)
