@@ -707,7 +707,7 @@ def precision_leg(args):
 
 def lbfgs_leg(args):
     """L-BFGS at full history (memory 1000, the reference's default): the optimiser's cost per
-    iteration on the C3 networks (three sub-networks of 15,041 parameters) once every one of
+    iteration on the C3 networks (three sub-networks of 15,210 parameters) once every one of
     the 1,000 history slots holds a pair, against its cost with 10 slots.  The iterations run
     the full training step on a 64-structure C3 sample, without line search and with the
     quasi-Newton step capped at the maximal displacement, so that every iteration adds a pair;
