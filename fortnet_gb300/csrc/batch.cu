@@ -1161,6 +1161,43 @@ __global__ void pack_x_kernel(const T *feat, const int32_t *bpos, int nf, int K0
   st8(x + t * (int64_t)x_bytes, tc::core_off(r, g * 8, kRows), v);
 }
 
+// The same packing for FP32 features whose width is a multiple of 4, one CTA per tile: the
+// rows' feature offsets resolved once into shared memory, then every thread sweeps (row,
+// 4-column chunk) items with 16-byte loads (consecutive threads, consecutive chunks of a row),
+// the BF16 values placed in the tile's core-matrix layout in shared memory, and the finished
+// tile written with 16-byte stores to consecutive addresses.  Same values and layout as
+// pack_x_kernel.
+constexpr int kPackThreads = 256;
+__global__ void __launch_bounds__(kPackThreads) pack_x_tile_kernel(
+    const float *feat, const int32_t *bpos, int nf, int K0p, const int32_t *tile_atoms,
+    uint32_t x_bytes, unsigned char *x, int64_t natoms) {
+  extern __shared__ __align__(16) unsigned char tile[];
+  __shared__ int64_t rowoff[kRows];  // first feature of each row, -1 for padding rows
+  const int64_t t = blockIdx.x;
+  if (threadIdx.x < kRows) {
+    const int atom = tile_atom(tile_atoms, t * kRows + threadIdx.x, natoms);
+    rowoff[threadIdx.x] = atom >= 0 ? (int64_t)bpos[atom] * nf : -1;
+  }
+  __syncthreads();
+  const int nq = nf / 4, nc = K0p / 4;  // feature chunks, chunks per row
+  for (int it = threadIdx.x; it < kRows * nc; it += kPackThreads) {
+    const int r = it / nc, c = it - r * nc;
+    const int64_t ro = rowoff[r];
+    float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (ro >= 0) {
+      if (c < nq) v = *reinterpret_cast<const float4 *>(feat + ro + 4 * c);
+      else if (c == nq) v.x = 1.f;  // the constant input of the first layer's bias
+    }
+    const __nv_bfloat162 lo = __floats2bfloat162_rn(v.x, v.y), hi = __floats2bfloat162_rn(v.z, v.w);
+    *reinterpret_cast<uint2 *>(tile + tc::core_off(r, 4 * c, kRows)) =
+        make_uint2(*reinterpret_cast<const uint32_t *>(&lo), *reinterpret_cast<const uint32_t *>(&hi));
+  }
+  __syncthreads();
+  uint4 *dst = reinterpret_cast<uint4 *>(x + t * (int64_t)x_bytes);
+  const uint4 *src = reinterpret_cast<const uint4 *>(tile);
+  for (uint32_t q = threadIdx.x; q < x_bytes / 16; q += kPackThreads) dst[q] = src[q];
+}
+
 // FP64 master parameters (reference order) -> per-species BF16 weight images + FP32 output
 // layer: W0 image rows = first hidden units, columns = inputs (+ bias column nf); W1 forward
 // image rows = second hidden units, columns = first (+ bias column H1); W1 reverse image rows =
@@ -1639,6 +1676,20 @@ int pack_features(fnetg_ctx *ctx) {
   BatchState &b = *ctx->batch;
   const int64_t total = b.ntiles * kRows * (b.net.K0p / 8);
   LaunchScope ls(ctx, "tc_pack");
+  if (sizeof(T) == 4 && b.net.nf % 4 == 0) {
+    const void *k = (const void *)pack_x_tile_kernel;
+    FNETG_CUDA(raise_smem_limit(k, b.net.x_bytes));
+    const float *f = ctx->d_feat.as<float>();
+    const int32_t *bp = ctx->d_bpos.as<int32_t>(), *ta = b.d_tile_atoms.as<int32_t>();
+    int nf = b.net.nf, K0p = b.net.K0p;
+    uint32_t xb = b.net.x_bytes;
+    unsigned char *x = b.d_x.as<unsigned char>();
+    int64_t natoms = ctx->N;
+    void *args[] = {&f, &bp, &nf, &K0p, &ta, &xb, &x, &natoms};
+    FNETG_CUDA(cudaLaunchKernel(k, dim3((unsigned)b.ntiles), dim3(kPackThreads), args, b.net.x_bytes,
+                                ctx->stream));
+    return FNETG_OK;
+  }
   pack_x_kernel<T><<<ceil_div(total, 256), 256, 0, ctx->stream>>>(
       ctx->d_feat.as<T>(), ctx->d_bpos.as<int32_t>(), b.net.nf, b.net.K0p,
       b.d_tile_atoms.as<int32_t>(), b.ntiles, b.net.x_bytes, b.d_x.as<unsigned char>(), ctx->N);
