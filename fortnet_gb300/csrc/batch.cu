@@ -1415,7 +1415,8 @@ struct BatchState {
   // what the tile plan was built for
   int plan_S = -1, plan_nsp = 0;
   int64_t plan_N = -1;
-  std::vector<int32_t> plan_dims, plan_species;
+  std::vector<int32_t> plan_dims;
+  uint64_t plan_layout = 0;  // the context's structure/species generation of the plan
   // captured epoch
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
@@ -1779,7 +1780,7 @@ int fnetg_batch_setup(fnetg_ctx *ctx, int32_t batch_structures) {
   if (!ctx->batch) ctx->batch = new BatchState();
   BatchState &b = *ctx->batch;
   if (b.B == batch_structures && b.plan_S == ctx->S && b.plan_N == ctx->N &&
-      b.plan_dims == ctx->dims && b.plan_nsp == ctx->nsp && b.plan_species == ctx->h_species) {
+      b.plan_dims == ctx->dims && b.plan_nsp == ctx->nsp && b.plan_layout == ctx->layout_gen) {
     // same structures, species, network shape and batch size: the tile plan, the graph and the
     // tuned launch shapes stay; only the features and weights are packed again
     int rc = ctx->prec == FNETG_FP64 ? pack_features<double>(ctx) : pack_features<float>(ctx);
@@ -1851,7 +1852,7 @@ int fnetg_batch_setup(fnetg_ctx *ctx, int32_t batch_structures) {
   b.plan_N = ctx->N;
   b.plan_dims = ctx->dims;
   b.plan_nsp = ctx->nsp;
-  b.plan_species = ctx->h_species;
+  b.plan_layout = ctx->layout_gen;
   FNETG_CUDA(cudaStreamSynchronize(ctx->stream));
   return FNETG_OK;
 }

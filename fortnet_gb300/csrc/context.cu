@@ -365,6 +365,7 @@ int fnetg_upload_structures(fnetg_ctx *ctx, int32_t nstruct, const int64_t *atom
   ctx->targets_set = false;
   // default: every atom in sub-network 0 until fnetg_set_species
   ctx->h_species.assign(N, 0);
+  ctx->layout_gen++;
   ctx->species_set = false;
   int rc = refresh_codes(ctx);
   if (rc) return rc;
@@ -459,6 +460,7 @@ int fnetg_set_species(fnetg_ctx *ctx, const int32_t *species) {
     for (int64_t a = 0; a < ctx->N; a++)
       FNETG_CHECK(species[a] < ctx->nsp, FNETG_E_SHAPE, "species index >= number of networks");
   ctx->h_species.assign(species, species + ctx->N);
+  ctx->layout_gen++;
   ctx->species_set = true;
   // features are stored in bucket order; a new order needs a fresh featurisation
   return rebuild_buckets(ctx, true);

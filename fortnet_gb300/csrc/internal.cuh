@@ -179,6 +179,8 @@ struct fnetg_ctx {
   // species (sub-network index per atom) and bucketing
   bool species_set = false;
   std::vector<int32_t> h_species;
+  // bumped whenever the structures or the atoms' species change (plans built on them compare it)
+  uint64_t layout_gen = 0;
   std::vector<int64_t> h_bucket_off;  // [nsp+1] rows of every species bucket
   std::vector<int64_t> h_tiles;       // packed (species, row0, nrows) triples for MLP tiles
   fnetg::DBuf d_species, d_bpos, d_bperm, d_tiles;
